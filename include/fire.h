@@ -1,0 +1,193 @@
+/*
+ * fire.h -- C ABI of the GB300-native FiRE local-energy hot path.
+ *
+ * All array pointers are DEVICE pointers owned by the caller, except where a
+ * comment says "host".  No entry point allocates device memory: scratch space is
+ * the caller's workspace, sized by fire_workspace_size().  Every call is
+ * asynchronous on `stream`; failures detected on the device (capacity overflow,
+ * non-finite results) are written to the int32 status word array `status`
+ * (FIRE_STATUS_WORDS entries, device memory) and never trap.  The return value
+ * reports argument errors and launch failures only.
+ *
+ * The entry points replace these functions of the reference (MScherbela/sparse_wf,
+ * paths relative to its src/sparse_wf/):
+ *   fire_neighbors      model/new_sparse_model.py:238-263 get_pair_indices,
+ *                       :399-437 get_static_input, :476-481 get_neighbouring_nuclei
+ *   fire_triplets       model/sparse_fwd_lap.py:252-291 _get_triplet_indices
+ *   fire_logpsi         model/wave_function.py:183-198 MoonLikeWaveFunction.signed
+ *   fire_local_energy   hamiltonian.py:69-81 local_energy (kinetic via
+ *                       wave_function.py:215-221, potential via hamiltonian.py:15-26),
+ *                       batched like update.py:95-100 and reduced like update.py:130-134
+ *   fire_mcmc_block     mcmc.py:38-97 mcmc_steps_all_electron
+ *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
+ *                       (used by the initialiser, new_sparse_model.py:378-379)
+ */
+#ifndef FIRE_H
+#define FIRE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIRE_NO_NEIGHBOUR 1000000 /* model/graph_utils.py:14 NO_NEIGHBOUR */
+#define FIRE_STATUS_WORDS 8
+#define FIRE_ABI_VERSION 1
+
+typedef enum {
+  FIRE_OK = 0,
+  FIRE_ERR_INVALID = 1,     /* bad argument (host-side check) */
+  FIRE_ERR_UNSUPPORTED = 2, /* architecture/size outside what the kernels are built for */
+  FIRE_ERR_WORKSPACE = 3,   /* workspace too small */
+  FIRE_ERR_CUDA = 4         /* a launch failed; cudaGetLastError() has the cause */
+} fire_status;
+
+/* bits of status[0] (sticky; the caller clears the status array) */
+#define FIRE_FLAG_PAIR_OVERFLOW 1     /* e-e pairs of a walker exceeded cap_pairs */
+#define FIRE_FLAG_NUC_OVERFLOW 2      /* e-n neighbours of an electron exceeded cap_nuc */
+#define FIRE_FLAG_NONFINITE 4         /* a non-finite log|psi| or E_loc was produced */
+#define FIRE_FLAG_TRIPLET_OVERFLOW 8  /* triplet list exceeded its capacity */
+#define FIRE_FLAG_SINGULAR 16         /* an orbital matrix had a zero pivot */
+/* status[1] = max pairs of any walker seen, status[2] = max e-n neighbours seen,
+ * status[3] = max triplets (sum_m deg(m)^2) seen; the host grows capacities from these,
+ * like StaticScheduler (static_args.py:62-84). */
+
+typedef enum {
+  FIRE_PREC_FP32 = 0,  /* everything in FP32 SIMT, orbital LU/inverse in FP64 */
+  FIRE_PREC_MIXED = 1, /* BF16 tensor-core MLP GEMMs (FP32 accumulate), rest FP32, LU in FP64 */
+  FIRE_PREC_FP64 = 2   /* everything in FP64 (validation build of the same kernels) */
+} fire_precision;
+
+typedef struct {
+  int32_t n_el;          /* electrons per walker */
+  int32_t n_up;          /* spin-up electrons (the first n_up) */
+  int32_t n_nuc;         /* nuclei */
+  int32_t n_walkers;     /* walkers in this call */
+  float cutoff;          /* e-e neighbour cutoff (bohr), embedding.new.cutoff */
+  float cutoff_1el;      /* e-n neighbour cutoff (bohr), embedding.new.cutoff_1el */
+  int32_t cap_pairs;     /* capacity: directed e-e pairs per walker (same + diff) */
+  int32_t cap_nuc;       /* capacity: e-n neighbours per electron */
+  int32_t precision;     /* fire_precision */
+  int32_t chunk_walkers; /* walkers per internal pass; 0 = choose from the workspace */
+} fire_problem;
+
+/* Parameter slots of the flat parameter blob (float32), in blob order.  Shapes with
+ * F = 256, D = 4 determinants, n = n_el, N = n_nuc are given by fire_param_layout. */
+enum fire_param_slot {
+  FIRE_P_EN_SCALES, FIRE_P_EN_KERNEL, FIRE_P_EN_BIAS, FIRE_P_EN_NUC_EMB,
+  FIRE_P_EI_DIR_W, FIRE_P_EI_DIR_B, FIRE_P_EI_ENV_W, FIRE_P_EI_GAMMA_W, FIRE_P_EI_EDGE_W,
+  FIRE_P_EI_LN_SCALE, FIRE_P_EI_LN_BIAS, FIRE_P_EI_GLU_W, FIRE_P_EI_DENSE_W, FIRE_P_EI_DENSE_B,
+  FIRE_P_EI_OUT_W, FIRE_P_EI_OUT_B,
+  FIRE_P_EESAME_SCALE, FIRE_P_EESAME_KERNEL, FIRE_P_EESAME_BIAS, FIRE_P_EESAME_DIR_W,
+  FIRE_P_EESAME_DIR_B, FIRE_P_EESAME_ENV_W, FIRE_P_EESAME_GAMMA_W, FIRE_P_EESAME_EDGE_W,
+  FIRE_P_EESAME_EDGE_B,
+  FIRE_P_EEDIFF_SCALE, FIRE_P_EEDIFF_KERNEL, FIRE_P_EEDIFF_BIAS, FIRE_P_EEDIFF_DIR_W,
+  FIRE_P_EEDIFF_DIR_B, FIRE_P_EEDIFF_ENV_W, FIRE_P_EEDIFF_GAMMA_W, FIRE_P_EEDIFF_EDGE_W,
+  FIRE_P_EEDIFF_EDGE_B,
+  FIRE_P_UPD1_W, FIRE_P_UPD1_B, FIRE_P_UPD2_W, FIRE_P_UPD2_B, FIRE_P_SCALES, FIRE_P_CUTOFF_PARAM,
+  FIRE_P_ORB_UP_W, FIRE_P_ORB_UP_B, FIRE_P_ORB_DN_W, FIRE_P_ORB_DN_B,
+  FIRE_P_ENV_UP_SIGMA, FIRE_P_ENV_UP_PI, FIRE_P_ENV_DN_SIGMA, FIRE_P_ENV_DN_PI,
+  FIRE_P_CUSP,
+  FIRE_P_JMLP1_W, FIRE_P_JMLP1_B, FIRE_P_JMLP2_W, FIRE_P_JMLP2_B, FIRE_P_JMLP3_W, FIRE_P_JMLP3_B,
+  FIRE_P_MLP_SCALE, FIRE_P_LOG_BIAS,
+  FIRE_P_ATT_KEYS, FIRE_P_ATT_Q_W, FIRE_P_ATT_Q_B, FIRE_P_ATT_V_W, FIRE_P_ATT_V_B,
+  FIRE_P_ATT_OUT1_W, FIRE_P_ATT_OUT1_B, FIRE_P_ATT_OUT2_W, FIRE_P_ATT_OUT2_B,
+  FIRE_P_ATT_OUT3_W, FIRE_P_ATT_OUT3_B, FIRE_P_ATT_SCALE, FIRE_P_ATT_BIAS,
+  FIRE_P_COUNT
+};
+
+/* ---- sizes (host functions, no device work) -------------------------------------------------- */
+int32_t fire_abi_version(void);
+
+/* offsets[FIRE_P_COUNT + 1] (host): element offset of every slot, 64-element aligned;
+ * offsets[FIRE_P_COUNT] = total blob length.  Mirrors the MoonLikeParams tree
+ * (model/wave_function.py:54-57) flattened. */
+fire_status fire_param_layout(const fire_problem* prob, int64_t* offsets);
+
+/* bytes of the prepared-parameter buffer (derived weights: folded scales, fused attention
+ * query/key weights, BF16 copies for the mixed path). */
+fire_status fire_prepared_size(const fire_problem* prob, size_t* bytes);
+
+/* bytes of workspace needed to process `chunk` walkers per pass (chunk <= 0: the whole batch). */
+fire_status fire_workspace_size(const fire_problem* prob, int32_t chunk, size_t* bytes);
+
+/* ---- parameters ------------------------------------------------------------------------------- */
+/* Builds the prepared buffer from the float32 blob (device) and its offsets (host array). */
+fire_status fire_prepare_params(void* stream, const fire_problem* prob, const float* blob,
+                                const int64_t* offsets_host, void* prepared, size_t prepared_bytes);
+
+/* ---- neighbour lists (bit-exact with get_pair_indices) ----------------------------------------- */
+typedef struct {
+  /* each may be NULL; per walker, padded with FIRE_NO_NEIGHBOUR (jac_* padding: n_el + P) */
+  int32_t* ct_same; int32_t* nb_same; int32_t* jac_same; /* [B, cap_same] */
+  int32_t* ct_diff; int32_t* nb_diff; int32_t* jac_diff; /* [B, cap_diff] */
+  int32_t* jac_ctr; int32_t* jac_dep;                    /* [B, n_el + cap_same + cap_diff] */
+  int32_t* en_idx;                                       /* [B, n_el, cap_nuc] */
+  int32_t* counts;  /* [B, 4]: n_pairs_same, n_pairs_diff, n_triplets, n_neighbours_en */
+  int32_t cap_same, cap_diff;
+} fire_neighbor_out;
+
+/* r: [B, n_el, 3] float32 (float64 when prob->precision == FIRE_PREC_FP64); R: [n_nuc, 3] float32 */
+fire_status fire_neighbors(void* stream, const fire_problem* prob, const void* r, const float* R,
+                           const fire_neighbor_out* out, int32_t* status);
+
+/* Triplet index quadruples (in, k, kn, i) in _get_triplet_indices order, [B, cap_triplets] each,
+ * total per walker n_el + 2P + sum_m deg(m)^2 (padded with FIRE_NO_NEIGHBOUR). */
+fire_status fire_triplets(void* stream, const fire_problem* prob, const void* r, int32_t cap_triplets,
+                          int32_t* trip_in, int32_t* trip_k, int32_t* trip_kn, int32_t* trip_i,
+                          void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* ---- wavefunction ----------------------------------------------------------------------------- */
+/* sign, logpsi: [B] in the walkers' dtype */
+fire_status fire_logpsi(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                        const void* prepared, const void* r, void* sign, void* logpsi,
+                        void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Optional intermediate outputs of fire_local_energy (any pointer may be NULL). */
+typedef struct {
+  void* kinetic;   /* [B] */
+  void* potential; /* [B] */
+  double* logdet;  /* [B, 4] */
+  double* sign_det;/* [B, 4] */
+  void* jastrow;   /* [B] log Jastrow value */
+  void* grad;      /* [B, n_el, 3] gradient of log|psi| */
+  void* lap;       /* [B] Laplacian of log|psi| */
+} fire_eloc_debug;
+
+/* logpsi, sign, e_loc: [B] in the walkers' dtype (may be NULL except e_loc);
+ * e_stats: [2] float64 = (mean, std) of e_loc over the batch (may be NULL). */
+fire_status fire_local_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                              const void* prepared, const void* r, void* logpsi, void* sign,
+                              void* e_loc, double* e_stats, const fire_eloc_debug* debug,
+                              void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Embedding value path for initialisation and stage checks:
+ * h_contract [B, n, 256] = h0 + messages (before the first normalize scale),
+ * h_update [B, n, 256] = SparseMLP(h_contract * scales[0]) (before scales[1]). Either may be NULL. */
+fire_status fire_embedding(void* stream, const fire_problem* prob, const float* R, const void* prepared,
+                           const void* r, void* h_contract, void* h_update, void* workspace,
+                           size_t workspace_bytes, int32_t* status);
+
+/* Metropolis block of all-electron Gaussian moves (mcmc.py:38-97).
+ * r [B, n, 3] and logpsi [B] are updated in place (logpsi must hold log|psi(r)| on entry).
+ * Proposals: r' = r + width * eps.  eps and u come from Philox4x32-10 keyed by (seed, counter,
+ * step, walker) unless replay_noise [steps, B, n, 3] and replay_log_u [steps, B] are given.
+ * n_accept [B] int32 (accepted moves per walker), may be NULL.
+ * static_max [4] int32: max over steps/walkers of (n_pairs_same, n_pairs_diff, 0, n_neighbours_en)
+ * of the proposals (the laplacian=False statics of mcmc.py:290-294), may be NULL. */
+fire_status fire_mcmc_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                            const void* prepared, void* r, void* logpsi, int32_t steps, float width,
+                            uint64_t seed, uint64_t counter, const void* replay_noise,
+                            const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
+                            void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Coulomb potential of every walker (hamiltonian.py:15-26): out [B] in the walkers' dtype. */
+fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r,
+                                  const float* R, const float* Z, void* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIRE_H */

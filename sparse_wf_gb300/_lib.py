@@ -1,0 +1,87 @@
+"""ctypes binding of ``libfire.so`` (declarations in ``include/fire.h``).
+
+The library is the product path; there is no CPU fallback.  ``load()`` raises when
+the shared library is missing or cannot be loaded.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libfire.so"
+
+FIRE_OK = 0
+STATUS_WORDS = 8
+NO_NEIGHBOUR = 1_000_000
+PREC = {"fp32": 0, "mixed": 1, "fp64": 2}
+FLAG_PAIR_OVERFLOW = 1
+FLAG_NUC_OVERFLOW = 2
+FLAG_NONFINITE = 4
+FLAG_TRIPLET_OVERFLOW = 8
+FLAG_SINGULAR = 16
+ERRORS = {1: "invalid argument", 2: "unsupported size", 3: "workspace too small", 4: "CUDA launch failed"}
+
+# exported entry points, in header order
+SYMBOLS = [
+    "fire_abi_version", "fire_param_layout", "fire_prepared_size", "fire_workspace_size",
+    "fire_prepare_params", "fire_neighbors", "fire_triplets", "fire_logpsi", "fire_local_energy",
+    "fire_embedding", "fire_mcmc_block", "fire_potential_energy",
+]
+
+
+class Problem(C.Structure):
+    _fields_ = [
+        ("n_el", C.c_int32), ("n_up", C.c_int32), ("n_nuc", C.c_int32), ("n_walkers", C.c_int32),
+        ("cutoff", C.c_float), ("cutoff_1el", C.c_float), ("cap_pairs", C.c_int32), ("cap_nuc", C.c_int32),
+        ("precision", C.c_int32), ("chunk_walkers", C.c_int32),
+    ]
+
+
+class NeighborOut(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "ct_same", "nb_same", "jac_same", "ct_diff", "nb_diff", "jac_diff", "jac_ctr", "jac_dep", "en_idx",
+        "counts")] + [("cap_same", C.c_int32), ("cap_diff", C.c_int32)]
+
+
+class ElocDebug(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in
+                ("kinetic", "potential", "logdet", "sign_det", "jastrow", "grad", "lap")]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH.name} is not built; run sparse_wf_gb300.build.build()")
+    lib = C.CDLL(str(LIB_PATH))
+    P = C.POINTER(Problem)
+    vp, i32, u64, f32, sz = C.c_void_p, C.c_int32, C.c_uint64, C.c_float, C.c_size_t
+    sig = {
+        "fire_abi_version": ([], i32),
+        "fire_param_layout": ([P, C.POINTER(C.c_int64)], i32),
+        "fire_prepared_size": ([P, C.POINTER(sz)], i32),
+        "fire_workspace_size": ([P, i32, C.POINTER(sz)], i32),
+        "fire_prepare_params": ([vp, P, vp, C.POINTER(C.c_int64), vp, sz], i32),
+        "fire_neighbors": ([vp, P, vp, vp, C.POINTER(NeighborOut), vp], i32),
+        "fire_triplets": ([vp, P, vp, i32, vp, vp, vp, vp, vp, sz, vp], i32),
+        "fire_logpsi": ([vp, P, vp, vp, vp, vp, vp, vp, vp, sz, vp], i32),
+        "fire_local_energy": ([vp, P, vp, vp, vp, vp, vp, vp, vp, vp, C.POINTER(ElocDebug), vp, sz, vp], i32),
+        "fire_embedding": ([vp, P, vp, vp, vp, vp, vp, vp, sz, vp], i32),
+        "fire_mcmc_block": ([vp, P, vp, vp, vp, vp, vp, i32, f32, u64, u64, vp, vp, vp, vp, vp, sz, vp], i32),
+        "fire_potential_energy": ([vp, P, vp, vp, vp, vp], i32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != FIRE_OK:
+        raise RuntimeError(f"{what}: {ERRORS.get(rc, rc)}")

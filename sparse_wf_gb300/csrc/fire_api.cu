@@ -1,0 +1,976 @@
+// fire_api.cu -- the C ABI (include/fire.h): layouts, workspace planning and the chunked pipelines.
+//
+// Stage order of one chunk of walkers for the local energy (the forward-Laplacian path,
+// wave_function.py:165-181 + hamiltonian.py:69-81):
+//   neighbours -> layout -> ElecInit (edges, LayerNorm) -> GLU/Dense/Dense GEMMs on [x, jac, lap]
+//   -> e-e edges + messages -> update MLP (2 x silu layers) -> envelopes -> orbitals
+//   -> FP64 Gauss-Jordan -> determinant Laplacian -> attention Jastrow -> MLP Jastrow -> assembly.
+// The value path (log|psi|, the MCMC building block) runs the same stages without tangents.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "fire_gemm.cuh"
+#include "fire_kernels.cuh"
+
+using namespace fire;
+
+namespace {
+
+// ------------------------------------------------------------------------------ parameter layout
+void slot_sizes(const fire_problem* p, int64_t* sz) {
+  const int64_t n = p->n_el, N = p->n_nuc, D = NDET, Fl = F;
+  const int64_t s[FIRE_P_COUNT] = {
+      N * NENV_EN, N * 4 * F0, N * F0, N * Fl,                      // en
+      F0 * F1, F1, NENV_EN * F1, F1 * Fl, 4 * Fl,                   // ei filter, gamma, edge
+      Fl, Fl, Fl * 2 * Fl, Fl * Fl, Fl, Fl * 5 * Fl, 5 * Fl,        // ln, glu, dense, out
+      F0, 4 * F0, F0, F0 * F1, F1, NENV_EE * F1, F1 * Fl, 4 * Fl, Fl,  // ee same
+      F0, 4 * F0, F0, F0 * F1, F1, NENV_EE * F1, F1 * Fl, 4 * Fl, Fl,  // ee diff
+      Fl * Fl, Fl, Fl * Fl, Fl, 2, 1,                               // updates, scales, cutoff_param
+      Fl * D * n, D * n, Fl * D * n, D * n,                         // orbitals
+      N * D * NENV_ORB, N * D * NENV_ORB * n, N * D * NENV_ORB, N * D * NENV_ORB * n,  // envelopes
+      4,                                                            // cusp
+      Fl * Fl, Fl, Fl * Fl, Fl, Fl * 2, 2, 2, 1,                    // MLP Jastrow
+      HEADS * HDIM, Fl * Fl, Fl, Fl * Fl, Fl,                       // attention keys, Q, V
+      2 * Fl * Fl, Fl, Fl * Fl, Fl, Fl * 2, 2, 2, 1};               // readout, scale, bias
+  for (int k = 0; k < FIRE_P_COUNT; ++k) sz[k] = s[k];
+}
+int64_t align64(int64_t x) { return (x + 63) / 64 * 64; }
+void blob_offsets(const fire_problem* p, int64_t* off) {
+  int64_t sz[FIRE_P_COUNT];
+  slot_sizes(p, sz);
+  int64_t o = 0;
+  for (int k = 0; k < FIRE_P_COUNT; ++k) {
+    off[k] = o;
+    o += align64(sz[k]);
+  }
+  off[FIRE_P_COUNT] = o;
+}
+// prepared slots (elements of the compute type)
+void prep_offsets(const fire_problem* p, int64_t* off) {
+  blob_offsets(p, off);
+  const int64_t n = p->n_el, N = p->n_nuc, D = NDET;
+  int64_t o = off[FIRE_P_COUNT];
+  const int64_t ds[PR_COUNT - PR_UPD1_W_S0] = {
+      F * F, F * D * n, F * D * n, F * F, F * HEADS, HEADS, F * F, N * NENV_EN, NENV_EE, NENV_EE,
+      N * D * NENV_ORB, N * D * NENV_ORB, D * N * NENV_ORB * n, D * N * NENV_ORB * n, 8};
+  for (int k = PR_UPD1_W_S0; k < PR_COUNT; ++k) {
+    off[k] = o;
+    o += align64(ds[k - PR_UPD1_W_S0]);
+  }
+  off[PR_COUNT] = o;
+}
+size_t elem_size(const fire_problem* p) { return p->precision == FIRE_PREC_FP64 ? 8 : 4; }
+
+bool valid(const fire_problem* p) {
+  return p && p->n_el >= 2 && p->n_el <= MAX_EL && p->n_up >= 0 && p->n_up <= p->n_el && p->n_nuc >= 1 &&
+         p->n_walkers >= 1 && p->cutoff > 0 && p->cutoff_1el > 0 && p->cap_pairs >= 1 && p->cap_nuc >= 1 &&
+         p->precision >= 0 && p->precision <= 2;
+}
+
+// ------------------------------------------------------------------------------ workspace plan
+struct Plan {
+  // int
+  size_t deg, rowptr, nbr, rev, en_cnt, en_idx, counts, pos_off, pos_ctr, pos_dep, dep_pos;
+  // T
+  size_t E5a, Z1, E5o, HX, HL, HJ, B1X, B1L, B1J, B2X, B2L, B2J, Zx, jsq;
+  size_t env, rawx, rjs, Apl, lapA, Jorb, coef_up, coef_dn, Ainv, dgrad;
+  size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, jsqr;
+  size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn;
+  // double
+  size_t ld, sd, dlap;
+  size_t total;
+};
+
+Plan make_plan(const fire_problem* p, int Wc, bool fl) {
+  Plan P;
+  std::memset(&P, 0, sizeof(P));
+  const size_t es = elem_size(p);
+  const size_t n = p->n_el, nu = p->n_up, nd = p->n_el - p->n_up, N = p->n_nuc, cp = p->cap_pairs,
+               cn = p->cap_nuc, W = Wc;
+  const size_t G = W * n, Pc = W * (n + cp), Jr = 3 * Pc, DN = NDET * n, NV = fl ? 5 : 1;
+  size_t o = 0;
+  auto take = [&](size_t& field, size_t count, size_t bytes_per) {
+    o = (o + 255) / 256 * 256;
+    field = o;
+    o += count * bytes_per;
+  };
+  take(P.deg, G, 4);
+  take(P.rowptr, W * (n + 1), 4);
+  take(P.nbr, W * cp, 4);
+  take(P.rev, W * cp, 4);
+  take(P.en_cnt, G, 4);
+  take(P.en_idx, G * cn, 4);
+  take(P.counts, W * 4, 4);
+  if (fl) {
+    take(P.pos_off, W + 1, 4);
+    take(P.pos_ctr, Pc, 4);
+    take(P.pos_dep, Pc, 4);
+    take(P.dep_pos, Pc, 4);
+  }
+  take(P.E5a, G * NV * F, es);
+  take(P.Z1, G * NV * 2 * F, es);
+  take(P.E5o, G * NV * 5 * F, es);
+  take(P.HX, G * F, es);
+  take(P.B1X, G * F, es);
+  take(P.B2X, G * F, es);
+  take(P.Zx, G * F, es);
+  if (fl) {
+    take(P.HL, G * F, es);
+    take(P.HJ, Jr * F, es);
+    take(P.B1L, G * F, es);
+    take(P.B1J, Jr * F, es);
+    take(P.B2L, G * F, es);
+    take(P.B2J, Jr * F, es);
+    take(P.jsq, G * F, es);
+  }
+  take(P.env, G * NV * DN, es);
+  take(P.rawx, G * DN, es);
+  take(P.Apl, G * DN, es);
+  take(P.coef_up, NDET * W * nu * NV * N * NENV_ORB, es);
+  take(P.coef_dn, NDET * W * nd * NV * N * NENV_ORB, es);
+  if (fl) {
+    take(P.rjs, G * 3 * DN, es);
+    take(P.lapA, G * DN, es);
+    take(P.Jorb, Jr * DN, es);
+    take(P.Ainv, W * NDET * n * n, es);
+    take(P.dgrad, W * NDET * n * 3, es);
+  }
+  take(P.aX, G * HEADS, es);
+  take(P.Ax, W * 2 * 272, es);
+  take(P.RX, W * 512, es);
+  take(P.R1X, W * F, es);
+  take(P.R2X, W * F, es);
+  take(P.Zr, W * F, es);
+  take(P.JAx, W * 2, es);
+  take(P.Xo2, G * 2, es);
+  take(P.JMx, W * 2, es);
+  if (fl) {
+    take(P.aJ, Jr * HEADS, es);
+    take(P.aL, G * HEADS, es);
+    take(P.Al, W * 2 * 272, es);
+    take(P.AJ, W * 3 * n * 2 * 272, es);
+    take(P.RJ, W * 3 * n * 512, es);
+    take(P.RL, W * 512, es);
+    take(P.R1J, W * 3 * n * F, es);
+    take(P.R1L, W * F, es);
+    take(P.R2J, W * 3 * n * F, es);
+    take(P.R2L, W * F, es);
+    take(P.jsqr, W * F, es);
+    take(P.JAj, W * 3 * n * 2, es);
+    take(P.JAl, W * 2, es);
+    take(P.Jo2, Jr * 2, es);
+    take(P.Lo2, G * 2, es);
+    take(P.JMl, W * 2, es);
+    take(P.JMj, W * 3 * n * 2, es);
+  }
+  take(P.rn, G * 3, es);
+  take(P.lpn, W, es);
+  take(P.ld, W * NDET, 8);
+  take(P.sd, W * NDET, 8);
+  take(P.dlap, W * NDET, 8);
+  P.total = (o + 255) / 256 * 256;
+  return P;
+}
+
+int choose_chunk(const fire_problem* p, size_t ws_bytes, bool fl) {
+  int B = p->n_walkers;
+  if (p->chunk_walkers > 0) {
+    const int c = std::min(B, p->chunk_walkers);
+    return make_plan(p, c, fl).total <= ws_bytes ? c : 0;
+  }
+  int lo = 0, hi = B;
+  while (lo < hi) {  // largest c with plan(c) <= ws
+    const int mid = (lo + hi + 1) / 2;
+    if (make_plan(p, mid, fl).total <= ws_bytes) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------------------------ prepare kernels
+template <typename T>
+__global__ void k_convert(const float* __restrict__ in, T* __restrict__ out, long n) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)in[i];
+}
+template <typename T>
+__global__ void k_scale_copy(const float* __restrict__ in, T* __restrict__ out, long n, const float* __restrict__ sc) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)((double)in[i] * (double)sc[0]);
+}
+template <typename T>
+__global__ void k_qk(const float* __restrict__ QW, const float* __restrict__ Qb, const float* __restrict__ K,
+                     const float* __restrict__ s1, T* __restrict__ W, T* __restrict__ b) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;  // f * 16 + h
+  if (idx < F * HEADS) {
+    const int f = idx / HEADS, h = idx % HEADS;
+    double s = 0.0;
+    for (int d = 0; d < HDIM; ++d) s += (double)QW[f * F + h * HDIM + d] * K[h * HDIM + d];
+    W[idx] = (T)(s * s1[0]);
+  }
+  if (idx < HEADS) {
+    double s = 0.0;
+    for (int d = 0; d < HDIM; ++d) s += (double)Qb[idx * HDIM + d] * K[idx * HDIM + d];
+    b[idx] = (T)s;
+  }
+}
+template <typename T>
+__global__ void k_softplus(const float* __restrict__ in, T* __restrict__ out, long n, int invert) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double x = in[i];
+    const double sp = x > 30.0 ? x : log1p(exp(x));
+    out[i] = (T)(invert ? 1.0 / sp : sp);
+  }
+}
+template <typename T>
+__global__ void k_pi_perdet(const float* __restrict__ pi, T* __restrict__ out, int N, int n) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over (d, I, k, o)
+  const long total = (long)NDET * N * NENV_ORB * n;
+  if (idx >= total) return;
+  const int o = (int)(idx % n);
+  const int k = (int)((idx / n) % NENV_ORB);
+  const int I = (int)((idx / ((long)n * NENV_ORB)) % N);
+  const int d = (int)(idx / ((long)n * NENV_ORB * N));
+  out[idx] = (T)pi[(((long)I * NDET + d) * NENV_ORB + k) * n + o];
+}
+template <typename T>
+__global__ void k_scalars(const float* __restrict__ cutoff_param, const float* __restrict__ log_bias, float cutoff,
+                          T* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    const double cp = cutoff_param[0];
+    out[0] = (T)((double)cutoff / (1.0 + exp(-cp)));
+    out[1] = T(0);
+    out[2] = (T)log_bias[0];
+    for (int k = 3; k < 8; ++k) out[k] = T(0);
+  }
+}
+
+inline unsigned nblk(long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+template <typename T>
+fire_status prepare_impl(cudaStream_t s, const fire_problem* p, const float* blob, const int64_t* boff,
+                         void* prepared) {
+  int64_t off[PR_COUNT + 1];
+  prep_offsets(p, off);
+  T* out = reinterpret_cast<T*>(prepared);
+  const long nb = (long)off[FIRE_P_COUNT];
+  k_convert<T><<<nblk(nb), 256, 0, s>>>(blob, out, nb);
+  const float* s0 = blob + boff[FIRE_P_SCALES];
+  const float* s1 = blob + boff[FIRE_P_SCALES] + 1;
+  const long n = p->n_el, N = p->n_nuc;
+  auto scl = [&](int src, int dst, long cnt, const float* sc) {
+    k_scale_copy<T><<<nblk(cnt), 256, 0, s>>>(blob + boff[src], out + off[dst], cnt, sc);
+  };
+  scl(FIRE_P_UPD1_W, PR_UPD1_W_S0, (long)F * F, s0);
+  scl(FIRE_P_ORB_UP_W, PR_ORB_UP_W_S1, (long)F * NDET * n, s1);
+  scl(FIRE_P_ORB_DN_W, PR_ORB_DN_W_S1, (long)F * NDET * n, s1);
+  scl(FIRE_P_JMLP1_W, PR_JMLP1_W_S1, (long)F * F, s1);
+  scl(FIRE_P_ATT_V_W, PR_V_W_S1, (long)F * F, s1);
+  k_qk<T><<<nblk(F * HEADS), 256, 0, s>>>(blob + boff[FIRE_P_ATT_Q_W], blob + boff[FIRE_P_ATT_Q_B],
+                                          blob + boff[FIRE_P_ATT_KEYS], s1, out + off[PR_QK_W_S1],
+                                          out + off[PR_QK_B]);
+  k_softplus<T><<<nblk(N * NENV_EN), 256, 0, s>>>(blob + boff[FIRE_P_EN_SCALES], out + off[PR_EN_INVSCALE],
+                                                  N * NENV_EN, 1);
+  k_softplus<T><<<1, 256, 0, s>>>(blob + boff[FIRE_P_EESAME_SCALE], out + off[PR_EESAME_INVSCALE], NENV_EE, 1);
+  k_softplus<T><<<1, 256, 0, s>>>(blob + boff[FIRE_P_EEDIFF_SCALE], out + off[PR_EEDIFF_INVSCALE], NENV_EE, 1);
+  k_softplus<T><<<nblk(N * NDET * NENV_ORB), 256, 0, s>>>(blob + boff[FIRE_P_ENV_UP_SIGMA], out + off[PR_ENV_UP_SP],
+                                                          N * NDET * NENV_ORB, 0);
+  k_softplus<T><<<nblk(N * NDET * NENV_ORB), 256, 0, s>>>(blob + boff[FIRE_P_ENV_DN_SIGMA], out + off[PR_ENV_DN_SP],
+                                                          N * NDET * NENV_ORB, 0);
+  k_pi_perdet<T><<<nblk((long)NDET * N * NENV_ORB * n), 256, 0, s>>>(blob + boff[FIRE_P_ENV_UP_PI],
+                                                                      out + off[PR_ENV_UP_PI], (int)N, (int)n);
+  k_pi_perdet<T><<<nblk((long)NDET * N * NENV_ORB * n), 256, 0, s>>>(blob + boff[FIRE_P_ENV_DN_PI],
+                                                                      out + off[PR_ENV_DN_PI], (int)N, (int)n);
+  k_scalars<T><<<1, 32, 0, s>>>(blob + boff[FIRE_P_CUTOFF_PARAM], blob + boff[FIRE_P_LOG_BIAS], p->cutoff,
+                                out + off[PR_SCALARS]);
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+template <typename T>
+Weights<T> make_weights(const fire_problem* p, const void* prepared) {
+  int64_t off[PR_COUNT + 1];
+  prep_offsets(p, off);
+  Weights<T> W;
+  const T* base = reinterpret_cast<const T*>(prepared);
+  for (int k = 0; k < PR_COUNT; ++k) W.w[k] = base + off[k];
+  return W;
+}
+
+// ------------------------------------------------------------------------------ chunk context
+template <typename T>
+struct Ctx {
+  const fire_problem* p;
+  cudaStream_t s;
+  int Wc;     // walkers in this chunk
+  int Wmax;   // planned chunk size
+  int w0;
+  int B;
+  const T* r;  // chunk base
+  const float* R;
+  const float* Z;
+  Weights<T> W;
+  int32_t* status;
+  unsigned char* ws;
+  Plan P;
+  Nbr nb;
+  Layout L;
+  template <typename U>
+  U* buf(size_t off) const {
+    return reinterpret_cast<U*>(ws + off);
+  }
+};
+
+template <typename T>
+void setup_ctx(Ctx<T>& c, bool fl) {
+  const fire_problem* p = c.p;
+  c.nb.W = c.Wc;
+  c.nb.n = p->n_el;
+  c.nb.n_up = p->n_up;
+  c.nb.N = p->n_nuc;
+  c.nb.cap_p = p->cap_pairs;
+  c.nb.cap_nuc = p->cap_nuc;
+  c.nb.deg = c.template buf<int>(c.P.deg);
+  c.nb.rowptr = c.template buf<int>(c.P.rowptr);
+  c.nb.nbr = c.template buf<int>(c.P.nbr);
+  c.nb.rev = c.template buf<int>(c.P.rev);
+  c.nb.en_cnt = c.template buf<int>(c.P.en_cnt);
+  c.nb.en_idx = c.template buf<int>(c.P.en_idx);
+  c.nb.counts = c.template buf<int>(c.P.counts);
+  if (fl) {
+    c.L.pos_off = c.template buf<int>(c.P.pos_off);
+    c.L.pos_ctr = c.template buf<int>(c.P.pos_ctr);
+    c.L.pos_dep = c.template buf<int>(c.P.pos_dep);
+    c.L.dep_pos = c.template buf<int>(c.P.dep_pos);
+    c.L.cap_pos = c.Wc * (p->n_el + p->cap_pairs);
+  } else {
+    std::memset(&c.L, 0, sizeof(c.L));
+  }
+}
+
+template <typename T>
+GemmP<T> gp0() {
+  GemmP<T> g;
+  std::memset(&g, 0, sizeof(g));
+  g.node_div = 1;
+  g.M_scale = 1;
+  g.env_nv = 1;
+  return g;
+}
+
+template <typename T, int MODE>
+cudaError_t gemm(const Ctx<T>& c, GemmP<T> g) {
+  return launch_gemm<T, MODE>(g, c.s);
+}
+
+// neighbour lists (+ layout for the forward-Laplacian path)
+template <typename T>
+cudaError_t stage_neighbors(Ctx<T>& c, bool fl) {
+  const int n = c.p->n_el;
+  const size_t smem = 3 * n * sizeof(T) + (5 * n + 2) * sizeof(int);
+  fire_neighbor_out ext;
+  std::memset(&ext, 0, sizeof(ext));
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_neighbors<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_neighbors<T><<<c.Wc, 512, smem, c.s>>>(c.r, c.R, (T)c.p->cutoff, (T)c.p->cutoff_1el, c.nb, ext, c.status);
+  if (fl) {
+    k_pos_scan<<<1, 1024, 0, c.s>>>(c.nb, c.L.pos_off);
+    k_layout<<<c.Wc, 256, 0, c.s>>>(c.nb, c.L);
+  }
+  return cudaGetLastError();
+}
+
+// ElecInit + GLU/Dense/Dense on the electron carriers, then edges + messages -> H
+template <typename T, int NT>
+cudaError_t stage_embedding(Ctx<T>& c) {
+  constexpr int NV = NT > 0 ? NT + 2 : 1;
+  const int n = c.p->n_el, G = c.Wc * n;
+  T* E5a = c.template buf<T>(c.P.E5a);
+  T* Z1 = c.template buf<T>(c.P.Z1);
+  T* E5o = c.template buf<T>(c.P.E5o);
+  k_elec_init<T, NT><<<G, 256, 0, c.s>>>(c.r, c.R, c.nb, c.W, (T)(1.0 / c.p->cutoff_1el), E5a);
+  GemmP<T> g = gp0<T>();
+  g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_GLU_W]; g.ldb = 2 * F; g.C = Z1; g.ldc = 2 * F;
+  g.M = G * NV; g.N = 2 * F; g.K = F;
+  gemm<T, EPI_PLAIN>(c, g);
+  k_glu<T, NT><<<nblk((long)G * F), 256, 0, c.s>>>(Z1, E5a, G);
+  g = gp0<T>();
+  g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_DENSE_W]; g.ldb = F; g.C = Z1; g.ldc = F;
+  g.bias = c.W.w[FIRE_P_EI_DENSE_B]; g.bias_period = NV;
+  g.M = G * NV; g.N = F; g.K = F;
+  gemm<T, EPI_PLAIN>(c, g);
+  k_silu5<T, NT><<<nblk((long)G * F), 256, 0, c.s>>>(Z1, G);
+  g = gp0<T>();
+  g.A = Z1; g.lda = F; g.B = c.W.w[FIRE_P_EI_OUT_W]; g.ldb = 5 * F; g.C = E5o; g.ldc = 5 * F;
+  g.bias = c.W.w[FIRE_P_EI_OUT_B]; g.bias_period = NV;
+  g.M = G * NV; g.N = 5 * F; g.K = F;
+  gemm<T, EPI_PLAIN>(c, g);
+  k_edge_contract<T, NT><<<G, 256, 0, c.s>>>(c.r, c.nb, c.L, c.W, E5o, c.template buf<T>(c.P.HX),
+                                             NT ? c.template buf<T>(c.P.HL) : nullptr,
+                                             NT ? c.template buf<T>(c.P.HJ) : nullptr);
+  return cudaGetLastError();
+}
+
+struct Planes {
+  size_t X, J, L;
+};
+
+// Linear(F -> N) + SiLU on a sparse node (value path: X plane only)
+template <typename T>
+cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, const T* b, int K, int N,
+                       int rowsX, int rowsJcap, const int* rowsJdev, const int* node_map, int node_div, size_t zx,
+                       size_t jsq) {
+  GemmP<T> g = gp0<T>();
+  g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.C = c.template buf<T>(out.X);
+  g.ldc = N; g.M = rowsX; g.N = N; g.K = K; g.aux0 = c.template buf<T>(zx); g.ld_aux = N;
+  gemm<T, EPI_SILU_X>(c, g);
+  if (!fl) return cudaGetLastError();
+  cudaMemsetAsync(c.template buf<T>(jsq), 0, sizeof(T) * (size_t)rowsX * N, c.s);
+  g = gp0<T>();
+  g.A = c.template buf<T>(in.J); g.lda = K; g.B = Wt; g.ldb = N; g.C = c.template buf<T>(out.J); g.ldc = N;
+  g.M = rowsJcap; g.M_dev = rowsJdev; g.M_scale = 3; g.N = N; g.K = K; g.node_map = node_map;
+  g.node_div = node_div; g.aux1 = c.template buf<T>(zx); g.aux2 = c.template buf<T>(jsq); g.ld_aux = N;
+  gemm<T, EPI_SILU_J>(c, g);
+  g = gp0<T>();
+  g.A = c.template buf<T>(in.L); g.lda = K; g.B = Wt; g.ldb = N; g.C = c.template buf<T>(out.L); g.ldc = N;
+  g.M = rowsX; g.N = N; g.K = K; g.aux1 = c.template buf<T>(zx); g.aux3 = c.template buf<T>(jsq); g.ld_aux = N;
+  gemm<T, EPI_SILU_L>(c, g);
+  return cudaGetLastError();
+}
+
+// Linear(F -> N) without activation on a node (bias on X only)
+template <typename T>
+cudaError_t linear_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, const T* b, int K, int N,
+                         int rowsX, int rowsJcap, const int* rowsJdev) {
+  GemmP<T> g = gp0<T>();
+  g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.bias_period = 1;
+  g.C = c.template buf<T>(out.X); g.ldc = N; g.M = rowsX; g.N = N; g.K = K;
+  gemm<T, EPI_PLAIN>(c, g);
+  if (!fl) return cudaGetLastError();
+  g.A = c.template buf<T>(in.J); g.bias = nullptr; g.C = c.template buf<T>(out.J); g.M = rowsJcap;
+  g.M_dev = rowsJdev; g.M_scale = rowsJdev ? 3 : 1;
+  gemm<T, EPI_PLAIN>(c, g);
+  g.A = c.template buf<T>(in.L); g.C = c.template buf<T>(out.L); g.M = rowsX; g.M_dev = nullptr; g.M_scale = 1;
+  gemm<T, EPI_PLAIN>(c, g);
+  return cudaGetLastError();
+}
+
+// envelopes + orbital matrices (+ their Jacobian/Laplacian planes)
+template <typename T, int NT>
+cudaError_t stage_orbitals(Ctx<T>& c) {
+  constexpr int NV = NT > 0 ? NT + 2 : 1;
+  const bool fl = NT > 0;
+  const int n = c.p->n_el, nu = c.p->n_up, N = c.p->n_nuc, G = c.Wc * n, DN = NDET * n;
+  T* env = c.template buf<T>(c.P.env);
+  for (int s = 0; s < 2; ++s) {
+    const int ns = s == 0 ? nu : n - nu;
+    if (ns == 0) continue;
+    T* coef = c.template buf<T>(s == 0 ? c.P.coef_up : c.P.coef_dn);
+    const long tot = (long)c.Wc * ns * N * NENV_ORB;
+    k_env_coef<T, NV><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, c.W.w[s == 0 ? PR_ENV_UP_SP : PR_ENV_DN_SP], n, ns,
+                                                  s == 0 ? 0 : nu, N, c.Wc, coef);
+    const long rows = (long)c.Wc * ns * NV, K8 = (long)N * NENV_ORB;
+    for (int d = 0; d < NDET; ++d) {
+      GemmP<T> g = gp0<T>();
+      g.A = coef + d * rows * K8; g.lda = K8;
+      g.B = c.W.w[s == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (long)d * K8 * n; g.ldb = n;
+      g.C = env + (long)d * n; g.ldc = DN; g.M = (int)rows; g.N = n; g.K = (int)K8;
+      g.n_el = n; g.env_ns = ns; g.env_soff = s == 0 ? 0 : nu; g.env_nv = NV;
+      gemm<T, EPI_ENV>(c, g);
+    }
+  }
+  GemmP<T> g = gp0<T>();
+  g.A = c.template buf<T>(c.P.B2X); g.lda = F; g.B = c.W.w[PR_ORB_UP_W_S1]; g.B2 = c.W.w[PR_ORB_DN_W_S1];
+  g.ldb = DN; g.bias = c.W.w[FIRE_P_ORB_UP_B]; g.bias2 = c.W.w[FIRE_P_ORB_DN_B];
+  g.C = c.template buf<T>(c.P.Apl); g.ldc = DN; g.M = G; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
+  g.aux0 = c.template buf<T>(c.P.rawx); g.aux1 = env; g.ld_aux = DN; g.env_nv = NV;
+  gemm<T, EPI_ORB_X>(c, g);
+  if (!fl) return cudaGetLastError();
+  g = gp0<T>();
+  g.A = c.template buf<T>(c.P.B2J); g.lda = F; g.B = c.W.w[PR_ORB_UP_W_S1]; g.B2 = c.W.w[PR_ORB_DN_W_S1];
+  g.ldb = DN; g.C = c.template buf<T>(c.P.Jorb); g.ldc = DN; g.M = 3 * c.L.cap_pos;
+  g.M_dev = c.L.pos_off + c.Wc; g.M_scale = 3; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
+  g.node_map = c.L.pos_ctr; g.node_div = 3; g.dep_map = c.L.pos_dep; g.aux1 = env;
+  g.aux2 = c.template buf<T>(c.P.rjs); g.aux3 = c.template buf<T>(c.P.rawx); g.ld_aux = DN; g.env_nv = 5;
+  gemm<T, EPI_ORB_J>(c, g);
+  g = gp0<T>();
+  g.A = c.template buf<T>(c.P.B2L); g.lda = F; g.B = c.W.w[PR_ORB_UP_W_S1]; g.B2 = c.W.w[PR_ORB_DN_W_S1];
+  g.ldb = DN; g.C = c.template buf<T>(c.P.lapA); g.ldc = DN; g.M = G; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
+  g.aux1 = env; g.aux2 = c.template buf<T>(c.P.rjs); g.aux3 = c.template buf<T>(c.P.rawx); g.ld_aux = DN;
+  g.env_nv = 5;
+  gemm<T, EPI_ORB_L>(c, g);
+  return cudaGetLastError();
+}
+
+int gj_cluster(int n, size_t es, size_t* smem_out) {
+  const int cls[5] = {1, 2, 4, 8, 16};
+  for (int k = 0; k < 5; ++k) {
+    const int CL = cls[k];
+    const size_t wc = (n + CL - 1) / CL;
+    const size_t sm = (size_t)n * wc * es + (size_t)n * es + wc * es + 2 * (size_t)n * 4 + 64;
+    if (sm <= 220 * 1024) {
+      *smem_out = sm;
+      return CL;
+    }
+  }
+  return 0;
+}
+
+template <typename S, typename TI, typename TO, bool INV>
+cudaError_t launch_gj(const Ctx<TI>& c, const TI* A, TO* Ainv) {
+  const int n = c.p->n_el;
+  size_t smem = 0;
+  const int CL = gj_cluster(n, sizeof(S), &smem);
+  if (CL == 0) return cudaErrorInvalidValue;
+  auto kern = k_gauss_jordan<S, TI, TO, INV>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (CL > 8) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(CL, c.Wc * NDET, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = c.s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, A, n, CL, c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
+                            Ainv, c.status);
+}
+
+// Jastrow: attention (Q.keys narrow + V + sums + readout MLP) and MLP Jastrow; H and B1 are scratch.
+template <typename T, int NT>
+cudaError_t stage_jastrow(Ctx<T>& c) {
+  constexpr bool FLM = NT > 0;
+  const int n = c.p->n_el, G = c.Wc * n, Wc = c.Wc;
+  const int Jcap = 3 * c.L.cap_pos;
+  const int* Jdev = FLM ? c.L.pos_off + c.Wc : nullptr;
+  const Planes B2{c.P.B2X, c.P.B2J, c.P.B2L}, B1{c.P.B1X, c.P.B1J, c.P.B1L}, H{c.P.HX, c.P.HJ, c.P.HL};
+  // attention logits exp(-(h W_Qk + b_Qk) / 4)
+  k_narrow<T, HEADS, 1, FLM><<<G, 256, 0, c.s>>>(
+      c.template buf<T>(B2.X), FLM ? c.template buf<T>(B2.J) : nullptr, FLM ? c.template buf<T>(B2.L) : nullptr,
+      c.nb, c.L, c.W.w[PR_QK_W_S1], c.W.w[PR_QK_B], nullptr, nullptr, c.template buf<T>(c.P.aX),
+      FLM ? c.template buf<T>(c.P.aJ) : nullptr, FLM ? c.template buf<T>(c.P.aL) : nullptr, c.status);
+  linear_layer<T>(c, FLM, B2, B1, c.W.w[PR_V_W_S1], c.W.w[FIRE_P_ATT_V_B], F, F, G, Jcap, Jdev);
+  cudaMemsetAsync(c.template buf<T>(c.P.Ax), 0, sizeof(T) * Wc * 2 * 272, c.s);
+  if (FLM) cudaMemsetAsync(c.template buf<T>(c.P.Al), 0, sizeof(T) * Wc * 2 * 272, c.s);
+  k_att_sums<T, FLM><<<dim3(n, Wc), 256, 0, c.s>>>(
+      c.nb, c.L, c.template buf<T>(c.P.aX), FLM ? c.template buf<T>(c.P.aJ) : nullptr,
+      FLM ? c.template buf<T>(c.P.aL) : nullptr, c.template buf<T>(B1.X), FLM ? c.template buf<T>(B1.J) : nullptr,
+      FLM ? c.template buf<T>(B1.L) : nullptr, c.template buf<T>(c.P.Ax), FLM ? c.template buf<T>(c.P.Al) : nullptr,
+      FLM ? c.template buf<T>(c.P.AJ) : nullptr);
+  k_readout_in<T, FLM><<<Wc, 512, 0, c.s>>>(n, c.template buf<T>(c.P.Ax), FLM ? c.template buf<T>(c.P.Al) : nullptr,
+                                            FLM ? c.template buf<T>(c.P.AJ) : nullptr, c.template buf<T>(c.P.RX),
+                                            FLM ? c.template buf<T>(c.P.RJ) : nullptr,
+                                            FLM ? c.template buf<T>(c.P.RL) : nullptr);
+  // readout MLP 512 -> 256 -> 256 -> 2 on the dense carrier (node = walker, tangents 3n)
+  const Planes RI{c.P.RX, c.P.RJ, c.P.RL}, R1{c.P.R1X, c.P.R1J, c.P.R1L}, R2{c.P.R2X, c.P.R2J, c.P.R2L};
+  {
+    GemmP<T> g = gp0<T>();
+    // layer 1/2 with dense Jacobian rows: node of a J row = row / (3n)
+    auto dense_silu = [&](Planes in, Planes out, const T* Wt, const T* b, int K) {
+      GemmP<T> q = gp0<T>();
+      q.A = c.template buf<T>(in.X); q.lda = K; q.B = Wt; q.ldb = F; q.bias = b; q.C = c.template buf<T>(out.X);
+      q.ldc = F; q.M = Wc; q.N = F; q.K = K; q.aux0 = c.template buf<T>(c.P.Zr); q.ld_aux = F;
+      gemm<T, EPI_SILU_X>(c, q);
+      if (!FLM) return;
+      cudaMemsetAsync(c.template buf<T>(c.P.jsqr), 0, sizeof(T) * Wc * F, c.s);
+      q = gp0<T>();
+      q.A = c.template buf<T>(in.J); q.lda = K; q.B = Wt; q.ldb = F; q.C = c.template buf<T>(out.J); q.ldc = F;
+      q.M = Wc * 3 * n; q.N = F; q.K = K; q.node_div = 3 * n; q.aux1 = c.template buf<T>(c.P.Zr);
+      q.aux2 = c.template buf<T>(c.P.jsqr); q.ld_aux = F;
+      gemm<T, EPI_SILU_J>(c, q);
+      q = gp0<T>();
+      q.A = c.template buf<T>(in.L); q.lda = K; q.B = Wt; q.ldb = F; q.C = c.template buf<T>(out.L); q.ldc = F;
+      q.M = Wc; q.N = F; q.K = K; q.aux1 = c.template buf<T>(c.P.Zr); q.aux3 = c.template buf<T>(c.P.jsqr);
+      q.ld_aux = F;
+      gemm<T, EPI_SILU_L>(c, q);
+    };
+    dense_silu(RI, R1, c.W.w[FIRE_P_ATT_OUT1_W], c.W.w[FIRE_P_ATT_OUT1_B], 2 * F);
+    dense_silu(R1, R2, c.W.w[FIRE_P_ATT_OUT2_W], c.W.w[FIRE_P_ATT_OUT2_B], F);
+    g.A = c.template buf<T>(R2.X); g.lda = F; g.B = c.W.w[FIRE_P_ATT_OUT3_W]; g.ldb = 2; g.bias = c.W.w[FIRE_P_ATT_OUT3_B];
+    g.bias_period = 1; g.C = c.template buf<T>(c.P.JAx); g.ldc = 2; g.M = Wc; g.N = 2; g.K = F;
+    gemm<T, EPI_PLAIN>(c, g);
+    if (FLM) {
+      g.A = c.template buf<T>(R2.J); g.bias = nullptr; g.C = c.template buf<T>(c.P.JAj); g.M = Wc * 3 * n;
+      gemm<T, EPI_PLAIN>(c, g);
+      g.A = c.template buf<T>(R2.L); g.C = c.template buf<T>(c.P.JAl); g.M = Wc;
+      gemm<T, EPI_PLAIN>(c, g);
+    }
+  }
+  // MLP Jastrow: SparseMLP [256, 256, 2] (silu on every layer), * mlp_scale + [0, log_bias], sum over nodes
+  silu_layer<T>(c, FLM, B2, B1, c.W.w[PR_JMLP1_W_S1], c.W.w[FIRE_P_JMLP1_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3,
+                c.P.Zx, c.P.jsq);
+  silu_layer<T>(c, FLM, B1, H, c.W.w[FIRE_P_JMLP2_W], c.W.w[FIRE_P_JMLP2_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3,
+                c.P.Zx, c.P.jsq);
+  k_narrow<T, 2, 0, FLM><<<G, 256, 0, c.s>>>(
+      c.template buf<T>(H.X), FLM ? c.template buf<T>(H.J) : nullptr, FLM ? c.template buf<T>(H.L) : nullptr, c.nb,
+      c.L, c.W.w[FIRE_P_JMLP3_W], c.W.w[FIRE_P_JMLP3_B], c.W.w[FIRE_P_MLP_SCALE], c.W.w[PR_SCALARS] + 1,
+      c.template buf<T>(c.P.Xo2), FLM ? c.template buf<T>(c.P.Jo2) : nullptr,
+      FLM ? c.template buf<T>(c.P.Lo2) : nullptr, c.status);
+  k_mlp_sum<T, FLM><<<Wc, 256, 0, c.s>>>(c.nb, c.L, c.template buf<T>(c.P.Xo2),
+                                         FLM ? c.template buf<T>(c.P.Jo2) : nullptr,
+                                         FLM ? c.template buf<T>(c.P.Lo2) : nullptr, c.template buf<T>(c.P.JMx),
+                                         FLM ? c.template buf<T>(c.P.JMl) : nullptr,
+                                         FLM ? c.template buf<T>(c.P.JMj) : nullptr);
+  return cudaGetLastError();
+}
+
+// update MLP: H -> B1 -> B2 (scales[0] folded into the first weight, scales[1] into the consumers)
+template <typename T, int NT>
+cudaError_t stage_update(Ctx<T>& c) {
+  constexpr bool FLM = NT > 0;
+  const int G = c.Wc * c.p->n_el;
+  const int Jcap = 3 * c.L.cap_pos;
+  const int* Jdev = FLM ? c.L.pos_off + c.Wc : nullptr;
+  const Planes H{c.P.HX, c.P.HJ, c.P.HL}, B1{c.P.B1X, c.P.B1J, c.P.B1L}, B2{c.P.B2X, c.P.B2J, c.P.B2L};
+  silu_layer<T>(c, FLM, H, B1, c.W.w[PR_UPD1_W_S0], c.W.w[FIRE_P_UPD1_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3, c.P.Zx,
+                c.P.jsq);
+  silu_layer<T>(c, FLM, B1, B2, c.W.w[FIRE_P_UPD2_W], c.W.w[FIRE_P_UPD2_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3, c.P.Zx,
+                c.P.jsq);
+  return cudaGetLastError();
+}
+
+// value path for one chunk: writes logpsi/sign via the assembly (indices w0 + w)
+template <typename T>
+cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
+  setup_ctx(c, false);
+  stage_neighbors(c, false);
+  stage_embedding<T, 0>(c);
+  stage_update<T, 0>(c);
+  stage_orbitals<T, 0>(c);
+  // slogdet only: FP32 LU for the FP32/mixed value path, FP64 in the FP64 build
+  if constexpr (sizeof(T) == 8)
+    launch_gj<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
+  else
+    launch_gj<float, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
+  stage_jastrow<T, 0>(c);
+  AssembleOut o;
+  std::memset(&o, 0, sizeof(o));
+  o.logpsi = logpsi;
+  o.sign = sign;
+  k_assemble<T, false><<<c.Wc, 256, 3 * c.p->n_el * sizeof(double), c.s>>>(
+      c.p->n_el, c.p->n_up, c.p->n_nuc, w0_out, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
+      c.template buf<double>(c.P.sd), nullptr, nullptr, c.template buf<T>(c.P.JAx), nullptr, nullptr,
+      c.template buf<T>(c.P.JMx), nullptr, nullptr, o, c.status);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fire_eloc_debug* dbg) {
+  setup_ctx(c, true);
+  stage_neighbors(c, true);
+  stage_embedding<T, 3>(c);
+  stage_update<T, 3>(c);
+  stage_orbitals<T, 3>(c);
+  launch_gj<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+  cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
+  {
+    const size_t es = sizeof(T);
+    const size_t smem = es * (3 * DL_CMAX_DECL * (DL_CMAX_DECL + 1) + 3 * DL_CMAX_DECL * 33 + 32 * (DL_CMAX_DECL + 1));
+    cudaFuncSetAttribute(k_detlap<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_detlap<T><<<dim3(c.p->n_el, NDET, c.Wc), 256, smem, c.s>>>(
+        c.nb, c.L, c.template buf<T>(c.P.Jorb), c.template buf<T>(c.P.Ainv), c.template buf<T>(c.P.lapA),
+        c.template buf<T>(c.P.dgrad), c.template buf<double>(c.P.dlap), c.status);
+  }
+  stage_jastrow<T, 3>(c);
+  AssembleOut o;
+  std::memset(&o, 0, sizeof(o));
+  o.logpsi = logpsi;
+  o.sign = sign;
+  o.eloc = eloc;
+  if (dbg) o.dbg = *dbg;
+  k_assemble<T, true><<<c.Wc, 256, 3 * c.p->n_el * sizeof(double), c.s>>>(
+      c.p->n_el, c.p->n_up, c.p->n_nuc, c.w0, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
+      c.template buf<double>(c.P.sd), c.template buf<T>(c.P.dgrad), c.template buf<double>(c.P.dlap),
+      c.template buf<T>(c.P.JAx), c.template buf<T>(c.P.JAj), c.template buf<T>(c.P.JAl), c.template buf<T>(c.P.JMx),
+      c.template buf<T>(c.P.JMj), c.template buf<T>(c.P.JMl), o, c.status);
+  return cudaGetLastError();
+}
+
+template <typename T>
+Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
+                int32_t* status, void* ws, int Wmax, bool fl) {
+  Ctx<T> c;
+  c.p = p;
+  c.s = s;
+  c.Wmax = Wmax;
+  c.B = p->n_walkers;
+  c.R = R;
+  c.Z = Z;
+  c.W = make_weights<T>(p, prepared);
+  c.status = status;
+  c.ws = reinterpret_cast<unsigned char*>(ws);
+  c.P = make_plan(p, Wmax, fl);
+  return c;
+}
+
+template <typename T>
+fire_status run_eloc(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
+                     const void* r, void* logpsi, void* sign, void* eloc, double* stats, const fire_eloc_debug* dbg,
+                     void* ws, size_t wsb, int32_t* status) {
+  const int Wc = choose_chunk(p, wsb, true);
+  if (Wc <= 0) return FIRE_ERR_WORKSPACE;
+  Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, true);
+  const T* rr = reinterpret_cast<const T*>(r);
+  for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {
+    c.w0 = w0;
+    c.Wc = std::min(Wc, p->n_walkers - w0);
+    c.r = rr + (size_t)w0 * p->n_el * 3;
+    if (chunk_eloc<T>(c, logpsi, sign, eloc, dbg) != cudaSuccess) return FIRE_ERR_CUDA;
+  }
+  if (stats) k_stats<T><<<1, 1024, 0, s>>>(reinterpret_cast<const T*>(eloc), p->n_walkers, stats);
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+template <typename T>
+fire_status run_logpsi(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
+                       const void* r, void* sign, void* logpsi, void* ws, size_t wsb, int32_t* status) {
+  const int Wc = choose_chunk(p, wsb, false);
+  if (Wc <= 0) return FIRE_ERR_WORKSPACE;
+  Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
+  const T* rr = reinterpret_cast<const T*>(r);
+  for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {
+    c.w0 = w0;
+    c.Wc = std::min(Wc, p->n_walkers - w0);
+    c.r = rr + (size_t)w0 * p->n_el * 3;
+    if (chunk_logpsi<T>(c, logpsi, sign, w0) != cudaSuccess) return FIRE_ERR_CUDA;
+  }
+  return FIRE_OK;
+}
+
+template <typename T>
+fire_status run_embedding(const fire_problem* p, cudaStream_t s, const float* R, const void* prepared,
+                          const void* r, void* hc, void* hu, void* ws, size_t wsb, int32_t* status) {
+  const int Wc = choose_chunk(p, wsb, false);
+  if (Wc <= 0) return FIRE_ERR_WORKSPACE;
+  Ctx<T> c = make_ctx<T>(p, s, R, nullptr, prepared, status, ws, Wc, false);
+  const T* rr = reinterpret_cast<const T*>(r);
+  for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {
+    c.w0 = w0;
+    c.Wc = std::min(Wc, p->n_walkers - w0);
+    c.r = rr + (size_t)w0 * p->n_el * 3;
+    setup_ctx(c, false);
+    stage_neighbors(c, false);
+    stage_embedding<T, 0>(c);
+    stage_update<T, 0>(c);
+    const size_t cnt = (size_t)c.Wc * p->n_el * F;
+    if (hc)
+      cudaMemcpyAsync(reinterpret_cast<T*>(hc) + (size_t)w0 * p->n_el * F, c.template buf<T>(c.P.HX),
+                      cnt * sizeof(T), cudaMemcpyDeviceToDevice, s);
+    if (hu)
+      cudaMemcpyAsync(reinterpret_cast<T*>(hu) + (size_t)w0 * p->n_el * F, c.template buf<T>(c.P.B2X),
+                      cnt * sizeof(T), cudaMemcpyDeviceToDevice, s);
+    if (cudaGetLastError() != cudaSuccess) return FIRE_ERR_CUDA;
+  }
+  return FIRE_OK;
+}
+
+template <typename T>
+fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
+                     void* r, void* logpsi, int steps, float width, uint64_t seed, uint64_t counter,
+                     const void* noise, const void* logu, int32_t* n_accept, int32_t* static_max, void* ws,
+                     size_t wsb, int32_t* status) {
+  const int Wc = choose_chunk(p, wsb, false);
+  if (Wc <= 0) return FIRE_ERR_WORKSPACE;
+  Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
+  T* rr = reinterpret_cast<T*>(r);
+  const int n = p->n_el;
+  for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {
+    c.w0 = w0;
+    c.Wc = std::min(Wc, p->n_walkers - w0);
+    T* rn = c.template buf<T>(c.P.rn);
+    T* lpn = c.template buf<T>(c.P.lpn);
+    for (int st = 0; st < steps; ++st) {
+      k_propose<T><<<nblk((long)c.Wc * n), 256, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, c.Wc, w0, p->n_walkers, st,
+                                                        (T)width, seed, counter,
+                                                        reinterpret_cast<const T*>(noise));
+      c.r = rn;
+      if (chunk_logpsi<T>(c, lpn, nullptr, 0) != cudaSuccess) return FIRE_ERR_CUDA;
+      k_accept<T><<<c.Wc, 128, 0, s>>>(rr, rn, reinterpret_cast<T*>(logpsi), lpn, n, w0, p->n_walkers, st, seed,
+                                      counter, reinterpret_cast<const T*>(logu), n_accept, c.nb.counts, static_max);
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+}  // namespace
+
+// ================================================================================== C ABI
+extern "C" {
+
+int32_t fire_abi_version(void) { return FIRE_ABI_VERSION; }
+
+fire_status fire_param_layout(const fire_problem* prob, int64_t* offsets) {
+  if (!valid(prob) || !offsets) return FIRE_ERR_INVALID;
+  blob_offsets(prob, offsets);
+  return FIRE_OK;
+}
+
+fire_status fire_prepared_size(const fire_problem* prob, size_t* bytes) {
+  if (!valid(prob) || !bytes) return FIRE_ERR_INVALID;
+  int64_t off[PR_COUNT + 1];
+  prep_offsets(prob, off);
+  *bytes = (size_t)off[PR_COUNT] * elem_size(prob);
+  return FIRE_OK;
+}
+
+fire_status fire_workspace_size(const fire_problem* prob, int32_t chunk, size_t* bytes) {
+  if (!valid(prob) || !bytes) return FIRE_ERR_INVALID;
+  const int c = chunk > 0 ? std::min(chunk, prob->n_walkers) : prob->n_walkers;
+  *bytes = make_plan(prob, c, true).total;
+  return FIRE_OK;
+}
+
+fire_status fire_prepare_params(void* stream, const fire_problem* prob, const float* blob,
+                                const int64_t* offsets_host, void* prepared, size_t prepared_bytes) {
+  if (!valid(prob) || !blob || !offsets_host || !prepared) return FIRE_ERR_INVALID;
+  int64_t ref[FIRE_P_COUNT + 1];
+  blob_offsets(prob, ref);
+  for (int k = 0; k <= FIRE_P_COUNT; ++k)
+    if (offsets_host[k] != ref[k]) return FIRE_ERR_INVALID;
+  size_t need = 0;
+  fire_prepared_size(prob, &need);
+  if (prepared_bytes < need) return FIRE_ERR_WORKSPACE;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64) return prepare_impl<double>(s, prob, blob, offsets_host, prepared);
+  return prepare_impl<float>(s, prob, blob, offsets_host, prepared);
+}
+
+fire_status fire_neighbors(void* stream, const fire_problem* prob, const void* r, const float* R,
+                           const fire_neighbor_out* out, int32_t* status) {
+  if (!valid(prob) || !r || !R || !out) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  Nbr nb;
+  std::memset(&nb, 0, sizeof(nb));
+  nb.W = prob->n_walkers;
+  nb.n = prob->n_el;
+  nb.n_up = prob->n_up;
+  nb.N = prob->n_nuc;
+  nb.cap_p = prob->cap_pairs;
+  nb.cap_nuc = prob->cap_nuc;
+  const int n = prob->n_el;
+  if (prob->precision == FIRE_PREC_FP64) {
+    const size_t smem = 3 * n * sizeof(double) + (5 * n + 2) * sizeof(int);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_neighbors<double><<<prob->n_walkers, 512, smem, s>>>(reinterpret_cast<const double*>(r), R,
+                                                          (double)prob->cutoff, (double)prob->cutoff_1el, nb, *out,
+                                                          status);
+  } else {
+    const size_t smem = 3 * n * sizeof(float) + (5 * n + 2) * sizeof(int);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_neighbors<float><<<prob->n_walkers, 512, smem, s>>>(reinterpret_cast<const float*>(r), R, prob->cutoff,
+                                                         prob->cutoff_1el, nb, *out, status);
+  }
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+fire_status fire_triplets(void* stream, const fire_problem* prob, const void* r, int32_t cap_triplets,
+                          int32_t* trip_in, int32_t* trip_k, int32_t* trip_kn, int32_t* trip_i, void* workspace,
+                          size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !r || !trip_in || !trip_k || !trip_kn || !trip_i || cap_triplets < 1)
+    return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int n = prob->n_el, B = prob->n_walkers;
+  const size_t need = (size_t)B * (n + (n + 1) + 2 * prob->cap_pairs + n + (size_t)n * prob->cap_nuc + 4) * 4 + 1024;
+  if (workspace_bytes < need || !workspace) return FIRE_ERR_WORKSPACE;
+  int* w = reinterpret_cast<int*>(workspace);
+  Nbr nb;
+  nb.W = B; nb.n = n; nb.n_up = prob->n_up; nb.N = prob->n_nuc; nb.cap_p = prob->cap_pairs; nb.cap_nuc = prob->cap_nuc;
+  nb.deg = w; w += (size_t)B * n;
+  nb.rowptr = w; w += (size_t)B * (n + 1);
+  nb.nbr = w; w += (size_t)B * prob->cap_pairs;
+  nb.rev = w; w += (size_t)B * prob->cap_pairs;
+  nb.en_cnt = w; w += (size_t)B * n;
+  nb.en_idx = w; w += (size_t)B * n * prob->cap_nuc;
+  nb.counts = w;
+  fire_neighbor_out ext;
+  std::memset(&ext, 0, sizeof(ext));
+  // R is not needed for the e-e structure; nuclei enter only the e-n lists, which are skipped here
+  static_assert(sizeof(int) == 4, "int32");
+  Nbr nb2 = nb;
+  nb2.N = 0;
+  if (prob->precision == FIRE_PREC_FP64) {
+    const size_t smem = 3 * n * sizeof(double) + (5 * n + 2) * sizeof(int);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_neighbors<double><<<B, 512, smem, s>>>(reinterpret_cast<const double*>(r), nullptr, (double)prob->cutoff,
+                                            (double)prob->cutoff_1el, nb2, ext, status);
+  } else {
+    const size_t smem = 3 * n * sizeof(float) + (5 * n + 2) * sizeof(int);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_neighbors<float><<<B, 512, smem, s>>>(reinterpret_cast<const float*>(r), nullptr, prob->cutoff,
+                                           prob->cutoff_1el, nb2, ext, status);
+  }
+  k_triplets<<<B, 256, 0, s>>>(nb, cap_triplets, trip_in, trip_k, trip_kn, trip_i, status);
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+fire_status fire_logpsi(void* stream, const fire_problem* prob, const float* R, const float* Z, const void* prepared,
+                        const void* r, void* sign, void* logpsi, void* workspace, size_t workspace_bytes,
+                        int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_logpsi<double>(prob, s, R, Z, prepared, r, sign, logpsi, workspace, workspace_bytes, status);
+  return run_logpsi<float>(prob, s, R, Z, prepared, r, sign, logpsi, workspace, workspace_bytes, status);
+}
+
+fire_status fire_local_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                              const void* prepared, const void* r, void* logpsi, void* sign, void* e_loc,
+                              double* e_stats, const fire_eloc_debug* debug, void* workspace, size_t workspace_bytes,
+                              int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !e_loc || !workspace) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_eloc<double>(prob, s, R, Z, prepared, r, logpsi, sign, e_loc, e_stats, debug, workspace,
+                            workspace_bytes, status);
+  return run_eloc<float>(prob, s, R, Z, prepared, r, logpsi, sign, e_loc, e_stats, debug, workspace, workspace_bytes,
+                         status);
+}
+
+fire_status fire_embedding(void* stream, const fire_problem* prob, const float* R, const void* prepared, const void* r,
+                           void* h_contract, void* h_update, void* workspace, size_t workspace_bytes,
+                           int32_t* status) {
+  if (!valid(prob) || !R || !prepared || !r || !workspace) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_embedding<double>(prob, s, R, prepared, r, h_contract, h_update, workspace, workspace_bytes, status);
+  return run_embedding<float>(prob, s, R, prepared, r, h_contract, h_update, workspace, workspace_bytes, status);
+}
+
+fire_status fire_mcmc_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                            const void* prepared, void* r, void* logpsi, int32_t steps, float width, uint64_t seed,
+                            uint64_t counter, const void* replay_noise, const void* replay_log_u, int32_t* n_accept,
+                            int32_t* static_max, void* workspace, size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0) return FIRE_ERR_INVALID;
+  if ((replay_noise == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise,
+                            replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
+  return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise, replay_log_u,
+                         n_accept, static_max, workspace, workspace_bytes, status);
+}
+
+fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r, const float* R,
+                                  const float* Z, void* out) {
+  if (!valid(prob) || !r || !R || !Z || !out) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    k_potential<double><<<prob->n_walkers, 256, 0, s>>>(prob->n_el, prob->n_nuc, reinterpret_cast<const double*>(r),
+                                                        R, Z, reinterpret_cast<double*>(out));
+  else
+    k_potential<float><<<prob->n_walkers, 256, 0, s>>>(prob->n_el, prob->n_nuc, reinterpret_cast<const float*>(r), R,
+                                                       Z, reinterpret_cast<float*>(out));
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,266 @@
+// fire_gemm.cuh -- CUDA-core GEMM C = A[M,K] * B[K,N] with fused forward-Laplacian epilogues.
+//
+// This is the contraction engine of the FP32 and FP64 paths.  Every dense layer of the sparse
+// forward Laplacian (sparse_fwd_lap.py:160-225) is applied to three "planes" of one node:
+//   X plane  [nodes, K]        values            (bias added)
+//   J plane  [3 * positions, K] Jacobian rows    (sorted by center)
+//   L plane  [nodes, K]        Laplacians
+// and the ElementWise rule (sparse_fwd_lap.py:196-206) is fused into the epilogues:
+//   X:  z = acc + b;  store z and silu(z)
+//   J:  out = acc * silu'(z[center]);  jsq[center] += acc^2  (segmented over the tile's rows)
+//   L:  out = acc * silu'(z) + jsq * silu''(z)
+// The orbital layer (orbitals.py:148-174 + multiply_with_1el_fn, sparse_fwd_lap.py:322-335) uses
+// per-spin weights (rows of spin-up centers use B, spin-down centers B2) and multiplies by the
+// envelope carrier in its epilogues.
+#pragma once
+#include "fire_common.cuh"
+
+namespace fire {
+
+enum EpiMode { EPI_PLAIN = 0, EPI_SILU_X, EPI_SILU_J, EPI_SILU_L, EPI_ORB_X, EPI_ORB_J, EPI_ORB_L, EPI_ENV };
+
+template <typename T>
+struct GemmP {
+  const T* A;
+  long lda;
+  const T* B;
+  long ldb;
+  const T* B2;  // spin-down weights (or nullptr)
+  const T* bias;
+  const T* bias2;
+  int bias_period;  // bias added on rows with row % bias_period == 0 (0: no bias)
+  T* C;
+  long ldc;
+  int M;             // row capacity
+  const int* M_dev;  // optional device row count: rows = min(M, M_scale * *M_dev)
+  int M_scale;
+  int N, K;
+  const int* node_map;  // node of a row = node_map ? node_map[row / node_div] : row / node_div
+  int node_div;
+  int n_el, n_up;       // spin of node g: (g % n_el) < n_up
+  T* aux0;
+  const T* aux1;
+  T* aux2;
+  const T* aux3;
+  long ld_aux;
+  const int* dep_map;  // ORB_J: a position is "self" when dep_map[pos] == node
+  int env_ns, env_soff;  // ENV: rows are (w * env_ns + i) * env_nv + v  ->  electron w * n_el + env_soff + i
+  int env_nv;            // rows per electron of the envelope carrier (5: x, jac xyz, lap; 1: value)
+};
+
+constexpr int GBM = 128, GBN = 128, GBK = 8, GTHREADS = 256;
+
+template <typename T>
+__device__ __forceinline__ int gemm_node(const GemmP<T>& p, int row) {
+  return p.node_map ? p.node_map[row / p.node_div] : row / p.node_div;
+}
+
+template <typename T, int MODE>
+__device__ __forceinline__ void gemm_store(const GemmP<T>& p, int row, int col, T acc, int pass_spin) {
+  if (MODE == EPI_PLAIN) {
+    T v = acc;
+    if (p.bias && p.bias_period > 0 && (row % p.bias_period) == 0) v += p.bias[col];
+    p.C[(long)row * p.ldc + col] = v;
+  } else if (MODE == EPI_SILU_X) {
+    T z = acc + (p.bias ? p.bias[col] : T(0));
+    p.aux0[(long)row * p.ld_aux + col] = z;
+    p.C[(long)row * p.ldc + col] = silu(z);
+  } else if (MODE == EPI_SILU_J) {
+    const int node = gemm_node(p, row);
+    T y, d1, d2;
+    silu3(p.aux1[(long)node * p.ld_aux + col], y, d1, d2);
+    p.C[(long)row * p.ldc + col] = acc * d1;
+  } else if (MODE == EPI_SILU_L) {
+    T y, d1, d2;
+    silu3(p.aux1[(long)row * p.ld_aux + col], y, d1, d2);
+    p.C[(long)row * p.ldc + col] = acc * d1 + p.aux3[(long)row * p.ld_aux + col] * d2;
+  } else if (MODE == EPI_ORB_X) {
+    const T* b = pass_spin == 0 ? p.bias : p.bias2;
+    const T raw = acc + b[col];
+    p.aux0[(long)row * p.ld_aux + col] = raw;
+    p.C[(long)row * p.ldc + col] = raw * p.aux1[(long)row * p.env_nv * p.ld_aux + col];
+  } else if (MODE == EPI_ORB_J) {
+    const int pos = row / 3, t = row - 3 * (row / 3);
+    const int node = p.node_map[pos];
+    const T* env = p.aux1 + (long)node * 5 * p.ld_aux;
+    const T ex = env[col];
+    if (p.dep_map[pos] == node) {
+      const T raw = p.aux3[(long)node * p.ld_aux + col];
+      p.C[(long)row * p.ldc + col] = raw * env[(1 + t) * p.ld_aux + col] + ex * acc;
+      p.aux2[((long)node * 3 + t) * p.ld_aux + col] = acc;
+    } else {
+      p.C[(long)row * p.ldc + col] = ex * acc;
+    }
+  } else if (MODE == EPI_ORB_L) {
+    const T* env = p.aux1 + (long)row * 5 * p.ld_aux;
+    const T* rjs = p.aux2 + (long)row * 3 * p.ld_aux;
+    T v = acc * env[col] + env[4 * p.ld_aux + col] * p.aux3[(long)row * p.ld_aux + col];
+    v += T(2) * (rjs[col] * env[p.ld_aux + col] + rjs[p.ld_aux + col] * env[2 * p.ld_aux + col] +
+                 rjs[2 * p.ld_aux + col] * env[3 * p.ld_aux + col]);
+    p.C[(long)row * p.ldc + col] = v;
+  } else if (MODE == EPI_ENV) {
+    const int rr = row / p.env_nv, v = row - p.env_nv * rr;
+    const int g = (rr / p.env_ns) * p.n_el + p.env_soff + rr % p.env_ns;
+    p.C[((long)g * p.env_nv + v) * p.ldc + col] = acc;
+  }
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(GTHREADS) k_gemm(GemmP<T> p) {
+  __shared__ __align__(16) T As[2][GBK][GBM];
+  __shared__ __align__(16) T Bs[2][GBK][GBN];
+  extern __shared__ __align__(16) unsigned char gemm_dyn[];  // SILU_J: [GBM][GBN + 1] squares
+  __shared__ int row_node[GBM];
+
+  int rows = p.M;
+  if (p.M_dev) rows = min(rows, p.M_scale * (*p.M_dev));
+  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+  if (m0 >= rows) return;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+
+  // spin composition of the tile (per-spin weights)
+  int passes = 1, first_spin = 0;
+  if (p.B2) {
+    int up = 0, dn = 0;
+    if (tid < GBM && m0 + tid < rows) {
+      const int node = gemm_node(p, m0 + tid);
+      if ((node % p.n_el) < p.n_up) up = 1; else dn = 1;
+    }
+    up = __syncthreads_or(up);
+    dn = __syncthreads_or(dn);
+    first_spin = up ? 0 : 1;
+    passes = up + dn;
+  }
+  if (MODE == EPI_SILU_J) {
+    if (tid < GBM) row_node[tid] = (m0 + tid < rows) ? gemm_node(p, m0 + tid) : -1;
+  }
+
+  for (int pass = 0; pass < passes; ++pass) {
+    const int spin = first_spin + pass;
+    const T* Bp = spin == 0 ? p.B : p.B2;
+    T acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+
+    // global -> register staging: A: row a_r, k a_k..a_k+3; B: k b_k, cols b_c..b_c+3
+    const int a_r = tid >> 1, a_k = (tid & 1) * 4;
+    const int b_k = tid >> 5, b_c = (tid & 31) * 4;
+    T ra[4], rb[4];
+    auto load_tile = [&](int k0) {
+      const int gr = m0 + a_r;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int gk = k0 + a_k + u;
+        ra[u] = (gr < rows && gk < p.K) ? p.A[(long)gr * p.lda + gk] : T(0);
+      }
+      const int gk = k0 + b_k;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int gc = n0 + b_c + u;
+        rb[u] = (gk < p.K && gc < p.N) ? Bp[(long)gk * p.ldb + gc] : T(0);
+      }
+    };
+    auto store_tile = [&](int buf) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) As[buf][a_k + u][a_r] = ra[u];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) Bs[buf][b_k][b_c + u] = rb[u];
+    };
+    load_tile(0);
+    store_tile(0);
+    __syncthreads();
+    int buf = 0;
+    for (int k0 = 0; k0 < p.K; k0 += GBK) {
+      const bool more = k0 + GBK < p.K;
+      if (more) load_tile(k0 + GBK);
+#pragma unroll
+      for (int kk = 0; kk < GBK; ++kk) {
+        T a[8], b[8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          a[i] = As[buf][kk][ty * 4 + i];
+          a[4 + i] = As[buf][kk][64 + ty * 4 + i];
+          b[i] = Bs[buf][kk][tx * 4 + i];
+          b[4 + i] = Bs[buf][kk][64 + tx * 4 + i];
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] += a[i] * b[j];
+      }
+      if (more) {
+        store_tile(buf ^ 1);
+        __syncthreads();
+        buf ^= 1;
+      }
+    }
+
+    // ---- epilogue
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int lr = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+      const int row = m0 + lr;
+      if (row >= rows) continue;
+      if (p.B2) {
+        const int node = gemm_node(p, row);
+        const int s = ((node % p.n_el) < p.n_up) ? 0 : 1;
+        if (s != spin) continue;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int col = n0 + ((j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+        if (col < p.N) gemm_store<T, MODE>(p, row, col, acc[i][j], spin);
+      }
+    }
+    if (MODE == EPI_SILU_J) {
+      // segmented sum of acc^2 over rows of the same center, one atomic per (segment, column)
+      T* sq = reinterpret_cast<T*>(gemm_dyn);
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int lr = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int lc = (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
+          sq[lr * (GBN + 1) + lc] = acc[i][j] * acc[i][j];
+        }
+      }
+      __syncthreads();
+      // 256 threads: column lc = tid & 127, rows half (tid >> 7)
+      const int lc = tid & (GBN - 1), half = tid >> 7;
+      const int col = n0 + lc;
+      if (col < p.N) {
+        int cur = -1;
+        T s = T(0);
+        for (int lr = half * 64; lr < half * 64 + 64; ++lr) {
+          const int nd = row_node[lr];
+          if (nd != cur) {
+            if (cur >= 0) atomic_add(&p.aux2[(long)cur * p.ld_aux + col], s);
+            cur = nd;
+            s = T(0);
+          }
+          if (nd >= 0) s += sq[lr * (GBN + 1) + lc];
+        }
+        if (cur >= 0) atomic_add(&p.aux2[(long)cur * p.ld_aux + col], s);
+      }
+    }
+    if (pass + 1 < passes) __syncthreads();
+  }
+}
+
+template <typename T, int MODE>
+inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
+  dim3 grid((p.N + GBN - 1) / GBN, (p.M + GBM - 1) / GBM);
+  size_t dyn = (MODE == EPI_SILU_J) ? sizeof(T) * GBM * (GBN + 1) : 0;
+  if (dyn > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_gemm<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+  }
+  if (grid.y == 0 || grid.x == 0) return cudaSuccess;
+  k_gemm<T, MODE><<<grid, GTHREADS, dyn, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace fire

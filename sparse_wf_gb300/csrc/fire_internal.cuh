@@ -1,0 +1,36 @@
+// fire_internal.cuh -- device-side data structures shared by the pipeline stages.
+#pragma once
+#include "fire_common.cuh"
+
+namespace fire {
+
+// Neighbour structure of one chunk of walkers (all walkers of a chunk share n, n_up, n_nuc).
+// Per walker w and electron i the directed e-e pairs (i, j), j != i, |r_i - r_j| < cutoff, are
+// stored CSR-style sorted by (i, j): the same row-major order as jnp.where in get_pair_indices
+// (model/new_sparse_model.py:238-263).
+struct Nbr {
+  int W, n, n_up, N, cap_p, cap_nuc;
+  int* deg;     // [W, n]        neighbours of i
+  int* rowptr;  // [W, n + 1]    exclusive prefix of deg
+  int* nbr;     // [W, cap_p]    neighbour j of pair p
+  int* rev;     // [W, cap_p]    index of the reverse pair (j, i)
+  int* en_cnt;  // [W, n]        e-n neighbours (capped at cap_nuc)
+  int* en_idx;  // [W, n, cap_nuc] nucleus indices, ascending
+  int* counts;  // [W, 4]        n_pairs_same, n_pairs_diff, n_triplets, n_neighbours_en
+};
+
+// Sparse forward-Laplacian layout of a chunk ("positions" = Jacobian rows of NodeWithFwdLap,
+// sparse_fwd_lap.py:14-22).  Per walker w the positions of center i are
+//   q = pos_off[w] + rowptr[w][i] + i + k,  k = 0 (self, dep = i) and k = 1..deg(i) (pair (i, j_k)),
+// i.e. positions are sorted by center.  Jacobian plane rows are 3 * q + xyz.
+// dep_pos lists, for every dep m, the positions (i, m), i in {m} + N(m): slot
+//   pos_off[w] + rowptr[w][m] + m + k holds the global position of the k-th of them.
+struct Layout {
+  int* pos_off;  // [W + 1]
+  int* pos_ctr;  // [cap_pos] global electron id (w * n + i) of the center
+  int* pos_dep;  // [cap_pos] global electron id of the dependency
+  int* dep_pos;  // [cap_pos] positions grouped by dependency
+  int cap_pos;   // capacity = W * (n + cap_p)
+};
+
+}  // namespace fire

@@ -1,0 +1,75 @@
+// fire_kernels.cuh -- declarations of the kernels defined (and explicitly instantiated) in the
+// stage translation units, so that fire_api.cu can launch them.
+#pragma once
+#include "fire_internal.cuh"
+
+namespace fire {
+
+// fire_neighbors.cu
+template <typename T>
+__global__ void k_neighbors(const T* r, const float* R, T cutoff, T cutoff_1el, Nbr nb, fire_neighbor_out ext,
+                            int32_t* status);
+__global__ void k_triplets(Nbr nb, int cap_t, int32_t* t_in, int32_t* t_k, int32_t* t_kn, int32_t* t_i,
+                           int32_t* status);
+__global__ void k_pos_scan(Nbr nb, int* pos_off);
+__global__ void k_layout(Nbr nb, Layout L);
+
+// fire_embed.cu
+template <typename T, int NT>
+__global__ void k_elec_init(const T* r, const float* R, Nbr nb, Weights<T> W, T inv_cutoff1, T* E5);
+template <typename T, int NT>
+__global__ void k_glu(const T* Z, T* out, int G);
+template <typename T, int NT>
+__global__ void k_silu5(T* Z, int G);
+template <typename T, int NT>
+__global__ void k_edge_contract(const T* r, Nbr nb, Layout L, Weights<T> W, const T* E5o, T* X, T* Lp, T* Jp);
+
+// fire_det.cu
+template <typename T, int NV>
+__global__ void k_env_coef(const T* r, const float* R, const T* sp, int n, int n_s, int s_off, int N, int Wn,
+                           T* coef);
+template <typename S, typename TI, typename TO, bool INV>
+__global__ void k_gauss_jordan(const TI* A, int n, int CL, double* logdet, double* sign, TO* Ainv,
+                               int32_t* status);
+template <typename T>
+__global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* lapA, T* grad, double* lap,
+                         int32_t* status);
+constexpr int DL_CMAX_DECL = 64;
+
+// fire_jastrow.cu
+struct AssembleOut {
+  void* logpsi;
+  void* sign;
+  void* eloc;
+  fire_eloc_debug dbg;
+};
+template <typename T, int NC, int ACT, bool FLM>
+__global__ void k_narrow(const T* X, const T* Jp, const T* Lp, Nbr nb, Layout L, const T* Wn, const T* bn,
+                         const T* post_scale, const T* post_shift, T* Xo, T* Jo, T* Lo, int32_t* status);
+template <typename T, bool FLM>
+__global__ void k_mlp_sum(Nbr nb, Layout L, const T* Xo, const T* Jo, const T* Lo, T* ox, T* ol, T* oj);
+template <typename T, bool FLM>
+__global__ void k_att_sums(Nbr nb, Layout L, const T* aX, const T* aJ, const T* aL, const T* VX, const T* VJ,
+                           const T* VL, T* Ax, T* Al, T* AJ);
+template <typename T, bool FLM>
+__global__ void k_readout_in(int n, const T* Ax, const T* Al, const T* AJ, T* RX, T* RJ, T* RL);
+template <typename T, bool FLM>
+__global__ void k_assemble(int n, int n_up, int N, int w0, const T* r, const float* R, const float* Z,
+                           Weights<T> W, const double* ld, const double* sd, const T* dgrad, const double* dlap,
+                           const T* JAx, const T* JAj, const T* JAl, const T* JMx, const T* JMj, const T* JMl,
+                           AssembleOut out, int32_t* status);
+template <typename T>
+__global__ void k_potential(int n, int N, const T* r, const float* R, const float* Z, T* out);
+template <typename T>
+__global__ void k_stats(const T* e, int B, double* out);
+
+// fire_mcmc.cu
+template <typename T>
+__global__ void k_propose(const T* r, T* rn, int n, int Wc, int w0, int B, int step, T width, uint64_t seed,
+                          uint64_t counter, const T* replay);
+template <typename T>
+__global__ void k_accept(T* r, const T* rn, T* logpsi, const T* logpsi_new, int n, int w0, int B, int step,
+                         uint64_t seed, uint64_t counter, const T* replay_log_u, int32_t* n_accept, const int* counts,
+                         int32_t* static_max);
+
+}  // namespace fire

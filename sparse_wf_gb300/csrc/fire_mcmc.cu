@@ -1,0 +1,106 @@
+// fire_mcmc.cu -- all-electron Metropolis proposal and accept/reject (mcmc.py:38-97).
+//
+// Random numbers: Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11), counter = (step, walker, electron, stream counter), key = seed; normals by Box-Muller.
+// jax.random (threefry) cannot be reproduced here, so bit-level parity of the chain is checked in
+// replay mode, where the caller supplies the normal draws and log-uniforms.
+#include "fire_internal.cuh"
+
+namespace fire {
+
+struct Philox {
+  uint32_t c[4];
+};
+
+__device__ __forceinline__ void philox_round(uint32_t (&ctr)[4], uint32_t (&key)[2]) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t hi0 = __umulhi(M0, ctr[0]), lo0 = M0 * ctr[0];
+  const uint32_t hi1 = __umulhi(M1, ctr[2]), lo1 = M1 * ctr[2];
+  const uint32_t n0 = hi1 ^ ctr[1] ^ key[0], n1 = lo1, n2 = hi0 ^ ctr[3] ^ key[1], n3 = lo0;
+  ctr[0] = n0; ctr[1] = n1; ctr[2] = n2; ctr[3] = n3;
+}
+
+__device__ __forceinline__ void philox10(uint32_t (&ctr)[4], uint64_t seed) {
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    philox_round(ctr, key);
+    key[0] += 0x9E3779B9u;
+    key[1] += 0xBB67AE85u;
+  }
+}
+
+__device__ __forceinline__ double u01(uint32_t x) { return ((double)(x >> 8) + 0.5) * (1.0 / 16777216.0); }
+
+// r_new = r + width * eps for every electron of every walker of the chunk.
+template <typename T>
+__global__ void k_propose(const T* __restrict__ r, T* __restrict__ rn, int n, int Wc, int w0, int B, int step,
+                          T width, uint64_t seed, uint64_t counter, const T* __restrict__ replay) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;  // (w, e)
+  if (idx >= (long)Wc * n) return;
+  const int w = (int)(idx / n), e = (int)(idx - (long)w * n);
+  const long gw = w0 + w;
+  T eps[3];
+  if (replay) {
+    const T* src = replay + (((long)step * B + gw) * n + e) * 3;
+    eps[0] = src[0]; eps[1] = src[1]; eps[2] = src[2];
+  } else {
+    uint32_t ctr[4] = {(uint32_t)step, (uint32_t)gw, (uint32_t)e, (uint32_t)counter};
+    philox10(ctr, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
+    const double r1 = sqrt(-2.0 * log(u01(ctr[0]))), t1 = 6.283185307179586 * u01(ctr[1]);
+    const double r2 = sqrt(-2.0 * log(u01(ctr[2]))), t2 = 6.283185307179586 * u01(ctr[3]);
+    eps[0] = (T)(r1 * cos(t1));
+    eps[1] = (T)(r1 * sin(t1));
+    eps[2] = (T)(r2 * cos(t2));
+  }
+  const long base = idx * 3;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) rn[base + c] = r[base + c] + width * eps[c];
+}
+
+// Accept if 2 (logpsi_new - logpsi_old) > log u (mcmc.py:68-73); one CTA per walker.
+// r, logpsi: whole batch (global walker index); rn, logpsi_new, counts: this chunk (local index).
+template <typename T>
+__global__ void k_accept(T* __restrict__ r, const T* __restrict__ rn, T* __restrict__ logpsi,
+                         const T* __restrict__ logpsi_new, int n, int w0, int B, int step, uint64_t seed,
+                         uint64_t counter, const T* __restrict__ replay_log_u, int32_t* __restrict__ n_accept,
+                         const int* __restrict__ counts, int32_t* __restrict__ static_max) {
+  const int w = blockIdx.x;
+  const long gw = w0 + w;
+  __shared__ int acc_s;
+  if (threadIdx.x == 0) {
+    double logu;
+    if (replay_log_u) {
+      logu = (double)replay_log_u[(long)step * B + gw];
+    } else {
+      uint32_t ctr[4] = {(uint32_t)step, (uint32_t)gw, 0xFFFFFFFFu, (uint32_t)counter};
+      philox10(ctr, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
+      logu = log(u01(ctr[0]));
+    }
+    const double ratio = 2.0 * ((double)logpsi_new[w] - (double)logpsi[gw]);
+    const int a = ratio > logu ? 1 : 0;
+    acc_s = a;
+    if (a) logpsi[gw] = logpsi_new[w];
+    if (n_accept) n_accept[gw] += a;
+    if (static_max && counts) {
+      atomicMax(&static_max[0], counts[w * 4 + 0]);
+      atomicMax(&static_max[1], counts[w * 4 + 1]);
+      atomicMax(&static_max[3], counts[w * 4 + 3]);
+    }
+  }
+  __syncthreads();
+  if (acc_s) {
+    for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) r[gw * 3 * n + k] = rn[(long)w * 3 * n + k];
+  }
+}
+
+template __global__ void k_propose<float>(const float*, float*, int, int, int, int, int, float, uint64_t, uint64_t,
+                                          const float*);
+template __global__ void k_propose<double>(const double*, double*, int, int, int, int, int, double, uint64_t,
+                                           uint64_t, const double*);
+template __global__ void k_accept<float>(float*, const float*, float*, const float*, int, int, int, int, uint64_t,
+                                         uint64_t, const float*, int32_t*, const int*, int32_t*);
+template __global__ void k_accept<double>(double*, const double*, double*, const double*, int, int, int, int,
+                                          uint64_t, uint64_t, const double*, int32_t*, const int*, int32_t*);
+
+}  // namespace fire

@@ -1,0 +1,362 @@
+"""Host-side mirror of the reference's wavefunction / local-energy / MCMC interface.
+
+``FireWaveFunction`` follows ``MoonLikeWaveFunction`` (``src/sparse_wf/model/wave_function.py:67-221``)
+for the ``new_sparse`` embedding: ``init``, ``get_static_input``, ``signed``, ``__call__``,
+``kinetic_energy``; ``make_local_energy`` follows ``hamiltonian.py:49-83`` (all-electron, no
+pseudopotentials) and ``make_mcmc`` the all-electron branch of ``mcmc.py:278-346``.  Every numerical
+call goes to ``libfire.so`` through its C ABI (``include/fire.h``) on the current CUDA stream; torch
+only provides device memory and streams.
+
+Static shapes: the reference compiles for padded ``StaticArgs`` sizes and grows them on the host
+(``static_args.py:62-84``).  Here the sizes are capacities of the device buffers; the kernels report
+overflow in a status word instead of truncating silently, and the host grows the capacity from the
+observed maxima and re-runs the call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .params import ModelDims, init_params, pack_params, param_offsets
+from .systems import Molecule, spin_counts
+
+
+@dataclasses.dataclass(frozen=True)
+class StaticArgs:
+    """Neighbour-count static input (``StaticArgs``, ``model/new_sparse_model.py:46-80``)."""
+
+    n_pairs_same: int
+    n_pairs_diff: int
+    n_triplets: int
+    n_neighbours_en: int
+
+    @property
+    def n_pairs(self) -> int:
+        return self.n_pairs_same + self.n_pairs_diff
+
+    def round_with_padding(self, padding_factor: float, n_el: int, n_up: int, n_nuc: int) -> "StaticArgs":
+        """``round_with_padding`` (``static_args.py:9-14``) capped by ``StaticArgs.get_max``."""
+        n_dn = n_el - n_up
+        mx = (n_up * (n_up - 1) + n_dn * (n_dn - 1), 2 * n_up * n_dn, n_el * (n_el - 1) ** 2, n_nuc)
+
+        def rnd(x, m):
+            if x <= 0:
+                return 0
+            if padding_factor <= 1.0:
+                return min(x, m)
+            return int(min(padding_factor ** math.ceil(math.log(x) / math.log(padding_factor)), m))
+
+        vals = (self.n_pairs_same, self.n_pairs_diff, self.n_triplets, self.n_neighbours_en)
+        return StaticArgs(*(rnd(v, m) for v, m in zip(vals, mx)))
+
+
+class DeviceParams:
+    """Parameters resident on the device: the float32 blob and the prepared buffer."""
+
+    def __init__(self, wf: "FireWaveFunction", params: dict[str, np.ndarray]):
+        self.host = params
+        blob, offs = pack_params(wf.dims, params, np.float32)
+        self.offsets = offs
+        self.blob = torch.from_numpy(blob).to(wf.device)
+        lib = _lib.load()
+        prob = wf._problem(1, None)
+        nbytes = C.c_size_t()
+        _lib.check(lib.fire_prepared_size(C.byref(prob), C.byref(nbytes)), "fire_prepared_size")
+        self.prepared = torch.empty(int(nbytes.value), dtype=torch.uint8, device=wf.device)
+        offs_c = (C.c_int64 * len(offs))(*[int(o) for o in offs])
+        _lib.check(
+            lib.fire_prepare_params(wf._stream(), C.byref(prob), C.c_void_p(self.blob.data_ptr()), offs_c,
+                                    C.c_void_p(self.prepared.data_ptr()), C.c_size_t(self.prepared.numel())),
+            "fire_prepare_params",
+        )
+
+
+class FireWaveFunction:
+    """FiRE wavefunction (new_sparse embedding, isotropic envelopes, psiformer cusp + MLP/attention
+    Jastrow) evaluated by the sm_103a kernels of ``libfire.so``."""
+
+    def __init__(self, mol: Molecule, cutoff: float = 5.0, cutoff_1el: float = 20.0, precision: str = "fp32",
+                 device: str | torch.device = "cuda", chunk_walkers: int = 0):
+        if precision not in _lib.PREC:
+            raise ValueError(f"precision must be one of {list(_lib.PREC)}")
+        self.mol = mol
+        self.R = np.asarray(mol.R, np.float32)
+        self.Z = np.asarray(mol.Z)
+        self.n_electrons = mol.n_el
+        self.n_up, _ = spin_counts(mol)
+        self.n_nuclei = mol.n_nuc
+        self.cutoff = float(cutoff)
+        self.cutoff_1el = float(cutoff_1el)
+        self.precision = precision
+        self.device = torch.device(device)
+        self.chunk_walkers = int(chunk_walkers)
+        self.dims = ModelDims(self.n_electrons, self.n_up, self.n_nuclei, self.cutoff, self.cutoff_1el)
+        self.dtype = torch.float64 if precision == "fp64" else torch.float32
+        self.R_dev = torch.from_numpy(self.R).to(self.device)
+        self.Z_dev = torch.from_numpy(self.Z.astype(np.float32)).to(self.device)
+        self._ws: Optional[torch.Tensor] = None
+        self._status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=self.device)
+        _lib.load()
+
+    # ------------------------------------------------------------------ plumbing
+    @classmethod
+    def create(cls, mol: Molecule, **kw) -> "FireWaveFunction":
+        return cls(mol, **kw)
+
+    def _stream(self):
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _problem(self, n_walkers: int, static: Optional[StaticArgs]) -> _lib.Problem:
+        cap_p = static.n_pairs if static is not None else 1
+        cap_n = static.n_neighbours_en if static is not None else 1
+        return _lib.Problem(self.n_electrons, self.n_up, self.n_nuclei, int(n_walkers), self.cutoff,
+                            self.cutoff_1el, max(1, int(cap_p)), max(1, int(cap_n)), _lib.PREC[self.precision],
+                            self.chunk_walkers)
+
+    def _workspace(self, prob: _lib.Problem) -> torch.Tensor:
+        lib = _lib.load()
+        nbytes = C.c_size_t()
+        chunk = self.chunk_walkers if self.chunk_walkers > 0 else prob.n_walkers
+        _lib.check(lib.fire_workspace_size(C.byref(prob), chunk, C.byref(nbytes)), "fire_workspace_size")
+        need = int(nbytes.value)
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = None
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def _electrons(self, electrons) -> torch.Tensor:
+        r = torch.as_tensor(electrons)
+        if r.ndim == 2:
+            r = r[None]
+        return r.to(device=self.device, dtype=self.dtype).contiguous()
+
+    def _params(self, params) -> DeviceParams:
+        return params if isinstance(params, DeviceParams) else DeviceParams(self, params)
+
+    def _read_status(self) -> np.ndarray:
+        return self._status.cpu().numpy()
+
+    def _run(self, fn, static: StaticArgs, n_walkers: int, retries: int = 4):
+        """Runs fn(problem, workspace) with overflow-driven capacity growth; returns the static used."""
+        for _ in range(retries):
+            self._status.zero_()
+            prob = self._problem(n_walkers, static)
+            fn(prob, self._workspace(prob))
+            st = self._read_status()
+            flags = int(st[0])
+            if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
+                pairs = max(int(st[1]), static.n_pairs)
+                nucs = max(int(st[2]), static.n_neighbours_en)
+                half = (pairs + 1) // 2
+                static = StaticArgs(half, pairs - half, max(static.n_triplets, int(st[3])), nucs)
+                static = static.round_with_padding(1.1, self.n_electrons, self.n_up, self.n_nuclei)
+                continue
+            if flags & _lib.FLAG_NONFINITE:
+                pass  # NaNs propagate to the caller like the reference (train.py:263-264)
+            return static
+        raise RuntimeError("neighbour capacity did not converge")
+
+    # ------------------------------------------------------------------ reference interface
+    def init(self, seed: int, electrons) -> dict[str, np.ndarray]:
+        """Random-init parameters; the two normalize scales are 1/std of the embedding on the first
+        walker, as in ``NewSparseEmbedding.init`` (``new_sparse_model.py:354-380``)."""
+        params = init_params(self.dims, seed)
+        r = self._electrons(electrons)[:1]
+        static = self.get_static_input(r)
+        h_c, _ = self.embedding(params, r, static)
+        s0 = 1.0 / float(np.std(h_c.double().cpu().numpy()))
+        params["scales"] = np.array([s0 if np.isfinite(s0) else 1.0, 1.0])
+        _, h_u = self.embedding(params, r, static)
+        s1 = 1.0 / float(np.std(h_u.double().cpu().numpy()))
+        params["scales"][1] = s1 if np.isfinite(s1) else 1.0
+        return params
+
+    def get_static_input(self, electrons) -> StaticArgs:
+        """``get_static_input`` (``model/new_sparse_model.py:399-437``): counts maximised over walkers."""
+        r = self._electrons(electrons)
+        B = r.shape[0]
+        counts = torch.zeros((B, 4), dtype=torch.int32, device=self.device)
+        out = _lib.NeighborOut()
+        out.counts = counts.data_ptr()
+        prob = self._problem(B, StaticArgs(1, 0, 0, self.n_nuclei))
+        lib = _lib.load()
+        self._status.zero_()
+        _lib.check(lib.fire_neighbors(self._stream(), C.byref(prob), C.c_void_p(r.data_ptr()),
+                                      C.c_void_p(self.R_dev.data_ptr()), C.byref(out),
+                                      C.c_void_p(self._status.data_ptr())), "fire_neighbors")
+        c = counts.max(dim=0).values.cpu().numpy()
+        return StaticArgs(int(c[0]), int(c[1]), int(c[2]), int(c[3]))
+
+    def neighbor_lists(self, electrons, static: StaticArgs) -> dict[str, np.ndarray]:
+        """``get_pair_indices`` + ``get_neighbouring_nuclei`` in the reference's padded format."""
+        r = self._electrons(electrons)
+        B, n = r.shape[0], self.n_electrons
+        cs, cd = static.n_pairs_same, static.n_pairs_diff
+        dev = dict(dtype=torch.int32, device=self.device)
+        t = {k: torch.empty((B, cs), **dev) for k in ("ct_same", "nb_same", "jac_same")}
+        t.update({k: torch.empty((B, cd), **dev) for k in ("ct_diff", "nb_diff", "jac_diff")})
+        t.update({k: torch.empty((B, n + cs + cd), **dev) for k in ("jac_ctr", "jac_dep")})
+        t["en_idx"] = torch.empty((B, n, max(1, static.n_neighbours_en)), **dev)
+        t["counts"] = torch.empty((B, 4), **dev)
+        out = _lib.NeighborOut()
+        for k, v in t.items():
+            setattr(out, k, v.data_ptr())
+        out.cap_same, out.cap_diff = cs, cd
+        prob = self._problem(B, static)
+        self._status.zero_()
+        _lib.check(_lib.load().fire_neighbors(self._stream(), C.byref(prob), C.c_void_p(r.data_ptr()),
+                                              C.c_void_p(self.R_dev.data_ptr()), C.byref(out),
+                                              C.c_void_p(self._status.data_ptr())), "fire_neighbors")
+        res = {k: v.cpu().numpy() for k, v in t.items()}
+        res["status"] = self._read_status()
+        return res
+
+    def embedding(self, params, electrons, static: StaticArgs):
+        """Value-path embedding: (h after message passing, h after the update MLP before scales[1])."""
+        p = self._params(params)
+        r = self._electrons(electrons)
+        B = r.shape[0]
+        hc = torch.empty((B, self.n_electrons, 256), dtype=self.dtype, device=self.device)
+        hu = torch.empty_like(hc)
+
+        def fn(prob, ws):
+            _lib.check(_lib.load().fire_embedding(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(p.prepared.data_ptr()),
+                C.c_void_p(r.data_ptr()), C.c_void_p(hc.data_ptr()), C.c_void_p(hu.data_ptr()),
+                C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()), C.c_void_p(self._status.data_ptr())),
+                "fire_embedding")
+
+        self._run(fn, static, B)
+        return hc, hu
+
+    def signed(self, params, electrons, static: StaticArgs):
+        """(sign, log|psi|) per walker (``wave_function.py:183-190``)."""
+        p = self._params(params)
+        r = self._electrons(electrons)
+        B = r.shape[0]
+        sign = torch.empty(B, dtype=self.dtype, device=self.device)
+        logpsi = torch.empty(B, dtype=self.dtype, device=self.device)
+
+        def fn(prob, ws):
+            _lib.check(_lib.load().fire_logpsi(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(sign.data_ptr()),
+                C.c_void_p(logpsi.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_logpsi")
+
+        self._run(fn, static, B)
+        return sign, logpsi
+
+    def __call__(self, params, electrons, static: StaticArgs):
+        return self.signed(params, electrons, static)[1]
+
+    def local_energy_full(self, params, electrons, static: StaticArgs, debug: bool = False):
+        """E_loc per walker plus (log|psi|, sign, (mean, std) in FP64, debug dict, static used)."""
+        p = self._params(params)
+        r = self._electrons(electrons)
+        B = r.shape[0]
+        dev = dict(dtype=self.dtype, device=self.device)
+        eloc = torch.empty(B, **dev)
+        logpsi = torch.empty(B, **dev)
+        sign = torch.empty(B, **dev)
+        stats = torch.empty(2, dtype=torch.float64, device=self.device)
+        dbg = _lib.ElocDebug()
+        dbg_t = {}
+        if debug:
+            dbg_t = dict(kinetic=torch.empty(B, **dev), potential=torch.empty(B, **dev),
+                         logdet=torch.empty((B, 4), dtype=torch.float64, device=self.device),
+                         sign_det=torch.empty((B, 4), dtype=torch.float64, device=self.device),
+                         jastrow=torch.empty(B, **dev), grad=torch.empty((B, self.n_electrons, 3), **dev),
+                         lap=torch.empty(B, **dev))
+            for k, v in dbg_t.items():
+                setattr(dbg, k, v.data_ptr())
+
+        def fn(prob, ws):
+            _lib.check(_lib.load().fire_local_energy(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(logpsi.data_ptr()),
+                C.c_void_p(sign.data_ptr()), C.c_void_p(eloc.data_ptr()), C.c_void_p(stats.data_ptr()),
+                C.byref(dbg) if debug else None, C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_local_energy")
+
+        used = self._run(fn, static, B)
+        return eloc, dict(logpsi=logpsi, sign=sign, stats=stats, debug=dbg_t, static=used)
+
+    def kinetic_energy(self, params, electrons, static: StaticArgs):
+        """``kinetic_energy`` (``wave_function.py:215-221``) through the sparse forward Laplacian."""
+        _, aux = self.local_energy_full(params, electrons, static, debug=True)
+        return aux["debug"]["kinetic"]
+
+    def potential_energy(self, electrons):
+        r = self._electrons(electrons)
+        out = torch.empty(r.shape[0], dtype=self.dtype, device=self.device)
+        prob = self._problem(r.shape[0], None)
+        _lib.check(_lib.load().fire_potential_energy(self._stream(), C.byref(prob), C.c_void_p(r.data_ptr()),
+                                                     C.c_void_p(self.R_dev.data_ptr()),
+                                                     C.c_void_p(self.Z_dev.data_ptr()), C.c_void_p(out.data_ptr())),
+                   "fire_potential_energy")
+        return out
+
+    def mcmc_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs, steps: int,
+                   width: float, seed: int = 0, counter: int = 0, replay_noise=None, replay_log_u=None):
+        """In-place all-electron Metropolis block; returns (n_accept per walker, static_max)."""
+        p = self._params(params)
+        r = electrons
+        assert r.is_contiguous() and r.dtype == self.dtype
+        B = r.shape[0]
+        n_acc = torch.zeros(B, dtype=torch.int32, device=self.device)
+        smax = torch.zeros(4, dtype=torch.int32, device=self.device)
+        noise = None if replay_noise is None else self._electrons(replay_noise).reshape(steps, B, -1, 3).contiguous()
+        logu = None if replay_log_u is None else torch.as_tensor(replay_log_u).to(self.device, self.dtype).contiguous()
+        r0 = r.clone()
+        lp0 = logpsi.clone()
+
+        def fn(prob, ws):
+            r.copy_(r0)
+            logpsi.copy_(lp0)
+            n_acc.zero_()
+            smax.zero_()
+            _lib.check(_lib.load().fire_mcmc_block(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(logpsi.data_ptr()),
+                int(steps), float(width), C.c_uint64(seed), C.c_uint64(counter),
+                C.c_void_p(noise.data_ptr()) if noise is not None else None,
+                C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_mcmc_block")
+
+        self._run(fn, static, B)
+        sm = smax.cpu().numpy()
+        return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
+
+
+def make_local_energy(wf: FireWaveFunction):
+    """``make_local_energy`` (``hamiltonian.py:49-83``) for all-electron systems:
+    ``local_energy(key, params, electrons, static) -> (E_loc, new_static)``."""
+
+    def local_energy(key, params, electrons, static: StaticArgs):
+        eloc, aux = wf.local_energy_full(params, electrons, static)
+        return eloc, aux["static"]
+
+    return local_energy
+
+
+def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1):
+    """All-electron branch of ``make_mcmc`` (``mcmc.py:278-346``):
+    ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed."""
+
+    def mcmc_step(key, params, electrons, static: StaticArgs, width):
+        p = wf._params(params)
+        r = wf._electrons(electrons).clone()
+        _, logpsi = wf.signed(p, r, static)
+        n_acc, smax = wf.mcmc_block(p, r, logpsi, static, steps, float(width), seed=int(key))
+        stats = dict(pmove=float(n_acc.float().mean().item()) / max(steps, 1), static_max=smax, stepsize=width)
+        return r, stats
+
+    return mcmc_step, init_width

@@ -1,0 +1,169 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle on the same inputs.
+
+Tolerances: neighbour lists and triplets bit-exact; FP64 build <= 1e-10 relative; FP32 path
+<= 1e-5 relative per walker for log|psi| and E_loc (the orbital LU/inverse is FP64 in both)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import case, golden, rel
+from oracle import fire_oracle as O
+from sparse_wf_gb300 import _lib, systems
+from sparse_wf_gb300.wavefunction import FireWaveFunction, StaticArgs
+
+pytestmark = pytest.mark.gpu
+TOL = {"fp32": 1e-5, "fp64": 1e-10}
+
+
+def _wf(name, precision):
+    mol, nu, r, p, blob, offs = case(name)
+    wf = FireWaveFunction(mol, precision=precision)
+    return wf, mol, nu, r, p
+
+
+def _static(wf, r, pad=1.0):
+    s = wf.get_static_input(r)
+    return StaticArgs(s.n_pairs_same, s.n_pairs_diff, s.n_triplets, s.n_neighbours_en)
+
+
+@pytest.mark.parametrize("name", ["h10", "c2h6", "c10h22"])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_neighbor_lists_bit_exact(cuda_lib, name, precision):
+    g = golden(name)
+    wf, mol, nu, r, p = _wf(name, precision)
+    rr = r.astype(np.float64) if precision == "fp64" else r
+    static = StaticArgs(int(g["cap_same"]), int(g["cap_diff"]), 0, int(g["cap_nuc"]))
+    out = wf.neighbor_lists(rr, static)
+    assert out["status"][0] == 0
+    for k in ("ct_same", "nb_same", "jac_same", "ct_diff", "nb_diff", "jac_diff", "jac_ctr", "jac_dep", "en_idx"):
+        np.testing.assert_array_equal(out[k], g["nl_" + k], err_msg=k)
+    np.testing.assert_array_equal(out["counts"], g["counts"])
+
+
+def test_neighbor_lists_c40h82_exact(cuda_lib):
+    mol = systems.alkane(40)
+    nu, _ = systems.spin_counts(mol)
+    r = systems.init_electrons(mol, 6, 4242)
+    wf = FireWaveFunction(mol, precision="fp32")
+    counts = np.array([O.static_counts(w, mol.R, nu, 5.0, 20.0) for w in r])
+    static = StaticArgs(int(counts[:, 0].max()), int(counts[:, 1].max()) + 5, 0, int(counts[:, 3].max()))
+    out = wf.neighbor_lists(r, static)
+    np.testing.assert_array_equal(out["counts"], counts)
+    for k, w in enumerate(r):
+        (a, b, c), (d, e, f), (gg, h) = O.pair_indices(w, nu, 5.0, static.n_pairs_same, static.n_pairs_diff)
+        for key, v in zip(("ct_same", "nb_same", "jac_same", "ct_diff", "nb_diff", "jac_diff", "jac_ctr", "jac_dep"),
+                          (a, b, c, d, e, f, gg, h)):
+            np.testing.assert_array_equal(out[key][k], v, err_msg=key)
+        np.testing.assert_array_equal(out["en_idx"][k], O.neighbouring_nuclei(w, mol.R, 20.0, static.n_neighbours_en))
+
+
+def test_neighbor_overflow_is_reported(cuda_lib):
+    g = golden("c2h6")
+    wf, mol, nu, r, p = _wf("c2h6", "fp32")
+    out = wf.neighbor_lists(r, StaticArgs(3, 3, 0, 2))
+    assert out["status"][0] & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW)
+    assert out["status"][1] == (g["counts"][:, 0] + g["counts"][:, 1]).max()
+
+
+@pytest.mark.parametrize("name", ["h10", "c2h6"])
+def test_triplets_exact(cuda_lib, name):
+    g = golden(name)
+    wf, mol, nu, r, p = _wf(name, "fp32")
+    B, n = r.shape[0], mol.n_el
+    cap = g["triplets"].shape[2]
+    st = _static(wf, r)
+    prob = wf._problem(B, StaticArgs(st.n_pairs_same, st.n_pairs_diff + 4, 0, st.n_neighbours_en))
+    rt = torch.from_numpy(r).cuda()
+    outs = [torch.full((B, cap), -7, dtype=torch.int32, device="cuda") for _ in range(4)]
+    ws = torch.empty(64 << 20, dtype=torch.uint8, device="cuda")
+    status = torch.zeros(8, dtype=torch.int32, device="cuda")
+    rc = cuda_lib.fire_triplets(wf._stream(), C.byref(prob), C.c_void_p(rt.data_ptr()), cap,
+                                *[C.c_void_p(o.data_ptr()) for o in outs], C.c_void_p(ws.data_ptr()),
+                                C.c_size_t(ws.numel()), C.c_void_p(status.data_ptr()))
+    assert rc == 0
+    got = np.stack([o.cpu().numpy() for o in outs], axis=1)
+    np.testing.assert_array_equal(got, g["triplets"])
+    assert status[0].item() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_potential_energy(cuda_lib, precision):
+    wf, mol, nu, r, p = _wf("c10h22", precision)
+    rr = r.astype(np.float64) if precision == "fp64" else r
+    got = wf.potential_energy(rr).double().cpu().numpy()
+    ref = np.array([O.potential_energy(w.astype(np.float64), mol.R, mol.Z) for w in r])
+    assert rel(got, ref).max() < (1e-6 if precision == "fp32" else 1e-12)
+
+
+@pytest.mark.parametrize("name", ["h10", "c2h6", "c10h22"])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_embedding(cuda_lib, name, precision):
+    wf, mol, nu, r, p = _wf(name, precision)
+    rr = r.astype(np.float64) if precision == "fp64" else r
+    static = _static(wf, rr)
+    hc, hu = wf.embedding(p, rr, static)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    for k, w in enumerate(r.astype(np.float64)):
+        c_ref, u_ref = O.embedding_value(prob, p, w, return_pre_scale=True)
+        c, u = hc[k].double().cpu().numpy(), hu[k].double().cpu().numpy()
+        assert np.linalg.norm(c - c_ref) / np.linalg.norm(c_ref) < TOL[precision]
+        assert np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("name", ["h10", "h10_plain", "c2h6", "c10h22"])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_logpsi(cuda_lib, name, precision):
+    wf, mol, nu, r, p = _wf(name, precision)
+    rr = r.astype(np.float64) if precision == "fp64" else r
+    static = _static(wf, rr)
+    sign, logpsi = wf.signed(p, rr, static)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    ref = np.array([O.logpsi(prob, p, w) for w in r.astype(np.float64)])
+    np.testing.assert_array_equal(sign.cpu().numpy(), ref[:, 0])
+    err = np.abs(logpsi.double().cpu().numpy() - ref[:, 1]) / np.maximum(1.0, np.abs(ref[:, 1]))
+    assert err.max() < TOL[precision] * (10 if precision == "fp32" else 1)
+
+
+@pytest.mark.parametrize("name", ["h10", "h10_plain", "c2h6", "c10h22"])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_local_energy(cuda_lib, name, precision):
+    wf, mol, nu, r, p = _wf(name, precision)
+    rr = r.astype(np.float64) if precision == "fp64" else r
+    static = _static(wf, rr)
+    eloc, aux = wf.local_energy_full(p, rr, static, debug=True)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    fl = [O.logpsi_fl(prob, p, w) for w in r.astype(np.float64)]
+    ekin = np.array([-0.5 * (x[2] + x[1] @ x[1]) for x in fl])
+    epot = np.array([O.potential_energy(w, mol.R, mol.Z) for w in r.astype(np.float64)])
+    lp = np.array([x[0] for x in fl])
+    got = eloc.double().cpu().numpy()
+    dbg = {k: v.double().cpu().numpy() for k, v in aux["debug"].items()}
+    assert rel(dbg["potential"], epot).max() < TOL[precision]
+    assert np.abs(aux["logpsi"].double().cpu().numpy() - lp).max() < TOL[precision] * max(1, np.abs(lp).max()) * 10
+    grad_ref = np.array([x[1] for x in fl]).reshape(dbg["grad"].shape)
+    assert np.linalg.norm(dbg["grad"] - grad_ref) / np.linalg.norm(grad_ref) < TOL[precision] * 10
+    assert rel(dbg["kinetic"], ekin).max() < TOL[precision], (dbg["kinetic"], ekin)
+    assert rel(got, ekin + epot).max() < TOL[precision]
+    st = aux["stats"].cpu().numpy()
+    assert abs(st[0] - got.mean()) < 1e-9 * max(1, abs(got.mean()))
+
+
+@pytest.mark.parametrize("name", ["h10", "c2h6"])
+def test_mcmc_replay(cuda_lib, name):
+    g = golden(name)
+    wf, mol, nu, r, p = _wf(name, "fp64")
+    rr = torch.from_numpy(r.astype(np.float64)).cuda().contiguous()
+    static = _static(wf, rr)
+    dp = wf._params(p)
+    _, logpsi = wf.signed(dp, rr, static)
+    steps = g["mcmc_noise"].shape[0]
+    n_acc, smax = wf.mcmc_block(dp, rr, logpsi, static, steps, float(g["mcmc_width"]),
+                                replay_noise=g["mcmc_noise"].astype(np.float64),
+                                replay_log_u=g["mcmc_logu"].astype(np.float64))
+    sure = np.all(np.abs(g["mcmc_margin"]) > 1e-6, axis=1)
+    assert sure.any()
+    np.testing.assert_array_equal(n_acc.cpu().numpy()[sure], g["mcmc_nacc"][sure])
+    np.testing.assert_allclose(rr.cpu().numpy()[sure], g["mcmc_r"][sure], atol=1e-12)
+    assert smax[0] + smax[1] > 0

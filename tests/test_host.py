@@ -1,0 +1,141 @@
+"""Host-side logic: the C-ABI library (load + exported symbols + host-only size functions), the
+parameter layout shared by Python and C, static-capacity padding, synthetic systems and the
+multi-process walker sharding (gloo, world size 2)."""
+import ctypes as C
+import os
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from sparse_wf_gb300 import _lib, params as P, systems
+from sparse_wf_gb300.build import build
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build()
+    return _lib.load()
+
+
+def header_symbols():
+    hdr = (ROOT / "include" / "fire.h").read_text()
+    return re.findall(r"^\s*(?:fire_status|int32_t)\s+(fire_\w+)\s*\(", hdr, re.M)
+
+
+def test_library_exports_every_header_symbol(lib):
+    syms = header_symbols()
+    assert len(syms) == 12
+    assert sorted(syms) == sorted(_lib.SYMBOLS)
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert lib.fire_abi_version() == 1
+
+
+def test_header_slot_enum_matches_python():
+    hdr = (ROOT / "include" / "fire.h").read_text()
+    enum = re.search(r"enum fire_param_slot \{(.*?)\};", hdr, re.S).group(1)
+    names = [x.strip() for x in enum.replace("\n", " ").split(",") if x.strip()]
+    assert names[-1] == "FIRE_P_COUNT"
+    assert [x.replace("FIRE_P_", "").lower() for x in names[:-1]] == [x.lower() for x in P.PARAM_SLOT_NAMES]
+
+
+@pytest.mark.parametrize("mol", [systems.hydrogen_chain(10), systems.alkane(10), systems.alkane(40)])
+def test_param_layout_matches(lib, mol):
+    nu, _ = systems.spin_counts(mol)
+    d = P.ModelDims(mol.n_el, nu, mol.n_nuc)
+    prob = _lib.Problem(mol.n_el, nu, mol.n_nuc, 4, 5.0, 20.0, 100, 10, 0, 0)
+    offs = (C.c_int64 * (len(P.PARAM_SLOT_NAMES) + 1))()
+    assert lib.fire_param_layout(C.byref(prob), offs) == 0
+    np.testing.assert_array_equal(np.array(offs[:]), P.param_offsets(d))
+    p = P.init_params(d, 0)
+    blob, o = P.pack_params(d, p)
+    q = P.unpack_params(d, blob, o)
+    for k in p:
+        np.testing.assert_allclose(q[k], p[k].astype(np.float32), rtol=0, atol=0)
+
+
+def test_sizes_and_invalid_arguments(lib):
+    prob = _lib.Problem(82, 41, 32, 64, 5.0, 20.0, 2500, 40, 0, 0)
+    a, b, c = C.c_size_t(), C.c_size_t(), C.c_size_t()
+    assert lib.fire_workspace_size(C.byref(prob), 8, C.byref(a)) == 0
+    assert lib.fire_workspace_size(C.byref(prob), 16, C.byref(b)) == 0
+    assert b.value > a.value > 0
+    assert lib.fire_prepared_size(C.byref(prob), C.byref(c)) == 0
+    assert c.value >= 4 * P.param_offsets(P.ModelDims(82, 41, 32))[-1]
+    bad = _lib.Problem(82, 90, 32, 64, 5.0, 20.0, 2500, 40, 0, 0)  # n_up > n_el
+    assert lib.fire_workspace_size(C.byref(bad), 8, C.byref(a)) == 1
+    bad = _lib.Problem(82, 41, 32, 64, 5.0, 20.0, 2500, 40, 7, 0)  # unknown precision
+    assert lib.fire_prepared_size(C.byref(bad), C.byref(a)) == 1
+    prob_fp64 = _lib.Problem(82, 41, 32, 64, 5.0, 20.0, 2500, 40, 2, 0)
+    assert lib.fire_workspace_size(C.byref(prob_fp64), 8, C.byref(c)) == 0 and c.value > a.value
+
+
+def test_static_padding_mirrors_reference():
+    from sparse_wf_gb300.wavefunction import StaticArgs
+
+    s = StaticArgs(100, 120, 5000, 30).round_with_padding(1.1, 82, 41, 32)
+    assert s.n_pairs_same >= 100 and s.n_pairs_diff >= 120 and s.n_neighbours_en == 30  # int(1.1**36)
+    assert StaticArgs(7, 3, 9, 2).round_with_padding(1.0, 10, 5, 10) == StaticArgs(7, 3, 9, 2)
+    big = StaticArgs(10**6, 10**6, 10**9, 10**3).round_with_padding(1.2, 10, 5, 4)
+    assert big == StaticArgs(40, 50, 810, 4)
+
+
+def test_alkane_geometry():
+    for k in (1, 2, 5, 40):
+        m = systems.alkane(k)
+        assert m.n_el == 8 * k + 2 and m.n_nuc == 3 * k + 2
+        assert systems.spin_counts(m) == (4 * k + 1, 4 * k + 1)
+        d = np.linalg.norm(m.R[:, None] - m.R[None], axis=-1)
+        np.fill_diagonal(d, np.inf)
+        assert d.min() > 2.0
+        if k > 1:
+            assert np.isclose(d[:k, :k].min(), systems.C_C, atol=1e-5)
+        ind = systems.assign_spins_to_atoms(m.R, m.Z)
+        assert np.all(np.bincount(ind, minlength=m.n_nuc) == m.Z)
+    h = systems.hydrogen_chain(10, 1.8)
+    assert systems.spin_counts(h) == (5, 5)
+    r = systems.init_electrons(h, 3, 1000)
+    assert r.shape == (3, 10, 3) and r.dtype == np.float32
+
+
+def _gloo_worker(rank, world, port, q):
+    import torch
+    import torch.distributed as dist
+    from sparse_wf_gb300.distributed import energy_stats, shard
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    e = torch.from_numpy(np.random.default_rng(5).normal(-100.0, 3.0, 101))
+    a, b = shard(101, rank, world)
+    q.put((rank, a, b, energy_stats(e[a:b])))
+    dist.destroy_process_group()
+
+
+def test_walker_sharding_gloo():
+    import multiprocessing as mp
+    import socket
+
+    from sparse_wf_gb300.distributed import shard
+
+    assert [shard(10, r, 3) for r in range(3)] == [(0, 4), (4, 7), (7, 10)]
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+    e = np.random.default_rng(5).normal(-100.0, 3.0, 101)
+    res.sort()
+    assert res[0][1:3] == (0, 51) and res[1][1:3] == (51, 101)
+    for _, _, _, (mean, std) in res:
+        assert abs(mean - e.mean()) < 1e-12 and abs(std - e.std()) < 1e-12
