@@ -187,6 +187,14 @@ fire_status fire_mcmc_block(void* stream, const fire_problem* prob, const float*
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r,
                                   const float* R, const float* Z, void* out);
 
+/* ---- diagnostics (no counterpart in the reference) ----------------------------------------------- */
+/* Per-stage device timing: while enabled, every stage and every contraction (GEMM) launch of the calls
+ * above is bracketed by CUDA events on its stream.  fire_profile_enable(1) clears the records;
+ * fire_profile_report waits for the recorded events and writes one line per stage,
+ * "<stage> <launches> <total_ms>\n", into buf (host memory, NUL-terminated, truncated to len). */
+fire_status fire_profile_enable(int32_t on);
+fire_status fire_profile_report(char* buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

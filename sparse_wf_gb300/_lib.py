@@ -25,7 +25,7 @@ ERRORS = {1: "invalid argument", 2: "unsupported size", 3: "workspace too small"
 SYMBOLS = [
     "fire_abi_version", "fire_param_layout", "fire_prepared_size", "fire_workspace_size",
     "fire_prepare_params", "fire_neighbors", "fire_triplets", "fire_logpsi", "fire_local_energy",
-    "fire_embedding", "fire_mcmc_block", "fire_potential_energy",
+    "fire_embedding", "fire_mcmc_block", "fire_potential_energy", "fire_profile_enable", "fire_profile_report",
 ]
 
 
@@ -73,6 +73,8 @@ def load() -> C.CDLL:
         "fire_embedding": ([vp, P, vp, vp, vp, vp, vp, vp, sz, vp], i32),
         "fire_mcmc_block": ([vp, P, vp, vp, vp, vp, vp, i32, f32, u64, u64, vp, vp, vp, vp, vp, sz, vp], i32),
         "fire_potential_energy": ([vp, P, vp, vp, vp, vp], i32),
+        "fire_profile_enable": ([i32], i32),
+        "fire_profile_report": ([C.c_char_p, sz], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -85,3 +87,18 @@ def load() -> C.CDLL:
 def check(rc: int, what: str) -> None:
     if rc != FIRE_OK:
         raise RuntimeError(f"{what}: {ERRORS.get(rc, rc)}")
+
+
+def profile_enable(on: bool) -> None:
+    check(load().fire_profile_enable(1 if on else 0), "fire_profile_enable")
+
+
+def profile_report() -> dict[str, tuple[int, float]]:
+    """{stage: (launches, total_ms)} of the calls made while profiling was enabled (waits for them)."""
+    buf = C.create_string_buffer(1 << 16)
+    check(load().fire_profile_report(buf, len(buf)), "fire_profile_report")
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, k, ms = line.split()
+        out[name] = (int(k), float(ms))
+    return out

@@ -7,6 +7,8 @@
 //   -> FP64 Gauss-Jordan -> determinant Laplacian -> attention Jastrow -> MLP Jastrow -> assembly.
 // The value path (log|psi|, the MCMC building block) runs the same stages without tangents.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -16,6 +18,53 @@
 using namespace fire;
 
 namespace {
+
+// Converts the last launch error into a status; with FIRE_DEBUG set in the environment the CUDA error
+// string is printed to stderr.
+fire_status launch_status(const char* where) {
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return FIRE_OK;
+  if (std::getenv("FIRE_DEBUG")) std::fprintf(stderr, "[fire] %s: %s\n", where, cudaGetErrorString(e));
+  return FIRE_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------------------ stage profiling
+struct ProfRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+bool g_prof = false;
+long long g_nlaunch = 0;  // kernels launched by this library since the last fire_profile_enable
+std::vector<ProfRec> g_recs;
+std::vector<cudaEvent_t> g_pool;
+cudaEvent_t prof_event() {
+  if (!g_pool.empty()) {
+    cudaEvent_t e = g_pool.back();
+    g_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+struct Prof {
+  const char* name;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr;
+  Prof(const char* n, cudaStream_t st) : name(n), s(st) {
+    if (g_prof) {
+      a = prof_event();
+      cudaEventRecord(a, s);
+    }
+  }
+  ~Prof() {
+    if (g_prof && a) {
+      cudaEvent_t b = prof_event();
+      cudaEventRecord(b, s);
+      g_recs.push_back({name, a, b});
+    }
+  }
+};
 
 // ------------------------------------------------------------------------------ parameter layout
 void slot_sizes(const fire_problem* p, int64_t* sz) {
@@ -255,11 +304,13 @@ fire_status prepare_impl(cudaStream_t s, const fire_problem* p, const float* blo
   prep_offsets(p, off);
   T* out = reinterpret_cast<T*>(prepared);
   const long nb = (long)off[FIRE_P_COUNT];
+  g_nlaunch++;
   k_convert<T><<<nblk(nb), 256, 0, s>>>(blob, out, nb);
   const float* s0 = blob + boff[FIRE_P_SCALES];
   const float* s1 = blob + boff[FIRE_P_SCALES] + 1;
   const long n = p->n_el, N = p->n_nuc;
   auto scl = [&](int src, int dst, long cnt, const float* sc) {
+    g_nlaunch++;
     k_scale_copy<T><<<nblk(cnt), 256, 0, s>>>(blob + boff[src], out + off[dst], cnt, sc);
   };
   scl(FIRE_P_UPD1_W, PR_UPD1_W_S0, (long)F * F, s0);
@@ -267,24 +318,33 @@ fire_status prepare_impl(cudaStream_t s, const fire_problem* p, const float* blo
   scl(FIRE_P_ORB_DN_W, PR_ORB_DN_W_S1, (long)F * NDET * n, s1);
   scl(FIRE_P_JMLP1_W, PR_JMLP1_W_S1, (long)F * F, s1);
   scl(FIRE_P_ATT_V_W, PR_V_W_S1, (long)F * F, s1);
+  g_nlaunch++;
   k_qk<T><<<nblk(F * HEADS), 256, 0, s>>>(blob + boff[FIRE_P_ATT_Q_W], blob + boff[FIRE_P_ATT_Q_B],
                                           blob + boff[FIRE_P_ATT_KEYS], s1, out + off[PR_QK_W_S1],
                                           out + off[PR_QK_B]);
+  g_nlaunch++;
   k_softplus<T><<<nblk(N * NENV_EN), 256, 0, s>>>(blob + boff[FIRE_P_EN_SCALES], out + off[PR_EN_INVSCALE],
                                                   N * NENV_EN, 1);
+  g_nlaunch++;
   k_softplus<T><<<1, 256, 0, s>>>(blob + boff[FIRE_P_EESAME_SCALE], out + off[PR_EESAME_INVSCALE], NENV_EE, 1);
+  g_nlaunch++;
   k_softplus<T><<<1, 256, 0, s>>>(blob + boff[FIRE_P_EEDIFF_SCALE], out + off[PR_EEDIFF_INVSCALE], NENV_EE, 1);
+  g_nlaunch++;
   k_softplus<T><<<nblk(N * NDET * NENV_ORB), 256, 0, s>>>(blob + boff[FIRE_P_ENV_UP_SIGMA], out + off[PR_ENV_UP_SP],
                                                           N * NDET * NENV_ORB, 0);
+  g_nlaunch++;
   k_softplus<T><<<nblk(N * NDET * NENV_ORB), 256, 0, s>>>(blob + boff[FIRE_P_ENV_DN_SIGMA], out + off[PR_ENV_DN_SP],
                                                           N * NDET * NENV_ORB, 0);
+  g_nlaunch++;
   k_pi_perdet<T><<<nblk((long)NDET * N * NENV_ORB * n), 256, 0, s>>>(blob + boff[FIRE_P_ENV_UP_PI],
                                                                       out + off[PR_ENV_UP_PI], (int)N, (int)n);
+  g_nlaunch++;
   k_pi_perdet<T><<<nblk((long)NDET * N * NENV_ORB * n), 256, 0, s>>>(blob + boff[FIRE_P_ENV_DN_PI],
                                                                       out + off[PR_ENV_DN_PI], (int)N, (int)n);
+  g_nlaunch++;
   k_scalars<T><<<1, 32, 0, s>>>(blob + boff[FIRE_P_CUTOFF_PARAM], blob + boff[FIRE_P_LOG_BIAS], p->cutoff,
                                 out + off[PR_SCALARS]);
-  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+  return launch_status(__func__);
 }
 
 template <typename T>
@@ -360,24 +420,30 @@ GemmP<T> gp0() {
 
 template <typename T, int MODE>
 cudaError_t gemm(const Ctx<T>& c, GemmP<T> g) {
+  Prof pr("gemm", c.s);
+  g_nlaunch++;
   return launch_gemm<T, MODE>(g, c.s);
 }
 
 // neighbour lists (+ layout for the forward-Laplacian path)
 template <typename T>
 cudaError_t stage_neighbors(Ctx<T>& c, bool fl) {
+  Prof pr("neighbors", c.s);
   const int n = c.p->n_el;
   const size_t smem = 3 * n * sizeof(T) + (5 * n + 2) * sizeof(int);
   fire_neighbor_out ext;
   std::memset(&ext, 0, sizeof(ext));
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_neighbors<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  g_nlaunch++;
   k_neighbors<T><<<c.Wc, 512, smem, c.s>>>(c.r, c.R, (T)c.p->cutoff, (T)c.p->cutoff_1el, c.nb, ext, c.status);
   if (fl) {
+    g_nlaunch++;
     k_pos_scan<<<1, 1024, 0, c.s>>>(c.nb, c.L.pos_off);
+    g_nlaunch++;
     k_layout<<<c.Wc, 256, 0, c.s>>>(c.nb, c.L);
   }
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 // ElecInit + GLU/Dense/Dense on the electron carriers, then edges + messages -> H
@@ -388,27 +454,35 @@ cudaError_t stage_embedding(Ctx<T>& c) {
   T* E5a = c.template buf<T>(c.P.E5a);
   T* Z1 = c.template buf<T>(c.P.Z1);
   T* E5o = c.template buf<T>(c.P.E5o);
-  k_elec_init<T, NT><<<G, 256, 0, c.s>>>(c.r, c.R, c.nb, c.W, (T)(1.0 / c.p->cutoff_1el), E5a);
+  {
+    Prof pr("elec_init", c.s);
+    g_nlaunch++;
+    k_elec_init<T, NT><<<G, 256, 0, c.s>>>(c.r, c.R, c.nb, c.W, (T)(1.0 / c.p->cutoff_1el), E5a);
+  }
+  Prof pr_e5("elec_mlp", c.s);
   GemmP<T> g = gp0<T>();
   g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_GLU_W]; g.ldb = 2 * F; g.C = Z1; g.ldc = 2 * F;
   g.M = G * NV; g.N = 2 * F; g.K = F;
   gemm<T, EPI_PLAIN>(c, g);
+  g_nlaunch++;
   k_glu<T, NT><<<nblk((long)G * F), 256, 0, c.s>>>(Z1, E5a, G);
   g = gp0<T>();
   g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_DENSE_W]; g.ldb = F; g.C = Z1; g.ldc = F;
   g.bias = c.W.w[FIRE_P_EI_DENSE_B]; g.bias_period = NV;
   g.M = G * NV; g.N = F; g.K = F;
   gemm<T, EPI_PLAIN>(c, g);
+  g_nlaunch++;
   k_silu5<T, NT><<<nblk((long)G * F), 256, 0, c.s>>>(Z1, G);
   g = gp0<T>();
   g.A = Z1; g.lda = F; g.B = c.W.w[FIRE_P_EI_OUT_W]; g.ldb = 5 * F; g.C = E5o; g.ldc = 5 * F;
   g.bias = c.W.w[FIRE_P_EI_OUT_B]; g.bias_period = NV;
   g.M = G * NV; g.N = 5 * F; g.K = F;
   gemm<T, EPI_PLAIN>(c, g);
+  Prof pr("edge_contract", c.s);
   k_edge_contract<T, NT><<<G, 256, 0, c.s>>>(c.r, c.nb, c.L, c.W, E5o, c.template buf<T>(c.P.HX),
                                              NT ? c.template buf<T>(c.P.HL) : nullptr,
                                              NT ? c.template buf<T>(c.P.HJ) : nullptr);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 struct Planes {
@@ -424,7 +498,7 @@ cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, c
   g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.C = c.template buf<T>(out.X);
   g.ldc = N; g.M = rowsX; g.N = N; g.K = K; g.aux0 = c.template buf<T>(zx); g.ld_aux = N;
   gemm<T, EPI_SILU_X>(c, g);
-  if (!fl) return cudaGetLastError();
+  if (!fl) return cudaPeekAtLastError();
   cudaMemsetAsync(c.template buf<T>(jsq), 0, sizeof(T) * (size_t)rowsX * N, c.s);
   g = gp0<T>();
   g.A = c.template buf<T>(in.J); g.lda = K; g.B = Wt; g.ldb = N; g.C = c.template buf<T>(out.J); g.ldc = N;
@@ -435,7 +509,7 @@ cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, c
   g.A = c.template buf<T>(in.L); g.lda = K; g.B = Wt; g.ldb = N; g.C = c.template buf<T>(out.L); g.ldc = N;
   g.M = rowsX; g.N = N; g.K = K; g.aux1 = c.template buf<T>(zx); g.aux3 = c.template buf<T>(jsq); g.ld_aux = N;
   gemm<T, EPI_SILU_L>(c, g);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 // Linear(F -> N) without activation on a node (bias on X only)
@@ -446,13 +520,13 @@ cudaError_t linear_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt,
   g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.bias_period = 1;
   g.C = c.template buf<T>(out.X); g.ldc = N; g.M = rowsX; g.N = N; g.K = K;
   gemm<T, EPI_PLAIN>(c, g);
-  if (!fl) return cudaGetLastError();
+  if (!fl) return cudaPeekAtLastError();
   g.A = c.template buf<T>(in.J); g.bias = nullptr; g.C = c.template buf<T>(out.J); g.M = rowsJcap;
   g.M_dev = rowsJdev; g.M_scale = rowsJdev ? 3 : 1;
   gemm<T, EPI_PLAIN>(c, g);
   g.A = c.template buf<T>(in.L); g.C = c.template buf<T>(out.L); g.M = rowsX; g.M_dev = nullptr; g.M_scale = 1;
   gemm<T, EPI_PLAIN>(c, g);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 // envelopes + orbital matrices (+ their Jacobian/Laplacian planes)
@@ -462,11 +536,13 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   const bool fl = NT > 0;
   const int n = c.p->n_el, nu = c.p->n_up, N = c.p->n_nuc, G = c.Wc * n, DN = NDET * n;
   T* env = c.template buf<T>(c.P.env);
+  Prof pr("orbitals", c.s);
   for (int s = 0; s < 2; ++s) {
     const int ns = s == 0 ? nu : n - nu;
     if (ns == 0) continue;
     T* coef = c.template buf<T>(s == 0 ? c.P.coef_up : c.P.coef_dn);
     const long tot = (long)c.Wc * ns * N * NENV_ORB;
+    g_nlaunch++;
     k_env_coef<T, NV><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, c.W.w[s == 0 ? PR_ENV_UP_SP : PR_ENV_DN_SP], n, ns,
                                                   s == 0 ? 0 : nu, N, c.Wc, coef);
     const long rows = (long)c.Wc * ns * NV, K8 = (long)N * NENV_ORB;
@@ -485,7 +561,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   g.C = c.template buf<T>(c.P.Apl); g.ldc = DN; g.M = G; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
   g.aux0 = c.template buf<T>(c.P.rawx); g.aux1 = env; g.ld_aux = DN; g.env_nv = NV;
   gemm<T, EPI_ORB_X>(c, g);
-  if (!fl) return cudaGetLastError();
+  if (!fl) return cudaPeekAtLastError();
   g = gp0<T>();
   g.A = c.template buf<T>(c.P.B2J); g.lda = F; g.B = c.W.w[PR_ORB_UP_W_S1]; g.B2 = c.W.w[PR_ORB_DN_W_S1];
   g.ldb = DN; g.C = c.template buf<T>(c.P.Jorb); g.ldc = DN; g.M = 3 * c.L.cap_pos;
@@ -499,7 +575,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   g.aux1 = env; g.aux2 = c.template buf<T>(c.P.rjs); g.aux3 = c.template buf<T>(c.P.rawx); g.ld_aux = DN;
   g.env_nv = 5;
   gemm<T, EPI_ORB_L>(c, g);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 int gj_cluster(int n, size_t es, size_t* smem_out) {
@@ -542,6 +618,7 @@ cudaError_t launch_gj(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  g_nlaunch++;
   return cudaLaunchKernelEx(&cfg, kern, A, n, CL, c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
                             Ainv, c.status);
 }
@@ -554,7 +631,9 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
   const int Jcap = 3 * c.L.cap_pos;
   const int* Jdev = FLM ? c.L.pos_off + c.Wc : nullptr;
   const Planes B2{c.P.B2X, c.P.B2J, c.P.B2L}, B1{c.P.B1X, c.P.B1J, c.P.B1L}, H{c.P.HX, c.P.HJ, c.P.HL};
+  Prof pr("jastrow", c.s);
   // attention logits exp(-(h W_Qk + b_Qk) / 4)
+  g_nlaunch++;
   k_narrow<T, HEADS, 1, FLM><<<G, 256, 0, c.s>>>(
       c.template buf<T>(B2.X), FLM ? c.template buf<T>(B2.J) : nullptr, FLM ? c.template buf<T>(B2.L) : nullptr,
       c.nb, c.L, c.W.w[PR_QK_W_S1], c.W.w[PR_QK_B], nullptr, nullptr, c.template buf<T>(c.P.aX),
@@ -562,6 +641,7 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
   linear_layer<T>(c, FLM, B2, B1, c.W.w[PR_V_W_S1], c.W.w[FIRE_P_ATT_V_B], F, F, G, Jcap, Jdev);
   cudaMemsetAsync(c.template buf<T>(c.P.Ax), 0, sizeof(T) * Wc * 2 * 272, c.s);
   if (FLM) cudaMemsetAsync(c.template buf<T>(c.P.Al), 0, sizeof(T) * Wc * 2 * 272, c.s);
+  g_nlaunch++;
   k_att_sums<T, FLM><<<dim3(n, Wc), 256, 0, c.s>>>(
       c.nb, c.L, c.template buf<T>(c.P.aX), FLM ? c.template buf<T>(c.P.aJ) : nullptr,
       FLM ? c.template buf<T>(c.P.aL) : nullptr, c.template buf<T>(B1.X), FLM ? c.template buf<T>(B1.J) : nullptr,
@@ -611,6 +691,7 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
                 c.P.Zx, c.P.jsq);
   silu_layer<T>(c, FLM, B1, H, c.W.w[FIRE_P_JMLP2_W], c.W.w[FIRE_P_JMLP2_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3,
                 c.P.Zx, c.P.jsq);
+  g_nlaunch++;
   k_narrow<T, 2, 0, FLM><<<G, 256, 0, c.s>>>(
       c.template buf<T>(H.X), FLM ? c.template buf<T>(H.J) : nullptr, FLM ? c.template buf<T>(H.L) : nullptr, c.nb,
       c.L, c.W.w[FIRE_P_JMLP3_W], c.W.w[FIRE_P_JMLP3_B], c.W.w[FIRE_P_MLP_SCALE], c.W.w[PR_SCALARS] + 1,
@@ -621,7 +702,7 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
                                          FLM ? c.template buf<T>(c.P.Lo2) : nullptr, c.template buf<T>(c.P.JMx),
                                          FLM ? c.template buf<T>(c.P.JMl) : nullptr,
                                          FLM ? c.template buf<T>(c.P.JMj) : nullptr);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 // update MLP: H -> B1 -> B2 (scales[0] folded into the first weight, scales[1] into the consumers)
@@ -632,11 +713,12 @@ cudaError_t stage_update(Ctx<T>& c) {
   const int Jcap = 3 * c.L.cap_pos;
   const int* Jdev = FLM ? c.L.pos_off + c.Wc : nullptr;
   const Planes H{c.P.HX, c.P.HJ, c.P.HL}, B1{c.P.B1X, c.P.B1J, c.P.B1L}, B2{c.P.B2X, c.P.B2J, c.P.B2L};
+  Prof pr("update_mlp", c.s);
   silu_layer<T>(c, FLM, H, B1, c.W.w[PR_UPD1_W_S0], c.W.w[FIRE_P_UPD1_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3, c.P.Zx,
                 c.P.jsq);
   silu_layer<T>(c, FLM, B1, B2, c.W.w[FIRE_P_UPD2_W], c.W.w[FIRE_P_UPD2_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3, c.P.Zx,
                 c.P.jsq);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 // value path for one chunk: writes logpsi/sign via the assembly (indices w0 + w)
@@ -648,6 +730,7 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   stage_update<T, 0>(c);
   stage_orbitals<T, 0>(c);
   // slogdet only: FP32 LU for the FP32/mixed value path, FP64 in the FP64 build
+  Prof pr_lu("lu", c.s);
   if constexpr (sizeof(T) == 8)
     launch_gj<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
   else
@@ -657,11 +740,12 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   std::memset(&o, 0, sizeof(o));
   o.logpsi = logpsi;
   o.sign = sign;
+  g_nlaunch++;
   k_assemble<T, false><<<c.Wc, 256, 3 * c.p->n_el * sizeof(double), c.s>>>(
       c.p->n_el, c.p->n_up, c.p->n_nuc, w0_out, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
       c.template buf<double>(c.P.sd), nullptr, nullptr, c.template buf<T>(c.P.JAx), nullptr, nullptr,
       c.template buf<T>(c.P.JMx), nullptr, nullptr, o, c.status);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 template <typename T>
@@ -671,12 +755,17 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   stage_embedding<T, 3>(c);
   stage_update<T, 3>(c);
   stage_orbitals<T, 3>(c);
-  launch_gj<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+  {
+    Prof pr("gauss_jordan", c.s);
+    launch_gj<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+  }
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {
     const size_t es = sizeof(T);
     const size_t smem = es * (3 * DL_CMAX_DECL * (DL_CMAX_DECL + 1) + 3 * DL_CMAX_DECL * 33 + 32 * (DL_CMAX_DECL + 1));
     cudaFuncSetAttribute(k_detlap<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    Prof pr("detlap", c.s);
+    g_nlaunch++;
     k_detlap<T><<<dim3(c.p->n_el, NDET, c.Wc), 256, smem, c.s>>>(
         c.nb, c.L, c.template buf<T>(c.P.Jorb), c.template buf<T>(c.P.Ainv), c.template buf<T>(c.P.lapA),
         c.template buf<T>(c.P.dgrad), c.template buf<double>(c.P.dlap), c.status);
@@ -688,12 +777,14 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   o.sign = sign;
   o.eloc = eloc;
   if (dbg) o.dbg = *dbg;
+  Prof pr("assemble", c.s);
+  g_nlaunch++;
   k_assemble<T, true><<<c.Wc, 256, 3 * c.p->n_el * sizeof(double), c.s>>>(
       c.p->n_el, c.p->n_up, c.p->n_nuc, c.w0, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
       c.template buf<double>(c.P.sd), c.template buf<T>(c.P.dgrad), c.template buf<double>(c.P.dlap),
       c.template buf<T>(c.P.JAx), c.template buf<T>(c.P.JAj), c.template buf<T>(c.P.JAl), c.template buf<T>(c.P.JMx),
       c.template buf<T>(c.P.JMj), c.template buf<T>(c.P.JMl), o, c.status);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 template <typename T>
@@ -725,10 +816,11 @@ fire_status run_eloc(const fire_problem* p, cudaStream_t s, const float* R, cons
     c.w0 = w0;
     c.Wc = std::min(Wc, p->n_walkers - w0);
     c.r = rr + (size_t)w0 * p->n_el * 3;
-    if (chunk_eloc<T>(c, logpsi, sign, eloc, dbg) != cudaSuccess) return FIRE_ERR_CUDA;
+    if (chunk_eloc<T>(c, logpsi, sign, eloc, dbg) != cudaSuccess) return launch_status("local_energy chunk");
   }
+  g_nlaunch++;
   if (stats) k_stats<T><<<1, 1024, 0, s>>>(reinterpret_cast<const T*>(eloc), p->n_walkers, stats);
-  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+  return launch_status(__func__);
 }
 
 template <typename T>
@@ -742,7 +834,7 @@ fire_status run_logpsi(const fire_problem* p, cudaStream_t s, const float* R, co
     c.w0 = w0;
     c.Wc = std::min(Wc, p->n_walkers - w0);
     c.r = rr + (size_t)w0 * p->n_el * 3;
-    if (chunk_logpsi<T>(c, logpsi, sign, w0) != cudaSuccess) return FIRE_ERR_CUDA;
+    if (chunk_logpsi<T>(c, logpsi, sign, w0) != cudaSuccess) return launch_status("logpsi chunk");
   }
   return FIRE_OK;
 }
@@ -769,7 +861,7 @@ fire_status run_embedding(const fire_problem* p, cudaStream_t s, const float* R,
     if (hu)
       cudaMemcpyAsync(reinterpret_cast<T*>(hu) + (size_t)w0 * p->n_el * F, c.template buf<T>(c.P.B2X),
                       cnt * sizeof(T), cudaMemcpyDeviceToDevice, s);
-    if (cudaGetLastError() != cudaSuccess) return FIRE_ERR_CUDA;
+    if (launch_status("embedding chunk") != FIRE_OK) return FIRE_ERR_CUDA;
   }
   return FIRE_OK;
 }
@@ -790,16 +882,18 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
     T* rn = c.template buf<T>(c.P.rn);
     T* lpn = c.template buf<T>(c.P.lpn);
     for (int st = 0; st < steps; ++st) {
+      g_nlaunch++;
       k_propose<T><<<nblk((long)c.Wc * n), 256, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, c.Wc, w0, p->n_walkers, st,
                                                         (T)width, seed, counter,
                                                         reinterpret_cast<const T*>(noise));
       c.r = rn;
-      if (chunk_logpsi<T>(c, lpn, nullptr, 0) != cudaSuccess) return FIRE_ERR_CUDA;
+      if (chunk_logpsi<T>(c, lpn, nullptr, 0) != cudaSuccess) return launch_status("mcmc chunk");
+      g_nlaunch++;
       k_accept<T><<<c.Wc, 128, 0, s>>>(rr, rn, reinterpret_cast<T*>(logpsi), lpn, n, w0, p->n_walkers, st, seed,
                                       counter, reinterpret_cast<const T*>(logu), n_accept, c.nb.counts, static_max);
     }
   }
-  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+  return launch_status(__func__);
 }
 
 }  // namespace
@@ -861,16 +955,18 @@ fire_status fire_neighbors(void* stream, const fire_problem* prob, const void* r
   if (prob->precision == FIRE_PREC_FP64) {
     const size_t smem = 3 * n * sizeof(double) + (5 * n + 2) * sizeof(int);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    g_nlaunch++;
     k_neighbors<double><<<prob->n_walkers, 512, smem, s>>>(reinterpret_cast<const double*>(r), R,
                                                           (double)prob->cutoff, (double)prob->cutoff_1el, nb, *out,
                                                           status);
   } else {
     const size_t smem = 3 * n * sizeof(float) + (5 * n + 2) * sizeof(int);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    g_nlaunch++;
     k_neighbors<float><<<prob->n_walkers, 512, smem, s>>>(reinterpret_cast<const float*>(r), R, prob->cutoff,
                                                          prob->cutoff_1el, nb, *out, status);
   }
-  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+  return launch_status(__func__);
 }
 
 fire_status fire_triplets(void* stream, const fire_problem* prob, const void* r, int32_t cap_triplets,
@@ -901,16 +997,19 @@ fire_status fire_triplets(void* stream, const fire_problem* prob, const void* r,
   if (prob->precision == FIRE_PREC_FP64) {
     const size_t smem = 3 * n * sizeof(double) + (5 * n + 2) * sizeof(int);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    g_nlaunch++;
     k_neighbors<double><<<B, 512, smem, s>>>(reinterpret_cast<const double*>(r), nullptr, (double)prob->cutoff,
                                             (double)prob->cutoff_1el, nb2, ext, status);
   } else {
     const size_t smem = 3 * n * sizeof(float) + (5 * n + 2) * sizeof(int);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    g_nlaunch++;
     k_neighbors<float><<<B, 512, smem, s>>>(reinterpret_cast<const float*>(r), nullptr, prob->cutoff,
                                            prob->cutoff_1el, nb2, ext, status);
   }
+  g_nlaunch++;
   k_triplets<<<B, 256, 0, s>>>(nb, cap_triplets, trip_in, trip_k, trip_kn, trip_i, status);
-  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+  return launch_status(__func__);
 }
 
 fire_status fire_logpsi(void* stream, const fire_problem* prob, const float* R, const float* Z, const void* prepared,
@@ -964,13 +1063,55 @@ fire_status fire_potential_energy(void* stream, const fire_problem* prob, const 
                                   const float* Z, void* out) {
   if (!valid(prob) || !r || !R || !Z || !out) return FIRE_ERR_INVALID;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  g_nlaunch++;
   if (prob->precision == FIRE_PREC_FP64)
     k_potential<double><<<prob->n_walkers, 256, 0, s>>>(prob->n_el, prob->n_nuc, reinterpret_cast<const double*>(r),
                                                         R, Z, reinterpret_cast<double*>(out));
   else
     k_potential<float><<<prob->n_walkers, 256, 0, s>>>(prob->n_el, prob->n_nuc, reinterpret_cast<const float*>(r), R,
                                                        Z, reinterpret_cast<float*>(out));
-  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+  return launch_status(__func__);
+}
+
+fire_status fire_profile_enable(int32_t on) {
+  for (auto& r : g_recs) {
+    g_pool.push_back(r.a);
+    g_pool.push_back(r.b);
+  }
+  g_recs.clear();
+  g_prof = on != 0;
+  g_nlaunch = 0;
+  return FIRE_OK;
+}
+
+fire_status fire_profile_report(char* buf, size_t len) {
+  if (!buf || len == 0) return FIRE_ERR_INVALID;
+  std::vector<std::pair<const char*, std::pair<int, double>>> acc;
+  for (auto& r : g_recs) {
+    if (cudaEventSynchronize(r.b) != cudaSuccess) return launch_status("profile");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    bool found = false;
+    for (auto& a : acc)
+      if (std::strcmp(a.first, r.name) == 0) {
+        a.second.first += 1;
+        a.second.second += ms;
+        found = true;
+      }
+    if (!found) acc.push_back({r.name, {1, (double)ms}});
+  }
+  size_t o = 0;
+  buf[0] = 0;
+  {
+    const int w = std::snprintf(buf, len, "kernels_launched %lld 0\n", g_nlaunch);
+    if (w > 0 && (size_t)w < len) o = (size_t)w;
+  }
+  for (auto& a : acc) {
+    const int w = std::snprintf(buf + o, len - o, "%s %d %.6f\n", a.first, a.second.first, a.second.second);
+    if (w < 0 || (size_t)w >= len - o) break;
+    o += (size_t)w;
+  }
+  return FIRE_OK;
 }
 
 }  // extern "C"

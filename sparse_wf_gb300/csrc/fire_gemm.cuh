@@ -260,7 +260,7 @@ inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
   }
   if (grid.y == 0 || grid.x == 0) return cudaSuccess;
   k_gemm<T, MODE><<<grid, GTHREADS, dyn, s>>>(p);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 }  // namespace fire

@@ -33,4 +33,12 @@ struct Layout {
   int cap_pos;   // capacity = W * (n + cap_p)
 };
 
+// Output pointers of the per-walker assembly (k_assemble).
+struct AssembleOut {
+  void* logpsi;
+  void* sign;
+  void* eloc;
+  fire_eloc_debug dbg;
+};
+
 }  // namespace fire

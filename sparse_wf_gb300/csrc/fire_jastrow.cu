@@ -14,7 +14,7 @@
 //                log|J1| + J0 (_mlp_to_logpsi, jastrow.py:372-382), the e-e cusp (ElElCusp 48-64,
 //                analytic), the kinetic energy -1/2 (lap + |grad|^2) (wave_function.py:215-221) and the
 //                Coulomb potential (hamiltonian.py:15-26).
-#include "fire_kernels.cuh"
+#include "fire_internal.cuh"
 
 namespace fire {
 

@@ -1,5 +1,7 @@
 // fire_kernels.cuh -- declarations of the kernels defined (and explicitly instantiated) in the
-// stage translation units, so that fire_api.cu can launch them.
+// stage translation units, so that fire_api.cu can launch them.  Only fire_api.cu includes this
+// header: a translation unit that sees these declarations before its own template definitions gets
+// launch stubs without device code ("invalid device function").
 #pragma once
 #include "fire_internal.cuh"
 
@@ -37,12 +39,6 @@ __global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* 
 constexpr int DL_CMAX_DECL = 64;
 
 // fire_jastrow.cu
-struct AssembleOut {
-  void* logpsi;
-  void* sign;
-  void* eloc;
-  fire_eloc_debug dbg;
-};
 template <typename T, int NC, int ACT, bool FLM>
 __global__ void k_narrow(const T* X, const T* Jp, const T* Lp, Nbr nb, Layout L, const T* Wn, const T* bn,
                          const T* post_scale, const T* post_shift, T* Xo, T* Jo, T* Lo, int32_t* status);

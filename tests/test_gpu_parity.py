@@ -1,7 +1,10 @@
 """Parity of the CUDA path (through the C ABI) with the oracle on the same inputs.
 
-Tolerances: neighbour lists and triplets bit-exact; FP64 build <= 1e-10 relative; FP32 path
-<= 1e-5 relative per walker for log|psi| and E_loc (the orbital LU/inverse is FP64 in both)."""
+Tolerances: neighbour lists and triplets bit-exact; FP64 build <= 1e-10 relative on log|psi|, its
+gradient, its Laplacian and E_loc; FP32 path <= 1e-5 relative per walker on the forward Laplacian
+(log|psi|, |grad log psi|, lap log psi).  In FP32, E_loc = -(lap + |grad|^2)/2 + V cancels two terms
+that are up to ~1e4 times larger than the kinetic energy near nodes of psi (an all-FP32 evaluation of
+the oracle shows the same), so FP32 E_loc is checked against that scale: |dE| <= 1e-5 (|lap| + |grad|^2)/2."""
 import ctypes as C
 
 import numpy as np
@@ -140,12 +143,20 @@ def test_local_energy(cuda_lib, name, precision):
     lp = np.array([x[0] for x in fl])
     got = eloc.double().cpu().numpy()
     dbg = {k: v.double().cpu().numpy() for k, v in aux["debug"].items()}
-    assert rel(dbg["potential"], epot).max() < TOL[precision]
-    assert np.abs(aux["logpsi"].double().cpu().numpy() - lp).max() < TOL[precision] * max(1, np.abs(lp).max()) * 10
+    tol = TOL[precision]
+    assert rel(dbg["potential"], epot).max() < tol
+    assert (np.abs(aux["logpsi"].double().cpu().numpy() - lp) / np.maximum(1, np.abs(lp))).max() < tol
     grad_ref = np.array([x[1] for x in fl]).reshape(dbg["grad"].shape)
-    assert np.linalg.norm(dbg["grad"] - grad_ref) / np.linalg.norm(grad_ref) < TOL[precision] * 10
-    assert rel(dbg["kinetic"], ekin).max() < TOL[precision], (dbg["kinetic"], ekin)
-    assert rel(got, ekin + epot).max() < TOL[precision]
+    lap_ref = np.array([x[2] for x in fl])
+    for k in range(len(r)):
+        assert np.linalg.norm(dbg["grad"][k] - grad_ref[k]) / np.linalg.norm(grad_ref[k]) < tol
+    assert rel(dbg["lap"], lap_ref).max() < tol, (dbg["lap"], lap_ref)
+    if precision == "fp64":
+        assert rel(dbg["kinetic"], ekin).max() < tol, (dbg["kinetic"], ekin)
+        assert rel(got, ekin + epot).max() < tol
+    else:
+        scale = 0.5 * (np.abs(lap_ref) + np.sum(grad_ref.reshape(len(r), -1) ** 2, axis=1))
+        assert (np.abs(got - (ekin + epot)) / scale).max() < tol
     st = aux["stats"].cpu().numpy()
     assert abs(st[0] - got.mean()) < 1e-9 * max(1, abs(got.mean()))
 
@@ -166,4 +177,4 @@ def test_mcmc_replay(cuda_lib, name):
     assert sure.any()
     np.testing.assert_array_equal(n_acc.cpu().numpy()[sure], g["mcmc_nacc"][sure])
     np.testing.assert_allclose(rr.cpu().numpy()[sure], g["mcmc_r"][sure], atol=1e-12)
-    assert smax[0] + smax[1] > 0
+    assert smax.n_pairs_same + smax.n_pairs_diff > 0
