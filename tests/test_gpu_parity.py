@@ -1,10 +1,14 @@
 """Parity of the CUDA path (through the C ABI) with the oracle on the same inputs.
 
 Tolerances: neighbour lists and triplets bit-exact; FP64 build <= 1e-10 relative on log|psi|, its
-gradient, its Laplacian and E_loc; FP32 path <= 1e-5 relative per walker on the forward Laplacian
-(log|psi|, |grad log psi|, lap log psi).  In FP32, E_loc = -(lap + |grad|^2)/2 + V cancels two terms
-that are up to ~1e4 times larger than the kinetic energy near nodes of psi (an all-FP32 evaluation of
-the oracle shows the same), so FP32 E_loc is checked against that scale: |dE| <= 1e-5 (|lap| + |grad|^2)/2."""
+gradient, its Laplacian and E_loc.  FP32 path: log|psi| <= 1e-5 relative; the forward Laplacian
+(grad log psi, lap log psi) and E_loc <= max(1e-5, 1e-6 * amp * kappa) relative, where kappa is the
+largest condition number of the four orbital matrices and amp = sum_d |w_d| / |sum_d w_d| the
+cancellation between the signed determinants.  The derivatives of log det A respond to a relative
+perturbation eps of A (FP32 rounding of the orbital values: eps ~ 6e-8) with errors ~ amp * kappa * eps;
+rounding only the value plane of an FP64 evaluation to FP32 reproduces the FP32 errors, so no FP32
+evaluation of this function is more accurate on ill-conditioned walkers.  E_loc is checked against the
+scale of the two terms that cancel in it, (|lap| + |grad|^2) / 2."""
 import ctypes as C
 
 import numpy as np
@@ -24,6 +28,17 @@ def _wf(name, precision):
     mol, nu, r, p, blob, offs = case(name)
     wf = FireWaveFunction(mol, precision=precision)
     return wf, mol, nu, r, p
+
+
+def conditioning(prob, p, w):
+    """amp * kappa of one walker (see the module docstring)."""
+    h = O.embedding_value(prob, p, w)
+    phi = O.orbitals_value(prob, p, w, h)
+    sl = [O.slogdet_lu(phi[d])[:2] for d in range(phi.shape[0])]
+    ld = np.array([x[1] for x in sl])
+    wts = np.array([x[0] for x in sl]) * np.exp(ld - ld.max())
+    amp = np.abs(wts).sum() / abs(wts.sum())
+    return amp * max(np.linalg.cond(phi[d]) for d in range(phi.shape[0]))
 
 
 def _static(wf, r, pad=1.0):
@@ -148,15 +163,19 @@ def test_local_energy(cuda_lib, name, precision):
     assert (np.abs(aux["logpsi"].double().cpu().numpy() - lp) / np.maximum(1, np.abs(lp))).max() < tol
     grad_ref = np.array([x[1] for x in fl]).reshape(dbg["grad"].shape)
     lap_ref = np.array([x[2] for x in fl])
+    if precision == "fp32":
+        tol = np.array([max(1e-5, 1e-6 * conditioning(prob, p, w)) for w in r.astype(np.float64)])
+    else:
+        tol = np.full(len(r), tol)
     for k in range(len(r)):
-        assert np.linalg.norm(dbg["grad"][k] - grad_ref[k]) / np.linalg.norm(grad_ref[k]) < tol
-    assert rel(dbg["lap"], lap_ref).max() < tol, (dbg["lap"], lap_ref)
+        assert np.linalg.norm(dbg["grad"][k] - grad_ref[k]) / np.linalg.norm(grad_ref[k]) < tol[k]
+    assert np.all(rel(dbg["lap"], lap_ref) < tol), (dbg["lap"], lap_ref, tol)
     if precision == "fp64":
-        assert rel(dbg["kinetic"], ekin).max() < tol, (dbg["kinetic"], ekin)
-        assert rel(got, ekin + epot).max() < tol
+        assert np.all(rel(dbg["kinetic"], ekin) < tol), (dbg["kinetic"], ekin)
+        assert np.all(rel(got, ekin + epot) < tol)
     else:
         scale = 0.5 * (np.abs(lap_ref) + np.sum(grad_ref.reshape(len(r), -1) ** 2, axis=1))
-        assert (np.abs(got - (ekin + epot)) / scale).max() < tol
+        assert np.all(np.abs(got - (ekin + epot)) / scale < tol)
     st = aux["stats"].cpu().numpy()
     assert abs(st[0] - got.mean()) < 1e-9 * max(1, abs(got.mean()))
 
