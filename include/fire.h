@@ -50,6 +50,7 @@ typedef enum {
 #define FIRE_FLAG_NONFINITE 4         /* a non-finite log|psi| or E_loc was produced */
 #define FIRE_FLAG_TRIPLET_OVERFLOW 8  /* triplet list exceeded its capacity */
 #define FIRE_FLAG_SINGULAR 16         /* an orbital matrix had a zero pivot */
+#define FIRE_FLAG_TIMEOUT 32          /* a bounded wait on a tensor-core completion barrier gave up */
 /* status[1] = max pairs of any walker seen, status[2] = max e-n neighbours seen,
  * status[3] = max triplets (sum_m deg(m)^2) seen; the host grows capacities from these,
  * like StaticScheduler (static_args.py:62-84). */
@@ -194,6 +195,12 @@ fire_status fire_potential_energy(void* stream, const fire_problem* prob, const 
  * "<stage> <launches> <total_ms>\n", into buf (host memory, NUL-terminated, truncated to len). */
 fire_status fire_profile_enable(int32_t on);
 fire_status fire_profile_report(char* buf, size_t len);
+
+/* The mixed-precision tensor-core contraction alone: C[M, N] = A[M, K] W[K, N] (all float32, row-major,
+ * device), computed with split-BF16 operands on tcgen05 (three BF16 products per element pair, FP32
+ * accumulation).  workspace: >= 4 * N * K bytes (the split, transposed weights).  K % 8 == 0. */
+fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const float* A, const float* W, float* C,
+                            void* workspace, size_t workspace_bytes, int32_t* status);
 
 #ifdef __cplusplus
 }

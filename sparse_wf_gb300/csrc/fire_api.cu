@@ -14,6 +14,7 @@
 
 #include "fire_gemm.cuh"
 #include "fire_kernels.cuh"
+#include "fire_tc.cuh"
 
 using namespace fire;
 
@@ -110,6 +111,28 @@ void prep_offsets(const fire_problem* p, int64_t* off) {
   off[PR_COUNT] = o;
 }
 size_t elem_size(const fire_problem* p) { return p->precision == FIRE_PREC_FP64 ? 8 : 4; }
+
+// Split BF16 copies of the contraction weights used on tensor cores (mixed precision only), stored
+// after the float slots of the prepared buffer: for each, hi [N][K] then lo [N][K].
+enum TcSlot { TC_UPD1, TC_UPD2, TC_ORB_UP, TC_ORB_DN, TC_V, TC_JMLP1, TC_JMLP2, TC_COUNT };
+struct TcSrc {
+  int slot;  // prepared slot (already scaled)
+  bool orb;  // N = NDET * n_el instead of F
+};
+const TcSrc kTcSrc[TC_COUNT] = {{PR_UPD1_W_S0, false}, {FIRE_P_UPD2_W, false}, {PR_ORB_UP_W_S1, true},
+                                {PR_ORB_DN_W_S1, true}, {PR_V_W_S1, false},    {PR_JMLP1_W_S1, false},
+                                {FIRE_P_JMLP2_W, false}};
+// byte offsets of the BF16 region (tc_off[TC_COUNT] = end)
+void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
+  size_t o = (float_bytes + 255) / 256 * 256;
+  for (int k = 0; k < TC_COUNT; ++k) {
+    off[k] = o;
+    const size_t N = kTcSrc[k].orb ? (size_t)NDET * p->n_el : (size_t)F;
+    o += 2 * N * F * sizeof(__nv_bfloat16);
+    o = (o + 255) / 256 * 256;
+  }
+  off[TC_COUNT] = o;
+}
 
 bool valid(const fire_problem* p) {
   return p && p->n_el >= 2 && p->n_el <= MAX_EL && p->n_up >= 0 && p->n_up <= p->n_el && p->n_nuc >= 1 &&
@@ -375,6 +398,8 @@ struct Ctx {
   Plan P;
   Nbr nb;
   Layout L;
+  bool mixed = false;
+  TcWeights tcw[TC_COUNT];
   template <typename U>
   U* buf(size_t off) const {
     return reinterpret_cast<U*>(ws + off);
@@ -419,9 +444,15 @@ GemmP<T> gp0() {
 }
 
 template <typename T, int MODE>
-cudaError_t gemm(const Ctx<T>& c, GemmP<T> g) {
+cudaError_t gemm(const Ctx<T>& c, GemmP<T> g, int tc_id = -1) {
   Prof pr("gemm", c.s);
   g_nlaunch++;
+  if constexpr (sizeof(T) == 4) {
+    if (c.mixed && tc_id >= 0) {
+      const int bn = g.N > 256 ? 128 : 256;
+      return gemm_tc(MODE, bn, g, c.tcw[tc_id], c.status, c.s);
+    }
+  }
   return launch_gemm<T, MODE>(g, c.s);
 }
 
@@ -493,7 +524,7 @@ struct Planes {
 template <typename T>
 cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, const T* b, int K, int N,
                        int rowsX, int rowsJcap, const int* rowsJdev, const int* node_map, int node_div, size_t zx,
-                       size_t jsq) {
+                       size_t jsq, int tc_id = -1) {
   GemmP<T> g = gp0<T>();
   g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.C = c.template buf<T>(out.X);
   g.ldc = N; g.M = rowsX; g.N = N; g.K = K; g.aux0 = c.template buf<T>(zx); g.ld_aux = N;
@@ -504,18 +535,18 @@ cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, c
   g.A = c.template buf<T>(in.J); g.lda = K; g.B = Wt; g.ldb = N; g.C = c.template buf<T>(out.J); g.ldc = N;
   g.M = rowsJcap; g.M_dev = rowsJdev; g.M_scale = 3; g.N = N; g.K = K; g.node_map = node_map;
   g.node_div = node_div; g.aux1 = c.template buf<T>(zx); g.aux2 = c.template buf<T>(jsq); g.ld_aux = N;
-  gemm<T, EPI_SILU_J>(c, g);
+  gemm<T, EPI_SILU_J>(c, g, tc_id);
   g = gp0<T>();
   g.A = c.template buf<T>(in.L); g.lda = K; g.B = Wt; g.ldb = N; g.C = c.template buf<T>(out.L); g.ldc = N;
   g.M = rowsX; g.N = N; g.K = K; g.aux1 = c.template buf<T>(zx); g.aux3 = c.template buf<T>(jsq); g.ld_aux = N;
-  gemm<T, EPI_SILU_L>(c, g);
+  gemm<T, EPI_SILU_L>(c, g, tc_id);
   return cudaPeekAtLastError();
 }
 
 // Linear(F -> N) without activation on a node (bias on X only)
 template <typename T>
 cudaError_t linear_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, const T* b, int K, int N,
-                         int rowsX, int rowsJcap, const int* rowsJdev) {
+                         int rowsX, int rowsJcap, const int* rowsJdev, int tc_id = -1) {
   GemmP<T> g = gp0<T>();
   g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.bias_period = 1;
   g.C = c.template buf<T>(out.X); g.ldc = N; g.M = rowsX; g.N = N; g.K = K;
@@ -523,9 +554,9 @@ cudaError_t linear_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt,
   if (!fl) return cudaPeekAtLastError();
   g.A = c.template buf<T>(in.J); g.bias = nullptr; g.C = c.template buf<T>(out.J); g.M = rowsJcap;
   g.M_dev = rowsJdev; g.M_scale = rowsJdev ? 3 : 1;
-  gemm<T, EPI_PLAIN>(c, g);
+  gemm<T, EPI_PLAIN>(c, g, tc_id);
   g.A = c.template buf<T>(in.L); g.C = c.template buf<T>(out.L); g.M = rowsX; g.M_dev = nullptr; g.M_scale = 1;
-  gemm<T, EPI_PLAIN>(c, g);
+  gemm<T, EPI_PLAIN>(c, g, tc_id);
   return cudaPeekAtLastError();
 }
 
@@ -568,13 +599,13 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   g.M_dev = c.L.pos_off + c.Wc; g.M_scale = 3; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
   g.node_map = c.L.pos_ctr; g.node_div = 3; g.dep_map = c.L.pos_dep; g.aux1 = env;
   g.aux2 = c.template buf<T>(c.P.rjs); g.aux3 = c.template buf<T>(c.P.rawx); g.ld_aux = DN; g.env_nv = 5;
-  gemm<T, EPI_ORB_J>(c, g);
+  gemm<T, EPI_ORB_J>(c, g, TC_ORB_UP);
   g = gp0<T>();
   g.A = c.template buf<T>(c.P.B2L); g.lda = F; g.B = c.W.w[PR_ORB_UP_W_S1]; g.B2 = c.W.w[PR_ORB_DN_W_S1];
   g.ldb = DN; g.C = c.template buf<T>(c.P.lapA); g.ldc = DN; g.M = G; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
   g.aux1 = env; g.aux2 = c.template buf<T>(c.P.rjs); g.aux3 = c.template buf<T>(c.P.rawx); g.ld_aux = DN;
   g.env_nv = 5;
-  gemm<T, EPI_ORB_L>(c, g);
+  gemm<T, EPI_ORB_L>(c, g, TC_ORB_UP);
   return cudaPeekAtLastError();
 }
 
@@ -638,7 +669,7 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
       c.template buf<T>(B2.X), FLM ? c.template buf<T>(B2.J) : nullptr, FLM ? c.template buf<T>(B2.L) : nullptr,
       c.nb, c.L, c.W.w[PR_QK_W_S1], c.W.w[PR_QK_B], nullptr, nullptr, c.template buf<T>(c.P.aX),
       FLM ? c.template buf<T>(c.P.aJ) : nullptr, FLM ? c.template buf<T>(c.P.aL) : nullptr, c.status);
-  linear_layer<T>(c, FLM, B2, B1, c.W.w[PR_V_W_S1], c.W.w[FIRE_P_ATT_V_B], F, F, G, Jcap, Jdev);
+  linear_layer<T>(c, FLM, B2, B1, c.W.w[PR_V_W_S1], c.W.w[FIRE_P_ATT_V_B], F, F, G, Jcap, Jdev, TC_V);
   cudaMemsetAsync(c.template buf<T>(c.P.Ax), 0, sizeof(T) * Wc * 2 * 272, c.s);
   if (FLM) cudaMemsetAsync(c.template buf<T>(c.P.Al), 0, sizeof(T) * Wc * 2 * 272, c.s);
   g_nlaunch++;
@@ -688,9 +719,9 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
   }
   // MLP Jastrow: SparseMLP [256, 256, 2] (silu on every layer), * mlp_scale + [0, log_bias], sum over nodes
   silu_layer<T>(c, FLM, B2, B1, c.W.w[PR_JMLP1_W_S1], c.W.w[FIRE_P_JMLP1_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3,
-                c.P.Zx, c.P.jsq);
+                c.P.Zx, c.P.jsq, TC_JMLP1);
   silu_layer<T>(c, FLM, B1, H, c.W.w[FIRE_P_JMLP2_W], c.W.w[FIRE_P_JMLP2_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3,
-                c.P.Zx, c.P.jsq);
+                c.P.Zx, c.P.jsq, TC_JMLP2);
   g_nlaunch++;
   k_narrow<T, 2, 0, FLM><<<G, 256, 0, c.s>>>(
       c.template buf<T>(H.X), FLM ? c.template buf<T>(H.J) : nullptr, FLM ? c.template buf<T>(H.L) : nullptr, c.nb,
@@ -715,9 +746,9 @@ cudaError_t stage_update(Ctx<T>& c) {
   const Planes H{c.P.HX, c.P.HJ, c.P.HL}, B1{c.P.B1X, c.P.B1J, c.P.B1L}, B2{c.P.B2X, c.P.B2J, c.P.B2L};
   Prof pr("update_mlp", c.s);
   silu_layer<T>(c, FLM, H, B1, c.W.w[PR_UPD1_W_S0], c.W.w[FIRE_P_UPD1_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3, c.P.Zx,
-                c.P.jsq);
+                c.P.jsq, TC_UPD1);
   silu_layer<T>(c, FLM, B1, B2, c.W.w[FIRE_P_UPD2_W], c.W.w[FIRE_P_UPD2_B], F, F, G, Jcap, Jdev, c.L.pos_ctr, 3, c.P.Zx,
-                c.P.jsq);
+                c.P.jsq, TC_UPD2);
   return cudaPeekAtLastError();
 }
 
@@ -801,6 +832,21 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
   c.status = status;
   c.ws = reinterpret_cast<unsigned char*>(ws);
   c.P = make_plan(p, Wmax, fl);
+  c.mixed = p->precision == FIRE_PREC_MIXED;
+  if (c.mixed) {
+    int64_t off[PR_COUNT + 1];
+    prep_offsets(p, off);
+    size_t to[TC_COUNT + 1];
+    tc_offsets(p, (size_t)off[PR_COUNT] * 4, to);
+    const unsigned char* base = reinterpret_cast<const unsigned char*>(prepared);
+    for (int k = 0; k < TC_COUNT; ++k) {
+      const size_t N = kTcSrc[k].orb ? (size_t)NDET * p->n_el : (size_t)F;
+      const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
+      c.tcw[k] = TcWeights{hi, hi + N * F, nullptr, nullptr};
+    }
+    c.tcw[TC_ORB_UP].hi2 = c.tcw[TC_ORB_DN].hi;
+    c.tcw[TC_ORB_UP].lo2 = c.tcw[TC_ORB_DN].lo;
+  }
   return c;
 }
 
@@ -914,6 +960,11 @@ fire_status fire_prepared_size(const fire_problem* prob, size_t* bytes) {
   int64_t off[PR_COUNT + 1];
   prep_offsets(prob, off);
   *bytes = (size_t)off[PR_COUNT] * elem_size(prob);
+  if (prob->precision == FIRE_PREC_MIXED) {
+    size_t to[TC_COUNT + 1];
+    tc_offsets(prob, *bytes, to);
+    *bytes = to[TC_COUNT];
+  }
   return FIRE_OK;
 }
 
@@ -936,7 +987,20 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
   if (prepared_bytes < need) return FIRE_ERR_WORKSPACE;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64) return prepare_impl<double>(s, prob, blob, offsets_host, prepared);
-  return prepare_impl<float>(s, prob, blob, offsets_host, prepared);
+  fire_status st = prepare_impl<float>(s, prob, blob, offsets_host, prepared);
+  if (st != FIRE_OK || prob->precision != FIRE_PREC_MIXED) return st;
+  int64_t off[PR_COUNT + 1];
+  prep_offsets(prob, off);
+  size_t to[TC_COUNT + 1];
+  tc_offsets(prob, (size_t)off[PR_COUNT] * 4, to);
+  unsigned char* base = reinterpret_cast<unsigned char*>(prepared);
+  for (int k = 0; k < TC_COUNT; ++k) {
+    const int N = kTcSrc[k].orb ? NDET * prob->n_el : F;
+    __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(base + to[k]);
+    g_nlaunch++;
+    split_transpose(reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot], F, N, hi, hi + (size_t)N * F, s);
+  }
+  return launch_status(__func__);
 }
 
 fire_status fire_neighbors(void* stream, const fire_problem* prob, const void* r, const float* R,
@@ -1070,6 +1134,22 @@ fire_status fire_potential_energy(void* stream, const fire_problem* prob, const 
   else
     k_potential<float><<<prob->n_walkers, 256, 0, s>>>(prob->n_el, prob->n_nuc, reinterpret_cast<const float*>(r), R,
                                                        Z, reinterpret_cast<float*>(out));
+  return launch_status(__func__);
+}
+
+fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const float* A, const float* W, float* C,
+                            void* workspace, size_t workspace_bytes, int32_t* status) {
+  if (M < 1 || N < 1 || K < 8 || K % 8 != 0 || !A || !W || !C || !workspace) return FIRE_ERR_INVALID;
+  if (workspace_bytes < 4 * (size_t)N * K) return FIRE_ERR_WORKSPACE;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(workspace);
+  g_nlaunch += 2;
+  split_transpose(W, K, N, hi, hi + (size_t)N * K, s);
+  GemmP<float> g;
+  std::memset(&g, 0, sizeof(g));
+  g.A = A; g.lda = K; g.C = C; g.ldc = N; g.M = M; g.N = N; g.K = K; g.node_div = 1; g.M_scale = 1; g.env_nv = 1;
+  TcWeights wt{hi, hi + (size_t)N * K, nullptr, nullptr};
+  gemm_tc(EPI_PLAIN, N > 128 ? 256 : 128, g, wt, status, s);
   return launch_status(__func__);
 }
 

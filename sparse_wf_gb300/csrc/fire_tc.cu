@@ -1,0 +1,42 @@
+// fire_tc.cu -- instantiations and host launchers of the tcgen05 contraction (fire_tc.cuh), and the
+// weight splitter that prepares its BF16 hi/lo, K-contiguous operands.
+#include "fire_tc.cuh"
+
+namespace fire {
+
+// hi/lo split of W[K][N] (row-major float) into transposed BF16 planes [N][K]
+__global__ void k_split_transpose(const float* __restrict__ W, int K, int N, __nv_bfloat16* __restrict__ hi,
+                                  __nv_bfloat16* __restrict__ lo) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over (n, k)
+  if (idx >= (long)N * K) return;
+  const int n = (int)(idx / K), k = (int)(idx % K);
+  const float w = W[(long)k * N + n];
+  const __nv_bfloat16 h = __float2bfloat16_rn(w);
+  hi[idx] = h;
+  lo[idx] = __float2bfloat16_rn(w - __bfloat162float(h));
+}
+
+cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __nv_bfloat16* lo, cudaStream_t s) {
+  const long tot = (long)N * K;
+  k_split_transpose<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, hi, lo);
+  return cudaPeekAtLastError();
+}
+
+cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt, int32_t* status, cudaStream_t s) {
+  if (p.K % 8 != 0 || p.lda % 4 != 0) return cudaErrorInvalidValue;
+#define FIRE_TC_CASE(M)                                                                   \
+  case M:                                                                                 \
+    return bn == 256 ? launch_gemm_tc<M, 256>(p, wt, status, s) : launch_gemm_tc<M, 128>(p, wt, status, s);
+  switch (mode) {
+    FIRE_TC_CASE(EPI_PLAIN)
+    FIRE_TC_CASE(EPI_SILU_J)
+    FIRE_TC_CASE(EPI_SILU_L)
+    FIRE_TC_CASE(EPI_ORB_J)
+    FIRE_TC_CASE(EPI_ORB_L)
+    default:
+      return cudaErrorInvalidValue;
+  }
+#undef FIRE_TC_CASE
+}
+
+}  // namespace fire

@@ -1,0 +1,31 @@
+"""The tcgen05 split-BF16 contraction against a torch FP64 reference of the same product."""
+import ctypes as C
+
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 256, 256), (300, 256, 256), (257, 200, 64), (1000, 1288, 256)])
+def test_gemm_mixed_matches_fp64(cuda_lib, M, N, K):
+    g = torch.Generator(device="cuda").manual_seed(M + N + K)
+    A = torch.randn(M, K, device="cuda", generator=g, dtype=torch.float32)
+    W = torch.randn(K, N, device="cuda", generator=g, dtype=torch.float32) / K**0.5
+    Cm = torch.full((M, N), float("nan"), device="cuda")
+    ws = torch.empty(4 * N * K, dtype=torch.uint8, device="cuda")
+    status = torch.zeros(8, dtype=torch.int32, device="cuda")
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = cuda_lib.fire_gemm_mixed(s, M, N, K, C.c_void_p(A.data_ptr()), C.c_void_p(W.data_ptr()),
+                                  C.c_void_p(Cm.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                                  C.c_void_p(status.data_ptr()))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(status[0]) == 0
+    ref = A.double() @ W.double()
+    err = (Cm.double() - ref).abs().max().item()
+    rms = ref.pow(2).mean().sqrt().item()
+    bf16 = (A.bfloat16().double() @ W.bfloat16().double() - ref).abs().max().item()
+    # split-BF16 products: ~2^-17 relative per product (plain BF16 ~2^-9)
+    assert err < 2e-5 * rms * K**0.5, (err, rms, bf16)
+    assert err < bf16 / 50
