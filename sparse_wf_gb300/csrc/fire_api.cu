@@ -14,7 +14,6 @@
 
 #include "fire_gemm.cuh"
 #include "fire_kernels.cuh"
-#include "fire_tc.cuh"
 
 using namespace fire;
 
@@ -148,7 +147,7 @@ struct Plan {
   size_t E5a, Z1, E5o, HX, HL, HJ, B1X, B1L, B1J, B2X, B2L, B2J, Zx, jsq;
   size_t env, rawx, rjs, Apl, lapA, Jorb, coef_up, coef_dn, Ainv, dgrad;
   size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, jsqr;
-  size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn;
+  size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, tile_mask;
   // double
   size_t ld, sd, dlap;
   size_t total;
@@ -236,6 +235,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.JMl, W * 2, es);
     take(P.JMj, W * 3 * n * 2, es);
   }
+  take(P.tile_mask, (fl ? 3 * Pc : G) / 128 + 2, 4);
   take(P.rn, G * 3, es);
   take(P.lpn, W, es);
   take(P.ld, W * NDET, 8);
@@ -450,7 +450,7 @@ cudaError_t gemm(const Ctx<T>& c, GemmP<T> g, int tc_id = -1) {
   if constexpr (sizeof(T) == 4) {
     if (c.mixed && tc_id >= 0) {
       const int bn = g.N > 256 ? 128 : 256;
-      return gemm_tc(MODE, bn, g, c.tcw[tc_id], c.status, c.s);
+      return gemm_tc(MODE, bn, g, c.tcw[tc_id], c.template buf<int>(c.P.tile_mask), c.status, c.s);
     }
   }
   return launch_gemm<T, MODE>(g, c.s);
@@ -1149,7 +1149,7 @@ fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const
   std::memset(&g, 0, sizeof(g));
   g.A = A; g.lda = K; g.C = C; g.ldc = N; g.M = M; g.N = N; g.K = K; g.node_div = 1; g.M_scale = 1; g.env_nv = 1;
   TcWeights wt{hi, hi + (size_t)N * K, nullptr, nullptr};
-  gemm_tc(EPI_PLAIN, N > 128 ? 256 : 128, g, wt, status, s);
+  gemm_tc(EPI_PLAIN, N > 128 ? 256 : 128, g, wt, nullptr, status, s);
   return launch_status(__func__);
 }
 

@@ -33,6 +33,15 @@ struct Layout {
   int cap_pos;   // capacity = W * (n + cap_p)
 };
 
+// Split-BF16 weights of a tensor-core contraction: hi/lo planes [N][K] (K contiguous); the second set
+// (spin-down weights of the orbital layer) may be null.
+struct TcWeights {
+  const __nv_bfloat16* hi;
+  const __nv_bfloat16* lo;
+  const __nv_bfloat16* hi2;
+  const __nv_bfloat16* lo2;
+};
+
 // Output pointers of the per-walker assembly (k_assemble).
 struct AssembleOut {
   void* logpsi;

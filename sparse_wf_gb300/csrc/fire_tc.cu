@@ -22,11 +22,21 @@ cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __n
   return cudaPeekAtLastError();
 }
 
-cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt, int32_t* status, cudaStream_t s) {
-  if (p.K % 8 != 0 || p.lda % 4 != 0) return cudaErrorInvalidValue;
-#define FIRE_TC_CASE(M)                                                                   \
-  case M:                                                                                 \
-    return bn == 256 ? launch_gemm_tc<M, 256>(p, wt, status, s) : launch_gemm_tc<M, 128>(p, wt, status, s);
+cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt, int* mask_buf, int32_t* status,
+                    cudaStream_t s) {
+  if (p.K % 8 != 0 || p.lda % 4 != 0 || p.ldc % 4 != 0 || (p.ld_aux % 4 != 0 && mode != EPI_PLAIN))
+    return cudaErrorInvalidValue;
+  static int num_sms = 0;
+  if (num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (num_sms <= 0) num_sms = 1;
+  }
+  (void)bn;
+#define FIRE_TC_CASE(M) \
+  case M:               \
+    return launch_gemm_tc<M>(p, wt, mask_buf, status, s, num_sms);
   switch (mode) {
     FIRE_TC_CASE(EPI_PLAIN)
     FIRE_TC_CASE(EPI_SILU_J)

@@ -13,7 +13,10 @@
 // matrices LBO = 128 bytes apart, 8-row groups SBO = 1024 bytes apart.  One thread issues the MMAs and
 // commits them to an mbarrier per stage; all waits are bounded and report FIRE_FLAG_TIMEOUT.
 #pragma once
+#include <algorithm>
+
 #include "fire_gemm.cuh"
+#include "fire_internal.cuh"
 
 namespace fire {
 
@@ -21,12 +24,6 @@ constexpr int TC_BM = 128, TC_BK = 64, TC_THREADS = 256;
 constexpr uint32_t TC_LBO = 128, TC_SBO = 1024;
 constexpr long TC_SPIN_LIMIT = 1L << 22;
 
-struct TcWeights {
-  const __nv_bfloat16* hi;   // [N][K] (K contiguous)
-  const __nv_bfloat16* lo;
-  const __nv_bfloat16* hi2;  // second weight set (spin down) or nullptr
-  const __nv_bfloat16* lo2;
-};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -98,212 +95,362 @@ __device__ __forceinline__ uint32_t tc_off(int row, int k) {
   return (uint32_t)((row & 7) * 16 + (row >> 3) * TC_SBO + (k & 7) * 2 + (k >> 3) * TC_LBO);
 }
 
-template <int BN>
-struct TcSmem {
-  static constexpr int A_BYTES = TC_BM * TC_BK * 2;  // 16 KB per BF16 plane
-  static constexpr int B_BYTES = BN * TC_BK * 2;
-  static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;  // a_hi, a_lo, b_hi, b_lo
-  static constexpr int TOTAL = 2 * STAGE + 1024;           // + barriers / tmem holder / row ids
-};
+// ----------------------------------------------------------------------------- vectorised epilogues
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
-template <int MODE, int BN>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(GemmP<float> p, TcWeights wt, int32_t* status) {
-  extern __shared__ __align__(1024) unsigned char tc_smem[];
-  using SM = TcSmem<BN>;
-  unsigned char* stage_base = tc_smem;
-  unsigned char* misc = tc_smem + 2 * SM::STAGE;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(misc);       // [2]
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(misc + 64);
-  int* row_node = reinterpret_cast<int*>(misc + 128);       // [128] (SILU_J)
-
-  int rows = p.M;
-  if (p.M_dev) rows = min(rows, p.M_scale * (*p.M_dev));
-  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
-  if (m0 >= rows) return;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-
-  int passes = 1, first_spin = 0;
-  if (wt.hi2) {
-    int up = 0, dn = 0;
-    if (tid < TC_BM && m0 + tid < rows) {
-      const int node = gemm_node(p, m0 + tid);
-      if ((node % p.n_el) < p.n_up) up = 1; else dn = 1;
+// Applies the epilogue of MODE to columns col..col+3 of one row (col % 4 == 0, col + 3 < N).
+template <int MODE>
+__device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int node, int col, const float* a,
+                                          int spin) {
+  if (MODE == EPI_PLAIN) {
+    float4 v = make_float4(a[0], a[1], a[2], a[3]);
+    if (p.bias && p.bias_period > 0 && (row % p.bias_period) == 0) {
+      const float4 b = ld4(p.bias + col);
+      v.x += b.x; v.y += b.y; v.z += b.z; v.w += b.w;
     }
-    up = __syncthreads_or(up);
-    dn = __syncthreads_or(dn);
-    first_spin = up ? 0 : 1;
-    passes = up + dn;
-  }
-  if (MODE == EPI_SILU_J && tid < TC_BM) row_node[tid] = (m0 + tid < rows) ? gemm_node(p, m0 + tid) : -1;
-  if (tid == 0) {
-    mbar_init(smem_u32(&mbar[0]), 1);
-    mbar_init(smem_u32(&mbar[1]), 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
-                 "r"(BN));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tmem_holder;
-  const uint32_t idesc = tc_idesc<BN>();
-  const int nk = (p.K + TC_BK - 1) / TC_BK;
-  uint32_t commits[2] = {0, 0};  // completed-commit counters per stage (tracked identically by all threads)
-  bool ok = true;
-
-  for (int pass = 0; pass < passes && ok; ++pass) {
-    const int spin = first_spin + pass;
-    const __nv_bfloat16* Bhi = spin == 0 ? wt.hi : wt.hi2;
-    const __nv_bfloat16* Blo = spin == 0 ? wt.lo : wt.lo2;
-    for (int kt = 0; kt < nk && ok; ++kt) {
-      const int s = kt & 1;
-      unsigned char* st = stage_base + s * SM::STAGE;
-      if (commits[s] > 0) {
-        // the MMAs that last read this stage must be complete before it is overwritten; the decision
-        // is made uniform across the CTA so every thread takes the same path
-        const bool w = mbar_wait(smem_u32(&mbar[s]), (commits[s] - 1) & 1);
-        ok = __syncthreads_and(w) != 0;
-      }
-      if (!ok) break;
-      const int k0 = kt * TC_BK;
-      // ---- stage A (FP32 -> BF16 hi/lo), 128 x 64: 2048 float4, 8 per thread
-      unsigned char* a_hi = st;
-      unsigned char* a_lo = st + SM::A_BYTES;
-#pragma unroll 4
-      for (int q = tid; q < TC_BM * TC_BK / 4; q += TC_THREADS) {
-        const int r = q / (TC_BK / 4), kq = (q % (TC_BK / 4)) * 4;
-        const int gr = m0 + r, gk = k0 + kq;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gr < rows) {
-          const float* src = p.A + (long)gr * p.lda + gk;
-          if (gk + 3 < p.K) v = *reinterpret_cast<const float4*>(src);
-          else {
-            if (gk < p.K) v.x = src[0];
-            if (gk + 1 < p.K) v.y = src[1];
-            if (gk + 2 < p.K) v.z = src[2];
-          }
-        }
-        const __nv_bfloat16 h0 = __float2bfloat16_rn(v.x), h1 = __float2bfloat16_rn(v.y),
-                            h2 = __float2bfloat16_rn(v.z), h3 = __float2bfloat16_rn(v.w);
-        const __nv_bfloat16 l0 = __float2bfloat16_rn(v.x - __bfloat162float(h0)),
-                            l1 = __float2bfloat16_rn(v.y - __bfloat162float(h1)),
-                            l2 = __float2bfloat16_rn(v.z - __bfloat162float(h2)),
-                            l3 = __float2bfloat16_rn(v.w - __bfloat162float(h3));
-        const uint32_t off = tc_off(r, kq);
-        uint2 hv, lv;
-        hv.x = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-        hv.y = (uint32_t)__bfloat16_as_ushort(h2) | ((uint32_t)__bfloat16_as_ushort(h3) << 16);
-        lv.x = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-        lv.y = (uint32_t)__bfloat16_as_ushort(l2) | ((uint32_t)__bfloat16_as_ushort(l3) << 16);
-        *reinterpret_cast<uint2*>(a_hi + off) = hv;
-        *reinterpret_cast<uint2*>(a_lo + off) = lv;
-      }
-      // ---- stage B (pre-split BF16, [N][K]), BN x 64: 16-byte chunks of 8 elements
-      unsigned char* b_hi = st + 2 * SM::A_BYTES;
-      unsigned char* b_lo = b_hi + SM::B_BYTES;
-      for (int q = tid; q < BN * (TC_BK / 8); q += TC_THREADS) {
-        const int r = q / (TC_BK / 8), c = q % (TC_BK / 8);
-        const int gn = n0 + r, gk = k0 + c * 8;
-        uint4 h = make_uint4(0, 0, 0, 0), l = make_uint4(0, 0, 0, 0);
-        if (gn < p.N && gk < p.K) {
-          h = *reinterpret_cast<const uint4*>(Bhi + (long)gn * p.K + gk);
-          l = *reinterpret_cast<const uint4*>(Blo + (long)gn * p.K + gk);
-        }
-        const uint32_t off = tc_off(r, c * 8);
-        *reinterpret_cast<uint4*>(b_hi + off) = h;
-        *reinterpret_cast<uint4*>(b_lo + off) = l;
-      }
-      proxy_fence();
-      __syncthreads();
-      if (tid == 0) {
-        tc_fence_after();
-        const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+    st4(p.C + (long)row * p.ldc + col, v);
+  } else if (MODE == EPI_SILU_J || MODE == EPI_SILU_L) {
+    const float4 z = ld4(p.aux1 + (long)node * p.ld_aux + col);
+    const float zz[4] = {z.x, z.y, z.z, z.w};
+    float o[4];
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (MODE == EPI_SILU_L) q = ld4(p.aux3 + (long)row * p.ld_aux + col);
+    const float qq[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-        for (int kk = 0; kk < TC_BK / 16; ++kk) {
-          const uint32_t step = kk * 2 * TC_LBO;
-          tc_mma(tmem, tc_desc(ah + step), tc_desc(bh + step), idesc, (kt > 0 || kk > 0) ? 1u : 0u);
-          tc_mma(tmem, tc_desc(ah + step), tc_desc(bl + step), idesc, 1u);
-          tc_mma(tmem, tc_desc(al + step), tc_desc(bh + step), idesc, 1u);
-        }
-        tc_commit(smem_u32(&mbar[s]));
-      }
-      commits[s] += 1;
+    for (int k = 0; k < 4; ++k) {
+      float y, d1, d2;
+      silu3(zz[k], y, d1, d2);
+      o[k] = MODE == EPI_SILU_J ? a[k] * d1 : a[k] * d1 + qq[k] * d2;
     }
-    // ---- wait for the last commit, then the epilogue from TMEM
-    if (ok) {
-      const int s_last = (nk - 1) & 1;
-      const bool w = mbar_wait(smem_u32(&mbar[s_last]), (commits[s_last] - 1) & 1);
-      ok = __syncthreads_and(w) != 0;
-      // the other stage's last commit precedes it in issue order and is therefore complete too
+    st4(p.C + (long)row * p.ldc + col, make_float4(o[0], o[1], o[2], o[3]));
+  } else if (MODE == EPI_ORB_J) {
+    const int pos = row / 3, t = row - 3 * pos;
+    const float* env = p.aux1 + (long)node * 5 * p.ld_aux;
+    const float4 ex = ld4(env + col);
+    if (p.dep_map[pos] == node) {
+      const float4 raw = ld4(p.aux3 + (long)node * p.ld_aux + col);
+      const float4 ej = ld4(env + (1 + t) * p.ld_aux + col);
+      st4(p.C + (long)row * p.ldc + col, make_float4(raw.x * ej.x + ex.x * a[0], raw.y * ej.y + ex.y * a[1],
+                                                     raw.z * ej.z + ex.z * a[2], raw.w * ej.w + ex.w * a[3]));
+      st4(p.aux2 + ((long)node * 3 + t) * p.ld_aux + col, make_float4(a[0], a[1], a[2], a[3]));
+    } else {
+      st4(p.C + (long)row * p.ldc + col, make_float4(ex.x * a[0], ex.y * a[1], ex.z * a[2], ex.w * a[3]));
     }
-    tc_fence_after();
-    if (ok) {
-      const int wq = warp & 3, half = warp >> 2;
-      const int row_l = wq * 32 + lane;
-      const int row = m0 + row_l;
-      bool row_ok = row < rows;
-      if (row_ok && wt.hi2) {
-        const int node = gemm_node(p, row);
-        row_ok = (((node % p.n_el) < p.n_up) ? 0 : 1) == spin;
-      }
-      float* sq = reinterpret_cast<float*>(stage_base);  // SILU_J squares [128][BN + 1] (reuses stage memory)
-      for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 16) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)c0, v);
+  } else if (MODE == EPI_ORB_L) {
+    const float* env = p.aux1 + (long)row * 5 * p.ld_aux;
+    const float* rjs = p.aux2 + (long)row * 3 * p.ld_aux;
+    const float4 ex = ld4(env + col), el = ld4(env + 4 * p.ld_aux + col), raw = ld4(p.aux3 + (long)row * p.ld_aux + col);
+    float4 v = make_float4(a[0] * ex.x + el.x * raw.x, a[1] * ex.y + el.y * raw.y, a[2] * ex.z + el.z * raw.z,
+                           a[3] * ex.w + el.w * raw.w);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int col = n0 + c0 + j;
-          if (row_ok && col < p.N) gemm_store<float, MODE>(p, row, col, v[j], spin);
-          if (MODE == EPI_SILU_J) sq[row_l * (BN + 1) + c0 + j] = (row < rows) ? v[j] * v[j] : 0.f;
-        }
-      }
-      if (MODE == EPI_SILU_J) {
-        __syncthreads();
-        for (int lc = tid; lc < BN; lc += TC_THREADS) {
-          const int col = n0 + lc;
-          if (col >= p.N) continue;
-          int cur = -1;
-          float acc = 0.f;
-          for (int lr = 0; lr < TC_BM; ++lr) {
-            const int nd = row_node[lr];
-            if (nd != cur) {
-              if (cur >= 0) atomicAdd(&p.aux2[(long)cur * p.ld_aux + col], acc);
-              cur = nd;
-              acc = 0.f;
-            }
-            if (nd >= 0) acc += sq[lr * (BN + 1) + lc];
-          }
-          if (cur >= 0) atomicAdd(&p.aux2[(long)cur * p.ld_aux + col], acc);
-        }
-      }
+    for (int t = 0; t < 3; ++t) {
+      const float4 r = ld4(rjs + t * p.ld_aux + col), e = ld4(env + (1 + t) * p.ld_aux + col);
+      v.x += 2.f * r.x * e.x; v.y += 2.f * r.y * e.y; v.z += 2.f * r.z * e.z; v.w += 2.f * r.w * e.w;
     }
-    tc_fence_before();
-    __syncthreads();  // TMEM reads of this pass are done before the next pass's MMAs overwrite it
-    tc_fence_after();
-  }
-  if (!ok && tid == 0) set_flag(status, FIRE_FLAG_TIMEOUT);
-  if (!ok) {
-    // drain: wait (bounded) for any MMA still in flight before releasing tensor memory
-    for (int s = 0; s < 2; ++s)
-      if (commits[s] > 0) mbar_wait(smem_u32(&mbar[s]), (commits[s] - 1) & 1);
-  }
-  __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    st4(p.C + (long)row * p.ldc + col, v);
   }
 }
 
-template <int MODE, int BN>
-inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, int32_t* status, cudaStream_t s) {
-  const int smem = TcSmem<BN>::TOTAL;
-  cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<MODE, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+// ----------------------------------------------------------------------------- persistent kernel
+// Each CTA owns one 128-column slice of the output (n_tile = blockIdx.x % nt) and keeps the split
+// weights of that slice resident in shared memory (K <= 256: 128 KB); it walks the 128-row tiles
+// m = blockIdx.x / nt, + gridDim.x / nt, ...  Only A (FP32 -> BF16 hi/lo) streams through a 3-stage
+// ring.  Warp roles: warps 0-7 epilogue (TMEM lane quadrant = warp % 4, column half = warp / 4),
+// warps 8-11 loaders, warp 12 lane 0 issues the MMAs; TMEM holds two 128-column accumulators so the
+// epilogue of one tile overlaps the MMAs of the next.  spin_filter >= 0 restricts the launch to the rows
+// of one spin (the orbital layer runs once per spin with that spin's weights).
+constexpr int TCP_THREADS = 416, TCP_BN = 128, TCP_KMAX = 256, TCP_STAGES = 3;
+struct TcCfg {
+  static constexpr int A_BYTES = TC_BM * TC_BK * 2;              // one BF16 plane of an A stage
+  static constexpr int A_STAGE = 2 * A_BYTES;                    // hi + lo
+  static constexpr int BK_BYTES = TCP_BN * TC_BK * 2;            // one BF16 plane of one resident k-tile
+  static constexpr int B_BYTES = 2 * BK_BYTES * (TCP_KMAX / TC_BK);  // hi + lo, all k-tiles
+  static constexpr int TOTAL = B_BYTES + TCP_STAGES * A_STAGE + 256;
+};
+
+struct TcBar {
+  uint64_t full[TCP_STAGES], empty[TCP_STAGES], tfull[2], tempty[2];
+  uint32_t tmem;
+  int abort;
+};
+
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  const uint32_t a = smem_u32(bar);
+  for (long i = 0; i < TC_SPIN_LIMIT; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 63) == 63 && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+__device__ __forceinline__ void tc_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, const __nv_bfloat16* Bhi,
+                                                            const __nv_bfloat16* Blo, int spin_filter,
+                                                            const int* tile_mask, int32_t* status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  unsigned char* bres = tc_smem;                        // resident B: [k-tile][hi, lo][128 x 64]
+  unsigned char* astage = tc_smem + TcCfg::B_BYTES;     // [stage][hi, lo][128 x 64]
+  TcBar* bars = reinterpret_cast<TcBar*>(astage + TCP_STAGES * TcCfg::A_STAGE);
+  volatile int* abort = &bars->abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  int rows = p.M;
+  if (p.M_dev) rows = min(rows, p.M_scale * (*p.M_dev));
+  const int mt = (rows + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
+  const int groups = gridDim.x / nt;  // CTAs per n-tile
+  const int n_tile = blockIdx.x % nt, m_first = blockIdx.x / nt;
+  if (m_first >= mt || n_tile >= nt) return;
+  const int n0 = n_tile * TCP_BN;
+  const int nk = (p.K + TC_BK - 1) / TC_BK;
+
+  // resident weights of this column slice (all threads)
+  for (int q = tid; q < nk * TCP_BN * (TC_BK / 8); q += TCP_THREADS) {
+    const int kt = q / (TCP_BN * (TC_BK / 8));
+    const int rq = q % (TCP_BN * (TC_BK / 8));
+    const int r = rq >> 3, c = rq & 7;
+    const int gn = n0 + r, gk = kt * TC_BK + c * 8;
+    uint4 h = make_uint4(0, 0, 0, 0), l = h;
+    if (gn < p.N && gk < p.K) {
+      h = *reinterpret_cast<const uint4*>(Bhi + (long)gn * p.K + gk);
+      l = *reinterpret_cast<const uint4*>(Blo + (long)gn * p.K + gk);
+    }
+    unsigned char* bk = bres + kt * 2 * TcCfg::BK_BYTES;
+    const uint32_t off = tc_off(r, c * 8);
+    *reinterpret_cast<uint4*>(bk + off) = h;
+    *reinterpret_cast<uint4*>(bk + TcCfg::BK_BYTES + off) = l;
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TCP_STAGES; ++s) {
+      mbar_init(smem_u32(&bars->full[s]), 128);
+      mbar_init(smem_u32(&bars->empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&bars->tfull[b]), 1);
+      mbar_init(smem_u32(&bars->tempty[b]), 256);
+    }
+    bars->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 12) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem)),
+                 "r"(2 * TCP_BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  proxy_fence();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = bars->tmem;
+  auto skip = [&](int m) -> bool {
+    return spin_filter >= 0 && !((tile_mask[m] >> spin_filter) & 1);
+  };
+
+  if (warp >= 8 && warp < 12) {
+    // ------------------------------------------------------------------ loaders (128 threads)
+    const int lt = tid - 256;
+    long kc = 0;
+    for (int m = m_first; m < mt && !*abort; m += groups) {
+      if (skip(m)) continue;
+      const int m0 = m * TC_BM;
+      for (int kt = 0; kt < nk; ++kt, ++kc) {
+        const int s = (int)(kc % TCP_STAGES);
+        const long use = kc / TCP_STAGES;
+        if (use > 0 && !tc_wait(&bars->empty[s], (uint32_t)((use - 1) & 1), abort)) break;
+        unsigned char* a_hi = astage + s * TcCfg::A_STAGE;
+        unsigned char* a_lo = a_hi + TcCfg::A_BYTES;
+        const int k0 = kt * TC_BK;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          float4 v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int q = lt + 128 * (u + 8 * h);
+            const int r = q >> 4, kq = (q & 15) * 4;
+            const int gr = m0 + r, gk = k0 + kq;
+            v[u] = (gr < rows && gk < p.K) ? ld4(p.A + (long)gr * p.lda + gk) : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int q = lt + 128 * (u + 8 * h);
+            const int r = q >> 4, kq = (q & 15) * 4;
+            const float f[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+            uint32_t hw[2], lw[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const __nv_bfloat16 h0 = __float2bfloat16_rn(f[2 * e]), h1 = __float2bfloat16_rn(f[2 * e + 1]);
+              const __nv_bfloat16 l0 = __float2bfloat16_rn(f[2 * e] - __bfloat162float(h0));
+              const __nv_bfloat16 l1 = __float2bfloat16_rn(f[2 * e + 1] - __bfloat162float(h1));
+              hw[e] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+              lw[e] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+            }
+            const uint32_t off = tc_off(r, kq);
+            *reinterpret_cast<uint2*>(a_hi + off) = make_uint2(hw[0], hw[1]);
+            *reinterpret_cast<uint2*>(a_lo + off) = make_uint2(lw[0], lw[1]);
+          }
+        }
+        proxy_fence();
+        tc_arrive(&bars->full[s]);
+      }
+    }
+  } else if (warp == 12) {
+    // ------------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc<TCP_BN>();
+      const uint32_t b0 = smem_u32(bres), a0 = smem_u32(astage);
+      long kc = 0, uc = 0;
+      for (int m = m_first; m < mt && !*abort; m += groups) {
+        if (skip(m)) continue;
+        const int b = (int)(uc & 1);
+        const long ub = uc >> 1;
+        if (ub > 0 && !tc_wait(&bars->tempty[b], (uint32_t)((ub - 1) & 1), abort)) break;
+        tc_fence_after();
+        const uint32_t acc_t = tmem + (uint32_t)(b * TCP_BN);
+        for (int kt = 0; kt < nk; ++kt, ++kc) {
+          const int s = (int)(kc % TCP_STAGES);
+          if (!tc_wait(&bars->full[s], (uint32_t)((kc / TCP_STAGES) & 1), abort)) break;
+          tc_fence_after();
+          const uint32_t ah = a0 + s * TcCfg::A_STAGE, al = ah + TcCfg::A_BYTES;
+          const uint32_t bh = b0 + kt * 2 * TcCfg::BK_BYTES, bl = bh + TcCfg::BK_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 16; ++kk) {
+            const uint32_t step = kk * 2 * TC_LBO;
+            tc_mma(acc_t, tc_desc(ah + step), tc_desc(bh + step), idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+            tc_mma(acc_t, tc_desc(ah + step), tc_desc(bl + step), idesc, 1u);
+            tc_mma(acc_t, tc_desc(al + step), tc_desc(bh + step), idesc, 1u);
+          }
+          tc_commit(smem_u32(&bars->empty[s]));
+        }
+        if (*abort) break;
+        tc_commit(smem_u32(&bars->tfull[b]));
+        ++uc;
+      }
+    }
+  } else {
+    // ------------------------------------------------------------------ epilogue (warps 0-7, 256 threads)
+    const int quad = warp & 3, half = warp >> 2;
+    long uc = 0;
+    for (int m = m_first; m < mt && !*abort; m += groups) {
+      if (skip(m)) continue;
+      const int m0 = m * TC_BM;
+      const int row = m0 + quad * 32 + lane;
+      const bool valid = row < rows;
+      const int node = valid ? gemm_node(p, row) : -1;
+      const int b = (int)(uc & 1);
+      if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
+      tc_fence_after();
+      bool mine = valid;
+      if (valid && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
+      const int prev = __shfl_up_sync(0xffffffffu, node, 1);
+      const bool head = lane == 0 || prev != node;
+      const uint32_t base = tmem + (uint32_t)(b * TCP_BN) + ((uint32_t)(quad * 32) << 16);
+      for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
+        float v[16];
+        tmem_ld16(base + (uint32_t)c0, v);
+        if (mine) {
+#pragma unroll
+          for (int j = 0; j < 16; j += 4) {
+            const int col = n0 + c0 + j;
+            if (col + 3 < p.N) tc_store4<MODE>(p, row, node, col, v + j, spin_filter < 0 ? 0 : spin_filter);
+            else
+              for (int e = 0; e < 4; ++e)
+                if (col + e < p.N)
+                  gemm_store<float, MODE>(p, row, col + e, v[j + e], spin_filter < 0 ? 0 : spin_filter);
+          }
+        }
+        if (MODE == EPI_SILU_J) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float q = valid ? v[j] * v[j] : 0.f;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const float u = __shfl_down_sync(0xffffffffu, q, o);
+              const int nu = __shfl_down_sync(0xffffffffu, node, o);
+              if (lane + o < 32 && nu == node) q += u;
+            }
+            const int col = n0 + c0 + j;
+            if (valid && head && col < p.N) atomicAdd(&p.aux2[(long)node * p.ld_aux + col], q);
+          }
+        }
+      }
+      tc_fence_before();
+      tc_arrive(&bars->tempty[b]);
+      ++uc;
+    }
+  }
+  __syncthreads();
+  if (*abort && tid == 0) set_flag(status, FIRE_FLAG_TIMEOUT);
+  if (*abort && warp == 12 && lane == 0) {
+    // bounded drain: an MMA still in flight must finish before tensor memory is released
+    for (int s = 0; s < TCP_STAGES; ++s) {
+      const uint32_t a = smem_u32(&bars->empty[s]);
+      for (int i = 0; i < (1 << 16); ++i) {
+        uint32_t d0, d1;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d0)
+            : "r"(a)
+            : "memory");
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 1;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d1)
+            : "r"(a)
+            : "memory");
+        if (d0 || d1) break;
+      }
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 12) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TCP_BN));
+  }
+}
+
+__global__ void k_tile_mask(GemmP<float> p, int* mask) {
+  const int m_tile = blockIdx.x;
+  int rows = p.M;
+  if (p.M_dev) rows = min(rows, p.M_scale * (*p.M_dev));
+  const int row = m_tile * TC_BM + threadIdx.x;
+  int up = 0, dn = 0;
+  if (row < rows) {
+    const int node = gemm_node(p, row);
+    if ((node % p.n_el) < p.n_up) up = 1; else dn = 1;
+  }
+  up = __syncthreads_or(up);
+  dn = __syncthreads_or(dn);
+  if (threadIdx.x == 0) mask[m_tile] = up | (dn << 1);
+}
+
+template <int MODE>
+inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, int* mask_buf, int32_t* status,
+                                  cudaStream_t s, int num_sms) {
+  if (p.K > TCP_KMAX) return cudaErrorInvalidValue;
+  const int smem = TcCfg::TOTAL;
+  cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((p.N + BN - 1) / BN, (p.M + TC_BM - 1) / TC_BM);
-  if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-  k_gemm_tc<MODE, BN><<<grid, TC_THREADS, smem, s>>>(p, wt, status);
+  const long mt = (p.M + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
+  if (mt == 0 || nt == 0) return cudaSuccess;
+  const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
+  const unsigned grid = (unsigned)(groups * nt);
+  if (wt.hi2) {
+    if (!mask_buf) return cudaErrorInvalidValue;
+    k_tile_mask<<<(unsigned)mt, TC_BM, 0, s>>>(p, mask_buf);
+    k_gemm_tcp<MODE><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, 0, mask_buf, status);
+    k_gemm_tcp<MODE><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi2, wt.lo2, 1, mask_buf, status);
+  } else {
+    k_gemm_tcp<MODE><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status);
+  }
   return cudaPeekAtLastError();
 }
 
