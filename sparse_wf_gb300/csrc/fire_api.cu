@@ -609,17 +609,21 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   return cudaPeekAtLastError();
 }
 
+// Cluster size of the Gauss-Jordan kernel: the smallest power of two whose per-CTA column slice fits in
+// shared memory (fewer CTAs per matrix = fewer participants in every cluster barrier).
 int gj_cluster(int n, size_t es, size_t* smem_out) {
   const int cls[5] = {1, 2, 4, 8, 16};
-  for (int k = 0; k < 5; ++k) {
-    const int CL = cls[k];
-    const size_t wc = (n + CL - 1) / CL;
-    const size_t sm = (size_t)n * wc * es + (size_t)n * es + wc * es + 2 * (size_t)n * 4 + 64;
-    if (sm <= 220 * 1024) {
-      *smem_out = sm;
-      return CL;
+  const size_t limits[2] = {220 * 1024, 220 * 1024};
+  for (int pass = 0; pass < 2; ++pass)
+    for (int k = 0; k < 5; ++k) {
+      const int CL = cls[k];
+      const size_t wc = (n + CL - 1) / CL;
+      const size_t sm = (size_t)n * wc * es + 3 * (size_t)n * es + wc * es + 2 * (size_t)n * 4 + 64;
+      if (sm <= limits[pass] && wc <= 256) {
+        *smem_out = sm;
+        return CL;
+      }
     }
-  }
   return 0;
 }
 
@@ -793,7 +797,7 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {
     const size_t es = sizeof(T);
-    const size_t smem = es * (3 * DL_CMAX_DECL * (DL_CMAX_DECL + 1) + 3 * DL_CMAX_DECL * 33 + 32 * (DL_CMAX_DECL + 1));
+    const size_t smem = es * std::max<size_t>(32 * 196 + 32 * DL_CMAX_DECL, 3 * DL_CMAX_DECL * (DL_CMAX_DECL + 1));
     cudaFuncSetAttribute(k_detlap<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     Prof pr("detlap", c.s);
     g_nlaunch++;

@@ -55,10 +55,20 @@ __global__ void k_env_coef(const T* __restrict__ r, const float* __restrict__ R,
   }
 }
 
-// Gauss-Jordan inversion / LU with partial pivoting.  grid = (CL, matrices), cluster = (CL, 1, 1).
-// A: [matrices][lda-strided rows] with element (i, o) of matrix (w, d) at
-//    A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]).
+// Gauss-Jordan inversion / LU with partial pivoting.  grid = (CL, matrices), cluster = (CL, 1, 1),
+// 256 threads; thread (tx, ty) = (tid % wc, tid / wc) owns column tx of this CTA's slice and rows
+// ty, ty + ty_n, ...
+// Look-ahead: during step k the CTA that owns column k + 1 computes that column's post-step values first
+// and writes them into every CTA's colbuf[(k + 1) % 3] (distributed shared memory), then all threads
+// arrive on the cluster barrier; step k + 1 starts with the matching wait, so each step has a single
+// split cluster barrier and the pivot column is read from local shared memory.  Three buffers: the one
+// rewritten during step k was last read during step k - 2, which every CTA finished before arriving in
+// step k - 1 (the arrival the writer waited for).
+// A: element (i, o) of matrix (w, d) at A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]).
 // Outputs: logdet[w * NDET + d], sign[...] (double); Ainv[(w * NDET + d) * n * n + o * n + i] (if INV).
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
 template <typename S, typename TI, typename TO, bool INV>
 __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, int n, int CL,
                                                       double* __restrict__ logdet, double* __restrict__ sign,
@@ -71,27 +81,35 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
   const int wc = (n + CL - 1) / CL;
   const int j0 = c * wc, jn = max(0, min(wc, n - j0));
   S* a = reinterpret_cast<S*>(gj_smem);  // [n][wc]
-  S* col = a + (size_t)n * wc;           // [n]
-  S* rowk = col + n;                     // [wc]
-  int* perm = reinterpret_cast<int*>(rowk + wc);  // [n]
+  S* colbuf = a + (size_t)n * wc;        // [3][n] pivot columns (published by their owner)
+  S* rowk = colbuf + 3 * n;              // [wc]
+  int* perm = reinterpret_cast<int*>(rowk + wc);  // [n] (+ [n] scratch)
   __shared__ S redv[8];
   __shared__ int redi[8];
-  __shared__ int piv_s;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int ty_n = max(1, 256 / wc);
+  const int tx = tid % wc, ty = tid / wc;
+  const bool upd = ty < ty_n && tx < jn;
   for (int e = tid; e < n * wc; e += blockDim.x) {
     const int i = e / wc, jl = e - i * wc;
     a[e] = jl < jn ? (S)A[((long)(w * n + i) * NDET + d) * n + j0 + jl] : S(0);
   }
+  cluster.sync();  // every CTA of the cluster is running and has its slice
+  if (c == 0) {     // publish column 0
+    for (int i = tid; i < n; i += blockDim.x) {
+      const S v = a[(size_t)i * wc];
+      for (int r = 0; r < CL; ++r) cluster.map_shared_rank(colbuf, r)[i] = v;
+    }
+  }
+  __syncthreads();
+  cluster_arrive();
   double ld = 0.0;
   int neg = 0;
   bool singular = false;
   for (int k = 0; k < n; ++k) {
     const int owner = k / wc, kl = k - owner * wc;
-    cluster.sync();  // previous updates complete everywhere
-    const S* ra = cluster.map_shared_rank(a, owner);
-    for (int i = tid; i < n; i += blockDim.x) col[i] = ra[(size_t)i * wc + kl];
-    __syncthreads();
-    // pivot: first index of the max |col[i]|, i >= k
+    cluster_wait();  // column k has been published into colbuf[k % 3]
+    const S* col = colbuf + (k % 3) * n;
     S best = S(-1);
     int bi = n;
     for (int i = k + tid; i < n; i += blockDim.x) {
@@ -115,58 +133,66 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
       redi[wid] = bi;
     }
     __syncthreads();
-    if (tid == 0) {
-      S bv = redv[0];
-      int b = redi[0];
-      for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
-        if (redv[q] > bv || (redv[q] == bv && redi[q] < b)) {
-          bv = redv[q];
-          b = redi[q];
-        }
-      piv_s = b < n ? b : k;
-    }
-    __syncthreads();
-    const int p = piv_s;
-    cluster.sync();  // everyone has read column k before the owner overwrites it
+    S bv = redv[0];
+    int p = redi[0];
+    for (int q = 1; q < 8; ++q)
+      if (redv[q] > bv || (redv[q] == bv && redi[q] < p)) {
+        bv = redv[q];
+        p = redi[q];
+      }
+    if (p >= n) p = k;
     const S pv = col[p];
+    const S ipv = pv != S(0) ? S(1) / pv : S(0);
+    const S ck = col[k], cp = col[p];  // pivot-column entries; rows k and p are interchanged below
+    // look-ahead: the owner of column k + 1 publishes its post-step-k values
+    if (k + 1 < n) {
+      const int owner1 = (k + 1) / wc, kl1 = (k + 1) - owner1 * wc;
+      if (owner1 == c) {
+        const S rk = (INV ? a[(size_t)p * wc + kl1] * ipv : a[(size_t)p * wc + kl1]);
+        for (int i = tid; i < n; i += blockDim.x) {
+          S v;
+          const int src = i == k ? p : (i == p ? k : i);
+          const S ci = i == k ? cp : (i == p ? ck : col[i]);
+          if (INV) v = i == k ? rk : a[(size_t)src * wc + kl1] - ci * rk;
+          else v = i > k ? a[(size_t)src * wc + kl1] - ci * ipv * rk : a[(size_t)src * wc + kl1];
+          S* nb = colbuf + ((k + 1) % 3) * n;
+          for (int r = 0; r < CL; ++r) cluster.map_shared_rank(nb, r)[i] = v;
+        }
+      }
+      __syncthreads();
+      cluster_arrive();  // releases the published column
+    }
     if (tid == 0) perm[k] = p;
     if (pv == S(0)) singular = true;
     ld += log(fabs((double)pv));
     if (pv < S(0)) neg ^= 1;
     if (p != k) neg ^= 1;
-    // swap rows k, p (own columns) and entries of col
-    if (p != k) {
-      for (int jl = tid; jl < wc; jl += blockDim.x) {
-        const S t = a[(size_t)k * wc + jl];
-        a[(size_t)k * wc + jl] = a[(size_t)p * wc + jl];
-        a[(size_t)p * wc + jl] = t;
-      }
+    // row interchange k <-> p of this CTA's columns; rowk = new row k (scaled for Gauss-Jordan)
+    for (int jl = tid; jl < wc; jl += blockDim.x) {
+      const S vk = a[(size_t)k * wc + jl], vp = a[(size_t)p * wc + jl];
+      a[(size_t)k * wc + jl] = vp;
+      a[(size_t)p * wc + jl] = vk;
+      rowk[jl] = INV ? vp * ipv : vp;
     }
     __syncthreads();
-    if (tid == 0 && p != k) {
-      const S t = col[k];
-      col[k] = col[p];
-      col[p] = t;
-    }
-    __syncthreads();
-    const S ipv = pv != S(0) ? S(1) / pv : S(0);
     if (INV) {
-      for (int jl = tid; jl < wc; jl += blockDim.x) rowk[jl] = a[(size_t)k * wc + jl] * ipv;
-      __syncthreads();
-      for (int e = tid; e < n * wc; e += blockDim.x) {
-        const int i = e / wc, jl = e - i * wc;
-        const bool is_k_col = (owner == c && jl == kl);
-        if (i == k) {
-          a[e] = is_k_col ? ipv : rowk[jl];
-        } else {
-          a[e] = is_k_col ? -col[i] * ipv : a[e] - col[i] * rowk[jl];
+      if (upd) {
+        const bool kcol = owner == c && tx == kl;
+        const S rj = rowk[tx];
+        for (int i = ty; i < n; i += ty_n) {
+          const S ci = i == k ? cp : (i == p ? ck : col[i]);
+          S* e = a + (size_t)i * wc + tx;
+          if (i == k) *e = kcol ? ipv : rj;
+          else *e = kcol ? -ci * ipv : *e - ci * rj;
         }
       }
     } else {
-      // LU only: trailing update of rows > k, global columns > k
-      for (int e = tid; e < n * wc; e += blockDim.x) {
-        const int i = e / wc, jl = e - i * wc;
-        if (i > k && j0 + jl > k) a[e] -= col[i] * ipv * a[(size_t)k * wc + jl];
+      if (upd && j0 + tx > k) {
+        const S rj = rowk[tx];
+        for (int i = k + 1 + ty; i < n; i += ty_n) {
+          const S ci = i == p ? ck : col[i];
+          a[(size_t)i * wc + tx] -= ci * ipv * rj;
+        }
       }
     }
     __syncthreads();
@@ -209,8 +235,13 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
 
 // Determinant Laplacian for one (walker, det, dependency m).  Jp: orbital Jacobian plane
 // [3 * positions][NDET * n]; Ainv [W][NDET][n][n]; lapA [G][NDET * n].
-// Outputs: grad [W][NDET][n][3] (+=), lap [W * NDET] (double, +=).
-constexpr int DL_CMAX = 64;
+// Outputs: grad [W][NDET][n][3], lap [W * NDET] (double, +=).
+// B = J[(i, m) rows] (3c x n) @ Ainv[:, {i}] (n x c) is computed with 2 x 4 register tiles from K-chunks
+// staged (J transposed) in shared memory; the next chunk is prefetched into registers while the current
+// one is multiplied.  The result tile reuses the staging memory.
+constexpr int DL_CMAX = 64, DL_RP = 196, DL_OC = 32;
+constexpr int DL_JPT = 3 * DL_CMAX * DL_OC / 256;  // J chunk elements per thread (24)
+constexpr int DL_APT = DL_OC * DL_CMAX / 256;      // Ainv chunk elements per thread (8)
 template <typename T>
 __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __restrict__ Jp,
                                                 const T* __restrict__ Ainv, const T* __restrict__ lapA,
@@ -225,63 +256,94 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
     if (threadIdx.x == 0) set_flag(status, FIRE_FLAG_PAIR_OVERFLOW);
     return;
   }
-  constexpr int OC = 32;
-  T* Bm = reinterpret_cast<T*>(dl_smem);        // [3 * cnt][cnt + 1]
-  T* Jt = Bm + 3 * DL_CMAX * (DL_CMAX + 1);      // [3 * cnt][OC + 1]
-  T* At = Jt + 3 * DL_CMAX * (OC + 1);           // [OC][cnt + 1]
-  __shared__ int qs[DL_CMAX], is[DL_CMAX];
+  T* Jt = reinterpret_cast<T*>(dl_smem);  // [DL_OC][DL_RP]   J chunk, transposed
+  T* At = Jt + DL_OC * DL_RP;             // [DL_OC][DL_CMAX] Ainv chunk
+  T* Bm = reinterpret_cast<T*>(dl_smem);  // [3 * DL_CMAX][DL_CMAX + 1] after the main loop
+  __shared__ long qrow[3 * DL_CMAX];      // J plane row of local row rr
+  __shared__ int is[DL_CMAX];
   const int tid = threadIdx.x;
   const int off = L.pos_off[w];
   const int s0 = off + rp[m] + m;
+  const long ldj = (long)NDET * n;
   for (int k = tid; k < cnt; k += blockDim.x) {
     const int q = L.dep_pos[s0 + k];
-    qs[k] = q;
     is[k] = L.pos_ctr[q] - w * n;
+    for (int t = 0; t < 3; ++t) qrow[3 * k + t] = (3L * q + t) * ldj + (long)d * n;
   }
   __syncthreads();
-  const int nel = 3 * cnt * cnt;
-  constexpr int MAXE = 3 * DL_CMAX * DL_CMAX / 256;
-  T acc[MAXE];
+  const int R = 3 * cnt;
+  const int rt = (R + 1) / 2, ct = (cnt + 3) / 4, ntile = rt * ct;
+  constexpr int MAXT = (3 * DL_CMAX / 2) * (DL_CMAX / 4) / 256;  // 6
+  T acc[MAXT][8];
 #pragma unroll
-  for (int u = 0; u < MAXE; ++u) acc[u] = T(0);
+  for (int u = 0; u < MAXT; ++u)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[u][e] = T(0);
   const T* Ai = Ainv + ((size_t)w * NDET + d) * n * n;
-  const long ldj = (long)NDET * n;
-  for (int o0 = 0; o0 < n; o0 += OC) {
-    const int oc = min(OC, n - o0);
-    for (int e = tid; e < 3 * cnt * OC; e += blockDim.x) {
-      const int rr = e / OC, o = e - rr * OC;
-      const int k = rr / 3, t = rr - 3 * k;
-      Jt[rr * (OC + 1) + o] = o < oc ? Jp[(3L * qs[k] + t) * ldj + (long)d * n + o0 + o] : T(0);
-    }
-    for (int e = tid; e < OC * cnt; e += blockDim.x) {
-      const int o = e / cnt, k = e - o * cnt;
-      At[o * (DL_CMAX + 1) + k] = o < oc ? Ai[(size_t)(o0 + o) * n + is[k]] : T(0);
-    }
-    __syncthreads();
+  T jr[DL_JPT], ar[DL_APT];
+  auto fetch = [&](int o0) {
 #pragma unroll
-    for (int u = 0; u < MAXE; ++u) {
-      const int e = tid + u * 256;
-      if (e < nel) {
-        const int rr = e / cnt, k2 = e - rr * cnt;
-        T s = T(0);
+    for (int u = 0; u < DL_JPT; ++u) {
+      const int e = tid + 256 * u;
+      const int rr = e / DL_OC, o = e - rr * DL_OC;
+      jr[u] = (rr < R && o0 + o < n) ? Jp[qrow[rr] + o0 + o] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < DL_APT; ++u) {
+      const int e = tid + 256 * u;
+      const int o = e / DL_CMAX, k = e - o * DL_CMAX;
+      ar[u] = (k < cnt && o0 + o < n) ? Ai[(size_t)(o0 + o) * n + is[k]] : T(0);
+    }
+  };
+  fetch(0);
+  for (int o0 = 0; o0 < n; o0 += DL_OC) {
+#pragma unroll
+    for (int u = 0; u < DL_JPT; ++u) {
+      const int e = tid + 256 * u;
+      const int rr = e / DL_OC, o = e - rr * DL_OC;
+      Jt[o * DL_RP + rr] = jr[u];
+    }
+#pragma unroll
+    for (int u = 0; u < DL_APT; ++u) At[tid + 256 * u] = ar[u];
+    __syncthreads();
+    if (o0 + DL_OC < n) fetch(o0 + DL_OC);
+#pragma unroll
+    for (int u = 0; u < MAXT; ++u) {
+      const int tile = tid + u * 256;
+      if (tile < ntile) {
+        const int r0 = (tile / ct) * 2, c0 = (tile % ct) * 4;
 #pragma unroll 8
-        for (int o = 0; o < OC; ++o) s += Jt[rr * (OC + 1) + o] * At[o * (DL_CMAX + 1) + k2];
-        acc[u] += s;
+        for (int o = 0; o < DL_OC; ++o) {
+          const T a0 = Jt[o * DL_RP + r0], a1 = Jt[o * DL_RP + r0 + 1];
+          T b[4];
+#pragma unroll
+          for (int y = 0; y < 4; ++y) b[y] = At[o * DL_CMAX + c0 + y];
+#pragma unroll
+          for (int y = 0; y < 4; ++y) {
+            acc[u][y] += a0 * b[y];
+            acc[u][4 + y] += a1 * b[y];
+          }
+        }
       }
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int u = 0; u < MAXE; ++u) {
-    const int e = tid + u * 256;
-    if (e < nel) {
-      const int rr = e / cnt, k2 = e - rr * cnt;
-      Bm[rr * (DL_CMAX + 1) + k2] = acc[u];
+  for (int u = 0; u < MAXT; ++u) {
+    const int tile = tid + u * 256;
+    if (tile < ntile) {
+      const int r0 = (tile / ct) * 2, c0 = (tile % ct) * 4;
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y)
+          if (r0 + x < R && c0 + y < cnt) Bm[(r0 + x) * (DL_CMAX + 1) + c0 + y] = acc[u][4 * x + y];
     }
   }
   __syncthreads();
-  // gradient: sum_k B[(k, t)][k];  triplet term: sum_t sum_{k, k2} B[(k,t)][k2] * B[(k2,t)][k]
+  // triplet term: sum_t sum_{k, k2} B[(k, t)][k2] * B[(k2, t)][k];  gradient: sum_k B[(k, t)][k]
   double tl = 0.0;
+  const int nel = R * cnt;
   for (int e = tid; e < nel; e += blockDim.x) {
     const int rr = e / cnt, k2 = e - rr * cnt;
     const int k = rr / 3, t = rr - 3 * k;
@@ -297,9 +359,9 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
   if ((tid & 31) == 0) rs[tid >> 5] = v;
   __syncthreads();
   if (tid == 0) {
-    double s = 0.0;
-    for (int q = 0; q < 8; ++q) s += rs[q];
-    atomicAdd(&lap[w * NDET + d], s);
+    double sum = 0.0;
+    for (int q = 0; q < 8; ++q) sum += rs[q];
+    atomicAdd(&lap[w * NDET + d], sum);
   }
   if (tid < 3) {
     T gsum = T(0);
