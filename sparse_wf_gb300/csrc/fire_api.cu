@@ -791,8 +791,12 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   stage_update<T, 3>(c);
   stage_orbitals<T, 3>(c);
   {
+    // orbital-matrix inverse: native FP64 in the FP64 build, double-FP32 (48-bit significand) otherwise
     Prof pr("gauss_jordan", c.s);
-    launch_gj<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+    if constexpr (sizeof(T) == 8)
+      launch_gj<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+    else
+      launch_gj<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
   }
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {

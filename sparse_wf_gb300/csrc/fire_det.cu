@@ -5,7 +5,8 @@
 //               nucleus, determinant and envelope (EfficientIsotropicEnvelopes, envelopes.py:55-82);
 //               a GEMM with pi then gives the envelope carrier [x, jac(3), lap] per orbital.
 //  k_gauss_jordan  sign/log|det| and (optionally) the inverse of every orbital matrix, computed
-//               in FP64 by a thread-block cluster: the n x n matrix is split by columns over the
+//               in double precision (native FP64 in the FP64 build, double-FP32 "df64" with a 48-bit
+//               significand in the FP32 and mixed paths, fire_df64.cuh) by a thread-block cluster: the n x n matrix is split by columns over the
 //               cluster's CTAs and stays in their shared memory; the pivot column is read through
 //               distributed shared memory.  Partial pivoting like jax.lax.linalg.lu, sign/log|det|
 //               as slogdet_from_lu (model/utils.py:153-161), inverse as get_inverse_from_lu (144-150).
@@ -16,6 +17,7 @@
 //               accumulated row by row.
 #include <cooperative_groups.h>
 
+#include "fire_df64.cuh"
 #include "fire_internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
     S best = S(-1);
     int bi = n;
     for (int i = k + tid; i < n; i += blockDim.x) {
-      const S v = fabs(col[i]);
+      const S v = absv(col[i]);
       if (v > best) {
         best = v;
         bi = i;
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const S ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const S ov = shfl_xor_any(best, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
       if (ov > best || (ov == best && oi < bi)) {
         best = ov;
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
     }
     if (tid == 0) perm[k] = p;
     if (pv == S(0)) singular = true;
-    ld += log(fabs((double)pv));
+    ld += ::log(::fabs((double)pv));
     if (pv < S(0)) neg ^= 1;
     if (p != k) neg ^= 1;
     // row interchange k <-> p of this CTA's columns; rowk = new row k (scaled for Gauss-Jordan)
@@ -384,6 +386,10 @@ template __global__ void k_gauss_jordan<double, float, float, false>(const float
                                                                      float*, int32_t*);
 template __global__ void k_gauss_jordan<float, float, float, false>(const float*, int, int, double*, double*,
                                                                     float*, int32_t*);
+template __global__ void k_gauss_jordan<df64, float, float, true>(const float*, int, int, double*, double*, float*,
+                                                                  int32_t*);
+template __global__ void k_gauss_jordan<df64, float, float, false>(const float*, int, int, double*, double*, float*,
+                                                                   int32_t*);
 template __global__ void k_gauss_jordan<double, double, double, true>(const double*, int, int, double*,
                                                                       double*, double*, int32_t*);
 template __global__ void k_gauss_jordan<double, double, double, false>(const double*, int, int, double*,

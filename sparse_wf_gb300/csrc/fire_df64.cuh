@@ -1,0 +1,93 @@
+// fire_df64.cuh -- double-FP32 ("df64") arithmetic for the orbital-matrix elimination.
+//
+// A df64 number is an unevaluated sum hi + lo of two floats with |lo| <= ulp(hi)/2, giving a 48-bit
+// significand (relative rounding ~2^-48) with FP32's exponent range.  The operations are the classical
+// error-free transformations: Knuth's TwoSum, and TwoProd via a fused multiply-add (Dekker's product
+// with FMA), followed by renormalisation (Dekker 1971; Hida, Li & Bailey, "Library for double-double
+// and quad-double arithmetic", 2001).  On GB300 the FP32 pipes execute ~10x more df64 updates per cycle
+// than the FP64 pipe executes double FMAs, so the FP32 and mixed paths eliminate in df64 while the FP64
+// validation build uses native doubles.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fire {
+
+struct df64 {
+  float hi, lo;
+  __device__ __forceinline__ df64() {}
+  __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
+  __device__ __forceinline__ explicit df64(double d) {
+    hi = __double2float_rn(d);
+    lo = __double2float_rn(d - (double)hi);
+  }
+  __device__ __forceinline__ explicit df64(int v) : hi((float)v), lo(0.f) {}
+  __device__ __forceinline__ explicit df64(float v) : hi(v), lo(0.f) {}
+  __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ explicit operator float() const { return hi + lo; }
+};
+
+__device__ __forceinline__ df64 df_quick_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df64(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df64 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+  return df64(s, e);
+}
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  df64 s = df_two_sum(a.hi, b.hi);
+  const df64 t = df_two_sum(a.lo, b.lo);
+  s.lo = __fadd_rn(s.lo, t.hi);
+  s = df_quick_two_sum(s.hi, s.lo);
+  s.lo = __fadd_rn(s.lo, t.lo);
+  return df_quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);  // exact low part of a.hi * b.hi
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_quick_two_sum(p, e);
+}
+__device__ __forceinline__ df64 operator/(df64 a, df64 b) {
+  // q1 = a / b in float, one correction step with the df64 residual a - q1 b, then a second one
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  df64 r = a - b * df64(q1, 0.f);
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  r = r - b * df64(q2, 0.f);
+  const float q3 = __fdiv_rn(r.hi, b.hi);
+  df64 q = df_quick_two_sum(q1, q2);
+  return q + df64(q3, 0.f);
+}
+__device__ __forceinline__ bool operator==(df64 a, df64 b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator!=(df64 a, df64 b) { return !(a == b); }
+__device__ __forceinline__ bool operator<(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(df64 a, df64 b) { return b < a; }
+// |v| for double, float and df64 values
+template <typename S>
+__device__ __forceinline__ S absv(S v) {
+  return ::fabs(v);
+}
+template <>
+__device__ __forceinline__ df64 absv<df64>(df64 a) {
+  return a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f) ? -a : a;
+}
+__device__ __forceinline__ df64& operator-=(df64& a, df64 b) {
+  a = a - b;
+  return a;
+}
+// warp butterfly exchange for double, float and df64 values
+template <typename S>
+__device__ __forceinline__ S shfl_xor_any(S v, int o) {
+  return ::__shfl_xor_sync(0xffffffffu, v, o);
+}
+template <>
+__device__ __forceinline__ df64 shfl_xor_any<df64>(df64 v, int o) {
+  return df64(::__shfl_xor_sync(0xffffffffu, v.hi, o), ::__shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+
+}  // namespace fire

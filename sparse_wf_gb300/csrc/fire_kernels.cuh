@@ -3,6 +3,7 @@
 // header: a translation unit that sees these declarations before its own template definitions gets
 // launch stubs without device code ("invalid device function").
 #pragma once
+#include "fire_df64.cuh"
 #include "fire_internal.cuh"
 
 namespace fire {
