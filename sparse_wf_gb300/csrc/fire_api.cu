@@ -619,7 +619,7 @@ int gj_cluster(int n, size_t es, size_t* smem_out) {
       const int CL = cls[k];
       const size_t wc = (n + CL - 1) / CL;
       const size_t sm = (size_t)n * wc * es + 3 * (size_t)n * es + wc * es + 2 * (size_t)n * 4 + 64;
-      if (sm <= limits[pass] && wc <= 256) {
+      if (sm <= limits[pass] && wc <= 1024) {
         *smem_out = sm;
         return CL;
       }
@@ -643,7 +643,7 @@ cudaError_t launch_gj(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(CL, c.Wc * NDET, 1);
-  cfg.blockDim = dim3(256, 1, 1);
+  cfg.blockDim = dim3(1024, 1, 1);  // one CTA per SM: the elimination step is latency-bound
   cfg.dynamicSmemBytes = smem;
   cfg.stream = c.s;
   cudaLaunchAttribute attr[1];
@@ -653,6 +653,16 @@ cudaError_t launch_gj(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (std::getenv("FIRE_DEBUG")) {
+    static bool once = false;
+    if (!once) {
+      once = true;
+      int clusters = 0;
+      cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg);
+      std::fprintf(stderr, "[fire] gauss_jordan: n=%d cluster=%d smem=%zu threads=%d max active clusters=%d\n", n, CL,
+                   smem, (int)cfg.blockDim.x, clusters);
+    }
+  }
   g_nlaunch++;
   return cudaLaunchKernelEx(&cfg, kern, A, n, CL, c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
                             Ainv, c.status);

@@ -58,7 +58,7 @@ __global__ void k_env_coef(const T* __restrict__ r, const float* __restrict__ R,
 }
 
 // Gauss-Jordan inversion / LU with partial pivoting.  grid = (CL, matrices), cluster = (CL, 1, 1),
-// 256 threads; thread (tx, ty) = (tid % wc, tid / wc) owns column tx of this CTA's slice and rows
+// 1024 threads (many warps hide the dependent double-FP32 operation chains); thread (tx, ty) = (tid % wc, tid / wc) owns column tx of this CTA's slice and rows
 // ty, ty + ty_n, ...
 // Look-ahead: during step k the CTA that owns column k + 1 computes that column's post-step values first
 // and writes them into every CTA's colbuf[(k + 1) % 3] (distributed shared memory), then all threads
@@ -71,8 +71,9 @@ __global__ void k_env_coef(const T* __restrict__ r, const float* __restrict__ R,
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
+constexpr int GJ_THREADS = 1024;
 template <typename S, typename TI, typename TO, bool INV>
-__global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, int n, int CL,
+__global__ void __launch_bounds__(GJ_THREADS, 1) k_gauss_jordan(const TI* __restrict__ A, int n, int CL,
                                                       double* __restrict__ logdet, double* __restrict__ sign,
                                                       TO* __restrict__ Ainv, int32_t* status) {
   extern __shared__ __align__(16) unsigned char gj_smem[];
@@ -86,10 +87,10 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
   S* colbuf = a + (size_t)n * wc;        // [3][n] pivot columns (published by their owner)
   S* rowk = colbuf + 3 * n;              // [wc]
   int* perm = reinterpret_cast<int*>(rowk + wc);  // [n] (+ [n] scratch)
-  __shared__ S redv[8];
-  __shared__ int redi[8];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int ty_n = max(1, 256 / wc);
+  __shared__ S redv[32];
+  __shared__ int redi[32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarp = blockDim.x >> 5;
+  const int ty_n = max(1, (int)blockDim.x / wc);
   const int tx = tid % wc, ty = tid / wc;
   const bool upd = ty < ty_n && tx < jn;
   for (int e = tid; e < n * wc; e += blockDim.x) {
@@ -135,13 +136,18 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
       redi[wid] = bi;
     }
     __syncthreads();
-    S bv = redv[0];
-    int p = redi[0];
-    for (int q = 1; q < 8; ++q)
-      if (redv[q] > bv || (redv[q] == bv && redi[q] < p)) {
-        bv = redv[q];
-        p = redi[q];
+    // every warp reduces the per-warp candidates itself (no second barrier)
+    S bv = lane < nwarp ? redv[lane] : S(-1);
+    int p = lane < nwarp ? redi[lane] : n;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const S ov = shfl_xor_any(bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, p, o);
+      if (ov > bv || (ov == bv && oi < p)) {
+        bv = ov;
+        p = oi;
       }
+    }
     if (p >= n) p = k;
     const S pv = col[p];
     const S ipv = pv != S(0) ? S(1) / pv : S(0);
@@ -164,11 +170,13 @@ __global__ void __launch_bounds__(256) k_gauss_jordan(const TI* __restrict__ A, 
       __syncthreads();
       cluster_arrive();  // releases the published column
     }
-    if (tid == 0) perm[k] = p;
-    if (pv == S(0)) singular = true;
-    ld += ::log(::fabs((double)pv));
-    if (pv < S(0)) neg ^= 1;
-    if (p != k) neg ^= 1;
+    if (tid == 0) {  // one thread keeps the permutation, sign and log|det|
+      perm[k] = p;
+      if (pv == S(0)) singular = true;
+      ld += ::log(::fabs((double)pv));
+      if (pv < S(0)) neg ^= 1;
+      if (p != k) neg ^= 1;
+    }
     // row interchange k <-> p of this CTA's columns; rowk = new row k (scaled for Gauss-Jordan)
     for (int jl = tid; jl < wc; jl += blockDim.x) {
       const S vk = a[(size_t)k * wc + jl], vp = a[(size_t)p * wc + jl];
