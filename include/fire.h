@@ -140,6 +140,20 @@ fire_status fire_triplets(void* stream, const fire_problem* prob, const void* r,
                           int32_t* trip_in, int32_t* trip_k, int32_t* trip_kn, int32_t* trip_i,
                           void* workspace, size_t workspace_bytes, int32_t* status);
 
+/* Same outputs as fire_triplets, with no workspace argument and no allocation: the intermediate
+ * neighbour structure lives in a static device array of FIRE_TRIPLETS_STATIC_MAX_WORDS int32 words
+ * (16 MiB) per device.  No counterpart in the reference.  It serves callers that cannot allocate or
+ * pass device scratch (a handler inside another runtime's executable, a host program without a memory
+ * pool).  Needs n_walkers * (2 * n_el + 1 + 2 * cap_pairs) <= FIRE_TRIPLETS_STATIC_MAX_WORDS, else
+ * FIRE_ERR_UNSUPPORTED before any CUDA call.  The first call on a device (that device current) looks
+ * the array up with cudaGetSymbolAddress; make it before any stream capture.  The stream must belong
+ * to the current device.  Calls that can overlap on one device (other streams, other host threads)
+ * race on the shared array; calls ordered on one stream do not. */
+#define FIRE_TRIPLETS_STATIC_MAX_WORDS (4 * 1024 * 1024)
+fire_status fire_triplets_static(void* stream, const fire_problem* prob, const void* r, int32_t cap_triplets,
+                                 int32_t* trip_in, int32_t* trip_k, int32_t* trip_kn, int32_t* trip_i,
+                                 int32_t* status);
+
 /* ---- wavefunction ----------------------------------------------------------------------------- */
 /* sign, logpsi: [B] in the walkers' dtype */
 fire_status fire_logpsi(void* stream, const fire_problem* prob, const float* R, const float* Z,

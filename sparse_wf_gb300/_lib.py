@@ -20,6 +20,7 @@ FLAG_NONFINITE = 4
 FLAG_TRIPLET_OVERFLOW = 8
 FLAG_SINGULAR = 16
 FLAG_TIMEOUT = 32
+TRIPLETS_STATIC_MAX_WORDS = 4 * 1024 * 1024  # FIRE_TRIPLETS_STATIC_MAX_WORDS
 ERRORS = {1: "invalid argument", 2: "unsupported size", 3: "workspace too small", 4: "CUDA launch failed"}
 
 # exported entry points, in header order
@@ -27,7 +28,7 @@ SYMBOLS = [
     "fire_abi_version", "fire_param_layout", "fire_prepared_size", "fire_workspace_size",
     "fire_prepare_params", "fire_neighbors", "fire_triplets", "fire_logpsi", "fire_local_energy",
     "fire_embedding", "fire_mcmc_block", "fire_potential_energy", "fire_profile_enable", "fire_profile_report",
-    "fire_gemm_mixed",
+    "fire_gemm_mixed", "fire_triplets_static",
 ]
 
 
@@ -78,6 +79,7 @@ def load() -> C.CDLL:
         "fire_profile_enable": ([i32], i32),
         "fire_profile_report": ([C.c_char_p, sz], i32),
         "fire_gemm_mixed": ([vp, i32, i32, i32, vp, vp, vp, vp, sz, vp], i32),
+        "fire_triplets_static": ([vp, P, vp, i32, vp, vp, vp, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -1,7 +1,8 @@
 // fire_kernels.cuh -- declarations of the kernels defined (and explicitly instantiated) in the
-// stage translation units, so that fire_api.cu can launch them.  Only fire_api.cu includes this
-// header: a translation unit that sees these declarations before its own template definitions gets
-// launch stubs without device code ("invalid device function").
+// stage translation units, so that the entry-point files (fire_api.cu, fire_triplets_static.cu) can
+// launch them.  Only translation units that define none of these kernels include this header: one that
+// sees these declarations before its own template definitions gets launch stubs without device code
+// ("invalid device function").
 #pragma once
 #include "fire_df64.cuh"
 #include "fire_internal.cuh"
