@@ -2,16 +2,20 @@
 """Benchmark of the FiRE local-energy hot path: walker E_loc evaluations per second.
 
 Workload (default): all-trans C40H82 (322 electrons, 122 nuclei), 2048 walkers drawn around the nuclei
-(sigma = 1 bohr), random-init default-architecture parameters (seed 0), e-e cutoff 5 bohr.  One step
-= one local-energy evaluation (sparse forward Laplacian + Coulomb potential) of every walker.
-Synthetic data: there is no dataset; molecules, walkers and parameters are generated here.
+(sigma = 1 bohr), random-init default-architecture parameters (seed 0), e-e cutoff 5 bohr.  The walkers
+first go through a 20-step all-electron Metropolis block (Gaussian proposals, width 0.1 bohr; one
+untimed and one timed block); then one step = one local-energy evaluation (sparse forward Laplacian +
+Coulomb potential) of every walker.  Synthetic data: there is no dataset; molecules, walkers and
+parameters are generated here.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|mixed] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp32] [--impl reference]
 
-Prints one JSON line (rank 0).  `value` is device-resident throughput (inputs already in HBM), `e2e`
-the same metric through the public API with the walkers copied from pinned host memory and E_loc
-copied back inside the timed region.  `--impl reference` times the CPU oracle port of the reference
-algorithm (numpy, FP64, all host threads) on a bounded sample of the same workload.
+Prints one JSON line (rank 0).  `value` is the headline path's device-resident throughput (inputs
+already in HBM; default the mixed path), `e2e` the same metric through the public API with the walkers
+copied from pinned host memory and E_loc copied back inside the timed region.  `fp32_path` times the
+plain FP32 path on the same walkers the same way; `accuracy` compares both with the FP64 build on a
+sample of the walkers.  `--impl reference` times the CPU oracle port of the reference algorithm
+(numpy, FP64, all host threads) on a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -39,11 +43,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"], help="the timed (headline) path")
     ap.add_argument("--system", default="c40h82", choices=list(SYSTEMS))
     ap.add_argument("--walkers", type=int, default=2048)
     ap.add_argument("--chunk", type=int, default=0, help="walkers per internal pass (0: from --ws-gb)")
     ap.add_argument("--ws-gb", type=float, default=48.0, help="workspace budget in GB")
+    ap.add_argument("--mcmc-steps", type=int, default=20, help="Metropolis steps before the E_loc evaluation")
+    ap.add_argument("--mcmc-width", type=float, default=0.1)
+    ap.add_argument("--acc-walkers", type=int, default=256, help="walkers checked against the FP64 build")
+    ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
     ap.add_argument("--cpu-sample", type=int, default=2, help="walkers in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -174,6 +182,67 @@ def run_reference(args):
     }))
 
 
+def energy_error(e_path, e_ref):
+    """Per-walker and mean-energy differences (mHa) of two E_loc arrays of the same walkers; the clipped
+    mean is the one the reference's optimizer uses (median +- 5 mean-absolute-deviations,
+    update.py:45-62, 158-160; clip_local_energy 5.0, default.yaml:137-139)."""
+    import numpy as np
+
+    def clipped_mean(e):
+        c = np.median(e)
+        mad = np.mean(np.abs(e - c))
+        return float(np.clip(e, c - 5 * mad, c + 5 * mad).mean())
+
+    d = np.abs(e_path - e_ref) * 1e3
+    return {"max_abs_mHa": float(d.max()), "median_abs_mHa": float(np.median(d)),
+            "mean_energy_err_mHa": float(abs(e_path.mean() - e_ref.mean()) * 1e3),
+            "clipped_mean_energy_err_mHa": float(abs(clipped_mean(e_path) - clipped_mean(e_ref)) * 1e3)}
+
+
+def choose_chunk(wf, B, static, ws_gb):
+    """The largest walker chunk whose workspace fits the budget."""
+    import ctypes as C
+
+    from sparse_wf_gb300 import _lib
+
+    lo, hi = 1, B
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        prob = wf._problem(B, static)
+        nb = C.c_size_t()
+        _lib.check(_lib.load().fire_workspace_size(C.byref(prob), mid, C.byref(nb)), "fire_workspace_size")
+        if nb.value <= ws_gb * 1e9:
+            lo = mid
+        else:
+            hi = mid - 1
+    return lo
+
+
+def time_steps(step, n, stream, dist, world):
+    """Device time (ms) of one step averaged over n steps, bracketed by barriers and synchronizes; max over
+    ranks."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    out = None
+    for _ in range(n):
+        out = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1) / n
+    if world > 1:
+        t = torch.tensor([ms], device=stream.device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -185,7 +254,7 @@ def main():
     from sparse_wf_gb300 import _lib, systems
     from sparse_wf_gb300.build import build
     from sparse_wf_gb300.distributed import shard
-    from sparse_wf_gb300.wavefunction import FireWaveFunction, StaticArgs
+    from sparse_wf_gb300.wavefunction import FireWaveFunction
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -203,30 +272,34 @@ def main():
     n_up, _ = systems.spin_counts(mol)
     r_all = systems.init_electrons(mol, args.walkers * world, 1000)  # weak scaling: walkers per GPU fixed
     a, b = shard(len(r_all), rank, world)
-    r_np = r_all[a:b]
-    B = len(r_np)
+    B = b - a
     wf = FireWaveFunction(mol, precision=args.precision, device=dev)
     params = wf.init(0, r_all[:1])
     dp = wf._params(params)
-    r_dev = torch.from_numpy(r_np).to(dev)
+    r_dev = torch.from_numpy(r_all[a:b]).to(dev)
     static = wf.get_static_input(r_dev).round_with_padding(1.1, mol.n_el, n_up, mol.n_nuc)
-    # workspace: the largest chunk within the budget
-    if args.chunk > 0:
-        wf.chunk_walkers = args.chunk
-    else:
-        import ctypes as C
+    wf.chunk_walkers = args.chunk if args.chunk > 0 else choose_chunk(wf, B, static, args.ws_gb)
+    stream = torch.cuda.current_stream(dev)
 
-        lo, hi = 1, B
-        while lo < hi:
-            mid = (lo + hi + 1) // 2
-            prob = wf._problem(B, static)
-            nb = C.c_size_t()
-            _lib.load().fire_workspace_size(C.byref(prob), mid, C.byref(nb))
-            if nb.value <= args.ws_gb * 1e9:
-                lo = mid
-            else:
-                hi = mid - 1
-        wf.chunk_walkers = lo
+    # Metropolis block (all-electron Gaussian proposals) that moves the walkers before the E_loc steps:
+    # one untimed block, then one timed block
+    mcmc = None
+    if args.mcmc_steps > 0:
+        _, logpsi = wf.signed(dp, r_dev, static)
+        wf.mcmc_block(dp, r_dev, logpsi, static, args.mcmc_steps, args.mcmc_width, seed=1000 + rank, counter=0)
+        blk = {}
+
+        def block():
+            blk["acc"], blk["smax"] = wf.mcmc_block(dp, r_dev, logpsi, static, args.mcmc_steps, args.mcmc_width,
+                                                    seed=1000 + rank, counter=1)
+
+        ms_block, _ = time_steps(block, 1, stream, dist, world)
+        acc = float(blk["acc"].float().mean().item()) / args.mcmc_steps
+        mcmc = {"steps": args.mcmc_steps, "width_bohr": args.mcmc_width, "ms_per_block": ms_block,
+                "walker_steps_per_s": B * world * args.mcmc_steps / (ms_block / 1e3), "acceptance": acc,
+                "precision": args.precision}
+        static = wf.get_static_input(r_dev).round_with_padding(1.1, mol.n_el, n_up, mol.n_nuc)
+    r_np = r_dev.cpu().numpy()
 
     def step():
         return wf.local_energy_full(dp, r_dev, static)
@@ -234,25 +307,8 @@ def main():
     for _ in range(args.warmup):
         eloc, aux = step()
         static = aux["static"]
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            eloc, aux = step()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms, (eloc, aux) = time_steps(step, args.steps, stream, dist, world)
     total_walkers = args.walkers * world
     value = total_walkers / (ms / 1e3)
 
@@ -270,8 +326,8 @@ def main():
     achieved = flops / (g_ms / 1e3) / 1e12
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / peaks["bf16_tflops"], "traffic": None,
-                "kernel": "k_gemm (all dense contractions of one step)", "launches": g_launches,
-                "avg_launch_ms": g_ms / max(g_launches, 1), "peak_source": f"bf16 dense, {peak_kind}",
+                "kernel": "all dense contractions of one step (k_gemm_tcp + k_gemm)", "launches": g_launches,
+                "avg_launch_ms": g_ms / max(g_launches, 1), "peak_source": f"bf16 dense burst, {peak_kind}",
                 "flops_per_step": flops}
     stages = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items() if k != "kernels_launched"}
 
@@ -280,25 +336,60 @@ def main():
     if not args.no_e2e:
         r_host = torch.from_numpy(r_np).pin_memory()
         e_host = torch.empty(B, dtype=torch.float32).pin_memory()
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        t0 = time.perf_counter()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for _ in range(args.steps):
+
+        def e2e_step():
             r_dev.copy_(r_host, non_blocking=True)
-            eloc, aux = step()
-            e_host.copy_(eloc, non_blocking=True)
-        f1.record(stream)
-        torch.cuda.synchronize()
-        ms_e2e = max(f0.elapsed_time(f1), (time.perf_counter() - t0) * 1e3) / args.steps
-        if world > 1:
-            t = torch.tensor([ms_e2e], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms_e2e = float(t.item())
+            e, _ = step()
+            e_host.copy_(e, non_blocking=True)
+
+        t0 = time.perf_counter()
+        ms_e2e, _ = time_steps(e2e_step, args.steps, stream, dist, world)
+        ms_e2e = max(ms_e2e, (time.perf_counter() - t0) * 1e3 / args.steps)
         e2e = {"value": total_walkers / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(r_host.numel() * 4),
                "d2h_bytes_per_step": int(e_host.numel() * 4)}
+
+    # accuracy against the FP64 build of the same kernels (which matches the oracle to 1e-10) on the
+    # same walkers and parameters
+    accuracy = None
+    e_path = {args.precision: eloc.double().cpu().numpy()}
+    K = min(args.acc_walkers, B)
+    e64 = None
+    if K > 0:
+        wf._ws = None
+        torch.cuda.empty_cache()
+        wf64 = FireWaveFunction(mol, precision="fp64", device=dev)
+        wf64.chunk_walkers = min(K, 64)
+        r64 = r_dev[:K].double()
+        st64 = wf64.get_static_input(r64).round_with_padding(1.1, mol.n_el, n_up, mol.n_nuc)
+        e64 = wf64.local_energy_full(params, r64, st64)[0].cpu().numpy()
+        del wf64
+        torch.cuda.empty_cache()
+
+    # the plain FP32 path on the same walkers, timed the same way
+    fp32 = None
+    if args.precision == "mixed" and not args.no_compare:
+        wf._ws = None
+        torch.cuda.empty_cache()
+        wf32 = FireWaveFunction(mol, precision="fp32", device=dev)
+        wf32.chunk_walkers = wf.chunk_walkers
+        dp32 = wf32._params(params)
+        st32 = static
+
+        def step32():
+            return wf32.local_energy_full(dp32, r_dev, st32)
+
+        for _ in range(args.warmup):
+            e32, aux32 = step32()
+            st32 = aux32["static"]
+        ms32, (e32, _) = time_steps(step32, args.steps, stream, dist, world)
+        e_path["fp32"] = e32.double().cpu().numpy()
+        fp32 = {"value": total_walkers / (ms32 / 1e3), "unit": UNIT, "ms_per_step": ms32,
+                "chunk_walkers": wf32.chunk_walkers}
+        del wf32
+        torch.cuda.empty_cache()
+    if e64 is not None:
+        accuracy = {"walkers": K, "reference": "FP64 build of the same kernels (FP64 oracle to <= 1e-10)"}
+        accuracy.update({k: energy_error(v[:K], e64) for k, v in e_path.items()})
 
     # CPU baseline + oracle check on the same walkers (rank 0)
     cpu = None
@@ -307,9 +398,9 @@ def main():
         rate, e_ref, dt = cpu_baseline(mol, r_np, params, n_up, args.cpu_sample)
         cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                "sample": f"{args.cpu_sample} of {B} {mol.name} walkers, numpy FP64 oracle, {dt:.1f} s"}
-        got = eloc[: args.cpu_sample].double().cpu().numpy()
+        got = e_path[args.precision][: args.cpu_sample]
         check = {"walkers": args.cpu_sample, "max_abs_err_mHa": float(np.abs(got - e_ref).max() * 1e3),
-                 "mean_err_mHa": float(abs(got.mean() - e_ref.mean()) * 1e3), "reference": "FP64 oracle"}
+                 "reference": "FP64 oracle"}
 
     if rank == 0:
         st = aux["stats"].cpu().numpy()
@@ -318,15 +409,18 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16/f32",
             "data": "synthetic",
-            "config": {"workload": f"{mol.name} all-trans, {args.walkers} walkers per GPU, local energy "
-                                   f"(sparse forward Laplacian + Coulomb)", "n_el": mol.n_el, "n_nuc": mol.n_nuc,
-                       "walkers_per_gpu": args.walkers, "precision": args.precision,
-                       "chunk_walkers": wf.chunk_walkers, "mean_pairs_per_walker": pairs,
-                       "cap_pairs": static.n_pairs, "l2": "working set of every step >> L2 (GB-scale planes)",
+            "config": {"workload": f"{mol.name} all-trans, {args.walkers} walkers per GPU after a "
+                                   f"{args.mcmc_steps}-step Metropolis block; step = local energy "
+                                   f"(sparse forward Laplacian + Coulomb) of every walker",
+                       "n_el": mol.n_el, "n_nuc": mol.n_nuc, "walkers_per_gpu": args.walkers,
+                       "precision": args.precision, "chunk_walkers": wf.chunk_walkers,
+                       "mean_pairs_per_walker": pairs, "cap_pairs": static.n_pairs,
+                       "l2": "inputs larger than L2: every step streams GB-scale planes",
                        "parallelism": f"walker shards x{world}", "E_mean": float(st[0]), "E_std": float(st[1])},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": int(prof.get("kernels_launched", (0, 0))[0]) * args.steps,
-            "stages_ms": stages, "oracle_check": check,
+            "fp32_path": fp32, "mixed_over_fp32": (value / fp32["value"]) if fp32 else None,
+            "accuracy": accuracy, "mcmc": mcmc, "stages_ms": stages, "oracle_check": check,
         }
         print(json.dumps(line))
     if world > 1:
