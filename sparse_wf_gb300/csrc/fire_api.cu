@@ -144,9 +144,9 @@ struct Plan {
   // int
   size_t deg, rowptr, nbr, rev, en_cnt, en_idx, counts, pos_off, pos_ctr, pos_dep, dep_pos;
   // T
-  size_t E5a, Z1, E5o, HX, HL, HJ, B1X, B1L, B1J, B2X, B2L, B2J, Zx, jsq;
+  size_t E5a, Z1, E5o, HX, HL, HJ, B1X, B1L, B1J, B2X, B2L, B2J, Zx, Zx2, jsq;
   size_t env, rawx, rjs, Apl, lapA, Jorb, coef_up, coef_dn, Ainv, dgrad;
-  size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, jsqr;
+  size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, Zr2, jsqr;
   size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, tile_mask;
   // double
   size_t ld, sd, dlap;
@@ -194,6 +194,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.B2L, G * F, es);
     take(P.B2J, Jr * F, es);
     take(P.jsq, G * F, es);
+    take(P.Zx2, G * F, es);
   }
   take(P.env, G * NV * DN, es);
   take(P.rawx, G * DN, es);
@@ -228,6 +229,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.R2J, W * 3 * n * F, es);
     take(P.R2L, W * F, es);
     take(P.jsqr, W * F, es);
+    take(P.Zr2, W * F, es);
     take(P.JAj, W * 3 * n * 2, es);
     take(P.JAl, W * 2, es);
     take(P.Jo2, Jr * 2, es);
@@ -527,7 +529,11 @@ cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, c
                        size_t jsq, int tc_id = -1) {
   GemmP<T> g = gp0<T>();
   g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.C = c.template buf<T>(out.X);
-  g.ldc = N; g.M = rowsX; g.N = N; g.K = K; g.aux0 = c.template buf<T>(zx); g.ld_aux = N;
+  g.ldc = N; g.M = rowsX; g.N = N; g.K = K; g.ld_aux = N;
+  if (fl) {  // silu' and silu'' planes for the Jacobian / Laplacian epilogues
+    g.aux0 = c.template buf<T>(zx);
+    g.aux2 = c.template buf<T>(c.P.Zx2);
+  }
   gemm<T, EPI_SILU_X>(c, g);
   if (!fl) return cudaPeekAtLastError();
   cudaMemsetAsync(c.template buf<T>(jsq), 0, sizeof(T) * (size_t)rowsX * N, c.s);
@@ -538,7 +544,8 @@ cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, c
   gemm<T, EPI_SILU_J>(c, g, tc_id);
   g = gp0<T>();
   g.A = c.template buf<T>(in.L); g.lda = K; g.B = Wt; g.ldb = N; g.C = c.template buf<T>(out.L); g.ldc = N;
-  g.M = rowsX; g.N = N; g.K = K; g.aux1 = c.template buf<T>(zx); g.aux3 = c.template buf<T>(jsq); g.ld_aux = N;
+  g.M = rowsX; g.N = N; g.K = K; g.aux1 = c.template buf<T>(zx); g.aux0 = c.template buf<T>(c.P.Zx2);
+  g.aux3 = c.template buf<T>(jsq); g.ld_aux = N;
   gemm<T, EPI_SILU_L>(c, g, tc_id);
   return cudaPeekAtLastError();
 }
@@ -704,7 +711,11 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
     auto dense_silu = [&](Planes in, Planes out, const T* Wt, const T* b, int K) {
       GemmP<T> q = gp0<T>();
       q.A = c.template buf<T>(in.X); q.lda = K; q.B = Wt; q.ldb = F; q.bias = b; q.C = c.template buf<T>(out.X);
-      q.ldc = F; q.M = Wc; q.N = F; q.K = K; q.aux0 = c.template buf<T>(c.P.Zr); q.ld_aux = F;
+      q.ldc = F; q.M = Wc; q.N = F; q.K = K; q.ld_aux = F;
+      if (FLM) {
+        q.aux0 = c.template buf<T>(c.P.Zr);
+        q.aux2 = c.template buf<T>(c.P.Zr2);
+      }
       gemm<T, EPI_SILU_X>(c, q);
       if (!FLM) return;
       cudaMemsetAsync(c.template buf<T>(c.P.jsqr), 0, sizeof(T) * Wc * F, c.s);
@@ -715,8 +726,8 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
       gemm<T, EPI_SILU_J>(c, q);
       q = gp0<T>();
       q.A = c.template buf<T>(in.L); q.lda = K; q.B = Wt; q.ldb = F; q.C = c.template buf<T>(out.L); q.ldc = F;
-      q.M = Wc; q.N = F; q.K = K; q.aux1 = c.template buf<T>(c.P.Zr); q.aux3 = c.template buf<T>(c.P.jsqr);
-      q.ld_aux = F;
+      q.M = Wc; q.N = F; q.K = K; q.aux1 = c.template buf<T>(c.P.Zr); q.aux0 = c.template buf<T>(c.P.Zr2);
+      q.aux3 = c.template buf<T>(c.P.jsqr); q.ld_aux = F;
       gemm<T, EPI_SILU_L>(c, q);
     };
     dense_silu(RI, R1, c.W.w[FIRE_P_ATT_OUT1_W], c.W.w[FIRE_P_ATT_OUT1_B], 2 * F);

@@ -109,6 +109,15 @@ __global__ void __launch_bounds__(GJ_THREADS, 1) k_gauss_jordan(const TI* __rest
   double ld = 0.0;
   int neg = 0;
   bool singular = false;
+  // Rows k and p of step k are not written in place during step k: their new values wait in registers
+  // (one designated thread per column, and the look-ahead threads for column k + 1) and are stored at the
+  // start of step k + 1.  Every read of those rows in step k happens before the thread's cluster arrive,
+  // and the stores come after the next cluster wait, so one cluster barrier and one CTA barrier per step
+  // order all shared-memory traffic.
+  int pk = -1, pp = -1;                 // pending rows (designated update thread, column tx)
+  S uk = S(0), up = S(0);
+  int la_row = -1, la_col = 0;          // pending look-ahead element
+  S la_val = S(0);
   for (int k = 0; k < n; ++k) {
     const int owner = k / wc, kl = k - owner * wc;
     cluster_wait();  // column k has been published into colbuf[k % 3]
@@ -121,6 +130,15 @@ __global__ void __launch_bounds__(GJ_THREADS, 1) k_gauss_jordan(const TI* __rest
         best = v;
         bi = i;
       }
+    }
+    if (pk >= 0) {  // rows k - 1 and p(k - 1) of the previous step
+      a[(size_t)pk * wc + tx] = uk;
+      if (pp != pk) a[(size_t)pp * wc + tx] = up;
+      pk = -1;
+    }
+    if (la_row >= 0) {
+      a[(size_t)la_row * wc + la_col] = la_val;
+      la_row = -1;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -151,25 +169,34 @@ __global__ void __launch_bounds__(GJ_THREADS, 1) k_gauss_jordan(const TI* __rest
     if (p >= n) p = k;
     const S pv = col[p];
     const S ipv = pv != S(0) ? S(1) / pv : S(0);
-    const S ck = col[k], cp = col[p];  // pivot-column entries; rows k and p are interchanged below
-    // look-ahead: the owner of column k + 1 publishes its post-step-k values
-    if (k + 1 < n) {
-      const int owner1 = (k + 1) / wc, kl1 = (k + 1) - owner1 * wc;
-      if (owner1 == c) {
-        const S rk = (INV ? a[(size_t)p * wc + kl1] * ipv : a[(size_t)p * wc + kl1]);
-        for (int i = tid; i < n; i += blockDim.x) {
-          S v;
-          const int src = i == k ? p : (i == p ? k : i);
-          const S ci = i == k ? cp : (i == p ? ck : col[i]);
-          if (INV) v = i == k ? rk : a[(size_t)src * wc + kl1] - ci * rk;
-          else v = i > k ? a[(size_t)src * wc + kl1] - ci * ipv * rk : a[(size_t)src * wc + kl1];
-          S* nb = colbuf + ((k + 1) % 3) * n;
-          for (int r = 0; r < CL; ++r) cluster.map_shared_rank(nb, r)[i] = v;
+    const S ck = col[k], cp = col[p];  // pivot-column entries; rows k and p are interchanged
+    // look-ahead: the owner of column k + 1 computes and publishes its post-step-k values (and keeps them)
+    const int owner1 = (k + 1) / wc, kl1 = (k + 1) - owner1 * wc;
+    const bool la = k + 1 < n && owner1 == c;
+    if (la) {
+      const S rk = (INV ? a[(size_t)p * wc + kl1] * ipv : a[(size_t)p * wc + kl1]);
+      S* nb = colbuf + ((k + 1) % 3) * n;
+      for (int i = tid; i < n; i += blockDim.x) {
+        S v;
+        const int src = i == k ? p : (i == p ? k : i);
+        const S ci = i == k ? cp : (i == p ? ck : col[i]);
+        if (INV) v = i == k ? rk : a[(size_t)src * wc + kl1] - ci * rk;
+        else v = i > k ? a[(size_t)src * wc + kl1] - ci * ipv * rk : a[(size_t)src * wc + kl1];
+        for (int r = 0; r < CL; ++r) cluster.map_shared_rank(nb, r)[i] = v;
+        if (i == k || i == p) {
+          la_row = i;
+          la_col = kl1;
+          la_val = v;
+        } else {
+          a[(size_t)i * wc + kl1] = v;
         }
       }
-      __syncthreads();
-      cluster_arrive();  // releases the published column
     }
+    // rows p and k of this thread's column, read before the arrive
+    const bool mycol = upd && !(la && tx == kl1);
+    const S vp = mycol ? a[(size_t)p * wc + tx] : S(0);
+    const S vk = (mycol && ty == 0) ? a[(size_t)k * wc + tx] : S(0);
+    if (k + 1 < n) cluster_arrive();  // releases the published column
     if (tid == 0) {  // one thread keeps the permutation, sign and log|det|
       perm[k] = p;
       if (pv == S(0)) singular = true;
@@ -177,36 +204,50 @@ __global__ void __launch_bounds__(GJ_THREADS, 1) k_gauss_jordan(const TI* __rest
       if (pv < S(0)) neg ^= 1;
       if (p != k) neg ^= 1;
     }
-    // row interchange k <-> p of this CTA's columns; rowk = new row k (scaled for Gauss-Jordan)
-    for (int jl = tid; jl < wc; jl += blockDim.x) {
-      const S vk = a[(size_t)k * wc + jl], vp = a[(size_t)p * wc + jl];
-      a[(size_t)k * wc + jl] = vp;
-      a[(size_t)p * wc + jl] = vk;
-      rowk[jl] = INV ? vp * ipv : vp;
-    }
-    __syncthreads();
-    if (INV) {
-      if (upd) {
+    if (mycol) {
+      if (INV) {
         const bool kcol = owner == c && tx == kl;
-        const S rj = rowk[tx];
+        const S rj = vp * ipv;
         for (int i = ty; i < n; i += ty_n) {
-          const S ci = i == k ? cp : (i == p ? ck : col[i]);
+          if (i == k || i == p) continue;
+          const S ci = col[i];
           S* e = a + (size_t)i * wc + tx;
-          if (i == k) *e = kcol ? ipv : rj;
-          else *e = kcol ? -ci * ipv : *e - ci * rj;
+          *e = kcol ? -ci * ipv : *e - ci * rj;
         }
-      }
-    } else {
-      if (upd && j0 + tx > k) {
-        const S rj = rowk[tx];
-        for (int i = k + 1 + ty; i < n; i += ty_n) {
-          const S ci = i == p ? ck : col[i];
-          a[(size_t)i * wc + tx] -= ci * ipv * rj;
+        if (ty == 0) {
+          uk = kcol ? ipv : rj;
+          up = kcol ? -ck * ipv : vk - ck * rj;
+          pk = k;
+          pp = p;
+        }
+      } else {
+        if (j0 + tx > k) {
+          const S rj = vp;
+          for (int i = k + 1 + ty; i < n; i += ty_n) {
+            if (i == p) continue;
+            a[(size_t)i * wc + tx] -= col[i] * ipv * rj;
+          }
+          if (ty == 0) {
+            uk = vp;
+            up = vk - ck * ipv * vp;
+            pk = k;
+            pp = p;
+          }
+        } else if (ty == 0) {  // columns left of the pivot: rows k and p are only interchanged
+          uk = vp;
+          up = vk;
+          pk = k;
+          pp = p;
         }
       }
     }
-    __syncthreads();
   }
+  if (pk >= 0) {
+    a[(size_t)pk * wc + tx] = uk;
+    if (pp != pk) a[(size_t)pp * wc + tx] = up;
+  }
+  if (la_row >= 0) a[(size_t)la_row * wc + la_col] = la_val;
+  __syncthreads();
   if (c == 0 && tid == 0) {
     logdet[mat] = ld;
     sign[mat] = neg ? -1.0 : 1.0;

@@ -62,18 +62,22 @@ __device__ __forceinline__ void gemm_store(const GemmP<T>& p, int row, int col, 
     if (p.bias && p.bias_period > 0 && (row % p.bias_period) == 0) v += p.bias[col];
     p.C[(long)row * p.ldc + col] = v;
   } else if (MODE == EPI_SILU_X) {
+    // value plane; with aux0 set it also writes silu'(z) (aux0) and silu''(z) (aux2), which the
+    // Jacobian and Laplacian epilogues of the same layer read instead of re-evaluating them per row
     T z = acc + (p.bias ? p.bias[col] : T(0));
-    p.aux0[(long)row * p.ld_aux + col] = z;
     p.C[(long)row * p.ldc + col] = silu(z);
-  } else if (MODE == EPI_SILU_J) {
+    if (p.aux0) {
+      T y, d1, d2;
+      silu3(z, y, d1, d2);
+      p.aux0[(long)row * p.ld_aux + col] = d1;
+      p.aux2[(long)row * p.ld_aux + col] = d2;
+    }
+  } else if (MODE == EPI_SILU_J) {  // aux1: silu' plane
     const int node = gemm_node(p, row);
-    T y, d1, d2;
-    silu3(p.aux1[(long)node * p.ld_aux + col], y, d1, d2);
-    p.C[(long)row * p.ldc + col] = acc * d1;
-  } else if (MODE == EPI_SILU_L) {
-    T y, d1, d2;
-    silu3(p.aux1[(long)row * p.ld_aux + col], y, d1, d2);
-    p.C[(long)row * p.ldc + col] = acc * d1 + p.aux3[(long)row * p.ld_aux + col] * d2;
+    p.C[(long)row * p.ldc + col] = acc * p.aux1[(long)node * p.ld_aux + col];
+  } else if (MODE == EPI_SILU_L) {  // aux1: silu', aux0: silu'', aux3: sum of squared Jacobian rows
+    const long o = (long)row * p.ld_aux + col;
+    p.C[(long)row * p.ldc + col] = acc * p.aux1[o] + p.aux3[o] * p.aux0[o];
   } else if (MODE == EPI_ORB_X) {
     const T* b = pass_spin == 0 ? p.bias : p.bias2;
     const T raw = acc + b[col];

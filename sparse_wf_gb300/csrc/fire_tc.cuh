@@ -110,20 +110,14 @@ __device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int no
       v.x += b.x; v.y += b.y; v.z += b.z; v.w += b.w;
     }
     st4(p.C + (long)row * p.ldc + col, v);
-  } else if (MODE == EPI_SILU_J || MODE == EPI_SILU_L) {
-    const float4 z = ld4(p.aux1 + (long)node * p.ld_aux + col);
-    const float zz[4] = {z.x, z.y, z.z, z.w};
-    float o[4];
-    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (MODE == EPI_SILU_L) q = ld4(p.aux3 + (long)row * p.ld_aux + col);
-    const float qq[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      float y, d1, d2;
-      silu3(zz[k], y, d1, d2);
-      o[k] = MODE == EPI_SILU_J ? a[k] * d1 : a[k] * d1 + qq[k] * d2;
-    }
-    st4(p.C + (long)row * p.ldc + col, make_float4(o[0], o[1], o[2], o[3]));
+  } else if (MODE == EPI_SILU_J) {  // aux1: silu' plane (per center)
+    const float4 d = ld4(p.aux1 + (long)node * p.ld_aux + col);
+    st4(p.C + (long)row * p.ldc + col, make_float4(a[0] * d.x, a[1] * d.y, a[2] * d.z, a[3] * d.w));
+  } else if (MODE == EPI_SILU_L) {  // aux1: silu', aux0: silu'', aux3: sum of squared Jacobian rows
+    const long o = (long)row * p.ld_aux + col;
+    const float4 d1 = ld4(p.aux1 + o), d2 = ld4(p.aux0 + o), q = ld4(p.aux3 + o);
+    st4(p.C + (long)row * p.ldc + col, make_float4(a[0] * d1.x + q.x * d2.x, a[1] * d1.y + q.y * d2.y,
+                                                   a[2] * d1.z + q.z * d2.z, a[3] * d1.w + q.w * d2.w));
   } else if (MODE == EPI_ORB_J) {
     const int pos = row / 3, t = row - 3 * pos;
     const float* env = p.aux1 + (long)node * 5 * p.ld_aux;
@@ -149,6 +143,67 @@ __device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int no
       v.x += 2.f * r.x * e.x; v.y += 2.f * r.y * e.y; v.z += 2.f * r.z * e.z; v.w += 2.f * r.w * e.w;
     }
     st4(p.C + (long)row * p.ldc + col, v);
+  }
+}
+
+// Epilogue of 16 consecutive columns (col0 + 15 < N) of one row: all operand loads are issued before the
+// first store so that their latencies overlap (the stores could otherwise alias later loads).
+template <int MODE>
+__device__ __forceinline__ void tc_epi16(const GemmP<float>& p, int row, int node, int col0, const float (&v)[16],
+                                         int spin) {
+  float* out = p.C + (long)row * p.ldc + col0;
+  if (MODE == EPI_SILU_J) {
+    const float* d = p.aux1 + (long)node * p.ld_aux + col0;
+    float4 dd[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) dd[u] = ld4(d + 4 * u);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      st4(out + 4 * u, make_float4(v[4 * u] * dd[u].x, v[4 * u + 1] * dd[u].y, v[4 * u + 2] * dd[u].z,
+                                   v[4 * u + 3] * dd[u].w));
+  } else if (MODE == EPI_SILU_L) {
+    const long o = (long)row * p.ld_aux + col0;
+    float4 d1[4], d2[4], q[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      d1[u] = ld4(p.aux1 + o + 4 * u);
+      d2[u] = ld4(p.aux0 + o + 4 * u);
+      q[u] = ld4(p.aux3 + o + 4 * u);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      st4(out + 4 * u, make_float4(v[4 * u] * d1[u].x + q[u].x * d2[u].x, v[4 * u + 1] * d1[u].y + q[u].y * d2[u].y,
+                                   v[4 * u + 2] * d1[u].z + q[u].z * d2[u].z, v[4 * u + 3] * d1[u].w + q[u].w * d2[u].w));
+  } else if (MODE == EPI_ORB_J) {
+    const int pos = row / 3, t = row - 3 * pos;
+    const float* env = p.aux1 + (long)node * 5 * p.ld_aux + col0;
+    const bool self = p.dep_map[pos] == node;
+    float4 ex[4], raw[4], ej[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ex[u] = ld4(env + 4 * u);
+    if (self) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        raw[u] = ld4(p.aux3 + (long)node * p.ld_aux + col0 + 4 * u);
+        ej[u] = ld4(env + (1 + t) * p.ld_aux + 4 * u);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        st4(out + 4 * u, make_float4(raw[u].x * ej[u].x + ex[u].x * v[4 * u], raw[u].y * ej[u].y + ex[u].y * v[4 * u + 1],
+                                     raw[u].z * ej[u].z + ex[u].z * v[4 * u + 2],
+                                     raw[u].w * ej[u].w + ex[u].w * v[4 * u + 3]));
+        st4(p.aux2 + ((long)node * 3 + t) * p.ld_aux + col0 + 4 * u,
+            make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]));
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        st4(out + 4 * u, make_float4(ex[u].x * v[4 * u], ex[u].y * v[4 * u + 1], ex[u].z * v[4 * u + 2],
+                                     ex[u].w * v[4 * u + 3]));
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) tc_store4<MODE>(p, row, node, col0 + 4 * u, v + 4 * u, spin);
   }
 }
 
@@ -270,34 +325,35 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
         unsigned char* a_hi = astage + s * TcCfg::A_STAGE;
         unsigned char* a_lo = a_hi + TcCfg::A_BYTES;
         const int k0 = kt * TC_BK;
+        // warp lw converts 8-row x 16-column blocks blk = lw + 4 u (u < 16) of the 128 x 64 tile: lane
+        // (r8, kq) = (lane % 8, lane / 8) owns 4 K-consecutive elements, so a warp's loads cover 8 rows x
+        // 64 contiguous bytes and its 8-byte stores fill whole 128-byte core-matrix rows (no bank conflicts)
+        const int lw = lt >> 5, r8 = lane & 7, kq = lane >> 3;
+        float4 v[16];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          float4 v[8];
+        for (int u = 0; u < 16; ++u) {
+          const int blk = lw + 4 * u;
+          const int r = (blk >> 2) * 8 + r8, kk = (blk & 3) * 16 + kq * 4;
+          const int gr = m0 + r, gk = k0 + kk;
+          v[u] = (gr < rows && gk < p.K) ? ld4(p.A + (long)gr * p.lda + gk) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            const int q = lt + 128 * (u + 8 * h);
-            const int r = q >> 4, kq = (q & 15) * 4;
-            const int gr = m0 + r, gk = k0 + kq;
-            v[u] = (gr < rows && gk < p.K) ? ld4(p.A + (long)gr * p.lda + gk) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < 16; ++u) {
+          const int blk = lw + 4 * u;
+          const int r = (blk >> 2) * 8 + r8, kk = (blk & 3) * 16 + kq * 4;
+          const float f[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+          uint32_t hw[2], lw2[2];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const __nv_bfloat16 h0 = __float2bfloat16_rn(f[2 * e]), h1 = __float2bfloat16_rn(f[2 * e + 1]);
+            const __nv_bfloat16 l0 = __float2bfloat16_rn(f[2 * e] - __bfloat162float(h0));
+            const __nv_bfloat16 l1 = __float2bfloat16_rn(f[2 * e + 1] - __bfloat162float(h1));
+            hw[e] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+            lw2[e] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
           }
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            const int q = lt + 128 * (u + 8 * h);
-            const int r = q >> 4, kq = (q & 15) * 4;
-            const float f[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-            uint32_t hw[2], lw[2];
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-              const __nv_bfloat16 h0 = __float2bfloat16_rn(f[2 * e]), h1 = __float2bfloat16_rn(f[2 * e + 1]);
-              const __nv_bfloat16 l0 = __float2bfloat16_rn(f[2 * e] - __bfloat162float(h0));
-              const __nv_bfloat16 l1 = __float2bfloat16_rn(f[2 * e + 1] - __bfloat162float(h1));
-              hw[e] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-              lw[e] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-            }
-            const uint32_t off = tc_off(r, kq);
-            *reinterpret_cast<uint2*>(a_hi + off) = make_uint2(hw[0], hw[1]);
-            *reinterpret_cast<uint2*>(a_lo + off) = make_uint2(lw[0], lw[1]);
-          }
+          const uint32_t off = tc_off(r, kk);
+          *reinterpret_cast<uint2*>(a_hi + off) = make_uint2(hw[0], hw[1]);
+          *reinterpret_cast<uint2*>(a_lo + off) = make_uint2(lw2[0], lw2[1]);
         }
         proxy_fence();
         tc_arrive(&bars->full[s]);
@@ -353,19 +409,32 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
       if (valid && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
       const int prev = __shfl_up_sync(0xffffffffu, node, 1);
       const bool head = lane == 0 || prev != node;
+      // rows of one center are consecutive: bit k of segm says lane + 2^k belongs to this lane's center
+      unsigned segm = 0;
+      if (MODE == EPI_SILU_J) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const int nu = __shfl_down_sync(0xffffffffu, node, 1 << k);
+          if (lane + (1 << k) < 32 && nu == node) segm |= 1u << k;
+        }
+      }
       const uint32_t base = tmem + (uint32_t)(b * TCP_BN) + ((uint32_t)(quad * 32) << 16);
       for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
         float v[16];
         tmem_ld16(base + (uint32_t)c0, v);
         if (mine) {
+          const int spin = spin_filter < 0 ? 0 : spin_filter;
+          if (n0 + c0 + 15 < p.N) {
+            tc_epi16<MODE>(p, row, node, n0 + c0, v, spin);
+          } else {
 #pragma unroll
-          for (int j = 0; j < 16; j += 4) {
-            const int col = n0 + c0 + j;
-            if (col + 3 < p.N) tc_store4<MODE>(p, row, node, col, v + j, spin_filter < 0 ? 0 : spin_filter);
-            else
-              for (int e = 0; e < 4; ++e)
-                if (col + e < p.N)
-                  gemm_store<float, MODE>(p, row, col + e, v[j + e], spin_filter < 0 ? 0 : spin_filter);
+            for (int j = 0; j < 16; j += 4) {
+              const int col = n0 + c0 + j;
+              if (col + 3 < p.N) tc_store4<MODE>(p, row, node, col, v + j, spin);
+              else
+                for (int e = 0; e < 4; ++e)
+                  if (col + e < p.N) gemm_store<float, MODE>(p, row, col + e, v[j + e], spin);
+            }
           }
         }
         if (MODE == EPI_SILU_J) {
@@ -373,10 +442,9 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
           for (int j = 0; j < 16; ++j) {
             float q = valid ? v[j] * v[j] : 0.f;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const float u = __shfl_down_sync(0xffffffffu, q, o);
-              const int nu = __shfl_down_sync(0xffffffffu, node, o);
-              if (lane + o < 32 && nu == node) q += u;
+            for (int k = 0; k < 5; ++k) {
+              const float u = __shfl_down_sync(0xffffffffu, q, 1 << k);
+              if ((segm >> k) & 1u) q += u;
             }
             const int col = n0 + c0 + j;
             if (valid && head && col < p.N) atomicAdd(&p.aux2[(long)node * p.ld_aux + col], q);
