@@ -149,7 +149,7 @@ struct Plan {
   size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, Zr2, jsqr;
   size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, tile_mask;
   // double
-  size_t ld, sd, dlap;
+  size_t ld, sd, dlap, gjw;
   size_t total;
 };
 
@@ -237,6 +237,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.JMl, W * 2, es);
     take(P.JMj, W * 3 * n * 2, es);
   }
+  take(P.gjw, W * NDET * n * n, 8);  // working matrices of the Gauss-Jordan / LU kernel
   take(P.tile_mask, (fl ? 3 * Pc : G) / 128 + 2, 4);
   take(P.rn, G * 3, es);
   take(P.lpn, W, es);
@@ -616,63 +617,23 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   return cudaPeekAtLastError();
 }
 
-// Cluster size of the Gauss-Jordan kernel: the smallest power of two whose per-CTA column slice fits in
-// shared memory (fewer CTAs per matrix = fewer participants in every cluster barrier).
-int gj_cluster(int n, size_t es, size_t* smem_out) {
-  const int cls[5] = {1, 2, 4, 8, 16};
-  const size_t limits[2] = {220 * 1024, 220 * 1024};
-  for (int pass = 0; pass < 2; ++pass)
-    for (int k = 0; k < 5; ++k) {
-      const int CL = cls[k];
-      const size_t wc = (n + CL - 1) / CL;
-      const size_t sm = (size_t)n * wc * es + 3 * (size_t)n * es + wc * es + 2 * (size_t)n * 4 + 64;
-      if (sm <= limits[pass] && wc <= 1024) {
-        *smem_out = sm;
-        return CL;
-      }
-    }
-  return 0;
-}
-
+// Gauss-Jordan inversion (INV) or LU of every orbital matrix of the chunk, one CTA per matrix with the
+// working matrix in the workspace (k_gj_global).
 template <typename S, typename TI, typename TO, bool INV>
-cudaError_t launch_gj(const Ctx<TI>& c, const TI* A, TO* Ainv) {
+cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   const int n = c.p->n_el;
-  size_t smem = 0;
-  const int CL = gj_cluster(n, sizeof(S), &smem);
-  if (CL == 0) return cudaErrorInvalidValue;
-  auto kern = k_gauss_jordan<S, TI, TO, INV>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  if (CL > 8) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  constexpr int BW = GJG_BW_DECL;
+  const size_t smem = sizeof(S) * (2 * (size_t)n * BW + BW * BW + n + 2 * BW) + sizeof(int) * ((size_t)n + BW);
+  auto kern = k_gj_global<S, TI, TO, INV>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  cudaLaunchConfig_t cfg;
-  std::memset(&cfg, 0, sizeof(cfg));
-  cfg.gridDim = dim3(CL, c.Wc * NDET, 1);
-  cfg.blockDim = dim3(1024, 1, 1);  // one CTA per SM: the elimination step is latency-bound
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = c.s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CL;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  if (std::getenv("FIRE_DEBUG")) {
-    static bool once = false;
-    if (!once) {
-      once = true;
-      int clusters = 0;
-      cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg);
-      std::fprintf(stderr, "[fire] gauss_jordan: n=%d cluster=%d smem=%zu threads=%d max active clusters=%d\n", n, CL,
-                   smem, (int)cfg.blockDim.x, clusters);
-    }
-  }
   g_nlaunch++;
-  return cudaLaunchKernelEx(&cfg, kern, A, n, CL, c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
-                            Ainv, c.status);
+  kern<<<c.Wc * NDET, GJG_THREADS_DECL, smem, c.s>>>(A, n, c.template buf<S>(c.P.gjw),
+                                                      c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
+                                                      Ainv, c.status);
+  return cudaPeekAtLastError();
 }
 
 // Jastrow: attention (Q.keys narrow + V + sums + readout MLP) and MLP Jastrow; H and B1 are scratch.
@@ -788,9 +749,9 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   // slogdet only: FP32 LU for the FP32/mixed value path, FP64 in the FP64 build
   Prof pr_lu("lu", c.s);
   if constexpr (sizeof(T) == 8)
-    launch_gj<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
+    launch_gjg<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
   else
-    launch_gj<float, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
+    launch_gjg<float, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
   stage_jastrow<T, 0>(c);
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
@@ -815,9 +776,9 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
     // orbital-matrix inverse: native FP64 in the FP64 build, double-FP32 (48-bit significand) otherwise
     Prof pr("gauss_jordan", c.s);
     if constexpr (sizeof(T) == 8)
-      launch_gj<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+      launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
     else
-      launch_gj<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
   }
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {

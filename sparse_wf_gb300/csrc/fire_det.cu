@@ -4,23 +4,19 @@
 //  k_env_coef   forward-Laplacian coefficients of exp(-softplus(sigma) |r - R|) per electron,
 //               nucleus, determinant and envelope (EfficientIsotropicEnvelopes, envelopes.py:55-82);
 //               a GEMM with pi then gives the envelope carrier [x, jac(3), lap] per orbital.
-//  k_gauss_jordan  sign/log|det| and (optionally) the inverse of every orbital matrix, computed
-//               in double precision (native FP64 in the FP64 build, double-FP32 "df64" with a 48-bit
-//               significand in the FP32 and mixed paths, fire_df64.cuh) by a thread-block cluster: the n x n matrix is split by columns over the
-//               cluster's CTAs and stays in their shared memory; the pivot column is read through
-//               distributed shared memory.  Partial pivoting like jax.lax.linalg.lu, sign/log|det|
-//               as slogdet_from_lu (model/utils.py:153-161), inverse as get_inverse_from_lu (144-150).
+//  k_gj_global  sign/log|det| and (optionally) the inverse of every orbital matrix, computed in
+//               double precision (native FP64 in the FP64 build, double-FP32 "df64" with a 48-bit
+//               significand in the FP32 and mixed paths, fire_df64.cuh; the value-only path's LU in
+//               FP32), one CTA per matrix with the working matrix in the workspace, eliminated in
+//               panels.  Partial pivoting like jax.lax.linalg.lu, sign/log|det| as slogdet_from_lu
+//               (model/utils.py:153-161), inverse as get_inverse_from_lu (144-150).
 //  k_detlap     sparse_slogdet_with_fwd_lap (model/sparse_fwd_lap.py:294-319) restricted to the
 //               triplets: for every dependency m, B = J[(i, m) rows] @ A^-1[:, k] for i, k in {m} + N(m)
 //               gives d log det / d r_m = sum_i B[(i,m)][i] and the triplet term
 //               -sum_xyz sum_{i,k} B[(i,m)][k] B[(k,m)][i]; the first Laplacian term tr(lap A A^-1) is
 //               accumulated row by row.
-#include <cooperative_groups.h>
-
 #include "fire_df64.cuh"
 #include "fire_internal.cuh"
-
-namespace cg = cooperative_groups;
 
 namespace fire {
 
@@ -57,205 +53,212 @@ __global__ void k_env_coef(const T* __restrict__ r, const float* __restrict__ R,
   }
 }
 
-// Gauss-Jordan inversion / LU with partial pivoting.  grid = (CL, matrices), cluster = (CL, 1, 1),
-// 1024 threads (many warps hide the dependent double-FP32 operation chains); thread (tx, ty) = (tid % wc, tid / wc) owns column tx of this CTA's slice and rows
-// ty, ty + ty_n, ...
-// Look-ahead: during step k the CTA that owns column k + 1 computes that column's post-step values first
-// and writes them into every CTA's colbuf[(k + 1) % 3] (distributed shared memory), then all threads
-// arrive on the cluster barrier; step k + 1 starts with the matching wait, so each step has a single
-// split cluster barrier and the pivot column is read from local shared memory.  Three buffers: the one
-// rewritten during step k was last read during step k - 2, which every CTA finished before arriving in
-// step k - 1 (the arrival the writer waited for).
-// A: element (i, o) of matrix (w, d) at A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]).
-// Outputs: logdet[w * NDET + d], sign[...] (double); Ainv[(w * NDET + d) * n * n + o * n + i] (if INV).
-__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
-__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+constexpr int GJG_BW = 16, GJG_THREADS = 512;
 
-constexpr int GJ_THREADS = 1024;
+// Gauss-Jordan inversion / LU with partial pivoting, one matrix per CTA, the working matrix in global
+// memory (the caller's workspace, row-major [n][n] in the elimination type S) instead of shared memory, so
+// that every matrix of the batch is in flight at once (two CTAs per SM) and the kernel is bound by
+// arithmetic, not by the latency of n dependent steps.  Columns are eliminated in panels of GJG_BW:
+//  1. the panel is loaded into shared memory and factored there, recording the pivot row p_t of every
+//     step and the step's transform x <- x - w_t x[k_t] of any other column x (w_t kept in the final row
+//     order of the panel: later interchanges are applied to it as well);
+//  2. W~ = W L^-1 with L[t][s] = w_s[k_t] (unit lower triangular), so that the whole panel acts on another
+//     column as: interchange rows k_t <-> p_t, then x <- x - W~ x[k_0 .. k_{b-1}];
+//  3. every other column (LU: every column right of the panel) is streamed through shared memory in chunks
+//     of GJG_BW columns and updated with that rank-b product.
+// A: element (i, o) of matrix (w, d) at A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]).
+// Outputs: logdet[w * NDET + d], sign[...] (double); Ainv[(w * NDET + d) * n * n + o * n + i] (if INV),
+// written after undoing the column permutation.
 template <typename S, typename TI, typename TO, bool INV>
-__global__ void __launch_bounds__(GJ_THREADS, 1) k_gauss_jordan(const TI* __restrict__ A, int n, int CL,
-                                                      double* __restrict__ logdet, double* __restrict__ sign,
-                                                      TO* __restrict__ Ainv, int32_t* status) {
+__global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restrict__ A, int n, S* __restrict__ work,
+                                                             double* __restrict__ logdet, double* __restrict__ sign,
+                                                             TO* __restrict__ Ainv, int32_t* status) {
   extern __shared__ __align__(16) unsigned char gj_smem[];
-  cg::cluster_group cluster = cg::this_cluster();
-  const int c = (int)cluster.block_rank();
-  const int mat = blockIdx.y;
+  constexpr int BW = GJG_BW;
+  const int mat = blockIdx.x;
   const int w = mat / NDET, d = mat - w * NDET;
-  const int wc = (n + CL - 1) / CL;
-  const int j0 = c * wc, jn = max(0, min(wc, n - j0));
-  S* a = reinterpret_cast<S*>(gj_smem);  // [n][wc]
-  S* colbuf = a + (size_t)n * wc;        // [3][n] pivot columns (published by their owner)
-  S* rowk = colbuf + 3 * n;              // [wc]
-  int* perm = reinterpret_cast<int*>(rowk + wc);  // [n] (+ [n] scratch)
+  S* M = work + (size_t)mat * n * n;
+  S* pan = reinterpret_cast<S*>(gj_smem);  // [n][BW] the panel, then each chunk of other columns
+  S* W = pan + (size_t)n * BW;             // [n][BW] panel transforms (then W~)
+  S* Li = W + (size_t)n * BW;              // [BW][BW] L^-1
+  S* colk = Li + BW * BW;                  // [n] pivot column before the step (interchanged order)
+  S* rk = colk + n;                        // [BW] row k of the panel before the step
+  S* rp = rk + BW;                         // [BW] row p
+  int* perm = reinterpret_cast<int*>(rp + BW);  // [n]
+  int* piv = perm + n;                     // [BW]
   __shared__ S redv[32];
   __shared__ int redi[32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarp = blockDim.x >> 5;
-  const int ty_n = max(1, (int)blockDim.x / wc);
-  const int tx = tid % wc, ty = tid / wc;
-  const bool upd = ty < ty_n && tx < jn;
-  for (int e = tid; e < n * wc; e += blockDim.x) {
-    const int i = e / wc, jl = e - i * wc;
-    a[e] = jl < jn ? (S)A[((long)(w * n + i) * NDET + d) * n + j0 + jl] : S(0);
-  }
-  cluster.sync();  // every CTA of the cluster is running and has its slice
-  if (c == 0) {     // publish column 0
-    for (int i = tid; i < n; i += blockDim.x) {
-      const S v = a[(size_t)i * wc];
-      for (int r = 0; r < CL; ++r) cluster.map_shared_rank(colbuf, r)[i] = v;
-    }
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int i = e / n, o = e - i * n;
+    M[e] = (S)A[((long)(w * n + i) * NDET + d) * n + o];
   }
   __syncthreads();
-  cluster_arrive();
   double ld = 0.0;
-  int neg = 0;
-  bool singular = false;
-  // Rows k and p of step k are not written in place during step k: their new values wait in registers
-  // (one designated thread per column, and the look-ahead threads for column k + 1) and are stored at the
-  // start of step k + 1.  Every read of those rows in step k happens before the thread's cluster arrive,
-  // and the stores come after the next cluster wait, so one cluster barrier and one CTA barrier per step
-  // order all shared-memory traffic.
-  int pk = -1, pp = -1;                 // pending rows (designated update thread, column tx)
-  S uk = S(0), up = S(0);
-  int la_row = -1, la_col = 0;          // pending look-ahead element
-  S la_val = S(0);
-  for (int k = 0; k < n; ++k) {
-    const int owner = k / wc, kl = k - owner * wc;
-    cluster_wait();  // column k has been published into colbuf[k % 3]
-    const S* col = colbuf + (k % 3) * n;
-    S best = S(-1);
-    int bi = n;
-    for (int i = k + tid; i < n; i += blockDim.x) {
-      const S v = absv(col[i]);
-      if (v > best) {
-        best = v;
-        bi = i;
-      }
-    }
-    if (pk >= 0) {  // rows k - 1 and p(k - 1) of the previous step
-      a[(size_t)pk * wc + tx] = uk;
-      if (pp != pk) a[(size_t)pp * wc + tx] = up;
-      pk = -1;
-    }
-    if (la_row >= 0) {
-      a[(size_t)la_row * wc + la_col] = la_val;
-      la_row = -1;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const S ov = shfl_xor_any(best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) {
-        best = ov;
-        bi = oi;
-      }
-    }
-    if (lane == 0) {
-      redv[wid] = best;
-      redi[wid] = bi;
+  int neg = 0, sing = 0;
+  const int npan = (n + BW - 1) / BW;
+  const int cj = tid % BW, rg = tid / BW, rn = blockDim.x / BW;  // chunk update: column, row group
+  for (int P = 0; P < npan; ++P) {
+    const int k0 = P * BW, bw = min(BW, n - k0);
+    for (int e = tid; e < n * bw; e += blockDim.x) {
+      const int i = e / bw, j = e - i * bw;
+      pan[i * BW + j] = M[(size_t)i * n + k0 + j];
     }
     __syncthreads();
-    // every warp reduces the per-warp candidates itself (no second barrier)
-    S bv = lane < nwarp ? redv[lane] : S(-1);
-    int p = lane < nwarp ? redi[lane] : n;
+    // ---- factor the panel
+    for (int t = 0; t < bw; ++t) {
+      const int k = k0 + t;
+      S best = S(-1);
+      int bi = n;
+      for (int i = k + tid; i < n; i += blockDim.x) {
+        const S v = absv(pan[i * BW + t]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const S ov = shfl_xor_any(bv, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, p, o);
-      if (ov > bv || (ov == bv && oi < p)) {
-        bv = ov;
-        p = oi;
-      }
-    }
-    if (p >= n) p = k;
-    const S pv = col[p];
-    const S ipv = pv != S(0) ? S(1) / pv : S(0);
-    const S ck = col[k], cp = col[p];  // pivot-column entries; rows k and p are interchanged
-    // look-ahead: the owner of column k + 1 computes and publishes its post-step-k values (and keeps them)
-    const int owner1 = (k + 1) / wc, kl1 = (k + 1) - owner1 * wc;
-    const bool la = k + 1 < n && owner1 == c;
-    if (la) {
-      const S rk = (INV ? a[(size_t)p * wc + kl1] * ipv : a[(size_t)p * wc + kl1]);
-      S* nb = colbuf + ((k + 1) % 3) * n;
-      for (int i = tid; i < n; i += blockDim.x) {
-        S v;
-        const int src = i == k ? p : (i == p ? k : i);
-        const S ci = i == k ? cp : (i == p ? ck : col[i]);
-        if (INV) v = i == k ? rk : a[(size_t)src * wc + kl1] - ci * rk;
-        else v = i > k ? a[(size_t)src * wc + kl1] - ci * ipv * rk : a[(size_t)src * wc + kl1];
-        for (int r = 0; r < CL; ++r) cluster.map_shared_rank(nb, r)[i] = v;
-        if (i == k || i == p) {
-          la_row = i;
-          la_col = kl1;
-          la_val = v;
-        } else {
-          a[(size_t)i * wc + kl1] = v;
+      for (int o = 16; o > 0; o >>= 1) {
+        const S ov = shfl_xor_any(best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
         }
       }
-    }
-    // rows p and k of this thread's column, read before the arrive
-    const bool mycol = upd && !(la && tx == kl1);
-    const S vp = mycol ? a[(size_t)p * wc + tx] : S(0);
-    const S vk = (mycol && ty == 0) ? a[(size_t)k * wc + tx] : S(0);
-    if (k + 1 < n) cluster_arrive();  // releases the published column
-    if (tid == 0) {  // one thread keeps the permutation, sign and log|det|
-      perm[k] = p;
-      if (pv == S(0)) singular = true;
-      ld += ::log(::fabs((double)pv));
-      if (pv < S(0)) neg ^= 1;
-      if (p != k) neg ^= 1;
-    }
-    if (mycol) {
-      if (INV) {
-        const bool kcol = owner == c && tx == kl;
-        const S rj = vp * ipv;
-        for (int i = ty; i < n; i += ty_n) {
-          if (i == k || i == p) continue;
-          const S ci = col[i];
-          S* e = a + (size_t)i * wc + tx;
-          *e = kcol ? -ci * ipv : *e - ci * rj;
+      if (lane == 0) {
+        redv[wid] = best;
+        redi[wid] = bi;
+      }
+      __syncthreads();
+      S bv = lane < nwarp ? redv[lane] : S(-1);
+      int p = lane < nwarp ? redi[lane] : n;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const S ov = shfl_xor_any(bv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, p, o);
+        if (ov > bv || (ov == bv && oi < p)) {
+          bv = ov;
+          p = oi;
         }
-        if (ty == 0) {
-          uk = kcol ? ipv : rj;
-          up = kcol ? -ck * ipv : vk - ck * rj;
-          pk = k;
-          pp = p;
+      }
+      if (p >= n) p = k;
+      const S pv = pan[p * BW + t];
+      const S ipv = pv != S(0) ? S(1) / pv : S(0);
+      if (tid == 0) {
+        piv[t] = p;
+        perm[k] = p;
+        if (pv == S(0)) sing = 1;
+        ld += ::log(::fabs((double)pv));
+        if (pv < S(0)) neg ^= 1;
+        if (p != k) neg ^= 1;
+      }
+      for (int i = tid; i < n; i += blockDim.x) colk[i] = pan[(i == k ? p : (i == p ? k : i)) * BW + t];
+      for (int j = tid; j < bw; j += blockDim.x) {
+        rk[j] = pan[k * BW + j];
+        rp[j] = pan[p * BW + j];
+      }
+      if (p != k)  // earlier transforms follow the interchange
+        for (int s2 = tid; s2 < t; s2 += blockDim.x) {
+          const S tk = W[k * BW + s2];
+          W[k * BW + s2] = W[p * BW + s2];
+          W[p * BW + s2] = tk;
         }
-      } else {
-        if (j0 + tx > k) {
-          const S rj = vp;
-          for (int i = k + 1 + ty; i < n; i += ty_n) {
-            if (i == p) continue;
-            a[(size_t)i * wc + tx] -= col[i] * ipv * rj;
+      __syncthreads();
+      for (int e = tid; e < n * bw; e += blockDim.x) {
+        const int i = e / bw, j = e - i * bw;
+        S* el = pan + i * BW + j;
+        const S ci = colk[i];
+        if (INV) {
+          const S old = i == k ? rp[j] : (i == p ? rk[j] : *el);
+          const S rj = rp[j] * ipv;
+          if (j == t) *el = i == k ? ipv : -ci * ipv;
+          else *el = i == k ? rj : old - ci * rj;
+        } else if (j > t) {
+          const S old = i == k ? rp[j] : (i == p ? rk[j] : *el);
+          *el = i > k ? old - ci * ipv * rp[j] : old;
+        }
+      }
+      for (int i = tid; i < n; i += blockDim.x)
+        W[i * BW + t] = INV ? (i == k ? S(1) - ipv : colk[i] * ipv) : (i > k ? colk[i] * ipv : S(0));
+      __syncthreads();
+    }
+    // ---- L^-1 (one lane per column s: Li[t][s] = -sum_{u=s}^{t-1} L[t][u] Li[u][s]) and W~ = W L^-1
+    if (tid < bw) {
+      for (int t = 0; t < bw; ++t) {
+        S v = t == tid ? S(1) : S(0);
+        for (int u = tid; u < t; ++u) v -= W[(k0 + t) * BW + u] * Li[u * BW + tid];
+        Li[t * BW + tid] = v;
+      }
+    }
+    for (int e = tid; e < n * bw; e += blockDim.x) {  // panel back to the working matrix
+      const int i = e / bw, j = e - i * bw;
+      M[(size_t)i * n + k0 + j] = pan[i * BW + j];
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) {
+      S wr[BW];
+#pragma unroll
+      for (int q = 0; q < BW; ++q) wr[q] = q < bw ? W[i * BW + q] : S(0);
+#pragma unroll
+      for (int t = 0; t < BW; ++t) {
+        if (t >= bw) break;
+        S acc = S(0);
+#pragma unroll
+        for (int q = 0; q < BW; ++q)
+          if (q >= t && q < bw) acc += wr[q] * Li[q * BW + t];
+        W[i * BW + t] = acc;
+      }
+    }
+    __syncthreads();
+    // ---- apply the panel to the other columns, one chunk of BW columns at a time
+    for (int Q = INV ? 0 : P + 1; Q < npan; ++Q) {
+      if (Q == P) continue;
+      const int c0 = Q * BW, cb = min(BW, n - c0);
+      for (int e = tid; e < n * cb; e += blockDim.x) {
+        const int i = e / cb, j = e - i * cb;
+        pan[i * BW + j] = M[(size_t)i * n + c0 + j];
+      }
+      __syncthreads();
+      if (tid < cb)
+        for (int t = 0; t < bw; ++t) {
+          const int pt = piv[t];
+          if (pt != k0 + t) {
+            const S tmp = pan[(k0 + t) * BW + tid];
+            pan[(k0 + t) * BW + tid] = pan[pt * BW + tid];
+            pan[pt * BW + tid] = tmp;
           }
-          if (ty == 0) {
-            uk = vp;
-            up = vk - ck * ipv * vp;
-            pk = k;
-            pp = p;
-          }
-        } else if (ty == 0) {  // columns left of the pivot: rows k and p are only interchanged
-          uk = vp;
-          up = vk;
-          pk = k;
-          pp = p;
         }
+      __syncthreads();
+      S yv[BW];
+#pragma unroll
+      for (int t = 0; t < BW; ++t) yv[t] = (t < bw && cj < cb) ? pan[(k0 + t) * BW + cj] : S(0);
+      __syncthreads();  // every pivot-row value is read before any is updated
+      if (cj < cb)
+        for (int i = (INV ? 0 : k0) + rg; i < n; i += rn) {
+          S acc = pan[i * BW + cj];
+          const S* wi = W + i * BW;
+#pragma unroll
+          for (int t = 0; t < BW; ++t)
+            if (t < bw) acc -= wi[t] * yv[t];
+          pan[i * BW + cj] = acc;
+        }
+      __syncthreads();
+      for (int e = tid; e < n * cb; e += blockDim.x) {
+        const int i = e / cb, j = e - i * cb;
+        M[(size_t)i * n + c0 + j] = pan[i * BW + j];
       }
+      __syncthreads();
     }
   }
-  if (pk >= 0) {
-    a[(size_t)pk * wc + tx] = uk;
-    if (pp != pk) a[(size_t)pp * wc + tx] = up;
-  }
-  if (la_row >= 0) a[(size_t)la_row * wc + la_col] = la_val;
-  __syncthreads();
-  if (c == 0 && tid == 0) {
+  if (tid == 0) {
     logdet[mat] = ld;
     sign[mat] = neg ? -1.0 : 1.0;
-    if (singular) set_flag(status, FIRE_FLAG_SINGULAR);
+    if (sing) set_flag(status, FIRE_FLAG_SINGULAR);
   }
   if (INV) {
     // undo the row interchanges on the columns: final column jc holds working column src(jc)
-    int* src = perm + n;  // [n] scratch after perm (allocated by the launcher)
+    int* src = reinterpret_cast<int*>(colk);
     if (tid == 0) {
       for (int q = 0; q < n; ++q) src[q] = q;
       for (int k = n - 1; k >= 0; --k) {
@@ -267,20 +270,12 @@ __global__ void __launch_bounds__(GJ_THREADS, 1) k_gauss_jordan(const TI* __rest
         }
       }
     }
-    cluster.sync();
     __syncthreads();
     TO* out = Ainv + (size_t)mat * n * n;
-    for (int e = tid; e < n * jn; e += blockDim.x) {
-      const int i = e / jn, jl = e - i * jn;
-      const int jc = j0 + jl;
-      const int sc = src[jc];
-      const int ow = sc / wc;
-      const S* rs = cluster.map_shared_rank(a, ow);
-      out[(size_t)i * n + jc] = (TO)rs[(size_t)i * wc + (sc - ow * wc)];
+    for (int e = tid; e < n * n; e += blockDim.x) {
+      const int i = e / n, jc = e - i * n;
+      out[e] = (TO)M[(size_t)i * n + src[jc]];
     }
-    cluster.sync();  // keep shared memory alive until all remote reads are done
-  } else {
-    cluster.sync();
   }
 }
 
@@ -429,20 +424,14 @@ template __global__ void k_env_coef<double, 1>(const double*, const float*, cons
                                                int, double*);
 template __global__ void k_env_coef<double, 5>(const double*, const float*, const double*, int, int, int, int,
                                                int, double*);
-template __global__ void k_gauss_jordan<double, float, float, true>(const float*, int, int, double*, double*,
-                                                                    float*, int32_t*);
-template __global__ void k_gauss_jordan<double, float, float, false>(const float*, int, int, double*, double*,
-                                                                     float*, int32_t*);
-template __global__ void k_gauss_jordan<float, float, float, false>(const float*, int, int, double*, double*,
-                                                                    float*, int32_t*);
-template __global__ void k_gauss_jordan<df64, float, float, true>(const float*, int, int, double*, double*, float*,
-                                                                  int32_t*);
-template __global__ void k_gauss_jordan<df64, float, float, false>(const float*, int, int, double*, double*, float*,
-                                                                   int32_t*);
-template __global__ void k_gauss_jordan<double, double, double, true>(const double*, int, int, double*,
-                                                                      double*, double*, int32_t*);
-template __global__ void k_gauss_jordan<double, double, double, false>(const double*, int, int, double*,
-                                                                       double*, double*, int32_t*);
+template __global__ void k_gj_global<float, float, float, false>(const float*, int, float*, double*, double*,
+                                                                  float*, int32_t*);
+template __global__ void k_gj_global<df64, float, float, true>(const float*, int, df64*, double*, double*, float*,
+                                                                int32_t*);
+template __global__ void k_gj_global<double, double, double, true>(const double*, int, double*, double*, double*,
+                                                                    double*, int32_t*);
+template __global__ void k_gj_global<double, double, double, false>(const double*, int, double*, double*, double*,
+                                                                     double*, int32_t*);
 template __global__ void k_detlap<float>(Nbr, Layout, const float*, const float*, const float*, float*, double*,
                                          int32_t*);
 template __global__ void k_detlap<double>(Nbr, Layout, const double*, const double*, const double*, double*,

@@ -80,6 +80,10 @@ __device__ __forceinline__ df64& operator-=(df64& a, df64 b) {
   a = a - b;
   return a;
 }
+__device__ __forceinline__ df64& operator+=(df64& a, df64 b) {
+  a = a + b;
+  return a;
+}
 // warp butterfly exchange for double, float and df64 values
 template <typename S>
 __device__ __forceinline__ S shfl_xor_any(S v, int o) {

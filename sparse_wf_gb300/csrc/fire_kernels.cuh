@@ -33,8 +33,8 @@ template <typename T, int NV>
 __global__ void k_env_coef(const T* r, const float* R, const T* sp, int n, int n_s, int s_off, int N, int Wn,
                            T* coef);
 template <typename S, typename TI, typename TO, bool INV>
-__global__ void k_gauss_jordan(const TI* A, int n, int CL, double* logdet, double* sign, TO* Ainv,
-                               int32_t* status);
+__global__ void k_gj_global(const TI* A, int n, S* work, double* logdet, double* sign, TO* Ainv, int32_t* status);
+constexpr int GJG_BW_DECL = 16, GJG_THREADS_DECL = 512;
 template <typename T>
 __global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* lapA, T* grad, double* lap,
                          int32_t* status);
