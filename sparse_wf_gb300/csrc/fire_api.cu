@@ -623,7 +623,7 @@ template <typename S, typename TI, typename TO, bool INV>
 cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   const int n = c.p->n_el;
   constexpr int BW = GJG_BW_DECL;
-  const size_t smem = sizeof(S) * (2 * (size_t)n * BW + BW * BW + n + 2 * BW) + sizeof(int) * ((size_t)n + BW);
+  const size_t smem = sizeof(S) * (2 * (size_t)n * (BW + 1) + BW * BW + n + 2 * BW) + sizeof(int) * ((size_t)n + BW);
   auto kern = k_gj_global<S, TI, TO, INV>;
   if (smem > 48 * 1024) {
     const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

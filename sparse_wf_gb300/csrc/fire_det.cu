@@ -74,13 +74,13 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
                                                              double* __restrict__ logdet, double* __restrict__ sign,
                                                              TO* __restrict__ Ainv, int32_t* status) {
   extern __shared__ __align__(16) unsigned char gj_smem[];
-  constexpr int BW = GJG_BW;
+  constexpr int BW = GJG_BW, LD = GJG_BW + 1;  // shared rows padded: column walks spread over the banks
   const int mat = blockIdx.x;
   const int w = mat / NDET, d = mat - w * NDET;
   S* M = work + (size_t)mat * n * n;
-  S* pan = reinterpret_cast<S*>(gj_smem);  // [n][BW] the panel, then each chunk of other columns
-  S* W = pan + (size_t)n * BW;             // [n][BW] panel transforms (then W~)
-  S* Li = W + (size_t)n * BW;              // [BW][BW] L^-1
+  S* pan = reinterpret_cast<S*>(gj_smem);  // [n][LD] the panel, then each chunk of other columns
+  S* W = pan + (size_t)n * LD;             // [n][LD] panel transforms (then W~)
+  S* Li = W + (size_t)n * LD;              // [BW][BW] L^-1
   S* colk = Li + BW * BW;                  // [n] pivot column before the step (interchanged order)
   S* rk = colk + n;                        // [BW] row k of the panel before the step
   S* rp = rk + BW;                         // [BW] row p
@@ -100,10 +100,8 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   const int cj = tid % BW, rg = tid / BW, rn = blockDim.x / BW;  // chunk update: column, row group
   for (int P = 0; P < npan; ++P) {
     const int k0 = P * BW, bw = min(BW, n - k0);
-    for (int e = tid; e < n * bw; e += blockDim.x) {
-      const int i = e / bw, j = e - i * bw;
-      pan[i * BW + j] = M[(size_t)i * n + k0 + j];
-    }
+    if (cj < bw)
+      for (int i = rg; i < n; i += rn) pan[i * LD + cj] = M[(size_t)i * n + k0 + cj];
     __syncthreads();
     // ---- factor the panel
     for (int t = 0; t < bw; ++t) {
@@ -111,7 +109,7 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
       S best = S(-1);
       int bi = n;
       for (int i = k + tid; i < n; i += blockDim.x) {
-        const S v = absv(pan[i * BW + t]);
+        const S v = absv(pan[i * LD + t]);
         if (v > best) {
           best = v;
           bi = i;
@@ -143,7 +141,7 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
         }
       }
       if (p >= n) p = k;
-      const S pv = pan[p * BW + t];
+      const S pv = pan[p * LD + t];
       const S ipv = pv != S(0) ? S(1) / pv : S(0);
       if (tid == 0) {
         piv[t] = p;
@@ -153,53 +151,52 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
         if (pv < S(0)) neg ^= 1;
         if (p != k) neg ^= 1;
       }
-      for (int i = tid; i < n; i += blockDim.x) colk[i] = pan[(i == k ? p : (i == p ? k : i)) * BW + t];
+      for (int i = tid; i < n; i += blockDim.x) colk[i] = pan[(i == k ? p : (i == p ? k : i)) * LD + t];
       for (int j = tid; j < bw; j += blockDim.x) {
-        rk[j] = pan[k * BW + j];
-        rp[j] = pan[p * BW + j];
+        rk[j] = pan[k * LD + j];
+        rp[j] = pan[p * LD + j];
       }
       if (p != k)  // earlier transforms follow the interchange
         for (int s2 = tid; s2 < t; s2 += blockDim.x) {
-          const S tk = W[k * BW + s2];
-          W[k * BW + s2] = W[p * BW + s2];
-          W[p * BW + s2] = tk;
+          const S tk = W[k * LD + s2];
+          W[k * LD + s2] = W[p * LD + s2];
+          W[p * LD + s2] = tk;
         }
       __syncthreads();
-      for (int e = tid; e < n * bw; e += blockDim.x) {
-        const int i = e / bw, j = e - i * bw;
-        S* el = pan + i * BW + j;
+      for (int e = tid; e < n * BW; e += blockDim.x) {
+        const int i = e / BW, j = e - i * BW;  // BW is a power of two: shifts
+        if (j >= bw) continue;
+        S* el = pan + i * LD + j;
         const S ci = colk[i];
         if (INV) {
           const S old = i == k ? rp[j] : (i == p ? rk[j] : *el);
           const S rj = rp[j] * ipv;
           if (j == t) *el = i == k ? ipv : -ci * ipv;
-          else *el = i == k ? rj : old - ci * rj;
+          else *el = i == k ? rj : df_sub_mul(old, ci, rj);
         } else if (j > t) {
           const S old = i == k ? rp[j] : (i == p ? rk[j] : *el);
-          *el = i > k ? old - ci * ipv * rp[j] : old;
+          *el = i > k ? df_sub_mul(old, ci * ipv, rp[j]) : old;
         }
       }
       for (int i = tid; i < n; i += blockDim.x)
-        W[i * BW + t] = INV ? (i == k ? S(1) - ipv : colk[i] * ipv) : (i > k ? colk[i] * ipv : S(0));
+        W[i * LD + t] = INV ? (i == k ? S(1) - ipv : colk[i] * ipv) : (i > k ? colk[i] * ipv : S(0));
       __syncthreads();
     }
     // ---- L^-1 (one lane per column s: Li[t][s] = -sum_{u=s}^{t-1} L[t][u] Li[u][s]) and W~ = W L^-1
     if (tid < bw) {
       for (int t = 0; t < bw; ++t) {
         S v = t == tid ? S(1) : S(0);
-        for (int u = tid; u < t; ++u) v -= W[(k0 + t) * BW + u] * Li[u * BW + tid];
+        for (int u = tid; u < t; ++u) v = df_sub_mul(v, W[(k0 + t) * LD + u], Li[u * BW + tid]);
         Li[t * BW + tid] = v;
       }
     }
-    for (int e = tid; e < n * bw; e += blockDim.x) {  // panel back to the working matrix
-      const int i = e / bw, j = e - i * bw;
-      M[(size_t)i * n + k0 + j] = pan[i * BW + j];
-    }
+    if (cj < bw)  // panel back to the working matrix
+      for (int i = rg; i < n; i += rn) M[(size_t)i * n + k0 + cj] = pan[i * LD + cj];
     __syncthreads();
     for (int i = tid; i < n; i += blockDim.x) {
       S wr[BW];
 #pragma unroll
-      for (int q = 0; q < BW; ++q) wr[q] = q < bw ? W[i * BW + q] : S(0);
+      for (int q = 0; q < BW; ++q) wr[q] = q < bw ? W[i * LD + q] : S(0);
 #pragma unroll
       for (int t = 0; t < BW; ++t) {
         if (t >= bw) break;
@@ -207,7 +204,7 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
 #pragma unroll
         for (int q = 0; q < BW; ++q)
           if (q >= t && q < bw) acc += wr[q] * Li[q * BW + t];
-        W[i * BW + t] = acc;
+        W[i * LD + t] = acc;
       }
     }
     __syncthreads();
@@ -215,39 +212,35 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
     for (int Q = INV ? 0 : P + 1; Q < npan; ++Q) {
       if (Q == P) continue;
       const int c0 = Q * BW, cb = min(BW, n - c0);
-      for (int e = tid; e < n * cb; e += blockDim.x) {
-        const int i = e / cb, j = e - i * cb;
-        pan[i * BW + j] = M[(size_t)i * n + c0 + j];
-      }
+      if (cj < cb)
+        for (int i = rg; i < n; i += rn) pan[i * LD + cj] = M[(size_t)i * n + c0 + cj];
       __syncthreads();
       if (tid < cb)
         for (int t = 0; t < bw; ++t) {
           const int pt = piv[t];
           if (pt != k0 + t) {
-            const S tmp = pan[(k0 + t) * BW + tid];
-            pan[(k0 + t) * BW + tid] = pan[pt * BW + tid];
-            pan[pt * BW + tid] = tmp;
+            const S tmp = pan[(k0 + t) * LD + tid];
+            pan[(k0 + t) * LD + tid] = pan[pt * LD + tid];
+            pan[pt * LD + tid] = tmp;
           }
         }
       __syncthreads();
       S yv[BW];
 #pragma unroll
-      for (int t = 0; t < BW; ++t) yv[t] = (t < bw && cj < cb) ? pan[(k0 + t) * BW + cj] : S(0);
+      for (int t = 0; t < BW; ++t) yv[t] = (t < bw && cj < cb) ? pan[(k0 + t) * LD + cj] : S(0);
       __syncthreads();  // every pivot-row value is read before any is updated
       if (cj < cb)
         for (int i = (INV ? 0 : k0) + rg; i < n; i += rn) {
-          S acc = pan[i * BW + cj];
-          const S* wi = W + i * BW;
+          S acc = pan[i * LD + cj];
+          const S* wi = W + i * LD;
 #pragma unroll
           for (int t = 0; t < BW; ++t)
-            if (t < bw) acc -= wi[t] * yv[t];
-          pan[i * BW + cj] = acc;
+            if (t < bw) acc = df_sub_mul(acc, wi[t], yv[t]);
+          pan[i * LD + cj] = acc;
         }
       __syncthreads();
-      for (int e = tid; e < n * cb; e += blockDim.x) {
-        const int i = e / cb, j = e - i * cb;
-        M[(size_t)i * n + c0 + j] = pan[i * BW + j];
-      }
+      if (cj < cb)
+        for (int i = rg; i < n; i += rn) M[(size_t)i * n + c0 + cj] = pan[i * LD + cj];
       __syncthreads();
     }
   }
