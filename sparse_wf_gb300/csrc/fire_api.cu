@@ -113,21 +113,26 @@ size_t elem_size(const fire_problem* p) { return p->precision == FIRE_PREC_FP64 
 
 // Split BF16 copies of the contraction weights used on tensor cores (mixed precision only), stored
 // after the float slots of the prepared buffer: for each, hi [N][K] then lo [N][K].
-enum TcSlot { TC_UPD1, TC_UPD2, TC_ORB_UP, TC_ORB_DN, TC_V, TC_JMLP1, TC_JMLP2, TC_COUNT };
-struct TcSrc {
-  int slot;  // prepared slot (already scaled)
-  bool orb;  // N = NDET * n_el instead of F
+enum TcSlot {
+  TC_UPD1, TC_UPD2, TC_ORB_UP, TC_ORB_DN, TC_V, TC_JMLP1, TC_JMLP2, TC_EI_GLU, TC_EI_DENSE, TC_EI_OUT, TC_COUNT
 };
-const TcSrc kTcSrc[TC_COUNT] = {{PR_UPD1_W_S0, false}, {FIRE_P_UPD2_W, false}, {PR_ORB_UP_W_S1, true},
-                                {PR_ORB_DN_W_S1, true}, {PR_V_W_S1, false},    {PR_JMLP1_W_S1, false},
-                                {FIRE_P_JMLP2_W, false}};
+struct TcSrc {
+  int slot;   // prepared slot (already scaled); K = F for every one
+  int ncols;  // N in units of F, or 0 for NDET * n_el (orbitals)
+};
+const TcSrc kTcSrc[TC_COUNT] = {{PR_UPD1_W_S0, 1},   {FIRE_P_UPD2_W, 1},    {PR_ORB_UP_W_S1, 0},
+                                {PR_ORB_DN_W_S1, 0}, {PR_V_W_S1, 1},        {PR_JMLP1_W_S1, 1},
+                                {FIRE_P_JMLP2_W, 1}, {FIRE_P_EI_GLU_W, 2},  {FIRE_P_EI_DENSE_W, 1},
+                                {FIRE_P_EI_OUT_W, 5}};
+size_t tc_cols(int k, const fire_problem* p) {
+  return kTcSrc[k].ncols == 0 ? (size_t)NDET * p->n_el : (size_t)kTcSrc[k].ncols * F;
+}
 // byte offsets of the BF16 region (tc_off[TC_COUNT] = end)
 void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
   size_t o = (float_bytes + 255) / 256 * 256;
   for (int k = 0; k < TC_COUNT; ++k) {
     off[k] = o;
-    const size_t N = kTcSrc[k].orb ? (size_t)NDET * p->n_el : (size_t)F;
-    o += 2 * N * F * sizeof(__nv_bfloat16);
+    o += 2 * tc_cols(k, p) * F * sizeof(__nv_bfloat16);
     o = (o + 255) / 256 * 256;
   }
   off[TC_COUNT] = o;
@@ -481,6 +486,26 @@ cudaError_t stage_neighbors(Ctx<T>& c, bool fl) {
 }
 
 // ElecInit + GLU/Dense/Dense on the electron carriers, then edges + messages -> H
+// ElecInit contraction over the interleaved [x, jac(3), lap] rows of every electron.  In the mixed path
+// the tensor cores take the derivative rows (the value rows they also compute are not stored) and the
+// CUDA cores the value rows, read with a stride of NV rows: the value plane stays FP32.
+template <typename T>
+cudaError_t ei_gemm(Ctx<T>& c, const GemmP<T>& g, int NV, int tc_id) {
+  if (!(c.mixed && NV > 1)) return gemm<T, EPI_PLAIN>(c, g);
+  GemmP<T> gt = g;
+  gt.bias = nullptr;
+  gt.bias_period = 0;
+  gt.row_skip = NV;
+  cudaError_t e = gemm<T, EPI_PLAIN>(c, gt, tc_id);
+  if (e != cudaSuccess) return e;
+  GemmP<T> gv = g;
+  gv.lda = g.lda * NV;
+  gv.ldc = g.ldc * NV;
+  gv.M = g.M / NV;
+  gv.bias_period = g.bias ? 1 : 0;
+  return gemm<T, EPI_PLAIN>(c, gv);
+}
+
 template <typename T, int NT>
 cudaError_t stage_embedding(Ctx<T>& c) {
   constexpr int NV = NT > 0 ? NT + 2 : 1;
@@ -497,21 +522,21 @@ cudaError_t stage_embedding(Ctx<T>& c) {
   GemmP<T> g = gp0<T>();
   g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_GLU_W]; g.ldb = 2 * F; g.C = Z1; g.ldc = 2 * F;
   g.M = G * NV; g.N = 2 * F; g.K = F;
-  gemm<T, EPI_PLAIN>(c, g);
+  ei_gemm<T>(c, g, NV, TC_EI_GLU);
   g_nlaunch++;
   k_glu<T, NT><<<nblk((long)G * F), 256, 0, c.s>>>(Z1, E5a, G);
   g = gp0<T>();
   g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_DENSE_W]; g.ldb = F; g.C = Z1; g.ldc = F;
   g.bias = c.W.w[FIRE_P_EI_DENSE_B]; g.bias_period = NV;
   g.M = G * NV; g.N = F; g.K = F;
-  gemm<T, EPI_PLAIN>(c, g);
+  ei_gemm<T>(c, g, NV, TC_EI_DENSE);
   g_nlaunch++;
   k_silu5<T, NT><<<nblk((long)G * F), 256, 0, c.s>>>(Z1, G);
   g = gp0<T>();
   g.A = Z1; g.lda = F; g.B = c.W.w[FIRE_P_EI_OUT_W]; g.ldb = 5 * F; g.C = E5o; g.ldc = 5 * F;
   g.bias = c.W.w[FIRE_P_EI_OUT_B]; g.bias_period = NV;
   g.M = G * NV; g.N = 5 * F; g.K = F;
-  gemm<T, EPI_PLAIN>(c, g);
+  ei_gemm<T>(c, g, NV, TC_EI_OUT);
   Prof pr("edge_contract", c.s);
   k_edge_contract<T, NT><<<G, 256, 0, c.s>>>(c.r, c.nb, c.L, c.W, E5o, c.template buf<T>(c.P.HX),
                                              NT ? c.template buf<T>(c.P.HL) : nullptr,
@@ -830,7 +855,7 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
     tc_offsets(p, (size_t)off[PR_COUNT] * 4, to);
     const unsigned char* base = reinterpret_cast<const unsigned char*>(prepared);
     for (int k = 0; k < TC_COUNT; ++k) {
-      const size_t N = kTcSrc[k].orb ? (size_t)NDET * p->n_el : (size_t)F;
+      const size_t N = tc_cols(k, p);
       const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
       c.tcw[k] = TcWeights{hi, hi + N * F, nullptr, nullptr};
     }
@@ -985,7 +1010,7 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
   tc_offsets(prob, (size_t)off[PR_COUNT] * 4, to);
   unsigned char* base = reinterpret_cast<unsigned char*>(prepared);
   for (int k = 0; k < TC_COUNT; ++k) {
-    const int N = kTcSrc[k].orb ? NDET * prob->n_el : F;
+    const int N = (int)tc_cols(k, prob);
     __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(base + to[k]);
     g_nlaunch++;
     split_transpose(reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot], F, N, hi, hi + (size_t)N * F, s);

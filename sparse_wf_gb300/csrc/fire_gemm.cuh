@@ -46,6 +46,7 @@ struct GemmP {
   const int* dep_map;  // ORB_J: a position is "self" when dep_map[pos] == node
   int env_ns, env_soff;  // ENV: rows are (w * env_ns + i) * env_nv + v  ->  electron w * n_el + env_soff + i
   int env_nv;            // rows per electron of the envelope carrier (5: x, jac xyz, lap; 1: value)
+  int row_skip;          // tensor-core path: rows with row % row_skip == 0 are not stored (0: none)
 };
 
 constexpr int GBM = 128, GBN = 128, GBK = 8, GTHREADS = 256;

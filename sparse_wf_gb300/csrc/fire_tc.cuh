@@ -405,8 +405,8 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
       const int b = (int)(uc & 1);
       if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
       tc_fence_after();
-      bool mine = valid;
-      if (valid && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
+      bool mine = valid && !(p.row_skip > 0 && row % p.row_skip == 0);
+      if (mine && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
       const int prev = __shfl_up_sync(0xffffffffu, node, 1);
       const bool head = lane == 0 || prev != node;
       // rows of one center are consecutive: bit k of segm says lane + 2^k belongs to this lane's center
