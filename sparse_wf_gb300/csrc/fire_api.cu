@@ -114,25 +114,34 @@ size_t elem_size(const fire_problem* p) { return p->precision == FIRE_PREC_FP64 
 // Split BF16 copies of the contraction weights used on tensor cores (mixed precision only), stored
 // after the float slots of the prepared buffer: for each, hi [N][K] then lo [N][K].
 enum TcSlot {
-  TC_UPD1, TC_UPD2, TC_ORB_UP, TC_ORB_DN, TC_V, TC_JMLP1, TC_JMLP2, TC_EI_GLU, TC_EI_DENSE, TC_EI_OUT, TC_COUNT
+  TC_UPD1, TC_UPD2, TC_ORB_UP, TC_ORB_DN, TC_V, TC_JMLP1, TC_JMLP2, TC_EI_GLU, TC_EI_DENSE, TC_EI_OUT,
+  TC_ENV_UP, TC_ENV_DN, TC_COUNT
 };
 struct TcSrc {
-  int slot;   // prepared slot (already scaled); K = F for every one
-  int ncols;  // N in units of F, or 0 for NDET * n_el (orbitals)
+  int slot;  // prepared slot (already scaled), row-major [K][N] per matrix
+  int kind;  // > 0: K = F, N = kind * F;  0: K = F, N = NDET * n_el (orbitals);
+             // -1: NDET matrices with K = 8 n_nuc, N = n_el (envelope weights per determinant)
 };
 const TcSrc kTcSrc[TC_COUNT] = {{PR_UPD1_W_S0, 1},   {FIRE_P_UPD2_W, 1},    {PR_ORB_UP_W_S1, 0},
                                 {PR_ORB_DN_W_S1, 0}, {PR_V_W_S1, 1},        {PR_JMLP1_W_S1, 1},
                                 {FIRE_P_JMLP2_W, 1}, {FIRE_P_EI_GLU_W, 2},  {FIRE_P_EI_DENSE_W, 1},
-                                {FIRE_P_EI_OUT_W, 5}};
-size_t tc_cols(int k, const fire_problem* p) {
-  return kTcSrc[k].ncols == 0 ? (size_t)NDET * p->n_el : (size_t)kTcSrc[k].ncols * F;
+                                {FIRE_P_EI_OUT_W, 5}, {PR_ENV_UP_PI, -1},   {PR_ENV_DN_PI, -1}};
+// K, N and the number of matrices of a slot; its BF16 copy is hi [cnt][N][K] followed by lo [cnt][N][K]
+void tc_shape(int k, const fire_problem* p, size_t* K, size_t* N, int* cnt) {
+  const int kind = kTcSrc[k].kind;
+  *K = kind < 0 ? (size_t)NENV_ORB * p->n_nuc : (size_t)F;
+  *N = kind > 0 ? (size_t)kind * F : (kind == 0 ? (size_t)NDET * p->n_el : (size_t)p->n_el);
+  *cnt = kind < 0 ? NDET : 1;
 }
 // byte offsets of the BF16 region (tc_off[TC_COUNT] = end)
 void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
   size_t o = (float_bytes + 255) / 256 * 256;
   for (int k = 0; k < TC_COUNT; ++k) {
     off[k] = o;
-    o += 2 * tc_cols(k, p) * F * sizeof(__nv_bfloat16);
+    size_t K, N;
+    int cnt;
+    tc_shape(k, p, &K, &N, &cnt);
+    o += 2 * (size_t)cnt * N * K * sizeof(__nv_bfloat16);
     o = (o + 255) / 256 * 256;
   }
   off[TC_COUNT] = o;
@@ -594,6 +603,37 @@ cudaError_t linear_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt,
 }
 
 // envelopes + orbital matrices (+ their Jacobian/Laplacian planes)
+// Envelope contraction of one determinant and spin (EPI_ENV).  In the mixed path the derivative rows of
+// the [x, jac(3), lap] carrier run on the tensor cores with the split weights of that determinant, the
+// value rows (every NV-th) on the CUDA cores in FP32.
+template <typename T>
+cudaError_t env_gemm(Ctx<T>& c, const GemmP<T>& g, int NV, int tc_slot, int d) {
+  if constexpr (sizeof(T) == 4) {
+    if (c.mixed && NV > 1) {
+      size_t K, N;
+      int cnt;
+      tc_shape(tc_slot, c.p, &K, &N, &cnt);
+      const TcWeights wd{c.tcw[tc_slot].hi + (size_t)d * N * K, c.tcw[tc_slot].lo + (size_t)d * N * K, nullptr,
+                         nullptr};
+      GemmP<T> gt = g;
+      gt.row_skip = NV;
+      {
+        Prof pr("gemm", c.s);
+        g_nlaunch++;
+        const cudaError_t e = gemm_tc(EPI_ENV, 128, gt, wd, nullptr, c.status, c.s);
+        if (e != cudaSuccess) return e;
+      }
+      GemmP<T> gv = g;  // value rows: electron rows of stride NV, destination rows of stride NV
+      gv.lda = g.lda * NV;
+      gv.M = g.M / NV;
+      gv.env_nv = 1;
+      gv.ldc = g.ldc * NV;
+      return gemm<T, EPI_ENV>(c, gv);
+    }
+  }
+  return gemm<T, EPI_ENV>(c, g);
+}
+
 template <typename T, int NT>
 cudaError_t stage_orbitals(Ctx<T>& c) {
   constexpr int NV = NT > 0 ? NT + 2 : 1;
@@ -616,7 +656,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
       g.B = c.W.w[s == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (long)d * K8 * n; g.ldb = n;
       g.C = env + (long)d * n; g.ldc = DN; g.M = (int)rows; g.N = n; g.K = (int)K8;
       g.n_el = n; g.env_ns = ns; g.env_soff = s == 0 ? 0 : nu; g.env_nv = NV;
-      gemm<T, EPI_ENV>(c, g);
+      env_gemm<T>(c, g, NV, s == 0 ? TC_ENV_UP : TC_ENV_DN, d);
     }
   }
   GemmP<T> g = gp0<T>();
@@ -855,9 +895,11 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
     tc_offsets(p, (size_t)off[PR_COUNT] * 4, to);
     const unsigned char* base = reinterpret_cast<const unsigned char*>(prepared);
     for (int k = 0; k < TC_COUNT; ++k) {
-      const size_t N = tc_cols(k, p);
+      size_t K, N;
+      int cnt;
+      tc_shape(k, p, &K, &N, &cnt);
       const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
-      c.tcw[k] = TcWeights{hi, hi + N * F, nullptr, nullptr};
+      c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr};
     }
     c.tcw[TC_ORB_UP].hi2 = c.tcw[TC_ORB_DN].hi;
     c.tcw[TC_ORB_UP].lo2 = c.tcw[TC_ORB_DN].lo;
@@ -1010,10 +1052,16 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
   tc_offsets(prob, (size_t)off[PR_COUNT] * 4, to);
   unsigned char* base = reinterpret_cast<unsigned char*>(prepared);
   for (int k = 0; k < TC_COUNT; ++k) {
-    const int N = (int)tc_cols(k, prob);
+    size_t K, N;
+    int cnt;
+    tc_shape(k, prob, &K, &N, &cnt);
     __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(base + to[k]);
-    g_nlaunch++;
-    split_transpose(reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot], F, N, hi, hi + (size_t)N * F, s);
+    __nv_bfloat16* lo = hi + (size_t)cnt * N * K;
+    for (int m = 0; m < cnt; ++m) {
+      g_nlaunch++;
+      split_transpose(reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot] + (size_t)m * K * N, (int)K,
+                      (int)N, hi + (size_t)m * N * K, lo + (size_t)m * N * K, s);
+    }
   }
   return launch_status(__func__);
 }
@@ -1164,7 +1212,8 @@ fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const
   std::memset(&g, 0, sizeof(g));
   g.A = A; g.lda = K; g.C = C; g.ldc = N; g.M = M; g.N = N; g.K = K; g.node_div = 1; g.M_scale = 1; g.env_nv = 1;
   TcWeights wt{hi, hi + (size_t)N * K, nullptr, nullptr};
-  gemm_tc(EPI_PLAIN, N > 128 ? 256 : 128, g, wt, nullptr, status, s);
+  const cudaError_t e = gemm_tc(EPI_PLAIN, N > 128 ? 256 : 128, g, wt, nullptr, status, s);
+  if (e == cudaErrorInvalidValue) return FIRE_ERR_UNSUPPORTED;
   return launch_status(__func__);
 }
 

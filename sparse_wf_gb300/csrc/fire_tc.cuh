@@ -103,7 +103,13 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 template <int MODE>
 __device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int node, int col, const float* a,
                                           int spin) {
-  if (MODE == EPI_PLAIN) {
+  if (MODE == EPI_ENV) {
+    const int rr = row / p.env_nv, v = row - p.env_nv * rr;
+    const int g = (rr / p.env_ns) * p.n_el + p.env_soff + rr % p.env_ns;
+    float* out = p.C + ((long)g * p.env_nv + v) * p.ldc + col;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = a[k];
+  } else if (MODE == EPI_PLAIN) {
     float4 v = make_float4(a[0], a[1], a[2], a[3]);
     if (p.bias && p.bias_period > 0 && (row % p.bias_period) == 0) {
       const float4 b = ld4(p.bias + col);
@@ -222,6 +228,9 @@ struct TcCfg {
   static constexpr int BK_BYTES = TCP_BN * TC_BK * 2;            // one BF16 plane of one resident k-tile
   static constexpr int B_BYTES = 2 * BK_BYTES * (TCP_KMAX / TC_BK);  // hi + lo, all k-tiles
   static constexpr int TOTAL = B_BYTES + TCP_STAGES * A_STAGE + 256;
+  // streamed weights (K > TCP_KMAX): every stage carries its A and B k-tiles
+  static constexpr int SB_STAGE = A_STAGE + 2 * BK_BYTES;
+  static constexpr int TOTAL_SB = TCP_STAGES * SB_STAGE + 256;
 };
 
 struct TcBar {
@@ -249,14 +258,16 @@ __device__ __forceinline__ void tc_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int MODE>
+// SB: the weights stream through the stages with A (any K % 8 == 0) instead of staying resident (K <= 256).
+template <int MODE, bool SB>
 __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, const __nv_bfloat16* Bhi,
                                                             const __nv_bfloat16* Blo, int spin_filter,
                                                             const int* tile_mask, int32_t* status) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  unsigned char* bres = tc_smem;                        // resident B: [k-tile][hi, lo][128 x 64]
-  unsigned char* astage = tc_smem + TcCfg::B_BYTES;     // [stage][hi, lo][128 x 64]
-  TcBar* bars = reinterpret_cast<TcBar*>(astage + TCP_STAGES * TcCfg::A_STAGE);
+  constexpr int STAGE = SB ? TcCfg::SB_STAGE : TcCfg::A_STAGE;
+  unsigned char* bres = tc_smem;                                 // resident B: [k-tile][hi, lo][128 x 64]
+  unsigned char* astage = tc_smem + (SB ? 0 : TcCfg::B_BYTES);   // [stage][A hi, A lo (, B hi, B lo)]
+  TcBar* bars = reinterpret_cast<TcBar*>(astage + TCP_STAGES * STAGE);
   volatile int* abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -270,7 +281,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
   const int nk = (p.K + TC_BK - 1) / TC_BK;
 
   // resident weights of this column slice (all threads)
-  for (int q = tid; q < nk * TCP_BN * (TC_BK / 8); q += TCP_THREADS) {
+  for (int q = tid; !SB && q < nk * TCP_BN * (TC_BK / 8); q += TCP_THREADS) {
     const int kt = q / (TCP_BN * (TC_BK / 8));
     const int rq = q % (TCP_BN * (TC_BK / 8));
     const int r = rq >> 3, c = rq & 7;
@@ -322,7 +333,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
         const int s = (int)(kc % TCP_STAGES);
         const long use = kc / TCP_STAGES;
         if (use > 0 && !tc_wait(&bars->empty[s], (uint32_t)((use - 1) & 1), abort)) break;
-        unsigned char* a_hi = astage + s * TcCfg::A_STAGE;
+        unsigned char* a_hi = astage + s * STAGE;
         unsigned char* a_lo = a_hi + TcCfg::A_BYTES;
         const int k0 = kt * TC_BK;
         // warp lw converts 8-row x 16-column blocks blk = lw + 4 u (u < 16) of the 128 x 64 tile: lane
@@ -355,6 +366,18 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
           *reinterpret_cast<uint2*>(a_hi + off) = make_uint2(hw[0], hw[1]);
           *reinterpret_cast<uint2*>(a_lo + off) = make_uint2(lw2[0], lw2[1]);
         }
+        if (SB) {  // this k-tile of the weights: 128 rows x 64 K of the hi and the lo plane
+          unsigned char* b_hi = a_hi + TcCfg::A_STAGE;
+#pragma unroll 4
+          for (int u = 0; u < 16; ++u) {
+            const int idx = lt + 128 * u;
+            const int pl = idx >> 10, rq = idx & 1023, r = rq >> 3, c8 = rq & 7;
+            const int gn = n0 + r, gk = k0 + c8 * 8;
+            uint4 v4 = make_uint4(0, 0, 0, 0);
+            if (gn < p.N && gk < p.K) v4 = *reinterpret_cast<const uint4*>((pl ? Blo : Bhi) + (long)gn * p.K + gk);
+            *reinterpret_cast<uint4*>(b_hi + pl * TcCfg::BK_BYTES + tc_off(r, c8 * 8)) = v4;
+          }
+        }
         proxy_fence();
         tc_arrive(&bars->full[s]);
       }
@@ -376,8 +399,8 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
           const int s = (int)(kc % TCP_STAGES);
           if (!tc_wait(&bars->full[s], (uint32_t)((kc / TCP_STAGES) & 1), abort)) break;
           tc_fence_after();
-          const uint32_t ah = a0 + s * TcCfg::A_STAGE, al = ah + TcCfg::A_BYTES;
-          const uint32_t bh = b0 + kt * 2 * TcCfg::BK_BYTES, bl = bh + TcCfg::BK_BYTES;
+          const uint32_t ah = a0 + s * STAGE, al = ah + TcCfg::A_BYTES;
+          const uint32_t bh = SB ? ah + TcCfg::A_STAGE : b0 + kt * 2 * TcCfg::BK_BYTES, bl = bh + TcCfg::BK_BYTES;
 #pragma unroll
           for (int kk = 0; kk < TC_BK / 16; ++kk) {
             const uint32_t step = kk * 2 * TC_LBO;
@@ -503,9 +526,19 @@ __global__ void k_tile_mask(GemmP<float> p, int* mask) {
 template <int MODE>
 inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, int* mask_buf, int32_t* status,
                                   cudaStream_t s, int num_sms) {
-  if (p.K > TCP_KMAX) return cudaErrorInvalidValue;
+  if (p.K > TCP_KMAX) {
+    if (wt.hi2) return cudaErrorInvalidValue;
+    constexpr int smem = TcCfg::TOTAL_SB;
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const long mt = (p.M + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
+    if (mt == 0 || nt == 0) return cudaSuccess;
+    const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
+    k_gemm_tcp<MODE, true><<<(unsigned)(groups * nt), TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status);
+    return cudaPeekAtLastError();
+  }
   const int smem = TcCfg::TOTAL;
-  cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const long mt = (p.M + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
   if (mt == 0 || nt == 0) return cudaSuccess;
@@ -514,10 +547,10 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
   if (wt.hi2) {
     if (!mask_buf) return cudaErrorInvalidValue;
     k_tile_mask<<<(unsigned)mt, TC_BM, 0, s>>>(p, mask_buf);
-    k_gemm_tcp<MODE><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, 0, mask_buf, status);
-    k_gemm_tcp<MODE><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi2, wt.lo2, 1, mask_buf, status);
+    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, 0, mask_buf, status);
+    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi2, wt.lo2, 1, mask_buf, status);
   } else {
-    k_gemm_tcp<MODE><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status);
+    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status);
   }
   return cudaPeekAtLastError();
 }

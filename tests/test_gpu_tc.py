@@ -7,7 +7,9 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 256, 256), (300, 256, 256), (257, 200, 64), (1000, 1288, 256)])
+# K > 256 streams the weights through the pipeline stages instead of keeping them resident
+@pytest.mark.parametrize("M,N,K", [(128, 256, 256), (300, 256, 256), (257, 200, 64), (1000, 1288, 256),
+                                   (645, 324, 976), (130, 40, 264)])
 def test_gemm_mixed_matches_fp64(cuda_lib, M, N, K):
     g = torch.Generator(device="cuda").manual_seed(M + N + K)
     A = torch.randn(M, K, device="cuda", generator=g, dtype=torch.float32)
@@ -29,3 +31,18 @@ def test_gemm_mixed_matches_fp64(cuda_lib, M, N, K):
     # split-BF16 products: ~2^-17 relative per product (plain BF16 ~2^-9)
     assert err < 2e-5 * rms * K**0.5, (err, rms, bf16)
     assert err < bf16 / 50
+
+
+def test_gemm_mixed_rejects_unaligned_rows(cuda_lib):
+    """Row strides that are not a multiple of 4 floats cannot use the vector epilogue: rejected, not run."""
+    M, N, K = 64, 322, 256
+    A = torch.randn(M, K, device="cuda")
+    W = torch.randn(K, N, device="cuda")
+    Cm = torch.full((M, N), float("nan"), device="cuda")
+    ws = torch.empty(4 * N * K, dtype=torch.uint8, device="cuda")
+    status = torch.zeros(8, dtype=torch.int32, device="cuda")
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = cuda_lib.fire_gemm_mixed(s, M, N, K, C.c_void_p(A.data_ptr()), C.c_void_p(W.data_ptr()),
+                                  C.c_void_p(Cm.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                                  C.c_void_p(status.data_ptr()))
+    assert rc == 2  # FIRE_ERR_UNSUPPORTED
