@@ -24,6 +24,43 @@ cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __n
   return cudaPeekAtLastError();
 }
 
+namespace {
+// cuTensorMapEncodeTiled, looked up through the runtime (no link-time dependency on the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+}  // namespace
+
+bool tc_c_map(const GemmP<float>& p, CUtensorMap* map) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn || !p.C || p.M < 1 || p.N < 16 || (p.ldc * sizeof(float)) % 16 != 0 ||
+      (reinterpret_cast<uintptr_t>(p.C) & 15) != 0)
+    return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)p.N, (cuuint64_t)p.M};
+  const cuuint64_t strides[1] = {(cuuint64_t)p.ldc * sizeof(float)};
+  const cuuint32_t box[2] = {16, 32};
+  const cuuint32_t elem[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, p.C, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
 cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt, int* mask_buf, int32_t* status,
                     cudaStream_t s) {
   if (p.K % 8 != 0 || p.lda % 4 != 0 || p.ldc % 4 != 0 || (p.ld_aux % 4 != 0 && mode != EPI_PLAIN))

@@ -13,7 +13,10 @@
 // matrices LBO = 128 bytes apart, 8-row groups SBO = 1024 bytes apart.  One thread issues the MMAs and
 // commits them to an mbarrier per stage; all waits are bounded and report FIRE_FLAG_TIMEOUT.
 #pragma once
+#include <cuda.h>
+
 #include <algorithm>
+#include <cstring>
 
 #include "fire_gemm.cuh"
 #include "fire_internal.cuh"
@@ -77,6 +80,17 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// TMA store of a box of C (tensor map in kernel-parameter space) from shared memory; bulk async-groups
+// belong to the issuing thread
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, uint32_t src, int x, int y) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(src), "r"(x), "r"(y)
+               : "memory");
+}
+__device__ __forceinline__ void tma_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void tma_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void tma_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
@@ -99,31 +113,26 @@ __device__ __forceinline__ uint32_t tc_off(int row, int k) {
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
-// Applies the epilogue of MODE to columns col..col+3 of one row (col % 4 == 0, col + 3 < N).
+// Epilogue values of columns col..col+3 of one row (col % 4 == 0, col + 3 < N): everything but the store
+// of C (the orbital Jacobian epilogue stores its side output itself).  Not for EPI_ENV.
 template <int MODE>
-__device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int node, int col, const float* a,
+__device__ __forceinline__ float4 tc_val4(const GemmP<float>& p, int row, int node, int col, const float* a,
                                           int spin) {
-  if (MODE == EPI_ENV) {
-    const int rr = row / p.env_nv, v = row - p.env_nv * rr;
-    const int g = (rr / p.env_ns) * p.n_el + p.env_soff + rr % p.env_ns;
-    float* out = p.C + ((long)g * p.env_nv + v) * p.ldc + col;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) out[k] = a[k];
-  } else if (MODE == EPI_PLAIN) {
+  if (MODE == EPI_PLAIN) {
     float4 v = make_float4(a[0], a[1], a[2], a[3]);
     if (p.bias && p.bias_period > 0 && (row % p.bias_period) == 0) {
       const float4 b = ld4(p.bias + col);
       v.x += b.x; v.y += b.y; v.z += b.z; v.w += b.w;
     }
-    st4(p.C + (long)row * p.ldc + col, v);
+    return v;
   } else if (MODE == EPI_SILU_J) {  // aux1: silu' plane (per center)
     const float4 d = ld4(p.aux1 + (long)node * p.ld_aux + col);
-    st4(p.C + (long)row * p.ldc + col, make_float4(a[0] * d.x, a[1] * d.y, a[2] * d.z, a[3] * d.w));
+    return make_float4(a[0] * d.x, a[1] * d.y, a[2] * d.z, a[3] * d.w);
   } else if (MODE == EPI_SILU_L) {  // aux1: silu', aux0: silu'', aux3: sum of squared Jacobian rows
     const long o = (long)row * p.ld_aux + col;
     const float4 d1 = ld4(p.aux1 + o), d2 = ld4(p.aux0 + o), q = ld4(p.aux3 + o);
-    st4(p.C + (long)row * p.ldc + col, make_float4(a[0] * d1.x + q.x * d2.x, a[1] * d1.y + q.y * d2.y,
-                                                   a[2] * d1.z + q.z * d2.z, a[3] * d1.w + q.w * d2.w));
+    return make_float4(a[0] * d1.x + q.x * d2.x, a[1] * d1.y + q.y * d2.y, a[2] * d1.z + q.z * d2.z,
+                       a[3] * d1.w + q.w * d2.w);
   } else if (MODE == EPI_ORB_J) {
     const int pos = row / 3, t = row - 3 * pos;
     const float* env = p.aux1 + (long)node * 5 * p.ld_aux;
@@ -131,13 +140,12 @@ __device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int no
     if (p.dep_map[pos] == node) {
       const float4 raw = ld4(p.aux3 + (long)node * p.ld_aux + col);
       const float4 ej = ld4(env + (1 + t) * p.ld_aux + col);
-      st4(p.C + (long)row * p.ldc + col, make_float4(raw.x * ej.x + ex.x * a[0], raw.y * ej.y + ex.y * a[1],
-                                                     raw.z * ej.z + ex.z * a[2], raw.w * ej.w + ex.w * a[3]));
       st4(p.aux2 + ((long)node * 3 + t) * p.ld_aux + col, make_float4(a[0], a[1], a[2], a[3]));
-    } else {
-      st4(p.C + (long)row * p.ldc + col, make_float4(ex.x * a[0], ex.y * a[1], ex.z * a[2], ex.w * a[3]));
+      return make_float4(raw.x * ej.x + ex.x * a[0], raw.y * ej.y + ex.y * a[1], raw.z * ej.z + ex.z * a[2],
+                         raw.w * ej.w + ex.w * a[3]);
     }
-  } else if (MODE == EPI_ORB_L) {
+    return make_float4(ex.x * a[0], ex.y * a[1], ex.z * a[2], ex.w * a[3]);
+  } else {  // EPI_ORB_L
     const float* env = p.aux1 + (long)row * 5 * p.ld_aux;
     const float* rjs = p.aux2 + (long)row * 3 * p.ld_aux;
     const float4 ex = ld4(env + col), el = ld4(env + 4 * p.ld_aux + col), raw = ld4(p.aux3 + (long)row * p.ld_aux + col);
@@ -148,16 +156,30 @@ __device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int no
       const float4 r = ld4(rjs + t * p.ld_aux + col), e = ld4(env + (1 + t) * p.ld_aux + col);
       v.x += 2.f * r.x * e.x; v.y += 2.f * r.y * e.y; v.z += 2.f * r.z * e.z; v.w += 2.f * r.w * e.w;
     }
-    st4(p.C + (long)row * p.ldc + col, v);
+    return v;
   }
 }
 
-// Epilogue of 16 consecutive columns (col0 + 15 < N) of one row: all operand loads are issued before the
-// first store so that their latencies overlap (the stores could otherwise alias later loads).
+// Applies the epilogue of MODE to columns col..col+3 of one row and stores C.
 template <int MODE>
-__device__ __forceinline__ void tc_epi16(const GemmP<float>& p, int row, int node, int col0, const float (&v)[16],
-                                         int spin) {
-  float* out = p.C + (long)row * p.ldc + col0;
+__device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int node, int col, const float* a,
+                                          int spin) {
+  if (MODE == EPI_ENV) {  // scalar stores: the destination of one determinant may start mid-vector
+    const int rr = row / p.env_nv, v = row - p.env_nv * rr;
+    const int g = (rr / p.env_ns) * p.n_el + p.env_soff + rr % p.env_ns;
+    float* out = p.C + ((long)g * p.env_nv + v) * p.ldc + col;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = a[k];
+  } else {
+    st4(p.C + (long)row * p.ldc + col, tc_val4<MODE>(p, row, node, col, a, spin));
+  }
+}
+
+// Epilogue values of 16 consecutive columns (col0 + 15 < N) of one row, into o: all operand loads are
+// issued before the first store so that their latencies overlap.  Not for EPI_ENV.
+template <int MODE>
+__device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int node, int col0, const float (&v)[16],
+                                         int spin, float4 (&o)[4]) {
   if (MODE == EPI_SILU_J) {
     const float* d = p.aux1 + (long)node * p.ld_aux + col0;
     float4 dd[4];
@@ -165,29 +187,29 @@ __device__ __forceinline__ void tc_epi16(const GemmP<float>& p, int row, int nod
     for (int u = 0; u < 4; ++u) dd[u] = ld4(d + 4 * u);
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      st4(out + 4 * u, make_float4(v[4 * u] * dd[u].x, v[4 * u + 1] * dd[u].y, v[4 * u + 2] * dd[u].z,
-                                   v[4 * u + 3] * dd[u].w));
+      o[u] = make_float4(v[4 * u] * dd[u].x, v[4 * u + 1] * dd[u].y, v[4 * u + 2] * dd[u].z, v[4 * u + 3] * dd[u].w);
   } else if (MODE == EPI_SILU_L) {
-    const long o = (long)row * p.ld_aux + col0;
+    const long of = (long)row * p.ld_aux + col0;
     float4 d1[4], d2[4], q[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      d1[u] = ld4(p.aux1 + o + 4 * u);
-      d2[u] = ld4(p.aux0 + o + 4 * u);
-      q[u] = ld4(p.aux3 + o + 4 * u);
+      d1[u] = ld4(p.aux1 + of + 4 * u);
+      d2[u] = ld4(p.aux0 + of + 4 * u);
+      q[u] = ld4(p.aux3 + of + 4 * u);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      st4(out + 4 * u, make_float4(v[4 * u] * d1[u].x + q[u].x * d2[u].x, v[4 * u + 1] * d1[u].y + q[u].y * d2[u].y,
-                                   v[4 * u + 2] * d1[u].z + q[u].z * d2[u].z, v[4 * u + 3] * d1[u].w + q[u].w * d2[u].w));
+      o[u] = make_float4(v[4 * u] * d1[u].x + q[u].x * d2[u].x, v[4 * u + 1] * d1[u].y + q[u].y * d2[u].y,
+                         v[4 * u + 2] * d1[u].z + q[u].z * d2[u].z, v[4 * u + 3] * d1[u].w + q[u].w * d2[u].w);
   } else if (MODE == EPI_ORB_J) {
     const int pos = row / 3, t = row - 3 * pos;
     const float* env = p.aux1 + (long)node * 5 * p.ld_aux + col0;
     const bool self = p.dep_map[pos] == node;
-    float4 ex[4], raw[4], ej[4];
+    float4 ex[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) ex[u] = ld4(env + 4 * u);
     if (self) {
+      float4 raw[4], ej[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         raw[u] = ld4(p.aux3 + (long)node * p.ld_aux + col0 + 4 * u);
@@ -195,21 +217,19 @@ __device__ __forceinline__ void tc_epi16(const GemmP<float>& p, int row, int nod
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        st4(out + 4 * u, make_float4(raw[u].x * ej[u].x + ex[u].x * v[4 * u], raw[u].y * ej[u].y + ex[u].y * v[4 * u + 1],
-                                     raw[u].z * ej[u].z + ex[u].z * v[4 * u + 2],
-                                     raw[u].w * ej[u].w + ex[u].w * v[4 * u + 3]));
+        o[u] = make_float4(raw[u].x * ej[u].x + ex[u].x * v[4 * u], raw[u].y * ej[u].y + ex[u].y * v[4 * u + 1],
+                           raw[u].z * ej[u].z + ex[u].z * v[4 * u + 2], raw[u].w * ej[u].w + ex[u].w * v[4 * u + 3]);
         st4(p.aux2 + ((long)node * 3 + t) * p.ld_aux + col0 + 4 * u,
             make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]));
       }
     } else {
 #pragma unroll
       for (int u = 0; u < 4; ++u)
-        st4(out + 4 * u, make_float4(ex[u].x * v[4 * u], ex[u].y * v[4 * u + 1], ex[u].z * v[4 * u + 2],
-                                     ex[u].w * v[4 * u + 3]));
+        o[u] = make_float4(ex[u].x * v[4 * u], ex[u].y * v[4 * u + 1], ex[u].z * v[4 * u + 2], ex[u].w * v[4 * u + 3]);
     }
   } else {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) tc_store4<MODE>(p, row, node, col0 + 4 * u, v + 4 * u, spin);
+    for (int u = 0; u < 4; ++u) o[u] = tc_val4<MODE>(p, row, node, col0 + 4 * u, v + 4 * u, spin);
   }
 }
 
@@ -227,10 +247,14 @@ struct TcCfg {
   static constexpr int A_STAGE = 2 * A_BYTES;                    // hi + lo
   static constexpr int BK_BYTES = TCP_BN * TC_BK * 2;            // one BF16 plane of one resident k-tile
   static constexpr int B_BYTES = 2 * BK_BYTES * (TCP_KMAX / TC_BK);  // hi + lo, all k-tiles
-  static constexpr int TOTAL = B_BYTES + TCP_STAGES * A_STAGE + 256;
+  // epilogue staging for the TMA stores of C: [warp][2 buffers][32 rows][16 columns] float
+  static constexpr int STG_BYTES = 8 * 2 * 32 * 16 * 4;
+  static constexpr int STAGES = 2;  // A stages next to the resident weights
+  static constexpr int TOTAL = B_BYTES + STAGES * A_STAGE + STG_BYTES + 256;
   // streamed weights (K > TCP_KMAX): every stage carries its A and B k-tiles
   static constexpr int SB_STAGE = A_STAGE + 2 * BK_BYTES;
-  static constexpr int TOTAL_SB = TCP_STAGES * SB_STAGE + 256;
+  static constexpr int STAGES_SB = 3;
+  static constexpr int TOTAL_SB = STAGES_SB * SB_STAGE + STG_BYTES + 256;
 };
 
 struct TcBar {
@@ -259,15 +283,20 @@ __device__ __forceinline__ void tc_arrive(uint64_t* bar) {
 }
 
 // SB: the weights stream through the stages with A (any K % 8 == 0) instead of staying resident (K <= 256).
+// tma != 0: warps whose 32 rows all belong to the launch store full 16-column chunks of C through shared
+// memory with TMA (tensor map tmC over C, box 16 columns x 32 rows); other chunks use vector stores.
 template <int MODE, bool SB>
 __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, const __nv_bfloat16* Bhi,
                                                             const __nv_bfloat16* Blo, int spin_filter,
-                                                            const int* tile_mask, int32_t* status) {
+                                                            const int* tile_mask, int32_t* status,
+                                                            const __grid_constant__ CUtensorMap tmC, int tma) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   constexpr int STAGE = SB ? TcCfg::SB_STAGE : TcCfg::A_STAGE;
+  constexpr int NS = SB ? TcCfg::STAGES_SB : TcCfg::STAGES;
   unsigned char* bres = tc_smem;                                 // resident B: [k-tile][hi, lo][128 x 64]
   unsigned char* astage = tc_smem + (SB ? 0 : TcCfg::B_BYTES);   // [stage][A hi, A lo (, B hi, B lo)]
-  TcBar* bars = reinterpret_cast<TcBar*>(astage + TCP_STAGES * STAGE);
+  float* stg = reinterpret_cast<float*>(astage + NS * STAGE);    // epilogue staging
+  TcBar* bars = reinterpret_cast<TcBar*>(astage + NS * STAGE + TcCfg::STG_BYTES);
   volatile int* abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -297,7 +326,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
     *reinterpret_cast<uint4*>(bk + TcCfg::BK_BYTES + off) = l;
   }
   if (tid == 0) {
-    for (int s = 0; s < TCP_STAGES; ++s) {
+    for (int s = 0; s < NS; ++s) {
       mbar_init(smem_u32(&bars->full[s]), 128);
       mbar_init(smem_u32(&bars->empty[s]), 1);
     }
@@ -330,8 +359,8 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
       if (skip(m)) continue;
       const int m0 = m * TC_BM;
       for (int kt = 0; kt < nk; ++kt, ++kc) {
-        const int s = (int)(kc % TCP_STAGES);
-        const long use = kc / TCP_STAGES;
+        const int s = (int)(kc % NS);
+        const long use = kc / NS;
         if (use > 0 && !tc_wait(&bars->empty[s], (uint32_t)((use - 1) & 1), abort)) break;
         unsigned char* a_hi = astage + s * STAGE;
         unsigned char* a_lo = a_hi + TcCfg::A_BYTES;
@@ -396,8 +425,8 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
         tc_fence_after();
         const uint32_t acc_t = tmem + (uint32_t)(b * TCP_BN);
         for (int kt = 0; kt < nk; ++kt, ++kc) {
-          const int s = (int)(kc % TCP_STAGES);
-          if (!tc_wait(&bars->full[s], (uint32_t)((kc / TCP_STAGES) & 1), abort)) break;
+          const int s = (int)(kc % NS);
+          if (!tc_wait(&bars->full[s], (uint32_t)((kc / NS) & 1), abort)) break;
           tc_fence_after();
           const uint32_t ah = a0 + s * STAGE, al = ah + TcCfg::A_BYTES;
           const uint32_t bh = SB ? ah + TcCfg::A_STAGE : b0 + kt * 2 * TcCfg::BK_BYTES, bl = bh + TcCfg::BK_BYTES;
@@ -419,6 +448,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
     // ------------------------------------------------------------------ epilogue (warps 0-7, 256 threads)
     const int quad = warp & 3, half = warp >> 2;
     long uc = 0;
+    int nst = 0;  // TMA stores issued by this warp (lane 0 owns the bulk groups)
     for (int m = m_first; m < mt && !*abort; m += groups) {
       if (skip(m)) continue;
       const int m0 = m * TC_BM;
@@ -430,6 +460,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
       tc_fence_after();
       bool mine = valid && !(p.row_skip > 0 && row % p.row_skip == 0);
       if (mine && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
+      const bool tma_warp = tma != 0 && __all_sync(0xffffffffu, mine);
       const int prev = __shfl_up_sync(0xffffffffu, node, 1);
       const bool head = lane == 0 || prev != node;
       // rows of one center are consecutive: bit k of segm says lane + 2^k belongs to this lane's center
@@ -445,10 +476,28 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
       for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
         float v[16];
         tmem_ld16(base + (uint32_t)c0, v);
-        if (mine) {
-          const int spin = spin_filter < 0 ? 0 : spin_filter;
-          if (n0 + c0 + 15 < p.N) {
-            tc_epi16<MODE>(p, row, node, n0 + c0, v, spin);
+        const int spin = spin_filter < 0 ? 0 : spin_filter;
+        if (MODE != EPI_ENV && tma_warp && n0 + c0 + 15 < p.N) {
+          float4 o[4];
+          tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
+          float* sb = stg + (size_t)(warp * 2 + (nst & 1)) * 32 * 16;
+          if (lane == 0 && nst >= 2) tma_wait_read1();  // the store from this buffer two chunks ago has read it
+          __syncwarp();
+#pragma unroll
+          for (int u = 0; u < 4; ++u) *reinterpret_cast<float4*>(sb + lane * 16 + 4 * u) = o[u];
+          proxy_fence();
+          __syncwarp();
+          if (lane == 0) {
+            tma_store_2d(&tmC, smem_u32(sb), n0 + c0, m0 + quad * 32);
+            tma_commit();
+          }
+          ++nst;
+        } else if (mine) {
+          if (MODE != EPI_ENV && n0 + c0 + 15 < p.N) {
+            float4 o[4];
+            tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) st4(p.C + (long)row * p.ldc + n0 + c0 + 4 * u, o[u]);
           } else {
 #pragma unroll
             for (int j = 0; j < 16; j += 4) {
@@ -478,12 +527,13 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
       tc_arrive(&bars->tempty[b]);
       ++uc;
     }
+    if (lane == 0 && nst > 0) tma_wait_all();  // C written and the staging buffers read
   }
   __syncthreads();
   if (*abort && tid == 0) set_flag(status, FIRE_FLAG_TIMEOUT);
   if (*abort && warp == 12 && lane == 0) {
     // bounded drain: an MMA still in flight must finish before tensor memory is released
-    for (int s = 0; s < TCP_STAGES; ++s) {
+    for (int s = 0; s < NS; ++s) {
       const uint32_t a = smem_u32(&bars->empty[s]);
       for (int i = 0; i < (1 << 16); ++i) {
         uint32_t d0, d1;
@@ -523,9 +573,15 @@ __global__ void k_tile_mask(GemmP<float> p, int* mask) {
   if (threadIdx.x == 0) mask[m_tile] = up | (dn << 1);
 }
 
+// Tensor map over C for the TMA-store epilogue (box 16 columns x 32 rows); false if unavailable.
+bool tc_c_map(const GemmP<float>& p, CUtensorMap* map);
+
 template <int MODE>
 inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, int* mask_buf, int32_t* status,
                                   cudaStream_t s, int num_sms) {
+  CUtensorMap tmC;
+  std::memset(&tmC, 0, sizeof(tmC));
+  const int tma = (MODE != EPI_ENV && tc_c_map(p, &tmC)) ? 1 : 0;
   if (p.K > TCP_KMAX) {
     if (wt.hi2) return cudaErrorInvalidValue;
     constexpr int smem = TcCfg::TOTAL_SB;
@@ -534,7 +590,7 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
     const long mt = (p.M + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
     if (mt == 0 || nt == 0) return cudaSuccess;
     const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
-    k_gemm_tcp<MODE, true><<<(unsigned)(groups * nt), TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status);
+    k_gemm_tcp<MODE, true><<<(unsigned)(groups * nt), TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status, tmC, tma);
     return cudaPeekAtLastError();
   }
   const int smem = TcCfg::TOTAL;
@@ -547,10 +603,10 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
   if (wt.hi2) {
     if (!mask_buf) return cudaErrorInvalidValue;
     k_tile_mask<<<(unsigned)mt, TC_BM, 0, s>>>(p, mask_buf);
-    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, 0, mask_buf, status);
-    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi2, wt.lo2, 1, mask_buf, status);
+    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, 0, mask_buf, status, tmC, tma);
+    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi2, wt.lo2, 1, mask_buf, status, tmC, tma);
   } else {
-    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status);
+    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status, tmC, tma);
   }
   return cudaPeekAtLastError();
 }
