@@ -115,23 +115,26 @@ size_t elem_size(const fire_problem* p) { return p->precision == FIRE_PREC_FP64 
 // after the float slots of the prepared buffer: for each, hi [N][K] then lo [N][K].
 enum TcSlot {
   TC_UPD1, TC_UPD2, TC_ORB_UP, TC_ORB_DN, TC_V, TC_JMLP1, TC_JMLP2, TC_EI_GLU, TC_EI_DENSE, TC_EI_OUT,
-  TC_ENV_UP, TC_ENV_DN, TC_COUNT
+  TC_ENV_UP, TC_ENV_DN, TC_QK, TC_COUNT
 };
 struct TcSrc {
   int slot;  // prepared slot (already scaled), row-major [K][N] per matrix
   int kind;  // > 0: K = F, N = kind * F;  0: K = F, N = NDET * n_el (orbitals);
-             // -1: NDET matrices with K = 8 n_nuc, N = n_el (envelope weights per determinant)
+             // -1: NDET matrices with K = 8 n_nuc, N = n_el (envelope weights per determinant);
+             // -2: K = F, N = HEADS (attention logits)
 };
 const TcSrc kTcSrc[TC_COUNT] = {{PR_UPD1_W_S0, 1},   {FIRE_P_UPD2_W, 1},    {PR_ORB_UP_W_S1, 0},
                                 {PR_ORB_DN_W_S1, 0}, {PR_V_W_S1, 1},        {PR_JMLP1_W_S1, 1},
                                 {FIRE_P_JMLP2_W, 1}, {FIRE_P_EI_GLU_W, 2},  {FIRE_P_EI_DENSE_W, 1},
-                                {FIRE_P_EI_OUT_W, 5}, {PR_ENV_UP_PI, -1},   {PR_ENV_DN_PI, -1}};
+                                {FIRE_P_EI_OUT_W, 5}, {PR_ENV_UP_PI, -1},   {PR_ENV_DN_PI, -1},
+                                {PR_QK_W_S1, -2}};
 // K, N and the number of matrices of a slot; its BF16 copy is hi [cnt][N][K] followed by lo [cnt][N][K]
 void tc_shape(int k, const fire_problem* p, size_t* K, size_t* N, int* cnt) {
   const int kind = kTcSrc[k].kind;
-  *K = kind < 0 ? (size_t)NENV_ORB * p->n_nuc : (size_t)F;
-  *N = kind > 0 ? (size_t)kind * F : (kind == 0 ? (size_t)NDET * p->n_el : (size_t)p->n_el);
-  *cnt = kind < 0 ? NDET : 1;
+  *K = kind == -1 ? (size_t)NENV_ORB * p->n_nuc : (size_t)F;
+  *N = kind > 0 ? (size_t)kind * F
+                : (kind == 0 ? (size_t)NDET * p->n_el : (kind == -1 ? (size_t)p->n_el : (size_t)HEADS));
+  *cnt = kind == -1 ? NDET : 1;
 }
 // byte offsets of the BF16 region (tc_off[TC_COUNT] = end)
 void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
@@ -161,7 +164,7 @@ struct Plan {
   size_t E5a, Z1, E5o, HX, HL, HJ, B1X, B1L, B1J, B2X, B2L, B2J, Zx, Zx2, jsq;
   size_t env, rawx, rjs, Apl, lapA, Jorb, coef_up, coef_dn, Ainv, dgrad;
   size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, Zr2, jsqr;
-  size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, tile_mask;
+  size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, tile_mask, aD1, aD2, ajsq;
   // double
   size_t ld, sd, dlap, gjw;
   size_t total;
@@ -233,6 +236,9 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
   take(P.JMx, W * 2, es);
   if (fl) {
     take(P.aJ, Jr * HEADS, es);
+    take(P.aD1, G * HEADS, es);
+    take(P.aD2, G * HEADS, es);
+    take(P.ajsq, G * HEADS, es);
     take(P.aL, G * HEADS, es);
     take(P.Al, W * 2 * 272, es);
     take(P.AJ, W * 3 * n * 2 * 272, es);
@@ -711,11 +717,35 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
   const Planes B2{c.P.B2X, c.P.B2J, c.P.B2L}, B1{c.P.B1X, c.P.B1J, c.P.B1L}, H{c.P.HX, c.P.HJ, c.P.HL};
   Prof pr("jastrow", c.s);
   // attention logits exp(-(h W_Qk + b_Qk) / 4)
-  g_nlaunch++;
-  k_narrow<T, HEADS, 1, FLM><<<G, 256, 0, c.s>>>(
-      c.template buf<T>(B2.X), FLM ? c.template buf<T>(B2.J) : nullptr, FLM ? c.template buf<T>(B2.L) : nullptr,
-      c.nb, c.L, c.W.w[PR_QK_W_S1], c.W.w[PR_QK_B], nullptr, nullptr, c.template buf<T>(c.P.aX),
-      FLM ? c.template buf<T>(c.P.aJ) : nullptr, FLM ? c.template buf<T>(c.P.aL) : nullptr, c.status);
+  if (FLM && c.mixed) {
+    // mixed path: value rows and the activation derivatives on the CUDA cores, Jacobian and Laplacian rows
+    // as tensor-core contractions with the derivative-plane epilogues
+    g_nlaunch++;
+    k_narrow<T, HEADS, 1, false><<<G, 256, 0, c.s>>>(
+        c.template buf<T>(B2.X), nullptr, nullptr, c.nb, c.L, c.W.w[PR_QK_W_S1], c.W.w[PR_QK_B], nullptr, nullptr,
+        c.template buf<T>(c.P.aX), nullptr, nullptr, c.status, c.template buf<T>(c.P.aD1),
+        c.template buf<T>(c.P.aD2));
+    cudaMemsetAsync(c.template buf<T>(c.P.ajsq), 0, sizeof(T) * (size_t)G * HEADS, c.s);
+    GemmP<T> g = gp0<T>();
+    g.A = c.template buf<T>(B2.J); g.lda = F; g.B = c.W.w[PR_QK_W_S1]; g.ldb = HEADS;
+    g.C = c.template buf<T>(c.P.aJ); g.ldc = HEADS; g.M = Jcap; g.M_dev = Jdev; g.M_scale = 3; g.N = HEADS;
+    g.K = F; g.node_map = c.L.pos_ctr; g.node_div = 3; g.aux1 = c.template buf<T>(c.P.aD1);
+    g.aux2 = c.template buf<T>(c.P.ajsq); g.ld_aux = HEADS;
+    gemm<T, EPI_SILU_J>(c, g, TC_QK);
+    g = gp0<T>();
+    g.A = c.template buf<T>(B2.L); g.lda = F; g.B = c.W.w[PR_QK_W_S1]; g.ldb = HEADS;
+    g.C = c.template buf<T>(c.P.aL); g.ldc = HEADS; g.M = G; g.N = HEADS; g.K = F;
+    g.aux1 = c.template buf<T>(c.P.aD1); g.aux0 = c.template buf<T>(c.P.aD2);
+    g.aux3 = c.template buf<T>(c.P.ajsq); g.ld_aux = HEADS;
+    gemm<T, EPI_SILU_L>(c, g, TC_QK);
+  } else {
+    g_nlaunch++;
+    k_narrow<T, HEADS, 1, FLM><<<G, 256, 0, c.s>>>(
+        c.template buf<T>(B2.X), FLM ? c.template buf<T>(B2.J) : nullptr, FLM ? c.template buf<T>(B2.L) : nullptr,
+        c.nb, c.L, c.W.w[PR_QK_W_S1], c.W.w[PR_QK_B], nullptr, nullptr, c.template buf<T>(c.P.aX),
+        FLM ? c.template buf<T>(c.P.aJ) : nullptr, FLM ? c.template buf<T>(c.P.aL) : nullptr, c.status, nullptr,
+        nullptr);
+  }
   linear_layer<T>(c, FLM, B2, B1, c.W.w[PR_V_W_S1], c.W.w[FIRE_P_ATT_V_B], F, F, G, Jcap, Jdev, TC_V);
   cudaMemsetAsync(c.template buf<T>(c.P.Ax), 0, sizeof(T) * Wc * 2 * 272, c.s);
   if (FLM) cudaMemsetAsync(c.template buf<T>(c.P.Al), 0, sizeof(T) * Wc * 2 * 272, c.s);
@@ -778,7 +808,7 @@ cudaError_t stage_jastrow(Ctx<T>& c) {
       c.template buf<T>(H.X), FLM ? c.template buf<T>(H.J) : nullptr, FLM ? c.template buf<T>(H.L) : nullptr, c.nb,
       c.L, c.W.w[FIRE_P_JMLP3_W], c.W.w[FIRE_P_JMLP3_B], c.W.w[FIRE_P_MLP_SCALE], c.W.w[PR_SCALARS] + 1,
       c.template buf<T>(c.P.Xo2), FLM ? c.template buf<T>(c.P.Jo2) : nullptr,
-      FLM ? c.template buf<T>(c.P.Lo2) : nullptr, c.status);
+      FLM ? c.template buf<T>(c.P.Lo2) : nullptr, c.status, nullptr, nullptr);
   k_mlp_sum<T, FLM><<<Wc, 256, 0, c.s>>>(c.nb, c.L, c.template buf<T>(c.P.Xo2),
                                          FLM ? c.template buf<T>(c.P.Jo2) : nullptr,
                                          FLM ? c.template buf<T>(c.P.Lo2) : nullptr, c.template buf<T>(c.P.JMx),

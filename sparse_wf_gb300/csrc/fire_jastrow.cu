@@ -38,7 +38,8 @@ __global__ void __launch_bounds__(256) k_narrow(const T* __restrict__ X, const T
                                                 const T* __restrict__ Lp, Nbr nb, Layout L, const T* __restrict__ Wn,
                                                 const T* __restrict__ bn, const T* __restrict__ post_scale,
                                                 const T* __restrict__ post_shift, T* __restrict__ Xo,
-                                                T* __restrict__ Jo, T* __restrict__ Lo, int32_t* status) {
+                                                T* __restrict__ Jo, T* __restrict__ Lo, int32_t* status,
+                                                T* __restrict__ D1o, T* __restrict__ D2o) {
   // weights staged in shared memory (the FP64 validation build reads them through L1 instead, to stay
   // within the static shared-memory limit)
   constexpr bool kSmemW = sizeof(T) == 4;
@@ -93,6 +94,10 @@ __global__ void __launch_bounds__(256) k_narrow(const T* __restrict__ X, const T
     const T ps = post_scale ? post_scale[c] : T(1);
     const T sh = post_shift ? post_shift[c] : T(0);
     Xo[(size_t)g * NC + c] = f * ps + sh;
+    if (!FLM && D1o) {  // value mode: derivative planes for separately computed Jacobian / Laplacian rows
+      D1o[(size_t)g * NC + c] = f1 * ps;
+      D2o[(size_t)g * NC + c] = f2 * ps;
+    }
     if (FLM) {
       T jsq = T(0);
       for (int rr = 1; rr < nrows - 1; ++rr) {
@@ -442,13 +447,13 @@ __global__ void k_stats(const T* __restrict__ e, int B, double* __restrict__ out
 
 #define FIRE_INST_JAS(T)                                                                                         \
   template __global__ void k_narrow<T, 16, 1, true>(const T*, const T*, const T*, Nbr, Layout, const T*, const T*, \
-                                                    const T*, const T*, T*, T*, T*, int32_t*);                   \
+                                                    const T*, const T*, T*, T*, T*, int32_t*, T*, T*);                   \
   template __global__ void k_narrow<T, 16, 1, false>(const T*, const T*, const T*, Nbr, Layout, const T*,         \
-                                                     const T*, const T*, const T*, T*, T*, T*, int32_t*);        \
+                                                     const T*, const T*, const T*, T*, T*, T*, int32_t*, T*, T*);        \
   template __global__ void k_narrow<T, 2, 0, true>(const T*, const T*, const T*, Nbr, Layout, const T*, const T*,  \
-                                                   const T*, const T*, T*, T*, T*, int32_t*);                    \
+                                                   const T*, const T*, T*, T*, T*, int32_t*, T*, T*);                    \
   template __global__ void k_narrow<T, 2, 0, false>(const T*, const T*, const T*, Nbr, Layout, const T*, const T*, \
-                                                    const T*, const T*, T*, T*, T*, int32_t*);                   \
+                                                    const T*, const T*, T*, T*, T*, int32_t*, T*, T*);                   \
   template __global__ void k_mlp_sum<T, true>(Nbr, Layout, const T*, const T*, const T*, T*, T*, T*);             \
   template __global__ void k_mlp_sum<T, false>(Nbr, Layout, const T*, const T*, const T*, T*, T*, T*);            \
   template __global__ void k_att_sums<T, true>(Nbr, Layout, const T*, const T*, const T*, const T*, const T*,     \

@@ -43,7 +43,8 @@ constexpr int DL_CMAX_DECL = 64;
 // fire_jastrow.cu
 template <typename T, int NC, int ACT, bool FLM>
 __global__ void k_narrow(const T* X, const T* Jp, const T* Lp, Nbr nb, Layout L, const T* Wn, const T* bn,
-                         const T* post_scale, const T* post_shift, T* Xo, T* Jo, T* Lo, int32_t* status);
+                         const T* post_scale, const T* post_shift, T* Xo, T* Jo, T* Lo, int32_t* status, T* D1o,
+                         T* D2o);
 template <typename T, bool FLM>
 __global__ void k_mlp_sum(Nbr nb, Layout L, const T* Xo, const T* Jo, const T* Lo, T* ox, T* ol, T* oj);
 template <typename T, bool FLM>
