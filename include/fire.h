@@ -212,7 +212,8 @@ fire_status fire_profile_report(char* buf, size_t len);
 
 /* The mixed-precision tensor-core contraction alone: C[M, N] = A[M, K] W[K, N] (all float32, row-major,
  * device), computed with split-BF16 operands on tcgen05 (three BF16 products per element pair, FP32
- * accumulation).  workspace: >= 4 * N * K bytes (the split, transposed weights).  K % 8 == 0, N % 4 == 0
+ * accumulation).  workspace: the split weights, 32768 * ceil(N / 128) * ceil(K / 64) bytes for K <= 256,
+ * else 4 * N * K bytes.  K % 8 == 0, N % 4 == 0
  * and 16-byte aligned A and C (else FIRE_ERR_UNSUPPORTED); K > 256 streams the weights through the
  * pipeline instead of keeping them in shared memory. */
 fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const float* A, const float* W, float* C,

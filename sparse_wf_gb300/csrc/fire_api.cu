@@ -128,7 +128,9 @@ const TcSrc kTcSrc[TC_COUNT] = {{PR_UPD1_W_S0, 1},   {FIRE_P_UPD2_W, 1},    {PR_
                                 {FIRE_P_JMLP2_W, 1}, {FIRE_P_EI_GLU_W, 2},  {FIRE_P_EI_DENSE_W, 1},
                                 {FIRE_P_EI_OUT_W, 5}, {PR_ENV_UP_PI, -1},   {PR_ENV_DN_PI, -1},
                                 {PR_QK_W_S1, -2}};
-// K, N and the number of matrices of a slot; its BF16 copy is hi [cnt][N][K] followed by lo [cnt][N][K]
+// K, N and the number of matrices of a slot.  Its BF16 copy: for K <= 256 the pre-tiled split of every
+// matrix (tc_tiles_bytes each, for the A-resident kernel), else hi [cnt][N][K] followed by lo [cnt][N][K]
+// (for the streamed-weight kernel).
 void tc_shape(int k, const fire_problem* p, size_t* K, size_t* N, int* cnt) {
   const int kind = kTcSrc[k].kind;
   *K = kind == -1 ? (size_t)NENV_ORB * p->n_nuc : (size_t)F;
@@ -144,7 +146,7 @@ void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
     size_t K, N;
     int cnt;
     tc_shape(k, p, &K, &N, &cnt);
-    o += 2 * (size_t)cnt * N * K * sizeof(__nv_bfloat16);
+    o += K <= 256 ? (size_t)cnt * tc_tiles_bytes(K, N) : 2 * (size_t)cnt * N * K * sizeof(__nv_bfloat16);
     o = (o + 255) / 256 * 256;
   }
   off[TC_COUNT] = o;
@@ -619,8 +621,12 @@ cudaError_t env_gemm(Ctx<T>& c, const GemmP<T>& g, int NV, int tc_slot, int d) {
       size_t K, N;
       int cnt;
       tc_shape(tc_slot, c.p, &K, &N, &cnt);
-      const TcWeights wd{c.tcw[tc_slot].hi + (size_t)d * N * K, c.tcw[tc_slot].lo + (size_t)d * N * K, nullptr,
-                         nullptr};
+      TcWeights wd{};
+      if (K <= 256) wd.tiles = c.tcw[tc_slot].tiles + (size_t)d * tc_tiles_bytes(K, N) / 2;
+      else {
+        wd.hi = c.tcw[tc_slot].hi + (size_t)d * N * K;
+        wd.lo = c.tcw[tc_slot].lo + (size_t)d * N * K;
+      }
       GemmP<T> gt = g;
       gt.row_skip = NV;
       {
@@ -929,10 +935,10 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
       int cnt;
       tc_shape(k, p, &K, &N, &cnt);
       const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
-      c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr};
+      if (K <= 256) c.tcw[k] = TcWeights{nullptr, nullptr, nullptr, nullptr, hi, nullptr};
+      else c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr, nullptr, nullptr};
     }
-    c.tcw[TC_ORB_UP].hi2 = c.tcw[TC_ORB_DN].hi;
-    c.tcw[TC_ORB_UP].lo2 = c.tcw[TC_ORB_DN].lo;
+    c.tcw[TC_ORB_UP].tiles2 = c.tcw[TC_ORB_DN].tiles;
   }
   return c;
 }
@@ -1088,9 +1094,10 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
     __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(base + to[k]);
     __nv_bfloat16* lo = hi + (size_t)cnt * N * K;
     for (int m = 0; m < cnt; ++m) {
+      const float* src = reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot] + (size_t)m * K * N;
       g_nlaunch++;
-      split_transpose(reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot] + (size_t)m * K * N, (int)K,
-                      (int)N, hi + (size_t)m * N * K, lo + (size_t)m * N * K, s);
+      if (K <= 256) split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s);
+      else split_transpose(src, (int)K, (int)N, hi + (size_t)m * N * K, lo + (size_t)m * N * K, s);
     }
   }
   return launch_status(__func__);
@@ -1233,15 +1240,23 @@ fire_status fire_potential_energy(void* stream, const fire_problem* prob, const 
 fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const float* A, const float* W, float* C,
                             void* workspace, size_t workspace_bytes, int32_t* status) {
   if (M < 1 || N < 1 || K < 8 || K % 8 != 0 || !A || !W || !C || !workspace) return FIRE_ERR_INVALID;
-  if (workspace_bytes < 4 * (size_t)N * K) return FIRE_ERR_WORKSPACE;
+  const size_t need = K <= 256 ? tc_tiles_bytes(K, N) : 4 * (size_t)N * K;
+  if (workspace_bytes < need) return FIRE_ERR_WORKSPACE;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(workspace);
   g_nlaunch += 2;
-  split_transpose(W, K, N, hi, hi + (size_t)N * K, s);
+  TcWeights wt{};
+  if (K <= 256) {
+    split_tiles(W, K, N, hi, s);
+    wt.tiles = hi;
+  } else {
+    split_transpose(W, K, N, hi, hi + (size_t)N * K, s);
+    wt.hi = hi;
+    wt.lo = hi + (size_t)N * K;
+  }
   GemmP<float> g;
   std::memset(&g, 0, sizeof(g));
   g.A = A; g.lda = K; g.C = C; g.ldc = N; g.M = M; g.N = N; g.K = K; g.node_div = 1; g.M_scale = 1; g.env_nv = 1;
-  TcWeights wt{hi, hi + (size_t)N * K, nullptr, nullptr};
   const cudaError_t e = gemm_tc(EPI_PLAIN, N > 128 ? 256 : 128, g, wt, nullptr, status, s);
   if (e == cudaErrorInvalidValue) return FIRE_ERR_UNSUPPORTED;
   return launch_status(__func__);

@@ -36,11 +36,15 @@ struct Layout {
 // Split-BF16 weights of a tensor-core contraction: hi/lo planes [N][K] (K contiguous); the second set
 // (spin-down weights of the orbital layer) may be null.
 struct TcWeights {
-  const __nv_bfloat16* hi;
+  const __nv_bfloat16* hi;  // split weights transposed [N][K] (hi, lo): the streamed-weight kernel (K > 256)
   const __nv_bfloat16* lo;
-  const __nv_bfloat16* hi2;
+  const __nv_bfloat16* hi2;  // the other spin's weights (orbitals), or nullptr
   const __nv_bfloat16* lo2;
+  const __nv_bfloat16* tiles;   // split weights pre-tiled for the A-resident kernel (K <= 256)
+  const __nv_bfloat16* tiles2;  // the other spin's tiles, or nullptr
 };
+// bytes of the pre-tiled split weights of a K x N matrix: 32 KB per 128-column x 64-deep tile
+inline size_t tc_tiles_bytes(size_t K, size_t N) { return ((N + 127) / 128) * ((K + 63) / 64) * 32768; }
 
 // Output pointers of the per-walker assembly (k_assemble).
 struct AssembleOut {

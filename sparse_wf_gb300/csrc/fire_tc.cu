@@ -18,6 +18,29 @@ __global__ void k_split_transpose(const float* __restrict__ W, int K, int N, __n
   lo[idx] = __float2bfloat16_rn(w - __bfloat162float(h));
 }
 
+// hi/lo split of W[K][N] into tiles of 128 columns x 64 K: tile (j, kb) at block j * ceil(K / 64) + kb holds the
+// hi plane then the lo plane, each [8 k-groups][128 columns][8 k] (zero padding beyond N and K)
+__global__ void k_split_tiles(const float* __restrict__ W, int K, int N, __nv_bfloat16* __restrict__ Bt) {
+  const int nkt = (K + 63) / 64, nnt = (N + 127) / 128;
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over (block, g, r, e)
+  if (idx >= (long)nnt * nkt * 8192) return;
+  const long blk = idx >> 13;
+  const int w = (int)(idx & 8191), g = w >> 10, r = (w >> 3) & 127, e = w & 7;
+  const int j = (int)(blk / nkt), kb = (int)(blk % nkt);
+  const int n = j * 128 + r, k = kb * 64 + g * 8 + e;
+  const float v = (n < N && k < K) ? W[(long)k * N + n] : 0.f;
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  __nv_bfloat16* base = Bt + blk * 16384;
+  base[w] = h;
+  base[8192 + w] = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s) {
+  const long tot = (long)((N + 127) / 128) * ((K + 63) / 64) * 8192;
+  k_split_tiles<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, Bt);
+  return cudaPeekAtLastError();
+}
+
 cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __nv_bfloat16* lo, cudaStream_t s) {
   const long tot = (long)N * K;
   k_split_transpose<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, hi, lo);

@@ -26,6 +26,7 @@ namespace fire {
 constexpr int TC_BM = 128, TC_BK = 64, TC_THREADS = 256;
 constexpr uint32_t TC_LBO = 128, TC_SBO = 1024;
 constexpr long TC_SPIN_LIMIT = 1L << 22;
+constexpr int TCP_THREADS = 416, TCP_BN = 128, TCP_KMAX = 256, TCP_STAGES = 3;
 
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -39,6 +40,17 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
   d |= (uint64_t)((TC_SBO >> 4) & 0x3FFF) << 32;
   d |= (uint64_t)1 << 46;  // descriptor version for sm_100-family tensor cores
   // base offset 0, relative LBO mode, swizzle none (bits 61-63 = 0)
+  return d;
+}
+
+// K-major no-swizzle descriptor with explicit byte strides between core matrices along K (lbo) and along
+// M / N (sbo)
+__device__ __forceinline__ uint64_t tc_desc_s(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
   return d;
 }
 
@@ -91,6 +103,14 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, uint32_t sr
 __device__ __forceinline__ void tma_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void tma_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void tma_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// one contiguous global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16) completing on an
+// mbarrier that expects its bytes
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
@@ -233,6 +253,86 @@ __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int nod
   }
 }
 
+// Epilogue of one 128-row x 128-column accumulator tile (rows [m0, m0 + 128), columns [n0, n0 + 128)) held
+// in tensor memory at column tacc.  Called by the 8 epilogue warps: warp w reads TMEM lane quadrant w % 4
+// (rows m0 + 32 (w % 4) + lane) and column half w / 4.  Whole-warp full 16-column chunks go out through the
+// shared staging buffers stg with TMA (tma != 0), the rest with vector / scalar stores; nst counts this
+// warp's TMA stores (lane 0 owns their bulk groups).
+template <int MODE>
+__device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows, int m0, int n0, uint32_t tacc,
+                                                 int spin_filter, int tma, const CUtensorMap* tmC, float* stg,
+                                                 int& nst, int warp, int lane) {
+  const int quad = warp & 3, half = warp >> 2;
+  const int row = m0 + quad * 32 + lane;
+  const bool valid = row < rows;
+  const int node = valid ? gemm_node(p, row) : -1;
+  bool mine = valid && !(p.row_skip > 0 && row % p.row_skip == 0);
+  if (mine && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
+  const bool tma_warp = tma != 0 && __all_sync(0xffffffffu, mine);
+  const int prev = __shfl_up_sync(0xffffffffu, node, 1);
+  const bool head = lane == 0 || prev != node;
+  // rows of one center are consecutive: bit k of segm says lane + 2^k belongs to this lane's center
+  unsigned segm = 0;
+  if (MODE == EPI_SILU_J) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const int nu = __shfl_down_sync(0xffffffffu, node, 1 << k);
+      if (lane + (1 << k) < 32 && nu == node) segm |= 1u << k;
+    }
+  }
+  const uint32_t base = tacc + ((uint32_t)(quad * 32) << 16);
+  for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
+    float v[16];
+    tmem_ld16(base + (uint32_t)c0, v);
+    const int spin = spin_filter < 0 ? 0 : spin_filter;
+    if (MODE != EPI_ENV && tma_warp && n0 + c0 + 15 < p.N) {
+      float4 o[4];
+      tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
+      float* sb = stg + (size_t)(warp * 2 + (nst & 1)) * 32 * 16;
+      if (lane == 0 && nst >= 2) tma_wait_read1();  // the store from this buffer two chunks ago has read it
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) *reinterpret_cast<float4*>(sb + lane * 16 + 4 * u) = o[u];
+      proxy_fence();
+      __syncwarp();
+      if (lane == 0) {
+        tma_store_2d(tmC, smem_u32(sb), n0 + c0, m0 + quad * 32);
+        tma_commit();
+      }
+      ++nst;
+    } else if (mine) {
+      if (MODE != EPI_ENV && n0 + c0 + 15 < p.N) {
+        float4 o[4];
+        tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) st4(p.C + (long)row * p.ldc + n0 + c0 + 4 * u, o[u]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; j += 4) {
+          const int col = n0 + c0 + j;
+          if (col + 3 < p.N) tc_store4<MODE>(p, row, node, col, v + j, spin);
+          else
+            for (int e = 0; e < 4; ++e)
+              if (col + e < p.N) gemm_store<float, MODE>(p, row, col + e, v[j + e], spin);
+        }
+      }
+    }
+    if (MODE == EPI_SILU_J) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        float q = valid ? v[j] * v[j] : 0.f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const float u = __shfl_down_sync(0xffffffffu, q, 1 << k);
+          if ((segm >> k) & 1u) q += u;
+        }
+        const int col = n0 + c0 + j;
+        if (valid && head && col < p.N) atomicAdd(&p.aux2[(long)node * p.ld_aux + col], q);
+      }
+    }
+  }
+}
+
 // ----------------------------------------------------------------------------- persistent kernel
 // Each CTA owns one 128-column slice of the output (n_tile = blockIdx.x % nt) and keeps the split
 // weights of that slice resident in shared memory (K <= 256: 128 KB); it walks the 128-row tiles
@@ -241,7 +341,6 @@ __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int nod
 // warps 8-11 loaders, warp 12 lane 0 issues the MMAs; TMEM holds two 128-column accumulators so the
 // epilogue of one tile overlaps the MMAs of the next.  spin_filter >= 0 restricts the launch to the rows
 // of one spin (the orbital layer runs once per spin with that spin's weights).
-constexpr int TCP_THREADS = 416, TCP_BN = 128, TCP_KMAX = 256, TCP_STAGES = 3;
 struct TcCfg {
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;              // one BF16 plane of an A stage
   static constexpr int A_STAGE = 2 * A_BYTES;                    // hi + lo
@@ -446,83 +545,16 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
     }
   } else {
     // ------------------------------------------------------------------ epilogue (warps 0-7, 256 threads)
-    const int quad = warp & 3, half = warp >> 2;
     long uc = 0;
     int nst = 0;  // TMA stores issued by this warp (lane 0 owns the bulk groups)
     for (int m = m_first; m < mt && !*abort; m += groups) {
       if (skip(m)) continue;
       const int m0 = m * TC_BM;
-      const int row = m0 + quad * 32 + lane;
-      const bool valid = row < rows;
-      const int node = valid ? gemm_node(p, row) : -1;
       const int b = (int)(uc & 1);
       if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
       tc_fence_after();
-      bool mine = valid && !(p.row_skip > 0 && row % p.row_skip == 0);
-      if (mine && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
-      const bool tma_warp = tma != 0 && __all_sync(0xffffffffu, mine);
-      const int prev = __shfl_up_sync(0xffffffffu, node, 1);
-      const bool head = lane == 0 || prev != node;
-      // rows of one center are consecutive: bit k of segm says lane + 2^k belongs to this lane's center
-      unsigned segm = 0;
-      if (MODE == EPI_SILU_J) {
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          const int nu = __shfl_down_sync(0xffffffffu, node, 1 << k);
-          if (lane + (1 << k) < 32 && nu == node) segm |= 1u << k;
-        }
-      }
-      const uint32_t base = tmem + (uint32_t)(b * TCP_BN) + ((uint32_t)(quad * 32) << 16);
-      for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
-        float v[16];
-        tmem_ld16(base + (uint32_t)c0, v);
-        const int spin = spin_filter < 0 ? 0 : spin_filter;
-        if (MODE != EPI_ENV && tma_warp && n0 + c0 + 15 < p.N) {
-          float4 o[4];
-          tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
-          float* sb = stg + (size_t)(warp * 2 + (nst & 1)) * 32 * 16;
-          if (lane == 0 && nst >= 2) tma_wait_read1();  // the store from this buffer two chunks ago has read it
-          __syncwarp();
-#pragma unroll
-          for (int u = 0; u < 4; ++u) *reinterpret_cast<float4*>(sb + lane * 16 + 4 * u) = o[u];
-          proxy_fence();
-          __syncwarp();
-          if (lane == 0) {
-            tma_store_2d(&tmC, smem_u32(sb), n0 + c0, m0 + quad * 32);
-            tma_commit();
-          }
-          ++nst;
-        } else if (mine) {
-          if (MODE != EPI_ENV && n0 + c0 + 15 < p.N) {
-            float4 o[4];
-            tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
-#pragma unroll
-            for (int u = 0; u < 4; ++u) st4(p.C + (long)row * p.ldc + n0 + c0 + 4 * u, o[u]);
-          } else {
-#pragma unroll
-            for (int j = 0; j < 16; j += 4) {
-              const int col = n0 + c0 + j;
-              if (col + 3 < p.N) tc_store4<MODE>(p, row, node, col, v + j, spin);
-              else
-                for (int e = 0; e < 4; ++e)
-                  if (col + e < p.N) gemm_store<float, MODE>(p, row, col + e, v[j + e], spin);
-            }
-          }
-        }
-        if (MODE == EPI_SILU_J) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            float q = valid ? v[j] * v[j] : 0.f;
-#pragma unroll
-            for (int k = 0; k < 5; ++k) {
-              const float u = __shfl_down_sync(0xffffffffu, q, 1 << k);
-              if ((segm >> k) & 1u) q += u;
-            }
-            const int col = n0 + c0 + j;
-            if (valid && head && col < p.N) atomicAdd(&p.aux2[(long)node * p.ld_aux + col], q);
-          }
-        }
-      }
+      tc_epilogue_tile<MODE>(p, rows, m0, n0, tmem + (uint32_t)(b * TCP_BN), spin_filter, tma, &tmC, stg, nst, warp,
+                             lane);
       tc_fence_before();
       tc_arrive(&bars->tempty[b]);
       ++uc;
@@ -535,6 +567,242 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
     // bounded drain: an MMA still in flight must finish before tensor memory is released
     for (int s = 0; s < NS; ++s) {
       const uint32_t a = smem_u32(&bars->empty[s]);
+      for (int i = 0; i < (1 << 16); ++i) {
+        uint32_t d0, d1;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d0)
+            : "r"(a)
+            : "memory");
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 1;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d1)
+            : "r"(a)
+            : "memory");
+        if (d0 || d1) break;
+      }
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 12) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TCP_BN));
+  }
+}
+
+// ----------------------------------------------------------------------------- A-resident kernel (K <= 256)
+// Each CTA walks its 128-row tiles m = blockIdx.x, + gridDim.x, ... and, for each, every 128-column tile of
+// the output: the split A tile (hi, lo, all of K) stays in shared memory and is converted once per row tile,
+// while the split weights stream through a 2-stage ring by bulk copies of pre-tiled 32 KB blocks (one
+// 128-column x 64-deep tile, hi and lo planes, already in the canonical K-major layout: k-groups 2048 bytes
+// apart, 8-row groups 128 bytes apart).  A is a ring of 64-deep blocks: block kb is released once the MMAs of
+// the last column tile have read it, so the next row tile's conversion overlaps the current tile's tail.
+// Warp roles: 0-7 epilogue, 8-11 A converters, 12 (lane 0) MMA issuer, 13 (lane 0) weight loader.
+constexpr int TCA_THREADS = 448, TCA_KB = 4, TCA_BSTAGES = 2;
+struct TcaCfg {
+  static constexpr int A_BYTES = TC_BM * TC_BK * 2;  // one BF16 plane of a 128 x 64 block
+  static constexpr int A_BLOCK = 2 * A_BYTES;        // hi + lo
+  static constexpr int B_BLOCK = 2 * TCP_BN * TC_BK * 2;  // one tiled weight block (hi + lo)
+  static constexpr int STG_BYTES = TcCfg::STG_BYTES;
+  static constexpr int TOTAL = TCA_KB * A_BLOCK + TCA_BSTAGES * B_BLOCK + STG_BYTES + 256;
+};
+struct TcaBar {
+  uint64_t afull[TCA_KB], aempty[TCA_KB], bfull[TCA_BSTAGES], bempty[TCA_BSTAGES], tfull[2], tempty[2];
+  uint32_t tmem;
+  int abort;
+};
+
+// Bt: tiled weights [ceil(N / 128)][ceil(K / 64)] blocks of TcaCfg::B_BLOCK bytes
+template <int MODE>
+__global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, const __nv_bfloat16* Bt, int spin_filter,
+                                                            const int* tile_mask, int32_t* status,
+                                                            const __grid_constant__ CUtensorMap tmC, int tma) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  unsigned char* ares = tc_smem;                                   // [kb][hi, lo][128 x 64], LBO 128, SBO 1024
+  unsigned char* bst = tc_smem + TCA_KB * TcaCfg::A_BLOCK;         // [stage][hi, lo][8 k-groups][128 rows][16 B]
+  float* stg = reinterpret_cast<float*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK);
+  TcaBar* bars = reinterpret_cast<TcaBar*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK + TcaCfg::STG_BYTES);
+  volatile int* abort = &bars->abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  int rows = p.M;
+  if (p.M_dev) rows = min(rows, p.M_scale * (*p.M_dev));
+  const int mt = (rows + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
+  const int nk = (p.K + TC_BK - 1) / TC_BK;  // <= TCA_KB
+  if ((int)blockIdx.x >= mt) return;
+  auto skip = [&](int m) -> bool { return spin_filter >= 0 && !((tile_mask[m] >> spin_filter) & 1); };
+
+  if (tid == 0) {
+    for (int k = 0; k < TCA_KB; ++k) {
+      mbar_init(smem_u32(&bars->afull[k]), 128);
+      mbar_init(smem_u32(&bars->aempty[k]), 1);
+    }
+    for (int s2 = 0; s2 < TCA_BSTAGES; ++s2) {
+      mbar_init(smem_u32(&bars->bfull[s2]), 1);
+      mbar_init(smem_u32(&bars->bempty[s2]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&bars->tfull[b]), 1);
+      mbar_init(smem_u32(&bars->tempty[b]), 256);
+    }
+    bars->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 12) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem)),
+                 "r"(2 * TCP_BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  proxy_fence();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = bars->tmem;
+  long bc_issued = 0;  // weight blocks issued (loader lane)
+
+  if (warp >= 8 && warp < 12) {
+    // ------------------------------------------------------------------ A converters (128 threads)
+    const int lt = tid - 256, lw = lt >> 5, r8 = lane & 7, kq = lane >> 3;
+    long ua = 0;
+    for (int m = blockIdx.x; m < mt && !*abort; m += gridDim.x) {
+      if (skip(m)) continue;
+      const int m0 = m * TC_BM;
+      for (int kb = 0; kb < nk; ++kb) {
+        if (ua > 0 && !tc_wait(&bars->aempty[kb], (uint32_t)((ua - 1) & 1), abort)) break;
+        unsigned char* a_hi = ares + kb * TcaCfg::A_BLOCK;
+        unsigned char* a_lo = a_hi + TcaCfg::A_BYTES;
+        const int k0 = kb * TC_BK;
+        float4 v[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int blk = lw + 4 * u;
+          const int r = (blk >> 2) * 8 + r8, kk = (blk & 3) * 16 + kq * 4;
+          const int gr = m0 + r, gk = k0 + kk;
+          v[u] = (gr < rows && gk < p.K) ? ld4(p.A + (long)gr * p.lda + gk) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int blk = lw + 4 * u;
+          const int r = (blk >> 2) * 8 + r8, kk = (blk & 3) * 16 + kq * 4;
+          const float f[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+          uint32_t hw[2], lw2[2];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const __nv_bfloat16 h0 = __float2bfloat16_rn(f[2 * e]), h1 = __float2bfloat16_rn(f[2 * e + 1]);
+            const __nv_bfloat16 l0 = __float2bfloat16_rn(f[2 * e] - __bfloat162float(h0));
+            const __nv_bfloat16 l1 = __float2bfloat16_rn(f[2 * e + 1] - __bfloat162float(h1));
+            hw[e] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+            lw2[e] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+          }
+          const uint32_t off = tc_off(r, kk);
+          *reinterpret_cast<uint2*>(a_hi + off) = make_uint2(hw[0], hw[1]);
+          *reinterpret_cast<uint2*>(a_lo + off) = make_uint2(lw2[0], lw2[1]);
+        }
+        proxy_fence();
+        tc_arrive(&bars->afull[kb]);
+      }
+      ++ua;
+    }
+  } else if (warp == 13) {
+    // ------------------------------------------------------------------ weight loader
+    if (lane == 0) {
+      long bc = 0;
+      for (int m = blockIdx.x; m < mt && !*abort; m += gridDim.x) {
+        if (skip(m)) continue;
+        for (int j = 0; j < nt && !*abort; ++j)
+          for (int kb = 0; kb < nk; ++kb, ++bc) {
+            const int s2 = (int)(bc % TCA_BSTAGES);
+            const long use = bc / TCA_BSTAGES;
+            if (use > 0 && !tc_wait(&bars->bempty[s2], (uint32_t)((use - 1) & 1), abort)) break;
+            const unsigned char* src = reinterpret_cast<const unsigned char*>(Bt) +
+                                       ((size_t)j * nk + kb) * (size_t)TcaCfg::B_BLOCK;
+            bulk_load(smem_u32(bst + s2 * TcaCfg::B_BLOCK), src, TcaCfg::B_BLOCK, smem_u32(&bars->bfull[s2]));
+            bc_issued = bc + 1;
+          }
+      }
+    }
+  } else if (warp == 12) {
+    // ------------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc<TCP_BN>();
+      const uint32_t a0 = smem_u32(ares), b0 = smem_u32(bst);
+      long ua = 0, bc = 0, uc = 0;
+      for (int m = blockIdx.x; m < mt && !*abort; m += gridDim.x) {
+        if (skip(m)) continue;
+        for (int j = 0; j < nt && !*abort; ++j) {
+          const int b = (int)(uc & 1);
+          const long ub = uc >> 1;
+          if (ub > 0 && !tc_wait(&bars->tempty[b], (uint32_t)((ub - 1) & 1), abort)) break;
+          tc_fence_after();
+          const uint32_t acc_t = tmem + (uint32_t)(b * TCP_BN);
+          for (int kb = 0; kb < nk; ++kb, ++bc) {
+            if (j == 0 && !tc_wait(&bars->afull[kb], (uint32_t)(ua & 1), abort)) break;
+            const int s2 = (int)(bc % TCA_BSTAGES);
+            if (!tc_wait(&bars->bfull[s2], (uint32_t)((bc / TCA_BSTAGES) & 1), abort)) break;
+            tc_fence_after();
+            const uint32_t ah = a0 + kb * TcaCfg::A_BLOCK, al = ah + TcaCfg::A_BYTES;
+            const uint32_t bh = b0 + s2 * TcaCfg::B_BLOCK, bl = bh + TcaCfg::B_BLOCK / 2;
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; ++kk) {
+              const uint32_t sa = kk * 2 * TC_LBO, sb = kk * 2 * 2048;
+              const uint64_t dah = tc_desc(ah + sa), dal = tc_desc(al + sa);
+              const uint64_t dbh = tc_desc_s(bh + sb, 2048, 128), dbl = tc_desc_s(bl + sb, 2048, 128);
+              tc_mma(acc_t, dah, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+              tc_mma(acc_t, dah, dbl, idesc, 1u);
+              tc_mma(acc_t, dal, dbh, idesc, 1u);
+            }
+            tc_commit(smem_u32(&bars->bempty[s2]));
+            if (j == nt - 1) tc_commit(smem_u32(&bars->aempty[kb]));
+          }
+          if (*abort) break;
+          tc_commit(smem_u32(&bars->tfull[b]));
+          ++uc;
+        }
+        ++ua;
+      }
+    }
+  } else {
+    // ------------------------------------------------------------------ epilogue (warps 0-7, 256 threads)
+    long uc = 0;
+    int nst = 0;
+    for (int m = blockIdx.x; m < mt && !*abort; m += gridDim.x) {
+      if (skip(m)) continue;
+      const int m0 = m * TC_BM;
+      for (int j = 0; j < nt && !*abort; ++j) {
+        const int b = (int)(uc & 1);
+        if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
+        tc_fence_after();
+        tc_epilogue_tile<MODE>(p, rows, m0, j * TCP_BN, tmem + (uint32_t)(b * TCP_BN), spin_filter, tma, &tmC, stg,
+                               nst, warp, lane);
+        tc_fence_before();
+        tc_arrive(&bars->tempty[b]);
+        ++uc;
+      }
+    }
+    if (lane == 0 && nst > 0) tma_wait_all();
+  }
+  __syncthreads();
+  if (*abort && tid == 0) set_flag(status, FIRE_FLAG_TIMEOUT);
+  if (*abort && warp == 13 && lane == 0) {
+    // bounded drain: weight copies still in flight must land before the CTA's shared memory goes away
+    for (long q = bc_issued > TCA_BSTAGES ? bc_issued - TCA_BSTAGES : 0; q < bc_issued; ++q) {
+      const uint32_t a = smem_u32(&bars->bfull[q % TCA_BSTAGES]);
+      const uint32_t par = (uint32_t)((q / TCA_BSTAGES) & 1);
+      for (int i = 0; i < (1 << 16); ++i) {
+        uint32_t d0;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d0)
+            : "r"(a), "r"(par)
+            : "memory");
+        if (d0) break;
+      }
+    }
+  }
+  if (*abort && warp == 12 && lane == 0) {
+    // bounded drain: an MMA still in flight must finish before tensor memory is released
+    for (int s2 = 0; s2 < TCA_BSTAGES; ++s2) {
+      const uint32_t a = smem_u32(&bars->bempty[s2]);
       for (int i = 0; i < (1 << 16); ++i) {
         uint32_t d0, d1;
         asm volatile(
@@ -582,6 +850,24 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
   CUtensorMap tmC;
   std::memset(&tmC, 0, sizeof(tmC));
   const int tma = (MODE != EPI_ENV && tc_c_map(p, &tmC)) ? 1 : 0;
+  if (p.K <= TCP_KMAX) {  // A-resident kernel with pre-tiled weights
+    if (!wt.tiles) return cudaErrorInvalidValue;
+    constexpr int smem = TcaCfg::TOTAL;
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tca<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const long mt = (p.M + TC_BM - 1) / TC_BM;
+    if (mt == 0 || p.N == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)std::min<long>(mt, num_sms);
+    if (wt.tiles2) {
+      if (!mask_buf) return cudaErrorInvalidValue;
+      k_tile_mask<<<(unsigned)mt, TC_BM, 0, s>>>(p, mask_buf);
+      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles, 0, mask_buf, status, tmC, tma);
+      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles2, 1, mask_buf, status, tmC, tma);
+    } else {
+      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles, -1, nullptr, status, tmC, tma);
+    }
+    return cudaPeekAtLastError();
+  }
   if (p.K > TCP_KMAX) {
     if (wt.hi2) return cudaErrorInvalidValue;
     constexpr int smem = TcCfg::TOTAL_SB;

@@ -15,7 +15,7 @@ def test_gemm_mixed_matches_fp64(cuda_lib, M, N, K):
     A = torch.randn(M, K, device="cuda", generator=g, dtype=torch.float32)
     W = torch.randn(K, N, device="cuda", generator=g, dtype=torch.float32) / K**0.5
     Cm = torch.full((M, N), float("nan"), device="cuda")
-    ws = torch.empty(4 * N * K, dtype=torch.uint8, device="cuda")
+    ws = torch.empty(max(4 * N * K, 32768 * -(-N // 128) * -(-K // 64)), dtype=torch.uint8, device="cuda")
     status = torch.zeros(8, dtype=torch.int32, device="cuda")
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     rc = cuda_lib.fire_gemm_mixed(s, M, N, K, C.c_void_p(A.data_ptr()), C.c_void_p(W.data_ptr()),
@@ -39,7 +39,7 @@ def test_gemm_mixed_rejects_unaligned_rows(cuda_lib):
     A = torch.randn(M, K, device="cuda")
     W = torch.randn(K, N, device="cuda")
     Cm = torch.full((M, N), float("nan"), device="cuda")
-    ws = torch.empty(4 * N * K, dtype=torch.uint8, device="cuda")
+    ws = torch.empty(max(4 * N * K, 32768 * -(-N // 128) * -(-K // 64)), dtype=torch.uint8, device="cuda")
     status = torch.zeros(8, dtype=torch.int32, device="cuda")
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     rc = cuda_lib.fire_gemm_mixed(s, M, N, K, C.c_void_p(A.data_ptr()), C.c_void_p(W.data_ptr()),
