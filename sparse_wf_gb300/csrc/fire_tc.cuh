@@ -8,10 +8,12 @@
 // tensor memory:  a_hi b_hi + a_hi b_lo + a_lo b_hi  (relative error ~2^-17 per product instead of
 // BF16's 2^-9).
 //
-// Tile: 128 rows (TMEM lanes) x BN columns, K staged 64 deep, two shared-memory stages.  Shared memory
-// uses the canonical K-major layout without swizzle: 8-row x 16-byte core matrices, K-adjacent core
-// matrices LBO = 128 bytes apart, 8-row groups SBO = 1024 bytes apart.  One thread issues the MMAs and
-// commits them to an mbarrier per stage; all waits are bounded and report FIRE_FLAG_TIMEOUT.
+// Two kernels share the epilogues: k_gemm_tca (K <= 256; the A tile stays in shared memory, the pre-tiled
+// weights stream in by bulk copies) and k_gemm_tcs (K > 256; A and weight k-tiles stream together).  Tiles
+// are 128 rows (TMEM lanes) x 128 columns, K staged 64 deep, in the canonical K-major layout without
+// swizzle (8-row x 16-byte core matrices; A: K-adjacent core matrices 128 bytes apart, 8-row groups 1024
+// bytes apart; pre-tiled weights: 2048 and 128 bytes).  One thread issues the MMAs and commits them to
+// mbarriers; every wait is bounded and reports FIRE_FLAG_TIMEOUT.
 #pragma once
 #include <cuda.h>
 
@@ -23,7 +25,7 @@
 
 namespace fire {
 
-constexpr int TC_BM = 128, TC_BK = 64, TC_THREADS = 256;
+constexpr int TC_BM = 128, TC_BK = 64;
 constexpr uint32_t TC_LBO = 128, TC_SBO = 1024;
 constexpr long TC_SPIN_LIMIT = 1L << 22;
 constexpr int TCP_THREADS = 416, TCP_BN = 128, TCP_KMAX = 256, TCP_STAGES = 3;
@@ -67,18 +69,6 @@ __device__ __forceinline__ uint32_t tc_idesc() {
 
 __device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count));
-}
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
-  for (long i = 0; i < TC_SPIN_LIMIT; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
@@ -333,25 +323,20 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
   }
 }
 
-// ----------------------------------------------------------------------------- persistent kernel
-// Each CTA owns one 128-column slice of the output (n_tile = blockIdx.x % nt) and keeps the split
-// weights of that slice resident in shared memory (K <= 256: 128 KB); it walks the 128-row tiles
-// m = blockIdx.x / nt, + gridDim.x / nt, ...  Only A (FP32 -> BF16 hi/lo) streams through a 3-stage
-// ring.  Warp roles: warps 0-7 epilogue (TMEM lane quadrant = warp % 4, column half = warp / 4),
-// warps 8-11 loaders, warp 12 lane 0 issues the MMAs; TMEM holds two 128-column accumulators so the
-// epilogue of one tile overlaps the MMAs of the next.  spin_filter >= 0 restricts the launch to the rows
-// of one spin (the orbital layer runs once per spin with that spin's weights).
+// ----------------------------------------------------------------------------- streamed-weight kernel
+// For K > 256 (the envelope contraction, K = 8 n_nuc): each CTA owns one 128-column slice of the output
+// (n_tile = blockIdx.x % nt) and walks the 128-row tiles m = blockIdx.x / nt, + gridDim.x / nt, ...; every
+// stage of a 3-stage ring carries one 64-deep k-tile of A (converted from FP32 to BF16 hi/lo by the loader
+// warps) and of the split weights (copied by the same warps).  Warp roles: warps 0-7 epilogue (TMEM lane
+// quadrant = warp % 4, column half = warp / 4), warps 8-11 loaders, warp 12 lane 0 issues the MMAs; TMEM
+// holds two 128-column accumulators so the epilogue of one tile overlaps the MMAs of the next.
 struct TcCfg {
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;              // one BF16 plane of an A stage
   static constexpr int A_STAGE = 2 * A_BYTES;                    // hi + lo
-  static constexpr int BK_BYTES = TCP_BN * TC_BK * 2;            // one BF16 plane of one resident k-tile
-  static constexpr int B_BYTES = 2 * BK_BYTES * (TCP_KMAX / TC_BK);  // hi + lo, all k-tiles
+  static constexpr int BK_BYTES = TCP_BN * TC_BK * 2;            // one BF16 plane of a weight k-tile
   // epilogue staging for the TMA stores of C: [warp][2 buffers][32 rows][16 columns] float
   static constexpr int STG_BYTES = 8 * 2 * 32 * 16 * 4;
-  static constexpr int STAGES = 2;  // A stages next to the resident weights
-  static constexpr int TOTAL = B_BYTES + STAGES * A_STAGE + STG_BYTES + 256;
-  // streamed weights (K > TCP_KMAX): every stage carries its A and B k-tiles
-  static constexpr int SB_STAGE = A_STAGE + 2 * BK_BYTES;
+  static constexpr int SB_STAGE = A_STAGE + 2 * BK_BYTES;        // A and weight k-tiles
   static constexpr int STAGES_SB = 3;
   static constexpr int TOTAL_SB = STAGES_SB * SB_STAGE + STG_BYTES + 256;
 };
@@ -381,19 +366,18 @@ __device__ __forceinline__ void tc_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// SB: the weights stream through the stages with A (any K % 8 == 0) instead of staying resident (K <= 256).
 // tma != 0: warps whose 32 rows all belong to the launch store full 16-column chunks of C through shared
 // memory with TMA (tensor map tmC over C, box 16 columns x 32 rows); other chunks use vector stores.
-template <int MODE, bool SB>
-__global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, const __nv_bfloat16* Bhi,
-                                                            const __nv_bfloat16* Blo, int spin_filter,
-                                                            const int* tile_mask, int32_t* status,
+template <int MODE>
+__global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcs(GemmP<float> p, const __nv_bfloat16* Bhi,
+                                                            const __nv_bfloat16* Blo, int32_t* status,
                                                             const __grid_constant__ CUtensorMap tmC, int tma) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  constexpr int STAGE = SB ? TcCfg::SB_STAGE : TcCfg::A_STAGE;
-  constexpr int NS = SB ? TcCfg::STAGES_SB : TcCfg::STAGES;
-  unsigned char* bres = tc_smem;                                 // resident B: [k-tile][hi, lo][128 x 64]
-  unsigned char* astage = tc_smem + (SB ? 0 : TcCfg::B_BYTES);   // [stage][A hi, A lo (, B hi, B lo)]
+  constexpr int STAGE = TcCfg::SB_STAGE;
+  constexpr int NS = TcCfg::STAGES_SB;
+  constexpr int spin_filter = -1;
+  const int* tile_mask = nullptr;
+  unsigned char* astage = tc_smem;                               // [stage][A hi, A lo, B hi, B lo]
   float* stg = reinterpret_cast<float*>(astage + NS * STAGE);    // epilogue staging
   TcBar* bars = reinterpret_cast<TcBar*>(astage + NS * STAGE + TcCfg::STG_BYTES);
   volatile int* abort = &bars->abort;
@@ -408,22 +392,6 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
   const int n0 = n_tile * TCP_BN;
   const int nk = (p.K + TC_BK - 1) / TC_BK;
 
-  // resident weights of this column slice (all threads)
-  for (int q = tid; !SB && q < nk * TCP_BN * (TC_BK / 8); q += TCP_THREADS) {
-    const int kt = q / (TCP_BN * (TC_BK / 8));
-    const int rq = q % (TCP_BN * (TC_BK / 8));
-    const int r = rq >> 3, c = rq & 7;
-    const int gn = n0 + r, gk = kt * TC_BK + c * 8;
-    uint4 h = make_uint4(0, 0, 0, 0), l = h;
-    if (gn < p.N && gk < p.K) {
-      h = *reinterpret_cast<const uint4*>(Bhi + (long)gn * p.K + gk);
-      l = *reinterpret_cast<const uint4*>(Blo + (long)gn * p.K + gk);
-    }
-    unsigned char* bk = bres + kt * 2 * TcCfg::BK_BYTES;
-    const uint32_t off = tc_off(r, c * 8);
-    *reinterpret_cast<uint4*>(bk + off) = h;
-    *reinterpret_cast<uint4*>(bk + TcCfg::BK_BYTES + off) = l;
-  }
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(smem_u32(&bars->full[s]), 128);
@@ -494,7 +462,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
           *reinterpret_cast<uint2*>(a_hi + off) = make_uint2(hw[0], hw[1]);
           *reinterpret_cast<uint2*>(a_lo + off) = make_uint2(lw2[0], lw2[1]);
         }
-        if (SB) {  // this k-tile of the weights: 128 rows x 64 K of the hi and the lo plane
+        {  // this k-tile of the weights: 128 rows x 64 K of the hi and the lo plane
           unsigned char* b_hi = a_hi + TcCfg::A_STAGE;
 #pragma unroll 4
           for (int u = 0; u < 16; ++u) {
@@ -514,7 +482,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
     // ------------------------------------------------------------------ MMA issuer
     if (lane == 0) {
       const uint32_t idesc = tc_idesc<TCP_BN>();
-      const uint32_t b0 = smem_u32(bres), a0 = smem_u32(astage);
+      const uint32_t a0 = smem_u32(astage);
       long kc = 0, uc = 0;
       for (int m = m_first; m < mt && !*abort; m += groups) {
         if (skip(m)) continue;
@@ -528,7 +496,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcp(GemmP<float> p, con
           if (!tc_wait(&bars->full[s], (uint32_t)((kc / NS) & 1), abort)) break;
           tc_fence_after();
           const uint32_t ah = a0 + s * STAGE, al = ah + TcCfg::A_BYTES;
-          const uint32_t bh = SB ? ah + TcCfg::A_STAGE : b0 + kt * 2 * TcCfg::BK_BYTES, bl = bh + TcCfg::BK_BYTES;
+          const uint32_t bh = ah + TcCfg::A_STAGE, bl = bh + TcCfg::BK_BYTES;
 #pragma unroll
           for (int kk = 0; kk < TC_BK / 16; ++kk) {
             const uint32_t step = kk * 2 * TC_LBO;
@@ -868,32 +836,15 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
     }
     return cudaPeekAtLastError();
   }
-  if (p.K > TCP_KMAX) {
-    if (wt.hi2) return cudaErrorInvalidValue;
-    constexpr int smem = TcCfg::TOTAL_SB;
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    const long mt = (p.M + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
-    if (mt == 0 || nt == 0) return cudaSuccess;
-    const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
-    k_gemm_tcp<MODE, true><<<(unsigned)(groups * nt), TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status, tmC, tma);
-    return cudaPeekAtLastError();
-  }
-  const int smem = TcCfg::TOTAL;
-  cudaError_t e = cudaFuncSetAttribute(k_gemm_tcp<MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  // K > 256: streamed weights
+  if (!wt.hi || wt.hi2) return cudaErrorInvalidValue;
+  constexpr int smem = TcCfg::TOTAL_SB;
+  cudaError_t e = cudaFuncSetAttribute(k_gemm_tcs<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const long mt = (p.M + TC_BM - 1) / TC_BM, nt = (p.N + TCP_BN - 1) / TCP_BN;
   if (mt == 0 || nt == 0) return cudaSuccess;
   const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
-  const unsigned grid = (unsigned)(groups * nt);
-  if (wt.hi2) {
-    if (!mask_buf) return cudaErrorInvalidValue;
-    k_tile_mask<<<(unsigned)mt, TC_BM, 0, s>>>(p, mask_buf);
-    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, 0, mask_buf, status, tmC, tma);
-    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi2, wt.lo2, 1, mask_buf, status, tmC, tma);
-  } else {
-    k_gemm_tcp<MODE, false><<<grid, TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, -1, nullptr, status, tmC, tma);
-  }
+  k_gemm_tcs<MODE><<<(unsigned)(groups * nt), TCP_THREADS, smem, s>>>(p, wt.hi, wt.lo, status, tmC, tma);
   return cudaPeekAtLastError();
 }
 
