@@ -139,3 +139,29 @@ def test_walker_sharding_gloo():
     assert res[0][1:3] == (0, 51) and res[1][1:3] == (51, 101)
     for _, _, _, (mean, std) in res:
         assert abs(mean - e.mean()) < 1e-12 and abs(std - e.std()) < 1e-12
+
+
+def test_serving_trace_and_summary():
+    """Poisson traces are reproducible and the latency summary reads the completed requests."""
+    from sparse_wf_gb300.serving import poisson_trace, summarize
+
+    a = poisson_trace(50, 20.0, seed=3)
+    b = poisson_trace(50, 20.0, seed=3)
+    assert [(r.kind, r.n_carbon, r.walkers, r.arrival) for r in a] == [(r.kind, r.n_carbon, r.walkers, r.arrival)
+                                                                          for r in b]
+    arr = [r.arrival for r in a]
+    assert all(x < y for x, y in zip(arr, arr[1:]))
+    assert all(4 <= r.n_carbon <= 60 and 256 <= r.walkers <= 2048 for r in a)
+    for k, r in enumerate(a):
+        r.done = r.arrival + 0.001 * (k + 1)
+    m = summarize(a, 10.0)
+    assert abs(m["p50_ms"] - np.percentile([r.latency * 1e3 for r in a], 50)) < 1e-9
+    assert m["max_ms"] == pytest.approx(50.0)
+
+
+def test_ragged_batch_draws():
+    from sparse_wf_gb300.ragged import ragged_alkanes
+
+    ns, ws = ragged_alkanes(64, seed=4)
+    assert len(ns) == 64 and min(ns) >= 2 and max(ns) <= 40 and min(ws) >= 64 and max(ws) <= 1024
+    assert ragged_alkanes(64, seed=4) == (ns, ws)
