@@ -52,6 +52,12 @@ def parse():
     ap.add_argument("--mcmc-width", type=float, default=0.1)
     ap.add_argument("--acc-walkers", type=int, default=256, help="walkers checked against the FP64 build")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
+    ap.add_argument("--serving-requests", type=int, default=40, help="requests of the serving segment (0: skip)")
+    ap.add_argument("--serving-rate", type=float, default=3.0, help="offered load, requests per second")
+    ap.add_argument("--serving-carbons", default="4,20", help="alkane sizes C_n of the serving requests (min,max)")
+    ap.add_argument("--serving-walkers", default="256,1024", help="walkers per serving request (min,max)")
+    ap.add_argument("--ragged", action="store_true",
+                    help="also time the 64-alkane ragged batch: one CUDA-graph launch vs one call per molecule")
     ap.add_argument("--cpu-sample", type=int, default=2, help="walkers in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -391,6 +397,47 @@ def main():
         accuracy = {"walkers": K, "reference": "FP64 build of the same kernels (FP64 oracle to <= 1e-10)"}
         accuracy.update({k: energy_error(v[:K], e64) for k, v in e_path.items()})
 
+    # serving segment: Poisson-arriving E_loc / 10-step MCMC requests of mixed molecule sizes (rank 0)
+    serving = None
+    if rank == 0 and args.serving_requests > 0:
+        from sparse_wf_gb300.serving import ServingEngine, poisson_trace
+
+        wf._ws = None
+        torch.cuda.empty_cache()
+        nr = tuple(int(x) for x in args.serving_carbons.split(","))
+        wr = tuple(int(x) for x in args.serving_walkers.split(","))
+        serving = {"offered_rate_per_s": args.serving_rate, "carbons": list(nr), "walkers": list(wr),
+                   "mcmc_steps": 10, "slots": 4}
+        for prec in ([args.precision, "fp32"] if args.precision == "mixed" and not args.no_compare
+                     else [args.precision]):
+            trace = poisson_trace(args.serving_requests, args.serving_rate, seed=5, n_range=nr, walker_range=wr)
+            eng = ServingEngine(prec, lanes=4, chunk=32, max_carbon=nr[1], max_walkers=wr[1], device=dev)
+            serving[prec] = eng.run(trace)
+            del eng
+            torch.cuda.empty_cache()
+
+    ragged = None
+    if rank == 0 and args.ragged:
+        from sparse_wf_gb300.ragged import RaggedBatch, ragged_alkanes
+
+        wf._ws = None
+        torch.cuda.empty_cache()
+        ns, ws = ragged_alkanes(64, seed=4)
+        rb = RaggedBatch([systems.alkane(k) for k in ns], ws, args.precision, lanes=4, chunk=64, device=dev)
+        rb.run_eager()
+        t0 = time.perf_counter()
+        rb.run_eager()
+        te = time.perf_counter() - t0
+        rb.run()
+        t0 = time.perf_counter()
+        rb.replay()
+        torch.cuda.synchronize()
+        tg = time.perf_counter() - t0
+        ragged = {"molecules": 64, "walkers": int(sum(ws)), "one_graph_launch_s": tg, "per_molecule_calls_s": te,
+                  "walker_evals_per_s": sum(ws) / tg, "lanes": 4, "chunk_walkers": 64}
+        del rb
+        torch.cuda.empty_cache()
+
     # CPU baseline + oracle check on the same walkers (rank 0)
     cpu = None
     check = None
@@ -420,7 +467,8 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": int(prof.get("kernels_launched", (0, 0))[0]) * args.steps,
             "fp32_path": fp32, "mixed_over_fp32": (value / fp32["value"]) if fp32 else None,
-            "accuracy": accuracy, "mcmc": mcmc, "stages_ms": stages, "oracle_check": check,
+            "accuracy": accuracy, "mcmc": mcmc, "serving": serving, "ragged": ragged, "stages_ms": stages,
+            "oracle_check": check,
         }
         print(json.dumps(line))
     if world > 1:

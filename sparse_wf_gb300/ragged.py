@@ -111,6 +111,7 @@ class RaggedBatch:
     def _call(self, j: _Job, stream: torch.cuda.Stream, ws: Optional[torch.Tensor] = None):
         ws = self._ws[j.lane] if ws is None else ws
         prob = self._problem(j)
+        prob.chunk_walkers = 0  # smaller molecules of a lane take more walkers per pass in the same workspace
         with torch.cuda.stream(stream):
             j.status.zero_()
         _lib.check(_lib.load().fire_local_energy(

@@ -167,6 +167,7 @@ class ServingEngine:
             status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=self.device)
             r.copy_(r_host, non_blocking=True)
         prob = m.problem(B, static)
+        prob.chunk_walkers = 0  # as many walkers per internal pass as the slot's workspace holds
         ws = self.ws[lane]
         lib = _lib.load()
         sp = C.c_void_p(s.cuda_stream)
