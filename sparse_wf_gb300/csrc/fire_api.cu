@@ -259,7 +259,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.JMl, W * 2, es);
     take(P.JMj, W * 3 * n * 2, es);
   }
-  take(P.gjw, W * NDET * n * n, 8);  // working matrices of the Gauss-Jordan / LU kernel
+  take(P.gjw, 2 * W * NDET * n * n, 8);  // two working copies per matrix for the Gauss-Jordan / LU kernel
   take(P.tile_mask, (fl ? 3 * Pc : G) / 128 + 2, 4);
   take(P.rn, G * 3, es);
   take(P.lpn, W, es);
@@ -700,7 +700,8 @@ template <typename S, typename TI, typename TO, bool INV>
 cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   const int n = c.p->n_el;
   constexpr int BW = GJG_BW_DECL;
-  const size_t smem = sizeof(S) * (2 * (size_t)n * (BW + 1) + BW * BW + n + 2 * BW) + sizeof(int) * ((size_t)n + BW);
+  const size_t smem =
+      sizeof(S) * (2 * (size_t)n * (BW + 1) + BW * BW + n + 2 * BW) + sizeof(int) * (2 * (size_t)n + BW);
   auto kern = k_gj_global<S, TI, TO, INV>;
   if (smem > 48 * 1024) {
     const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

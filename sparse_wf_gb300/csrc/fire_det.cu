@@ -77,7 +77,8 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   constexpr int BW = GJG_BW, LD = GJG_BW + 1;  // shared rows padded: column walks spread over the banks
   const int mat = blockIdx.x;
   const int w = mat / NDET, d = mat - w * NDET;
-  S* M = work + (size_t)mat * n * n;
+  // two working copies per matrix: every panel reads one and writes the other
+  S* Mb[2] = {work + (size_t)mat * n * n, work + ((size_t)gridDim.x + mat) * n * n};
   S* pan = reinterpret_cast<S*>(gj_smem);  // [n][LD] the panel, then each chunk of other columns
   S* W = pan + (size_t)n * LD;             // [n][LD] panel transforms (then W~)
   S* Li = W + (size_t)n * LD;              // [BW][BW] L^-1
@@ -86,12 +87,13 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   S* rp = rk + BW;                         // [BW] row p
   int* perm = reinterpret_cast<int*>(rp + BW);  // [n]
   int* piv = perm + n;                     // [BW]
+  int* rowmap = piv + BW;                  // [n] source row of every row after the panel's interchanges
   __shared__ S redv[32];
   __shared__ int redi[32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarp = blockDim.x >> 5;
   for (int e = tid; e < n * n; e += blockDim.x) {
     const int i = e / n, o = e - i * n;
-    M[e] = (S)A[((long)(w * n + i) * NDET + d) * n + o];
+    Mb[0][e] = (S)A[((long)(w * n + i) * NDET + d) * n + o];
   }
   __syncthreads();
   double ld = 0.0;
@@ -100,8 +102,10 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   const int cj = tid % BW, rg = tid / BW, rn = blockDim.x / BW;  // chunk update: column, row group
   for (int P = 0; P < npan; ++P) {
     const int k0 = P * BW, bw = min(BW, n - k0);
+    const S* src = Mb[P & 1];
+    S* dst = Mb[(P + 1) & 1];
     if (cj < bw)
-      for (int i = rg; i < n; i += rn) pan[i * LD + cj] = M[(size_t)i * n + k0 + cj];
+      for (int i = rg; i < n; i += rn) pan[i * LD + cj] = src[(size_t)i * n + k0 + cj];
     __syncthreads();
     // ---- factor the panel
     for (int t = 0; t < bw; ++t) {
@@ -151,7 +155,7 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
         if (pv < S(0)) neg ^= 1;
         if (p != k) neg ^= 1;
       }
-      for (int i = tid; i < n; i += blockDim.x) colk[i] = pan[(i == k ? p : (i == p ? k : i)) * LD + t];
+      for (int i = (INV ? 0 : k) + tid; i < n; i += blockDim.x) colk[i] = pan[(i == k ? p : (i == p ? k : i)) * LD + t];
       for (int j = tid; j < bw; j += blockDim.x) {
         rk[j] = pan[k * LD + j];
         rp[j] = pan[p * LD + j];
@@ -163,19 +167,24 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
           W[p * LD + s2] = tk;
         }
       __syncthreads();
-      for (int e = tid; e < n * BW; e += blockDim.x) {
-        const int i = e / BW, j = e - i * BW;  // BW is a power of two: shifts
-        if (j >= bw) continue;
-        S* el = pan + i * LD + j;
-        const S ci = colk[i];
-        if (INV) {
+      if (INV) {  // Gauss-Jordan: every row of every panel column
+        for (int e = tid; e < n * BW; e += blockDim.x) {
+          const int i = e / BW, j = e - i * BW;  // BW is a power of two: shifts
+          if (j >= bw) continue;
+          S* el = pan + i * LD + j;
+          const S ci = colk[i];
           const S old = i == k ? rp[j] : (i == p ? rk[j] : *el);
           const S rj = rp[j] * ipv;
           if (j == t) *el = i == k ? ipv : -ci * ipv;
           else *el = i == k ? rj : df_sub_mul(old, ci, rj);
-        } else if (j > t) {
+        }
+      } else {  // LU: rows k.. of the panel columns right of the pivot (rows above k do not change)
+        const int nc = bw - t - 1, nr = n - k;
+        for (int e = tid; e < nr * nc; e += blockDim.x) {
+          const int ii = e / nc, i = k + ii, j = t + 1 + (e - ii * nc);
+          S* el = pan + i * LD + j;
           const S old = i == k ? rp[j] : (i == p ? rk[j] : *el);
-          *el = i > k ? df_sub_mul(old, ci * ipv, rp[j]) : old;
+          *el = i > k ? df_sub_mul(old, colk[i] * ipv, rp[j]) : old;
         }
       }
       for (int i = tid; i < n; i += blockDim.x)
@@ -190,8 +199,17 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
         Li[t * BW + tid] = v;
       }
     }
-    if (cj < bw)  // panel back to the working matrix
-      for (int i = rg; i < n; i += rn) M[(size_t)i * n + k0 + cj] = pan[i * LD + cj];
+    if (INV && cj < bw)  // panel into the next working copy (the LU never reads finished panels again)
+      for (int i = rg; i < n; i += rn) dst[(size_t)i * n + k0 + cj] = pan[i * LD + cj];
+    if (tid == 0) {  // the panel's row interchanges as one permutation
+      for (int i = 0; i < n; ++i) rowmap[i] = i;
+      for (int t = 0; t < bw; ++t) {
+        const int q = piv[t];
+        const int tmp = rowmap[k0 + t];
+        rowmap[k0 + t] = rowmap[q];
+        rowmap[q] = tmp;
+      }
+    }
     __syncthreads();
     for (int i = tid; i < n; i += blockDim.x) {
       S wr[BW];
@@ -208,41 +226,26 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
       }
     }
     __syncthreads();
-    // ---- apply the panel to the other columns, one chunk of BW columns at a time
+    // ---- apply the panel to the other columns: each thread owns one column of a BW-wide chunk and walks its
+    // rows, reading the interchanged rows of src and writing dst (no in-place hazard, no barrier per chunk)
     for (int Q = INV ? 0 : P + 1; Q < npan; ++Q) {
       if (Q == P) continue;
       const int c0 = Q * BW, cb = min(BW, n - c0);
-      if (cj < cb)
-        for (int i = rg; i < n; i += rn) pan[i * LD + cj] = M[(size_t)i * n + c0 + cj];
-      __syncthreads();
-      if (tid < cb)
-        for (int t = 0; t < bw; ++t) {
-          const int pt = piv[t];
-          if (pt != k0 + t) {
-            const S tmp = pan[(k0 + t) * LD + tid];
-            pan[(k0 + t) * LD + tid] = pan[pt * LD + tid];
-            pan[pt * LD + tid] = tmp;
-          }
-        }
-      __syncthreads();
+      if (cj >= cb) continue;
+      const S* sc = src + c0 + cj;
       S yv[BW];
 #pragma unroll
-      for (int t = 0; t < BW; ++t) yv[t] = (t < bw && cj < cb) ? pan[(k0 + t) * LD + cj] : S(0);
-      __syncthreads();  // every pivot-row value is read before any is updated
-      if (cj < cb)
-        for (int i = (INV ? 0 : k0) + rg; i < n; i += rn) {
-          S acc = pan[i * LD + cj];
-          const S* wi = W + i * LD;
+      for (int t = 0; t < BW; ++t) yv[t] = t < bw ? sc[(size_t)rowmap[k0 + t] * n] : S(0);
+      for (int i = (INV ? 0 : k0) + rg; i < n; i += rn) {
+        S acc = sc[(size_t)rowmap[i] * n];
+        const S* wi = W + i * LD;
 #pragma unroll
-          for (int t = 0; t < BW; ++t)
-            if (t < bw) acc = df_sub_mul(acc, wi[t], yv[t]);
-          pan[i * LD + cj] = acc;
-        }
-      __syncthreads();
-      if (cj < cb)
-        for (int i = rg; i < n; i += rn) M[(size_t)i * n + c0 + cj] = pan[i * LD + cj];
-      __syncthreads();
+        for (int t = 0; t < BW; ++t)
+          if (t < bw) acc = df_sub_mul(acc, wi[t], yv[t]);
+        dst[(size_t)i * n + c0 + cj] = acc;
+      }
     }
+    __syncthreads();  // dst complete before the next panel reads it
   }
   if (tid == 0) {
     logdet[mat] = ld;
@@ -251,23 +254,24 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   }
   if (INV) {
     // undo the row interchanges on the columns: final column jc holds working column src(jc)
-    int* src = reinterpret_cast<int*>(colk);
+    int* srcc = reinterpret_cast<int*>(colk);
     if (tid == 0) {
-      for (int q = 0; q < n; ++q) src[q] = q;
+      for (int q = 0; q < n; ++q) srcc[q] = q;
       for (int k = n - 1; k >= 0; --k) {
         const int p = perm[k];
         if (p != k) {
-          const int t = src[k];
-          src[k] = src[p];
-          src[p] = t;
+          const int t = srcc[k];
+          srcc[k] = srcc[p];
+          srcc[p] = t;
         }
       }
     }
     __syncthreads();
     TO* out = Ainv + (size_t)mat * n * n;
+    const S* M = Mb[npan & 1];
     for (int e = tid; e < n * n; e += blockDim.x) {
       const int i = e / n, jc = e - i * n;
-      out[e] = (TO)M[(size_t)i * n + src[jc]];
+      out[e] = (TO)M[(size_t)i * n + srcc[jc]];
     }
   }
 }
