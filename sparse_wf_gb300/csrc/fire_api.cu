@@ -885,7 +885,7 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {
     const size_t es = sizeof(T);
-    const size_t smem = es * std::max<size_t>(32 * 196 + 32 * DL_CMAX_DECL, 3 * DL_CMAX_DECL * (DL_CMAX_DECL + 1));
+    const size_t smem = es * std::max<size_t>(32 * DL_RP_DECL + 32 * DL_CMAX_DECL, 3 * DL_CMAX_DECL * (DL_CMAX_DECL + 1));
     cudaFuncSetAttribute(k_detlap<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     Prof pr("detlap", c.s);
     g_nlaunch++;

@@ -236,7 +236,21 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
       S yv[BW];
 #pragma unroll
       for (int t = 0; t < BW; ++t) yv[t] = t < bw ? sc[(size_t)rowmap[k0 + t] * n] : S(0);
-      for (int i = (INV ? 0 : k0) + rg; i < n; i += rn) {
+      // two rows per pass: independent multiply-subtract chains hide each other's latency
+      int i = (INV ? 0 : k0) + rg;
+      for (; i + rn < n; i += 2 * rn) {
+        S a0 = sc[(size_t)rowmap[i] * n], a1 = sc[(size_t)rowmap[i + rn] * n];
+        const S *w0 = W + i * LD, *w1 = W + (i + rn) * LD;
+#pragma unroll
+        for (int t = 0; t < BW; ++t)
+          if (t < bw) {
+            a0 = df_sub_mul(a0, w0[t], yv[t]);
+            a1 = df_sub_mul(a1, w1[t], yv[t]);
+          }
+        dst[(size_t)i * n + c0 + cj] = a0;
+        dst[(size_t)(i + rn) * n + c0 + cj] = a1;
+      }
+      if (i < n) {
         S acc = sc[(size_t)rowmap[i] * n];
         const S* wi = W + i * LD;
 #pragma unroll
@@ -282,7 +296,7 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
 // B = J[(i, m) rows] (3c x n) @ Ainv[:, {i}] (n x c) is computed with 2 x 4 register tiles from K-chunks
 // staged (J transposed) in shared memory; the next chunk is prefetched into registers while the current
 // one is multiplied.  The result tile reuses the staging memory.
-constexpr int DL_CMAX = 64, DL_RP = 196, DL_OC = 32;
+constexpr int DL_CMAX = 64, DL_RP = 197, DL_OC = 32;  // odd row stride: conflict-free transposed stores
 constexpr int DL_JPT = 3 * DL_CMAX * DL_OC / 256;  // J chunk elements per thread (24)
 constexpr int DL_APT = DL_OC * DL_CMAX / 256;      // Ainv chunk elements per thread (8)
 template <typename T>
@@ -359,8 +373,13 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
         for (int o = 0; o < DL_OC; ++o) {
           const T a0 = Jt[o * DL_RP + r0], a1 = Jt[o * DL_RP + r0 + 1];
           T b[4];
+          if constexpr (sizeof(T) == 4) {  // c0 % 4 == 0: one 16-byte load
+            const float4 bv = *reinterpret_cast<const float4*>(&At[o * DL_CMAX + c0]);
+            b[0] = bv.x; b[1] = bv.y; b[2] = bv.z; b[3] = bv.w;
+          } else {
 #pragma unroll
-          for (int y = 0; y < 4; ++y) b[y] = At[o * DL_CMAX + c0 + y];
+            for (int y = 0; y < 4; ++y) b[y] = At[o * DL_CMAX + c0 + y];
+          }
 #pragma unroll
           for (int y = 0; y < 4; ++y) {
             acc[u][y] += a0 * b[y];
