@@ -168,7 +168,7 @@ struct Plan {
   size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, Zr2, jsqr;
   size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, tile_mask, aD1, aD2, ajsq;
   // double
-  size_t ld, sd, dlap, gjw;
+  size_t ld, sd, dlap, gjw, enn;
   size_t total;
 };
 
@@ -260,6 +260,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.JMj, W * 3 * n * 2, es);
   }
   take(P.gjw, 2 * W * NDET * n * n, 8);  // two working copies per matrix for the Gauss-Jordan / LU kernel
+  take(P.enn, 1, 8);
   take(P.tile_mask, (fl ? 3 * Pc : G) / 128 + 2, 4);
   take(P.rn, G * 3, es);
   take(P.lpn, W, es);
@@ -857,6 +858,9 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   stage_jastrow<T, 0>(c);
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
+  g_nlaunch++;
+  k_nn_energy<<<1, 256, 0, c.s>>>(c.R, c.Z, c.p->n_nuc, c.template buf<double>(c.P.enn));
+  o.enn = c.template buf<double>(c.P.enn);
   o.logpsi = logpsi;
   o.sign = sign;
   g_nlaunch++;
@@ -896,6 +900,9 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   stage_jastrow<T, 3>(c);
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
+  g_nlaunch++;
+  k_nn_energy<<<1, 256, 0, c.s>>>(c.R, c.Z, c.p->n_nuc, c.template buf<double>(c.P.enn));
+  o.enn = c.template buf<double>(c.P.enn);
   o.logpsi = logpsi;
   o.sign = sign;
   o.eloc = eloc;

@@ -52,6 +52,7 @@ struct AssembleOut {
   void* sign;
   void* eloc;
   fire_eloc_debug dbg;
+  const double* enn;  // input: nucleus-nucleus repulsion of the molecule (one value)
 };
 
 }  // namespace fire

@@ -250,49 +250,85 @@ __global__ void __launch_bounds__(512) k_readout_in(int n, const T* __restrict__
                                T(2) * vn * iN * iN;
 }
 
-// e-e cusp (value, gradient per electron, Laplacian) and Coulomb potential of one walker; used by
-// k_assemble.  grad_s: shared [n][3] (double).
+// e-e cusp (value, gradient per electron, Laplacian) and electronic Coulomb potential of one walker (the
+// nucleus-nucleus term enn is added once); used by k_assemble.  grad_s: shared [n][3] (double).  In FP32 the
+// per-pair terms are FP32 and every per-thread sum is compensated (Kahan), then reduced in FP64 across the CTA;
+// the FP64 build stays in double.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
 template <typename T>
 __device__ void cusp_and_potential(const T* r, const float* R, const float* Z, int n, int n_up, int N,
-                                   const T* cusp, double* grad_s, double& cval, double& clap, double& pot,
-                                   double* red) {
+                                   const T* cusp, double enn, double* grad_s, double& cval, double& clap,
+                                   double& pot, double* red) {
   const int tid = threadIdx.x;
-  const double as = (double)cusp[0], ad = (double)cusp[1], fs = (double)cusp[2], fd = (double)cusp[3];
-  double v = 0.0, l = 0.0, p = 0.0;
-  for (int e = tid; e < n; e += blockDim.x) {
-    const T xe = r[3 * e], ye = r[3 * e + 1], ze = r[3 * e + 2];
-    double gx = 0.0, gy = 0.0, gz = 0.0;
-    const bool se = e < n_up;
-    for (int j = 0; j < n; ++j) {
-      if (j == e) continue;
-      const T dx = xe - r[3 * j], dy = ye - r[3 * j + 1], dz = ze - r[3 * j + 2];
-      const double d = (double)dsqrt(dx * dx + dy * dy + dz * dz);
-      const bool same = (j < n_up) == se;
-      const double a = same ? as : ad, fac = same ? fs : fd;
-      const double ia = 1.0 / (a + d);
-      const double u = a * a * ia, u1 = -a * a * ia * ia, u2 = 2.0 * a * a * ia * ia * ia;
-      v += 0.5 * fac * u;
-      l += fac * (u2 + 2.0 * u1 / d);
-      const double gd = fac * u1 / d;
-      gx += gd * (double)dx;
-      gy += gd * (double)dy;
-      gz += gd * (double)dz;
-      if (j > e) p += 1.0 / d;
+  double v = 0.0, l = 0.0, p = tid == 0 ? enn : 0.0;
+  if constexpr (sizeof(T) == 4) {
+    const float as = cusp[0], ad = cusp[1], fs = cusp[2], fd = cusp[3];
+    float sv = 0.f, cv = 0.f, sl = 0.f, cl = 0.f, sp = 0.f, cp = 0.f;
+    for (int e = tid; e < n; e += blockDim.x) {
+      const float xe = r[3 * e], ye = r[3 * e + 1], ze = r[3 * e + 2];
+      float gx = 0.f, gy = 0.f, gz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+      const bool se = e < n_up;
+      for (int j = 0; j < n; ++j) {
+        if (j == e) continue;
+        const float dx = xe - r[3 * j], dy = ye - r[3 * j + 1], dz = ze - r[3 * j + 2];
+        const float d = sqrtf(dx * dx + dy * dy + dz * dz), id = 1.f / d;
+        const bool same = (j < n_up) == se;
+        const float a = same ? as : ad, fac = same ? fs : fd;
+        const float ia = 1.f / (a + d);
+        const float u = a * a * ia, u1 = -u * ia, u2 = -2.f * u1 * ia;
+        kahan_add(sv, cv, 0.5f * fac * u);
+        kahan_add(sl, cl, fac * (u2 + 2.f * u1 * id));
+        const float gd = fac * u1 * id;
+        kahan_add(gx, cx, gd * dx);
+        kahan_add(gy, cy, gd * dy);
+        kahan_add(gz, cz, gd * dz);
+        if (j > e) kahan_add(sp, cp, id);
+      }
+      for (int I = 0; I < N; ++I) {
+        const float dx = xe - R[3 * I], dy = ye - R[3 * I + 1], dz = ze - R[3 * I + 2];
+        kahan_add(sp, cp, -Z[I] / sqrtf(dx * dx + dy * dy + dz * dz));
+      }
+      grad_s[3 * e] = (double)gx - (double)cx;
+      grad_s[3 * e + 1] = (double)gy - (double)cy;
+      grad_s[3 * e + 2] = (double)gz - (double)cz;
     }
-    for (int I = 0; I < N; ++I) {
-      const T dx = xe - (T)R[3 * I], dy = ye - (T)R[3 * I + 1], dz = ze - (T)R[3 * I + 2];
-      p -= (double)Z[I] / (double)dsqrt(dx * dx + dy * dy + dz * dz);
-    }
-    grad_s[3 * e] = gx;
-    grad_s[3 * e + 1] = gy;
-    grad_s[3 * e + 2] = gz;
-  }
-  for (int k = tid; k < N * N; k += blockDim.x) {
-    const int I = k / N, J = k - I * N;
-    if (J > I) {
-      const double dx = (double)R[3 * I] - R[3 * J], dy = (double)R[3 * I + 1] - R[3 * J + 1],
-                   dz = (double)R[3 * I + 2] - R[3 * J + 2];
-      p += (double)Z[I] * Z[J] / sqrt(dx * dx + dy * dy + dz * dz);
+    v += (double)sv - (double)cv;
+    l += (double)sl - (double)cl;
+    p += (double)sp - (double)cp;
+  } else {
+    const double as = (double)cusp[0], ad = (double)cusp[1], fs = (double)cusp[2], fd = (double)cusp[3];
+    for (int e = tid; e < n; e += blockDim.x) {
+      const T xe = r[3 * e], ye = r[3 * e + 1], ze = r[3 * e + 2];
+      double gx = 0.0, gy = 0.0, gz = 0.0;
+      const bool se = e < n_up;
+      for (int j = 0; j < n; ++j) {
+        if (j == e) continue;
+        const T dx = xe - r[3 * j], dy = ye - r[3 * j + 1], dz = ze - r[3 * j + 2];
+        const double d = (double)dsqrt(dx * dx + dy * dy + dz * dz);
+        const bool same = (j < n_up) == se;
+        const double a = same ? as : ad, fac = same ? fs : fd;
+        const double ia = 1.0 / (a + d);
+        const double u = a * a * ia, u1 = -a * a * ia * ia, u2 = 2.0 * a * a * ia * ia * ia;
+        v += 0.5 * fac * u;
+        l += fac * (u2 + 2.0 * u1 / d);
+        const double gd = fac * u1 / d;
+        gx += gd * (double)dx;
+        gy += gd * (double)dy;
+        gz += gd * (double)dz;
+        if (j > e) p += 1.0 / d;
+      }
+      for (int I = 0; I < N; ++I) {
+        const T dx = xe - (T)R[3 * I], dy = ye - (T)R[3 * I + 1], dz = ze - (T)R[3 * I + 2];
+        p -= (double)Z[I] / (double)dsqrt(dx * dx + dy * dy + dz * dz);
+      }
+      grad_s[3 * e] = gx;
+      grad_s[3 * e + 1] = gy;
+      grad_s[3 * e + 2] = gz;
     }
   }
   double vv[3] = {v, l, p};
@@ -318,7 +354,8 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
   const int w = blockIdx.x, tid = threadIdx.x;
   const T* rw = r + (size_t)w * n * 3;
   double cval, clap, pot;
-  cusp_and_potential<T>(rw, R, Z, n, n_up, N, W.w[FIRE_P_CUSP], grad_s, cval, clap, pot, red);
+  cusp_and_potential<T>(rw, R, Z, n, n_up, N, W.w[FIRE_P_CUSP], out.enn ? *out.enn : 0.0, grad_s, cval, clap, pot,
+                        red);
   __syncthreads();
   // determinants
   double mx = -1e300;
@@ -389,6 +426,24 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
       for (int d = 0; d < NDET; ++d) out.dbg.sign_det[(size_t)(w0 + w) * NDET + d] = sd[w * NDET + d];
     if (!isfinite(eloc) || !isfinite(logpsi)) set_flag(status, FIRE_FLAG_NONFINITE);
   }
+}
+
+// Nucleus-nucleus repulsion sum_{I<J} Z_I Z_J / |R_I - R_J| (hamiltonian.py:15-26), once per call.
+__global__ void __launch_bounds__(256) k_nn_energy(const float* __restrict__ R, const float* __restrict__ Z, int N,
+                                                   double* __restrict__ out) {
+  __shared__ double red[32];
+  double p = 0.0;
+  for (int k = threadIdx.x; k < N * N; k += blockDim.x) {
+    const int I = k / N, J = k - I * N;
+    if (J > I) {
+      const double dx = (double)R[3 * I] - R[3 * J], dy = (double)R[3 * I + 1] - R[3 * J + 1],
+                   dz = (double)R[3 * I + 2] - R[3 * J + 2];
+      p += (double)Z[I] * Z[J] / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+  }
+  double v[1] = {p};
+  block_sum<double, 1>(v, red);
+  if (threadIdx.x == 0) out[0] = v[0];
 }
 
 // Coulomb potential only (fire_potential_energy).

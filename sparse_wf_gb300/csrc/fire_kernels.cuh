@@ -41,6 +41,7 @@ __global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* 
 constexpr int DL_CMAX_DECL = 64, DL_RP_DECL = 197;
 
 // fire_jastrow.cu
+__global__ void k_nn_energy(const float* R, const float* Z, int N, double* out);
 template <typename T, int NC, int ACT, bool FLM>
 __global__ void k_narrow(const T* X, const T* Jp, const T* Lp, Nbr nb, Layout L, const T* Wn, const T* bn,
                          const T* post_scale, const T* post_shift, T* Xo, T* Jo, T* Lo, int32_t* status, T* D1o,
