@@ -246,7 +246,8 @@ __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int nod
 // Epilogue of one 128-row x 128-column accumulator tile (rows [m0, m0 + 128), columns [n0, n0 + 128)) held
 // in tensor memory at column tacc.  Called by the 8 epilogue warps: warp w reads TMEM lane quadrant w % 4
 // (rows m0 + 32 (w % 4) + lane) and column half w / 4.  Whole-warp full 16-column chunks go out through the
-// shared staging buffers stg with TMA (tma != 0), the rest with vector / scalar stores; nst counts this
+// shared staging buffers stg with TMA (tma != 0), the rest with vector / scalar stores; in SILU_J mode every
+// chunk first passes its squared values through the same buffer for the per-center sums.  nst counts this
 // warp's TMA stores (lane 0 owns their bulk groups).
 template <int MODE>
 __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows, int m0, int n0, uint32_t tacc,
@@ -259,28 +260,53 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
   bool mine = valid && !(p.row_skip > 0 && row % p.row_skip == 0);
   if (mine && spin_filter >= 0) mine = ((((node % p.n_el) < p.n_up) ? 0 : 1) == spin_filter);
   const bool tma_warp = tma != 0 && __all_sync(0xffffffffu, mine);
-  const int prev = __shfl_up_sync(0xffffffffu, node, 1);
-  const bool head = lane == 0 || prev != node;
-  // rows of one center are consecutive: bit k of segm says lane + 2^k belongs to this lane's center
-  unsigned segm = 0;
+  // per-center sums of squared Jacobian rows: lanes 0-15 sum the even rows of column lane % 16 of a chunk,
+  // lanes 16-31 the odd rows; the centers of those rows are fetched once per tile
+  int nodes_h[16];
   if (MODE == EPI_SILU_J) {
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      const int nu = __shfl_down_sync(0xffffffffu, node, 1 << k);
-      if (lane + (1 << k) < 32 && nu == node) segm |= 1u << k;
-    }
+    for (int i = 0; i < 16; ++i) nodes_h[i] = __shfl_sync(0xffffffffu, valid ? node : -1, 2 * i + (lane >> 4));
   }
   const uint32_t base = tacc + ((uint32_t)(quad * 32) << 16);
   for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
     float v[16];
     tmem_ld16(base + (uint32_t)c0, v);
     const int spin = spin_filter < 0 ? 0 : spin_filter;
-    if (MODE != EPI_ENV && tma_warp && n0 + c0 + 15 < p.N) {
-      float4 o[4];
-      tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
-      float* sb = stg + (size_t)(warp * 2 + (nst & 1)) * 32 * 16;
+    const bool full = MODE != EPI_ENV && n0 + c0 + 15 < p.N;
+    const bool use_tma = tma_warp && full;
+    float* sb = stg + (size_t)(warp * 2 + (nst & 1)) * 32 * 16;  // this chunk's staging buffer
+    if (use_tma || MODE == EPI_SILU_J) {
       if (lane == 0 && nst >= 2) tma_wait_read1();  // the store from this buffer two chunks ago has read it
       __syncwarp();
+    }
+    if (MODE == EPI_SILU_J) {
+      // squared pre-activation values through the staging buffer (row-major, 16-column rows, column index
+      // XOR-swizzled by row / 2: conflict-free both ways), then segmented column sums, one atomic per center
+      // run; the last runs of the two half-warps merge when they belong to the same center
+#pragma unroll
+      for (int c = 0; c < 16; ++c) sb[lane * 16 + (c ^ ((lane >> 1) & 15))] = valid ? v[c] * v[c] : 0.f;
+      __syncwarp();
+      const int c = lane & 15, h = lane >> 4, col = n0 + c0 + c;
+      float s2 = 0.f;
+      int cur = nodes_h[0];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        if (nodes_h[i] != cur) {
+          if (cur >= 0 && col < p.N) atomicAdd(&p.aux2[(long)cur * p.ld_aux + col], s2);
+          s2 = 0.f;
+          cur = nodes_h[i];
+        }
+        s2 += sb[(2 * i + h) * 16 + (c ^ i)];
+      }
+      const int other = __shfl_xor_sync(0xffffffffu, cur, 16);
+      const float s2o = __shfl_xor_sync(0xffffffffu, s2, 16);
+      if (other == cur) s2 = h ? 0.f : s2 + s2o;
+      if (cur >= 0 && col < p.N && !(other == cur && h)) atomicAdd(&p.aux2[(long)cur * p.ld_aux + col], s2);
+      __syncwarp();
+    }
+    if (use_tma) {
+      float4 o[4];
+      tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
 #pragma unroll
       for (int u = 0; u < 4; ++u) *reinterpret_cast<float4*>(sb + lane * 16 + 4 * u) = o[u];
       proxy_fence();
@@ -291,7 +317,7 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
       }
       ++nst;
     } else if (mine) {
-      if (MODE != EPI_ENV && n0 + c0 + 15 < p.N) {
+      if (full) {
         float4 o[4];
         tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
 #pragma unroll
@@ -305,19 +331,6 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
             for (int e = 0; e < 4; ++e)
               if (col + e < p.N) gemm_store<float, MODE>(p, row, col + e, v[j + e], spin);
         }
-      }
-    }
-    if (MODE == EPI_SILU_J) {
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        float q = valid ? v[j] * v[j] : 0.f;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          const float u = __shfl_down_sync(0xffffffffu, q, 1 << k);
-          if ((segm >> k) & 1u) q += u;
-        }
-        const int col = n0 + c0 + j;
-        if (valid && head && col < p.N) atomicAdd(&p.aux2[(long)node * p.ld_aux + col], q);
       }
     }
   }
