@@ -53,6 +53,24 @@ __global__ void k_env_coef(const T* __restrict__ r, const float* __restrict__ R,
   }
 }
 
+// two adjacent elements with one 16-byte (double, df64) or 8-byte (float) shared-memory load; p is aligned to
+// twice the element size
+__device__ __forceinline__ void ld_pair(const float* p, float& a, float& b) {
+  const float2 v = *reinterpret_cast<const float2*>(p);
+  a = v.x;
+  b = v.y;
+}
+__device__ __forceinline__ void ld_pair(const double* p, double& a, double& b) {
+  const double2 v = *reinterpret_cast<const double2*>(p);
+  a = v.x;
+  b = v.y;
+}
+__device__ __forceinline__ void ld_pair(const df64* p, df64& a, df64& b) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  a = df64(v.x, v.y);
+  b = df64(v.z, v.w);
+}
+
 constexpr int GJG_BW = 16, GJG_THREADS = 512;
 
 // Gauss-Jordan inversion / LU with partial pivoting, one matrix per CTA, the working matrix in global
@@ -194,9 +212,9 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
     // ---- L^-1 (one lane per column s: Li[t][s] = -sum_{u=s}^{t-1} L[t][u] Li[u][s]) and W~ = W L^-1
     if (tid < bw) {
       for (int t = 0; t < bw; ++t) {
-        S v = t == tid ? S(1) : S(0);
-        for (int u = tid; u < t; ++u) v = df_sub_mul(v, W[(k0 + t) * LD + u], Li[u * BW + tid]);
-        Li[t * BW + tid] = v;
+        SubDot<S> acc;
+        for (int u = tid; u < t; ++u) acc.add(W[(k0 + t) * LD + u], Li[u * BW + tid]);
+        Li[t * BW + tid] = acc.finish(t == tid ? S(1) : S(0));
       }
     }
     if (INV && cj < bw)  // panel into the next working copy (the LU never reads finished panels again)
@@ -218,45 +236,86 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
 #pragma unroll
       for (int t = 0; t < BW; ++t) {
         if (t >= bw) break;
-        S acc = S(0);
+        SubDot<S> acc;
 #pragma unroll
         for (int q = 0; q < BW; ++q)
-          if (q >= t && q < bw) acc += wr[q] * Li[q * BW + t];
-        W[i * LD + t] = acc;
+          if (q >= t && q < bw) acc.add(wr[q], Li[q * BW + t]);
+        W[i * LD + t] = acc.sum();
       }
     }
     __syncthreads();
-    // ---- apply the panel to the other columns: each thread owns one column of a BW-wide chunk and walks its
-    // rows, reading the interchanged rows of src and writing dst (no in-place hazard, no barrier per chunk)
-    for (int Q = INV ? 0 : P + 1; Q < npan; ++Q) {
-      if (Q == P) continue;
-      const int c0 = Q * BW, cb = min(BW, n - c0);
-      if (cj >= cb) continue;
-      const S* sc = src + c0 + cj;
-      S yv[BW];
+    // ---- apply the panel to the other columns (LU: the columns right of the panel, rows from k0):
+    // x <- x - W~ y with y the panel's pivot rows of x.  Y (the bw pivot rows of every column, interchanged
+    // order, rows padded to an even length) is staged over the panel buffer, which is free now; each thread
+    // owns a pair of adjacent columns and walks its rows two at a time (2 x 2 tiles: three shared loads per
+    // four products), reading the interchanged rows of src and writing dst (no in-place hazard).
+    S* Y = pan;
+    const int ldy = n + (n & 1);
+    for (int t = 0; t < bw; ++t) {
+      const S* yr = src + (size_t)rowmap[k0 + t] * n;
+      for (int c = (INV ? 0 : k0 + bw) + tid; c < n; c += blockDim.x) Y[t * ldy + c] = yr[c];
+    }
+    __syncthreads();
+    {
+      const int cp = tid & 15, rg = tid >> 4, rn2 = blockDim.x >> 4;  // column pair, row group
+      const int i0 = INV ? 0 : k0;
+      for (int c = (INV ? 0 : k0 + bw) + 2 * cp; c < n; c += 32) {
+        if (INV && c >= k0 && c < k0 + bw) continue;  // the panel's own columns (pairs never straddle it)
+        const bool c1 = c + 1 < n;
+        int i = i0 + rg;
+        for (; i + rn2 < n; i += 2 * rn2) {
+          const S* s0 = src + (size_t)rowmap[i] * n + c;
+          const S* s1 = src + (size_t)rowmap[i + rn2] * n + c;
+          const S a00 = s0[0], a10 = s1[0];
+          const S a01 = c1 ? s0[1] : S(0), a11 = c1 ? s1[1] : S(0);
+          const S *w0 = W + i * LD, *w1 = W + (i + rn2) * LD;
+          SubDot<S> d00, d01, d10, d11;
+          if (bw == BW) {
 #pragma unroll
-      for (int t = 0; t < BW; ++t) yv[t] = t < bw ? sc[(size_t)rowmap[k0 + t] * n] : S(0);
-      // two rows per pass: independent multiply-subtract chains hide each other's latency
-      int i = (INV ? 0 : k0) + rg;
-      for (; i + rn < n; i += 2 * rn) {
-        S a0 = sc[(size_t)rowmap[i] * n], a1 = sc[(size_t)rowmap[i + rn] * n];
-        const S *w0 = W + i * LD, *w1 = W + (i + rn) * LD;
-#pragma unroll
-        for (int t = 0; t < BW; ++t)
-          if (t < bw) {
-            a0 = df_sub_mul(a0, w0[t], yv[t]);
-            a1 = df_sub_mul(a1, w1[t], yv[t]);
+            for (int t = 0; t < BW; ++t) {
+              S y0, y1;
+              ld_pair(Y + t * ldy + c, y0, y1);
+              const S wa = w0[t], wb = w1[t];
+              d00.add(wa, y0);
+              d01.add(wa, y1);
+              d10.add(wb, y0);
+              d11.add(wb, y1);
+            }
+          } else {
+            for (int t = 0; t < bw; ++t) {
+              S y0, y1;
+              ld_pair(Y + t * ldy + c, y0, y1);
+              const S wa = w0[t], wb = w1[t];
+              d00.add(wa, y0);
+              d01.add(wa, y1);
+              d10.add(wb, y0);
+              d11.add(wb, y1);
+            }
           }
-        dst[(size_t)i * n + c0 + cj] = a0;
-        dst[(size_t)(i + rn) * n + c0 + cj] = a1;
-      }
-      if (i < n) {
-        S acc = sc[(size_t)rowmap[i] * n];
-        const S* wi = W + i * LD;
-#pragma unroll
-        for (int t = 0; t < BW; ++t)
-          if (t < bw) acc = df_sub_mul(acc, wi[t], yv[t]);
-        dst[(size_t)i * n + c0 + cj] = acc;
+          S* o0 = dst + (size_t)i * n + c;
+          S* o1 = dst + (size_t)(i + rn2) * n + c;
+          o0[0] = d00.finish(a00);
+          o1[0] = d10.finish(a10);
+          if (c1) {
+            o0[1] = d01.finish(a01);
+            o1[1] = d11.finish(a11);
+          }
+        }
+        if (i < n) {
+          const S* s0 = src + (size_t)rowmap[i] * n + c;
+          const S a00 = s0[0], a01 = c1 ? s0[1] : S(0);
+          const S* w0 = W + i * LD;
+          SubDot<S> d00, d01;
+          for (int t = 0; t < bw; ++t) {
+            S y0, y1;
+            ld_pair(Y + t * ldy + c, y0, y1);
+            d00.add(w0[t], y0);
+            d01.add(w0[t], y1);
+          }
+          S* o0 = dst + (size_t)i * n + c;
+          o0[0] = d00.finish(a00);
+          if (c1) o0[1] = d01.finish(a01);
+        }
       }
     }
     __syncthreads();  // dst complete before the next panel reads it

@@ -76,6 +76,42 @@ __device__ __forceinline__ df64 df_sub_mul(df64 a, df64 b, df64 c) {
   const float t = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(-p, v));
   return df_quick_two_sum(s, __fadd_rn(t, __fsub_rn(a.lo, e)));
 }
+// a - sum_t b_t y_t for float, double and df64.  The df64 form is the compensated dot product "Dot2" of
+// Ogita, Rump & Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005), extended to double-FP32
+// factors: the FP32 sum s of the leading products carries a TwoSum per term, and every rounding error (the
+// exact low part of b.hi y.hi by FMA, the cross terms b.hi y.lo + b.lo y.hi, the TwoSum errors) goes into one
+// FP32 correction c.  12 FP32 operations per term with a one-add dependency chain on s (df_sub_mul chains ~9
+// dependent operations per term); a itself enters once at the end, so loading it overlaps the products.
+template <typename S>
+struct SubDot {
+  S s;
+  __device__ __forceinline__ SubDot() : s(S(0)) {}
+  __device__ __forceinline__ void add(S b, S y) { s = fma(b, y, s); }
+  __device__ __forceinline__ S finish(S a) const { return a - s; }
+  __device__ __forceinline__ S sum() const { return s; }
+};
+template <>
+struct SubDot<df64> {
+  float s, c;
+  __device__ __forceinline__ SubDot() : s(0.f), c(0.f) {}
+  __device__ __forceinline__ void add(df64 b, df64 y) {
+    const float p = __fmul_rn(b.hi, y.hi);
+    const float e = __fmaf_rn(b.hi, y.hi, -p);
+    c = __fmaf_rn(b.hi, y.lo, c);
+    c = __fmaf_rn(b.lo, y.hi, c);
+    const float s1 = __fadd_rn(s, p);
+    const float bb = __fsub_rn(s1, s);
+    const float q = __fadd_rn(__fsub_rn(s, __fsub_rn(s1, bb)), __fsub_rn(p, bb));
+    c = __fadd_rn(c, __fadd_rn(q, e));
+    s = s1;
+  }
+  // a - (s + c) and s + c; full TwoSums (once per dot product): after cancellation c may outweigh s
+  __device__ __forceinline__ df64 finish(df64 a) const {
+    const df64 r = df_two_sum(a.hi, -s);
+    return df_two_sum(r.hi, __fadd_rn(r.lo, __fsub_rn(a.lo, c)));
+  }
+  __device__ __forceinline__ df64 sum() const { return df_two_sum(s, c); }
+};
 __device__ __forceinline__ bool operator==(df64 a, df64 b) { return a.hi == b.hi && a.lo == b.lo; }
 __device__ __forceinline__ bool operator!=(df64 a, df64 b) { return !(a == b); }
 __device__ __forceinline__ bool operator<(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }

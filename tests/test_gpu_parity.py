@@ -148,6 +148,25 @@ def test_logpsi(cuda_lib, name, precision):
 @pytest.mark.parametrize("precision", ["fp32", "fp64", "mixed"])
 def test_local_energy(cuda_lib, name, precision):
     wf, mol, nu, r, p = _wf(name, precision)
+    _check_local_energy(wf, mol, nu, r, p, precision)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64", "mixed"])
+def test_local_energy_odd_electron_count(cuda_lib, precision):
+    """H21 chain: 21 electrons (11 up, 10 down), so the elimination's last panel is 5 columns wide, the last
+    column of the matrix has no pair partner and the staged pivot rows are padded; walkers and parameters
+    from seeds, the oracle evaluated here."""
+    from make_golden import make_params
+
+    mol = systems.hydrogen_chain(21, 1.8)
+    nu, _ = systems.spin_counts(mol)
+    r = systems.init_electrons(mol, 3, 21).astype(np.float32)
+    _, p, _, _ = make_params(mol, nu, r[0], seed=5, activate=True)
+    wf = FireWaveFunction(mol, precision=precision)
+    _check_local_energy(wf, mol, nu, r, p, precision)
+
+
+def _check_local_energy(wf, mol, nu, r, p, precision):
     rr = r.astype(np.float64) if precision == "fp64" else r
     static = _static(wf, rr)
     eloc, aux = wf.local_energy_full(p, rr, static, debug=True)
