@@ -128,9 +128,9 @@ const TcSrc kTcSrc[TC_COUNT] = {{PR_UPD1_W_S0, 1},   {FIRE_P_UPD2_W, 1},    {PR_
                                 {FIRE_P_JMLP2_W, 1}, {FIRE_P_EI_GLU_W, 2},  {FIRE_P_EI_DENSE_W, 1},
                                 {FIRE_P_EI_OUT_W, 5}, {PR_ENV_UP_PI, -1},   {PR_ENV_DN_PI, -1},
                                 {PR_QK_W_S1, -2}};
-// K, N and the number of matrices of a slot.  Its BF16 copy: for K <= 256 the pre-tiled split of every
-// matrix (tc_tiles_bytes each, for the A-resident kernel), else hi [cnt][N][K] followed by lo [cnt][N][K]
-// (for the streamed-weight kernel).
+// K, N and the number of matrices of a slot.  Its BF16 copy: the pre-tiled split of every matrix
+// (tc_tiles_bytes each) for the A-resident kernel (K <= 256) and the envelope kernel, else hi [cnt][N][K]
+// followed by lo [cnt][N][K] (for the streamed-weight kernel).
 void tc_shape(int k, const fire_problem* p, size_t* K, size_t* N, int* cnt) {
   const int kind = kTcSrc[k].kind;
   *K = kind == -1 ? (size_t)NENV_ORB * p->n_nuc : (size_t)F;
@@ -138,6 +138,7 @@ void tc_shape(int k, const fire_problem* p, size_t* K, size_t* N, int* cnt) {
                 : (kind == 0 ? (size_t)NDET * p->n_el : (kind == -1 ? (size_t)p->n_el : (size_t)HEADS));
   *cnt = kind == -1 ? NDET : 1;
 }
+bool tc_tiled(int k, size_t K) { return K <= 256 || kTcSrc[k].kind == -1; }
 // byte offsets of the BF16 region (tc_off[TC_COUNT] = end)
 void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
   size_t o = (float_bytes + 255) / 256 * 256;
@@ -146,7 +147,7 @@ void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
     size_t K, N;
     int cnt;
     tc_shape(k, p, &K, &N, &cnt);
-    o += K <= 256 ? (size_t)cnt * tc_tiles_bytes(K, N) : 2 * (size_t)cnt * N * K * sizeof(__nv_bfloat16);
+    o += tc_tiled(k, K) ? (size_t)cnt * tc_tiles_bytes(K, N) : 2 * (size_t)cnt * N * K * sizeof(__nv_bfloat16);
     o = (o + 255) / 256 * 256;
   }
   off[TC_COUNT] = o;
@@ -612,41 +613,6 @@ cudaError_t linear_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt,
 }
 
 // envelopes + orbital matrices (+ their Jacobian/Laplacian planes)
-// Envelope contraction of one determinant and spin (EPI_ENV).  In the mixed path the derivative rows of
-// the [x, jac(3), lap] carrier run on the tensor cores with the split weights of that determinant, the
-// value rows (every NV-th) on the CUDA cores in FP32.
-template <typename T>
-cudaError_t env_gemm(Ctx<T>& c, const GemmP<T>& g, int NV, int tc_slot, int d) {
-  if constexpr (sizeof(T) == 4) {
-    if (c.mixed && NV > 1) {
-      size_t K, N;
-      int cnt;
-      tc_shape(tc_slot, c.p, &K, &N, &cnt);
-      TcWeights wd{};
-      if (K <= 256) wd.tiles = c.tcw[tc_slot].tiles + (size_t)d * tc_tiles_bytes(K, N) / 2;
-      else {
-        wd.hi = c.tcw[tc_slot].hi + (size_t)d * N * K;
-        wd.lo = c.tcw[tc_slot].lo + (size_t)d * N * K;
-      }
-      GemmP<T> gt = g;
-      gt.row_skip = NV;
-      {
-        Prof pr("gemm", c.s);
-        g_nlaunch++;
-        const cudaError_t e = gemm_tc(EPI_ENV, 128, gt, wd, nullptr, c.status, c.s);
-        if (e != cudaSuccess) return e;
-      }
-      GemmP<T> gv = g;  // value rows: electron rows of stride NV, destination rows of stride NV
-      gv.lda = g.lda * NV;
-      gv.M = g.M / NV;
-      gv.env_nv = 1;
-      gv.ldc = g.ldc * NV;
-      return gemm<T, EPI_ENV>(c, gv);
-    }
-  }
-  return gemm<T, EPI_ENV>(c, g);
-}
-
 template <typename T, int NT>
 cudaError_t stage_orbitals(Ctx<T>& c) {
   constexpr int NV = NT > 0 ? NT + 2 : 1;
@@ -658,18 +624,40 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
     const int ns = s == 0 ? nu : n - nu;
     if (ns == 0) continue;
     T* coef = c.template buf<T>(s == 0 ? c.P.coef_up : c.P.coef_dn);
-    const long tot = (long)c.Wc * ns * N * NENV_ORB;
+    const T* sp = c.W.w[s == 0 ? PR_ENV_UP_SP : PR_ENV_DN_SP];
+    const long tot = (long)c.Wc * ns * N * NENV_ORB, K8 = (long)N * NENV_ORB;
+    // mixed path: the derivative rows come from k_env_tc (coefficients generated on chip, tensor cores), so
+    // only the value coefficients are materialised, for the FP32 contraction of the value rows
+    const bool tc_env = sizeof(T) == 4 && c.mixed && NV > 1;
+    const int nvc = tc_env ? 1 : NV;  // coefficient rows per electron
     g_nlaunch++;
-    k_env_coef<T, NV><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, c.W.w[s == 0 ? PR_ENV_UP_SP : PR_ENV_DN_SP], n, ns,
-                                                  s == 0 ? 0 : nu, N, c.Wc, coef);
-    const long rows = (long)c.Wc * ns * NV, K8 = (long)N * NENV_ORB;
+    if (tc_env)
+      k_env_coef<T, 1><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, sp, n, ns, s == 0 ? 0 : nu, N, c.Wc, coef);
+    else
+      k_env_coef<T, NV><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, sp, n, ns, s == 0 ? 0 : nu, N, c.Wc, coef);
+    const long rows = (long)c.Wc * ns * nvc;
     for (int d = 0; d < NDET; ++d) {
+      if constexpr (sizeof(T) == 4) {
+        if (tc_env) {
+          const int slot = s == 0 ? TC_ENV_UP : TC_ENV_DN;
+          float* C = env + (long)d * n;
+          const long ldc = (long)DN;
+          const uintptr_t a = reinterpret_cast<uintptr_t>(C);
+          const int vec = (a % 16 == 0 && ldc % 4 == 0) ? 4 : ((a % 8 == 0 && ldc % 2 == 0) ? 2 : 1);
+          const EnvTcP ep{c.r, c.R, sp, C, ldc, n, ns, s == 0 ? 0 : nu, N, c.Wc, d, NV, vec};
+          Prof pg("gemm", c.s);
+          g_nlaunch++;
+          const cudaError_t e =
+              env_tc(ep, c.tcw[slot].tiles + (size_t)d * tc_tiles_bytes((size_t)K8, (size_t)n) / 2, c.status, c.s);
+          if (e != cudaSuccess) return e;
+        }
+      }
       GemmP<T> g = gp0<T>();
       g.A = coef + d * rows * K8; g.lda = K8;
       g.B = c.W.w[s == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (long)d * K8 * n; g.ldb = n;
-      g.C = env + (long)d * n; g.ldc = DN; g.M = (int)rows; g.N = n; g.K = (int)K8;
-      g.n_el = n; g.env_ns = ns; g.env_soff = s == 0 ? 0 : nu; g.env_nv = NV;
-      env_gemm<T>(c, g, NV, s == 0 ? TC_ENV_UP : TC_ENV_DN, d);
+      g.C = env + (long)d * n; g.ldc = (long)DN * (NV / nvc); g.M = (int)rows; g.N = n; g.K = (int)K8;
+      g.n_el = n; g.env_ns = ns; g.env_soff = s == 0 ? 0 : nu; g.env_nv = nvc;
+      gemm<T, EPI_ENV>(c, g);
     }
   }
   GemmP<T> g = gp0<T>();
@@ -943,7 +931,7 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
       int cnt;
       tc_shape(k, p, &K, &N, &cnt);
       const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
-      if (K <= 256) c.tcw[k] = TcWeights{nullptr, nullptr, nullptr, nullptr, hi, nullptr};
+      if (tc_tiled(k, K)) c.tcw[k] = TcWeights{nullptr, nullptr, nullptr, nullptr, hi, nullptr};
       else c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr, nullptr, nullptr};
     }
     c.tcw[TC_ORB_UP].tiles2 = c.tcw[TC_ORB_DN].tiles;
@@ -1104,7 +1092,7 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
     for (int m = 0; m < cnt; ++m) {
       const float* src = reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot] + (size_t)m * K * N;
       g_nlaunch++;
-      if (K <= 256) split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s);
+      if (tc_tiled(k, K)) split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s);
       else split_transpose(src, (int)K, (int)N, hi + (size_t)m * N * K, lo + (size_t)m * N * K, s);
     }
   }

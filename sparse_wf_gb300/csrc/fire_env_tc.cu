@@ -1,0 +1,307 @@
+// fire_env_tc.cu -- envelope contraction of the mixed path with its coefficients generated on chip.
+//
+// For electron g of one spin block and determinant d, the derivative rows of the envelope carrier are
+//   env[g][v][d n + o] = sum_{I, k} c_v(g, I, k) pi_d[8 I + k][o],   v = jac x, y, z and lap,
+// with the forward-Laplacian coefficients of exp(-a |r_g - R_I|), a = softplus(sigma)[I][d][k]
+// (EfficientIsotropicEnvelopes, envelopes.py:55-82; the same expressions as k_env_coef):
+//   jac: -a e (r_g - R_I) / rho,   lap: e (a^2 - 2 a / rho),   e = exp(-a rho), rho = |r_g - R_I|.
+// The coefficient matrix (8 N columns for each of 4 rows per electron) is never written to memory.  Four
+// producer warps compute every 128 x 64 A block -- 32 electrons x 4 planes (plane-major: tile row
+// v * 32 + electron) by 8 nuclei x 8 envelopes -- directly into shared memory as split BF16 (hi + lo, as in
+// k_gemm_tca): one thread per (electron, nucleus) evaluates rho once and the 8 exponentials and writes whole
+// 16-byte core-matrix rows.  The determinant's pre-tiled split weights stream in by bulk copies; three
+// BF16 MMAs per 16-deep step into a TMEM accumulator, two accumulators so that the epilogue of one tile
+// overlaps the MMAs of the next; every wait is bounded.  The value row (coefficient e) stays on the FP32
+// CUDA-core contraction.
+#include "fire_tc.cuh"
+
+namespace fire {
+
+constexpr int ENV_THREADS = 448, ENV_STAGES = 3;
+struct EnvCfg {
+  static constexpr int A_BYTES = TC_BM * TC_BK * 2;       // one BF16 plane of a 128 x 64 A block
+  static constexpr int A_BLOCK = 2 * A_BYTES;             // hi + lo
+  static constexpr int B_BLOCK = 2 * TCP_BN * TC_BK * 2;  // one pre-tiled weight block (hi + lo)
+  static constexpr int STAGE = A_BLOCK + B_BLOCK;
+  static constexpr int TOTAL = ENV_STAGES * STAGE + 256;
+};
+struct EnvBar {
+  uint64_t afull[ENV_STAGES], bfull[ENV_STAGES], empty[ENV_STAGES], tfull[2], tempty[2];
+  uint32_t tmem;
+  int abort;
+};
+
+// the 4 derivative coefficients of the 8 envelopes of nucleus I for an electron at (rx, ry, rz), split into
+// BF16 hi and lo planes: word w of plane v holds envelopes 2w (low half) and 2w + 1
+__device__ __forceinline__ void env_coef_rows(const EnvTcP& p, bool ok, float rx, float ry, float rz, int I,
+                                              uint4 (&hi)[4], uint4 (&lo)[4]) {
+  float c[4][NENV_ORB];
+  if (ok) {
+    const float dx = rx - p.R[3 * I], dy = ry - p.R[3 * I + 1], dz = rz - p.R[3 * I + 2];
+    const float rho = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float irho = 1.f / rho;
+    const float* a = p.sp + ((long)I * NDET + p.d) * NENV_ORB;
+#pragma unroll
+    for (int k = 0; k < NENV_ORB; ++k) {
+      const float ak = a[k];
+      const float e = expf(-ak * rho);
+      const float gj = -ak * e * irho;
+      c[0][k] = gj * dx;
+      c[1][k] = gj * dy;
+      c[2][k] = gj * dz;
+      c[3][k] = e * (ak * ak - 2.f * ak * irho);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+      for (int k = 0; k < NENV_ORB; ++k) c[v][k] = 0.f;
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const __nv_bfloat162 hb = __floats2bfloat162_rn(c[v][2 * w], c[v][2 * w + 1]);
+      const float2 hf = __bfloat1622float2(hb);
+      const __nv_bfloat162 lb = __floats2bfloat162_rn(c[v][2 * w] - hf.x, c[v][2 * w + 1] - hf.y);
+      h[w] = *reinterpret_cast<const uint32_t*>(&hb);
+      l[w] = *reinterpret_cast<const uint32_t*>(&lb);
+    }
+    hi[v] = make_uint4(h[0], h[1], h[2], h[3]);
+    lo[v] = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+// Bt: the determinant's tiled split weights [ceil(n / 128)][ceil(8 N / 64)] blocks of EnvCfg::B_BLOCK bytes.
+// Each CTA owns one 128-column slice of the output (blockIdx.x % nt) and walks the 32-electron tiles.
+__global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_bfloat16* Bt, int32_t* status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];  // [stage][A hi, A lo, B hi, B lo]
+  EnvBar* bars = reinterpret_cast<EnvBar*>(tc_smem + ENV_STAGES * EnvCfg::STAGE);
+  volatile int* abort = &bars->abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n_e = p.Wc * p.ns;
+  const int mt = (n_e + 31) / 32, nt = (p.n + TCP_BN - 1) / TCP_BN;
+  const int nk = (NENV_ORB * p.N + TC_BK - 1) / TC_BK;
+  const int groups = gridDim.x / nt;
+  const int j = blockIdx.x % nt, m_first = blockIdx.x / nt;
+  if (m_first >= mt) return;
+  const int n0 = j * TCP_BN;
+
+  if (tid == 0) {
+    for (int s = 0; s < ENV_STAGES; ++s) {
+      mbar_init(smem_u32(&bars->afull[s]), 128);
+      mbar_init(smem_u32(&bars->bfull[s]), 1);
+      mbar_init(smem_u32(&bars->empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&bars->tfull[b]), 1);
+      mbar_init(smem_u32(&bars->tempty[b]), 256);
+    }
+    bars->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 12) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem)),
+                 "r"(2 * TCP_BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  proxy_fence();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = bars->tmem;
+  long b_issued = 0;  // weight blocks issued (loader lane)
+
+  if (warp >= 8 && warp < 12) {
+    // ------------------------------------------------------------------ A producers (128 threads)
+    // thread (lw, lane): electron lane of the tile, nuclei 2 lw and 2 lw + 1 of every 8-nucleus block
+    const int lw = warp - 8;
+    long kc = 0;
+    for (int m = m_first; m < mt && !*abort; m += groups) {
+      const int e = m * 32 + lane;
+      const bool ve = e < n_e;
+      float rx = 0.f, ry = 0.f, rz = 0.f;
+      if (ve) {
+        const long g = (long)(e / p.ns) * p.n + p.soff + e % p.ns;
+        rx = p.r[3 * g];
+        ry = p.r[3 * g + 1];
+        rz = p.r[3 * g + 2];
+      }
+      for (int kb = 0; kb < nk; ++kb, ++kc) {
+        const int s = (int)(kc % ENV_STAGES);
+        const long use = kc / ENV_STAGES;
+        if (use > 0 && !tc_wait(&bars->empty[s], (uint32_t)((use - 1) & 1), abort)) break;
+        unsigned char* a_hi = tc_smem + s * EnvCfg::STAGE;
+        unsigned char* a_lo = a_hi + EnvCfg::A_BYTES;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int il = 2 * lw + q, I = kb * 8 + il;
+          uint4 hi[4], lo[4];
+          env_coef_rows(p, ve && I < p.N, rx, ry, rz, I, hi, lo);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const uint32_t off = tc_off(v * 32 + lane, il * 8);
+            *reinterpret_cast<uint4*>(a_hi + off) = hi[v];
+            *reinterpret_cast<uint4*>(a_lo + off) = lo[v];
+          }
+        }
+        proxy_fence();
+        tc_arrive(&bars->afull[s]);
+      }
+    }
+  } else if (warp == 13) {
+    // ------------------------------------------------------------------ weight loader
+    if (lane == 0) {
+      long kc = 0;
+      for (int m = m_first; m < mt && !*abort; m += groups)
+        for (int kb = 0; kb < nk; ++kb, ++kc) {
+          const int s = (int)(kc % ENV_STAGES);
+          const long use = kc / ENV_STAGES;
+          if (use > 0 && !tc_wait(&bars->empty[s], (uint32_t)((use - 1) & 1), abort)) break;
+          const unsigned char* src =
+              reinterpret_cast<const unsigned char*>(Bt) + ((size_t)j * nk + kb) * (size_t)EnvCfg::B_BLOCK;
+          bulk_load(smem_u32(tc_smem + s * EnvCfg::STAGE + EnvCfg::A_BLOCK), src, EnvCfg::B_BLOCK,
+                    smem_u32(&bars->bfull[s]));
+          b_issued = kc + 1;
+        }
+    }
+  } else if (warp == 12) {
+    // ------------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc<TCP_BN>();
+      long kc = 0, uc = 0;
+      for (int m = m_first; m < mt && !*abort; m += groups) {
+        const int b = (int)(uc & 1);
+        const long ub = uc >> 1;
+        if (ub > 0 && !tc_wait(&bars->tempty[b], (uint32_t)((ub - 1) & 1), abort)) break;
+        tc_fence_after();
+        const uint32_t acc_t = tmem + (uint32_t)(b * TCP_BN);
+        for (int kb = 0; kb < nk; ++kb, ++kc) {
+          const int s = (int)(kc % ENV_STAGES);
+          const uint32_t par = (uint32_t)((kc / ENV_STAGES) & 1);
+          if (!tc_wait(&bars->afull[s], par, abort) || !tc_wait(&bars->bfull[s], par, abort)) break;
+          tc_fence_after();
+          const uint32_t ah = smem_u32(tc_smem + s * EnvCfg::STAGE), al = ah + EnvCfg::A_BYTES;
+          const uint32_t bh = ah + EnvCfg::A_BLOCK, bl = bh + EnvCfg::B_BLOCK / 2;
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 16; ++kk) {
+            const uint32_t sa = kk * 2 * TC_LBO, sb = kk * 2 * 2048;
+            const uint64_t dah = tc_desc(ah + sa), dal = tc_desc(al + sa);
+            const uint64_t dbh = tc_desc_s(bh + sb, 2048, 128), dbl = tc_desc_s(bl + sb, 2048, 128);
+            tc_mma(acc_t, dah, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            tc_mma(acc_t, dah, dbl, idesc, 1u);
+            tc_mma(acc_t, dal, dbh, idesc, 1u);
+          }
+          tc_commit(smem_u32(&bars->empty[s]));
+        }
+        if (*abort) break;
+        tc_commit(smem_u32(&bars->tfull[b]));
+        ++uc;
+      }
+    }
+  } else {
+    // ------------------------------------------------------------------ epilogue (warps 0-7, 256 threads)
+    // warp w: TMEM lane quadrant w % 4 = plane v (jac x, y, z, lap), lane = electron, column half w / 4
+    const int quad = warp & 3, half = warp >> 2;
+    long uc = 0;
+    for (int m = m_first; m < mt && !*abort; m += groups) {
+      const int b = (int)(uc & 1);
+      if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
+      tc_fence_after();
+      const int e = m * 32 + lane;
+      float* out = nullptr;
+      if (e < n_e) {
+        const long g = (long)(e / p.ns) * p.n + p.soff + e % p.ns;
+        out = p.C + (g * p.nv + quad + 1) * p.ldc;
+      }
+      const uint32_t base = tmem + (uint32_t)(b * TCP_BN) + ((uint32_t)(quad * 32) << 16);
+      for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
+        const int col = n0 + c0;
+        if (col >= p.n) break;  // warp-uniform
+        float v[16];
+        tmem_ld16(base + (uint32_t)c0, v);
+        if (!out) continue;
+        if (p.vec == 4 && col + 15 < p.n) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) st4(out + col + 4 * u, make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]));
+        } else if (p.vec == 2 && col + 15 < p.n) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) *reinterpret_cast<float2*>(out + col + 2 * u) = make_float2(v[2 * u], v[2 * u + 1]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if (col + k < p.n) out[col + k] = v[k];
+        }
+      }
+      tc_fence_before();
+      tc_arrive(&bars->tempty[b]);
+      ++uc;
+    }
+  }
+  __syncthreads();
+  if (*abort && tid == 0) set_flag(status, FIRE_FLAG_TIMEOUT);
+  if (*abort && warp == 13 && lane == 0) {
+    // bounded drain: weight copies still in flight must land before the CTA's shared memory goes away
+    for (long q = b_issued > ENV_STAGES ? b_issued - ENV_STAGES : 0; q < b_issued; ++q) {
+      const uint32_t a = smem_u32(&bars->bfull[q % ENV_STAGES]);
+      const uint32_t par = (uint32_t)((q / ENV_STAGES) & 1);
+      for (int i = 0; i < (1 << 16); ++i) {
+        uint32_t d0;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d0)
+            : "r"(a), "r"(par)
+            : "memory");
+        if (d0) break;
+      }
+    }
+  }
+  if (*abort && warp == 12 && lane == 0) {
+    // bounded drain: an MMA still in flight must finish before tensor memory is released
+    for (int s = 0; s < ENV_STAGES; ++s) {
+      const uint32_t a = smem_u32(&bars->empty[s]);
+      for (int i = 0; i < (1 << 16); ++i) {
+        uint32_t d0, d1;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d0)
+            : "r"(a)
+            : "memory");
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 1;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(d1)
+            : "r"(a)
+            : "memory");
+        if (d0 || d1) break;
+      }
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 12) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TCP_BN));
+  }
+}
+
+cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cudaStream_t s) {
+  static int num_sms = 0;
+  if (num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (num_sms <= 0) num_sms = 1;
+  }
+  if (!Bt || (reinterpret_cast<uintptr_t>(Bt) & 15) != 0) return cudaErrorInvalidValue;
+  const long n_e = (long)p.Wc * p.ns;
+  if (n_e <= 0 || p.n <= 0) return cudaSuccess;
+  const long mt = (n_e + 31) / 32, nt = (p.n + TCP_BN - 1) / TCP_BN;
+  const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
+  constexpr int smem = EnvCfg::TOTAL;
+  const cudaError_t e = cudaFuncSetAttribute(k_env_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_env_tc<<<(unsigned)(groups * nt), ENV_THREADS, smem, s>>>(p, Bt, status);
+  return cudaPeekAtLastError();
+}
+
+}  // namespace fire

@@ -43,6 +43,17 @@ struct TcWeights {
   const __nv_bfloat16* tiles;   // split weights pre-tiled for the A-resident kernel (K <= 256)
   const __nv_bfloat16* tiles2;  // the other spin's tiles, or nullptr
 };
+// Envelope derivative rows of the mixed path (k_env_tc): electrons of one spin block (ns per walker, offset
+// soff) of Wc walkers, determinant d.  C = env + d n, row stride ldc floats, nv carrier rows per electron;
+// vec = 4 / 2 / 1: widest store the alignment of C and ldc allows.
+struct EnvTcP {
+  const float* r;   // electron positions [W][n][3]
+  const float* R;   // nuclei [N][3]
+  const float* sp;  // softplus(sigma) [N][NDET][NENV_ORB]
+  float* C;
+  long ldc;
+  int n, ns, soff, N, Wc, d, nv, vec;
+};
 // bytes of the pre-tiled split weights of a K x N matrix: 32 KB per 128-column x 64-deep tile
 inline size_t tc_tiles_bytes(size_t K, size_t N) { return ((N + 127) / 128) * ((K + 63) / 64) * 32768; }
 

@@ -75,6 +75,7 @@ __global__ void k_accept(T* r, const T* rn, T* logpsi, const T* logpsi_new, int 
 // fire_tc.cu (host launchers)
 cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __nv_bfloat16* lo, cudaStream_t s);
 cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s);
+cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cudaStream_t s);
 template <typename T>
 struct GemmP;
 cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt, int* mask_buf, int32_t* status,

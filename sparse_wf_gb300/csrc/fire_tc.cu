@@ -35,6 +35,21 @@ __global__ void k_split_tiles(const float* __restrict__ W, int K, int N, __nv_bf
   base[8192 + w] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
+__global__ void k_tile_mask(GemmP<float> p, int* mask) {
+  const int m_tile = blockIdx.x;
+  int rows = p.M;
+  if (p.M_dev) rows = min(rows, p.M_scale * (*p.M_dev));
+  const int row = m_tile * TC_BM + threadIdx.x;
+  int up = 0, dn = 0;
+  if (row < rows) {
+    const int node = gemm_node(p, row);
+    if ((node % p.n_el) < p.n_up) up = 1; else dn = 1;
+  }
+  up = __syncthreads_or(up);
+  dn = __syncthreads_or(dn);
+  if (threadIdx.x == 0) mask[m_tile] = up | (dn << 1);
+}
+
 cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s) {
   const long tot = (long)((N + 127) / 128) * ((K + 63) / 64) * 8192;
   k_split_tiles<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, Bt);
@@ -110,7 +125,6 @@ cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt
     FIRE_TC_CASE(EPI_SILU_L)
     FIRE_TC_CASE(EPI_ORB_J)
     FIRE_TC_CASE(EPI_ORB_L)
-    FIRE_TC_CASE(EPI_ENV)
     default:
       return cudaErrorInvalidValue;
   }

@@ -807,20 +807,8 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
   }
 }
 
-__global__ void k_tile_mask(GemmP<float> p, int* mask) {
-  const int m_tile = blockIdx.x;
-  int rows = p.M;
-  if (p.M_dev) rows = min(rows, p.M_scale * (*p.M_dev));
-  const int row = m_tile * TC_BM + threadIdx.x;
-  int up = 0, dn = 0;
-  if (row < rows) {
-    const int node = gemm_node(p, row);
-    if ((node % p.n_el) < p.n_up) up = 1; else dn = 1;
-  }
-  up = __syncthreads_or(up);
-  dn = __syncthreads_or(dn);
-  if (threadIdx.x == 0) mask[m_tile] = up | (dn << 1);
-}
+// per 128-row tile: bit 0 if it holds a spin-up electron's row, bit 1 if a spin-down one (fire_tc.cu)
+__global__ void k_tile_mask(GemmP<float> p, int* mask);
 
 // Tensor map over C for the TMA-store epilogue (box 16 columns x 32 rows); false if unavailable.
 bool tc_c_map(const GemmP<float>& p, CUtensorMap* map);
