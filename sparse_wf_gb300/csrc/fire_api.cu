@@ -225,7 +225,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.rjs, G * 3 * DN, es);
     take(P.lapA, G * DN, es);
     take(P.Jorb, Jr * DN, es);
-    take(P.Ainv, W * NDET * n * n, es);
+    take(P.Ainv, W * NDET * n * (size_t)ainv_ld((int)n), es);
     take(P.dgrad, W * NDET * n * 3, es);
   }
   take(P.aX, G * HEADS, es);
@@ -877,7 +877,7 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {
     const size_t es = sizeof(T);
-    const size_t smem = es * std::max<size_t>(32 * DL_RP_DECL + 32 * DL_CMAX_DECL, 3 * DL_CMAX_DECL * (DL_CMAX_DECL + 1));
+    const size_t smem = es * DL_SMEM_ELEMS;
     cudaFuncSetAttribute(k_detlap<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     Prof pr("detlap", c.s);
     g_nlaunch++;

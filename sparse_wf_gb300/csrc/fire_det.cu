@@ -71,6 +71,10 @@ __device__ __forceinline__ void ld_pair(const df64* p, df64& a, df64& b) {
   b = df64(v.z, v.w);
 }
 
+__device__ __forceinline__ uint32_t smem_u32_det(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
 constexpr int GJG_BW = 16, GJG_THREADS = 512;
 
 // Gauss-Jordan inversion / LU with partial pivoting, one matrix per CTA, the working matrix in global
@@ -85,8 +89,9 @@ constexpr int GJG_BW = 16, GJG_THREADS = 512;
 //  3. every other column (LU: every column right of the panel) is streamed through shared memory in chunks
 //     of GJG_BW columns and updated with that rank-b product.
 // A: element (i, o) of matrix (w, d) at A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]).
-// Outputs: logdet[w * NDET + d], sign[...] (double); Ainv[(w * NDET + d) * n * n + o * n + i] (if INV),
-// written after undoing the column permutation.
+// Outputs: logdet[w * NDET + d], sign[...] (double); if INV the inverse, transposed and aligned for
+// k_detlap: Ainv[((w * NDET + d) * n + i) * ainv_ld(n) + sh + o] = (A^-1)[o][i] with sh = (d n) mod 4 and zeros
+// in the other entries of the row, written after undoing the column permutation.
 template <typename S, typename TI, typename TO, bool INV>
 __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restrict__ A, int n, S* __restrict__ work,
                                                              double* __restrict__ logdet, double* __restrict__ sign,
@@ -340,30 +345,68 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
       }
     }
     __syncthreads();
-    TO* out = Ainv + (size_t)mat * n * n;
+    // transposed output, row i = column i of the inverse, shifted by the determinant's offset sh within the
+    // orbital plane and zero-padded (see ainv_ld): 32 rows of the working matrix at a time are staged in
+    // shared memory (the panel buffers are free) so that both the reads and the writes are row-contiguous
+    const int nA = ainv_ld(n), sh = (d * n) & 3;
+    TO* out = Ainv + (size_t)mat * n * nA;
     const S* M = Mb[npan & 1];
-    for (int e = tid; e < n * n; e += blockDim.x) {
-      const int i = e / n, jc = e - i * n;
-      out[e] = (TO)M[(size_t)i * n + srcc[jc]];
+    S* tile = pan;  // [32][n]
+    for (int o0 = 0; o0 < n; o0 += 32) {
+      const int ro = min(32, n - o0);
+      for (int e = tid; e < ro * n; e += blockDim.x) tile[e] = M[(size_t)o0 * n + e];
+      __syncthreads();
+      for (int e = tid; e < n * 32; e += blockDim.x) {
+        const int i = e >> 5, r = e & 31;
+        if (r < ro) out[(size_t)i * nA + sh + o0 + r] = (TO)tile[r * n + srcc[i]];
+      }
+      __syncthreads();
+    }
+    const int npad = nA - n;
+    for (int e = tid; e < n * npad; e += blockDim.x) {
+      const int i = e / npad, q = e - i * npad;
+      out[(size_t)i * nA + (q < sh ? q : n + q)] = TO(0);
     }
   }
 }
 
 // Determinant Laplacian for one (walker, det, dependency m).  Jp: orbital Jacobian plane
-// [3 * positions][NDET * n]; Ainv [W][NDET][n][n]; lapA [G][NDET * n].
+// [3 * positions][NDET * n]; AinvT: the transposed, shifted inverse written by k_gj_global; lapA [G][NDET * n].
 // Outputs: grad [W][NDET][n][3], lap [W * NDET] (double, +=).
-// B = J[(i, m) rows] (3c x n) @ Ainv[:, {i}] (n x c) is computed with 2 x 4 register tiles from K-chunks
-// staged (J transposed) in shared memory; the next chunk is prefetched into registers while the current
-// one is multiplied.  The result tile reuses the staging memory.
-constexpr int DL_CMAX = 64, DL_RP = 197, DL_OC = 32;  // odd row stride: conflict-free transposed stores
-constexpr int DL_JPT = 3 * DL_CMAX * DL_OC / 256;  // J chunk elements per thread (24)
-constexpr int DL_APT = DL_OC * DL_CMAX / 256;      // Ainv chunk elements per thread (8)
+// B = J[(i, m) rows] (3c x n) @ A^-1[:, {i}] (n x c): both operands are read along the contraction index o
+// (J rows and rows of the transposed inverse), in 16-byte quads of x = o + sh where sh = (d n) mod 4 makes the
+// J rows of determinant d 16-byte aligned; the inverse rows carry the same shift and zeros outside o in [0, n),
+// which cancel the neighbouring columns the J quads pick up.  Chunks of DL_OC x are copied asynchronously
+// (cp.async) into double-buffered shared memory, rows of DL_LD elements; each thread accumulates 4 x 4 tiles
+// whose rows (r, r + TR, r + 2 TR, r + 3 TR) and columns (k, k + TC, ...) are strided, so that a warp's 16-byte
+// loads hit consecutive rows: 8 shared loads per 64 FMAs, no bank conflicts.  The result tile reuses the
+// staging memory.
+static_assert(3 * DL_CMAX * (DL_CMAX + 1) <= 2 * DL_JROWS * DL_LD, "result tile inside the staging buffers");
+constexpr int DL_MAXT = (3 * DL_CMAX / 4) * (DL_CMAX / 4) / 256;  // 4 x 4 tiles per thread (3)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool ok) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32_det(dst)), "l"(src), "r"(ok ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// four consecutive elements of a 16-byte aligned row
+__device__ __forceinline__ void ld_quad(const float* p, float (&v)[4]) {
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+__device__ __forceinline__ void ld_quad(const double* p, double (&v)[4]) {
+  const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
 template <typename T>
 __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __restrict__ Jp,
-                                                const T* __restrict__ Ainv, const T* __restrict__ lapA,
+                                                const T* __restrict__ AinvT, const T* __restrict__ lapA,
                                                 T* __restrict__ grad, double* __restrict__ lap, int32_t* status) {
   extern __shared__ __align__(16) unsigned char dl_smem[];
-  const int n = nb.n;
+  const int n = nb.n, nA = ainv_ld(n);
   const int m = blockIdx.x, d = blockIdx.y, w = blockIdx.z;
   const int* rp = nb.rowptr + (size_t)w * (n + 1);
   if (rp[n] > nb.cap_p) return;
@@ -372,93 +415,101 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
     if (threadIdx.x == 0) set_flag(status, FIRE_FLAG_PAIR_OVERFLOW);
     return;
   }
-  T* Jt = reinterpret_cast<T*>(dl_smem);  // [DL_OC][DL_RP]   J chunk, transposed
-  T* At = Jt + DL_OC * DL_RP;             // [DL_OC][DL_CMAX] Ainv chunk
+  T* Js = reinterpret_cast<T*>(dl_smem);  // [2][DL_JROWS][DL_LD] J rows, x chunk
+  T* As = Js + 2 * DL_JROWS * DL_LD;      // [2][DL_AROWS][DL_LD] inverse rows is[k], x chunk
   T* Bm = reinterpret_cast<T*>(dl_smem);  // [3 * DL_CMAX][DL_CMAX + 1] after the main loop
-  __shared__ long qrow[3 * DL_CMAX];      // J plane row of local row rr
+  __shared__ long qrow[3 * DL_CMAX];      // element index of x = 0 of J row rr
   __shared__ int is[DL_CMAX];
   const int tid = threadIdx.x;
   const int off = L.pos_off[w];
   const int s0 = off + rp[m] + m;
   const long ldj = (long)NDET * n;
+  const int sh = (d * n) & 3, XN = (sh + n + 3) & ~3;
   for (int k = tid; k < cnt; k += blockDim.x) {
     const int q = L.dep_pos[s0 + k];
     is[k] = L.pos_ctr[q] - w * n;
-    for (int t = 0; t < 3; ++t) qrow[3 * k + t] = (3L * q + t) * ldj + (long)d * n;
+    for (int t = 0; t < 3; ++t) qrow[3 * k + t] = (3L * q + t) * ldj + (long)d * n - sh;
   }
   __syncthreads();
   const int R = 3 * cnt;
-  const int rt = (R + 1) / 2, ct = (cnt + 3) / 4, ntile = rt * ct;
-  constexpr int MAXT = (3 * DL_CMAX / 2) * (DL_CMAX / 4) / 256;  // 6
-  T acc[MAXT][8];
+  const T* Ab = AinvT + ((size_t)w * NDET + d) * n * nA;
+  constexpr int QPR = DL_OC / 4;           // quads per row and chunk
+  constexpr int CPQ = 4 * sizeof(T) / 16;  // 16-byte copies per quad
+  const int nq = (R + cnt) * QPR;
+  auto stage = [&](int buf, int x0) {
+    for (int e = tid; e < nq; e += blockDim.x) {
+      const int row = e / QPR, qx = e - row * QPR;
+      const int x = x0 + 4 * qx;
+      T* dst;
+      const T* src;
+      if (row < R) {
+        dst = Js + ((size_t)buf * DL_JROWS + row) * DL_LD + 4 * qx;
+        src = Jp + qrow[row] + x;
+      } else {
+        const int k = row - R;
+        dst = As + ((size_t)buf * DL_AROWS + k) * DL_LD + 4 * qx;
+        src = Ab + (size_t)is[k] * nA + x;
+      }
+      const bool ok = x < XN;
 #pragma unroll
-  for (int u = 0; u < MAXT; ++u)
-#pragma unroll
-    for (int e = 0; e < 8; ++e) acc[u][e] = T(0);
-  const T* Ai = Ainv + ((size_t)w * NDET + d) * n * n;
-  T jr[DL_JPT], ar[DL_APT];
-  auto fetch = [&](int o0) {
-#pragma unroll
-    for (int u = 0; u < DL_JPT; ++u) {
-      const int e = tid + 256 * u;
-      const int rr = e / DL_OC, o = e - rr * DL_OC;
-      jr[u] = (rr < R && o0 + o < n) ? Jp[qrow[rr] + o0 + o] : T(0);
-    }
-#pragma unroll
-    for (int u = 0; u < DL_APT; ++u) {
-      const int e = tid + 256 * u;
-      const int o = e / DL_CMAX, k = e - o * DL_CMAX;
-      ar[u] = (k < cnt && o0 + o < n) ? Ai[(size_t)(o0 + o) * n + is[k]] : T(0);
+      for (int h = 0; h < CPQ; ++h) cp_async16(dst + h * (16 / sizeof(T)), ok ? src + h * (16 / sizeof(T)) : Ab, ok);
     }
   };
-  fetch(0);
-  for (int o0 = 0; o0 < n; o0 += DL_OC) {
+  const int TR = (R + 3) / 4, TC = (cnt + 3) / 4, ntile = TR * TC;
+  T acc[DL_MAXT][16];
 #pragma unroll
-    for (int u = 0; u < DL_JPT; ++u) {
-      const int e = tid + 256 * u;
-      const int rr = e / DL_OC, o = e - rr * DL_OC;
-      Jt[o * DL_RP + rr] = jr[u];
+  for (int u = 0; u < DL_MAXT; ++u)
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[u][e] = T(0);
+  const int nch = (XN + DL_OC - 1) / DL_OC;
+  stage(0, 0);
+  cp_async_commit();
+  for (int ch = 0; ch < nch; ++ch) {
+    if (ch + 1 < nch) {
+      stage((ch + 1) & 1, (ch + 1) * DL_OC);
+      cp_async_commit();
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
-#pragma unroll
-    for (int u = 0; u < DL_APT; ++u) At[tid + 256 * u] = ar[u];
     __syncthreads();
-    if (o0 + DL_OC < n) fetch(o0 + DL_OC);
+    const T* Jb = Js + (size_t)(ch & 1) * DL_JROWS * DL_LD;
+    const T* Ac = As + (size_t)(ch & 1) * DL_AROWS * DL_LD;
 #pragma unroll
-    for (int u = 0; u < MAXT; ++u) {
-      const int tile = tid + u * 256;
-      if (tile < ntile) {
-        const int r0 = (tile / ct) * 2, c0 = (tile % ct) * 4;
-#pragma unroll 8
-        for (int o = 0; o < DL_OC; ++o) {
-          const T a0 = Jt[o * DL_RP + r0], a1 = Jt[o * DL_RP + r0 + 1];
-          T b[4];
-          if constexpr (sizeof(T) == 4) {  // c0 % 4 == 0: one 16-byte load
-            const float4 bv = *reinterpret_cast<const float4*>(&At[o * DL_CMAX + c0]);
-            b[0] = bv.x; b[1] = bv.y; b[2] = bv.z; b[3] = bv.w;
-          } else {
+    for (int u = 0; u < DL_MAXT; ++u) {
+      const int t = tid + u * 256;
+      if (t < ntile) {
+        const int r0 = t / TC, k0 = t - r0 * TC;
+#pragma unroll 2
+        for (int qx = 0; qx < QPR; ++qx) {
+          T a[4][4], b[4][4];
 #pragma unroll
-            for (int y = 0; y < 4; ++y) b[y] = At[o * DL_CMAX + c0 + y];
-          }
+          for (int j = 0; j < 4; ++j) ld_quad(Jb + (r0 + TR * j) * DL_LD + 4 * qx, a[j]);
 #pragma unroll
-          for (int y = 0; y < 4; ++y) {
-            acc[u][y] += a0 * b[y];
-            acc[u][4 + y] += a1 * b[y];
-          }
+          for (int y = 0; y < 4; ++y) ld_quad(Ac + (k0 + TC * y) * DL_LD + 4 * qx, b[y]);
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int y = 0; y < 4; ++y)
+#pragma unroll
+              for (int o = 0; o < 4; ++o) acc[u][4 * j + y] += a[j][o] * b[y][o];
         }
       }
     }
-    __syncthreads();
+    __syncthreads();  // this buffer is restaged two chunks later
   }
 #pragma unroll
-  for (int u = 0; u < MAXT; ++u) {
-    const int tile = tid + u * 256;
-    if (tile < ntile) {
-      const int r0 = (tile / ct) * 2, c0 = (tile % ct) * 4;
+  for (int u = 0; u < DL_MAXT; ++u) {
+    const int t = tid + u * 256;
+    if (t < ntile) {
+      const int r0 = t / TC, k0 = t - r0 * TC;
 #pragma unroll
-      for (int x = 0; x < 2; ++x)
+      for (int j = 0; j < 4; ++j)
 #pragma unroll
-        for (int y = 0; y < 4; ++y)
-          if (r0 + x < R && c0 + y < cnt) Bm[(r0 + x) * (DL_CMAX + 1) + c0 + y] = acc[u][4 * x + y];
+        for (int y = 0; y < 4; ++y) {
+          const int r = r0 + TR * j, k = k0 + TC * y;
+          if (r < R && k < cnt) Bm[r * (DL_CMAX + 1) + k] = acc[u][4 * j + y];
+        }
     }
   }
   __syncthreads();
@@ -473,7 +524,7 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
   // tr(lap A A^-1) row m: sum_o lapA[m][o] Ainv[o][m]
   double tr = 0.0;
   for (int o = tid; o < n; o += blockDim.x)
-    tr += (double)lapA[((size_t)w * n + m) * ldj + (long)d * n + o] * (double)Ai[(size_t)o * n + m];
+    tr += (double)lapA[((size_t)w * n + m) * ldj + (long)d * n + o] * (double)Ab[(size_t)m * nA + sh + o];
   double v = tr - tl;
   v = warp_sum(v);
   __shared__ double rs[8];

@@ -54,6 +54,16 @@ struct EnvTcP {
   long ldc;
   int n, ns, soff, N, Wc, d, nv, vec;
 };
+// k_detlap staging: up to DL_CMAX positions per dependency (3 J rows each), contraction chunks of DL_OC elements
+// in shared-memory rows of DL_LD (16-byte aligned, consecutive rows on distinct bank quads); + 4 rows because
+// a thread's strided tile rows may run past the last one.  DL_SMEM_ELEMS: two J and two inverse buffers.
+constexpr int DL_CMAX = 64, DL_OC = 32, DL_LD = DL_OC + 4;
+constexpr int DL_JROWS = 3 * DL_CMAX + 4, DL_AROWS = DL_CMAX + 4;
+constexpr int DL_SMEM_ELEMS = 2 * (DL_JROWS + DL_AROWS) * DL_LD;
+// Row length of the transposed orbital-matrix inverse handed from the elimination to the determinant
+// Laplacian: room in front for the determinant's alignment shift (d n) mod 4 within the orbital plane, rounded
+// to 4 elements (16-byte rows in FP32)
+__host__ __device__ inline int ainv_ld(int n) { return (n + 6) / 4 * 4; }
 // bytes of the pre-tiled split weights of a K x N matrix: 32 KB per 128-column x 64-deep tile
 inline size_t tc_tiles_bytes(size_t K, size_t N) { return ((N + 127) / 128) * ((K + 63) / 64) * 32768; }
 

@@ -38,7 +38,6 @@ constexpr int GJG_BW_DECL = 16, GJG_THREADS_DECL = 512;
 template <typename T>
 __global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* lapA, T* grad, double* lap,
                          int32_t* status);
-constexpr int DL_CMAX_DECL = 64, DL_RP_DECL = 197;
 
 // fire_jastrow.cu
 __global__ void k_nn_energy(const float* R, const float* Z, int N, double* out);
