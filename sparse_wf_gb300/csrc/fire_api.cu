@@ -876,14 +876,24 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   }
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {
-    const size_t es = sizeof(T);
-    const size_t smem = es * DL_SMEM_ELEMS;
-    cudaFuncSetAttribute(k_detlap<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // FP32: dependencies with at most DL_CSPLIT positions in 128-thread CTAs (4 per SM), the rest in 256-thread
+    // CTAs; each launch leaves the other's dependencies alone.  FP64: one 256-thread launch.
     Prof pr("detlap", c.s);
-    g_nlaunch++;
-    k_detlap<T><<<dim3(c.p->n_el, NDET, c.Wc), 256, smem, c.s>>>(
-        c.nb, c.L, c.template buf<T>(c.P.Jorb), c.template buf<T>(c.P.Ainv), c.template buf<T>(c.P.lapA),
-        c.template buf<T>(c.P.dgrad), c.template buf<double>(c.P.dlap), c.status);
+    const dim3 grid(c.p->n_el, NDET, c.Wc);
+    auto go = [&](auto kern, int threads, int chi) {
+      const size_t smem = sizeof(T) * (size_t)dl_smem_elems(chi);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      g_nlaunch++;
+      kern<<<grid, threads, smem, c.s>>>(c.nb, c.L, c.template buf<T>(c.P.Jorb), c.template buf<T>(c.P.Ainv),
+                                         c.template buf<T>(c.P.lapA), c.template buf<T>(c.P.dgrad),
+                                         c.template buf<double>(c.P.dlap), c.status);
+    };
+    if constexpr (sizeof(T) == 4) {
+      go(k_detlap<T, 128, 0, DL_CSPLIT>, 128, DL_CSPLIT);
+      go(k_detlap<T, 256, DL_CSPLIT, DL_CMAX>, 256, DL_CMAX);
+    } else {
+      go(k_detlap<T, 256, 0, DL_CMAX>, 256, DL_CMAX);
+    }
   }
   stage_jastrow<T, 3>(c);
   AssembleOut o;

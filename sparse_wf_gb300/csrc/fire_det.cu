@@ -377,12 +377,12 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
 // (J rows and rows of the transposed inverse), in 16-byte quads of x = o + sh where sh = (d n) mod 4 makes the
 // J rows of determinant d 16-byte aligned; the inverse rows carry the same shift and zeros outside o in [0, n),
 // which cancel the neighbouring columns the J quads pick up.  Chunks of DL_OC x are copied asynchronously
-// (cp.async) into double-buffered shared memory, rows of DL_LD elements; each thread accumulates 4 x 4 tiles
+// (cp.async) into a ring of DL_STAGES shared-memory buffers, rows of DL_LD elements; each thread accumulates 4 x 4 tiles
 // whose rows (r, r + TR, r + 2 TR, r + 3 TR) and columns (k, k + TC, ...) are strided, so that a warp's 16-byte
 // loads hit consecutive rows: 8 shared loads per 64 FMAs, no bank conflicts.  The result tile reuses the
 // staging memory.
-static_assert(3 * DL_CMAX * (DL_CMAX + 1) <= 2 * DL_JROWS * DL_LD, "result tile inside the staging buffers");
-constexpr int DL_MAXT = (3 * DL_CMAX / 4) * (DL_CMAX / 4) / 256;  // 4 x 4 tiles per thread (3)
+static_assert(3 * DL_CMAX * (DL_CMAX + 1) <= dl_smem_elems(DL_CMAX), "result tile inside the staging buffers");
+static_assert(3 * DL_CSPLIT * (DL_CSPLIT + 1) <= dl_smem_elems(DL_CSPLIT), "result tile inside the staging buffers");
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, bool ok) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32_det(dst)), "l"(src), "r"(ok ? 16 : 0)
                : "memory");
@@ -401,25 +401,30 @@ __device__ __forceinline__ void ld_quad(const double* p, double (&v)[4]) {
   const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
-template <typename T>
-__global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __restrict__ Jp,
-                                                const T* __restrict__ AinvT, const T* __restrict__ lapA,
-                                                T* __restrict__ grad, double* __restrict__ lap, int32_t* status) {
+// NT threads; jobs with CLO < cnt <= CHI (the others are left to the other instance; cnt > DL_CMAX reports a
+// pair overflow)
+template <typename T, int NT, int CLO, int CHI>
+__global__ void __launch_bounds__(NT) k_detlap(Nbr nb, Layout L, const T* __restrict__ Jp,
+                                               const T* __restrict__ AinvT, const T* __restrict__ lapA,
+                                               T* __restrict__ grad, double* __restrict__ lap, int32_t* status) {
+  constexpr int JROWS = dl_jrows(CHI), STAGE = dl_stage_elems(CHI), BLD = CHI + 1;
+  constexpr int MAXT = ((3 * CHI + 3) / 4 * ((CHI + 3) / 4) + NT - 1) / NT;  // 4 x 4 tiles per thread
+  constexpr int RPT = (4 * CHI + NT - 1) / NT;                              // staged rows per thread
   extern __shared__ __align__(16) unsigned char dl_smem[];
   const int n = nb.n, nA = ainv_ld(n);
   const int m = blockIdx.x, d = blockIdx.y, w = blockIdx.z;
   const int* rp = nb.rowptr + (size_t)w * (n + 1);
   if (rp[n] > nb.cap_p) return;
   const int cnt = rp[m + 1] - rp[m] + 1;
-  if (cnt > DL_CMAX) {
-    if (threadIdx.x == 0) set_flag(status, FIRE_FLAG_PAIR_OVERFLOW);
+  if (cnt <= CLO) return;
+  if (cnt > CHI) {
+    if (CHI == DL_CMAX && threadIdx.x == 0) set_flag(status, FIRE_FLAG_PAIR_OVERFLOW);
     return;
   }
-  T* Js = reinterpret_cast<T*>(dl_smem);  // [2][DL_JROWS][DL_LD] J rows, x chunk
-  T* As = Js + 2 * DL_JROWS * DL_LD;      // [2][DL_AROWS][DL_LD] inverse rows is[k], x chunk
-  T* Bm = reinterpret_cast<T*>(dl_smem);  // [3 * DL_CMAX][DL_CMAX + 1] after the main loop
-  __shared__ long qrow[3 * DL_CMAX];      // element index of x = 0 of J row rr
-  __shared__ int is[DL_CMAX];
+  T* stg = reinterpret_cast<T*>(dl_smem);  // [DL_STAGES][J rows JROWS, inverse rows CHI + 4][DL_LD]
+  T* Bm = reinterpret_cast<T*>(dl_smem);   // [3 * CHI][BLD] after the main loop
+  __shared__ long qrow[3 * CHI];           // element index of x = 0 of J row rr
+  __shared__ int is[CHI];
   const int tid = threadIdx.x;
   const int off = L.pos_off[w];
   const int s0 = off + rp[m] + m;
@@ -435,49 +440,65 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
   const T* Ab = AinvT + ((size_t)w * NDET + d) * n * nA;
   constexpr int QPR = DL_OC / 4;           // quads per row and chunk
   constexpr int CPQ = 4 * sizeof(T) / 16;  // 16-byte copies per quad
-  const int nq = (R + cnt) * QPR;
-  auto stage = [&](int buf, int x0) {
-    for (int e = tid; e < nq; e += blockDim.x) {
-      const int row = e / QPR, qx = e - row * QPR;
-      const int x = x0 + 4 * qx;
-      T* dst;
-      const T* src;
-      if (row < R) {
-        dst = Js + ((size_t)buf * DL_JROWS + row) * DL_LD + 4 * qx;
-        src = Jp + qrow[row] + x;
-      } else {
-        const int k = row - R;
-        dst = As + ((size_t)buf * DL_AROWS + k) * DL_LD + 4 * qx;
-        src = Ab + (size_t)is[k] * nA + x;
-      }
-      const bool ok = x < XN;
+  constexpr int EPC = 16 / sizeof(T);      // elements per copy
+  // staging: thread tid owns rows tid, tid + NT, ... of the R J rows followed by the cnt inverse rows is[k],
+  // for the whole job
+  const T* srow[RPT];
+  int drow[RPT];
 #pragma unroll
-      for (int h = 0; h < CPQ; ++h) cp_async16(dst + h * (16 / sizeof(T)), ok ? src + h * (16 / sizeof(T)) : Ab, ok);
+  for (int q = 0; q < RPT; ++q) {
+    const int row = tid + q * NT;
+    srow[q] = Ab;
+    drow[q] = -1;
+    if (row < R) {
+      srow[q] = Jp + qrow[row];
+      drow[q] = row * DL_LD;
+    } else if (row < R + cnt) {
+      srow[q] = Ab + (size_t)is[row - R] * nA;
+      drow[q] = (JROWS + row - R) * DL_LD;
+    }
+  }
+  auto stage = [&](int buf, int x0) {
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      if (drow[q] < 0) continue;
+      T* dst = stg + (size_t)buf * STAGE + drow[q];
+#pragma unroll
+      for (int qx = 0; qx < QPR; ++qx) {
+        const int x = x0 + 4 * qx;
+        const bool ok = x < XN;
+#pragma unroll
+        for (int h = 0; h < CPQ; ++h) cp_async16(dst + 4 * qx + h * EPC, ok ? srow[q] + x + h * EPC : Ab, ok);
+      }
     }
   };
   const int TR = (R + 3) / 4, TC = (cnt + 3) / 4, ntile = TR * TC;
-  T acc[DL_MAXT][16];
+  T acc[MAXT][16];
 #pragma unroll
-  for (int u = 0; u < DL_MAXT; ++u)
+  for (int u = 0; u < MAXT; ++u)
 #pragma unroll
     for (int e = 0; e < 16; ++e) acc[u][e] = T(0);
+  // DL_STAGES - 1 chunks ahead; one commit group per chunk (empty past the end), one barrier per chunk: the
+  // buffer restaged after the barrier of chunk ch held chunk ch - 1, which every thread has finished
   const int nch = (XN + DL_OC - 1) / DL_OC;
-  stage(0, 0);
-  cp_async_commit();
-  for (int ch = 0; ch < nch; ++ch) {
-    if (ch + 1 < nch) {
-      stage((ch + 1) & 1, (ch + 1) * DL_OC);
-      cp_async_commit();
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
-    __syncthreads();
-    const T* Jb = Js + (size_t)(ch & 1) * DL_JROWS * DL_LD;
-    const T* Ac = As + (size_t)(ch & 1) * DL_AROWS * DL_LD;
 #pragma unroll
-    for (int u = 0; u < DL_MAXT; ++u) {
-      const int t = tid + u * 256;
+  for (int c = 0; c < DL_STAGES - 1; ++c) {
+    if (c < nch) stage(c, c * DL_OC);
+    cp_async_commit();
+  }
+  for (int ch = 0; ch < nch; ++ch) {
+    cp_async_wait<DL_STAGES - 2>();
+    __syncthreads();
+    {
+      const int nx = ch + DL_STAGES - 1;
+      if (nx < nch) stage(nx % DL_STAGES, nx * DL_OC);
+      cp_async_commit();
+    }
+    const T* Jb = stg + (size_t)(ch % DL_STAGES) * STAGE;
+    const T* Ac = Jb + JROWS * DL_LD;
+#pragma unroll
+    for (int u = 0; u < MAXT; ++u) {
+      const int t = tid + u * NT;
       if (t < ntile) {
         const int r0 = t / TC, k0 = t - r0 * TC;
 #pragma unroll 2
@@ -496,11 +517,12 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
         }
       }
     }
-    __syncthreads();  // this buffer is restaged two chunks later
   }
+  cp_async_wait<0>();
+  __syncthreads();  // every chunk consumed: the result tile overwrites the staging buffers
 #pragma unroll
-  for (int u = 0; u < DL_MAXT; ++u) {
-    const int t = tid + u * 256;
+  for (int u = 0; u < MAXT; ++u) {
+    const int t = tid + u * NT;
     if (t < ntile) {
       const int r0 = t / TC, k0 = t - r0 * TC;
 #pragma unroll
@@ -508,7 +530,7 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
 #pragma unroll
         for (int y = 0; y < 4; ++y) {
           const int r = r0 + TR * j, k = k0 + TC * y;
-          if (r < R && k < cnt) Bm[r * (DL_CMAX + 1) + k] = acc[u][4 * j + y];
+          if (r < R && k < cnt) Bm[r * BLD + k] = acc[u][4 * j + y];
         }
     }
   }
@@ -519,7 +541,7 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
   for (int e = tid; e < nel; e += blockDim.x) {
     const int rr = e / cnt, k2 = e - rr * cnt;
     const int k = rr / 3, t = rr - 3 * k;
-    tl += (double)Bm[rr * (DL_CMAX + 1) + k2] * (double)Bm[(3 * k2 + t) * (DL_CMAX + 1) + k];
+    tl += (double)Bm[rr * BLD + k2] * (double)Bm[(3 * k2 + t) * BLD + k];
   }
   // tr(lap A A^-1) row m: sum_o lapA[m][o] Ainv[o][m]
   double tr = 0.0;
@@ -527,17 +549,17 @@ __global__ void __launch_bounds__(256) k_detlap(Nbr nb, Layout L, const T* __res
     tr += (double)lapA[((size_t)w * n + m) * ldj + (long)d * n + o] * (double)Ab[(size_t)m * nA + sh + o];
   double v = tr - tl;
   v = warp_sum(v);
-  __shared__ double rs[8];
+  __shared__ double rs[NT / 32];
   if ((tid & 31) == 0) rs[tid >> 5] = v;
   __syncthreads();
   if (tid == 0) {
     double sum = 0.0;
-    for (int q = 0; q < 8; ++q) sum += rs[q];
+    for (int q = 0; q < NT / 32; ++q) sum += rs[q];
     atomicAdd(&lap[w * NDET + d], sum);
   }
   if (tid < 3) {
     T gsum = T(0);
-    for (int k = 0; k < cnt; ++k) gsum += Bm[(3 * k + tid) * (DL_CMAX + 1) + k];
+    for (int k = 0; k < cnt; ++k) gsum += Bm[(3 * k + tid) * BLD + k];
     grad[(((size_t)w * NDET + d) * n + m) * 3 + tid] = gsum;
   }
 }
@@ -558,9 +580,11 @@ template __global__ void k_gj_global<double, double, double, true>(const double*
                                                                     double*, int32_t*);
 template __global__ void k_gj_global<double, double, double, false>(const double*, int, double*, double*, double*,
                                                                      double*, int32_t*);
-template __global__ void k_detlap<float>(Nbr, Layout, const float*, const float*, const float*, float*, double*,
-                                         int32_t*);
-template __global__ void k_detlap<double>(Nbr, Layout, const double*, const double*, const double*, double*,
-                                          double*, int32_t*);
+template __global__ void k_detlap<float, 128, 0, DL_CSPLIT>(Nbr, Layout, const float*, const float*, const float*,
+                                                            float*, double*, int32_t*);
+template __global__ void k_detlap<float, 256, DL_CSPLIT, DL_CMAX>(Nbr, Layout, const float*, const float*,
+                                                                  const float*, float*, double*, int32_t*);
+template __global__ void k_detlap<double, 256, 0, DL_CMAX>(Nbr, Layout, const double*, const double*,
+                                                            const double*, double*, double*, int32_t*);
 
 }  // namespace fire

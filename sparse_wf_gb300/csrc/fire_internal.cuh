@@ -54,12 +54,14 @@ struct EnvTcP {
   long ldc;
   int n, ns, soff, N, Wc, d, nv, vec;
 };
-// k_detlap staging: up to DL_CMAX positions per dependency (3 J rows each), contraction chunks of DL_OC elements
-// in shared-memory rows of DL_LD (16-byte aligned, consecutive rows on distinct bank quads); + 4 rows because
-// a thread's strided tile rows may run past the last one.  DL_SMEM_ELEMS: two J and two inverse buffers.
-constexpr int DL_CMAX = 64, DL_OC = 32, DL_LD = DL_OC + 4;
-constexpr int DL_JROWS = 3 * DL_CMAX + 4, DL_AROWS = DL_CMAX + 4;
-constexpr int DL_SMEM_ELEMS = 2 * (DL_JROWS + DL_AROWS) * DL_LD;
+// k_detlap staging: up to chi positions per dependency (3 J rows each, DL_CMAX at most), contraction chunks of
+// DL_OC elements in shared-memory rows of DL_LD (16-byte aligned; consecutive rows on distinct bank quads); + 4
+// rows because a thread's strided tile rows may run past the last one; DL_STAGES chunks in flight.  Jobs with
+// at most DL_CSPLIT positions run in small CTAs (128 threads, 4 per SM), the rest in 256-thread CTAs.
+constexpr int DL_CMAX = 64, DL_CSPLIT = 44, DL_OC = 32, DL_LD = DL_OC + 4, DL_STAGES = 2;
+__host__ __device__ constexpr int dl_jrows(int chi) { return 3 * chi + 4; }
+__host__ __device__ constexpr int dl_stage_elems(int chi) { return (dl_jrows(chi) + chi + 4) * DL_LD; }
+__host__ __device__ constexpr int dl_smem_elems(int chi) { return DL_STAGES * dl_stage_elems(chi); }
 // Row length of the transposed orbital-matrix inverse handed from the elimination to the determinant
 // Laplacian: room in front for the determinant's alignment shift (d n) mod 4 within the orbital plane, rounded
 // to 4 elements (16-byte rows in FP32)

@@ -35,7 +35,7 @@ __global__ void k_env_coef(const T* r, const float* R, const T* sp, int n, int n
 template <typename S, typename TI, typename TO, bool INV>
 __global__ void k_gj_global(const TI* A, int n, S* work, double* logdet, double* sign, TO* Ainv, int32_t* status);
 constexpr int GJG_BW_DECL = 16, GJG_THREADS_DECL = 512;
-template <typename T>
+template <typename T, int NT, int CLO, int CHI>
 __global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* lapA, T* grad, double* lap,
                          int32_t* status);
 
