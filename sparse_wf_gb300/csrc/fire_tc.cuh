@@ -119,6 +119,28 @@ __device__ __forceinline__ uint32_t tc_off(int row, int k) {
   return (uint32_t)((row & 7) * 16 + (row >> 3) * TC_SBO + (k & 7) * 2 + (k >> 3) * TC_LBO);
 }
 
+// 16-byte global -> shared asynchronous copy (zero fill when !ok), commit and wait (n copies groups may stay
+// in flight, n <= 3)
+__device__ __forceinline__ void cp_async16_tc(void* dst, const void* src, bool ok) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(ok ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_tc() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_tc(int n) {
+  if (n <= 0) asm volatile("cp.async.wait_group 0;" ::: "memory");
+  else if (n == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
+  else if (n == 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
+  else asm volatile("cp.async.wait_group 3;" ::: "memory");
+}
+// a = hi + lo for two values: BF16 pairs (first value in the low half)
+__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
 // ----------------------------------------------------------------------------- vectorised epilogues
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
@@ -643,47 +665,63 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
 
   if (warp >= 8 && warp < 12) {
     // ------------------------------------------------------------------ A converters (128 threads)
-    const int lt = tid - 256, lw = lt >> 5, r8 = lane & 7, kq = lane >> 3;
+    // Each thread owns 8 (row, 8-deep k-group) items of every 64-deep block: one 16-byte core-matrix row in the hi
+    // plane and the same row in the lo plane.  The FP32 values of an item (32 bytes) are copied asynchronously
+    // straight into those two rows (first 4 into the hi row, last 4 into the lo row) as soon as the block's slot
+    // is free, then split in place by the same thread: no other thread touches these bytes, so the thread's own
+    // cp.async wait is the only synchronisation.  A row tile's copies are all issued before its first block is
+    // split, so its HBM latency is paid about once per row tile, not once per block.
+    const int lt = tid - 256, lw = lt >> 5, r8 = lane & 7, kq8 = lane >> 3;
     long ua = 0;
     for (int m = blockIdx.x; m < mt && !*abort; m += gridDim.x) {
       if (skip(m)) continue;
       const int m0 = m * TC_BM;
+      int issued = 0;
       for (int kb = 0; kb < nk; ++kb) {
         if (ua > 0 && !tc_wait(&bars->aempty[kb], (uint32_t)((ua - 1) & 1), abort)) break;
         unsigned char* a_hi = ares + kb * TcaCfg::A_BLOCK;
         unsigned char* a_lo = a_hi + TcaCfg::A_BYTES;
         const int k0 = kb * TC_BK;
-        float4 v[16];
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int blk = lw + 4 * u;
-          const int r = (blk >> 2) * 8 + r8, kk = (blk & 3) * 16 + kq * 4;
+        for (int it = 0; it < 8; ++it) {
+          const int blk = lw + 4 * it;  // (8-row group, k half)
+          const int r = (blk >> 1) * 8 + r8, kk = (blk & 1) * 32 + kq8 * 8;
           const int gr = m0 + r, gk = k0 + kk;
-          v[u] = (gr < rows && gk < p.K) ? ld4(p.A + (long)gr * p.lda + gk) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int blk = lw + 4 * u;
-          const int r = (blk >> 2) * 8 + r8, kk = (blk & 3) * 16 + kq * 4;
-          const float f[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-          uint32_t hw[2], lw2[2];
-#pragma unroll
-          for (int e = 0; e < 2; ++e) {
-            const __nv_bfloat16 h0 = __float2bfloat16_rn(f[2 * e]), h1 = __float2bfloat16_rn(f[2 * e + 1]);
-            const __nv_bfloat16 l0 = __float2bfloat16_rn(f[2 * e] - __bfloat162float(h0));
-            const __nv_bfloat16 l1 = __float2bfloat16_rn(f[2 * e + 1] - __bfloat162float(h1));
-            hw[e] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-            lw2[e] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-          }
+          const bool ok = gr < rows && gk < p.K;  // K % 8 == 0: the whole k-group is inside
+          const float* src = ok ? p.A + (long)gr * p.lda + gk : p.A;
           const uint32_t off = tc_off(r, kk);
-          *reinterpret_cast<uint2*>(a_hi + off) = make_uint2(hw[0], hw[1]);
-          *reinterpret_cast<uint2*>(a_lo + off) = make_uint2(lw2[0], lw2[1]);
+          cp_async16_tc(a_hi + off, src, ok);
+          cp_async16_tc(a_lo + off, src + 4, ok);
+        }
+        cp_async_commit_tc();
+        ++issued;
+      }
+      for (int kb = 0; kb < issued; ++kb) {
+        cp_async_wait_tc(issued - 1 - kb);
+        unsigned char* a_hi = ares + kb * TcaCfg::A_BLOCK;
+        unsigned char* a_lo = a_hi + TcaCfg::A_BYTES;
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+          const int blk = lw + 4 * it;
+          const int r = (blk >> 1) * 8 + r8, kk = (blk & 1) * 32 + kq8 * 8;
+          const uint32_t off = tc_off(r, kk);
+          const float4 x = *reinterpret_cast<const float4*>(a_hi + off);
+          const float4 y = *reinterpret_cast<const float4*>(a_lo + off);
+          uint4 hi, lo;
+          split_bf16x2(x.x, x.y, hi.x, lo.x);
+          split_bf16x2(x.z, x.w, hi.y, lo.y);
+          split_bf16x2(y.x, y.y, hi.z, lo.z);
+          split_bf16x2(y.z, y.w, hi.w, lo.w);
+          *reinterpret_cast<uint4*>(a_hi + off) = hi;
+          *reinterpret_cast<uint4*>(a_lo + off) = lo;
         }
         proxy_fence();
         tc_arrive(&bars->afull[kb]);
       }
+      if (issued < nk) break;  // aborted
       ++ua;
     }
+    cp_async_wait_tc(0);
   } else if (warp == 13) {
     // ------------------------------------------------------------------ weight loader
     if (lane == 0) {
