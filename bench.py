@@ -332,7 +332,7 @@ def main():
     achieved = flops / (g_ms / 1e3) / 1e12
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / peaks["bf16_tflops"], "traffic": None,
-                "kernel": "all dense contractions of one step (k_gemm_tcp + k_gemm)", "launches": g_launches,
+                "kernel": "all dense contractions of one step (k_gemm_tca + k_env_tc + k_gemm)", "launches": g_launches,
                 "avg_launch_ms": g_ms / max(g_launches, 1), "peak_source": f"bf16 dense burst, {peak_kind}",
                 "flops_per_step": flops}
     stages = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items() if k != "kernels_launched"}
