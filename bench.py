@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--ws-gb", type=float, default=48.0, help="workspace budget in GB")
     ap.add_argument("--mcmc-steps", type=int, default=20, help="Metropolis steps before the E_loc evaluation")
     ap.add_argument("--mcmc-width", type=float, default=0.1)
+    ap.add_argument("--mcmc-single-steps", type=int, default=32,
+                    help="single-electron Metropolis steps timed on a copy of the walkers (0: skip)")
+    ap.add_argument("--mcmc-single-width", type=float, default=0.5)
     ap.add_argument("--acc-walkers", type=int, default=256, help="walkers checked against the FP64 build")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
     ap.add_argument("--serving-requests", type=int, default=40, help="requests of the serving segment (0: skip)")
@@ -304,6 +307,23 @@ def main():
         mcmc = {"steps": args.mcmc_steps, "width_bohr": args.mcmc_width, "ms_per_block": ms_block,
                 "walker_steps_per_s": B * world * args.mcmc_steps / (ms_block / 1e3), "acceptance": acc,
                 "precision": args.precision}
+        if args.mcmc_single_steps > 0:
+            # single-electron proposals (the reference's default, sequential sweep) on a copy of the walkers, so
+            # the E_loc workload below is unchanged
+            r1, lp1 = r_dev.clone(), logpsi.clone()
+            blk1 = {}
+
+            def block1():
+                blk1["acc"], _ = wf.mcmc_single_block(dp, r1, lp1, static, args.mcmc_single_steps,
+                                                      args.mcmc_single_width, seed=2000 + rank, counter=0)
+
+            ms1, _ = time_steps(block1, 1, stream, dist, world)
+            mcmc["single_electron"] = {
+                "steps": args.mcmc_single_steps, "width_bohr": args.mcmc_single_width, "ms_per_block": ms1,
+                "walker_steps_per_s": B * world * args.mcmc_single_steps / (ms1 / 1e3),
+                "acceptance": float(blk1["acc"].float().mean().item()) / args.mcmc_single_steps,
+                "evaluation": "every proposal by the full value path (no low-rank update)"}
+            del r1, lp1
         static = wf.get_static_input(r_dev).round_with_padding(1.1, mol.n_el, n_up, mol.n_nuc)
     r_np = r_dev.cpu().numpy()
 

@@ -19,6 +19,8 @@
  *                       wave_function.py:215-221, potential via hamiltonian.py:15-26),
  *                       batched like update.py:95-100 and reduced like update.py:130-134
  *   fire_mcmc_block     mcmc.py:38-97 mcmc_steps_all_electron
+ *   fire_mcmc_single_block  mcmc.py:100-111, 196-275 proposal_single_electron + mcmc_steps_low_rank
+ *                       (each proposal evaluated in full, no low-rank state)
  *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
  *                       (used by the initialiser, new_sparse_model.py:378-379)
  */
@@ -197,6 +199,20 @@ fire_status fire_mcmc_block(void* stream, const fire_problem* prob, const float*
                             uint64_t seed, uint64_t counter, const void* replay_noise,
                             const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
                             void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Metropolis block of single-electron Gaussian moves: proposal_single_electron (mcmc.py:100-111) as run by
+ * mcmc_steps_low_rank (mcmc.py:196-275).  Step s (0 <= s < steps) moves electron (step_offset + s) mod n of
+ * every walker by width * eps, eps [3] ~ N(0, 1), and accepts if 2 (log|psi'| - log|psi|) > log u.
+ * log|psi'| is a full value-path evaluation of the proposed configuration (the reference reaches the same
+ * value by a low-rank update of a cached state, checked against the full evaluation in its
+ * tests/test_low_rank.py:29-61; that update is not built here, so one step costs one full evaluation).
+ * Draws from Philox4x32-10 keyed by (seed, counter, step, walker) unless replay_noise [steps, B, 3] and
+ * replay_log_u [steps, B] are given.  Other arguments and outputs as fire_mcmc_block. */
+fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                   const void* prepared, void* r, void* logpsi, int32_t steps, int32_t step_offset,
+                                   float width, uint64_t seed, uint64_t counter, const void* replay_noise,
+                                   const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
+                                   void* workspace, size_t workspace_bytes, int32_t* status);
 
 /* Coulomb potential of every walker (hamiltonian.py:15-26): out [B] in the walkers' dtype. */
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r,

@@ -26,7 +26,8 @@ What is restated (file:line in the reference project):
   (``orbitals.py:148-174``), ``sparse_slogdet_with_fwd_lap`` (``sparse_fwd_lap.py:294-319``),
   ``Jastrow.apply_with_fwd_lap`` (``jastrow.py:387-459``);
 * ``kinetic_energy`` (``wave_function.py:215-221``), ``potential_energy``
-  (``hamiltonian.py:15-26``), the all-electron Metropolis step (``mcmc.py:38-97``) with
+  (``hamiltonian.py:15-26``), the all-electron Metropolis step (``mcmc.py:38-97``), the single-electron step
+  (``mcmc.py:100-111, 196-275``) with
   externally supplied noise.
 
 folx (0.2.15, a dependency absent here) is replaced by ``FL``: a dense forward-mode
@@ -860,6 +861,29 @@ def mcmc_block(prob, p, r, noise, log_u, width):
     margins = []
     for s in range(noise.shape[0]):
         rn = r + noise[s] * width
+        lpn = 2.0 * logpsi(prob, p, rn)[1]
+        m = (lpn - lp) - log_u[s]
+        margins.append(m)
+        if m > 0:
+            r, lp = rn, lpn
+            n_acc += 1
+    return r, lp, n_acc, np.array(margins)
+
+
+def mcmc_single_block(prob, p, r, noise, log_u, width, offset=0):
+    """Single-electron Metropolis block: ``proposal_single_electron`` (``mcmc.py:100-111``) driven by
+    ``mcmc_steps_low_rank`` (``mcmc.py:196-275``) with externally supplied draws.  Step s moves electron
+    (offset + s) mod n by width * noise[s] ([steps, 3]); accept iff 2 (log|psi'| - log|psi|) > log_u[s].  log|psi'|
+    is evaluated in full (the reference's low-rank update reaches the same value, ``tests/test_low_rank.py``).
+    Returns (r, log_prob, n_accept, margins)."""
+    n = r.shape[0]
+    lp = 2.0 * logpsi(prob, p, r)[1]
+    n_acc = 0
+    margins = []
+    for s in range(noise.shape[0]):
+        e = (offset + s) % n
+        rn = r.copy()
+        rn[e] = r[e] + noise[s] * width
         lpn = 2.0 * logpsi(prob, p, rn)[1]
         m = (lpn - lp) - log_u[s]
         margins.append(m)

@@ -1011,11 +1011,13 @@ fire_status run_embedding(const fire_problem* p, cudaStream_t s, const float* R,
   return FIRE_OK;
 }
 
+// Metropolis block; single: one electron per step ((offset + step) mod n) instead of all of them.  Every
+// proposal is evaluated by the full value path.
 template <typename T>
 fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
                      void* r, void* logpsi, int steps, float width, uint64_t seed, uint64_t counter,
                      const void* noise, const void* logu, int32_t* n_accept, int32_t* static_max, void* ws,
-                     size_t wsb, int32_t* status) {
+                     size_t wsb, int32_t* status, bool single = false, int offset = 0) {
   const int Wc = choose_chunk(p, wsb, false);
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
@@ -1028,9 +1030,13 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
     T* lpn = c.template buf<T>(c.P.lpn);
     for (int st = 0; st < steps; ++st) {
       g_nlaunch++;
-      k_propose<T><<<nblk((long)c.Wc * n), 256, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, c.Wc, w0, p->n_walkers, st,
-                                                        (T)width, seed, counter,
-                                                        reinterpret_cast<const T*>(noise));
+      if (single)
+        k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, w0, p->n_walkers, st, offset,
+                                                 (T)width, seed, counter, reinterpret_cast<const T*>(noise));
+      else
+        k_propose<T><<<nblk((long)c.Wc * n), 256, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, c.Wc, w0, p->n_walkers,
+                                                          st, (T)width, seed, counter,
+                                                          reinterpret_cast<const T*>(noise));
       c.r = rn;
       if (chunk_logpsi<T>(c, lpn, nullptr, 0) != cudaSuccess) return launch_status("mcmc chunk");
       g_nlaunch++;
@@ -1227,6 +1233,22 @@ fire_status fire_mcmc_block(void* stream, const fire_problem* prob, const float*
                             replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
   return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise, replay_log_u,
                          n_accept, static_max, workspace, workspace_bytes, status);
+}
+
+fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                   const void* prepared, void* r, void* logpsi, int32_t steps, int32_t step_offset,
+                                   float width, uint64_t seed, uint64_t counter, const void* replay_noise,
+                                   const void* replay_log_u, int32_t* n_accept, int32_t* static_max, void* workspace,
+                                   size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || step_offset < 0)
+    return FIRE_ERR_INVALID;
+  if ((replay_noise == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise,
+                            replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, true, step_offset);
+  return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise, replay_log_u,
+                         n_accept, static_max, workspace, workspace_bytes, status, true, step_offset);
 }
 
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r, const float* R,

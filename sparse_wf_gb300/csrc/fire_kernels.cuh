@@ -67,6 +67,10 @@ template <typename T>
 __global__ void k_propose(const T* r, T* rn, int n, int Wc, int w0, int B, int step, T width, uint64_t seed,
                           uint64_t counter, const T* replay);
 template <typename T>
+__global__ void k_propose_single(const T* r, T* rn, int n, int w0, int B, int step, int offset, T width,
+                                 uint64_t seed, uint64_t counter, const T* replay);
+
+template <typename T>
 __global__ void k_accept(T* r, const T* rn, T* logpsi, const T* logpsi_new, int n, int w0, int B, int step,
                          uint64_t seed, uint64_t counter, const T* replay_log_u, int32_t* n_accept, const int* counts,
                          int32_t* static_max);

@@ -1,4 +1,5 @@
-// fire_mcmc.cu -- all-electron Metropolis proposal and accept/reject (mcmc.py:38-97).
+// fire_mcmc.cu -- Metropolis proposals (all-electron, mcmc.py:38-97; single-electron, mcmc.py:100-111) and
+// accept/reject.
 //
 // Random numbers: Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3",
 // SC'11), counter = (step, walker, electron, stream counter), key = seed; normals by Box-Muller.
@@ -58,6 +59,38 @@ __global__ void k_propose(const T* __restrict__ r, T* __restrict__ rn, int n, in
   for (int c = 0; c < 3; ++c) rn[base + c] = r[base + c] + width * eps[c];
 }
 
+// Single-electron proposal (proposal_single_electron, mcmc.py:100-111): r_new = r with electron
+// (offset + step) mod n moved by width * eps, eps [3] per walker and step; one CTA per walker of the chunk.
+// replay [steps, B, 3].
+template <typename T>
+__global__ void k_propose_single(const T* __restrict__ r, T* __restrict__ rn, int n, int w0, int B, int step,
+                                 int offset, T width, uint64_t seed, uint64_t counter, const T* __restrict__ replay) {
+  const int w = blockIdx.x;
+  const long gw = w0 + w;
+  const T* src = r + (long)w * 3 * n;
+  T* dst = rn + (long)w * 3 * n;
+  for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int e = (int)(((long)offset + step) % n);
+    T eps[3];
+    if (replay) {
+      const T* q = replay + ((long)step * B + gw) * 3;
+      eps[0] = q[0]; eps[1] = q[1]; eps[2] = q[2];
+    } else {
+      uint32_t ctr[4] = {(uint32_t)step, (uint32_t)gw, 0xFFFFFFFEu, (uint32_t)counter};
+      philox10(ctr, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
+      const double r1 = sqrt(-2.0 * log(u01(ctr[0]))), t1 = 6.283185307179586 * u01(ctr[1]);
+      const double r2 = sqrt(-2.0 * log(u01(ctr[2]))), t2 = 6.283185307179586 * u01(ctr[3]);
+      eps[0] = (T)(r1 * cos(t1));
+      eps[1] = (T)(r1 * sin(t1));
+      eps[2] = (T)(r2 * cos(t2));
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dst[3 * e + c] = src[3 * e + c] + width * eps[c];
+  }
+}
+
 // Accept if 2 (logpsi_new - logpsi_old) > log u (mcmc.py:68-73); one CTA per walker.
 // r, logpsi: whole batch (global walker index); rn, logpsi_new, counts: this chunk (local index).
 template <typename T>
@@ -98,6 +131,10 @@ template __global__ void k_propose<float>(const float*, float*, int, int, int, i
                                           const float*);
 template __global__ void k_propose<double>(const double*, double*, int, int, int, int, int, double, uint64_t,
                                            uint64_t, const double*);
+template __global__ void k_propose_single<float>(const float*, float*, int, int, int, int, int, float, uint64_t,
+                                                 uint64_t, const float*);
+template __global__ void k_propose_single<double>(const double*, double*, int, int, int, int, int, double,
+                                                  uint64_t, uint64_t, const double*);
 template __global__ void k_accept<float>(float*, const float*, float*, const float*, int, int, int, int, uint64_t,
                                          uint64_t, const float*, int32_t*, const int*, int32_t*);
 template __global__ void k_accept<double>(double*, const double*, double*, const double*, int, int, int, int,

@@ -336,6 +336,44 @@ class FireWaveFunction:
         return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
 
 
+    def mcmc_single_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
+                          steps: int, width: float, step_offset: int = 0, seed: int = 0, counter: int = 0,
+                          replay_noise=None, replay_log_u=None):
+        """In-place single-electron Metropolis block (``mcmc_steps_low_rank`` with ``proposal_single_electron``,
+        ``mcmc.py:100-111, 196-275``): step s moves electron (step_offset + s) mod n.  Every proposal is evaluated in
+        full (no low-rank state).  replay_noise [steps, B, 3], replay_log_u [steps, B].  Returns (n_accept per walker,
+        static_max)."""
+        p = self._params(params)
+        r = electrons
+        assert r.is_contiguous() and r.dtype == self.dtype
+        B = r.shape[0]
+        n_acc = torch.zeros(B, dtype=torch.int32, device=self.device)
+        smax = torch.zeros(4, dtype=torch.int32, device=self.device)
+        noise = None
+        if replay_noise is not None:
+            noise = torch.as_tensor(np.asarray(replay_noise)).to(self.device, self.dtype).reshape(steps, B, 3).contiguous()
+        logu = None if replay_log_u is None else torch.as_tensor(replay_log_u).to(self.device, self.dtype).contiguous()
+        r0 = r.clone()
+        lp0 = logpsi.clone()
+
+        def fn(prob, ws):
+            r.copy_(r0)
+            logpsi.copy_(lp0)
+            n_acc.zero_()
+            smax.zero_()
+            _lib.check(_lib.load().fire_mcmc_single_block(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(logpsi.data_ptr()),
+                int(steps), int(step_offset), float(width), C.c_uint64(seed), C.c_uint64(counter),
+                C.c_void_p(noise.data_ptr()) if noise is not None else None,
+                C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_mcmc_single_block")
+
+        self._run(fn, static, B)
+        sm = smax.cpu().numpy()
+        return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
+
 def make_local_energy(wf: FireWaveFunction):
     """``make_local_energy`` (``hamiltonian.py:49-83``) for all-electron systems:
     ``local_energy(key, params, electrons, static) -> (E_loc, new_static)``."""
@@ -347,16 +385,26 @@ def make_local_energy(wf: FireWaveFunction):
     return local_energy
 
 
-def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1):
-    """All-electron branch of ``make_mcmc`` (``mcmc.py:278-346``):
+def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, proposal: str = "all-electron",
+              sweeps: float = 2.0):
+    """``make_mcmc`` (``mcmc.py:278-346``) for the "all-electron" proposal (``steps`` moves of every electron) and
+    the "single-electron" proposal (``int(sweeps * n_el)`` one-electron moves in sequential order, the reference's
+    default; ``init_width`` 0.5 there, ``config/default.yaml``):
     ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed."""
+    proposal = proposal.lower()
+    if proposal not in ("all-electron", "single-electron"):
+        raise ValueError(f"Invalid proposal: {proposal}")
+    n_steps = steps if proposal == "all-electron" else int(sweeps * wf.mol.n_el)
 
     def mcmc_step(key, params, electrons, static: StaticArgs, width):
         p = wf._params(params)
         r = wf._electrons(electrons).clone()
         _, logpsi = wf.signed(p, r, static)
-        n_acc, smax = wf.mcmc_block(p, r, logpsi, static, steps, float(width), seed=int(key))
-        stats = dict(pmove=float(n_acc.float().mean().item()) / max(steps, 1), static_max=smax, stepsize=width)
+        if proposal == "all-electron":
+            n_acc, smax = wf.mcmc_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
+        else:
+            n_acc, smax = wf.mcmc_single_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
+        stats = dict(pmove=float(n_acc.float().mean().item()) / max(n_steps, 1), static_max=smax, stepsize=width)
         return r, stats
 
     return mcmc_step, init_width

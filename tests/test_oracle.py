@@ -121,3 +121,23 @@ def test_mcmc_block_replay_golden():
                                  g["mcmc_logu"][:, k].astype(np.float64), np.float32(0.1))
     np.testing.assert_allclose(rr, g["mcmc_r"][k], atol=1e-12)
     assert na == g["mcmc_nacc"][k]
+
+
+def test_single_electron_block_is_the_all_electron_block_with_one_electron_moved():
+    """mcmc_single_block (proposal_single_electron, mcmc.py:100-111) equals mcmc_block fed noise that is zero on every
+    electron but (offset + s) mod n at step s, decisions and positions included."""
+    mol, nu, r, p, *_ = case("h10")
+    prob = O.Problem(mol.R, mol.Z, nu)
+    rng = np.random.default_rng(5)
+    steps, n, off = 7, mol.n_el, 6
+    eps = rng.standard_normal((steps, 3))
+    logu = np.log(rng.uniform(size=steps))
+    full = np.zeros((steps, n, 3))
+    for s in range(steps):
+        full[s, (off + s) % n] = eps[s]
+    r0 = r[1].astype(np.float64)
+    a = O.mcmc_single_block(prob, p, r0, eps, logu, 0.3, offset=off)
+    b = O.mcmc_block(prob, p, r0, full, logu, 0.3)
+    np.testing.assert_array_equal(a[0], b[0])
+    assert a[2] == b[2] and 0 < a[2] < steps
+    np.testing.assert_allclose(a[3], b[3], rtol=0, atol=0)
