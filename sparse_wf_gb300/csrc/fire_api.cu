@@ -491,8 +491,8 @@ cudaError_t stage_neighbors(Ctx<T>& c, bool fl) {
   const size_t smem = 3 * n * sizeof(T) + (5 * n + 2) * sizeof(int);
   fire_neighbor_out ext;
   std::memset(&ext, 0, sizeof(ext));
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_neighbors<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // always opt in: the kernel's static shared memory adds to the dynamic size
+  cudaFuncSetAttribute(k_neighbors<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   g_nlaunch++;
   k_neighbors<T><<<c.Wc, 512, smem, c.s>>>(c.r, c.R, (T)c.p->cutoff, (T)c.p->cutoff_1el, c.nb, ext, c.status);
   if (fl) {
@@ -690,12 +690,11 @@ cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   const int n = c.p->n_el;
   constexpr int BW = GJG_BW_DECL;
   const size_t smem =
-      sizeof(S) * (2 * (size_t)n * (BW + 1) + BW * BW + n + 2 * BW) + sizeof(int) * (2 * (size_t)n + BW);
+      sizeof(S) * (2 * (size_t)n * (BW + 1) + BW * BW + n + 3 * BW) + sizeof(int) * (2 * (size_t)n + BW);
   auto kern = k_gj_global<S, TI, TO, INV>;
-  if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  // always opt in: the kernel's static shared memory adds to the dynamic size
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   g_nlaunch++;
   kern<<<c.Wc * NDET, GJG_THREADS_DECL, smem, c.s>>>(A, n, c.template buf<S>(c.P.gjw),
                                                       c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
@@ -1130,14 +1129,14 @@ fire_status fire_neighbors(void* stream, const fire_problem* prob, const void* r
   const int n = prob->n_el;
   if (prob->precision == FIRE_PREC_FP64) {
     const size_t smem = 3 * n * sizeof(double) + (5 * n + 2) * sizeof(int);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     g_nlaunch++;
     k_neighbors<double><<<prob->n_walkers, 512, smem, s>>>(reinterpret_cast<const double*>(r), R,
                                                           (double)prob->cutoff, (double)prob->cutoff_1el, nb, *out,
                                                           status);
   } else {
     const size_t smem = 3 * n * sizeof(float) + (5 * n + 2) * sizeof(int);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     g_nlaunch++;
     k_neighbors<float><<<prob->n_walkers, 512, smem, s>>>(reinterpret_cast<const float*>(r), R, prob->cutoff,
                                                          prob->cutoff_1el, nb, *out, status);
@@ -1172,13 +1171,13 @@ fire_status fire_triplets(void* stream, const fire_problem* prob, const void* r,
   nb2.N = 0;
   if (prob->precision == FIRE_PREC_FP64) {
     const size_t smem = 3 * n * sizeof(double) + (5 * n + 2) * sizeof(int);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     g_nlaunch++;
     k_neighbors<double><<<B, 512, smem, s>>>(reinterpret_cast<const double*>(r), nullptr, (double)prob->cutoff,
                                             (double)prob->cutoff_1el, nb2, ext, status);
   } else {
     const size_t smem = 3 * n * sizeof(float) + (5 * n + 2) * sizeof(int);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     g_nlaunch++;
     k_neighbors<float><<<B, 512, smem, s>>>(reinterpret_cast<const float*>(r), nullptr, prob->cutoff,
                                            prob->cutoff_1el, nb2, ext, status);

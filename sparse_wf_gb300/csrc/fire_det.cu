@@ -108,7 +108,8 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   S* colk = Li + BW * BW;                  // [n] pivot column before the step (interchanged order)
   S* rk = colk + n;                        // [BW] row k of the panel before the step
   S* rp = rk + BW;                         // [BW] row p
-  int* perm = reinterpret_cast<int*>(rp + BW);  // [n]
+  S* rj = rp + BW;                         // [BW] row p scaled by the inverse pivot
+  int* perm = reinterpret_cast<int*>(rj + BW);  // [n]
   int* piv = perm + n;                     // [BW]
   int* rowmap = piv + BW;                  // [n] source row of every row after the panel's interchanges
   __shared__ S redv[32];
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
       for (int j = tid; j < bw; j += blockDim.x) {
         rk[j] = pan[k * LD + j];
         rp[j] = pan[p * LD + j];
+        rj[j] = rp[j] * ipv;
       }
       if (p != k)  // earlier transforms follow the interchange
         for (int s2 = tid; s2 < t; s2 += blockDim.x) {
@@ -190,16 +192,19 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
           W[p * LD + s2] = tk;
         }
       __syncthreads();
-      if (INV) {  // Gauss-Jordan: every row of every panel column
-        for (int e = tid; e < n * BW; e += blockDim.x) {
-          const int i = e / BW, j = e - i * BW;  // BW is a power of two: shifts
-          if (j >= bw) continue;
-          S* el = pan + i * LD + j;
-          const S ci = colk[i];
-          const S old = i == k ? rp[j] : (i == p ? rk[j] : *el);
-          const S rj = rp[j] * ipv;
-          if (j == t) *el = i == k ? ipv : -ci * ipv;
-          else *el = i == k ? rj : df_sub_mul(old, ci, rj);
+      if (INV) {  // Gauss-Jordan: every row of the panel columns not yet eliminated (the eliminated ones are
+                  // rebuilt from W~ after the panel)
+        const int nc = bw - t - 1;
+        if (nc > 0) {
+          const float inc = 1.f / (float)nc;
+          for (int e = tid; e < n * nc; e += blockDim.x) {
+            int i = (int)((float)e * inc);
+            if (i * nc > e) --i;
+            else if ((i + 1) * nc <= e) ++i;
+            const int j = t + 1 + (e - i * nc);
+            S* el = pan + i * LD + j;
+            *el = i == k ? rj[j] : df_sub_mul(i == p ? rk[j] : *el, colk[i], rj[j]);
+          }
         }
       } else {  // LU: rows k.. of the panel columns right of the pivot (rows above k do not change)
         const int nc = bw - t - 1, nr = n - k;
@@ -222,8 +227,6 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
         Li[t * BW + tid] = acc.finish(t == tid ? S(1) : S(0));
       }
     }
-    if (INV && cj < bw)  // panel into the next working copy (the LU never reads finished panels again)
-      for (int i = rg; i < n; i += rn) dst[(size_t)i * n + k0 + cj] = pan[i * LD + cj];
     if (tid == 0) {  // the panel's row interchanges as one permutation
       for (int i = 0; i < n; ++i) rowmap[i] = i;
       for (int t = 0; t < bw; ++t) {
@@ -249,6 +252,8 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
       }
     }
     __syncthreads();
+    if (INV && cj < bw)  // the panel's final columns, e_{k0+s} - W~[:, s] (the LU never reads finished panels)
+      for (int i = rg; i < n; i += rn) dst[(size_t)i * n + k0 + cj] = (i == k0 + cj ? S(1) : S(0)) - W[i * LD + cj];
     // ---- apply the panel to the other columns (LU: the columns right of the panel, rows from k0):
     // x <- x - W~ y with y the panel's pivot rows of x.  Y (the bw pivot rows of every column, interchanged
     // order, rows padded to an even length) is staged over the panel buffer, which is free now; each thread

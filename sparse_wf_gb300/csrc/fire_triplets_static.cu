@@ -98,12 +98,12 @@ extern "C" fire_status fire_triplets_static(void* stream, const fire_problem* pr
   std::memset(&ext, 0, sizeof(ext));
   if (prob->precision == FIRE_PREC_FP64) {
     const size_t smem = 3 * n * sizeof(double) + (5 * n + 2) * sizeof(int);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_neighbors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_neighbors<double><<<B, 512, smem, s>>>(reinterpret_cast<const double*>(r), nullptr, (double)prob->cutoff,
                                             (double)prob->cutoff_1el, nb, ext, status);
   } else {
     const size_t smem = 3 * n * sizeof(float) + (5 * n + 2) * sizeof(int);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_neighbors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_neighbors<float><<<B, 512, smem, s>>>(reinterpret_cast<const float*>(r), nullptr, prob->cutoff,
                                            prob->cutoff_1el, nb, ext, status);
   }
