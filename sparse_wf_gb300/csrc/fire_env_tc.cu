@@ -33,14 +33,16 @@ struct EnvBar {
 
 // the 4 derivative coefficients of the 8 envelopes of nucleus I for an electron at (rx, ry, rz), split into
 // BF16 hi and lo planes: word w of plane v holds envelopes 2w (low half) and 2w + 1
-__device__ __forceinline__ void env_coef_rows(const EnvTcP& p, bool ok, float rx, float ry, float rz, int I,
-                                              uint4 (&hi)[4], uint4 (&lo)[4]) {
+// Rn: nuclear positions [N][3]; spd: this determinant's exponents of nucleus I at spd + I * sps (shared memory,
+// sps = NENV_ORB, when staged; else the global table, sps = NDET * NENV_ORB)
+__device__ __forceinline__ void env_coef_rows(const float* Rn, const float* spd, int sps, bool ok, float rx, float ry,
+                                              float rz, int I, uint4 (&hi)[4], uint4 (&lo)[4]) {
   float c[4][NENV_ORB];
   if (ok) {
-    const float dx = rx - p.R[3 * I], dy = ry - p.R[3 * I + 1], dz = rz - p.R[3 * I + 2];
+    const float dx = rx - Rn[3 * I], dy = ry - Rn[3 * I + 1], dz = rz - Rn[3 * I + 2];
     const float rho = sqrtf(dx * dx + dy * dy + dz * dz);
     const float irho = 1.f / rho;
-    const float* a = p.sp + ((long)I * NDET + p.d) * NENV_ORB;
+    const float* a = spd + (long)I * sps;
 #pragma unroll
     for (int k = 0; k < NENV_ORB; ++k) {
       const float ak = a[k];
@@ -75,9 +77,13 @@ __device__ __forceinline__ void env_coef_rows(const EnvTcP& p, bool ok, float rx
 
 // Bt: the determinant's tiled split weights [ceil(n / 128)][ceil(8 N / 64)] blocks of EnvCfg::B_BLOCK bytes.
 // Each CTA owns one 128-column slice of the output (blockIdx.x % nt) and walks the 32-electron tiles.
-__global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_bfloat16* Bt, int32_t* status) {
+__global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_bfloat16* Bt, int32_t* status,
+                                                           int stage_params) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];  // [stage][A hi, A lo, B hi, B lo]
   EnvBar* bars = reinterpret_cast<EnvBar*>(tc_smem + ENV_STAGES * EnvCfg::STAGE);
+  // the nuclear positions and this determinant's exponents, staged once (stage_params) after the barriers
+  float* Rsm = reinterpret_cast<float*>(tc_smem + EnvCfg::TOTAL);
+  float* spsm = Rsm + 3 * p.N;
   volatile int* abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n_e = p.Wc * p.ns;
@@ -106,12 +112,20 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
                  "r"(2 * TCP_BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  if (stage_params) {
+    for (int e = tid; e < 3 * p.N; e += blockDim.x) Rsm[e] = p.R[e];
+    for (int e = tid; e < NENV_ORB * p.N; e += blockDim.x)
+      spsm[e] = p.sp[((long)(e / NENV_ORB) * NDET + p.d) * NENV_ORB + e % NENV_ORB];
+  }
   proxy_fence();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = bars->tmem;
   long b_issued = 0;  // weight blocks issued (loader lane)
+  const float* Rn = stage_params ? Rsm : p.R;
+  const float* spd = stage_params ? spsm : p.sp + (long)p.d * NENV_ORB;
+  const int sps = stage_params ? NENV_ORB : NDET * NENV_ORB;
 
   if (warp >= 8 && warp < 12) {
     // ------------------------------------------------------------------ A producers (128 threads)
@@ -138,7 +152,7 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
         for (int q = 0; q < 2; ++q) {
           const int il = 2 * lw + q, I = kb * 8 + il;
           uint4 hi[4], lo[4];
-          env_coef_rows(p, ve && I < p.N, rx, ry, rz, I, hi, lo);
+          env_coef_rows(Rn, spd, sps, ve && I < p.N, rx, ry, rz, I, hi, lo);
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
             const uint32_t off = tc_off(v * 32 + lane, il * 8);
@@ -297,10 +311,19 @@ cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cu
   if (n_e <= 0 || p.n <= 0) return cudaSuccess;
   const long mt = (n_e + 31) / 32, nt = (p.n + TCP_BN - 1) / TCP_BN;
   const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
-  constexpr int smem = EnvCfg::TOTAL;
+  // the nuclear positions and this determinant's exponents go to shared memory when they fit
+  static int smem_max = 0;
+  if (smem_max == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  const size_t staged = (size_t)EnvCfg::TOTAL + sizeof(float) * (3 + NENV_ORB) * (size_t)p.N;
+  const int stage_params = staged <= (size_t)smem_max ? 1 : 0;
+  const int smem = stage_params ? (int)staged : EnvCfg::TOTAL;
   const cudaError_t e = cudaFuncSetAttribute(k_env_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_env_tc<<<(unsigned)(groups * nt), ENV_THREADS, smem, s>>>(p, Bt, status);
+  k_env_tc<<<(unsigned)(groups * nt), ENV_THREADS, smem, s>>>(p, Bt, status, stage_params);
   return cudaPeekAtLastError();
 }
 

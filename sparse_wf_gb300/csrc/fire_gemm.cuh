@@ -153,18 +153,31 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(GemmP<T> p) {
     const int a_r = tid >> 1, a_k = (tid & 1) * 4;
     const int b_k = tid >> 5, b_c = (tid & 31) * 4;
     T ra[4], rb[4];
+    // FP32 with 16-byte aligned rows: one vector load per operand whenever the 4 elements are in range
+    const bool va = sizeof(T) == 4 && p.lda % 4 == 0 && (reinterpret_cast<uintptr_t>(p.A) & 15) == 0;
+    const bool vb = sizeof(T) == 4 && p.ldb % 4 == 0 && (reinterpret_cast<uintptr_t>(Bp) & 15) == 0;
     auto load_tile = [&](int k0) {
       const int gr = m0 + a_r;
+      if (va && gr < rows && k0 + a_k + 3 < p.K) {
+        const float4 q = *reinterpret_cast<const float4*>(p.A + (long)gr * p.lda + k0 + a_k);
+        ra[0] = q.x; ra[1] = q.y; ra[2] = q.z; ra[3] = q.w;
+      } else {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int gk = k0 + a_k + u;
-        ra[u] = (gr < rows && gk < p.K) ? p.A[(long)gr * p.lda + gk] : T(0);
+        for (int u = 0; u < 4; ++u) {
+          const int gk = k0 + a_k + u;
+          ra[u] = (gr < rows && gk < p.K) ? p.A[(long)gr * p.lda + gk] : T(0);
+        }
       }
       const int gk = k0 + b_k;
+      if (vb && gk < p.K && n0 + b_c + 3 < p.N) {
+        const float4 q = *reinterpret_cast<const float4*>(Bp + (long)gk * p.ldb + n0 + b_c);
+        rb[0] = q.x; rb[1] = q.y; rb[2] = q.z; rb[3] = q.w;
+      } else {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int gc = n0 + b_c + u;
-        rb[u] = (gk < p.K && gc < p.N) ? Bp[(long)gk * p.ldb + gc] : T(0);
+        for (int u = 0; u < 4; ++u) {
+          const int gc = n0 + b_c + u;
+          rb[u] = (gk < p.K && gc < p.N) ? Bp[(long)gk * p.ldb + gc] : T(0);
+        }
       }
     };
     auto store_tile = [&](int buf) {
