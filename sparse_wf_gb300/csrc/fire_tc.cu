@@ -94,8 +94,10 @@ bool tc_c_map(const GemmP<float>& p, CUtensorMap* map) {
   const cuuint64_t strides[1] = {(cuuint64_t)p.ldc * sizeof(float)};
   const cuuint32_t box[2] = {16, 32};
   const cuuint32_t elem[2] = {1, 1};
+  // 64-byte swizzle: 16-byte chunk c of box row r sits at chunk c ^ ((r >> 1) & 3) in shared memory, so that a
+  // warp writing one chunk of each of its 32 rows hits every bank once per 8 rows (tc_epilogue_tile)
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, p.C, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+            CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
          CUDA_SUCCESS;
 }
 

@@ -330,7 +330,8 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
       float4 o[4];
       tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) *reinterpret_cast<float4*>(sb + lane * 16 + 4 * u) = o[u];
+      for (int u = 0; u < 4; ++u)  // the tensor map's 64-byte swizzle (staging buffers are 512-byte aligned)
+        *reinterpret_cast<float4*>(sb + lane * 16 + 4 * (u ^ ((lane >> 1) & 3))) = o[u];
       proxy_fence();
       __syncwarp();
       if (lane == 0) {
