@@ -940,8 +940,8 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
       int cnt;
       tc_shape(k, p, &K, &N, &cnt);
       const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
-      if (tc_tiled(k, K)) c.tcw[k] = TcWeights{nullptr, nullptr, nullptr, nullptr, hi, nullptr};
-      else c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr, nullptr, nullptr};
+      if (tc_tiled(k, K)) c.tcw[k] = TcWeights{nullptr, nullptr, hi, nullptr};
+      else c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr};
     }
     c.tcw[TC_ORB_UP].tiles2 = c.tcw[TC_ORB_DN].tiles;
   }

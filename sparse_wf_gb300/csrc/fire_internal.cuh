@@ -38,8 +38,6 @@ struct Layout {
 struct TcWeights {
   const __nv_bfloat16* hi;  // split weights transposed [N][K] (hi, lo): the streamed-weight kernel (K > 256)
   const __nv_bfloat16* lo;
-  const __nv_bfloat16* hi2;  // the other spin's weights (orbitals), or nullptr
-  const __nv_bfloat16* lo2;
   const __nv_bfloat16* tiles;   // split weights pre-tiled for the A-resident kernel (K <= 256)
   const __nv_bfloat16* tiles2;  // the other spin's tiles, or nullptr
 };

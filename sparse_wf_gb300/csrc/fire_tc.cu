@@ -105,10 +105,9 @@ cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt
                     cudaStream_t s) {
   if (p.K % 8 != 0 || p.lda % 4 != 0 || p.ldc % 4 != 0 || (p.ld_aux % 4 != 0 && mode != EPI_PLAIN))
     return cudaErrorInvalidValue;
-  // float4 operand loads and stores: A and every vector-accessed buffer 16-byte aligned (the envelope
-  // epilogue stores scalars: its destination may start mid-vector)
+  // float4 operand loads and stores: A, C and every vector-accessed buffer 16-byte aligned
   auto mis = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15) != 0; };
-  if (mis(p.A) || mis(p.aux0) || mis(p.aux1) || mis(p.aux2) || mis(p.aux3) || (mode != EPI_ENV && mis(p.C)))
+  if (mis(p.A) || mis(p.aux0) || mis(p.aux1) || mis(p.aux2) || mis(p.aux3) || mis(p.C))
     return cudaErrorInvalidValue;
   static int num_sms = 0;
   if (num_sms == 0) {

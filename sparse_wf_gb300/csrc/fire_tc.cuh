@@ -146,7 +146,7 @@ __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
 // Epilogue values of columns col..col+3 of one row (col % 4 == 0, col + 3 < N): everything but the store
-// of C (the orbital Jacobian epilogue stores its side output itself).  Not for EPI_ENV.
+// of C (the orbital Jacobian epilogue stores its side output itself).
 template <int MODE>
 __device__ __forceinline__ float4 tc_val4(const GemmP<float>& p, int row, int node, int col, const float* a,
                                           int spin) {
@@ -196,19 +196,11 @@ __device__ __forceinline__ float4 tc_val4(const GemmP<float>& p, int row, int no
 template <int MODE>
 __device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int node, int col, const float* a,
                                           int spin) {
-  if (MODE == EPI_ENV) {  // scalar stores: the destination of one determinant may start mid-vector
-    const int rr = row / p.env_nv, v = row - p.env_nv * rr;
-    const int g = (rr / p.env_ns) * p.n_el + p.env_soff + rr % p.env_ns;
-    float* out = p.C + ((long)g * p.env_nv + v) * p.ldc + col;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) out[k] = a[k];
-  } else {
-    st4(p.C + (long)row * p.ldc + col, tc_val4<MODE>(p, row, node, col, a, spin));
-  }
+  st4(p.C + (long)row * p.ldc + col, tc_val4<MODE>(p, row, node, col, a, spin));
 }
 
 // Epilogue values of 16 consecutive columns (col0 + 15 < N) of one row, into o: all operand loads are
-// issued before the first store so that their latencies overlap.  Not for EPI_ENV.
+// issued before the first store so that their latencies overlap.
 template <int MODE>
 __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int node, int col0, const float (&v)[16],
                                          int spin, float4 (&o)[4]) {
@@ -294,7 +286,7 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
     float v[16];
     tmem_ld16(base + (uint32_t)c0, v);
     const int spin = spin_filter < 0 ? 0 : spin_filter;
-    const bool full = MODE != EPI_ENV && n0 + c0 + 15 < p.N;
+    const bool full = n0 + c0 + 15 < p.N;
     const bool use_tma = tma_warp && full;
     float* sb = stg + (size_t)(warp * 2 + (nst & 1)) * 32 * 16;  // this chunk's staging buffer
     if (use_tma || MODE == EPI_SILU_J) {
@@ -857,7 +849,7 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
                                   cudaStream_t s, int num_sms) {
   CUtensorMap tmC;
   std::memset(&tmC, 0, sizeof(tmC));
-  const int tma = (MODE != EPI_ENV && tc_c_map(p, &tmC)) ? 1 : 0;
+  const int tma = tc_c_map(p, &tmC) ? 1 : 0;
   if (p.K <= TCP_KMAX) {  // A-resident kernel with pre-tiled weights
     if (!wt.tiles) return cudaErrorInvalidValue;
     constexpr int smem = TcaCfg::TOTAL;
@@ -877,7 +869,7 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
     return cudaPeekAtLastError();
   }
   // K > 256: streamed weights
-  if (!wt.hi || wt.hi2) return cudaErrorInvalidValue;
+  if (!wt.hi) return cudaErrorInvalidValue;
   constexpr int smem = TcCfg::TOTAL_SB;
   cudaError_t e = cudaFuncSetAttribute(k_gemm_tcs<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
