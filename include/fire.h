@@ -21,6 +21,7 @@
  *   fire_mcmc_block     mcmc.py:38-97 mcmc_steps_all_electron
  *   fire_mcmc_single_block  mcmc.py:100-111, 196-275 proposal_single_electron + mcmc_steps_low_rank
  *                       (each proposal evaluated in full, no low-rank state)
+ *   fire_mcmc_jump_block    mcmc.py:164-193 proposal_jump_to_atom (make_mcmc's jump_steps)
  *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
  *                       (used by the initialiser, new_sparse_model.py:378-379)
  */
@@ -213,6 +214,20 @@ fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const
                                    float width, uint64_t seed, uint64_t counter, const void* replay_noise,
                                    const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
                                    void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Metropolis block of jumps to the nuclei: proposal_jump_to_atom (mcmc.py:164-193) as run by
+ * mcmc_steps_low_rank for make_mcmc's jump_steps (mcmc.py:320-326).  Each step moves one random electron of
+ * every walker to R_I + sigma * eps, nucleus I drawn with probability Z_I / sum Z, and accepts if
+ * log(q(r_old) / q(r_new)) + 2 (log|psi'| - log|psi|) > log u, q(x) = sum_J Z_J exp(-|x - R_J|^2 / (2 sigma^2));
+ * log|psi'| is a full value-path evaluation.  Draws per step and walker (u_electron, u_nucleus, eps[3]) from
+ * Philox4x32-10 keyed by (seed, counter, step, walker), unless replay_draws [steps, B, 5] and replay_log_u
+ * [steps, B] are given: electron = min(floor(u_electron n), n - 1), nucleus = the first J whose cumulative
+ * charge exceeds u_nucleus sum Z.  Other arguments and outputs as fire_mcmc_block. */
+fire_status fire_mcmc_jump_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                 const void* prepared, void* r, void* logpsi, int32_t steps, float sigma,
+                                 uint64_t seed, uint64_t counter, const void* replay_draws,
+                                 const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
+                                 void* workspace, size_t workspace_bytes, int32_t* status);
 
 /* Coulomb potential of every walker (hamiltonian.py:15-26): out [B] in the walkers' dtype. */
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r,

@@ -27,7 +27,7 @@ What is restated (file:line in the reference project):
   ``Jastrow.apply_with_fwd_lap`` (``jastrow.py:387-459``);
 * ``kinetic_energy`` (``wave_function.py:215-221``), ``potential_energy``
   (``hamiltonian.py:15-26``), the all-electron Metropolis step (``mcmc.py:38-97``), the single-electron step
-  (``mcmc.py:100-111, 196-275``) with
+  (``mcmc.py:100-111, 196-275``), the jump to a nucleus (``mcmc.py:164-193``) with
   externally supplied noise.
 
 folx (0.2.15, a dependency absent here) is replaced by ``FL``: a dense forward-mode
@@ -863,6 +863,42 @@ def mcmc_block(prob, p, r, noise, log_u, width):
         rn = r + noise[s] * width
         lpn = 2.0 * logpsi(prob, p, rn)[1]
         m = (lpn - lp) - log_u[s]
+        margins.append(m)
+        if m > 0:
+            r, lp = rn, lpn
+            n_acc += 1
+    return r, lp, n_acc, np.array(margins)
+
+
+def jump_proposal(R, Z, r, d, sigma):
+    """``proposal_jump_to_atom`` (``mcmc.py:164-193``) for draws d = (u_electron, u_nucleus, eps[3]): electron
+    min(floor(u_e n), n - 1) moves to R_I + sigma eps, I the first nucleus whose cumulative charge exceeds
+    u_n sum Z.  Returns (r', log(q(r_old) / q(r_new))) with q(x) = sum_J Z_J exp(-|x - R_J|^2 / (2 sigma^2))."""
+    n = r.shape[0]
+    e = min(int(d[0] * n), n - 1)
+    cz = np.cumsum(np.asarray(Z, np.float64))
+    hit = np.nonzero(cz > d[1] * cz[-1])[0]
+    I = int(hit[0]) if len(hit) else len(Z) - 1
+    rn = r.copy()
+    rn[e] = np.asarray(R, np.float64)[I] + sigma * np.asarray(d[2:5], np.float64)
+
+    def q(x):
+        return np.sum(np.asarray(Z, np.float64) * np.exp(-0.5 / sigma**2 * np.sum((x - np.asarray(R, np.float64)) ** 2, axis=-1)))
+
+    return rn, np.log(q(r[e])) - np.log(q(rn[e]))
+
+
+def mcmc_jump_block(prob, p, r, draws, log_u, sigma):
+    """Metropolis block of jumps to the nuclei (``mcmc_steps_low_rank`` with ``proposal_jump_to_atom``,
+    ``mcmc.py:164-193, 196-275``) with externally supplied draws [steps, 5]: accept iff
+    log_ratio_proposal + 2 (log|psi'| - log|psi|) > log_u[s].  Returns (r, log_prob, n_accept, margins)."""
+    lp = 2.0 * logpsi(prob, p, r)[1]
+    n_acc = 0
+    margins = []
+    for s in range(draws.shape[0]):
+        rn, plr = jump_proposal(prob.R, prob.Z, r, draws[s], sigma)
+        lpn = 2.0 * logpsi(prob, p, rn)[1]
+        m = plr + (lpn - lp) - log_u[s]
         margins.append(m)
         if m > 0:
             r, lp = rn, lpn

@@ -167,7 +167,7 @@ struct Plan {
   size_t E5a, Z1, E5o, HX, HL, HJ, B1X, B1L, B1J, B2X, B2L, B2J, Zx, Zx2, jsq;
   size_t env, rawx, rjs, Apl, lapA, Jorb, coef_up, coef_dn, Ainv, dgrad;
   size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, Zr2, jsqr;
-  size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, tile_mask, aD1, aD2, ajsq;
+  size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, plr, tile_mask, aD1, aD2, ajsq;
   // double
   size_t ld, sd, dlap, gjw, enn;
   size_t total;
@@ -265,6 +265,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
   take(P.tile_mask, (fl ? 3 * Pc : G) / 128 + 2, 4);
   take(P.rn, G * 3, es);
   take(P.lpn, W, es);
+  take(P.plr, W, es);
   take(P.ld, W * NDET, 8);
   take(P.sd, W * NDET, 8);
   take(P.dlap, W * NDET, 8);
@@ -1010,13 +1011,15 @@ fire_status run_embedding(const fire_problem* p, cudaStream_t s, const float* R,
   return FIRE_OK;
 }
 
-// Metropolis block; single: one electron per step ((offset + step) mod n) instead of all of them.  Every
-// proposal is evaluated by the full value path.
+// Metropolis block.  Proposals: all electrons moved (MC_ALL), one electron per step, (offset + step) mod n
+// (MC_SINGLE), or one random electron jumping next to a nucleus with the proposal's log ratio in the test
+// (MC_JUMP, width = the jump's sigma).  Every proposal is evaluated by the full value path.
+enum McKind { MC_ALL = 0, MC_SINGLE = 1, MC_JUMP = 2 };
 template <typename T>
 fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
                      void* r, void* logpsi, int steps, float width, uint64_t seed, uint64_t counter,
                      const void* noise, const void* logu, int32_t* n_accept, int32_t* static_max, void* ws,
-                     size_t wsb, int32_t* status, bool single = false, int offset = 0) {
+                     size_t wsb, int32_t* status, int kind = MC_ALL, int offset = 0) {
   const int Wc = choose_chunk(p, wsb, false);
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
@@ -1027,11 +1030,15 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
     c.Wc = std::min(Wc, p->n_walkers - w0);
     T* rn = c.template buf<T>(c.P.rn);
     T* lpn = c.template buf<T>(c.P.lpn);
+    T* plr = kind == MC_JUMP ? c.template buf<T>(c.P.plr) : nullptr;
     for (int st = 0; st < steps; ++st) {
       g_nlaunch++;
-      if (single)
+      if (kind == MC_SINGLE)
         k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, w0, p->n_walkers, st, offset,
                                                  (T)width, seed, counter, reinterpret_cast<const T*>(noise));
+      else if (kind == MC_JUMP)
+        k_propose_jump<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, plr, n, w0, p->n_walkers, st, R, Z,
+                                               p->n_nuc, (T)width, seed, counter, reinterpret_cast<const T*>(noise));
       else
         k_propose<T><<<nblk((long)c.Wc * n), 256, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, c.Wc, w0, p->n_walkers,
                                                           st, (T)width, seed, counter,
@@ -1040,7 +1047,8 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
       if (chunk_logpsi<T>(c, lpn, nullptr, 0) != cudaSuccess) return launch_status("mcmc chunk");
       g_nlaunch++;
       k_accept<T><<<c.Wc, 128, 0, s>>>(rr, rn, reinterpret_cast<T*>(logpsi), lpn, n, w0, p->n_walkers, st, seed,
-                                      counter, reinterpret_cast<const T*>(logu), n_accept, c.nb.counts, static_max);
+                                      counter, reinterpret_cast<const T*>(logu), n_accept, c.nb.counts, static_max,
+                                      plr);
     }
   }
   return launch_status(__func__);
@@ -1245,9 +1253,26 @@ fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64)
     return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise,
-                            replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, true, step_offset);
+                            replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_SINGLE,
+                            step_offset);
   return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise, replay_log_u,
-                         n_accept, static_max, workspace, workspace_bytes, status, true, step_offset);
+                         n_accept, static_max, workspace, workspace_bytes, status, MC_SINGLE, step_offset);
+}
+
+fire_status fire_mcmc_jump_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                 const void* prepared, void* r, void* logpsi, int32_t steps, float sigma, uint64_t seed,
+                                 uint64_t counter, const void* replay_draws, const void* replay_log_u,
+                                 int32_t* n_accept, int32_t* static_max, void* workspace, size_t workspace_bytes,
+                                 int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || !(sigma > 0.f))
+    return FIRE_ERR_INVALID;
+  if ((replay_draws == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, sigma, seed, counter, replay_draws,
+                            replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
+  return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, sigma, seed, counter, replay_draws, replay_log_u,
+                         n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
 }
 
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r, const float* R,

@@ -73,7 +73,10 @@ __global__ void k_propose_single(const T* r, T* rn, int n, int w0, int B, int st
 template <typename T>
 __global__ void k_accept(T* r, const T* rn, T* logpsi, const T* logpsi_new, int n, int w0, int B, int step,
                          uint64_t seed, uint64_t counter, const T* replay_log_u, int32_t* n_accept, const int* counts,
-                         int32_t* static_max);
+                         int32_t* static_max, const T* plr);
+template <typename T>
+__global__ void k_propose_jump(const T* r, T* rn, T* plr, int n, int w0, int B, int step, const float* R,
+                               const float* Z, int N, T sigma, uint64_t seed, uint64_t counter, const T* replay);
 
 // fire_tc.cu (host launchers)
 cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __nv_bfloat16* lo, cudaStream_t s);

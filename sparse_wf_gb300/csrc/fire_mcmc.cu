@@ -1,5 +1,5 @@
-// fire_mcmc.cu -- Metropolis proposals (all-electron, mcmc.py:38-97; single-electron, mcmc.py:100-111) and
-// accept/reject.
+// fire_mcmc.cu -- Metropolis proposals (all-electron, mcmc.py:38-97; single-electron, mcmc.py:100-111; jump to a
+// nucleus, mcmc.py:164-193) and accept/reject.
 //
 // Random numbers: Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3",
 // SC'11), counter = (step, walker, electron, stream counter), key = seed; normals by Box-Muller.
@@ -91,13 +91,101 @@ __global__ void k_propose_single(const T* __restrict__ r, T* __restrict__ rn, in
   }
 }
 
+// Jump proposal (proposal_jump_to_atom, mcmc.py:164-193): a random electron of every walker is moved to
+// R_I + sigma * eps around a nucleus I drawn with probability Z_I / sum Z; plr[w] receives the proposal's
+// log ratio log(q(r_old) / q(r_new)), q(x) = sum_J Z_J exp(-|x - R_J|^2 / (2 sigma^2)).  Draws per walker
+// and step: d = (u_electron, u_nucleus, eps_x, eps_y, eps_z); electron = min(floor(u_e n), n - 1), nucleus =
+// the first J with cumulative charge > u_n sum Z.  replay [steps, B, 5]; one CTA per walker of the chunk.
+template <typename T>
+__global__ void k_propose_jump(const T* __restrict__ r, T* __restrict__ rn, T* __restrict__ plr, int n, int w0,
+                               int B, int step, const float* __restrict__ R, const float* __restrict__ Z, int N,
+                               T sigma, uint64_t seed, uint64_t counter, const T* __restrict__ replay) {
+  const int w = blockIdx.x;
+  const long gw = w0 + w;
+  const T* src = r + (long)w * 3 * n;
+  T* dst = rn + (long)w * 3 * n;
+  for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) dst[k] = src[k];
+  __shared__ double dr[5];
+  __shared__ int sel[2];
+  if (threadIdx.x == 0) {
+    if (replay) {
+      const T* q = replay + ((long)step * B + gw) * 5;
+      for (int k = 0; k < 5; ++k) dr[k] = (double)q[k];
+    } else {
+      uint32_t c0[4] = {(uint32_t)step, (uint32_t)gw, 0xFFFFFFFDu, (uint32_t)counter};
+      uint32_t c1[4] = {(uint32_t)step, (uint32_t)gw, 0xFFFFFFFCu, (uint32_t)counter};
+      philox10(c0, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
+      philox10(c1, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
+      dr[0] = u01(c0[0]);
+      dr[1] = u01(c0[1]);
+      const double r1 = sqrt(-2.0 * log(u01(c1[0]))), t1 = 6.283185307179586 * u01(c1[1]);
+      const double r2 = sqrt(-2.0 * log(u01(c1[2]))), t2 = 6.283185307179586 * u01(c1[3]);
+      dr[2] = r1 * cos(t1);
+      dr[3] = r1 * sin(t1);
+      dr[4] = r2 * cos(t2);
+    }
+    const int e = min((int)(dr[0] * n), n - 1);
+    double zs = 0.0;
+    for (int J = 0; J < N; ++J) zs += (double)Z[J];
+    const double tz = dr[1] * zs;
+    int I = N - 1;
+    double cz = 0.0;
+    for (int J = 0; J < N; ++J) {
+      cz += (double)Z[J];
+      if (cz > tz) {
+        I = J;
+        break;
+      }
+    }
+    sel[0] = e;
+    sel[1] = I;
+  }
+  __syncthreads();
+  const int e = sel[0], I = sel[1];
+  // new position (written after every thread has read the old one below)
+  const T xn = (T)R[3 * I] + sigma * (T)dr[2], yn = (T)R[3 * I + 1] + sigma * (T)dr[3],
+          zn = (T)R[3 * I + 2] + sigma * (T)dr[4];
+  const T xo = src[3 * e], yo = src[3 * e + 1], zo = src[3 * e + 2];
+  // q(old) and q(new) over the nuclei (block reduction in double)
+  const double inv2s2 = 0.5 / ((double)sigma * (double)sigma);
+  double qo = 0.0, qn = 0.0;
+  for (int J = threadIdx.x; J < N; J += blockDim.x) {
+    const double ax = (double)xo - R[3 * J], ay = (double)yo - R[3 * J + 1], az = (double)zo - R[3 * J + 2];
+    const double bx = (double)xn - R[3 * J], by = (double)yn - R[3 * J + 1], bz = (double)zn - R[3 * J + 2];
+    qo += (double)Z[J] * exp(-inv2s2 * (ax * ax + ay * ay + az * az));
+    qn += (double)Z[J] * exp(-inv2s2 * (bx * bx + by * by + bz * bz));
+  }
+  __shared__ double red[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    qo += __shfl_xor_sync(0xffffffffu, qo, o);
+    qn += __shfl_xor_sync(0xffffffffu, qn, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = qo;
+    red[1][threadIdx.x >> 5] = qn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double so = 0.0, sn = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      so += red[0][k];
+      sn += red[1][k];
+    }
+    plr[w] = (T)(log(so) - log(sn));
+    dst[3 * e] = xn;
+    dst[3 * e + 1] = yn;
+    dst[3 * e + 2] = zn;
+  }
+}
+
 // Accept if 2 (logpsi_new - logpsi_old) > log u (mcmc.py:68-73); one CTA per walker.
 // r, logpsi: whole batch (global walker index); rn, logpsi_new, counts: this chunk (local index).
+// plr (may be null): the proposals' log ratios log(q(r_old) / q(r_new)), added to the test (mcmc.py:238).
 template <typename T>
 __global__ void k_accept(T* __restrict__ r, const T* __restrict__ rn, T* __restrict__ logpsi,
                          const T* __restrict__ logpsi_new, int n, int w0, int B, int step, uint64_t seed,
                          uint64_t counter, const T* __restrict__ replay_log_u, int32_t* __restrict__ n_accept,
-                         const int* __restrict__ counts, int32_t* __restrict__ static_max) {
+                         const int* __restrict__ counts, int32_t* __restrict__ static_max, const T* __restrict__ plr) {
   const int w = blockIdx.x;
   const long gw = w0 + w;
   __shared__ int acc_s;
@@ -110,7 +198,7 @@ __global__ void k_accept(T* __restrict__ r, const T* __restrict__ rn, T* __restr
       philox10(ctr, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
       logu = log(u01(ctr[0]));
     }
-    const double ratio = 2.0 * ((double)logpsi_new[w] - (double)logpsi[gw]);
+    const double ratio = 2.0 * ((double)logpsi_new[w] - (double)logpsi[gw]) + (plr ? (double)plr[w] : 0.0);
     const int a = ratio > logu ? 1 : 0;
     acc_s = a;
     if (a) logpsi[gw] = logpsi_new[w];
@@ -135,9 +223,14 @@ template __global__ void k_propose_single<float>(const float*, float*, int, int,
                                                  uint64_t, const float*);
 template __global__ void k_propose_single<double>(const double*, double*, int, int, int, int, int, double,
                                                   uint64_t, uint64_t, const double*);
+template __global__ void k_propose_jump<float>(const float*, float*, float*, int, int, int, int, const float*,
+                                               const float*, int, float, uint64_t, uint64_t, const float*);
+template __global__ void k_propose_jump<double>(const double*, double*, double*, int, int, int, int, const float*,
+                                                const float*, int, double, uint64_t, uint64_t, const double*);
 template __global__ void k_accept<float>(float*, const float*, float*, const float*, int, int, int, int, uint64_t,
-                                         uint64_t, const float*, int32_t*, const int*, int32_t*);
+                                         uint64_t, const float*, int32_t*, const int*, int32_t*, const float*);
 template __global__ void k_accept<double>(double*, const double*, double*, const double*, int, int, int, int,
-                                          uint64_t, uint64_t, const double*, int32_t*, const int*, int32_t*);
+                                          uint64_t, uint64_t, const double*, int32_t*, const int*, int32_t*,
+                                          const double*);
 
 }  // namespace fire

@@ -374,6 +374,46 @@ class FireWaveFunction:
         sm = smax.cpu().numpy()
         return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
 
+    def mcmc_jump_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
+                        steps: int, sigma: float = 2.0, seed: int = 0, counter: int = 0, replay_draws=None,
+                        replay_log_u=None):
+        """In-place Metropolis block of jumps to the nuclei (``proposal_jump_to_atom``, ``mcmc.py:164-193``, run for
+        ``make_mcmc``'s ``jump_steps``): one random electron per step moves to R_I + sigma * eps, nucleus I drawn with
+        probability Z_I / sum Z, the proposal's log ratio in the test.  Every proposal is evaluated in full.
+        replay_draws [steps, B, 5] = (u_electron, u_nucleus, eps[3]), replay_log_u [steps, B].  Returns (n_accept
+        per walker, static_max)."""
+        p = self._params(params)
+        r = electrons
+        assert r.is_contiguous() and r.dtype == self.dtype
+        B = r.shape[0]
+        n_acc = torch.zeros(B, dtype=torch.int32, device=self.device)
+        smax = torch.zeros(4, dtype=torch.int32, device=self.device)
+        draws = None
+        if replay_draws is not None:
+            draws = torch.as_tensor(np.asarray(replay_draws)).to(self.device, self.dtype).reshape(steps, B, 5)
+            draws = draws.contiguous()
+        logu = None if replay_log_u is None else torch.as_tensor(replay_log_u).to(self.device, self.dtype).contiguous()
+        r0 = r.clone()
+        lp0 = logpsi.clone()
+
+        def fn(prob, ws):
+            r.copy_(r0)
+            logpsi.copy_(lp0)
+            n_acc.zero_()
+            smax.zero_()
+            _lib.check(_lib.load().fire_mcmc_jump_block(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(logpsi.data_ptr()),
+                int(steps), float(sigma), C.c_uint64(seed), C.c_uint64(counter),
+                C.c_void_p(draws.data_ptr()) if draws is not None else None,
+                C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_mcmc_jump_block")
+
+        self._run(fn, static, B)
+        sm = smax.cpu().numpy()
+        return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
+
 def make_local_energy(wf: FireWaveFunction):
     """``make_local_energy`` (``hamiltonian.py:49-83``) for all-electron systems:
     ``local_energy(key, params, electrons, static) -> (E_loc, new_static)``."""
@@ -386,10 +426,11 @@ def make_local_energy(wf: FireWaveFunction):
 
 
 def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, proposal: str = "all-electron",
-              sweeps: float = 2.0):
+              sweeps: float = 2.0, jump_steps: int = 0):
     """``make_mcmc`` (``mcmc.py:278-346``) for the "all-electron" proposal (``steps`` moves of every electron) and
     the "single-electron" proposal (``int(sweeps * n_el)`` one-electron moves in sequential order, the reference's
-    default; ``init_width`` 0.5 there, ``config/default.yaml``):
+    default; ``init_width`` 0.5 there, ``config/default.yaml``), preceded by ``jump_steps`` jumps to the nuclei
+    (sigma 2, ``mcmc.py:320-326, 332-335``; 20 in the reference's defaults):
     ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed."""
     proposal = proposal.lower()
     if proposal not in ("all-electron", "single-electron"):
@@ -400,11 +441,15 @@ def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, pr
         p = wf._params(params)
         r = wf._electrons(electrons).clone()
         _, logpsi = wf.signed(p, r, static)
+        stats = {}
+        if jump_steps > 0:
+            n_jump, _ = wf.mcmc_jump_block(p, r, logpsi, static, jump_steps, 2.0, seed=int(key), counter=1)
+            stats["pmove_jump"] = float(n_jump.float().mean().item()) / jump_steps
         if proposal == "all-electron":
             n_acc, smax = wf.mcmc_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
         else:
             n_acc, smax = wf.mcmc_single_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
-        stats = dict(pmove=float(n_acc.float().mean().item()) / max(n_steps, 1), static_max=smax, stepsize=width)
+        stats.update(pmove=float(n_acc.float().mean().item()) / max(n_steps, 1), static_max=smax, stepsize=width)
         return r, stats
 
     return mcmc_step, init_width

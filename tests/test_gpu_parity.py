@@ -258,3 +258,32 @@ def test_mcmc_single_electron_replay(cuda_lib, name):
     moved = np.any(got_r != r.astype(np.float64), axis=2)
     assert moved.sum() <= B * steps
     assert smax.n_pairs_same + smax.n_pairs_diff > 0
+
+
+@pytest.mark.parametrize("name", ["h10", "c2h6"])
+def test_mcmc_jump_replay(cuda_lib, name):
+    """Jumps to the nuclei (proposal_jump_to_atom, mcmc.py:164-193) in the FP64 build with replayed draws: accept
+    decisions and final positions equal the oracle's wherever its Metropolis margin (proposal log ratio included)
+    is clear of rounding."""
+    wf, mol, nu, r, p = _wf(name, "fp64")
+    B = r.shape[0]
+    steps, sigma = 12, 2.0
+    rng = np.random.default_rng(29)
+    draws = np.concatenate([rng.uniform(size=(steps, B, 2)), rng.standard_normal((steps, B, 3))], axis=2)
+    logu = np.log(rng.uniform(size=(steps, B)))
+    rr = torch.from_numpy(r.astype(np.float64)).cuda().contiguous()
+    static = _static(wf, rr)
+    dp = wf._params(p)
+    _, logpsi = wf.signed(dp, rr, static)
+    n_acc, _ = wf.mcmc_jump_block(dp, rr, logpsi, static, steps, sigma, replay_draws=draws, replay_log_u=logu)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    got_r, got_n = rr.cpu().numpy(), n_acc.cpu().numpy()
+    checked = 0
+    for w in range(B):
+        r_ref, lp_ref, na, mg = O.mcmc_jump_block(prob, p, r[w].astype(np.float64), draws[:, w], logu[:, w], sigma)
+        if np.all(np.abs(mg) > 1e-6):
+            checked += 1
+            assert got_n[w] == na, w
+            np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
+            np.testing.assert_allclose(logpsi[w].item(), 0.5 * lp_ref, rtol=1e-6)
+    assert checked > 0 and got_n.sum() > 0

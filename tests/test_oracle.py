@@ -141,3 +141,21 @@ def test_single_electron_block_is_the_all_electron_block_with_one_electron_moved
     np.testing.assert_array_equal(a[0], b[0])
     assert a[2] == b[2] and 0 < a[2] < steps
     np.testing.assert_allclose(a[3], b[3], rtol=0, atol=0)
+
+
+def test_jump_proposal_draw_mapping_and_log_ratio():
+    """proposal_jump_to_atom (mcmc.py:164-193): the electron and nucleus come from the two uniforms (nucleus by
+    cumulative charge), only that electron moves, to R_I + sigma eps, and the log ratio is log q(old) - log q(new)
+    with q(x) = sum_J Z_J exp(-|x - R_J|^2 / (2 sigma^2)) (the reference's weights Z / sum Z cancel)."""
+    R = np.array([[0.0, 0.0, 0.0], [2.0, 0.0, 0.0], [0.0, 3.0, 0.0]])
+    Z = np.array([6.0, 1.0, 1.0])
+    r = np.random.default_rng(3).standard_normal((5, 3))
+    sigma = 2.0
+    for d, e, I in (([0.0, 0.1, 0.5, -0.2, 0.3], 0, 0), ([0.99, 0.8, 0.0, 0.0, 0.0], 4, 1),
+                    ([0.41, 0.95, 1.0, 1.0, -1.0], 2, 2)):
+        rn, plr = O.jump_proposal(R, Z, r, np.array(d), sigma)
+        moved = np.any(rn != r, axis=1)
+        assert moved.sum() == 1 and moved[e]
+        np.testing.assert_allclose(rn[e], R[I] + sigma * np.array(d[2:]), atol=1e-15)
+        q = lambda x: np.sum(Z * np.exp(-np.sum((x - R) ** 2, axis=1) / (2 * sigma**2)))
+        assert abs(plr - (np.log(q(r[e])) - np.log(q(rn[e])))) < 1e-12
