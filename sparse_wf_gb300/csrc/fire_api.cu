@@ -685,7 +685,8 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
 }
 
 // Gauss-Jordan inversion (INV) or LU of every orbital matrix of the chunk, one CTA per matrix with the
-// working matrix in the workspace (k_gj_global).
+// working matrix in the workspace (k_gj_global).  Its shared memory (two panel buffers of n x 17 eight-byte
+// elements plus ~2.5 KB) limits the inverse, and so the local energy, to ELOC_MAX_EL electrons.
 template <typename S, typename TI, typename TO, bool INV>
 cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   const int n = c.p->n_el;
@@ -1210,6 +1211,7 @@ fire_status fire_local_energy(void* stream, const fire_problem* prob, const floa
                               double* e_stats, const fire_eloc_debug* debug, void* workspace, size_t workspace_bytes,
                               int32_t* status) {
   if (!valid(prob) || !R || !Z || !prepared || !r || !e_loc || !workspace) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL) return FIRE_ERR_UNSUPPORTED;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64)
     return run_eloc<double>(prob, s, R, Z, prepared, r, logpsi, sign, e_loc, e_stats, debug, workspace,

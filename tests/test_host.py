@@ -74,6 +74,16 @@ def test_sizes_and_invalid_arguments(lib):
     assert lib.fire_workspace_size(C.byref(prob_fp64), 8, C.byref(c)) == 0 and c.value > a.value
 
 
+def test_local_energy_rejects_problems_beyond_the_inverse_limit(lib):
+    """fire_local_energy returns FIRE_ERR_UNSUPPORTED (2) before any CUDA call for more than 798 electrons: the
+    orbital-matrix inverse is eliminated in shared memory; the pointers are never dereferenced."""
+    dummy = C.c_void_p(16)
+    big = _lib.Problem(800, 400, 100, 4, 5.0, 20.0, 100, 10, 0, 0)
+    rc = lib.fire_local_energy(None, C.byref(big), dummy, dummy, dummy, dummy, None, None, dummy, None, None, dummy,
+                               C.c_size_t(1), dummy)
+    assert rc == 2
+
+
 def test_static_padding_mirrors_reference():
     from sparse_wf_gb300.wavefunction import StaticArgs
 
