@@ -22,6 +22,7 @@
  *   fire_mcmc_single_block  mcmc.py:100-111, 196-275 proposal_single_electron + mcmc_steps_low_rank
  *                       (each proposal evaluated in full, no low-rank state)
  *   fire_mcmc_jump_block    mcmc.py:164-193 proposal_jump_to_atom (make_mcmc's jump_steps)
+ *   fire_mcmc_cluster_block mcmc.py:119-161 proposal_cluster_update (make_mcmc "cluster-update")
  *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
  *                       (used by the initialiser, new_sparse_model.py:378-379)
  */
@@ -216,6 +217,22 @@ fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const
                                    float width, uint64_t seed, uint64_t counter, const void* replay_noise,
                                    const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
                                    void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Metropolis block of cluster updates: proposal_cluster_update (mcmc.py:119-161) as run by mcmc_steps_low_rank
+ * (make_mcmc "cluster-update", mcmc.py:305-316).  Step s picks a center electron, (step_offset + s) mod n
+ * (random_sweep = 0) or uniformly at random, and moves the k = min(max_cluster_size, n) electrons closest to it
+ * (ties: lower index first) that lie within max_cluster_radius by width * eps (noise row i to the i-th closest);
+ * of 5 draws the first whose moved center has the same closest set is proposed, else the step is rejected
+ * (proposal log ratio log(0)).  log|psi'| is a full value-path evaluation.  Draws per step and walker: u_center,
+ * then eps [5][k][3] (Philox4x32-10 keyed by (seed, counter, step, walker), or replay_draws [steps, B, 1 + 15 k]
+ * with replay_log_u [steps, B]).  max_cluster_size <= 16.  Other arguments and outputs as fire_mcmc_block. */
+fire_status fire_mcmc_cluster_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                    const void* prepared, void* r, void* logpsi, int32_t steps, int32_t step_offset,
+                                    float width, int32_t max_cluster_size, float max_cluster_radius,
+                                    int32_t random_sweep, uint64_t seed, uint64_t counter,
+                                    const void* replay_draws, const void* replay_log_u, int32_t* n_accept,
+                                    int32_t* static_max, void* workspace, size_t workspace_bytes,
+                                    int32_t* status);
 
 /* Metropolis block of jumps to the nuclei: proposal_jump_to_atom (mcmc.py:164-193) as run by
  * mcmc_steps_low_rank for make_mcmc's jump_steps (mcmc.py:320-326).  Each step moves one random electron of

@@ -27,7 +27,7 @@ What is restated (file:line in the reference project):
   ``Jastrow.apply_with_fwd_lap`` (``jastrow.py:387-459``);
 * ``kinetic_energy`` (``wave_function.py:215-221``), ``potential_energy``
   (``hamiltonian.py:15-26``), the all-electron Metropolis step (``mcmc.py:38-97``), the single-electron step
-  (``mcmc.py:100-111, 196-275``), the jump to a nucleus (``mcmc.py:164-193``) with
+  (``mcmc.py:100-111, 196-275``), the jump to a nucleus (``mcmc.py:164-193``), the cluster update (``mcmc.py:119-161``) with
   externally supplied noise.
 
 folx (0.2.15, a dependency absent here) is replaced by ``FL``: a dense forward-mode
@@ -897,6 +897,56 @@ def mcmc_jump_block(prob, p, r, draws, log_u, sigma):
     margins = []
     for s in range(draws.shape[0]):
         rn, plr = jump_proposal(prob.R, prob.Z, r, draws[s], sigma)
+        lpn = 2.0 * logpsi(prob, p, rn)[1]
+        m = plr + (lpn - lp) - log_u[s]
+        margins.append(m)
+        if m > 0:
+            r, lp = rn, lpn
+            n_acc += 1
+    return r, lp, n_acc, np.array(margins)
+
+
+NO_NEIGHBOUR = 1_000_000  # model/graph_utils.py:14
+
+
+def closest_k(dist, dist_max, k):
+    """``_get_closest_k`` (``mcmc.py:114-117``): the k smallest distances (stable: lower index first on ties, as
+    ``jax.lax.top_k`` of -dist), NO_NEIGHBOUR where the distance exceeds dist_max."""
+    order = np.argsort(dist, kind="stable")[:k]
+    return np.where(dist[order] <= dist_max, order, NO_NEIGHBOUR)
+
+
+def cluster_proposal(r, d, k, radius, width, center):
+    """``proposal_cluster_update`` (``mcmc.py:119-161``) for draws d = (u_center, eps [5][k][3]) and a given center:
+    the k closest electrons within radius move by width * eps[t] (row i to the i-th closest); the first of 5 draws
+    whose moved center has the same closest set is proposed with log ratio 0, else the first draw with -inf.
+    Returns (r', log ratio)."""
+    idx = closest_k(np.linalg.norm(r - r[center], axis=-1), radius, k)
+    eps = np.asarray(d[1:], np.float64).reshape(5, k, 3)
+    props, valid = [], []
+    for t in range(5):
+        rp = r.copy()
+        for i in range(k):
+            if idx[i] != NO_NEIGHBOUR:
+                rp[idx[i]] = rp[idx[i]] + eps[t, i] * width
+        rev = closest_k(np.linalg.norm(rp - rp[center], axis=-1), radius, k)
+        props.append(rp)
+        valid.append(float(np.all(np.sort(idx) == np.sort(rev))))
+    t = int(np.argmax(valid))
+    return props[t], (0.0 if valid[t] > 0 else -np.inf)
+
+
+def mcmc_cluster_block(prob, p, r, draws, log_u, width, k, radius, random_sweep=False, offset=0):
+    """Metropolis block of cluster updates (``mcmc_steps_low_rank`` with ``proposal_cluster_update``) with
+    externally supplied draws [steps, 1 + 15 k]: center (offset + s) mod n, or min(floor(u_center n), n - 1) for a
+    random sweep.  Returns (r, log_prob, n_accept, margins)."""
+    n = r.shape[0]
+    lp = 2.0 * logpsi(prob, p, r)[1]
+    n_acc = 0
+    margins = []
+    for s in range(draws.shape[0]):
+        center = min(int(draws[s][0] * n), n - 1) if random_sweep else (offset + s) % n
+        rn, plr = cluster_proposal(r, draws[s], k, radius, width, center)
         lpn = 2.0 * logpsi(prob, p, rn)[1]
         m = plr + (lpn - lp) - log_u[s]
         margins.append(m)

@@ -29,6 +29,7 @@ SYMBOLS = [
     "fire_prepare_params", "fire_neighbors", "fire_triplets", "fire_logpsi", "fire_local_energy",
     "fire_embedding", "fire_mcmc_block", "fire_potential_energy", "fire_profile_enable", "fire_profile_report",
     "fire_gemm_mixed", "fire_triplets_static", "fire_mcmc_single_block", "fire_mcmc_jump_block",
+    "fire_mcmc_cluster_block",
 ]
 
 
@@ -78,6 +79,8 @@ def load() -> C.CDLL:
         "fire_mcmc_single_block": ([vp, P, vp, vp, vp, vp, vp, i32, i32, f32, u64, u64, vp, vp, vp, vp, vp, sz, vp],
                                    i32),
         "fire_mcmc_jump_block": ([vp, P, vp, vp, vp, vp, vp, i32, f32, u64, u64, vp, vp, vp, vp, vp, sz, vp], i32),
+        "fire_mcmc_cluster_block": ([vp, P, vp, vp, vp, vp, vp, i32, i32, f32, i32, f32, i32, u64, u64, vp, vp, vp, vp,
+                                     vp, sz, vp], i32),
         "fire_potential_energy": ([vp, P, vp, vp, vp, vp], i32),
         "fire_profile_enable": ([i32], i32),
         "fire_profile_report": ([C.c_char_p, sz], i32),

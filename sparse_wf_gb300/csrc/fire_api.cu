@@ -1015,12 +1015,15 @@ fire_status run_embedding(const fire_problem* p, cudaStream_t s, const float* R,
 // Metropolis block.  Proposals: all electrons moved (MC_ALL), one electron per step, (offset + step) mod n
 // (MC_SINGLE), or one random electron jumping next to a nucleus with the proposal's log ratio in the test
 // (MC_JUMP, width = the jump's sigma).  Every proposal is evaluated by the full value path.
-enum McKind { MC_ALL = 0, MC_SINGLE = 1, MC_JUMP = 2 };
+// MC_CLUSTER: the cluster update (ck electrons at most within cradius of the center, sequential or random
+// centers) with its validity in the test.
+enum McKind { MC_ALL = 0, MC_SINGLE = 1, MC_JUMP = 2, MC_CLUSTER = 3 };
 template <typename T>
 fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
                      void* r, void* logpsi, int steps, float width, uint64_t seed, uint64_t counter,
                      const void* noise, const void* logu, int32_t* n_accept, int32_t* static_max, void* ws,
-                     size_t wsb, int32_t* status, int kind = MC_ALL, int offset = 0) {
+                     size_t wsb, int32_t* status, int kind = MC_ALL, int offset = 0, int ck = 0, float cradius = 0.f,
+                     int crandom = 0) {
   const int Wc = choose_chunk(p, wsb, false);
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
@@ -1031,12 +1034,16 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
     c.Wc = std::min(Wc, p->n_walkers - w0);
     T* rn = c.template buf<T>(c.P.rn);
     T* lpn = c.template buf<T>(c.P.lpn);
-    T* plr = kind == MC_JUMP ? c.template buf<T>(c.P.plr) : nullptr;
+    T* plr = (kind == MC_JUMP || kind == MC_CLUSTER) ? c.template buf<T>(c.P.plr) : nullptr;
     for (int st = 0; st < steps; ++st) {
       g_nlaunch++;
       if (kind == MC_SINGLE)
         k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, w0, p->n_walkers, st, offset,
                                                  (T)width, seed, counter, reinterpret_cast<const T*>(noise));
+      else if (kind == MC_CLUSTER)
+        k_propose_cluster<T><<<c.Wc, 32, 0, s>>>(rr + (size_t)w0 * n * 3, rn, plr, n, w0, p->n_walkers, st, offset, ck,
+                                                 (T)cradius, (T)width, crandom, seed, counter,
+                                                 reinterpret_cast<const T*>(noise));
       else if (kind == MC_JUMP)
         k_propose_jump<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, plr, n, w0, p->n_walkers, st, R, Z,
                                                p->n_nuc, (T)width, seed, counter, reinterpret_cast<const T*>(noise));
@@ -1259,6 +1266,28 @@ fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const
                             step_offset);
   return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise, replay_log_u,
                          n_accept, static_max, workspace, workspace_bytes, status, MC_SINGLE, step_offset);
+}
+
+fire_status fire_mcmc_cluster_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                    const void* prepared, void* r, void* logpsi, int32_t steps, int32_t step_offset,
+                                    float width, int32_t max_cluster_size, float max_cluster_radius,
+                                    int32_t random_sweep, uint64_t seed, uint64_t counter, const void* replay_draws,
+                                    const void* replay_log_u, int32_t* n_accept, int32_t* static_max, void* workspace,
+                                    size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || step_offset < 0 ||
+      max_cluster_size < 1 || !(max_cluster_radius >= 0.f))
+    return FIRE_ERR_INVALID;
+  if (max_cluster_size > CLUSTER_KMAX) return FIRE_ERR_UNSUPPORTED;
+  if ((replay_draws == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  const int k = std::min<int>(max_cluster_size, prob->n_el);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_draws,
+                            replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_CLUSTER,
+                            step_offset, k, max_cluster_radius, random_sweep ? 1 : 0);
+  return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_draws, replay_log_u,
+                         n_accept, static_max, workspace, workspace_bytes, status, MC_CLUSTER, step_offset, k,
+                         max_cluster_radius, random_sweep ? 1 : 0);
 }
 
 fire_status fire_mcmc_jump_block(void* stream, const fire_problem* prob, const float* R, const float* Z,

@@ -60,6 +60,9 @@ constexpr int DL_CMAX = 64, DL_CSPLIT = 44, DL_OC = 32, DL_LD = DL_OC + 4, DL_ST
 __host__ __device__ constexpr int dl_jrows(int chi) { return 3 * chi + 4; }
 __host__ __device__ constexpr int dl_stage_elems(int chi) { return (dl_jrows(chi) + chi + 4) * DL_LD; }
 __host__ __device__ constexpr int dl_smem_elems(int chi) { return DL_STAGES * dl_stage_elems(chi); }
+// Cluster proposals: at most CLUSTER_KMAX electrons per cluster, CLUSTER_TRIALS draws per step
+// (proposal_cluster_update, mcmc.py:119-161).
+constexpr int CLUSTER_KMAX = 16, CLUSTER_TRIALS = 5;
 // Largest electron count of the local-energy path: the Gauss-Jordan inverse keeps two n x 17 panel buffers
 // of eight-byte elements (plus ~2.5 KB) in shared memory, 288 n + 2496 bytes within the 227 KB per CTA.
 constexpr int ELOC_MAX_EL = 798;

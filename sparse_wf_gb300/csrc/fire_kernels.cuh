@@ -75,6 +75,10 @@ __global__ void k_accept(T* r, const T* rn, T* logpsi, const T* logpsi_new, int 
                          uint64_t seed, uint64_t counter, const T* replay_log_u, int32_t* n_accept, const int* counts,
                          int32_t* static_max, const T* plr);
 template <typename T>
+__global__ void k_propose_cluster(const T* r, T* rn, T* plr, int n, int w0, int B, int step, int offset, int k,
+                                  T radius, T width, int random_sweep, uint64_t seed, uint64_t counter,
+                                  const T* replay);
+template <typename T>
 __global__ void k_propose_jump(const T* r, T* rn, T* plr, int n, int w0, int B, int step, const float* R,
                                const float* Z, int N, T sigma, uint64_t seed, uint64_t counter, const T* replay);
 

@@ -1,5 +1,5 @@
 // fire_mcmc.cu -- Metropolis proposals (all-electron, mcmc.py:38-97; single-electron, mcmc.py:100-111; jump to a
-// nucleus, mcmc.py:164-193) and accept/reject.
+// nucleus, mcmc.py:164-193; cluster update, mcmc.py:119-161) and accept/reject.
 //
 // Random numbers: Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3",
 // SC'11), counter = (step, walker, electron, stream counter), key = seed; normals by Box-Muller.
@@ -178,6 +178,130 @@ __global__ void k_propose_jump(const T* __restrict__ r, T* __restrict__ rn, T* _
   }
 }
 
+// The k electrons closest to position c (distance ascending, ties: lower index first, like jax.lax.top_k of
+// -dist) whose distance is at most radius; pos(j) gives electron j's position.  Returns how many qualify.
+template <typename T, typename PosFn>
+__device__ int closest_k(PosFn pos, int n, const T (&c)[3], int k, T radius, int (&idx)[CLUSTER_KMAX]) {
+  T best[CLUSTER_KMAX];
+  int m = 0;
+  for (int j = 0; j < n; ++j) {
+    T q[3];
+    pos(j, q);
+    const T dx = q[0] - c[0], dy = q[1] - c[1], dz = q[2] - c[2];
+    const T d = sqrt(dx * dx + dy * dy + dz * dz);
+    if (m == k && !(d < best[k - 1])) continue;
+    int i = m < k ? m++ : k - 1;
+    while (i > 0 && d < best[i - 1]) {
+      best[i] = best[i - 1];
+      idx[i] = idx[i - 1];
+      --i;
+    }
+    best[i] = d;
+    idx[i] = j;
+  }
+  int cnt = 0;
+  while (cnt < m && best[cnt] <= radius) ++cnt;
+  return cnt;
+}
+
+// Cluster proposal (proposal_cluster_update, mcmc.py:119-161): center (offset + step) mod n (sequential) or a
+// uniform draw (random); the k closest electrons within radius move by width * eps (noise row i to the i-th
+// closest); of CLUSTER_TRIALS draws the first whose moved center has the same k-closest set is used, plr = 0, else
+// the first draw with plr = -inf (always rejected).  Draws per walker and step: u_center, then eps
+// [CLUSTER_TRIALS][k][3]; replay [steps, B, 1 + 3 CLUSTER_TRIALS k].  One CTA per walker of the chunk.
+template <typename T>
+__global__ void k_propose_cluster(const T* __restrict__ r, T* __restrict__ rn, T* __restrict__ plr, int n, int w0,
+                                  int B, int step, int offset, int k, T radius, T width, int random_sweep,
+                                  uint64_t seed, uint64_t counter, const T* __restrict__ replay) {
+  const int w = blockIdx.x;
+  const long gw = w0 + w;
+  const T* src = r + (long)w * 3 * n;
+  T* dst = rn + (long)w * 3 * n;
+  for (int q = threadIdx.x; q < 3 * n; q += blockDim.x) dst[q] = src[q];
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const int nd = 1 + 3 * CLUSTER_TRIALS * k;
+  const T* rep = replay ? replay + ((long)step * B + gw) * nd : nullptr;
+  // draw m of this walker and step: uniform (m = 0) or standard normal (m >= 1)
+  double nbuf[4];
+  int nbase = -4;
+  auto draw = [&](int m) -> double {
+    if (rep) return (double)rep[m];
+    if (m == 0) {
+      uint32_t c0[4] = {(uint32_t)step, (uint32_t)gw, 0xFFFFFFFBu, (uint32_t)counter};
+      philox10(c0, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
+      return u01(c0[0]);
+    }
+    const int q = (m - 1) >> 2;
+    if (q * 4 != nbase) {
+      uint32_t c1[4] = {(uint32_t)step, (uint32_t)gw, 0x80000000u | (uint32_t)q, (uint32_t)counter};
+      philox10(c1, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
+      const double r1 = sqrt(-2.0 * log(u01(c1[0]))), t1 = 6.283185307179586 * u01(c1[1]);
+      const double r2 = sqrt(-2.0 * log(u01(c1[2]))), t2 = 6.283185307179586 * u01(c1[3]);
+      nbuf[0] = r1 * cos(t1);
+      nbuf[1] = r1 * sin(t1);
+      nbuf[2] = r2 * cos(t2);
+      nbuf[3] = r2 * sin(t2);
+      nbase = q * 4;
+    }
+    return nbuf[(m - 1) & 3];
+  };
+  const int center = random_sweep ? min((int)(draw(0) * n), n - 1) : (int)(((long)offset + step) % n);
+  T cpos[3] = {src[3 * center], src[3 * center + 1], src[3 * center + 2]};
+  int sel[CLUSTER_KMAX];
+  const int cnt = closest_k<T>([&](int j, T (&q)[3]) { q[0] = src[3 * j]; q[1] = src[3 * j + 1]; q[2] = src[3 * j + 2]; },
+                               n, cpos, k, radius, sel);
+  int sorted_sel[CLUSTER_KMAX];
+  for (int i = 0; i < cnt; ++i) sorted_sel[i] = sel[i];
+  for (int i = 1; i < cnt; ++i)
+    for (int a = i; a > 0 && sorted_sel[a] < sorted_sel[a - 1]; --a) {
+      const int t = sorted_sel[a];
+      sorted_sel[a] = sorted_sel[a - 1];
+      sorted_sel[a - 1] = t;
+    }
+  int chosen = -1;
+  T moved[CLUSTER_KMAX][3], first[CLUSTER_KMAX][3];
+  for (int t = 0; t < CLUSTER_TRIALS && chosen < 0; ++t) {
+    for (int i = 0; i < cnt; ++i)
+      for (int c = 0; c < 3; ++c)
+        moved[i][c] = src[3 * sel[i] + c] + width * (T)draw(1 + (t * k + i) * 3 + c);
+    if (t == 0)
+      for (int i = 0; i < cnt; ++i)
+        for (int c = 0; c < 3; ++c) first[i][c] = moved[i][c];
+    // the moved center (always in its own cluster, at distance 0)
+    T c2[3] = {cpos[0], cpos[1], cpos[2]};
+    for (int i = 0; i < cnt; ++i)
+      if (sel[i] == center) {
+        c2[0] = moved[i][0]; c2[1] = moved[i][1]; c2[2] = moved[i][2];
+      }
+    int rev[CLUSTER_KMAX];
+    const int cr = closest_k<T>(
+        [&](int j, T (&q)[3]) {
+          for (int i = 0; i < cnt; ++i)
+            if (sel[i] == j) {
+              q[0] = moved[i][0]; q[1] = moved[i][1]; q[2] = moved[i][2];
+              return;
+            }
+          q[0] = src[3 * j]; q[1] = src[3 * j + 1]; q[2] = src[3 * j + 2];
+        },
+        n, c2, k, radius, rev);
+    bool same = cr == cnt;
+    if (same) {
+      for (int i = 1; i < cr; ++i)
+        for (int a = i; a > 0 && rev[a] < rev[a - 1]; --a) {
+          const int tt = rev[a];
+          rev[a] = rev[a - 1];
+          rev[a - 1] = tt;
+        }
+      for (int i = 0; i < cr; ++i) same = same && rev[i] == sorted_sel[i];
+    }
+    if (same) chosen = t;
+  }
+  for (int i = 0; i < cnt; ++i)
+    for (int c = 0; c < 3; ++c) dst[3 * sel[i] + c] = chosen >= 0 ? moved[i][c] : first[i][c];
+  plr[w] = chosen >= 0 ? T(0) : T(-INFINITY);
+}
+
 // Accept if 2 (logpsi_new - logpsi_old) > log u (mcmc.py:68-73); one CTA per walker.
 // r, logpsi: whole batch (global walker index); rn, logpsi_new, counts: this chunk (local index).
 // plr (may be null): the proposals' log ratios log(q(r_old) / q(r_new)), added to the test (mcmc.py:238).
@@ -227,6 +351,10 @@ template __global__ void k_propose_jump<float>(const float*, float*, float*, int
                                                const float*, int, float, uint64_t, uint64_t, const float*);
 template __global__ void k_propose_jump<double>(const double*, double*, double*, int, int, int, int, const float*,
                                                 const float*, int, double, uint64_t, uint64_t, const double*);
+template __global__ void k_propose_cluster<float>(const float*, float*, float*, int, int, int, int, int, int, float,
+                                                  float, int, uint64_t, uint64_t, const float*);
+template __global__ void k_propose_cluster<double>(const double*, double*, double*, int, int, int, int, int, int,
+                                                   double, double, int, uint64_t, uint64_t, const double*);
 template __global__ void k_accept<float>(float*, const float*, float*, const float*, int, int, int, int, uint64_t,
                                          uint64_t, const float*, int32_t*, const int*, int32_t*, const float*);
 template __global__ void k_accept<double>(double*, const double*, double*, const double*, int, int, int, int,

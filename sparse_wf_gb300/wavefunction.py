@@ -414,6 +414,51 @@ class FireWaveFunction:
         sm = smax.cpu().numpy()
         return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
 
+    def mcmc_cluster_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
+                           steps: int, width: float, max_cluster_size: int = 5, max_cluster_radius: float = 2.0,
+                           sweep_type: str = "sequential", step_offset: int = 0, seed: int = 0, counter: int = 0,
+                           replay_draws=None, replay_log_u=None):
+        """In-place Metropolis block of cluster updates (``proposal_cluster_update``, ``mcmc.py:119-161``): each step
+        moves the electrons closest to a center (sequential or random) that lie within ``max_cluster_radius`` and
+        keeps the first of 5 draws whose cluster is unchanged around the moved center (none: rejected).  Every
+        proposal is evaluated in full.  replay_draws [steps, B, 1 + 15 k] = (u_center, eps [5][k][3]) with
+        k = min(max_cluster_size, n_el), replay_log_u [steps, B].  Returns (n_accept per walker, static_max)."""
+        if sweep_type not in ("sequential", "random"):
+            raise ValueError(f"Invalid sweep_type: {sweep_type}")
+        p = self._params(params)
+        r = electrons
+        assert r.is_contiguous() and r.dtype == self.dtype
+        B = r.shape[0]
+        k = min(int(max_cluster_size), self.mol.n_el)
+        n_acc = torch.zeros(B, dtype=torch.int32, device=self.device)
+        smax = torch.zeros(4, dtype=torch.int32, device=self.device)
+        draws = None
+        if replay_draws is not None:
+            draws = torch.as_tensor(np.asarray(replay_draws)).to(self.device, self.dtype).reshape(steps, B, 1 + 15 * k)
+            draws = draws.contiguous()
+        logu = None if replay_log_u is None else torch.as_tensor(replay_log_u).to(self.device, self.dtype).contiguous()
+        r0 = r.clone()
+        lp0 = logpsi.clone()
+
+        def fn(prob, ws):
+            r.copy_(r0)
+            logpsi.copy_(lp0)
+            n_acc.zero_()
+            smax.zero_()
+            _lib.check(_lib.load().fire_mcmc_cluster_block(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(logpsi.data_ptr()),
+                int(steps), int(step_offset), float(width), int(max_cluster_size), float(max_cluster_radius),
+                1 if sweep_type == "random" else 0, C.c_uint64(seed), C.c_uint64(counter),
+                C.c_void_p(draws.data_ptr()) if draws is not None else None,
+                C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_mcmc_cluster_block")
+
+        self._run(fn, static, B)
+        sm = smax.cpu().numpy()
+        return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
+
 def make_local_energy(wf: FireWaveFunction):
     """``make_local_energy`` (``hamiltonian.py:49-83``) for all-electron systems:
     ``local_energy(key, params, electrons, static) -> (E_loc, new_static)``."""
@@ -426,16 +471,23 @@ def make_local_energy(wf: FireWaveFunction):
 
 
 def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, proposal: str = "all-electron",
-              sweeps: float = 2.0, jump_steps: int = 0):
+              sweeps: float = 2.0, jump_steps: int = 0, max_cluster_size: int = 5, max_cluster_radius: float = 2.0,
+              sweep_type: str = "sequential"):
     """``make_mcmc`` (``mcmc.py:278-346``) for the "all-electron" proposal (``steps`` moves of every electron) and
     the "single-electron" proposal (``int(sweeps * n_el)`` one-electron moves in sequential order, the reference's
     default; ``init_width`` 0.5 there, ``config/default.yaml``), preceded by ``jump_steps`` jumps to the nuclei
-    (sigma 2, ``mcmc.py:320-326, 332-335``; 20 in the reference's defaults):
+    (sigma 2, ``mcmc.py:320-326, 332-335``; 20 in the reference's defaults); "cluster-update" runs
+    ``int(sweeps * n_el)`` cluster moves (``mcmc.py:305-316``; sequential sweeps must be whole):
     ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed."""
     proposal = proposal.lower()
-    if proposal not in ("all-electron", "single-electron"):
+    if proposal not in ("all-electron", "single-electron", "cluster-update"):
         raise ValueError(f"Invalid proposal: {proposal}")
     n_steps = steps if proposal == "all-electron" else int(sweeps * wf.mol.n_el)
+    if proposal == "cluster-update":
+        if sweep_type == "sequential" and n_steps % wf.mol.n_el != 0:
+            raise ValueError("Number of sweeps must be integer for sequential sweep")
+        if n_steps <= 0:
+            raise ValueError("Number of steps (sweeps * n_el) must be greater than 0")
 
     def mcmc_step(key, params, electrons, static: StaticArgs, width):
         p = wf._params(params)
@@ -447,6 +499,9 @@ def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, pr
             stats["pmove_jump"] = float(n_jump.float().mean().item()) / jump_steps
         if proposal == "all-electron":
             n_acc, smax = wf.mcmc_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
+        elif proposal == "cluster-update":
+            n_acc, smax = wf.mcmc_cluster_block(p, r, logpsi, static, n_steps, float(width), max_cluster_size,
+                                                max_cluster_radius, sweep_type, seed=int(key))
         else:
             n_acc, smax = wf.mcmc_single_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
         stats.update(pmove=float(n_acc.float().mean().item()) / max(n_steps, 1), static_max=smax, stepsize=width)

@@ -287,3 +287,35 @@ def test_mcmc_jump_replay(cuda_lib, name):
             np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
             np.testing.assert_allclose(logpsi[w].item(), 0.5 * lp_ref, rtol=1e-6)
     assert checked > 0 and got_n.sum() > 0
+
+
+@pytest.mark.parametrize("name,sweep", [("h10", "sequential"), ("h10", "random"), ("c2h6", "sequential")])
+def test_mcmc_cluster_replay(cuda_lib, name, sweep):
+    """Cluster updates (proposal_cluster_update, mcmc.py:119-161) in the FP64 build with replayed draws: accept
+    decisions and final positions equal the oracle's wherever its margin is clear of rounding (invalid clusters
+    give -inf)."""
+    wf, mol, nu, r, p = _wf(name, "fp64")
+    B, n = r.shape[0], mol.n_el
+    steps, off, width, kmax, radius = n + 2, 3, 0.5, 5, 2.0
+    k = min(kmax, n)
+    rng = np.random.default_rng(31)
+    draws = np.concatenate([rng.uniform(size=(steps, B, 1)), rng.standard_normal((steps, B, 15 * k))], axis=2)
+    logu = np.log(rng.uniform(size=(steps, B)))
+    rr = torch.from_numpy(r.astype(np.float64)).cuda().contiguous()
+    static = _static(wf, rr)
+    dp = wf._params(p)
+    _, logpsi = wf.signed(dp, rr, static)
+    n_acc, _ = wf.mcmc_cluster_block(dp, rr, logpsi, static, steps, width, kmax, radius, sweep, step_offset=off,
+                                     replay_draws=draws, replay_log_u=logu)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    got_r, got_n = rr.cpu().numpy(), n_acc.cpu().numpy()
+    checked = 0
+    for w in range(B):
+        r_ref, lp_ref, na, mg = O.mcmc_cluster_block(prob, p, r[w].astype(np.float64), draws[:, w], logu[:, w],
+                                                     float(np.float32(width)), k, float(np.float32(radius)),
+                                                     random_sweep=sweep == "random", offset=off)
+        if np.all(np.abs(mg) > 1e-6):
+            checked += 1
+            assert got_n[w] == na, w
+            np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
+    assert checked > 0 and got_n.sum() > 0

@@ -159,3 +159,26 @@ def test_jump_proposal_draw_mapping_and_log_ratio():
         np.testing.assert_allclose(rn[e], R[I] + sigma * np.array(d[2:]), atol=1e-15)
         q = lambda x: np.sum(Z * np.exp(-np.sum((x - R) ** 2, axis=1) / (2 * sigma**2)))
         assert abs(plr - (np.log(q(r[e])) - np.log(q(rn[e])))) < 1e-12
+
+
+def test_cluster_proposal_semantics():
+    """proposal_cluster_update (mcmc.py:119-161): the k closest electrons within the radius move (noise row i to the
+    i-th closest), a draw that changes the cluster around the moved center is skipped, none valid gives log 0."""
+    r = np.array([[0.0, 0, 0], [0.5, 0, 0], [1.0, 0, 0], [5.0, 0, 0], [0.0, 1.5, 0]])
+    idx = O.closest_k(np.linalg.norm(r - r[0], axis=-1), 1.2, 3)
+    np.testing.assert_array_equal(idx, [0, 1, 2])
+    idx = O.closest_k(np.linalg.norm(r - r[0], axis=-1), 0.7, 3)
+    np.testing.assert_array_equal(idx, [0, 1, O.NO_NEIGHBOUR])
+    k, width = 3, 1.0
+    eps = np.zeros((5, k, 3))
+    eps[0, 2] = [10.0, 0, 0]      # trial 0 throws the third member out of the cluster: invalid
+    eps[1, 0] = [0.05, 0, 0]      # trial 1 nudges the center: valid
+    d = np.concatenate([[0.0], eps.ravel()])
+    rn, plr = O.cluster_proposal(r, d, k, 1.2, width, 0)
+    assert plr == 0.0
+    np.testing.assert_allclose(rn[0], [0.05, 0, 0])
+    np.testing.assert_array_equal(rn[1:], r[1:])
+    eps[:, 2] = [10.0, 0, 0]      # every trial invalid: the first is proposed with log ratio -inf
+    d = np.concatenate([[0.0], eps.ravel()])
+    rn, plr = O.cluster_proposal(r, d, k, 1.2, width, 0)
+    assert plr == -np.inf and rn[2, 0] == 11.0
