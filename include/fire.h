@@ -177,8 +177,8 @@ typedef struct {
 
 /* logpsi, sign, e_loc: [B] in the walkers' dtype (may be NULL except e_loc);
  * e_stats: [2] float64 = (mean, std) of e_loc over the batch (may be NULL).
- * Up to 798 electrons (the inverse of the orbital matrices is eliminated in shared memory); larger problems
- * return FIRE_ERR_UNSUPPORTED. */
+ * Up to 798 electrons (the orbital matrices are eliminated in shared memory); larger problems return
+ * FIRE_ERR_UNSUPPORTED, here and in fire_logpsi and the Metropolis blocks. */
 fire_status fire_local_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,
                               const void* prepared, const void* r, void* logpsi, void* sign,
                               void* e_loc, double* e_stats, const fire_eloc_debug* debug,

@@ -838,12 +838,13 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   stage_embedding<T, 0>(c);
   stage_update<T, 0>(c);
   stage_orbitals<T, 0>(c);
-  // slogdet only: FP32 LU for the FP32/mixed value path, FP64 in the FP64 build
+  // slogdet only: double-FP32 LU in the FP32 and mixed paths (FP64-class, like the inverse of the local
+  // energy), native FP64 in the FP64 build
   Prof pr_lu("lu", c.s);
   if constexpr (sizeof(T) == 8)
     launch_gjg<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
   else
-    launch_gjg<float, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
+    launch_gjg<df64, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
   stage_jastrow<T, 0>(c);
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
@@ -1207,6 +1208,7 @@ fire_status fire_logpsi(void* stream, const fire_problem* prob, const float* R, 
                         const void* r, void* sign, void* logpsi, void* workspace, size_t workspace_bytes,
                         int32_t* status) {
   if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL) return FIRE_ERR_UNSUPPORTED;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64)
     return run_logpsi<double>(prob, s, R, Z, prepared, r, sign, logpsi, workspace, workspace_bytes, status);
@@ -1243,6 +1245,7 @@ fire_status fire_mcmc_block(void* stream, const fire_problem* prob, const float*
                             int32_t* static_max, void* workspace, size_t workspace_bytes, int32_t* status) {
   if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0) return FIRE_ERR_INVALID;
   if ((replay_noise == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL) return FIRE_ERR_UNSUPPORTED;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64)
     return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise,
@@ -1259,6 +1262,7 @@ fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const
   if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || step_offset < 0)
     return FIRE_ERR_INVALID;
   if ((replay_noise == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL) return FIRE_ERR_UNSUPPORTED;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64)
     return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_noise,
@@ -1280,6 +1284,7 @@ fire_status fire_mcmc_cluster_block(void* stream, const fire_problem* prob, cons
   if (max_cluster_size > CLUSTER_KMAX) return FIRE_ERR_UNSUPPORTED;
   if ((replay_draws == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
   const int k = std::min<int>(max_cluster_size, prob->n_el);
+  if (prob->n_el > ELOC_MAX_EL) return FIRE_ERR_UNSUPPORTED;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64)
     return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, width, seed, counter, replay_draws,
@@ -1298,6 +1303,7 @@ fire_status fire_mcmc_jump_block(void* stream, const fire_problem* prob, const f
   if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || !(sigma > 0.f))
     return FIRE_ERR_INVALID;
   if ((replay_draws == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL) return FIRE_ERR_UNSUPPORTED;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64)
     return run_mcmc<double>(prob, s, R, Z, prepared, r, logpsi, steps, sigma, seed, counter, replay_draws,

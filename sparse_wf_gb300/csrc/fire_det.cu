@@ -577,8 +577,8 @@ template __global__ void k_env_coef<double, 1>(const double*, const float*, cons
                                                int, double*);
 template __global__ void k_env_coef<double, 5>(const double*, const float*, const double*, int, int, int, int,
                                                int, double*);
-template __global__ void k_gj_global<float, float, float, false>(const float*, int, float*, double*, double*,
-                                                                  float*, int32_t*);
+template __global__ void k_gj_global<df64, float, float, false>(const float*, int, df64*, double*, double*, float*,
+                                                                 int32_t*);
 template __global__ void k_gj_global<df64, float, float, true>(const float*, int, df64*, double*, double*, float*,
                                                                 int32_t*);
 template __global__ void k_gj_global<double, double, double, true>(const double*, int, double*, double*, double*,
