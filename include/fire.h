@@ -60,8 +60,10 @@ typedef enum {
  * like StaticScheduler (static_args.py:62-84). */
 
 typedef enum {
-  FIRE_PREC_FP32 = 0,  /* everything in FP32 SIMT, orbital LU/inverse in FP64 */
-  FIRE_PREC_MIXED = 1, /* BF16 tensor-core MLP GEMMs (FP32 accumulate), rest FP32, LU in FP64 */
+  FIRE_PREC_FP32 = 0,  /* FP32 SIMT; orbital LU and inverse in double-FP32 (48-bit significand) */
+  FIRE_PREC_MIXED = 1, /* derivative planes of the contractions on tensor cores in split BF16 (three BF16
+                          products per FP32 product, FP32 accumulation), value planes FP32, orbital LU and
+                          inverse in double-FP32 */
   FIRE_PREC_FP64 = 2   /* everything in FP64 (validation build of the same kernels) */
 } fire_precision;
 
