@@ -851,6 +851,23 @@ def local_energy(prob, p, r):
     return kinetic_energy(prob, p, r) + potential_energy(r, prob.R, prob.Z)
 
 
+def woodbury_update(sign, logdet, A, Ainv, A_new, changed):
+    """``woodburry_update`` (``model/utils.py:216-245``): rows ``changed`` of A are replaced by those of A_new.
+    Matrix determinant lemma for the slogdet, det(A') = det(A) det(I + V A^-1[:, changed]) with V the row changes,
+    and the Woodbury identity for the inverse.  Indices outside [0, n) (NO_NEIGHBOUR padding of cluster moves)
+    contribute nothing, as the reference's ``mode="fill"`` gathers do.  Returns ((sign', logdet'), A'^-1)."""
+    n = A.shape[0]
+    changed = np.asarray(changed)
+    ok = (changed >= 0) & (changed < n)
+    safe = np.where(ok, changed, 0)
+    V = np.where(ok[:, None], A_new[safe] - A[safe], 0.0)          # [k, n]
+    AinvU = np.where(ok[None, :], Ainv[:, safe], 0.0)              # [n, k]
+    M = np.eye(len(changed)) + V @ AinvU
+    s_d, l_d = np.linalg.slogdet(M)
+    new_inv = Ainv - AinvU @ np.linalg.inv(M) @ V @ Ainv
+    return (sign * s_d, logdet + l_d), new_inv
+
+
 def mcmc_block(prob, p, r, noise, log_u, width):
     """All-electron Metropolis block (``mcmc.py:38-97``) with externally supplied draws.
 

@@ -182,3 +182,22 @@ def test_cluster_proposal_semantics():
     d = np.concatenate([[0.0], eps.ravel()])
     rn, plr = O.cluster_proposal(r, d, k, 1.2, width, 0)
     assert plr == -np.inf and rn[2, 0] == 11.0
+
+
+def test_woodbury_update_matches_recomputation():
+    """woodburry_update (model/utils.py:216-245), the determinant part of the reference's low-rank MCMC: replacing
+    k rows of A gives the slogdet and inverse of the new matrix, padded indices included (mode="fill")."""
+    rng = np.random.default_rng(8)
+    n = 24
+    A = rng.standard_normal((n, n))
+    s0, l0 = np.linalg.slogdet(A)
+    Ainv = np.linalg.inv(A)
+    for changed in ([3], [0, 7, 19], [5, O.NO_NEIGHBOUR, 11, O.NO_NEIGHBOUR]):
+        A_new = A.copy()
+        for i in changed:
+            if i < n:
+                A_new[i] = rng.standard_normal(n)
+        (s1, l1), inv1 = O.woodbury_update(s0, l0, A, Ainv, A_new, changed)
+        s_ref, l_ref = np.linalg.slogdet(A_new)
+        assert s1 == s_ref and abs(l1 - l_ref) < 1e-10
+        np.testing.assert_allclose(inv1, np.linalg.inv(A_new), rtol=0, atol=1e-9 * np.abs(np.linalg.inv(A_new)).max())
