@@ -494,9 +494,10 @@ def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, pr
         r = wf._electrons(electrons).clone()
         _, logpsi = wf.signed(p, r, static)
         stats = {}
-        if jump_steps > 0:
-            n_jump, _ = wf.mcmc_jump_block(p, r, logpsi, static, jump_steps, 2.0, seed=int(key), counter=1)
+        if jump_steps > 0:  # the reference keeps the jump block's statics apart (static_max["mcmc_jump"])
+            n_jump, smax_jump = wf.mcmc_jump_block(p, r, logpsi, static, jump_steps, 2.0, seed=int(key), counter=1)
             stats["pmove_jump"] = float(n_jump.float().mean().item()) / jump_steps
+            stats["static_max_jump"] = smax_jump
         if proposal == "all-electron":
             n_acc, smax = wf.mcmc_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
         elif proposal == "cluster-update":

@@ -175,3 +175,18 @@ def test_ragged_batch_draws():
     ns, ws = ragged_alkanes(64, seed=4)
     assert len(ns) == 64 and min(ns) >= 2 and max(ns) <= 40 and min(ws) >= 64 and max(ws) <= 1024
     assert ragged_alkanes(64, seed=4) == (ns, ws)
+
+
+def test_make_mcmc_proposal_selection_checks():
+    """make_mcmc (mcmc.py:278-346): unknown proposals are rejected, a sequential cluster sweep must cover whole
+    sweeps, and the step counts follow the reference (steps, int(sweeps * n_el)); no GPU call is made."""
+    from sparse_wf_gb300.wavefunction import FireWaveFunction, make_mcmc
+
+    wf = FireWaveFunction(systems.hydrogen_chain(10), precision="fp32", device="cpu")
+    with pytest.raises(ValueError):
+        make_mcmc(wf, proposal="gibbs")
+    with pytest.raises(ValueError):
+        make_mcmc(wf, proposal="cluster-update", sweeps=1.5)
+    make_mcmc(wf, proposal="cluster-update", sweeps=1.5, sweep_type="random")
+    _, width = make_mcmc(wf, proposal="single-electron", init_width=0.5, jump_steps=20)
+    assert width == 0.5
