@@ -319,3 +319,21 @@ def test_mcmc_cluster_replay(cuda_lib, name, sweep):
             assert got_n[w] == na, w
             np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
     assert checked > 0 and got_n.sum() > 0
+
+
+@pytest.mark.parametrize("proposal", ["all-electron", "single-electron", "cluster-update"])
+def test_make_mcmc_steps(cuda_lib, proposal):
+    """make_mcmc (mcmc.py:278-346) with 4 jump steps before the proposal: walkers keep their shape and move, the
+    acceptance fractions lie in [0, 1], the statics are reported for both blocks."""
+    from sparse_wf_gb300.wavefunction import make_mcmc
+
+    wf, mol, nu, r, p = _wf("h10", "fp32")
+    step, width = make_mcmc(wf, steps=3, init_width=0.3, proposal=proposal, sweeps=1.0, jump_steps=4)
+    rr = torch.from_numpy(r).cuda().contiguous()
+    static = _static(wf, rr)
+    r_new, stats = step(7, p, rr, static, width)
+    assert r_new.shape == rr.shape and torch.isfinite(r_new).all()
+    assert bool((r_new != rr).any())
+    assert 0.0 <= stats["pmove"] <= 1.0 and 0.0 <= stats["pmove_jump"] <= 1.0
+    assert stats["static_max"].n_pairs_same + stats["static_max"].n_pairs_diff > 0
+    assert stats["static_max_jump"].n_pairs_same + stats["static_max_jump"].n_pairs_diff > 0
