@@ -28,7 +28,13 @@ What is restated (file:line in the reference project):
 * ``kinetic_energy`` (``wave_function.py:215-221``), ``potential_energy``
   (``hamiltonian.py:15-26``), the all-electron Metropolis step (``mcmc.py:38-97``), the single-electron step
   (``mcmc.py:100-111, 196-275``), the jump to a nucleus (``mcmc.py:164-193``), the cluster update (``mcmc.py:119-161``) with
-  externally supplied noise.
+  externally supplied noise;
+* the low-rank update of a cached state: ``log_psi_with_state`` / ``log_psi_low_rank_update``
+  (``wave_function.py:226-287``), ``get_low_rank_pair_indices`` and ``NewSparseEmbedding.low_rank_update``
+  (``new_sparse_model.py:414-474, 553-629``), ``Orbitals.low_rank_update`` (``orbitals.py:121-146``),
+  ``woodburry_update`` (``model/utils.py:216-245``), ``Jastrow.low_rank_update`` (``jastrow.py:309-361``), driven by
+  ``mcmc_steps_low_rank`` (``mcmc.py:196-275``); pinned like the reference's ``tests/test_low_rank.py:29-61``, against
+  full evaluation.
 
 folx (0.2.15, a dependency absent here) is replaced by ``FL``: a dense forward-mode
 Laplacian carrier (value, Jacobian over T tangents, Laplacian), the published
@@ -45,11 +51,13 @@ bilinear ops.  Quirks of the reference that are reproduced on purpose:
 """
 from __future__ import annotations
 
+import dataclasses
+
 import numpy as np
 import scipy.linalg
 from scipy.special import expit
 
-NO_NEIGHBOUR = 1_000_000
+NO_NEIGHBOUR = 1_000_000  # model/graph_utils.py:14
 FEATURE_DIM = 256
 N_DET = 4
 ATT_HEADS = 16
@@ -408,30 +416,42 @@ class Problem:
         self.cutoff_1el = float(cutoff_1el)
 
 
-def embedding_value(prob, p, r, return_pre_scale=False):
-    """``NewSparseEmbedding.apply`` (``new_sparse_model.py:483-551``)."""
+def _contract(prob, p, r, ei, h, same_pairs, diff_pairs):
+    """Adds the messages of the (center, neighbour) pairs to h in place, same-spin pairs first
+    (``contract_pair``, ``new_sparse_model.py:82-93, 515-524``); ei is ElecInit's [n, 5F] output."""
     F = FEATURE_DIM
-    n = prob.n_el
-    _, _, n_trip, n_en = static_counts(r32(r), prob.R, prob.n_up, prob.cutoff, prob.cutoff_1el, False)
-    (cs, ns, _), (cd, nd, _), _ = pair_indices(r32(r), prob.n_up, prob.cutoff)
-    nb = neighbouring_nuclei(r32(r), prob.R, prob.cutoff_1el, n_en)
-    out = elec_init_value(p, r, prob.R, nb, prob.cutoff_1el)
-    h0, ct_s, ct_d, nb_s, nb_d = (out[:, k * F:(k + 1) * F] for k in range(5))
+    _, ct_s, ct_d, nb_s, nb_d = (ei[:, k * F:(k + 1) * F] for k in range(5))
     cutoff_eff = prob.cutoff * sigmoid(p["cutoff_param"][0])
-    h = h0.copy()
-    for tag, ct, nbi, mct, mnb in (("same", cs, ns, ct_s, nb_s), ("diff", cd, nd, ct_d, nb_d)):
+    for tag, (ct, nbi), mct, mnb in (("same", same_pairs, ct_s, nb_s), ("diff", diff_pairs, ct_d, nb_d)):
         if len(ct) == 0:
             continue
         gamma, edge = _edge_value(p, tag, r[ct], r[nbi], cutoff_eff)
-        msg = gamma * silu(edge + mct[ct] + mnb[nbi])
-        np.add.at(h, ct, msg)
-    h_contract = h
-    h = h * p["scales"][0]
-    h = silu(h @ p["upd1_W"] + p["upd1_b"])
+        np.add.at(h, ct, gamma * silu(edge + mct[ct] + mnb[nbi]))
+    return h
+
+
+def _node_update(p, h):
+    """Per-electron update between the two stored normalisation scales (``new_sparse_model.py:525-528``)."""
+    h = silu((h * p["scales"][0]) @ p["upd1_W"] + p["upd1_b"])
     h = silu(h @ p["upd2_W"] + p["upd2_b"])  # last-layer SiLU quirk (sparse_fwd_lap.py:218-224)
-    if return_pre_scale:
-        return h_contract, h
     return h * p["scales"][1]
+
+
+def embedding_value(prob, p, r, return_pre_scale=False, return_init=False):
+    """``NewSparseEmbedding.apply`` (``new_sparse_model.py:483-551``).  With ``return_init`` also returns
+    ElecInit's [n, 5F] output (h0 and the four message maps, the embedding part of the low-rank state)."""
+    F = FEATURE_DIM
+    _, _, n_trip, n_en = static_counts(r32(r), prob.R, prob.n_up, prob.cutoff, prob.cutoff_1el, False)
+    (cs, ns, _), (cd, nd, _), _ = pair_indices(r32(r), prob.n_up, prob.cutoff)
+    nb = neighbouring_nuclei(r32(r), prob.R, prob.cutoff_1el, n_en)
+    ei = elec_init_value(p, r, prob.R, nb, prob.cutoff_1el)
+    h = _contract(prob, p, r, ei, ei[:, :F].copy(), (cs, ns), (cd, nd))
+    if return_pre_scale:
+        h_contract = h
+        h = silu((h * p["scales"][0]) @ p["upd1_W"] + p["upd1_b"])
+        return h_contract, silu(h @ p["upd2_W"] + p["upd2_b"])
+    h = _node_update(p, h)
+    return (h, ei) if return_init else h
 
 
 def r32(r):
@@ -440,25 +460,33 @@ def r32(r):
     return np.asarray(r, np.float32) if r.dtype == np.float64 else r
 
 
+def _envelope_rows(prob, p, rs, spin):
+    """Envelope rows [m, D*n] of electrons ``rs`` of one spin ("up" or "dn")."""
+    d = np.linalg.norm(rs[:, None, :] - prob.R[None].astype(rs.dtype), axis=-1)  # [m, N]
+    ex = np.exp(-d[:, :, None, None] * softplus(p[f"env_{spin}_sigma"])[None])  # [m, N, D, K]
+    o = np.einsum("mNdk,Ndko->mdo", ex, p[f"env_{spin}_pi"])
+    return o.reshape(len(rs), -1)
+
+
 def envelopes_value(prob, p, r):
     """``EfficientIsotropicEnvelopes`` (``model/envelopes.py:55-82``) per spin: [n, D*n]."""
-    n, nu = prob.n_el, prob.n_up
-    out = []
-    for spin, rs in (("up", r[:nu]), ("dn", r[nu:])):
-        d = np.linalg.norm(rs[:, None, :] - prob.R[None].astype(r.dtype), axis=-1)  # [m, N]
-        ex = np.exp(-d[:, :, None, None] * softplus(p[f"env_{spin}_sigma"])[None])  # [m, N, D, K]
-        o = np.einsum("mNdk,Ndko->mdo", ex, p[f"env_{spin}_pi"])
-        out.append(o.reshape(len(rs), -1))
-    return np.concatenate(out, 0)
+    nu = prob.n_up
+    return np.concatenate([_envelope_rows(prob, p, r[:nu], "up"), _envelope_rows(prob, p, r[nu:], "dn")], 0)
+
+
+def _orbital_rows(prob, p, h):
+    """Raw orbital rows [n, D*n]: per-spin linear maps of the embeddings (``orbitals.py:109-115``)."""
+    nu = prob.n_up
+    return np.concatenate([h[:nu] @ p["orb_up_W"] + p["orb_up_b"], h[nu:] @ p["orb_dn_W"] + p["orb_dn_b"]], 0)
+
+
+def _orbital_matrices(prob, raw, env):
+    return (raw * env).reshape(prob.n_el, N_DET, prob.n_el).transpose(1, 0, 2)
 
 
 def orbitals_value(prob, p, r, h):
     """``Orbitals.__call__`` (``model/orbitals.py:109-119``): [D, n, n]."""
-    nu = prob.n_up
-    raw = np.concatenate([h[:nu] @ p["orb_up_W"] + p["orb_up_b"], h[nu:] @ p["orb_dn_W"] + p["orb_dn_b"]], 0)
-    env = envelopes_value(prob, p, r)
-    phi = raw * env
-    return phi.reshape(prob.n_el, N_DET, prob.n_el).transpose(1, 0, 2)
+    return _orbital_matrices(prob, _orbital_rows(prob, p, h), envelopes_value(prob, p, r))
 
 
 def _spin_pair_dists(r, n_up):
@@ -471,17 +499,27 @@ def _spin_pair_dists(r, n_up):
     return np.concatenate([same_up, same_dn]), d[:n_up, n_up:].reshape(-1)
 
 
-def jastrow_value(prob, p, r, h):
-    """``Jastrow.__call__`` (``model/jastrow.py:261-307``) with psiformer cusp, MLP/log Jastrow and attention."""
-    nu = prob.n_up
-    a_s, a_d, f_s, f_d = p["cusp"]
-    ds, dd = _spin_pair_dists(r, nu)
-    logpsi = f_s * np.sum(a_s**2 / (a_s + ds)) + f_d * np.sum(a_d**2 / (a_d + dd))
-    # attention (jastrow.py:85-100, 139-151)
+def _jastrow_rows(p, h):
+    """Per-electron Jastrow terms of embeddings h [m, F]: the MLP rows ``one_el`` [m, 2] (SparseMLP with final
+    SiLU, ``jastrow.py:213-216, 363-364``), attention weights ``att`` [m, H] and weighted values ``vals``
+    [m, H, A] (``jastrow.py:85-100``)."""
     q = (h @ p["att_Q_W"] + p["att_Q_b"]).reshape(-1, ATT_HEADS, ATT_DIM)
     v = (h @ p["att_V_W"] + p["att_V_b"]).reshape(-1, ATT_HEADS, ATT_DIM)
     att = np.exp(-(q * p["att_keys"]).sum(-1) / np.sqrt(ATT_DIM))
     vals = att[..., None] * v
+    m = silu(h @ p["jmlp1_W"] + p["jmlp1_b"])
+    m = silu(m @ p["jmlp2_W"] + p["jmlp2_b"])
+    m = silu(m @ p["jmlp3_W"] + p["jmlp3_b"])
+    one_el = m * p["mlp_scale"] + np.array([0.0, p["log_bias"][0]])
+    return one_el, att, vals
+
+
+def _jastrow_readout(prob, p, r, one_el, att, vals):
+    """Cusp of r plus the attention readout (``jastrow.py:139-151``) and the summed MLP rows: (sign, log J)."""
+    nu = prob.n_up
+    a_s, a_d, f_s, f_d = p["cusp"]
+    ds, dd = _spin_pair_dists(r, nu)
+    logpsi = f_s * np.sum(a_s**2 / (a_s + ds)) + f_d * np.sum(a_d**2 / (a_d + dd))
     norm = np.stack([att[:nu].sum(0), att[nu:].sum(0)])
     vals = np.stack([vals[:nu].sum(0), vals[nu:].sum(0)])
     x = (vals / norm[..., None]).reshape(-1)
@@ -489,13 +527,13 @@ def jastrow_value(prob, p, r, h):
     x = silu(x @ p["att_out2_W"] + p["att_out2_b"])
     x = x @ p["att_out3_W"] + p["att_out3_b"]
     J = x * p["att_scale"] + np.array([0.0, p["att_bias"][0]])
-    # MLP (SparseMLP with final SiLU, jastrow.py:213-216, 363-364)
-    m = silu(h @ p["jmlp1_W"] + p["jmlp1_b"])
-    m = silu(m @ p["jmlp2_W"] + p["jmlp2_b"])
-    m = silu(m @ p["jmlp3_W"] + p["jmlp3_b"])
-    m = m * p["mlp_scale"] + np.array([0.0, p["log_bias"][0]])
-    J = J + m.sum(0)
+    J = J + one_el.sum(0)
     return np.sign(J[1]), logpsi + J[0] + np.log(np.abs(J[1]))
+
+
+def jastrow_value(prob, p, r, h):
+    """``Jastrow.__call__`` (``model/jastrow.py:261-307``) with psiformer cusp, MLP/log Jastrow and attention."""
+    return _jastrow_readout(prob, p, r, *_jastrow_rows(p, h))
 
 
 def logsumexp_signed(logdets, signs):
@@ -868,6 +906,133 @@ def woodbury_update(sign, logdet, A, Ainv, A_new, changed):
     return (sign * s_d, logdet + l_d), new_inv
 
 
+# =============================================================================== low-rank update
+@dataclasses.dataclass
+class LowRankState:
+    """``LowRankState`` (``model/wave_function.py:226-247``) of one walker: what a move of a few electrons reuses.
+
+    r [n, 3]; ei [n, 5F] ElecInit output (h0 | msg_ct_same | msg_ct_diff | msg_nb_same | msg_nb_diff,
+    ``EmbeddingState``); h [n, F] embeddings; env, orb [n, D n] envelope and raw orbital rows (``OrbitalState``);
+    A, Ainv [D, n, n], signs, logdets [D] (``LogPsiState``); one_el [n, 2], att [n, H], vals [n, H, A]
+    (``JastrowState``)."""
+
+    r: np.ndarray
+    ei: np.ndarray
+    h: np.ndarray
+    env: np.ndarray
+    orb: np.ndarray
+    A: np.ndarray
+    Ainv: np.ndarray
+    signs: np.ndarray
+    logdets: np.ndarray
+    one_el: np.ndarray
+    att: np.ndarray
+    vals: np.ndarray
+
+
+def _moved(n, idx_changed):
+    """In-range moved electrons.  Padded entries (NO_NEIGHBOUR, from cluster moves) gather electron n - 1, as an
+    out-of-range JAX gather clamps, and are dropped by scatters."""
+    idx = np.asarray(idx_changed, np.int64)
+    return idx[(idx >= 0) & (idx < n)], np.clip(idx, 0, n - 1)
+
+
+def affected_electrons(prob, r_old, r_new, idx_changed):
+    """Electrons whose embedding changes when ``idx_changed`` move from r_old to r_new, and the pairs needed to
+    recompute them (``get_low_rank_pair_indices``, ``new_sparse_model.py:439-474``): every electron within the
+    cutoff of a moved electron before or after the move, plus the moved ones.  Returns (mask [n], required [n, n])
+    with required[i, j] = i affected and j a neighbour of i after the move."""
+    n = prob.n_el
+    moved, gathered = _moved(n, idx_changed)
+    inc_old = in_cutoff_matrix(r32(r_old), prob.cutoff)
+    inc_new = in_cutoff_matrix(r32(r_new), prob.cutoff)
+    aff = np.any(inc_old[:, gathered] | inc_new[:, gathered], axis=-1)
+    aff[moved] = True
+    return aff, inc_new & aff[:, None]
+
+
+def changed_counts(prob, r_old, r_new, idx_changed):
+    """The move statics of ``get_static_input`` (``new_sparse_model.py:414-424``):
+    (n_changed_hout, n_changed_pair_same, n_changed_pair_diff)."""
+    aff, req = affected_electrons(prob, r_old, r_new, idx_changed)
+    spin = np.arange(prob.n_el) < prob.n_up
+    same = spin[:, None] == spin[None, :]
+    return int(aff.sum()), int(np.sum(req & same)), int(np.sum(req & ~same))
+
+
+def logpsi_with_state(prob, p, r):
+    """``log_psi_with_state`` (``wave_function.py:226-247``): ((sign, log|psi|), LowRankState); the inverses
+    come from an LU (``slog_and_inverse``, ``model/utils.py:164-175``)."""
+    h, ei = embedding_value(prob, p, r, return_init=True)
+    env = envelopes_value(prob, p, r)
+    orb = _orbital_rows(prob, p, h)
+    A = _orbital_matrices(prob, orb, env)
+    sl = [slogdet_lu(A[d]) for d in range(N_DET)]
+    Ainv = np.stack([scipy.linalg.lu_solve(x[2], np.eye(prob.n_el)) for x in sl])
+    one_el, att, vals = _jastrow_rows(p, h)
+    st = LowRankState(r.copy(), ei, h, env, orb, A, Ainv, np.array([x[0] for x in sl]),
+                      np.array([x[1] for x in sl]), one_el, att, vals)
+    s_det, l_det = logsumexp_signed(st.logdets, st.signs)
+    s_j, l_j = _jastrow_readout(prob, p, r, one_el, att, vals)
+    return (s_det * s_j, l_det + l_j), st
+
+
+def logpsi_low_rank_update(prob, p, r, idx_changed, state):
+    """``log_psi_low_rank_update`` (``wave_function.py:249-287``): log|psi| at r, where only electrons
+    ``idx_changed`` moved since ``state``, from recomputed rows only.
+
+    * embedding (``NewSparseEmbedding.low_rank_update``, ``new_sparse_model.py:553-629``): ElecInit rows of the moved
+      electrons; every affected electron is reset to h0 and its messages are contracted again over its neighbours
+      after the move, then updated;
+    * orbitals (``Orbitals.low_rank_update``, ``orbitals.py:121-146``): envelope rows of the moved electrons, raw
+      orbital rows of the affected ones;
+    * determinants (``signed_log_psi_from_orbitals_low_rank``, ``model/utils.py:287-306``): the determinant lemma
+      and the Woodbury update of A^-1 over the affected rows;
+    * Jastrow (``Jastrow.low_rank_update``, ``jastrow.py:309-361``): MLP and attention rows of the affected
+      electrons, the cusp in full.
+
+    Returns ((sign, log|psi|), LowRankState at r)."""
+    F = FEATURE_DIM
+    n, nu = prob.n_el, prob.n_up
+    moved, _ = _moved(n, idx_changed)
+    aff, req = affected_electrons(prob, state.r, r, idx_changed)
+    rows = np.nonzero(aff)[0]
+    spin = np.arange(n) < nu
+    same = spin[:, None] == spin[None, :]
+
+    ei = state.ei.copy()
+    if len(moved):
+        n_en = static_counts(r32(r), prob.R, nu, prob.cutoff, prob.cutoff_1el, False)[3]
+        nb = neighbouring_nuclei(r32(r)[moved], prob.R, prob.cutoff_1el, n_en)
+        ei[moved] = elec_init_value(p, r[moved], prob.R, nb, prob.cutoff_1el)
+    h = state.h.copy()
+    h[rows] = ei[rows, :F]
+    h = _contract(prob, p, r, ei, h, np.nonzero(req & same), np.nonzero(req & ~same))
+    h[rows] = _node_update(p, h[rows])
+
+    env = state.env.copy()
+    for sp, sel in (("up", moved[moved < nu]), ("dn", moved[moved >= nu])):
+        if len(sel):
+            env[sel] = _envelope_rows(prob, p, r[sel], sp)
+    orb = state.orb.copy()
+    up, dn = rows[rows < nu], rows[rows >= nu]
+    orb[up] = h[up] @ p["orb_up_W"] + p["orb_up_b"]
+    orb[dn] = h[dn] @ p["orb_dn_W"] + p["orb_dn_b"]
+    A = _orbital_matrices(prob, orb, env)
+    signs, logdets, Ainv = state.signs.copy(), state.logdets.copy(), np.empty_like(state.Ainv)
+    for d in range(N_DET):
+        (signs[d], logdets[d]), Ainv[d] = woodbury_update(state.signs[d], state.logdets[d], state.A[d],
+                                                          state.Ainv[d], A[d], rows)
+
+    one_el, att, vals = state.one_el.copy(), state.att.copy(), state.vals.copy()
+    if len(rows):
+        one_el[rows], att[rows], vals[rows] = _jastrow_rows(p, h[rows])
+    st = LowRankState(r.copy(), ei, h, env, orb, A, Ainv, signs, logdets, one_el, att, vals)
+    s_det, l_det = logsumexp_signed(logdets, signs)
+    s_j, l_j = _jastrow_readout(prob, p, r, one_el, att, vals)
+    return (s_det * s_j, l_det + l_j), st
+
+
 def mcmc_block(prob, p, r, noise, log_u, width):
     """All-electron Metropolis block (``mcmc.py:38-97``) with externally supplied draws.
 
@@ -922,8 +1087,6 @@ def mcmc_jump_block(prob, p, r, draws, log_u, sigma):
             n_acc += 1
     return r, lp, n_acc, np.array(margins)
 
-
-NO_NEIGHBOUR = 1_000_000  # model/graph_utils.py:14
 
 
 def closest_k(dist, dist_max, k):
@@ -994,3 +1157,53 @@ def mcmc_single_block(prob, p, r, noise, log_u, width, offset=0):
             r, lp = rn, lpn
             n_acc += 1
     return r, lp, n_acc, np.array(margins)
+
+
+def mcmc_low_rank_block(prob, p, r, propose, log_u):
+    """``mcmc_steps_low_rank`` (``mcmc.py:196-275``) for one walker with the state carried between steps:
+    ``propose(s, r)`` returns (r', moved electrons, proposal log ratio); log|psi'| comes from
+    ``logpsi_low_rank_update`` and the state of an accepted proposal replaces the current one.  Returns
+    (r, log_prob, n_accept, margins, changed_max) with changed_max the elementwise maximum over the steps of the
+    proposals' ``changed_counts`` (the move statics the reference accumulates, ``mcmc.py:231-235``)."""
+    (_, l), st = logpsi_with_state(prob, p, r)
+    lp = 2.0 * l
+    n_acc = 0
+    margins = []
+    cmax = np.zeros(3, np.int64)
+    for s in range(len(log_u)):
+        rn, idx, plr = propose(s, r)
+        cmax = np.maximum(cmax, changed_counts(prob, r, rn, idx))
+        (_, ln), stn = logpsi_low_rank_update(prob, p, rn, idx, st)
+        m = plr + (2.0 * ln - lp) - log_u[s]
+        margins.append(m)
+        if m > 0:
+            r, lp, st = rn, 2.0 * ln, stn
+            n_acc += 1
+    return r, lp, n_acc, np.array(margins), cmax
+
+
+def single_electron_low_rank_block(prob, p, r, noise, log_u, width, offset=0):
+    """``mcmc_single_block``'s moves through ``mcmc_low_rank_block``."""
+    n = r.shape[0]
+
+    def propose(s, r):
+        e = (offset + s) % n
+        rn = r.copy()
+        rn[e] = r[e] + noise[s] * width
+        return rn, np.array([e]), 0.0
+
+    return mcmc_low_rank_block(prob, p, r, propose, log_u)
+
+
+def cluster_low_rank_block(prob, p, r, draws, log_u, width, k, radius, random_sweep=False, offset=0):
+    """``mcmc_cluster_block``'s moves through ``mcmc_low_rank_block``; the moved electrons are the center's k closest
+    before the move, NO_NEIGHBOUR-padded (``proposal_cluster_update``, ``mcmc.py:141-143``)."""
+    n = r.shape[0]
+
+    def propose(s, r):
+        center = min(int(draws[s][0] * n), n - 1) if random_sweep else (offset + s) % n
+        idx = closest_k(np.linalg.norm(r - r[center], axis=-1), radius, k)
+        rn, plr = cluster_proposal(r, draws[s], k, radius, width, center)
+        return rn, idx, plr
+
+    return mcmc_low_rank_block(prob, p, r, propose, log_u)

@@ -201,3 +201,84 @@ def test_woodbury_update_matches_recomputation():
         s_ref, l_ref = np.linalg.slogdet(A_new)
         assert s1 == s_ref and abs(l1 - l_ref) < 1e-10
         np.testing.assert_allclose(inv1, np.linalg.inv(A_new), rtol=0, atol=1e-9 * np.abs(np.linalg.inv(A_new)).max())
+
+
+_STATE_FIELDS = ("ei", "h", "env", "orb", "A", "Ainv", "signs", "logdets", "one_el", "att", "vals")
+
+
+def test_low_rank_update_matches_full_evaluation():
+    """log_psi_low_rank_update (model/wave_function.py:249-287) against log_psi_with_state at the moved positions,
+    as tests/test_low_rank.py:29-61 of the reference checks it: electron 3 moved by (2, 0, 0) twice, the updated
+    state carried into the second move, every state field and log|psi| within 1e-12 (determinants and inverses
+    within 1e-9)."""
+    mol, nu, r, p, *_ = case("h10")
+    prob = O.Problem(mol.R, mol.Z, nu)
+    w = r[0].astype(np.float64)
+    (s, l), st = O.logpsi_with_state(prob, p, w)
+    assert (s, l) == O.logpsi(prob, p, w)
+    for _ in range(2):
+        wn = w.copy()
+        wn[3] += [2.0, 0.0, 0.0]
+        (sf, lf), full = O.logpsi_with_state(prob, p, wn)
+        (su, lu), upd = O.logpsi_low_rank_update(prob, p, wn, np.array([3]), st)
+        assert su == sf
+        np.testing.assert_allclose(lu, lf, rtol=1e-12, atol=1e-12)
+        for key in _STATE_FIELDS:
+            tol = 1e-9 if key in ("A", "Ainv", "signs", "logdets") else 1e-12
+            np.testing.assert_allclose(getattr(upd, key), getattr(full, key), rtol=tol, atol=tol, err_msg=key)
+        w, st = wn, upd
+
+
+def test_changed_counts_are_the_recomputed_rows():
+    """The move statics (get_static_input, new_sparse_model.py:414-424): exactly the electrons counted in
+    n_changed_hout may change embedding; the pair counts are their neighbour counts after the move, split by spin;
+    a NO_NEIGHBOUR-padded index list gathers electron n - 1 like an out-of-range JAX gather (a superset)."""
+    mol, nu, r, p, *_ = case("c2h6")
+    prob = O.Problem(mol.R, mol.Z, nu)
+    w = r[0].astype(np.float64)
+    n = mol.n_el
+    h0 = O.embedding_value(prob, p, w)
+    rng = np.random.default_rng(11)
+    for moved in ([0], [n - 1], [2, 9], [4, O.NO_NEIGHBOUR]):
+        wn = w.copy()
+        for i in moved:
+            if i < n:
+                wn[i] += 0.7 * rng.standard_normal(3)
+        aff, req = O.affected_electrons(prob, w, wn, moved)
+        hout, ps, pd = O.changed_counts(prob, w, wn, moved)
+        assert hout == aff.sum() and ps + pd == req.sum()
+        inc = O.in_cutoff_matrix(wn.astype(np.float32), prob.cutoff)
+        np.testing.assert_array_equal(req.sum(1), np.where(aff, inc.sum(1), 0))
+        h1 = O.embedding_value(prob, p, wn)
+        np.testing.assert_allclose(h1[~aff], h0[~aff], rtol=1e-13, atol=1e-13)
+        if O.NO_NEIGHBOUR in moved:
+            unpadded = O.affected_electrons(prob, w, wn, [i for i in moved if i < n])[0]
+            assert np.all(aff >= unpadded) and aff[n - 1]
+
+
+@pytest.mark.parametrize("kind", ["single", "cluster", "cluster_random"])
+def test_low_rank_blocks_match_full_evaluation_blocks(kind):
+    """mcmc_steps_low_rank (mcmc.py:196-275) with the state carried between steps takes the same decisions as the
+    blocks that evaluate every proposal in full: same accepted count and final positions, margins within 1e-9.
+    Cluster moves of k = 4 within radius 1.2 include NO_NEIGHBOUR-padded index lists."""
+    mol, nu, r, p, *_ = case("h10")
+    prob = O.Problem(mol.R, mol.Z, nu)
+    w = r[1].astype(np.float64)
+    rng = np.random.default_rng(13)
+    steps = 10
+    logu = np.log(rng.uniform(size=steps))
+    if kind == "single":
+        noise = rng.standard_normal((steps, 3))
+        a = O.mcmc_single_block(prob, p, w, noise, logu, 0.5, offset=4)
+        b = O.single_electron_low_rank_block(prob, p, w, noise, logu, 0.5, offset=4)
+        assert tuple(b[4]) >= (1, 0, 0)
+    else:
+        k, rs = 4, kind == "cluster_random"
+        draws = np.concatenate([rng.uniform(size=(steps, 1)), rng.standard_normal((steps, 15 * k))], 1)
+        a = O.mcmc_cluster_block(prob, p, w, draws, logu, 0.3, k, 1.2, random_sweep=rs, offset=2)
+        b = O.cluster_low_rank_block(prob, p, w, draws, logu, 0.3, k, 1.2, random_sweep=rs, offset=2)
+    assert a[2] == b[2] and 0 < a[2] < steps
+    np.testing.assert_array_equal(a[0], b[0])
+    fin = np.isfinite(a[3])
+    np.testing.assert_array_equal(fin, np.isfinite(b[3]))
+    np.testing.assert_allclose(b[3][fin], a[3][fin], rtol=0, atol=1e-9)
