@@ -23,6 +23,8 @@
  *                       (each proposal evaluated in full, no low-rank state)
  *   fire_mcmc_jump_block    mcmc.py:164-193 proposal_jump_to_atom (make_mcmc's jump_steps)
  *   fire_mcmc_cluster_block mcmc.py:119-161 proposal_cluster_update (make_mcmc "cluster-update")
+ *   fire_mcmc_low_rank_block  mcmc.py:100-111, 196-275 with model/wave_function.py:226-287
+ *                       log_psi_with_state / log_psi_low_rank_update (the state-carrying single-electron block)
  *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
  *                       (used by the initialiser, new_sparse_model.py:378-379)
  */
@@ -55,9 +57,10 @@ typedef enum {
 #define FIRE_FLAG_TRIPLET_OVERFLOW 8  /* triplet list exceeded its capacity */
 #define FIRE_FLAG_SINGULAR 16         /* an orbital matrix had a zero pivot */
 #define FIRE_FLAG_TIMEOUT 32          /* a bounded wait on a tensor-core completion barrier gave up */
+#define FIRE_FLAG_CHANGED_OVERFLOW 64 /* a low-rank step's changed set exceeded cap_changed */
 /* status[1] = max pairs of any walker seen, status[2] = max e-n neighbours seen,
- * status[3] = max triplets (sum_m deg(m)^2) seen; the host grows capacities from these,
- * like StaticScheduler (static_args.py:62-84). */
+ * status[3] = max triplets (sum_m deg(m)^2) seen, status[4] = max changed set of a low-rank step seen;
+ * the host grows capacities from these, like StaticScheduler (static_args.py:62-84). */
 
 typedef enum {
   FIRE_PREC_FP32 = 0,  /* FP32 SIMT; orbital LU and inverse in double-FP32 (48-bit significand) */
@@ -249,6 +252,31 @@ fire_status fire_mcmc_jump_block(void* stream, const fire_problem* prob, const f
                                  uint64_t seed, uint64_t counter, const void* replay_draws,
                                  const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
                                  void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Workspace of fire_mcmc_low_rank_block for `chunk` walkers per pass and a changed set of at most cap_changed
+ * electrons per walker and step (cap_changed <= 128, else FIRE_ERR_UNSUPPORTED). */
+fire_status fire_low_rank_workspace_size(const fire_problem* prob, int32_t chunk, int32_t cap_changed,
+                                         size_t* bytes);
+
+/* Metropolis block of single-electron moves evaluated by the low-rank update of a cached state:
+ * mcmc_steps_low_rank (mcmc.py:196-275) with proposal_single_electron (mcmc.py:100-111) and
+ * log_psi_with_state / log_psi_low_rank_update (model/wave_function.py:226-287).  Per chunk of walkers the state
+ * comes from one value-path evaluation (log|psi| of r is written to logpsi) and keeps the inverse of every
+ * orbital matrix.  Step s moves electron e = (step_offset + s) mod n; the changed set is e and every electron
+ * within the cutoff of e before or after the move (get_low_rank_pair_indices, model/new_sparse_model.py:439-474).
+ * Their embeddings, raw orbital and Jastrow rows are recomputed, e's ElecInit and envelope rows, and log|psi'|
+ * follows from the determinant lemma det(A') = det(A) det(I + V A^-1[:, S]) with the Jastrow sums over all rows;
+ * an accepted step writes the rows into the state and updates the inverses by the Woodbury identity
+ * (model/utils.py:216-245).  Proposals, draws, acceptance, replay and n_accept as fire_mcmc_single_block.
+ * static_max [7] int32: (n_pairs_same, n_pairs_diff, 0, n_neighbours_en) of the proposals, then the move statics
+ * (n_changed_hout, n_changed_pair_same, n_changed_pair_diff) of get_static_input (model/new_sparse_model.py:414-424).
+ * A changed set larger than cap_changed sets FIRE_FLAG_CHANGED_OVERFLOW (status[4] = the largest set seen) and
+ * rejects that proposal: the caller reruns the block with a larger capacity.  Up to 798 electrons. */
+fire_status fire_mcmc_low_rank_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                     const void* prepared, void* r, void* logpsi, int32_t steps, int32_t step_offset,
+                                     float width, int32_t cap_changed, uint64_t seed, uint64_t counter,
+                                     const void* replay_noise, const void* replay_log_u, int32_t* n_accept,
+                                     int32_t* static_max, void* workspace, size_t workspace_bytes, int32_t* status);
 
 /* Coulomb potential of every walker (hamiltonian.py:15-26): out [B] in the walkers' dtype. */
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r,

@@ -20,6 +20,8 @@ FLAG_NONFINITE = 4
 FLAG_TRIPLET_OVERFLOW = 8
 FLAG_SINGULAR = 16
 FLAG_TIMEOUT = 32
+FLAG_CHANGED_OVERFLOW = 64
+LOW_RANK_MAX_CHANGED = 128  # LR_KMAX: capacity limit of a low-rank step's changed set
 TRIPLETS_STATIC_MAX_WORDS = 4 * 1024 * 1024  # FIRE_TRIPLETS_STATIC_MAX_WORDS
 ERRORS = {1: "invalid argument", 2: "unsupported size", 3: "workspace too small", 4: "CUDA launch failed"}
 
@@ -29,7 +31,7 @@ SYMBOLS = [
     "fire_prepare_params", "fire_neighbors", "fire_triplets", "fire_logpsi", "fire_local_energy",
     "fire_embedding", "fire_mcmc_block", "fire_potential_energy", "fire_profile_enable", "fire_profile_report",
     "fire_gemm_mixed", "fire_triplets_static", "fire_mcmc_single_block", "fire_mcmc_jump_block",
-    "fire_mcmc_cluster_block",
+    "fire_mcmc_cluster_block", "fire_low_rank_workspace_size", "fire_mcmc_low_rank_block",
 ]
 
 
@@ -81,6 +83,9 @@ def load() -> C.CDLL:
         "fire_mcmc_jump_block": ([vp, P, vp, vp, vp, vp, vp, i32, f32, u64, u64, vp, vp, vp, vp, vp, sz, vp], i32),
         "fire_mcmc_cluster_block": ([vp, P, vp, vp, vp, vp, vp, i32, i32, f32, i32, f32, i32, u64, u64, vp, vp, vp, vp,
                                      vp, sz, vp], i32),
+        "fire_low_rank_workspace_size": ([P, i32, i32, C.POINTER(sz)], i32),
+        "fire_mcmc_low_rank_block": ([vp, P, vp, vp, vp, vp, vp, i32, i32, f32, i32, u64, u64, vp, vp, vp, vp, vp, sz,
+                                      vp], i32),
         "fire_potential_energy": ([vp, P, vp, vp, vp, vp], i32),
         "fire_profile_enable": ([i32], i32),
         "fire_profile_report": ([C.c_char_p, sz], i32),

@@ -1057,7 +1057,314 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
       g_nlaunch++;
       k_accept<T><<<c.Wc, 128, 0, s>>>(rr, rn, reinterpret_cast<T*>(logpsi), lpn, n, w0, p->n_walkers, st, seed,
                                       counter, reinterpret_cast<const T*>(logu), n_accept, c.nb.counts, static_max,
-                                      plr);
+                                      plr, nullptr);
+    }
+  }
+  return launch_status(__func__);
+}
+
+// ------------------------------------------------------------------------------ low-rank single-electron block
+// Buffers of the low-rank block beyond the value path's plan of the same chunk (byte offsets into the workspace).
+// The state of a chunk is the value path's own buffers (E5o, B2X, rawx, env, Apl, aX, Xo2, ld, sd and the e-n
+// lists / statics of Nbr) plus `vals` (the attention value rows) and `B` (the transposed inverse of every orbital
+// matrix); the rest is per-step scratch of the proposal.
+struct LrPlan {
+  size_t vals, B;                                        // state
+  size_t S, S_cnt, en_cnt_p, en_idx_p, counts_p, acc;    // int
+  size_t re_p, E5p, HS, B1S, hS, rawU, rawD, coefE, env_p, aS, vS, oS, V, Zb, Qb;  // T
+  size_t Minv, ld_p, sd_p;                               // double
+  size_t total;
+};
+
+LrPlan make_lr_plan(const fire_problem* p, int Wc, int KS) {
+  LrPlan Q;
+  std::memset(&Q, 0, sizeof(Q));
+  const size_t es = elem_size(p);
+  const size_t n = p->n_el, W = Wc, G = W * n, DN = NDET * n, K8 = (size_t)p->n_nuc * NENV_ORB, R = W * KS;
+  size_t o = make_plan(p, Wc, false).total;
+  auto take = [&](size_t& field, size_t count, size_t bytes_per) {
+    o = (o + 255) / 256 * 256;
+    field = o;
+    o += count * bytes_per;
+  };
+  take(Q.vals, G * F, es);
+  take(Q.B, W * NDET * n * (size_t)ainv_ld((int)n), es);
+  take(Q.S, R, 4);
+  take(Q.S_cnt, W, 4);
+  take(Q.en_cnt_p, W, 4);
+  take(Q.en_idx_p, W * p->cap_nuc, 4);
+  take(Q.counts_p, W * 4, 4);
+  take(Q.acc, W, 4);
+  take(Q.re_p, W * 3, es);
+  take(Q.E5p, W * 5 * F, es);
+  take(Q.HS, R * F, es);
+  take(Q.B1S, R * F, es);
+  take(Q.hS, R * F, es);
+  take(Q.rawU, R * DN, es);
+  take(Q.rawD, R * DN, es);
+  take(Q.coefE, NDET * W * K8, es);
+  take(Q.env_p, W * DN, es);
+  take(Q.aS, R * HEADS, es);
+  take(Q.vS, R * F, es);
+  take(Q.oS, R * 2, es);
+  take(Q.V, W * NDET * KS * n, es);
+  take(Q.Zb, W * NDET * n * KS, es);
+  take(Q.Qb, W * NDET * KS * n, es);
+  take(Q.Minv, W * NDET * KS * KS, 8);
+  take(Q.ld_p, W * NDET, 8);
+  take(Q.sd_p, W * NDET, 8);
+  Q.total = (o + 255) / 256 * 256;
+  return Q;
+}
+
+int choose_chunk_lr(const fire_problem* p, size_t ws_bytes, int KS) {
+  const int B = p->n_walkers;
+  if (p->chunk_walkers > 0) {
+    const int c = std::min(B, p->chunk_walkers);
+    return make_lr_plan(p, c, KS).total <= ws_bytes ? c : 0;
+  }
+  int lo = 0, hi = B;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (make_lr_plan(p, mid, KS).total <= ws_bytes) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// the attention readout MLP 512 -> 256 -> 256 -> 2 on the value rows RX [W][512] -> JAx [W][2] (the value
+// path's part of stage_jastrow)
+template <typename T>
+void readout_value(Ctx<T>& c) {
+  const int Wc = c.Wc;
+  auto layer = [&](size_t in, size_t out, const T* Wt, const T* b, int K) {
+    GemmP<T> q = gp0<T>();
+    q.A = c.template buf<T>(in); q.lda = K; q.B = Wt; q.ldb = F; q.bias = b; q.C = c.template buf<T>(out);
+    q.ldc = F; q.M = Wc; q.N = F; q.K = K; q.ld_aux = F;
+    gemm<T, EPI_SILU_X>(c, q);
+  };
+  layer(c.P.RX, c.P.R1X, c.W.w[FIRE_P_ATT_OUT1_W], c.W.w[FIRE_P_ATT_OUT1_B], 2 * F);
+  layer(c.P.R1X, c.P.R2X, c.W.w[FIRE_P_ATT_OUT2_W], c.W.w[FIRE_P_ATT_OUT2_B], F);
+  GemmP<T> g = gp0<T>();
+  g.A = c.template buf<T>(c.P.R2X); g.lda = F; g.B = c.W.w[FIRE_P_ATT_OUT3_W]; g.ldb = 2;
+  g.bias = c.W.w[FIRE_P_ATT_OUT3_B]; g.bias_period = 1; g.C = c.template buf<T>(c.P.JAx); g.ldc = 2; g.M = Wc;
+  g.N = 2; g.K = F;
+  gemm<T, EPI_PLAIN>(c, g);
+}
+
+// State of one chunk: the value path with the inverse kept (Gauss-Jordan instead of the LU), the attention value
+// rows, and log|psi| of the chunk's walkers into logpsi (global walker index; log_psi_with_state,
+// wave_function.py:226-247).
+template <typename T>
+cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi) {
+  setup_ctx(c, false);
+  stage_neighbors(c, false);
+  stage_embedding<T, 0>(c);
+  stage_update<T, 0>(c);
+  stage_orbitals<T, 0>(c);
+  {
+    Prof pr("gauss_jordan", c.s);
+    if constexpr (sizeof(T) == 8)
+      launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(Q.B));
+    else
+      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(Q.B));
+  }
+  stage_jastrow<T, 0>(c);
+  const Planes B2{c.P.B2X, 0, 0}, VL{Q.vals, 0, 0};
+  linear_layer<T>(c, false, B2, VL, c.W.w[PR_V_W_S1], c.W.w[FIRE_P_ATT_V_B], F, F, c.Wc * c.p->n_el, 0, nullptr);
+  AssembleOut o;
+  std::memset(&o, 0, sizeof(o));
+  o.logpsi = logpsi;
+  g_nlaunch++;
+  k_assemble<T, false><<<c.Wc, 256, 3 * c.p->n_el * sizeof(double), c.s>>>(
+      c.p->n_el, c.p->n_up, c.p->n_nuc, c.w0, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
+      c.template buf<double>(c.P.sd), nullptr, nullptr, c.template buf<T>(c.P.JAx), nullptr, nullptr,
+      c.template buf<T>(c.P.JMx), nullptr, nullptr, o, c.status);
+  return cudaPeekAtLastError();
+}
+
+// One low-rank step of the chunk: electron e of every walker moved (proposal in c.P.rn), log|psi'| from the state,
+// accept, and on acceptance the state's rows and the Woodbury update of the inverse.
+template <typename T>
+cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int st, int e, uint64_t seed,
+                    uint64_t counter, const void* logu, int32_t* n_accept, int32_t* static_max) {
+  const fire_problem* p = c.p;
+  const int n = p->n_el, nu = p->n_up, N = p->n_nuc, Wc = c.Wc, DN = NDET * n, rows = Wc * KS;
+  const int K8 = N * NENV_ORB;
+  cudaStream_t s = c.s;
+  T* rn = c.template buf<T>(c.P.rn);
+  T* r_chunk = rr + (size_t)c.w0 * n * 3;
+  int* S = c.template buf<int>(Q.S);
+  int* S_cnt = c.template buf<int>(Q.S_cnt);
+  int* acc = c.template buf<int>(Q.acc);
+  Prof pr("low_rank_step", s);
+  g_nlaunch++;
+  k_lr_select<T><<<Wc, 256, 0, s>>>(r_chunk, rn, n, nu, e, c.R, N, (T)p->cutoff, (T)p->cutoff_1el, c.nb, KS, S,
+                                    S_cnt, c.template buf<T>(Q.re_p), c.template buf<int>(Q.en_cnt_p),
+                                    c.template buf<int>(Q.en_idx_p), c.template buf<int>(Q.counts_p), static_max,
+                                    c.status);
+  // ElecInit of the moved electron (one row per walker), then its GLU / Dense / Dense
+  {
+    Nbr nbe = c.nb;
+    nbe.en_cnt = c.template buf<int>(Q.en_cnt_p);
+    nbe.en_idx = c.template buf<int>(Q.en_idx_p);
+    T* E5a = c.template buf<T>(c.P.E5a);
+    T* Z1 = c.template buf<T>(c.P.Z1);
+    g_nlaunch++;
+    k_elec_init<T, 0><<<Wc, 256, 0, s>>>(c.template buf<T>(Q.re_p), c.R, nbe, c.W, (T)(1.0 / p->cutoff_1el), E5a);
+    GemmP<T> g = gp0<T>();
+    g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_GLU_W]; g.ldb = 2 * F; g.C = Z1; g.ldc = 2 * F;
+    g.M = Wc; g.N = 2 * F; g.K = F;
+    gemm<T, EPI_PLAIN>(c, g);
+    g_nlaunch++;
+    k_glu<T, 0><<<nblk((long)Wc * F), 256, 0, s>>>(Z1, E5a, Wc);
+    g = gp0<T>();
+    g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_DENSE_W]; g.ldb = F; g.C = Z1; g.ldc = F;
+    g.bias = c.W.w[FIRE_P_EI_DENSE_B]; g.bias_period = 1; g.M = Wc; g.N = F; g.K = F;
+    gemm<T, EPI_PLAIN>(c, g);
+    g_nlaunch++;
+    k_silu5<T, 0><<<nblk((long)Wc * F), 256, 0, s>>>(Z1, Wc);
+    g = gp0<T>();
+    g.A = Z1; g.lda = F; g.B = c.W.w[FIRE_P_EI_OUT_W]; g.ldb = 5 * F; g.C = c.template buf<T>(Q.E5p);
+    g.ldc = 5 * F; g.bias = c.W.w[FIRE_P_EI_OUT_B]; g.bias_period = 1; g.M = Wc; g.N = 5 * F; g.K = F;
+    gemm<T, EPI_PLAIN>(c, g);
+  }
+  // messages and update MLP of the changed centers
+  g_nlaunch++;
+  k_lr_contract<T><<<dim3(KS, Wc), 256, 0, s>>>(rn, n, nu, (T)p->cutoff, e, S, S_cnt, KS, c.W,
+                                                c.template buf<T>(c.P.E5o), c.template buf<T>(Q.E5p),
+                                                c.template buf<T>(Q.HS));
+  const Planes HS{Q.HS, 0, 0}, B1S{Q.B1S, 0, 0}, hS{Q.hS, 0, 0};
+  silu_layer<T>(c, false, HS, B1S, c.W.w[PR_UPD1_W_S0], c.W.w[FIRE_P_UPD1_B], F, F, rows, 0, nullptr, nullptr, 1, 0,
+                0);
+  silu_layer<T>(c, false, B1S, hS, c.W.w[FIRE_P_UPD2_W], c.W.w[FIRE_P_UPD2_B], F, F, rows, 0, nullptr, nullptr, 1, 0,
+                0);
+  // raw orbital rows of the changed centers (both spins' contractions, then each row's own)
+  for (int sp = 0; sp < 2; ++sp) {
+    GemmP<T> g = gp0<T>();
+    g.A = c.template buf<T>(Q.hS); g.lda = F; g.B = c.W.w[sp == 0 ? PR_ORB_UP_W_S1 : PR_ORB_DN_W_S1]; g.ldb = DN;
+    g.bias = c.W.w[sp == 0 ? FIRE_P_ORB_UP_B : FIRE_P_ORB_DN_B]; g.bias_period = 1;
+    g.C = c.template buf<T>(sp == 0 ? Q.rawU : Q.rawD); g.ldc = DN; g.M = rows; g.N = DN; g.K = F;
+    gemm<T, EPI_PLAIN>(c, g);
+  }
+  g_nlaunch++;
+  k_lr_orb<T><<<dim3(KS, Wc), 256, 0, s>>>(S, S_cnt, KS, nu, DN, c.template buf<T>(Q.rawU),
+                                           c.template buf<T>(Q.rawD));
+  // envelope row of the moved electron at its new position
+  {
+    const bool up = e < nu;
+    T* coef = c.template buf<T>(Q.coefE);
+    g_nlaunch++;
+    k_env_coef<T, 1><<<nblk((long)Wc * K8), 256, 0, s>>>(rn, c.R, c.W.w[up ? PR_ENV_UP_SP : PR_ENV_DN_SP], n, 1, e,
+                                                         N, Wc, coef);
+    for (int d = 0; d < NDET; ++d) {
+      GemmP<T> g = gp0<T>();
+      g.A = coef + (size_t)d * Wc * K8; g.lda = K8;
+      g.B = c.W.w[up ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (size_t)d * K8 * n; g.ldb = n;
+      g.C = c.template buf<T>(Q.env_p) + (size_t)d * n; g.ldc = DN; g.M = Wc; g.N = n; g.K = K8;
+      g.n_el = 1; g.env_ns = 1; g.env_soff = 0; g.env_nv = 1;
+      gemm<T, EPI_ENV>(c, g);
+    }
+  }
+  // determinant lemma
+  {
+    const size_t smem = sizeof(double) * (size_t)KS * KS + 2 * sizeof(T) * (size_t)KS * 33;
+    cudaFuncSetAttribute(k_lr_det<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    g_nlaunch++;
+    k_lr_det<T><<<dim3(NDET, Wc), 256, smem, s>>>(
+        S, S_cnt, KS, n, e, c.template buf<T>(Q.rawU), c.template buf<T>(c.P.env), c.template buf<T>(Q.env_p),
+        c.template buf<T>(c.P.Apl), c.template buf<T>(Q.B), c.template buf<double>(c.P.ld),
+        c.template buf<double>(c.P.sd), c.template buf<T>(Q.V), c.template buf<double>(Q.Minv),
+        c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p));
+  }
+  // Jastrow rows of the changed centers, the sums with the state's other rows, the readout
+  {
+    g_nlaunch++;
+    k_narrow<T, HEADS, 1, false><<<rows, 256, 0, s>>>(c.template buf<T>(Q.hS), nullptr, nullptr, c.nb, c.L,
+                                                      c.W.w[PR_QK_W_S1], c.W.w[PR_QK_B], nullptr, nullptr,
+                                                      c.template buf<T>(Q.aS), nullptr, nullptr, c.status, nullptr,
+                                                      nullptr);
+    const Planes vS{Q.vS, 0, 0};
+    linear_layer<T>(c, false, hS, vS, c.W.w[PR_V_W_S1], c.W.w[FIRE_P_ATT_V_B], F, F, rows, 0, nullptr);
+    silu_layer<T>(c, false, hS, HS, c.W.w[PR_JMLP1_W_S1], c.W.w[FIRE_P_JMLP1_B], F, F, rows, 0, nullptr, nullptr, 1,
+                  0, 0);
+    silu_layer<T>(c, false, HS, B1S, c.W.w[FIRE_P_JMLP2_W], c.W.w[FIRE_P_JMLP2_B], F, F, rows, 0, nullptr, nullptr,
+                  1, 0, 0);
+    g_nlaunch++;
+    k_narrow<T, 2, 0, false><<<rows, 256, 0, s>>>(c.template buf<T>(Q.B1S), nullptr, nullptr, c.nb, c.L,
+                                                  c.W.w[FIRE_P_JMLP3_W], c.W.w[FIRE_P_JMLP3_B],
+                                                  c.W.w[FIRE_P_MLP_SCALE], c.W.w[PR_SCALARS] + 1,
+                                                  c.template buf<T>(Q.oS), nullptr, nullptr, c.status, nullptr,
+                                                  nullptr);
+    g_nlaunch++;
+    k_lr_jsums<T><<<Wc, 256, 0, s>>>(n, nu, S, S_cnt, KS, c.template buf<T>(c.P.aX), c.template buf<T>(Q.vals),
+                                     c.template buf<T>(c.P.Xo2), c.template buf<T>(Q.aS), c.template buf<T>(Q.vS),
+                                     c.template buf<T>(Q.oS), c.template buf<T>(c.P.Ax), c.template buf<T>(c.P.JMx));
+    g_nlaunch++;
+    k_readout_in<T, false><<<Wc, 512, 0, s>>>(n, c.template buf<T>(c.P.Ax), nullptr, nullptr,
+                                              c.template buf<T>(c.P.RX), nullptr, nullptr);
+    readout_value<T>(c);
+  }
+  // log|psi'| and the Metropolis test
+  T* lpn = c.template buf<T>(c.P.lpn);
+  AssembleOut o;
+  std::memset(&o, 0, sizeof(o));
+  o.logpsi = lpn;
+  g_nlaunch++;
+  k_assemble<T, false><<<Wc, 256, 3 * n * sizeof(double), s>>>(
+      n, nu, N, 0, rn, c.R, c.Z, c.W, c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p), nullptr,
+      nullptr, c.template buf<T>(c.P.JAx), nullptr, nullptr, c.template buf<T>(c.P.JMx), nullptr, nullptr, o,
+      c.status);
+  g_nlaunch++;
+  k_accept<T><<<Wc, 128, 0, s>>>(rr, rn, reinterpret_cast<T*>(logpsi), lpn, n, c.w0, p->n_walkers, st, seed, counter,
+                                 reinterpret_cast<const T*>(logu), n_accept, c.template buf<int>(Q.counts_p),
+                                 static_max, nullptr, acc);
+  // accepted walkers: rows into the state, Woodbury update of the inverse
+  g_nlaunch++;
+  k_lr_commit<T><<<dim3(KS + 1, Wc), 256, 0, s>>>(
+      acc, S, S_cnt, KS, n, e, c.template buf<T>(Q.hS), c.template buf<T>(Q.rawU), c.template buf<T>(Q.env_p),
+      c.template buf<T>(Q.aS), c.template buf<T>(Q.vS), c.template buf<T>(Q.oS), c.template buf<T>(Q.E5p),
+      c.template buf<int>(Q.en_cnt_p), c.template buf<int>(Q.en_idx_p), c.template buf<int>(Q.counts_p),
+      c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p), c.template buf<T>(c.P.B2X),
+      c.template buf<T>(c.P.rawx), c.template buf<T>(c.P.env), c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.aX),
+      c.template buf<T>(Q.vals), c.template buf<T>(c.P.Xo2), c.template buf<T>(c.P.E5o), c.nb,
+      c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd));
+  const dim3 wg((n + 31) / 32, NDET, Wc);
+  g_nlaunch += 3;
+  k_lr_wb_z<T><<<wg, 256, 0, s>>>(acc, S_cnt, KS, n, c.template buf<T>(Q.B), c.template buf<T>(Q.V),
+                                  c.template buf<T>(Q.Zb));
+  k_lr_wb_q<T><<<wg, 256, 0, s>>>(acc, S, S_cnt, KS, n, c.template buf<T>(Q.B), c.template buf<double>(Q.Minv),
+                                  c.template buf<T>(Q.Qb));
+  k_lr_wb_apply<T><<<wg, 256, 0, s>>>(acc, S_cnt, KS, n, c.template buf<T>(Q.B), c.template buf<T>(Q.Zb),
+                                      c.template buf<T>(Q.Qb));
+  return cudaPeekAtLastError();
+}
+
+// Low-rank single-electron block (mcmc_steps_low_rank with proposal_single_electron): per chunk the state from one
+// value-path evaluation, then every step from the state.
+template <typename T>
+fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
+                        void* r, void* logpsi, int steps, int offset, float width, int KS, uint64_t seed,
+                        uint64_t counter, const void* noise, const void* logu, int32_t* n_accept,
+                        int32_t* static_max, void* ws, size_t wsb, int32_t* status) {
+  const int Wc = choose_chunk_lr(p, wsb, KS);
+  if (Wc <= 0) return FIRE_ERR_WORKSPACE;
+  Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
+  const LrPlan Q = make_lr_plan(p, Wc, KS);
+  T* rr = reinterpret_cast<T*>(r);
+  const int n = p->n_el;
+  for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {
+    c.w0 = w0;
+    c.Wc = std::min(Wc, p->n_walkers - w0);
+    c.r = rr + (size_t)w0 * n * 3;
+    if (chunk_state<T>(c, Q, logpsi) != cudaSuccess) return launch_status("low-rank state");
+    for (int st = 0; st < steps; ++st) {
+      g_nlaunch++;
+      k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), n, w0,
+                                               p->n_walkers, st, offset, (T)width, seed, counter,
+                                               reinterpret_cast<const T*>(noise));
+      const int e = (int)(((long)offset + st) % n);
+      if (lr_step<T>(c, Q, KS, rr, logpsi, st, e, seed, counter, logu, n_accept, static_max) != cudaSuccess)
+        return launch_status("low-rank step");
     }
   }
   return launch_status(__func__);
@@ -1310,6 +1617,33 @@ fire_status fire_mcmc_jump_block(void* stream, const fire_problem* prob, const f
                             replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
   return run_mcmc<float>(prob, s, R, Z, prepared, r, logpsi, steps, sigma, seed, counter, replay_draws, replay_log_u,
                          n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
+}
+
+fire_status fire_low_rank_workspace_size(const fire_problem* prob, int32_t chunk, int32_t cap_changed,
+                                         size_t* bytes) {
+  if (!valid(prob) || !bytes || chunk < 1 || cap_changed < 1) return FIRE_ERR_INVALID;
+  if (cap_changed > LR_KMAX) return FIRE_ERR_UNSUPPORTED;
+  *bytes = make_lr_plan(prob, std::min(chunk, prob->n_walkers), std::min<int>(cap_changed, prob->n_el)).total;
+  return FIRE_OK;
+}
+
+fire_status fire_mcmc_low_rank_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                     const void* prepared, void* r, void* logpsi, int32_t steps, int32_t step_offset,
+                                     float width, int32_t cap_changed, uint64_t seed, uint64_t counter,
+                                     const void* replay_noise, const void* replay_log_u, int32_t* n_accept,
+                                     int32_t* static_max, void* workspace, size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || step_offset < 0 ||
+      cap_changed < 1)
+    return FIRE_ERR_INVALID;
+  if ((replay_noise == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL || cap_changed > LR_KMAX) return FIRE_ERR_UNSUPPORTED;
+  const int KS = std::min<int>(cap_changed, prob->n_el);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_mcmc_lr<double>(prob, s, R, Z, prepared, r, logpsi, steps, step_offset, width, KS, seed, counter,
+                               replay_noise, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
+  return run_mcmc_lr<float>(prob, s, R, Z, prepared, r, logpsi, steps, step_offset, width, KS, seed, counter,
+                            replay_noise, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
 }
 
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r, const float* R,

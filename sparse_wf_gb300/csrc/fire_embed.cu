@@ -436,6 +436,108 @@ __global__ void __launch_bounds__(256) k_edge_contract(const T* __restrict__ r, 
   }
 }
 
+// Low-rank step, value path (NewSparseEmbedding.low_rank_update, new_sparse_model.py:553-629): one CTA (256
+// threads, thread = feature) per changed center c = S[w][slot] of walker w.  Its neighbours are taken in the proposed
+// configuration rn, ascending like the pair list, and the messages are those of k_edge_contract; the ElecInit rows
+// (h0 | ct_same | ct_diff | nb_same | nb_diff) come from the state E5 [W][n][5F] except for the moved electron e,
+// whose row is E5p [W][5F].  Output HS [W][KS][F] = h0[c] + sum of the messages (before the update MLP).
+template <typename T>
+__global__ void __launch_bounds__(256) k_lr_contract(const T* __restrict__ rn, int n, int n_up, T cutoff, int e,
+                                                     const int* __restrict__ S, const int* __restrict__ S_cnt, int KS,
+                                                     Weights<T> W, const T* __restrict__ E5, const T* __restrict__ E5p,
+                                                     T* __restrict__ HS) {
+  __shared__ T sB[EB][F1];
+  __shared__ T sS[EB][4];
+  __shared__ int sj[EB];
+  __shared__ FLv<T, 0> wS[8][F0];
+  __shared__ FLv<T, 0> wE[8][NENV_EE];
+  __shared__ int snb[ELOC_MAX_EL];
+  __shared__ int wcnt[8];
+  const int slot = blockIdx.x, w = blockIdx.y, f = threadIdx.x, lane = f & 31, wid = f >> 5;
+  if (slot >= min(S_cnt[w], KS)) return;
+  const int c = S[(size_t)w * KS + slot];
+  const T* rw = rn + (size_t)w * n * 3;
+  const T rx = rw[3 * c], ry = rw[3 * c + 1], rz = rw[3 * c + 2];
+  // neighbours of c after the move, ascending: 256 candidates per pass, compacted across the block
+  const unsigned lt = (1u << lane) - 1u;
+  int deg = 0;
+  for (int j0 = 0; j0 < n; j0 += 256) {
+    const int j = j0 + f;
+    bool in = false;
+    if (j < n && j != c) in = exact_dist(rx, ry, rz, rw[3 * j], rw[3 * j + 1], rw[3 * j + 2]) < cutoff;
+    const unsigned m = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) wcnt[wid] = __popc(m);
+    __syncthreads();
+    int off = deg, tot = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      off += q < wid ? wcnt[q] : 0;
+      tot += wcnt[q];
+    }
+    if (in) snb[off + __popc(m & lt)] = j;
+    deg += tot;
+    __syncthreads();
+  }
+  const bool si = c < n_up;
+  const T inv_c = T(1) / W.w[PR_SCALARS][0];
+  T wg[2][F1], we[2][4], be[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const T* Wg = W.w[s == 0 ? FIRE_P_EESAME_GAMMA_W : FIRE_P_EEDIFF_GAMMA_W];
+    const T* We = W.w[s == 0 ? FIRE_P_EESAME_EDGE_W : FIRE_P_EEDIFF_EDGE_W];
+#pragma unroll
+    for (int q = 0; q < F1; ++q) wg[s][q] = Wg[q * F + f];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) we[s][q] = We[q * F + f];
+    be[s] = W.w[s == 0 ? FIRE_P_EESAME_EDGE_B : FIRE_P_EEDIFF_EDGE_B][f];
+  }
+  const T* ec = c == e ? E5p + (size_t)w * 5 * F : E5 + ((size_t)w * n + c) * 5 * F;
+  const T h0 = ec[f], cts = ec[F + f], ctd = ec[2 * F + f];
+  T ax = T(0);
+  for (int k0 = 0; k0 < deg; k0 += EB) {
+    const int nbe = min(EB, deg - k0);
+    for (int q = wid; q < nbe; q += 8) {
+      const int j = snb[k0 + q];
+      const T diff[3] = {rx - rw[3 * j], ry - rw[3 * j + 1], rz - rw[3 * j + 2]};
+      const bool same = (j < n_up) == si;
+      if (same)
+        edge_filter_warp<T, 0, NENV_EE>(diff, W.w[FIRE_P_EESAME_KERNEL], W.w[FIRE_P_EESAME_BIAS],
+                                        W.w[PR_EESAME_INVSCALE], W.w[FIRE_P_EESAME_DIR_W], W.w[FIRE_P_EESAME_DIR_B],
+                                        W.w[FIRE_P_EESAME_ENV_W], inv_c, wS[wid], wE[wid], sB[q], sS[q]);
+      else
+        edge_filter_warp<T, 0, NENV_EE>(diff, W.w[FIRE_P_EEDIFF_KERNEL], W.w[FIRE_P_EEDIFF_BIAS],
+                                        W.w[PR_EEDIFF_INVSCALE], W.w[FIRE_P_EEDIFF_DIR_W], W.w[FIRE_P_EEDIFF_DIR_B],
+                                        W.w[FIRE_P_EEDIFF_ENV_W], inv_c, wS[wid], wE[wid], sB[q], sS[q]);
+      if (lane == 0) sj[q] = same ? j : -1 - j;
+    }
+    __syncthreads();
+    for (int q = 0; q < nbe; ++q) {
+      const int code = sj[q];
+      const bool same = code >= 0;
+      const int j = same ? code : -1 - code;
+      const int s = same ? 0 : 1;
+      T G = T(0), E = T(0);
+#pragma unroll
+      for (int u = 0; u < F1; ++u) G += wg[s][u] * sB[q][u];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) E += we[s][u] * sS[q][u];
+      E += be[s];
+      const T* ej = j == e ? E5p + (size_t)w * 5 * F : E5 + ((size_t)w * n + j) * 5 * F;
+      const T u = E + ((same ? cts : ctd) + ej[(same ? 3 : 4) * F + f]);
+      T y, d1, d2;
+      silu3(u, y, d1, d2);
+      ax += G * y;
+    }
+    __syncthreads();
+  }
+  HS[((size_t)w * KS + slot) * F + f] = h0 + ax;
+}
+
+template __global__ void k_lr_contract<float>(const float*, int, int, float, int, const int*, const int*, int,
+                                              Weights<float>, const float*, const float*, float*);
+template __global__ void k_lr_contract<double>(const double*, int, int, double, int, const int*, const int*, int,
+                                               Weights<double>, const double*, const double*, double*);
+
 #define FIRE_INST_EMBED(T, NT)                                                                              \
   template __global__ void k_elec_init<T, NT>(const T*, const float*, Nbr, Weights<T>, T, T*);            \
   template __global__ void k_glu<T, NT>(const T*, T*, int);                                                 \

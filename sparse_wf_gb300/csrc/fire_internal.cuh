@@ -63,6 +63,9 @@ __host__ __device__ constexpr int dl_smem_elems(int chi) { return DL_STAGES * dl
 // Cluster proposals: at most CLUSTER_KMAX electrons per cluster, CLUSTER_TRIALS draws per step
 // (proposal_cluster_update, mcmc.py:119-161).
 constexpr int CLUSTER_KMAX = 16, CLUSTER_TRIALS = 5;
+// Low-rank single-electron steps: at most LR_KMAX electrons in a step's changed set (the moved electron and its
+// neighbours before and after the move); the k x k determinant-lemma matrix is eliminated in shared memory.
+constexpr int LR_KMAX = 128;
 // Largest electron count of the local-energy and value paths: the double-FP32 / FP64 elimination keeps two n x 17 panel buffers
 // of eight-byte elements (plus ~2.5 KB) in shared memory, 288 n + 2496 bytes within the 227 KB per CTA.
 constexpr int ELOC_MAX_EL = 798;

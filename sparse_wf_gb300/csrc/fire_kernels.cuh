@@ -27,6 +27,9 @@ template <typename T, int NT>
 __global__ void k_silu5(T* Z, int G);
 template <typename T, int NT>
 __global__ void k_edge_contract(const T* r, Nbr nb, Layout L, Weights<T> W, const T* E5o, T* X, T* Lp, T* Jp);
+template <typename T>
+__global__ void k_lr_contract(const T* rn, int n, int n_up, T cutoff, int e, const int* S, const int* S_cnt, int KS,
+                              Weights<T> W, const T* E5, const T* E5p, T* HS);
 
 // fire_det.cu
 template <typename T, int NV>
@@ -73,7 +76,7 @@ __global__ void k_propose_single(const T* r, T* rn, int n, int w0, int B, int st
 template <typename T>
 __global__ void k_accept(T* r, const T* rn, T* logpsi, const T* logpsi_new, int n, int w0, int B, int step,
                          uint64_t seed, uint64_t counter, const T* replay_log_u, int32_t* n_accept, const int* counts,
-                         int32_t* static_max, const T* plr);
+                         int32_t* static_max, const T* plr, int32_t* acc_out);
 template <typename T>
 __global__ void k_propose_cluster(const T* r, T* rn, T* plr, int n, int w0, int B, int step, int offset, int k,
                                   T radius, T width, int random_sweep, uint64_t seed, uint64_t counter,
@@ -81,6 +84,34 @@ __global__ void k_propose_cluster(const T* r, T* rn, T* plr, int n, int w0, int 
 template <typename T>
 __global__ void k_propose_jump(const T* r, T* rn, T* plr, int n, int w0, int B, int step, const float* R,
                                const float* Z, int N, T sigma, uint64_t seed, uint64_t counter, const T* replay);
+
+// fire_lowrank.cu
+template <typename T>
+__global__ void k_lr_select(const T* r, const T* rn, int n, int n_up, int e, const float* R, int N, T cutoff,
+                            T cutoff_1el, Nbr nb, int KS, int* S, int* S_cnt, T* re_p, int* en_cnt_p, int* en_idx_p,
+                            int* counts_p, int32_t* static_max, int32_t* status);
+template <typename T>
+__global__ void k_lr_orb(const int* S, const int* S_cnt, int KS, int n_up, int DN, T* rawU, const T* rawD);
+template <typename T>
+__global__ void k_lr_det(const int* S, const int* S_cnt, int KS, int n, int e, const T* rawS, const T* env,
+                         const T* env_p, const T* Apl, const T* B, const double* ld, const double* sd, T* V,
+                         double* Minv, double* ld_p, double* sd_p);
+template <typename T>
+__global__ void k_lr_jsums(int n, int n_up, const int* S, const int* S_cnt, int KS, const T* aX, const T* vals,
+                           const T* Xo, const T* aS, const T* vS, const T* oS, T* Ax, T* JM);
+template <typename T>
+__global__ void k_lr_commit(const int* accf, const int* S, const int* S_cnt, int KS, int n, int e, const T* hS,
+                            const T* rawS, const T* env_p, const T* aS, const T* vS, const T* oS, const T* E5p,
+                            const int* en_cnt_p, const int* en_idx_p, const int* counts_p, const double* ld_p,
+                            const double* sd_p, T* h, T* rawx, T* env, T* Apl, T* aX, T* vals, T* Xo, T* E5o, Nbr nb,
+                            double* ld, double* sd);
+template <typename T>
+__global__ void k_lr_wb_z(const int* accf, const int* S_cnt, int KS, int n, const T* B, const T* V, T* Zb);
+template <typename T>
+__global__ void k_lr_wb_q(const int* accf, const int* S, const int* S_cnt, int KS, int n, const T* B,
+                          const double* Minv, T* Qb);
+template <typename T>
+__global__ void k_lr_wb_apply(const int* accf, const int* S_cnt, int KS, int n, T* B, const T* Zb, const T* Qb);
 
 // fire_tc.cu (host launchers)
 cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __nv_bfloat16* lo, cudaStream_t s);

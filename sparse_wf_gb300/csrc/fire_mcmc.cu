@@ -305,11 +305,13 @@ __global__ void k_propose_cluster(const T* __restrict__ r, T* __restrict__ rn, T
 // Accept if 2 (logpsi_new - logpsi_old) > log u (mcmc.py:68-73); one CTA per walker.
 // r, logpsi: whole batch (global walker index); rn, logpsi_new, counts: this chunk (local index).
 // plr (may be null): the proposals' log ratios log(q(r_old) / q(r_new)), added to the test (mcmc.py:238).
+// acc_out (may be null): the decision per walker of the chunk (1 accepted, 0 rejected).
 template <typename T>
 __global__ void k_accept(T* __restrict__ r, const T* __restrict__ rn, T* __restrict__ logpsi,
                          const T* __restrict__ logpsi_new, int n, int w0, int B, int step, uint64_t seed,
                          uint64_t counter, const T* __restrict__ replay_log_u, int32_t* __restrict__ n_accept,
-                         const int* __restrict__ counts, int32_t* __restrict__ static_max, const T* __restrict__ plr) {
+                         const int* __restrict__ counts, int32_t* __restrict__ static_max, const T* __restrict__ plr,
+                         int32_t* __restrict__ acc_out) {
   const int w = blockIdx.x;
   const long gw = w0 + w;
   __shared__ int acc_s;
@@ -325,6 +327,7 @@ __global__ void k_accept(T* __restrict__ r, const T* __restrict__ rn, T* __restr
     const double ratio = 2.0 * ((double)logpsi_new[w] - (double)logpsi[gw]) + (plr ? (double)plr[w] : 0.0);
     const int a = ratio > logu ? 1 : 0;
     acc_s = a;
+    if (acc_out) acc_out[w] = a;
     if (a) logpsi[gw] = logpsi_new[w];
     if (n_accept) n_accept[gw] += a;
     if (static_max && counts) {
@@ -356,9 +359,9 @@ template __global__ void k_propose_cluster<float>(const float*, float*, float*, 
 template __global__ void k_propose_cluster<double>(const double*, double*, double*, int, int, int, int, int, int,
                                                    double, double, int, uint64_t, uint64_t, const double*);
 template __global__ void k_accept<float>(float*, const float*, float*, const float*, int, int, int, int, uint64_t,
-                                         uint64_t, const float*, int32_t*, const int*, int32_t*, const float*);
+                                         uint64_t, const float*, int32_t*, const int*, int32_t*, const float*, int32_t*);
 template __global__ void k_accept<double>(double*, const double*, double*, const double*, int, int, int, int,
                                           uint64_t, uint64_t, const double*, int32_t*, const int*, int32_t*,
-                                          const double*);
+                                          const double*, int32_t*);
 
 }  // namespace fire

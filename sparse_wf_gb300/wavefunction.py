@@ -102,6 +102,7 @@ class FireWaveFunction:
         self.Z_dev = torch.from_numpy(self.Z.astype(np.float32)).to(self.device)
         self._ws: Optional[torch.Tensor] = None
         self._status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=self.device)
+        self._lr_cap = 0  # changed-set capacity of the last low-rank block (grown on overflow, like the statics)
         _lib.load()
 
     # ------------------------------------------------------------------ plumbing
@@ -119,11 +120,16 @@ class FireWaveFunction:
                             self.cutoff_1el, max(1, int(cap_p)), max(1, int(cap_n)), _lib.PREC[self.precision],
                             self.chunk_walkers)
 
-    def _workspace(self, prob: _lib.Problem) -> torch.Tensor:
+    def _workspace(self, prob: _lib.Problem, cap_changed: int = 0) -> torch.Tensor:
+        """Workspace of the local-energy and value paths, or (cap_changed > 0) of the low-rank block."""
         lib = _lib.load()
         nbytes = C.c_size_t()
         chunk = self.chunk_walkers if self.chunk_walkers > 0 else prob.n_walkers
-        _lib.check(lib.fire_workspace_size(C.byref(prob), chunk, C.byref(nbytes)), "fire_workspace_size")
+        if cap_changed > 0:
+            _lib.check(lib.fire_low_rank_workspace_size(C.byref(prob), chunk, int(cap_changed), C.byref(nbytes)),
+                       "fire_low_rank_workspace_size")
+        else:
+            _lib.check(lib.fire_workspace_size(C.byref(prob), chunk, C.byref(nbytes)), "fire_workspace_size")
         need = int(nbytes.value)
         if self._ws is None or self._ws.numel() < need:
             self._ws = None
@@ -142,6 +148,14 @@ class FireWaveFunction:
     def _read_status(self) -> np.ndarray:
         return self._status.cpu().numpy()
 
+    def _grown(self, st: np.ndarray, static: StaticArgs) -> StaticArgs:
+        """Capacities after a pair or e-n overflow: the largest counts the device saw, padded by 10 %."""
+        pairs = max(int(st[1]), static.n_pairs)
+        nucs = max(int(st[2]), static.n_neighbours_en)
+        half = (pairs + 1) // 2
+        static = StaticArgs(half, pairs - half, max(static.n_triplets, int(st[3])), nucs)
+        return static.round_with_padding(1.1, self.n_electrons, self.n_up, self.n_nuclei)
+
     def _run(self, fn, static: StaticArgs, n_walkers: int, retries: int = 4):
         """Runs fn(problem, workspace) with overflow-driven capacity growth; returns the static used."""
         for _ in range(retries):
@@ -151,11 +165,7 @@ class FireWaveFunction:
             st = self._read_status()
             flags = int(st[0])
             if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
-                pairs = max(int(st[1]), static.n_pairs)
-                nucs = max(int(st[2]), static.n_neighbours_en)
-                half = (pairs + 1) // 2
-                static = StaticArgs(half, pairs - half, max(static.n_triplets, int(st[3])), nucs)
-                static = static.round_with_padding(1.1, self.n_electrons, self.n_up, self.n_nuclei)
+                static = self._grown(st, static)
                 continue
             if flags & _lib.FLAG_NONFINITE:
                 pass  # NaNs propagate to the caller like the reference (train.py:263-264)
@@ -373,6 +383,71 @@ class FireWaveFunction:
         self._run(fn, static, B)
         sm = smax.cpu().numpy()
         return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
+
+    def mcmc_low_rank_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
+                            steps: int, width: float, step_offset: int = 0, seed: int = 0, counter: int = 0,
+                            replay_noise=None, replay_log_u=None, cap_changed: Optional[int] = None):
+        """In-place single-electron Metropolis block evaluated by the low-rank update of a cached state
+        (``mcmc_steps_low_rank`` with ``proposal_single_electron`` and ``log_psi_with_state`` /
+        ``log_psi_low_rank_update``, ``mcmc.py:100-111, 196-275``, ``wave_function.py:226-287``): the proposals,
+        draws and acceptance of ``mcmc_single_block``, with log|psi'| from the walker's state (changed rows, the
+        determinant lemma and a Woodbury update of the inverses) instead of a full evaluation.  logpsi receives
+        log|psi| of the walkers at the start (from their state) and follows the accepted moves.  cap_changed bounds
+        the changed set of a step (at most 128); an overflow reruns the block with the set the device saw, and the
+        capacity is kept for the next call.  Returns (n_accept per walker, static_max, (n_changed_hout,
+        n_changed_pair_same, n_changed_pair_diff)) with the maxima over steps and walkers."""
+        p = self._params(params)
+        r = electrons
+        assert r.is_contiguous() and r.dtype == self.dtype
+        B, n = r.shape[0], self.n_electrons
+        n_acc = torch.zeros(B, dtype=torch.int32, device=self.device)
+        smax = torch.zeros(7, dtype=torch.int32, device=self.device)
+        noise = None
+        if replay_noise is not None:
+            noise = torch.as_tensor(np.asarray(replay_noise)).to(self.device, self.dtype).reshape(steps, B, 3).contiguous()
+        logu = None if replay_log_u is None else torch.as_tensor(replay_log_u).to(self.device, self.dtype).contiguous()
+        r0 = r.clone()
+        lp0 = logpsi.clone()
+        limit = min(n, _lib.LOW_RANK_MAX_CHANGED)
+        if cap_changed is None:
+            # e and its neighbours before and after the move: about twice the mean degree, at least 16
+            cap_changed = self._lr_cap or max(16, 2 * static.n_pairs // max(1, n) + 1)
+        cap = min(int(cap_changed), limit)
+        lib = _lib.load()
+        for _ in range(6):
+            self._status.zero_()
+            r.copy_(r0)
+            logpsi.copy_(lp0)
+            n_acc.zero_()
+            smax.zero_()
+            prob = self._problem(B, static)
+            ws = self._workspace(prob, cap)
+            _lib.check(lib.fire_mcmc_low_rank_block(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(logpsi.data_ptr()),
+                int(steps), int(step_offset), float(width), int(cap), C.c_uint64(seed), C.c_uint64(counter),
+                C.c_void_p(noise.data_ptr()) if noise is not None else None,
+                C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_mcmc_low_rank_block")
+            st = self._read_status()
+            flags = int(st[0])
+            if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
+                static = self._grown(st, static)
+                continue
+            if flags & _lib.FLAG_CHANGED_OVERFLOW:
+                need = int(st[4])
+                if need > limit:
+                    raise RuntimeError(f"a changed set of {need} electrons exceeds the low-rank block's limit of "
+                                       f"{limit}; use mcmc_single_block")
+                cap = min(limit, max(need, int(need * 1.1) + 1))
+                continue
+            break
+        else:
+            raise RuntimeError("low-rank capacities did not converge")
+        self._lr_cap = cap
+        sm = smax.cpu().numpy()
+        return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3])), (int(sm[4]), int(sm[5]), int(sm[6]))
 
     def mcmc_jump_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
                         steps: int, sigma: float = 2.0, seed: int = 0, counter: int = 0, replay_draws=None,

@@ -1,0 +1,107 @@
+"""Parity of the low-rank single-electron block (fire_mcmc_low_rank_block: mcmc_steps_low_rank with the state-carrying
+log_psi_low_rank_update, mcmc.py:196-275, model/wave_function.py:226-287) with the oracle's state-carrying block and
+with the device's full-evaluation block, on replayed draws.
+
+The whole module is skipped until these kernels have had their first run on a GB300: they are compiled and their
+index arithmetic was checked by reading, but not yet executed."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import case
+from oracle import fire_oracle as O
+from sparse_wf_gb300.wavefunction import FireWaveFunction, StaticArgs
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skip(reason="low-rank kernels not yet run on a GPU")]
+
+
+def _setup(name, precision):
+    mol, nu, r, p, _, _ = case(name)
+    wf = FireWaveFunction(mol, precision=precision)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    rr = torch.from_numpy(r).to("cuda", dt).contiguous()
+    s = wf.get_static_input(rr)
+    static = StaticArgs(s.n_pairs_same, s.n_pairs_diff, s.n_triplets, s.n_neighbours_en)
+    return wf, mol, nu, r, p, rr, static
+
+
+def _draws(B, steps, seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((steps, B, 3)), np.log(rng.uniform(size=(steps, B)))
+
+
+@pytest.mark.parametrize("name", ["h10", "c2h6"])
+def test_low_rank_block_replay_matches_oracle(cuda_lib, name):
+    """FP64 build: the decisions of the oracle's state-carrying block (mcmc_low_rank_block) wherever its Metropolis
+    margin is clear of rounding (|margin| > 1e-6), the final positions (1e-12), log|psi| carried by the state
+    (1e-8 relative) and the move statics (n_changed_hout, n_changed_pair_same, n_changed_pair_diff) maximised over
+    the walkers."""
+    wf, mol, nu, r, p, rr, static = _setup(name, "fp64")
+    B, n = r.shape[0], mol.n_el
+    steps, off, width = n + 3, 1, 0.4
+    noise, logu = _draws(B, steps, 23)
+    dp = wf._params(p)
+    logpsi = torch.zeros(B, dtype=torch.float64, device="cuda")
+    n_acc, smax, changed = wf.mcmc_low_rank_block(dp, rr, logpsi, static, steps, width, step_offset=off,
+                                                  replay_noise=noise, replay_log_u=logu)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    got_r, got_n = rr.cpu().numpy(), n_acc.cpu().numpy()
+    cmax = np.zeros(3, np.int64)
+    checked = 0
+    for w in range(B):
+        r_ref, lp_ref, na, mg, cm = O.single_electron_low_rank_block(prob, p, r[w].astype(np.float64), noise[:, w],
+                                                                     logu[:, w], float(np.float32(width)), offset=off)
+        cmax = np.maximum(cmax, cm)
+        if np.all(np.abs(mg) > 1e-6):
+            checked += 1
+            assert got_n[w] == na, w
+            np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
+            np.testing.assert_allclose(logpsi[w].item(), 0.5 * lp_ref, rtol=1e-8)
+    assert checked > 0
+    assert tuple(changed) == tuple(int(x) for x in cmax)
+    assert smax.n_pairs_same + smax.n_pairs_diff > 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+@pytest.mark.parametrize("name", ["h10", "c10h22"])
+def test_low_rank_block_matches_full_evaluation_block(cuda_lib, name, precision):
+    """FP32 and mixed paths: the low-rank block and the full-evaluation block (fire_mcmc_single_block) on the same
+    replayed draws take the same decisions on nearly every walker (rounding can flip a marginal one), and log|psi|
+    carried by the state through n + 3 steps of Woodbury updates agrees with a fresh evaluation of the final
+    positions (1e-4 relative)."""
+    wf, mol, nu, r, p, rr, static = _setup(name, precision)
+    B, n = r.shape[0], mol.n_el
+    steps, width = n + 3, 0.4
+    noise, logu = _draws(B, steps, 29)
+    dp = wf._params(p)
+    r_full = rr.clone()
+    _, lp_full = wf.signed(dp, r_full, static)
+    acc_full, _ = wf.mcmc_single_block(dp, r_full, lp_full, static, steps, width, replay_noise=noise,
+                                       replay_log_u=logu)
+    lp_lr = torch.zeros_like(lp_full)
+    acc_lr, _, changed = wf.mcmc_low_rank_block(dp, rr, lp_lr, static, steps, width, replay_noise=noise,
+                                                replay_log_u=logu)
+    same = (acc_full == acc_lr).cpu().numpy()
+    assert same.sum() >= B - 1
+    _, lp_fresh = wf.signed(dp, rr, static)
+    np.testing.assert_allclose(lp_lr.cpu().numpy(), lp_fresh.cpu().numpy(), rtol=1e-4)
+    assert changed[0] >= 1
+
+
+def test_low_rank_capacity_overflow_reruns(cuda_lib):
+    """A changed-set capacity of 2 overflows (FIRE_FLAG_CHANGED_OVERFLOW); the wrapper reruns the block with the set
+    the device saw, and the result equals a run with a generous capacity."""
+    wf, mol, nu, r, p, rr, static = _setup("c2h6", "fp64")
+    B, n = r.shape[0], mol.n_el
+    steps, width = 6, 0.4
+    noise, logu = _draws(B, steps, 31)
+    dp = wf._params(p)
+    ra, rb = rr.clone(), rr.clone()
+    la, lb = torch.zeros(B, dtype=torch.float64, device="cuda"), torch.zeros(B, dtype=torch.float64, device="cuda")
+    na, _, ca = wf.mcmc_low_rank_block(dp, ra, la, static, steps, width, replay_noise=noise, replay_log_u=logu,
+                                       cap_changed=2)
+    nb_, _, cb = wf.mcmc_low_rank_block(dp, rb, lb, static, steps, width, replay_noise=noise, replay_log_u=logu,
+                                        cap_changed=min(n, 64))
+    assert ca == cb and ca[0] > 2 and wf._lr_cap >= ca[0]
+    assert torch.equal(na, nb_) and torch.equal(ra, rb)
+    np.testing.assert_allclose(la.cpu().numpy(), lb.cpu().numpy(), rtol=1e-12)

@@ -28,7 +28,7 @@ def header_symbols():
 
 def test_library_exports_every_header_symbol(lib):
     syms = header_symbols()
-    assert len(syms) == 19
+    assert len(syms) == 21
     assert sorted(syms) == sorted(_lib.SYMBOLS)
     for s in syms:
         assert hasattr(lib, s), s
@@ -82,6 +82,31 @@ def test_local_energy_rejects_problems_beyond_the_inverse_limit(lib):
     rc = lib.fire_local_energy(None, C.byref(big), dummy, dummy, dummy, dummy, None, None, dummy, None, None, dummy,
                                C.c_size_t(1), dummy)
     assert rc == 2
+
+
+def test_low_rank_block_sizes_and_argument_checks(lib):
+    """fire_low_rank_workspace_size / fire_mcmc_low_rank_block: the low-rank state (with the inverses) and the
+    per-step scratch grow with the changed-set capacity; capacities above 128, more than 798
+    electrons, a zero capacity or half a replay are rejected before any CUDA call (pointers never dereferenced)."""
+    prob = _lib.Problem(82, 41, 32, 64, 5.0, 20.0, 2500, 40, 0, 0)
+    a, b = C.c_size_t(), C.c_size_t()
+    assert lib.fire_low_rank_workspace_size(C.byref(prob), 8, 32, C.byref(a)) == 0
+    assert lib.fire_low_rank_workspace_size(C.byref(prob), 8, 64, C.byref(b)) == 0
+    # the transposed inverses alone: 8 walkers x 4 determinants x 82 x ainv_ld(82) floats
+    assert b.value > a.value > 8 * 4 * 82 * 88 * 4
+    assert lib.fire_low_rank_workspace_size(C.byref(prob), 8, 129, C.byref(a)) == 2
+    assert lib.fire_low_rank_workspace_size(C.byref(prob), 8, 0, C.byref(a)) == 1
+    dummy = C.c_void_p(16)
+
+    def call(pr, cap, noise=None, logu=None):
+        return lib.fire_mcmc_low_rank_block(None, C.byref(pr), dummy, dummy, dummy, dummy, dummy, 4, 0, 0.5, cap, 0, 0,
+                                            noise, logu, None, None, dummy, C.c_size_t(1), dummy)
+
+    assert call(prob, 129) == 2
+    assert call(prob, 0) == 1
+    assert call(prob, 32, noise=dummy) == 1
+    big = _lib.Problem(800, 400, 100, 4, 5.0, 20.0, 100, 10, 0, 0)
+    assert call(big, 32) == 2
 
 
 def test_static_padding_mirrors_reference():
