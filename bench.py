@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--mcmc-single-steps", type=int, default=32,
                     help="single-electron Metropolis steps timed on a copy of the walkers (0: skip)")
     ap.add_argument("--mcmc-single-width", type=float, default=0.5)
+    ap.add_argument("--mcmc-low-rank-steps", type=int, default=0,
+                    help="single-electron steps of the low-rank block, timed on a copy of the walkers (0: skip)")
     ap.add_argument("--acc-walkers", type=int, default=256, help="walkers checked against the FP64 build")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
     ap.add_argument("--serving-requests", type=int, default=40, help="requests of the serving segment (0: skip)")
@@ -324,6 +326,26 @@ def main():
                 "acceptance": float(blk1["acc"].float().mean().item()) / args.mcmc_single_steps,
                 "evaluation": "every proposal by the full value path (no low-rank update)"}
             del r1, lp1
+        if args.mcmc_low_rank_steps > 0:
+            # the same proposals evaluated from a state per walker (fire_mcmc_low_rank_block): one untimed block
+            # (it settles the changed-set capacity), then one timed block
+            r2, lp2 = r_dev.clone(), logpsi.clone()
+            blk2 = {}
+
+            def block2():
+                blk2["acc"], _, blk2["changed"] = wf.mcmc_low_rank_block(
+                    dp, r2, lp2, static, args.mcmc_low_rank_steps, args.mcmc_single_width, seed=3000 + rank,
+                    counter=0)
+
+            block2()
+            ms2, _ = time_steps(block2, 1, stream, dist, world)
+            mcmc["single_electron_low_rank"] = {
+                "steps": args.mcmc_low_rank_steps, "width_bohr": args.mcmc_single_width, "ms_per_block": ms2,
+                "walker_steps_per_s": B * world * args.mcmc_low_rank_steps / (ms2 / 1e3),
+                "acceptance": float(blk2["acc"].float().mean().item()) / args.mcmc_low_rank_steps,
+                "changed_max": list(blk2["changed"]), "cap_changed": wf._lr_cap,
+                "evaluation": "low-rank update of a state per walker (state built once per block)"}
+            del r2, lp2
         static = wf.get_static_input(r_dev).round_with_padding(1.1, mol.n_el, n_up, mol.n_nuc)
     r_np = r_dev.cpu().numpy()
 
