@@ -545,6 +545,43 @@ def make_local_energy(wf: FireWaveFunction):
     return local_energy
 
 
+@dataclasses.dataclass(frozen=True)
+class WidthSchedulerState:
+    """``WidthSchedulerState`` (``mcmc.py:349-378``): the proposal width, the ring of the last window_size
+    acceptance rates and the number of updates so far (float32 values, as in the reference)."""
+
+    width: np.float32
+    pmoves: tuple
+    i: int
+
+
+def make_width_scheduler(window_size: int = 20, target_pmove: float = 0.5, error: float = 0.025,
+                         width_multiplier: float = 1.1):
+    """``make_width_scheduler`` (``mcmc.py:349-378``): returns (init, update).  update(state, pmove) stores pmove in
+    the ring and, on the calls whose count so far is a multiple of window_size (the first call included), divides the
+    width by width_multiplier if the ring's mean is below target_pmove - error and multiplies it if above
+    target_pmove + error.  As in the reference the mean is that of the ring before pmove is stored, so the first call
+    sees the zero-initialised ring and narrows the width."""
+    mult = np.float32(width_multiplier)
+
+    def init(init_width: float) -> WidthSchedulerState:
+        return WidthSchedulerState(np.float32(init_width), (np.float32(0.0),) * window_size, 0)
+
+    def update(state: WidthSchedulerState, pmove: float) -> WidthSchedulerState:
+        ring = list(state.pmoves)
+        ring[state.i % window_size] = np.float32(pmove)
+        pm_mean = np.mean(np.asarray(state.pmoves, np.float32), dtype=np.float32)
+        width = state.width
+        if state.i % window_size == 0:
+            if pm_mean < np.float32(target_pmove - error):
+                width = np.float32(width / mult)
+            if pm_mean > np.float32(target_pmove + error):
+                width = np.float32(width * mult)
+        return WidthSchedulerState(width, tuple(ring), state.i + 1)
+
+    return init, update
+
+
 def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, proposal: str = "all-electron",
               sweeps: float = 2.0, jump_steps: int = 0, max_cluster_size: int = 5, max_cluster_radius: float = 2.0,
               sweep_type: str = "sequential"):

@@ -215,3 +215,21 @@ def test_make_mcmc_proposal_selection_checks():
     make_mcmc(wf, proposal="cluster-update", sweeps=1.5, sweep_type="random")
     _, width = make_mcmc(wf, proposal="single-electron", init_width=0.5, jump_steps=20)
     assert width == 0.5
+
+
+def test_width_scheduler_mirrors_reference():
+    """make_width_scheduler (mcmc.py:349-378): every window_size updates (the first included) the width shrinks by the
+    multiplier when the ring's mean acceptance, taken before the new rate is stored, is below target - error, grows
+    when above target + error and stays otherwise; the first update sees the zero ring and shrinks."""
+    from sparse_wf_gb300.wavefunction import make_width_scheduler
+
+    init, update = make_width_scheduler(window_size=3, target_pmove=0.5, error=0.025, width_multiplier=2.0)
+    s = init(0.8)
+    widths = []
+    for pm in [0.9, 0.9, 0.9, 0.9, 0.1, 0.1, 0.1, 0.5, 0.5, 0.5]:
+        s = update(s, pm)
+        widths.append(float(s.width))
+    # update 0: zero ring -> 0.4; updates 3, 6, 9 see the means of (0.9, 0.9, 0.9), (0.9, 0.1, 0.1), (0.1, 0.5, 0.5)
+    np.testing.assert_array_equal(np.float32(widths),
+                                  np.float32([0.4, 0.4, 0.4, 0.8, 0.8, 0.8, 0.4, 0.4, 0.4, 0.2]))
+    assert s.i == 10 and s.width.dtype == np.float32
