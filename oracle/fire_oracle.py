@@ -34,7 +34,9 @@ What is restated (file:line in the reference project):
   (``new_sparse_model.py:414-474, 553-629``), ``Orbitals.low_rank_update`` (``orbitals.py:121-146``),
   ``woodburry_update`` (``model/utils.py:216-245``), ``Jastrow.low_rank_update`` (``jastrow.py:309-361``), driven by
   ``mcmc_steps_low_rank`` (``mcmc.py:196-275``); pinned like the reference's ``tests/test_low_rank.py:29-61``, against
-  full evaluation.
+  full evaluation;
+* directional derivatives of log|psi| with respect to the parameters (``logpsi_jvp``, complex step): the checker of
+  the per-walker parameter gradient that feeds SPRING (``preconditioner.py:118-262``).
 
 folx (0.2.15, a dependency absent here) is replaced by ``FL``: a dense forward-mode
 Laplacian carrier (value, Jacobian over T tangents, Laplacian), the published
@@ -65,16 +67,25 @@ ATT_DIM = 16
 
 
 # =============================================================================== scalar functions
+# The value path also accepts complex parameters (the complex-step derivative of logpsi_jvp): for complex inputs
+# these use analytic forms; real inputs take exactly the real code.
 def sigmoid(x):
-    return expit(x)
+    return 1.0 / (1.0 + np.exp(-x)) if np.iscomplexobj(x) else expit(x)
 
 
 def softplus(x):
+    if np.iscomplexobj(x):
+        return np.where(x.real > 0, x + np.log1p(np.exp(-x)), np.log1p(np.exp(x)))
     return np.logaddexp(0.0, x)
 
 
 def silu(x):
-    return x * expit(x)
+    return x * sigmoid(x)
+
+
+def _log_abs(x):
+    """log|x|; for complex x (a real value plus a complex-step perturbation) the analytic log(x sign(Re x))."""
+    return np.log(x * np.sign(x.real)) if np.iscomplexobj(x) else np.log(np.abs(x))
 
 
 def dsilu(x):
@@ -92,7 +103,7 @@ def cutoff_function(d, p=4):
     a = -(p + 1) * (p + 2) * 0.5
     b = p * (p + 2)
     c = -p * (p + 1) * 0.5
-    return np.where(d < 1, 1 + a * d**p + b * d ** (p + 1) + c * d ** (p + 2), 0.0)
+    return np.where(np.real(d) < 1, 1 + a * d**p + b * d ** (p + 1) + c * d ** (p + 2), 0.0)
 
 
 # =============================================================================== dense forward-Laplacian carrier
@@ -528,7 +539,7 @@ def _jastrow_readout(prob, p, r, one_el, att, vals):
     x = x @ p["att_out3_W"] + p["att_out3_b"]
     J = x * p["att_scale"] + np.array([0.0, p["att_bias"][0]])
     J = J + one_el.sum(0)
-    return np.sign(J[1]), logpsi + J[0] + np.log(np.abs(J[1]))
+    return np.sign(np.real(J[1])), logpsi + J[0] + _log_abs(J[1])
 
 
 def jastrow_value(prob, p, r, h):
@@ -537,17 +548,17 @@ def jastrow_value(prob, p, r, h):
 
 
 def logsumexp_signed(logdets, signs):
-    m = np.max(logdets)
+    m = np.max(np.real(logdets))
     s = np.sum(signs * np.exp(logdets - m))
-    return np.sign(s), m + np.log(np.abs(s))
+    return np.sign(np.real(s)), m + _log_abs(s)
 
 
 def slogdet_lu(A):
     """``slogdet_from_lu`` (``model/utils.py:153-161``) on a partial-pivoting LU."""
     lu, piv = scipy.linalg.lu_factor(A, check_finite=False)
     diag = np.diag(lu)
-    parity = np.count_nonzero(piv != np.arange(len(piv))) + np.count_nonzero(diag < 0)
-    return (-1.0 if parity % 2 else 1.0), np.sum(np.log(np.abs(diag))), (lu, piv)
+    parity = np.count_nonzero(piv != np.arange(len(piv))) + np.count_nonzero(np.real(diag) < 0)
+    return (-1.0 if parity % 2 else 1.0), np.sum(_log_abs(diag)), (lu, piv)
 
 
 def logpsi(prob, p, r):
@@ -558,6 +569,17 @@ def logpsi(prob, p, r):
     s_det, l_det = logsumexp_signed(np.array([x[1] for x in sl]), np.array([x[0] for x in sl]))
     s_j, l_j = jastrow_value(prob, p, r, h)
     return s_det * s_j, l_det + l_j
+
+
+def logpsi_jvp(prob, p, r, v, h=1e-30):
+    """Directional derivative of log|psi| with respect to the parameters along v (a dict of arrays shaped like those
+    of p; absent slots are zero), by the complex step: Im log|psi|(p + i h v) / h, exact to rounding because no two
+    nearby values are subtracted (Squire and Trapp, SIAM Rev. 40, 1998).  It checks a per-walker parameter gradient g
+    of log|psi| (the rows of SPRING's Jacobian, ``preconditioner.py:118-262``; ``update.py:177-191``) through
+    <g, v> = logpsi_jvp(v) for any direction v."""
+    pc = {k: (np.asarray(p[k], np.float64) + 1j * h * np.asarray(v[k], np.float64)) if k in v else p[k] for k in p}
+    _, l = logpsi(prob, pc, np.asarray(r, np.float64))
+    return float(np.imag(l)) / h
 
 
 def potential_energy(r, R, Z):
