@@ -233,3 +233,98 @@ def test_width_scheduler_mirrors_reference():
     np.testing.assert_array_equal(np.float32(widths),
                                   np.float32([0.4, 0.4, 0.4, 0.8, 0.8, 0.8, 0.4, 0.4, 0.4, 0.2]))
     assert s.i == 10 and s.width.dtype == np.float32
+
+
+class _FakeLowRankLib:
+    """Stands in for libfire.so in the low-rank wrapper's host logic: a changed set of `need` electrons per step
+    (FIRE_FLAG_CHANGED_OVERFLOW below that capacity) and, optionally, one pair-capacity overflow first."""
+
+    def __init__(self, need, pair_overflow=False):
+        self.need, self.pair_overflow, self.calls = need, pair_overflow, []
+
+    def fire_prepared_size(self, prob, nbytes):
+        nbytes._obj.value = 64
+        return 0
+
+    def fire_prepare_params(self, *args):
+        return 0
+
+    def fire_low_rank_workspace_size(self, prob, chunk, cap, nbytes):
+        nbytes._obj.value = 1024 * int(cap)
+        return 0
+
+    def fire_mcmc_low_rank_block(self, stream, prob, R, Z, prepared, r, logpsi, steps, off, width, cap, seed, counter,
+                                 noise, logu, n_acc, smax, ws, ws_bytes, status):
+        pr = prob._obj
+        n3 = pr.n_walkers * pr.n_el * 3
+        rv = (C.c_float * n3).from_address(r.value)
+        self.calls.append((int(cap), int(pr.cap_pairs), float(rv[0])))
+        rv[0] += 1.0  # the block moves the walkers in place: a rerun must start from the original positions
+        st = (C.c_int32 * _lib.STATUS_WORDS).from_address(status.value)
+        if self.pair_overflow and len(self.calls) == 1:
+            st[0] |= _lib.FLAG_PAIR_OVERFLOW
+            st[1] = 4 * pr.cap_pairs
+            return 0
+        if cap < self.need:
+            st[0] |= _lib.FLAG_CHANGED_OVERFLOW
+            st[4] = self.need
+            return 0
+        sm = (C.c_int32 * 7).from_address(smax.value)
+        for k, v in enumerate([1, 2, 0, 3, self.need, 20, 21]):
+            sm[k] = v
+        na = (C.c_int32 * pr.n_walkers).from_address(n_acc.value)
+        for k in range(pr.n_walkers):
+            na[k] = 5
+        return 0
+
+
+def _fake_wf(monkeypatch, fake):
+    import torch
+
+    from sparse_wf_gb300.wavefunction import FireWaveFunction
+
+    monkeypatch.setattr(_lib, "load", lambda: fake)
+    mol = systems.alkane(2)
+    wf = FireWaveFunction(mol, precision="fp32", device="cpu")
+    wf._stream = lambda: None
+    r = torch.from_numpy(systems.init_electrons(mol, 2, 5)).contiguous()
+    return wf, mol, r
+
+
+def test_low_rank_wrapper_reruns_and_grows_capacities(monkeypatch):
+    """mcmc_low_rank_block's host logic: a changed-set overflow reruns the block from the original walkers and
+    log|psi| with the set the device reported (padded by 10 %, capped at the electron count), the capacity is kept
+    for the next call, a pair overflow grows the neighbour capacity first, and the 7 static words come back as
+    (StaticArgs, move statics)."""
+    import torch
+
+    from sparse_wf_gb300.wavefunction import StaticArgs
+
+    fake = _FakeLowRankLib(need=14, pair_overflow=True)
+    wf, mol, r = _fake_wf(monkeypatch, fake)
+    params = P.init_params(wf.dims, 0)
+    r0 = float(r[0, 0, 0])
+    lp = torch.zeros(2)
+    n_acc, smax, changed = wf.mcmc_low_rank_block(params, r, lp, StaticArgs(40, 40, 0, 8), 5, 0.5, cap_changed=4)
+    caps, pairs, starts = zip(*fake.calls)
+    assert caps == (4, 4, 16) and pairs[1] > pairs[0]
+    assert all(x == r0 for x in starts)
+    assert wf._lr_cap == 16 and changed == (14, 20, 21) and tuple(smax.__dict__.values()) == (1, 2, 0, 3)
+    assert n_acc.tolist() == [5, 5]
+    fake.calls.clear()
+    fake.pair_overflow = False
+    wf.mcmc_low_rank_block(params, r, lp, StaticArgs(40, 40, 0, 8), 5, 0.5)
+    assert [c[0] for c in fake.calls] == [16]
+
+
+def test_low_rank_wrapper_rejects_sets_beyond_the_limit(monkeypatch):
+    """A changed set larger than the electron count allows (here all 18 electrons are the limit) raises instead of
+    rerunning forever."""
+    import torch
+
+    from sparse_wf_gb300.wavefunction import StaticArgs
+
+    fake = _FakeLowRankLib(need=30)
+    wf, mol, r = _fake_wf(monkeypatch, fake)
+    with pytest.raises(RuntimeError, match="limit of 18"):
+        wf.mcmc_low_rank_block(P.init_params(wf.dims, 0), r, torch.zeros(2), StaticArgs(40, 40, 0, 8), 5, 0.5)
