@@ -25,6 +25,7 @@
  *   fire_mcmc_cluster_block mcmc.py:119-161 proposal_cluster_update (make_mcmc "cluster-update")
  *   fire_mcmc_low_rank_block  mcmc.py:100-111, 196-275 with model/wave_function.py:226-287
  *                       log_psi_with_state / log_psi_low_rank_update (the state-carrying single-electron block)
+ *   fire_ecp_energy     pseudopotentials.py:205-219, 272-398 local and non-local pseudopotential terms
  *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
  *                       (used by the initialiser, new_sparse_model.py:378-379)
  */
@@ -277,6 +278,37 @@ fire_status fire_mcmc_low_rank_block(void* stream, const fire_problem* prob, con
                                      float width, int32_t cap_changed, uint64_t seed, uint64_t counter,
                                      const void* replay_noise, const void* replay_log_u, int32_t* n_accept,
                                      int32_t* static_max, void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Effective core potentials of the pseudised nuclei (make_pseudopotential, pseudopotentials.py:411-457): the
+ * channels on the radial grid as eval_ecp_on_grid (pseudopotentials.py:149-202) tabulates them.  Device arrays. */
+typedef struct {
+  int32_t n_ecp;          /* pseudised nuclei */
+  int32_t n_grid;         /* radial grid points */
+  int32_t n_l;            /* non-local channels l = 0 .. n_l - 1 (n_l <= 4) */
+  int32_t max_quad;       /* host copy of the largest n_quad */
+  const int32_t* atom;    /* [n_ecp] nucleus index of each pseudised nucleus */
+  const double* grid;     /* [n_grid] ascending radii */
+  const double* v_loc;    /* [n_ecp, n_grid] local channel */
+  const double* v_nl;     /* [n_ecp, n_l, n_grid] non-local channels */
+  const double* cutoff;   /* [n_ecp] radius beyond which the non-local channels are neglected */
+  const int32_t* n_quad;  /* [n_ecp] quadrature points of each nucleus's sphere: 1, 2, 4, 6 or 12 */
+} fire_ecp;
+
+/* Pseudopotential energy of every walker, e_ecp [B] in the walkers' dtype.  The local term is summed over
+ * electrons and pseudised nuclei (make_local_pseudopotential, pseudopotentials.py:205-219).  For the non-local
+ * term (make_nonlocal_pseudopotential, :337-398), each electron within the cutoff of its closest pseudised nucleus
+ * is moved to that nucleus's quadrature points (build_all_integration_points, :272-334), on a sphere through the
+ * electron, rotated at random per walker and electron.  The sum is over l of v_l(d) w (2l + 1) P_l(cos theta)
+ * psi'/psi, the ratios from the low-rank update of a cached state as in fire_mcmc_low_rank_block.  Rotations: the
+ * columns of the Gram-Schmidt basis of two normal 3-vectors (random_rot_mat, :222-228) from Philox4x32-10 keyed by
+ * (seed, counter, walker, electron), unless replay_rotations [B, n, 3, 3] (walkers' dtype, rot[x][y]) is given.
+ * The Coulomb potential with the effective charges and the kinetic energy come from fire_local_energy called with
+ * Z = the effective charges.  cap_changed, workspace (fire_low_rank_workspace_size) and static_max [7] as
+ * fire_mcmc_low_rank_block. */
+fire_status fire_ecp_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                            const void* prepared, const void* r, const fire_ecp* ecp, int32_t cap_changed,
+                            uint64_t seed, uint64_t counter, const void* replay_rotations, void* e_ecp,
+                            int32_t* static_max, void* workspace, size_t workspace_bytes, int32_t* status);
 
 /* Coulomb potential of every walker (hamiltonian.py:15-26): out [B] in the walkers' dtype. */
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r,

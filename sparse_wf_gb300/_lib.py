@@ -31,7 +31,7 @@ SYMBOLS = [
     "fire_prepare_params", "fire_neighbors", "fire_triplets", "fire_logpsi", "fire_local_energy",
     "fire_embedding", "fire_mcmc_block", "fire_potential_energy", "fire_profile_enable", "fire_profile_report",
     "fire_gemm_mixed", "fire_triplets_static", "fire_mcmc_single_block", "fire_mcmc_jump_block",
-    "fire_mcmc_cluster_block", "fire_low_rank_workspace_size", "fire_mcmc_low_rank_block",
+    "fire_mcmc_cluster_block", "fire_low_rank_workspace_size", "fire_mcmc_low_rank_block", "fire_ecp_energy",
 ]
 
 
@@ -47,6 +47,11 @@ class NeighborOut(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in (
         "ct_same", "nb_same", "jac_same", "ct_diff", "nb_diff", "jac_diff", "jac_ctr", "jac_dep", "en_idx",
         "counts")] + [("cap_same", C.c_int32), ("cap_diff", C.c_int32)]
+
+
+class Ecp(C.Structure):
+    _fields_ = [("n_ecp", C.c_int32), ("n_grid", C.c_int32), ("n_l", C.c_int32), ("max_quad", C.c_int32)] + [
+        (name, C.c_void_p) for name in ("atom", "grid", "v_loc", "v_nl", "cutoff", "n_quad")]
 
 
 class ElocDebug(C.Structure):
@@ -86,6 +91,7 @@ def load() -> C.CDLL:
         "fire_low_rank_workspace_size": ([P, i32, i32, C.POINTER(sz)], i32),
         "fire_mcmc_low_rank_block": ([vp, P, vp, vp, vp, vp, vp, i32, i32, f32, i32, u64, u64, vp, vp, vp, vp, vp, sz,
                                       vp], i32),
+        "fire_ecp_energy": ([vp, P, vp, vp, vp, vp, C.POINTER(Ecp), i32, u64, u64, vp, vp, vp, vp, sz, vp], i32),
         "fire_potential_energy": ([vp, P, vp, vp, vp, vp], i32),
         "fire_profile_enable": ([i32], i32),
         "fire_profile_report": ([C.c_char_p, sz], i32),

@@ -7,6 +7,7 @@
 //   -> FP64 Gauss-Jordan -> determinant Laplacian -> attention Jastrow -> MLP Jastrow -> assembly.
 // The value path (log|psi|, the MCMC building block) runs the same stages without tangents.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -1073,6 +1074,7 @@ struct LrPlan {
   size_t S, S_cnt, en_cnt_p, en_idx_p, counts_p, acc;    // int
   size_t re_p, E5p, HS, B1S, hS, rawU, rawD, coefE, env_p, aS, vS, oS, V, Zb, Qb;  // T
   size_t Minv, ld_p, sd_p;                               // double
+  size_t lp0, sgn0, sgn_p, ecp_acc, ecp_pt;              // pseudopotential energy: T x 3, double x 2
   size_t total;
 };
 
@@ -1113,6 +1115,11 @@ LrPlan make_lr_plan(const fire_problem* p, int Wc, int KS) {
   take(Q.Minv, W * NDET * KS * KS, 8);
   take(Q.ld_p, W * NDET, 8);
   take(Q.sd_p, W * NDET, 8);
+  take(Q.lp0, W, es);
+  take(Q.sgn0, W, es);
+  take(Q.sgn_p, W, es);
+  take(Q.ecp_acc, W, 8);
+  take(Q.ecp_pt, W * 4, 8);
   Q.total = (o + 255) / 256 * 256;
   return Q;
 }
@@ -1152,10 +1159,10 @@ void readout_value(Ctx<T>& c) {
 }
 
 // State of one chunk: the value path with the inverse kept (Gauss-Jordan instead of the LU), the attention value
-// rows, and log|psi| of the chunk's walkers into logpsi (global walker index; log_psi_with_state,
-// wave_function.py:226-247).
+// rows, and log|psi| (and its sign, if sign is not null) of the chunk's walkers into logpsi[w0_out + w]
+// (log_psi_with_state, wave_function.py:226-247).
 template <typename T>
-cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi) {
+cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi, void* sign, int w0_out) {
   setup_ctx(c, false);
   stage_neighbors(c, false);
   stage_embedding<T, 0>(c);
@@ -1174,19 +1181,19 @@ cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi) {
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
   o.logpsi = logpsi;
+  o.sign = sign;
   g_nlaunch++;
   k_assemble<T, false><<<c.Wc, 256, 3 * c.p->n_el * sizeof(double), c.s>>>(
-      c.p->n_el, c.p->n_up, c.p->n_nuc, c.w0, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
+      c.p->n_el, c.p->n_up, c.p->n_nuc, w0_out, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
       c.template buf<double>(c.P.sd), nullptr, nullptr, c.template buf<T>(c.P.JAx), nullptr, nullptr,
       c.template buf<T>(c.P.JMx), nullptr, nullptr, o, c.status);
   return cudaPeekAtLastError();
 }
 
-// One low-rank step of the chunk: electron e of every walker moved (proposal in c.P.rn), log|psi'| from the state,
-// accept, and on acceptance the state's rows and the Woodbury update of the inverse.
+// log|psi'| (into c.P.lpn) and its sign (into sgn_out, may be null) of the chunk's proposal c.P.rn, in which electron
+// e of every walker moved, from the state; the proposal's rows stay in the plan's scratch for lr_commit.
 template <typename T>
-cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int st, int e, uint64_t seed,
-                    uint64_t counter, const void* logu, int32_t* n_accept, int32_t* static_max) {
+cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int e, int32_t* static_max, T* sgn_out) {
   const fire_problem* p = c.p;
   const int n = p->n_el, nu = p->n_up, N = p->n_nuc, Wc = c.Wc, DN = NDET * n, rows = Wc * KS;
   const int K8 = N * NENV_ORB;
@@ -1195,7 +1202,6 @@ cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int
   T* r_chunk = rr + (size_t)c.w0 * n * 3;
   int* S = c.template buf<int>(Q.S);
   int* S_cnt = c.template buf<int>(Q.S_cnt);
-  int* acc = c.template buf<int>(Q.acc);
   Prof pr("low_rank_step", s);
   g_nlaunch++;
   k_lr_select<T><<<Wc, 256, 0, s>>>(r_chunk, rn, n, nu, e, c.R, N, (T)p->cutoff, (T)p->cutoff_1el, c.nb, KS, S,
@@ -1305,15 +1311,33 @@ cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int
     readout_value<T>(c);
   }
   // log|psi'| and the Metropolis test
-  T* lpn = c.template buf<T>(c.P.lpn);
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
-  o.logpsi = lpn;
+  o.logpsi = c.template buf<T>(c.P.lpn);
+  o.sign = sgn_out;
   g_nlaunch++;
   k_assemble<T, false><<<Wc, 256, 3 * n * sizeof(double), s>>>(
       n, nu, N, 0, rn, c.R, c.Z, c.W, c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p), nullptr,
       nullptr, c.template buf<T>(c.P.JAx), nullptr, nullptr, c.template buf<T>(c.P.JMx), nullptr, nullptr, o,
       c.status);
+  return cudaPeekAtLastError();
+}
+
+// One low-rank Metropolis step of the chunk: the proposal c.P.rn (electron e moved) evaluated from the state, the
+// Metropolis test, and on acceptance the state's rows and the Woodbury update of the inverse.
+template <typename T>
+cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int st, int e, uint64_t seed,
+                    uint64_t counter, const void* logu, int32_t* n_accept, int32_t* static_max) {
+  const fire_problem* p = c.p;
+  const int n = p->n_el, Wc = c.Wc;
+  cudaStream_t s = c.s;
+  T* rn = c.template buf<T>(c.P.rn);
+  int* S = c.template buf<int>(Q.S);
+  int* S_cnt = c.template buf<int>(Q.S_cnt);
+  int* acc = c.template buf<int>(Q.acc);
+  const cudaError_t ev = lr_evaluate<T>(c, Q, KS, rr, e, static_max, nullptr);
+  if (ev != cudaSuccess) return ev;
+  T* lpn = c.template buf<T>(c.P.lpn);
   g_nlaunch++;
   k_accept<T><<<Wc, 128, 0, s>>>(rr, rn, reinterpret_cast<T*>(logpsi), lpn, n, c.w0, p->n_walkers, st, seed, counter,
                                  reinterpret_cast<const T*>(logu), n_accept, c.template buf<int>(Q.counts_p),
@@ -1339,6 +1363,82 @@ cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int
   return cudaPeekAtLastError();
 }
 
+// The unit-sphere quadratures of make_spherical_grid: 1 and 2 points, the tetrahedron, the octahedron and the
+// icosahedron (vertices the cyclic permutations of (0, +-1, +-phi) / sqrt(1 + phi^2), phi the golden ratio).
+EcpQuad ecp_quadratures() {
+  EcpQuad q;
+  std::memset(&q, 0, sizeof(q));
+  auto sph = [&](int row, double th, double ph) {
+    q.p[row][0] = std::sin(th) * std::cos(ph);
+    q.p[row][1] = std::sin(th) * std::sin(ph);
+    q.p[row][2] = std::cos(th);
+  };
+  const double pi = 3.141592653589793;
+  sph(0, 0.0, 0.0);
+  sph(1, 0.0, 0.0);
+  sph(2, pi, 0.0);
+  const double tet = std::acos(-1.0 / 3.0);
+  sph(3, 0.0, 0.0);
+  sph(4, tet, 0.0);
+  sph(5, tet, 2 * pi / 3);
+  sph(6, tet, 4 * pi / 3);
+  const double h = pi / 2;
+  sph(7, 0.0, 0.0);
+  sph(8, pi, 0.0);
+  sph(9, h, 0.0);
+  sph(10, h, h);
+  sph(11, h, pi);
+  sph(12, h, 3 * h);
+  const double phi = (1.0 + std::sqrt(5.0)) / 2.0, x = phi / std::sqrt(1.0 + phi * phi), y = 1.0 / std::sqrt(1.0 + phi * phi);
+  const double ico[12][3] = {{x, 0, -y}, {y, -x, 0}, {0, -y, x}, {x, 0, y},  {-y, -x, 0}, {0, y, -x},
+                             {-x, 0, -y}, {-y, x, 0}, {0, y, x}, {-x, 0, y}, {y, x, 0},   {0, -y, -x}};
+  for (int k = 0; k < 12; ++k)
+    for (int c = 0; c < 3; ++c) q.p[13 + k][c] = ico[k][c];
+  return q;
+}
+
+// Pseudopotential energy of every walker: per chunk the state from one value-path evaluation, the local term, and for
+// every electron e and quadrature point k the low-rank log|psi| of the moved configurations, accumulated into the
+// non-local term.
+template <typename T>
+fire_status run_ecp(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
+                    const void* r, const fire_ecp& ecp, int KS, uint64_t seed, uint64_t counter, const void* rot,
+                    void* out, int32_t* static_max, void* ws, size_t wsb, int32_t* status) {
+  const int Wc = choose_chunk_lr(p, wsb, KS);
+  if (Wc <= 0) return FIRE_ERR_WORKSPACE;
+  Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
+  const LrPlan Q = make_lr_plan(p, Wc, KS);
+  const EcpQuad qt = ecp_quadratures();
+  T* rr = const_cast<T*>(reinterpret_cast<const T*>(r));  // read only: nothing is committed
+  const int n = p->n_el;
+  for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {
+    c.w0 = w0;
+    c.Wc = std::min(Wc, p->n_walkers - w0);
+    c.r = rr + (size_t)w0 * n * 3;
+    T* lp0 = c.template buf<T>(Q.lp0);
+    T* sgn0 = c.template buf<T>(Q.sgn0);
+    double* acc = c.template buf<double>(Q.ecp_acc);
+    double* pt = c.template buf<double>(Q.ecp_pt);
+    if (chunk_state<T>(c, Q, lp0, sgn0, 0) != cudaSuccess) return launch_status("pseudopotential state");
+    g_nlaunch++;
+    k_ecp_local<T><<<c.Wc, 256, 0, s>>>(c.r, n, R, ecp, acc);
+    for (int e = 0; e < n; ++e)
+      for (int k = 0; k < ecp.max_quad; ++k) {
+        g_nlaunch++;
+        k_ecp_point<T><<<c.Wc, 128, 0, s>>>(c.r, c.template buf<T>(c.P.rn), n, e, k, R, ecp, qt, w0, seed, counter,
+                                            reinterpret_cast<const T*>(rot), pt);
+        if (lr_evaluate<T>(c, Q, KS, rr, e, static_max, c.template buf<T>(Q.sgn_p)) != cudaSuccess)
+          return launch_status("pseudopotential ratio");
+        g_nlaunch++;
+        k_ecp_accum<T><<<nblk(c.Wc), 256, 0, s>>>(c.Wc, pt, c.template buf<T>(c.P.lpn), c.template buf<T>(Q.sgn_p),
+                                                  lp0, sgn0, ecp, acc);
+      }
+    g_nlaunch++;
+    k_ecp_store<T><<<nblk(c.Wc), 256, 0, s>>>(c.Wc, w0, acc, reinterpret_cast<T*>(out));
+  }
+  return launch_status(__func__);
+}
+
 // Low-rank single-electron block (mcmc_steps_low_rank with proposal_single_electron): per chunk the state from one
 // value-path evaluation, then every step from the state.
 template <typename T>
@@ -1356,7 +1456,7 @@ fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, c
     c.w0 = w0;
     c.Wc = std::min(Wc, p->n_walkers - w0);
     c.r = rr + (size_t)w0 * n * 3;
-    if (chunk_state<T>(c, Q, logpsi) != cudaSuccess) return launch_status("low-rank state");
+    if (chunk_state<T>(c, Q, logpsi, nullptr, w0) != cudaSuccess) return launch_status("low-rank state");
     for (int st = 0; st < steps; ++st) {
       g_nlaunch++;
       k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), n, w0,
@@ -1644,6 +1744,25 @@ fire_status fire_mcmc_low_rank_block(void* stream, const fire_problem* prob, con
                                replay_noise, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
   return run_mcmc_lr<float>(prob, s, R, Z, prepared, r, logpsi, steps, step_offset, width, KS, seed, counter,
                             replay_noise, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
+}
+
+fire_status fire_ecp_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                            const void* prepared, const void* r, const fire_ecp* ecp, int32_t cap_changed,
+                            uint64_t seed, uint64_t counter, const void* replay_rotations, void* e_ecp,
+                            int32_t* static_max, void* workspace, size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !ecp || !e_ecp || !workspace || cap_changed < 1)
+    return FIRE_ERR_INVALID;
+  if (ecp->n_ecp < 1 || ecp->n_grid < 2 || ecp->n_l < 0 || ecp->n_l > 4 || !ecp->atom || !ecp->grid || !ecp->v_loc ||
+      (ecp->n_l > 0 && !ecp->v_nl) || !ecp->cutoff || !ecp->n_quad || ecp->max_quad < 1 || ecp->max_quad > 12)
+    return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL || cap_changed > LR_KMAX) return FIRE_ERR_UNSUPPORTED;
+  const int KS = std::min<int>(cap_changed, prob->n_el);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_ecp<double>(prob, s, R, Z, prepared, r, *ecp, KS, seed, counter, replay_rotations, e_ecp, static_max,
+                           workspace, workspace_bytes, status);
+  return run_ecp<float>(prob, s, R, Z, prepared, r, *ecp, KS, seed, counter, replay_rotations, e_ecp, static_max,
+                        workspace, workspace_bytes, status);
 }
 
 fire_status fire_potential_energy(void* stream, const fire_problem* prob, const void* r, const float* R,

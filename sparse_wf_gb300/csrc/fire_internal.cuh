@@ -66,6 +66,14 @@ constexpr int CLUSTER_KMAX = 16, CLUSTER_TRIALS = 5;
 // Low-rank single-electron steps: at most LR_KMAX electrons in a step's changed set (the moved electron and its
 // neighbours before and after the move); the k x k determinant-lemma matrix is eliminated in shared memory.
 constexpr int LR_KMAX = 128;
+// Unit-sphere quadratures of the pseudopotentials' non-local term, all five in one table passed by value: the 1-, 2-,
+// 4-, 6- and 12-point grids at rows 0, 1, 3, 7 and 13 (make_spherical_grid, pseudopotentials.py:44-133).
+struct EcpQuad {
+  double p[25][3];
+};
+__host__ __device__ inline int ecp_quad_row(int n_points) {
+  return n_points == 1 ? 0 : n_points == 2 ? 1 : n_points == 4 ? 3 : n_points == 6 ? 7 : 13;
+}
 // Largest electron count of the local-energy and value paths: the double-FP32 / FP64 elimination keeps two n x 17 panel buffers
 // of eight-byte elements (plus ~2.5 KB) in shared memory, 288 n + 2496 bytes within the 227 KB per CTA.
 constexpr int ELOC_MAX_EL = 798;

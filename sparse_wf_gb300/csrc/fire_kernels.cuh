@@ -113,6 +113,18 @@ __global__ void k_lr_wb_q(const int* accf, const int* S, const int* S_cnt, int K
 template <typename T>
 __global__ void k_lr_wb_apply(const int* accf, const int* S_cnt, int KS, int n, T* B, const T* Zb, const T* Qb);
 
+// fire_ecp.cu
+template <typename T>
+__global__ void k_ecp_local(const T* r, int n, const float* R, fire_ecp ecp, double* acc);
+template <typename T>
+__global__ void k_ecp_point(const T* r, T* rn, int n, int e, int k, const float* R, fire_ecp ecp, EcpQuad qt, int w0,
+                            uint64_t seed, uint64_t counter, const T* replay, double* pt);
+template <typename T>
+__global__ void k_ecp_accum(int Wc, const double* pt, const T* lpn, const T* sgn_n, const T* lp0, const T* sgn0,
+                            fire_ecp ecp, double* acc);
+template <typename T>
+__global__ void k_ecp_store(int Wc, int w0, const double* acc, T* out);
+
 // fire_tc.cu (host launchers)
 cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __nv_bfloat16* lo, cudaStream_t s);
 cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s);

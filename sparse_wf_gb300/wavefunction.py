@@ -449,6 +449,54 @@ class FireWaveFunction:
         sm = smax.cpu().numpy()
         return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3])), (int(sm[4]), int(sm[5]), int(sm[6]))
 
+    def ecp_energy(self, params, electrons, static: StaticArgs, ecp, seed: int = 0, counter: int = 0,
+                   replay_rotations=None, cap_changed: Optional[int] = None):
+        """Pseudopotential energy of every walker (``fire_ecp_energy``): the local term and the non-local quadrature
+        with psi ratios from the low-rank update of a cached state (``make_pseudopotential``,
+        ``pseudopotentials.py:205-219, 272-398``).  The wavefunction's molecule carries the effective charges
+        (``EcpTables.z_eff``); ecp is the ``DeviceEcp`` of its tables.  replay_rotations [B, n, 3, 3] replaces the
+        random rotations.  Returns (e_ecp [B], move statics maximised over the ratios)."""
+        p = self._params(params)
+        r = self._electrons(electrons)
+        B, n = r.shape[0], self.n_electrons
+        out = torch.zeros(B, dtype=self.dtype, device=self.device)
+        smax = torch.zeros(7, dtype=torch.int32, device=self.device)
+        rot = None
+        if replay_rotations is not None:
+            rot = torch.as_tensor(np.asarray(replay_rotations)).to(self.device, self.dtype).reshape(B, n, 3, 3)
+            rot = rot.contiguous()
+        limit = min(n, _lib.LOW_RANK_MAX_CHANGED)
+        cap = min(int(cap_changed or self._lr_cap or max(16, 2 * static.n_pairs // max(1, n) + 1)), limit)
+        lib = _lib.load()
+        for _ in range(6):
+            self._status.zero_()
+            smax.zero_()
+            prob = self._problem(B, static)
+            ws = self._workspace(prob, cap)
+            _lib.check(lib.fire_ecp_energy(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
+                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.byref(ecp.struct), int(cap),
+                C.c_uint64(seed), C.c_uint64(counter), C.c_void_p(rot.data_ptr()) if rot is not None else None,
+                C.c_void_p(out.data_ptr()), C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()),
+                C.c_size_t(ws.numel()), C.c_void_p(self._status.data_ptr())), "fire_ecp_energy")
+            st = self._read_status()
+            flags = int(st[0])
+            if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
+                static = self._grown(st, static)
+                continue
+            if flags & _lib.FLAG_CHANGED_OVERFLOW:
+                need = int(st[4])
+                if need > limit:
+                    raise RuntimeError(f"a changed set of {need} electrons exceeds the low-rank limit of {limit}")
+                cap = min(limit, max(need, int(need * 1.1) + 1))
+                continue
+            break
+        else:
+            raise RuntimeError("low-rank capacities did not converge")
+        self._lr_cap = cap
+        sm = smax.cpu().numpy()
+        return out, (int(sm[4]), int(sm[5]), int(sm[6]))
+
     def mcmc_jump_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
                         steps: int, sigma: float = 2.0, seed: int = 0, counter: int = 0, replay_draws=None,
                         replay_log_u=None):

@@ -104,3 +104,23 @@ def test_nonlocal_term_low_rank_ratios_equal_full_evaluations():
     assert a != 0.0
     assert abs(a - b) <= 1e-10 * max(1.0, abs(b))
     assert np.isfinite(E.local_energy(prob, p, ecp, w, rot))
+
+
+def test_product_tables_match_the_oracle():
+    """sparse_wf_gb300.ecp.EcpTables (the host tables fire_ecp_energy consumes) against the oracle's restatement of
+    make_pseudopotential: effective charges, pseudised nuclei, grid, local and non-local channels, cutoffs and
+    quadrature sizes."""
+    from sparse_wf_gb300.ecp import EcpTables
+
+    mol = systems.alkane(2)
+    ref = E.Ecp(mol.Z, mol.R, {6: CARBON}, n_quad={6: 4})
+    t = EcpTables(mol.Z, {6: CARBON}, n_quad={6: 4})
+    np.testing.assert_array_equal(t.z_eff, ref.z_eff)
+    np.testing.assert_array_equal(t.atom, np.nonzero(ref.mask)[0])
+    np.testing.assert_array_equal(t.grid, ref.grid)
+    np.testing.assert_allclose(t.v_loc, ref.v_loc, rtol=1e-15, atol=0)
+    np.testing.assert_allclose(t.v_nl, ref.v_nonloc, rtol=1e-15, atol=0)
+    np.testing.assert_array_equal(t.cutoffs, ref.cutoffs)
+    np.testing.assert_array_equal(t.n_quad, ref.n_quad)
+    with pytest.raises(ValueError):
+        EcpTables(mol.Z, {6: CARBON}, n_quad={6: 5})

@@ -1,6 +1,7 @@
 """Parity of the low-rank single-electron block (fire_mcmc_low_rank_block: mcmc_steps_low_rank with the state-carrying
 log_psi_low_rank_update, mcmc.py:196-275, model/wave_function.py:226-287) with the oracle's state-carrying block and
-with the device's full-evaluation block, on replayed draws.
+with the device's full-evaluation block, on replayed draws; and of the pseudopotential energy (fire_ecp_energy), whose
+psi ratios come from the same low-rank evaluation, with the oracle's restatement.
 
 The whole module is skipped until these kernels have had their first run on a GB300: they are compiled and their
 index arithmetic was checked by reading, but not yet executed."""
@@ -105,3 +106,39 @@ def test_low_rank_capacity_overflow_reruns(cuda_lib):
     assert ca == cb and ca[0] > 2 and wf._lr_cap >= ca[0]
     assert torch.equal(na, nb_) and torch.equal(ra, rb)
     np.testing.assert_allclose(la.cpu().numpy(), lb.cpu().numpy(), rtol=1e-12)
+
+
+def test_ecp_energy_matches_oracle(cuda_lib):
+    """fire_ecp_energy in the FP64 build with replayed rotations: the local term plus the non-local quadrature with
+    low-rank psi ratios against the oracle's restatement (oracle/ecp_oracle.py), 1e-8 relative, on C2H6 with a
+    synthetic pseudised carbon (2 core electrons, local, s and p channels; tetrahedral quadrature)."""
+    from oracle import ecp_oracle as E
+    from sparse_wf_gb300 import params as P, systems
+    from sparse_wf_gb300.ecp import EcpTables
+
+    carbon = (2, [(-1, [[], [(14.0, 4.0)], [(8.0, 50.0)], [(13.0, -25.0)]]), (0, [[], [], [(7.0, 50.0)]]),
+                  (1, [[], [], [(6.0, -10.0)]])])
+    mol = systems.alkane(2)
+    tables = EcpTables(mol.Z, {6: carbon}, n_quad={6: 4})
+    val = systems.Molecule("C2H6-valence", mol.R, tables.z_eff)
+    nu, _ = systems.spin_counts(val)
+    r = systems.init_electrons(val, 3, 91).astype(np.float64)
+    dims = P.ModelDims(val.n_el, nu, val.n_nuc)
+    p = P.unpack_params(dims, *P.pack_params(dims, P.activate_jastrow(P.init_params(dims, 0)), np.float32))
+    prob = O.Problem(val.R, val.Z, nu)
+    hc, _ = O.embedding_value(prob, p, r[0], return_pre_scale=True)
+    p["scales"] = np.array([1.0 / np.std(hc), 1.0])
+    _, hu = O.embedding_value(prob, p, r[0], return_pre_scale=True)
+    p["scales"][1] = 1.0 / np.std(hu)
+    rng = np.random.default_rng(7)
+    rot = np.stack([[E.rotation(rng.standard_normal((2, 3))) for _ in range(val.n_el)] for _ in range(len(r))])
+    wf = FireWaveFunction(val, precision="fp64")
+    rr = torch.from_numpy(r).cuda()
+    s = wf.get_static_input(rr)
+    static = StaticArgs(s.n_pairs_same, s.n_pairs_diff, s.n_triplets, s.n_neighbours_en)
+    got, changed = wf.ecp_energy(wf._params(p), rr, static, tables.device("cuda"), replay_rotations=rot)
+    ecp = E.Ecp(mol.Z, mol.R, {6: carbon}, n_quad={6: 4})
+    for w in range(len(r)):
+        ref = E.local_term(ecp, r[w]) + E.nonlocal_term(prob, p, ecp, r[w], rot[w])
+        assert abs(got[w].item() - ref) <= 1e-8 * max(1.0, abs(ref)), w
+    assert changed[0] >= 1
