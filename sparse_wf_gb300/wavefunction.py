@@ -582,12 +582,17 @@ class FireWaveFunction:
         sm = smax.cpu().numpy()
         return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
 
-def make_local_energy(wf: FireWaveFunction):
-    """``make_local_energy`` (``hamiltonian.py:49-83``) for all-electron systems:
-    ``local_energy(key, params, electrons, static) -> (E_loc, new_static)``."""
+def make_local_energy(wf: FireWaveFunction, pseudopotentials=None):
+    """``make_local_energy`` (``hamiltonian.py:49-83``): ``local_energy(key, params, electrons, static) -> (E_loc,
+    new_static)``.  With pseudopotentials (the ``DeviceEcp`` of the molecule's ``EcpTables``; the wavefunction's
+    molecule then carries the effective charges) the local and non-local pseudopotential terms are added, the
+    quadrature rotations keyed by key (an integer seed)."""
 
     def local_energy(key, params, electrons, static: StaticArgs):
         eloc, aux = wf.local_energy_full(params, electrons, static)
+        if pseudopotentials is not None:
+            e_pp, _ = wf.ecp_energy(params, electrons, aux["static"], pseudopotentials, seed=int(key))
+            eloc = eloc + e_pp
         return eloc, aux["static"]
 
     return local_energy
