@@ -215,7 +215,8 @@ fire_status fire_mcmc_block(void* stream, const fire_problem* prob, const float*
  * every walker by width * eps, eps [3] ~ N(0, 1), and accepts if 2 (log|psi'| - log|psi|) > log u.
  * log|psi'| is a full value-path evaluation of the proposed configuration (the reference reaches the same
  * value by a low-rank update of a cached state, checked against the full evaluation in its
- * tests/test_low_rank.py:29-61; that update is not built here, so one step costs one full evaluation).
+ * tests/test_low_rank.py:29-61; fire_mcmc_low_rank_block is that variant, this one costs a full evaluation
+ * per step).
  * Draws from Philox4x32-10 keyed by (seed, counter, step, walker) unless replay_noise [steps, B, 3] and
  * replay_log_u [steps, B] are given.  Other arguments and outputs as fire_mcmc_block. */
 fire_status fire_mcmc_single_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
