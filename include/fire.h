@@ -295,6 +295,10 @@ typedef struct {
   const int32_t* n_quad;  /* [n_ecp] quadrature points of each nucleus's sphere: 1, 2, 4, 6 or 12 */
 } fire_ecp;
 
+/* The unit-sphere quadrature of n_points (1, 2, 4, 6 or 12) points fire_ecp_energy uses (make_spherical_grid,
+ * pseudopotentials.py:44-133), points [n_points, 3] (host, float64); equal weights 1 / n_points.  Host only. */
+fire_status fire_ecp_quadrature(int32_t n_points, double* points);
+
 /* Pseudopotential energy of every walker, e_ecp [B] in the walkers' dtype.  The local term is summed over
  * electrons and pseudised nuclei (make_local_pseudopotential, pseudopotentials.py:205-219).  For the non-local
  * term (make_nonlocal_pseudopotential, :337-398), each electron within the cutoff of its closest pseudised nucleus

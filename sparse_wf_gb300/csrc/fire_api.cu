@@ -1746,6 +1746,16 @@ fire_status fire_mcmc_low_rank_block(void* stream, const fire_problem* prob, con
                             replay_noise, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
 }
 
+fire_status fire_ecp_quadrature(int32_t n_points, double* points) {
+  if (!points || !(n_points == 1 || n_points == 2 || n_points == 4 || n_points == 6 || n_points == 12))
+    return FIRE_ERR_INVALID;
+  const EcpQuad q = ecp_quadratures();
+  const int row = ecp_quad_row(n_points);
+  for (int k = 0; k < n_points; ++k)
+    for (int c = 0; c < 3; ++c) points[3 * k + c] = q.p[row + k][c];
+  return FIRE_OK;
+}
+
 fire_status fire_ecp_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,
                             const void* prepared, const void* r, const fire_ecp* ecp, int32_t cap_changed,
                             uint64_t seed, uint64_t counter, const void* replay_rotations, void* e_ecp,

@@ -124,3 +124,21 @@ def test_product_tables_match_the_oracle():
     np.testing.assert_array_equal(t.n_quad, ref.n_quad)
     with pytest.raises(ValueError):
         EcpTables(mol.Z, {6: CARBON}, n_quad={6: 5})
+
+
+@pytest.mark.parametrize("n_points", [1, 2, 4, 6, 12])
+def test_device_quadrature_table_matches_the_oracle(n_points):
+    """The quadrature table fire_ecp_energy uses (fire_ecp_quadrature, host only) equals the oracle's grids to
+    rounding, point for point."""
+    import ctypes as C
+
+    from sparse_wf_gb300 import _lib
+    from sparse_wf_gb300.build import build
+
+    build()
+    lib = _lib.load()
+    out = (C.c_double * (3 * n_points))()
+    assert lib.fire_ecp_quadrature(n_points, out) == 0
+    got = np.array(out[:]).reshape(n_points, 3)
+    np.testing.assert_allclose(got, E.spherical_grid(n_points)[0], rtol=0, atol=1e-15)
+    assert lib.fire_ecp_quadrature(5, out) == 1
