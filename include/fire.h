@@ -25,6 +25,7 @@
  *   fire_mcmc_cluster_block mcmc.py:119-161 proposal_cluster_update (make_mcmc "cluster-update")
  *   fire_mcmc_low_rank_block  mcmc.py:100-111, 196-275 with model/wave_function.py:226-287
  *                       log_psi_with_state / log_psi_low_rank_update (the state-carrying single-electron block)
+ *   fire_mcmc_low_rank_jump_block  mcmc.py:164-193 proposal_jump_to_atom with the low-rank state
  *   fire_ecp_energy     pseudopotentials.py:205-219, 272-398 local and non-local pseudopotential terms
  *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
  *                       (used by the initialiser, new_sparse_model.py:378-379)
@@ -294,6 +295,16 @@ typedef struct {
   const double* cutoff;   /* [n_ecp] radius beyond which the non-local channels are neglected */
   const int32_t* n_quad;  /* [n_ecp] quadrature points of each nucleus's sphere: 1, 2, 4, 6 or 12 */
 } fire_ecp;
+
+/* Metropolis block of jumps to the nuclei (proposal_jump_to_atom, mcmc.py:164-193, with its log ratio in the test)
+ * evaluated by the low-rank update of a cached state: the proposals, draws and replay of fire_mcmc_jump_block,
+ * each walker moving its own electron; state, capacity, workspace and static_max [7] as fire_mcmc_low_rank_block. */
+fire_status fire_mcmc_low_rank_jump_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                          const void* prepared, void* r, void* logpsi, int32_t steps, float sigma,
+                                          int32_t cap_changed, uint64_t seed, uint64_t counter,
+                                          const void* replay_draws, const void* replay_log_u, int32_t* n_accept,
+                                          int32_t* static_max, void* workspace, size_t workspace_bytes,
+                                          int32_t* status);
 
 /* The unit-sphere quadrature of n_points (1, 2, 4, 6 or 12) points fire_ecp_energy uses (make_spherical_grid,
  * pseudopotentials.py:44-133), points [n_points, 3] (host, float64); equal weights 1 / n_points.  Host only. */

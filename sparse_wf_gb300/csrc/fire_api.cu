@@ -1041,14 +1041,15 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
       g_nlaunch++;
       if (kind == MC_SINGLE)
         k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, w0, p->n_walkers, st, offset,
-                                                 (T)width, seed, counter, reinterpret_cast<const T*>(noise));
+                                                 (T)width, seed, counter, reinterpret_cast<const T*>(noise), nullptr);
       else if (kind == MC_CLUSTER)
         k_propose_cluster<T><<<c.Wc, 32, 0, s>>>(rr + (size_t)w0 * n * 3, rn, plr, n, w0, p->n_walkers, st, offset, ck,
                                                  (T)cradius, (T)width, crandom, seed, counter,
                                                  reinterpret_cast<const T*>(noise));
       else if (kind == MC_JUMP)
         k_propose_jump<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, plr, n, w0, p->n_walkers, st, R, Z,
-                                               p->n_nuc, (T)width, seed, counter, reinterpret_cast<const T*>(noise));
+                                               p->n_nuc, (T)width, seed, counter, reinterpret_cast<const T*>(noise),
+                                               nullptr);
       else
         k_propose<T><<<nblk((long)c.Wc * n), 256, 0, s>>>(rr + (size_t)w0 * n * 3, rn, n, c.Wc, w0, p->n_walkers,
                                                           st, (T)width, seed, counter,
@@ -1071,8 +1072,8 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
 // matrix); the rest is per-step scratch of the proposal.
 struct LrPlan {
   size_t vals, B;                                        // state
-  size_t S, S_cnt, en_cnt_p, en_idx_p, counts_p, acc;    // int
-  size_t re_p, E5p, HS, B1S, hS, rawU, rawD, coefE, env_p, aS, vS, oS, V, Zb, Qb;  // T
+  size_t S, S_cnt, en_cnt_p, en_idx_p, counts_p, acc, moved;  // int
+  size_t re_p, E5p, HS, B1S, hS, rawU, rawD, coefE, coefD, env_p, env_pD, aS, vS, oS, V, Zb, Qb;  // T
   size_t Minv, ld_p, sd_p;                               // double
   size_t lp0, sgn0, sgn_p, ecp_acc, ecp_pt;              // pseudopotential energy: T x 3, double x 2
   size_t total;
@@ -1097,6 +1098,7 @@ LrPlan make_lr_plan(const fire_problem* p, int Wc, int KS) {
   take(Q.en_idx_p, W * p->cap_nuc, 4);
   take(Q.counts_p, W * 4, 4);
   take(Q.acc, W, 4);
+  take(Q.moved, W, 4);
   take(Q.re_p, W * 3, es);
   take(Q.E5p, W * 5 * F, es);
   take(Q.HS, R * F, es);
@@ -1105,7 +1107,9 @@ LrPlan make_lr_plan(const fire_problem* p, int Wc, int KS) {
   take(Q.rawU, R * DN, es);
   take(Q.rawD, R * DN, es);
   take(Q.coefE, NDET * W * K8, es);
+  take(Q.coefD, NDET * W * K8, es);
   take(Q.env_p, W * DN, es);
+  take(Q.env_pD, W * DN, es);
   take(Q.aS, R * HEADS, es);
   take(Q.vS, R * F, es);
   take(Q.oS, R * 2, es);
@@ -1190,10 +1194,11 @@ cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi, void* sign, in
   return cudaPeekAtLastError();
 }
 
-// log|psi'| (into c.P.lpn) and its sign (into sgn_out, may be null) of the chunk's proposal c.P.rn, in which electron
-// e of every walker moved, from the state; the proposal's rows stay in the plan's scratch for lr_commit.
+// log|psi'| (into c.P.lpn) and its sign (into sgn_out, may be null) of the chunk's proposal c.P.rn, in which walker w
+// moved electron moved[w] (the plan's moved buffer), from the state; the proposal's rows stay in the plan's scratch
+// for the commit.
 template <typename T>
-cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int e, int32_t* static_max, T* sgn_out) {
+cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int32_t* static_max, T* sgn_out) {
   const fire_problem* p = c.p;
   const int n = p->n_el, nu = p->n_up, N = p->n_nuc, Wc = c.Wc, DN = NDET * n, rows = Wc * KS;
   const int K8 = N * NENV_ORB;
@@ -1202,9 +1207,10 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int e, int32_
   T* r_chunk = rr + (size_t)c.w0 * n * 3;
   int* S = c.template buf<int>(Q.S);
   int* S_cnt = c.template buf<int>(Q.S_cnt);
+  const int* moved = c.template buf<int>(Q.moved);
   Prof pr("low_rank_step", s);
   g_nlaunch++;
-  k_lr_select<T><<<Wc, 256, 0, s>>>(r_chunk, rn, n, nu, e, c.R, N, (T)p->cutoff, (T)p->cutoff_1el, c.nb, KS, S,
+  k_lr_select<T><<<Wc, 256, 0, s>>>(r_chunk, rn, n, nu, moved, c.R, N, (T)p->cutoff, (T)p->cutoff_1el, c.nb, KS, S,
                                     S_cnt, c.template buf<T>(Q.re_p), c.template buf<int>(Q.en_cnt_p),
                                     c.template buf<int>(Q.en_idx_p), c.template buf<int>(Q.counts_p), static_max,
                                     c.status);
@@ -1236,7 +1242,7 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int e, int32_
   }
   // messages and update MLP of the changed centers
   g_nlaunch++;
-  k_lr_contract<T><<<dim3(KS, Wc), 256, 0, s>>>(rn, n, nu, (T)p->cutoff, e, S, S_cnt, KS, c.W,
+  k_lr_contract<T><<<dim3(KS, Wc), 256, 0, s>>>(rn, n, nu, (T)p->cutoff, moved, S, S_cnt, KS, c.W,
                                                 c.template buf<T>(c.P.E5o), c.template buf<T>(Q.E5p),
                                                 c.template buf<T>(Q.HS));
   const Planes HS{Q.HS, 0, 0}, B1S{Q.B1S, 0, 0}, hS{Q.hS, 0, 0};
@@ -1255,21 +1261,26 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int e, int32_
   g_nlaunch++;
   k_lr_orb<T><<<dim3(KS, Wc), 256, 0, s>>>(S, S_cnt, KS, nu, DN, c.template buf<T>(Q.rawU),
                                            c.template buf<T>(Q.rawD));
-  // envelope row of the moved electron at its new position
+  // envelope row of the moved electron at its new position: coefficients of its own spin (zero in the other spin's
+  // set), both spins' contractions, their sum
   {
-    const bool up = e < nu;
-    T* coef = c.template buf<T>(Q.coefE);
+    T* coefU = c.template buf<T>(Q.coefE);
+    T* coefD = c.template buf<T>(Q.coefD);
     g_nlaunch++;
-    k_env_coef<T, 1><<<nblk((long)Wc * K8), 256, 0, s>>>(rn, c.R, c.W.w[up ? PR_ENV_UP_SP : PR_ENV_DN_SP], n, 1, e,
-                                                         N, Wc, coef);
-    for (int d = 0; d < NDET; ++d) {
-      GemmP<T> g = gp0<T>();
-      g.A = coef + (size_t)d * Wc * K8; g.lda = K8;
-      g.B = c.W.w[up ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (size_t)d * K8 * n; g.ldb = n;
-      g.C = c.template buf<T>(Q.env_p) + (size_t)d * n; g.ldc = DN; g.M = Wc; g.N = n; g.K = K8;
-      g.n_el = 1; g.env_ns = 1; g.env_soff = 0; g.env_nv = 1;
-      gemm<T, EPI_ENV>(c, g);
-    }
+    k_lr_env_coef<T><<<nblk((long)Wc * K8), 256, 0, s>>>(rn, c.R, c.W.w[PR_ENV_UP_SP], c.W.w[PR_ENV_DN_SP], moved, n,
+                                                         nu, N, Wc, coefU, coefD);
+    for (int sp = 0; sp < 2; ++sp)
+      for (int d = 0; d < NDET; ++d) {
+        GemmP<T> g = gp0<T>();
+        g.A = (sp == 0 ? coefU : coefD) + (size_t)d * Wc * K8; g.lda = K8;
+        g.B = c.W.w[sp == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (size_t)d * K8 * n; g.ldb = n;
+        g.C = c.template buf<T>(sp == 0 ? Q.env_p : Q.env_pD) + (size_t)d * n; g.ldc = DN; g.M = Wc; g.N = n;
+        g.K = K8; g.n_el = 1; g.env_ns = 1; g.env_soff = 0; g.env_nv = 1;
+        gemm<T, EPI_ENV>(c, g);
+      }
+    g_nlaunch++;
+    k_lr_env_add<T><<<nblk((long)Wc * DN), 256, 0, s>>>((long)Wc * DN, c.template buf<T>(Q.env_p),
+                                                        c.template buf<T>(Q.env_pD));
   }
   // determinant lemma
   {
@@ -1277,7 +1288,7 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int e, int32_
     cudaFuncSetAttribute(k_lr_det<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     g_nlaunch++;
     k_lr_det<T><<<dim3(NDET, Wc), 256, smem, s>>>(
-        S, S_cnt, KS, n, e, c.template buf<T>(Q.rawU), c.template buf<T>(c.P.env), c.template buf<T>(Q.env_p),
+        S, S_cnt, KS, n, moved, c.template buf<T>(Q.rawU), c.template buf<T>(c.P.env), c.template buf<T>(Q.env_p),
         c.template buf<T>(c.P.Apl), c.template buf<T>(Q.B), c.template buf<double>(c.P.ld),
         c.template buf<double>(c.P.sd), c.template buf<T>(Q.V), c.template buf<double>(Q.Minv),
         c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p));
@@ -1323,11 +1334,12 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int e, int32_
   return cudaPeekAtLastError();
 }
 
-// One low-rank Metropolis step of the chunk: the proposal c.P.rn (electron e moved) evaluated from the state, the
-// Metropolis test, and on acceptance the state's rows and the Woodbury update of the inverse.
+// One low-rank Metropolis step of the chunk: the proposal c.P.rn (walker w moved electron moved[w]) evaluated from the
+// state, the Metropolis test with the proposals' log ratios plr (may be null), and on acceptance the state's rows and
+// the Woodbury update of the inverse.
 template <typename T>
-cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int st, int e, uint64_t seed,
-                    uint64_t counter, const void* logu, int32_t* n_accept, int32_t* static_max) {
+cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int st, uint64_t seed, uint64_t counter,
+                    const void* logu, int32_t* n_accept, int32_t* static_max, const T* plr) {
   const fire_problem* p = c.p;
   const int n = p->n_el, Wc = c.Wc;
   cudaStream_t s = c.s;
@@ -1335,17 +1347,18 @@ cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int
   int* S = c.template buf<int>(Q.S);
   int* S_cnt = c.template buf<int>(Q.S_cnt);
   int* acc = c.template buf<int>(Q.acc);
-  const cudaError_t ev = lr_evaluate<T>(c, Q, KS, rr, e, static_max, nullptr);
+  const int* moved = c.template buf<int>(Q.moved);
+  const cudaError_t ev = lr_evaluate<T>(c, Q, KS, rr, static_max, nullptr);
   if (ev != cudaSuccess) return ev;
   T* lpn = c.template buf<T>(c.P.lpn);
   g_nlaunch++;
   k_accept<T><<<Wc, 128, 0, s>>>(rr, rn, reinterpret_cast<T*>(logpsi), lpn, n, c.w0, p->n_walkers, st, seed, counter,
                                  reinterpret_cast<const T*>(logu), n_accept, c.template buf<int>(Q.counts_p),
-                                 static_max, nullptr, acc);
+                                 static_max, plr, acc);
   // accepted walkers: rows into the state, Woodbury update of the inverse
   g_nlaunch++;
   k_lr_commit<T><<<dim3(KS + 1, Wc), 256, 0, s>>>(
-      acc, S, S_cnt, KS, n, e, c.template buf<T>(Q.hS), c.template buf<T>(Q.rawU), c.template buf<T>(Q.env_p),
+      acc, S, S_cnt, KS, n, moved, c.template buf<T>(Q.hS), c.template buf<T>(Q.rawU), c.template buf<T>(Q.env_p),
       c.template buf<T>(Q.aS), c.template buf<T>(Q.vS), c.template buf<T>(Q.oS), c.template buf<T>(Q.E5p),
       c.template buf<int>(Q.en_cnt_p), c.template buf<int>(Q.en_idx_p), c.template buf<int>(Q.counts_p),
       c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p), c.template buf<T>(c.P.B2X),
@@ -1426,8 +1439,8 @@ fire_status run_ecp(const fire_problem* p, cudaStream_t s, const float* R, const
       for (int k = 0; k < ecp.max_quad; ++k) {
         g_nlaunch++;
         k_ecp_point<T><<<c.Wc, 128, 0, s>>>(c.r, c.template buf<T>(c.P.rn), n, e, k, R, ecp, qt, w0, seed, counter,
-                                            reinterpret_cast<const T*>(rot), pt);
-        if (lr_evaluate<T>(c, Q, KS, rr, e, static_max, c.template buf<T>(Q.sgn_p)) != cudaSuccess)
+                                            reinterpret_cast<const T*>(rot), pt, c.template buf<int>(Q.moved));
+        if (lr_evaluate<T>(c, Q, KS, rr, static_max, c.template buf<T>(Q.sgn_p)) != cudaSuccess)
           return launch_status("pseudopotential ratio");
         g_nlaunch++;
         k_ecp_accum<T><<<nblk(c.Wc), 256, 0, s>>>(c.Wc, pt, c.template buf<T>(c.P.lpn), c.template buf<T>(Q.sgn_p),
@@ -1439,13 +1452,15 @@ fire_status run_ecp(const fire_problem* p, cudaStream_t s, const float* R, const
   return launch_status(__func__);
 }
 
-// Low-rank single-electron block (mcmc_steps_low_rank with proposal_single_electron): per chunk the state from one
-// value-path evaluation, then every step from the state.
+// Low-rank one-electron block (mcmc_steps_low_rank): per chunk the state from one value-path evaluation, then every
+// step from the state.  kind MC_SINGLE: proposal_single_electron (electron (offset + step) mod n moved by width
+// eps); MC_JUMP: proposal_jump_to_atom (a random electron per walker to a random nucleus, width = sigma, the
+// proposal's log ratio in the test).
 template <typename T>
 fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
                         void* r, void* logpsi, int steps, int offset, float width, int KS, uint64_t seed,
                         uint64_t counter, const void* noise, const void* logu, int32_t* n_accept,
-                        int32_t* static_max, void* ws, size_t wsb, int32_t* status) {
+                        int32_t* static_max, void* ws, size_t wsb, int32_t* status, int kind = MC_SINGLE) {
   const int Wc = choose_chunk_lr(p, wsb, KS);
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
@@ -1457,13 +1472,19 @@ fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, c
     c.Wc = std::min(Wc, p->n_walkers - w0);
     c.r = rr + (size_t)w0 * n * 3;
     if (chunk_state<T>(c, Q, logpsi, nullptr, w0) != cudaSuccess) return launch_status("low-rank state");
+    int* moved = c.template buf<int>(Q.moved);
+    T* plr = kind == MC_JUMP ? c.template buf<T>(c.P.plr) : nullptr;
     for (int st = 0; st < steps; ++st) {
       g_nlaunch++;
-      k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), n, w0,
-                                               p->n_walkers, st, offset, (T)width, seed, counter,
-                                               reinterpret_cast<const T*>(noise));
-      const int e = (int)(((long)offset + st) % n);
-      if (lr_step<T>(c, Q, KS, rr, logpsi, st, e, seed, counter, logu, n_accept, static_max) != cudaSuccess)
+      if (kind == MC_JUMP)
+        k_propose_jump<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), plr, n, w0,
+                                               p->n_walkers, st, R, Z, p->n_nuc, (T)width, seed, counter,
+                                               reinterpret_cast<const T*>(noise), moved);
+      else
+        k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), n, w0,
+                                                 p->n_walkers, st, offset, (T)width, seed, counter,
+                                                 reinterpret_cast<const T*>(noise), moved);
+      if (lr_step<T>(c, Q, KS, rr, logpsi, st, seed, counter, logu, n_accept, static_max, plr) != cudaSuccess)
         return launch_status("low-rank step");
     }
   }
@@ -1744,6 +1765,26 @@ fire_status fire_mcmc_low_rank_block(void* stream, const fire_problem* prob, con
                                replay_noise, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
   return run_mcmc_lr<float>(prob, s, R, Z, prepared, r, logpsi, steps, step_offset, width, KS, seed, counter,
                             replay_noise, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status);
+}
+
+fire_status fire_mcmc_low_rank_jump_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                          const void* prepared, void* r, void* logpsi, int32_t steps, float sigma,
+                                          int32_t cap_changed, uint64_t seed, uint64_t counter,
+                                          const void* replay_draws, const void* replay_log_u, int32_t* n_accept,
+                                          int32_t* static_max, void* workspace, size_t workspace_bytes,
+                                          int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || !(sigma > 0.f) ||
+      cap_changed < 1)
+    return FIRE_ERR_INVALID;
+  if ((replay_draws == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL || cap_changed > LR_KMAX) return FIRE_ERR_UNSUPPORTED;
+  const int KS = std::min<int>(cap_changed, prob->n_el);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_mcmc_lr<double>(prob, s, R, Z, prepared, r, logpsi, steps, 0, sigma, KS, seed, counter, replay_draws,
+                               replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
+  return run_mcmc_lr<float>(prob, s, R, Z, prepared, r, logpsi, steps, 0, sigma, KS, seed, counter, replay_draws,
+                            replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
 }
 
 fire_status fire_ecp_quadrature(int32_t n_points, double* points) {

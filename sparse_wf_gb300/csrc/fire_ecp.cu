@@ -50,12 +50,12 @@ __global__ void __launch_bounds__(256) k_ecp_local(const T* __restrict__ r, int 
 // a's grid has more than k points, electron e of rn moves to R_a + d (g_k rot), rot the walker's rotation for e:
 // replay [B][n][3][3] (rot[x][y]) or the Gram-Schmidt columns of two normal 3-vectors from Philox4x32-10.
 // pt [W][4] (double): the point's weight 1 / n_quad (0 when inactive), cos theta between g_k rot and r_e - R_a,
-// d, a.
+// d, a; moved [W] = e for the low-rank evaluation.
 template <typename T>
 __global__ void __launch_bounds__(128) k_ecp_point(const T* __restrict__ r, T* __restrict__ rn, int n, int e, int k,
                                                    const float* __restrict__ R, fire_ecp ecp, EcpQuad qt, int w0,
                                                    uint64_t seed, uint64_t counter, const T* __restrict__ replay,
-                                                   double* __restrict__ pt) {
+                                                   double* __restrict__ pt, int* __restrict__ moved) {
   const int w = blockIdx.x;
   const long gw = w0 + w;
   const T* src = r + (size_t)w * 3 * n;
@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(128) k_ecp_point(const T* __restrict__ r, T* _
   for (int q = threadIdx.x; q < 3 * n; q += blockDim.x) dst[q] = src[q];
   __syncthreads();
   if (threadIdx.x != 0) return;
+  moved[w] = e;
   const double ex = src[3 * e], ey = src[3 * e + 1], ez = src[3 * e + 2];
   int ab = 0;
   double db = 0.0;
@@ -92,7 +93,8 @@ __global__ void __launch_bounds__(128) k_ecp_point(const T* __restrict__ r, T* _
   } else {
     double u[6];
     for (int h = 0; h < 2; ++h) {
-      uint32_t ctr[4] = {(uint32_t)e, (uint32_t)gw, 0xFFFFFFFDu - (uint32_t)h, (uint32_t)counter};
+      // own counter domain (0xFFFFFFF0, 0xFFFFFFEF): the proposals use 0xFFFFFFFB .. 0xFFFFFFFF
+      uint32_t ctr[4] = {(uint32_t)e, (uint32_t)gw, 0xFFFFFFF0u - (uint32_t)h, (uint32_t)counter};
       philox10(ctr, seed ^ (counter >> 32) * 0x9E3779B97F4A7C15ull);
       const double r1 = sqrt(-2.0 * log(u01(ctr[0]))), t1 = 6.283185307179586 * u01(ctr[1]);
       const double r2 = sqrt(-2.0 * log(u01(ctr[2]))), t2 = 6.283185307179586 * u01(ctr[3]);
@@ -153,7 +155,7 @@ __global__ void k_ecp_store(int Wc, int w0, const double* __restrict__ acc, T* _
 #define FIRE_INST_ECP(T)                                                                                         \
   template __global__ void k_ecp_local<T>(const T*, int, const float*, fire_ecp, double*);                     \
   template __global__ void k_ecp_point<T>(const T*, T*, int, int, int, const float*, fire_ecp, EcpQuad, int,     \
-                                          uint64_t, uint64_t, const T*, double*);                              \
+                                          uint64_t, uint64_t, const T*, double*, int*);                        \
   template __global__ void k_ecp_accum<T>(int, const double*, const T*, const T*, const T*, const T*, fire_ecp, \
                                           double*);                                                            \
   template __global__ void k_ecp_store<T>(int, int, const double*, T*);

@@ -2,7 +2,8 @@
 // a state cached per walker instead of a full evaluation (log_psi_low_rank_update, model/wave_function.py:249-287,
 // driven by mcmc_steps_low_rank, mcmc.py:196-275).  The state is the value path's own buffers of the chunk (ElecInit
 // rows, embeddings, envelope / raw orbital / orbital-matrix rows, attention and MLP Jastrow rows, slogdets, e-n lists
-// and statics) plus the transposed inverse B = A^-T of every orbital matrix.  Per step, with e the moved electron:
+// and statics) plus the transposed inverse B = A^-T of every orbital matrix.  Per step, with e = moved[w] the electron
+// walker w moved:
 //
 //  k_lr_select  the changed set S (ascending): e and every electron within the cutoff of e before or after the move
 //               (get_low_rank_pair_indices, model/new_sparse_model.py:439-474); the proposal's statics
@@ -11,6 +12,8 @@
 //               and e's e-n list at its new position.
 //  k_lr_orb     the raw orbital rows of S, each from its spin's contraction (Orbitals.low_rank_update,
 //               orbitals.py:121-146).
+//  k_lr_env_coef, k_lr_env_add
+//               the envelope row of the moved electron at its new position, with its spin's envelope.
 //  k_lr_det     per walker and determinant: V = A'[S] - A[S], M = I + V A^-1[:, S], log|det M| and M^-1 by
 //               Gauss-Jordan with partial pivoting in FP64 (the determinant lemma of woodburry_update,
 //               model/utils.py:216-245).
@@ -29,12 +32,13 @@ constexpr int kAcc = LR_KMAX / 8;  // accumulators per thread of the Woodbury pr
 }  // namespace
 
 // One CTA (256 threads) per walker of the chunk.  r: the chunk's current positions; rn: the proposal (r with
-// electron e moved).  nb: the state's e-n counts [W][n] and statics [W][4].  Outputs S [W][KS] (the first KS
-// members), S_cnt [W] (the true size), re_p [W][3] (e's new position), en_cnt_p [W], en_idx_p [W][cap_nuc],
+// electron e = moved[w] moved).  nb: the state's e-n counts [W][n] and statics [W][4].  Outputs S [W][KS] (the first
+// KS members), S_cnt [W] (the true size), re_p [W][3] (e's new position), en_cnt_p [W], en_idx_p [W][cap_nuc],
 // counts_p [W][4] (the proposal's statics, triplets 0); static_max [7] entries 4..6 take the move statics.
 template <typename T>
 __global__ void __launch_bounds__(256) k_lr_select(const T* __restrict__ r, const T* __restrict__ rn, int n, int n_up,
-                                                   int e, const float* __restrict__ R, int N, T cutoff, T cutoff_1el,
+                                                   const int* __restrict__ moved, const float* __restrict__ R, int N,
+                                                   T cutoff, T cutoff_1el,
                                                    Nbr nb, int KS, int* __restrict__ S, int* __restrict__ S_cnt,
                                                    T* __restrict__ re_p, int* __restrict__ en_cnt_p,
                                                    int* __restrict__ en_idx_p, int* __restrict__ counts_p,
@@ -45,6 +49,7 @@ __global__ void __launch_bounds__(256) k_lr_select(const T* __restrict__ r, cons
   __shared__ int sS[LR_KMAX];
   __shared__ int ce_s;
   const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int e = moved[w];
   const unsigned lt = (1u << lane) - 1u;
   const T* ro = r + (size_t)w * n * 3;
   const T* rp = rn + (size_t)w * n * 3;
@@ -162,8 +167,43 @@ __global__ void __launch_bounds__(256) k_lr_orb(const int* __restrict__ S, const
   for (int q = threadIdx.x; q < DN; q += blockDim.x) rawU[row + q] = rawD[row + q];
 }
 
+// Envelope coefficients of each walker's moved electron e = moved[w] at its new position, with the softplus scales
+// of e's spin: coefU / coefD [NDET][W][N * 8] hold exp(-|r_e - R_I| sp[I][d][k]) for the walkers whose e is spin up /
+// down and zeros for the others, so that the two spins' contractions with their own envelope weights add up to e's
+// row.  One thread per (walker, nucleus, k).
+template <typename T>
+__global__ void k_lr_env_coef(const T* __restrict__ rn, const float* __restrict__ R, const T* __restrict__ sp_up,
+                              const T* __restrict__ sp_dn, const int* __restrict__ moved, int n, int n_up, int N,
+                              int Wc, T* __restrict__ coefU, T* __restrict__ coefD) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)Wc * N * NENV_ORB) return;
+  const int k = (int)(idx % NENV_ORB), I = (int)((idx / NENV_ORB) % N), w = (int)(idx / ((long)NENV_ORB * N));
+  const int e = moved[w];
+  const bool up = e < n_up;
+  const T* x = rn + ((size_t)w * n + e) * 3;
+  const T dx = x[0] - (T)R[3 * I], dy = x[1] - (T)R[3 * I + 1], dz = x[2] - (T)R[3 * I + 2];
+  const T rho = dsqrt(dx * dx + dy * dy + dz * dz);
+  const int K8 = N * NENV_ORB;
+  const T* sp = up ? sp_up : sp_dn;
+#pragma unroll
+  for (int d = 0; d < NDET; ++d) {
+    const long o = ((long)d * Wc + w) * K8 + I * NENV_ORB + k;
+    const T v = dexp(-sp[(I * NDET + d) * NENV_ORB + k] * rho);
+    coefU[o] = up ? v : T(0);
+    coefD[o] = up ? T(0) : v;
+  }
+}
+
+// env_p [W][DN] += env_d [W][DN]: the spin-down contraction added to the spin-up one (one of the two is zero).
+template <typename T>
+__global__ void k_lr_env_add(long total, T* __restrict__ env_p, const T* __restrict__ env_d) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total) env_p[i] += env_d[i];
+}
+
 // One CTA (256 threads) per (determinant d, walker w).  rawS [W][KS][DN]: raw orbital rows of S; env, Apl
-// [W][n][DN]: the state's envelope and orbital-matrix rows; env_p [W][DN]: e's envelope row after the move.  B: the
+// [W][n][DN]: the state's envelope and orbital-matrix rows; env_p [W][DN]: the envelope row of the moved electron
+// e = moved[w] after the move.  B: the
 // transposed inverse, B[((w NDET + d) n + i) nA + sh + o] = (A^-1)[o][i] with nA = ainv_ld(n), sh = (d n) mod 4.
 // Writes V [W][NDET][KS][n] (A'[S] - A[S]), Minv [W][NDET][KS][KS] (double) and the proposal's slogdet
 // (ld_p, sd_p) = (ld + log|det M|, sd sign(det M)).  A set larger than KS (flagged by k_lr_select) gives sign 0:
@@ -171,7 +211,8 @@ __global__ void __launch_bounds__(256) k_lr_orb(const int* __restrict__ S, const
 // of T (the staged V and B[S] columns).
 template <typename T>
 __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const int* __restrict__ S_cnt, int KS,
-                                                int n, int e, const T* __restrict__ rawS, const T* __restrict__ env,
+                                                int n, const int* __restrict__ moved, const T* __restrict__ rawS,
+                                                const T* __restrict__ env,
                                                 const T* __restrict__ env_p, const T* __restrict__ Apl,
                                                 const T* __restrict__ B, const double* __restrict__ ld,
                                                 const double* __restrict__ sd, T* __restrict__ V,
@@ -186,7 +227,7 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
   __shared__ double fac[LR_KMAX];
   __shared__ int piv_row;
   const int d = blockIdx.x, w = blockIdx.y, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int cnt = S_cnt[w];
+  const int e = moved[w], cnt = S_cnt[w];
   const size_t md = (size_t)w * NDET + d;
   if (cnt > KS) {
     if (tid == 0) {
@@ -371,7 +412,8 @@ __global__ void __launch_bounds__(256) k_lr_jsums(int n, int n_up, const int* __
 // block KS: the moved electron's ElecInit and envelope rows, its e-n list, the statics and the slogdets.
 template <typename T>
 __global__ void __launch_bounds__(256) k_lr_commit(const int* __restrict__ accf, const int* __restrict__ S,
-                                                   const int* __restrict__ S_cnt, int KS, int n, int e,
+                                                   const int* __restrict__ S_cnt, int KS, int n,
+                                                   const int* __restrict__ moved,
                                                    const T* __restrict__ hS, const T* __restrict__ rawS,
                                                    const T* __restrict__ env_p, const T* __restrict__ aS,
                                                    const T* __restrict__ vS, const T* __restrict__ oS,
@@ -384,7 +426,7 @@ __global__ void __launch_bounds__(256) k_lr_commit(const int* __restrict__ accf,
                                                    double* __restrict__ ld, double* __restrict__ sd) {
   const int slot = blockIdx.x, w = blockIdx.y, tid = threadIdx.x;
   if (!accf[w]) return;
-  const int DN = NDET * n;
+  const int DN = NDET * n, e = moved[w];
   if (slot == KS) {
     const size_t g = (size_t)w * n + e;
     for (int q = tid; q < 5 * F; q += blockDim.x) E5o[g * 5 * F + q] = E5p[(size_t)w * 5 * F + q];
@@ -555,14 +597,18 @@ __global__ void __launch_bounds__(256) k_lr_wb_apply(const int* __restrict__ acc
 }
 
 #define FIRE_INST_LR(T)                                                                                             \
-  template __global__ void k_lr_select<T>(const T*, const T*, int, int, int, const float*, int, T, T, Nbr, int, int*, \
-                                          int*, T*, int*, int*, int*, int32_t*, int32_t*);                           \
+  template __global__ void k_lr_select<T>(const T*, const T*, int, int, const int*, const float*, int, T, T, Nbr, int, \
+                                          int*, int*, T*, int*, int*, int*, int32_t*, int32_t*);                     \
+  template __global__ void k_lr_env_coef<T>(const T*, const float*, const T*, const T*, const int*, int, int, int, int,  \
+                                            T*, T*);                                                                  \
+  template __global__ void k_lr_env_add<T>(long, T*, const T*);                                                      \
   template __global__ void k_lr_orb<T>(const int*, const int*, int, int, int, T*, const T*);                         \
-  template __global__ void k_lr_det<T>(const int*, const int*, int, int, int, const T*, const T*, const T*, const T*, \
-                                       const T*, const double*, const double*, T*, double*, double*, double*);       \
+  template __global__ void k_lr_det<T>(const int*, const int*, int, int, const int*, const T*, const T*, const T*,   \
+                                       const T*, const T*, const double*, const double*, T*, double*, double*,       \
+                                       double*);                                                                      \
   template __global__ void k_lr_jsums<T>(int, int, const int*, const int*, int, const T*, const T*, const T*,        \
                                          const T*, const T*, const T*, T*, T*);                                       \
-  template __global__ void k_lr_commit<T>(const int*, const int*, const int*, int, int, int, const T*, const T*,     \
+  template __global__ void k_lr_commit<T>(const int*, const int*, const int*, int, int, const int*, const T*, const T*, \
                                           const T*, const T*, const T*, const T*, const T*, const int*, const int*,   \
                                           const int*, const double*, const double*, T*, T*, T*, T*, T*, T*, T*, T*, \
                                           Nbr, double*, double*);                                                     \

@@ -38,10 +38,11 @@ __global__ void k_propose(const T* __restrict__ r, T* __restrict__ rn, int n, in
 
 // Single-electron proposal (proposal_single_electron, mcmc.py:100-111): r_new = r with electron
 // (offset + step) mod n moved by width * eps, eps [3] per walker and step; one CTA per walker of the chunk.
-// replay [steps, B, 3].
+// replay [steps, B, 3]; moved (may be null) receives the moved electron of every walker of the chunk.
 template <typename T>
 __global__ void k_propose_single(const T* __restrict__ r, T* __restrict__ rn, int n, int w0, int B, int step,
-                                 int offset, T width, uint64_t seed, uint64_t counter, const T* __restrict__ replay) {
+                                 int offset, T width, uint64_t seed, uint64_t counter, const T* __restrict__ replay,
+                                 int* __restrict__ moved) {
   const int w = blockIdx.x;
   const long gw = w0 + w;
   const T* src = r + (long)w * 3 * n;
@@ -50,6 +51,7 @@ __global__ void k_propose_single(const T* __restrict__ r, T* __restrict__ rn, in
   __syncthreads();
   if (threadIdx.x == 0) {
     const int e = (int)(((long)offset + step) % n);
+    if (moved) moved[w] = e;
     T eps[3];
     if (replay) {
       const T* q = replay + ((long)step * B + gw) * 3;
@@ -72,11 +74,13 @@ __global__ void k_propose_single(const T* __restrict__ r, T* __restrict__ rn, in
 // R_I + sigma * eps around a nucleus I drawn with probability Z_I / sum Z; plr[w] receives the proposal's
 // log ratio log(q(r_old) / q(r_new)), q(x) = sum_J Z_J exp(-|x - R_J|^2 / (2 sigma^2)).  Draws per walker
 // and step: d = (u_electron, u_nucleus, eps_x, eps_y, eps_z); electron = min(floor(u_e n), n - 1), nucleus =
-// the first J with cumulative charge > u_n sum Z.  replay [steps, B, 5]; one CTA per walker of the chunk.
+// the first J with cumulative charge > u_n sum Z.  replay [steps, B, 5]; moved (may be null) receives the jumped
+// electron of every walker of the chunk; one CTA per walker of the chunk.
 template <typename T>
 __global__ void k_propose_jump(const T* __restrict__ r, T* __restrict__ rn, T* __restrict__ plr, int n, int w0,
                                int B, int step, const float* __restrict__ R, const float* __restrict__ Z, int N,
-                               T sigma, uint64_t seed, uint64_t counter, const T* __restrict__ replay) {
+                               T sigma, uint64_t seed, uint64_t counter, const T* __restrict__ replay,
+                               int* __restrict__ moved) {
   const int w = blockIdx.x;
   const long gw = w0 + w;
   const T* src = r + (long)w * 3 * n;
@@ -116,6 +120,7 @@ __global__ void k_propose_jump(const T* __restrict__ r, T* __restrict__ rn, T* _
     }
     sel[0] = e;
     sel[1] = I;
+    if (moved) moved[w] = e;
   }
   __syncthreads();
   const int e = sel[0], I = sel[1];
@@ -324,13 +329,13 @@ template __global__ void k_propose<float>(const float*, float*, int, int, int, i
 template __global__ void k_propose<double>(const double*, double*, int, int, int, int, int, double, uint64_t,
                                            uint64_t, const double*);
 template __global__ void k_propose_single<float>(const float*, float*, int, int, int, int, int, float, uint64_t,
-                                                 uint64_t, const float*);
+                                                 uint64_t, const float*, int*);
 template __global__ void k_propose_single<double>(const double*, double*, int, int, int, int, int, double,
-                                                  uint64_t, uint64_t, const double*);
+                                                  uint64_t, uint64_t, const double*, int*);
 template __global__ void k_propose_jump<float>(const float*, float*, float*, int, int, int, int, const float*,
-                                               const float*, int, float, uint64_t, uint64_t, const float*);
+                                               const float*, int, float, uint64_t, uint64_t, const float*, int*);
 template __global__ void k_propose_jump<double>(const double*, double*, double*, int, int, int, int, const float*,
-                                                const float*, int, double, uint64_t, uint64_t, const double*);
+                                                const float*, int, double, uint64_t, uint64_t, const double*, int*);
 template __global__ void k_propose_cluster<float>(const float*, float*, float*, int, int, int, int, int, int, float,
                                                   float, int, uint64_t, uint64_t, const float*);
 template __global__ void k_propose_cluster<double>(const double*, double*, double*, int, int, int, int, int, int,

@@ -384,6 +384,55 @@ class FireWaveFunction:
         sm = smax.cpu().numpy()
         return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3]))
 
+    def _low_rank(self, fn_name, r, logpsi, static: StaticArgs, cap_changed, launch):
+        """Runs a low-rank block, launch(lib_fn, prob, ws, cap, n_acc, smax), with the reruns it needs: from the
+        original walkers and log|psi| after a pair / e-n overflow (grown neighbour capacities) or a changed-set
+        overflow (the set the device saw, padded by 10 %; above the limit an error).  Keeps the capacity for the
+        next call.  Returns (n_accept per walker, static_max, move statics)."""
+        assert r.is_contiguous() and r.dtype == self.dtype
+        B, n = r.shape[0], self.n_electrons
+        n_acc = torch.zeros(B, dtype=torch.int32, device=self.device)
+        smax = torch.zeros(7, dtype=torch.int32, device=self.device)
+        r0 = r.clone()
+        lp0 = logpsi.clone()
+        limit = min(n, _lib.LOW_RANK_MAX_CHANGED)
+        if cap_changed is None:
+            # the moved electron and its neighbours before and after the move: about twice the mean degree, >= 16
+            cap_changed = self._lr_cap or max(16, 2 * static.n_pairs // max(1, n) + 1)
+        cap = min(int(cap_changed), limit)
+        fn = getattr(_lib.load(), fn_name)
+        for _ in range(6):
+            self._status.zero_()
+            r.copy_(r0)
+            logpsi.copy_(lp0)
+            n_acc.zero_()
+            smax.zero_()
+            prob = self._problem(B, static)
+            _lib.check(launch(fn, prob, self._workspace(prob, cap), cap, n_acc, smax), fn_name)
+            st = self._read_status()
+            flags = int(st[0])
+            if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
+                static = self._grown(st, static)
+                continue
+            if flags & _lib.FLAG_CHANGED_OVERFLOW:
+                need = int(st[4])
+                if need > limit:
+                    raise RuntimeError(f"a changed set of {need} electrons exceeds the low-rank block's limit of "
+                                       f"{limit}; use the full-evaluation block")
+                cap = min(limit, max(need, int(need * 1.1) + 1))
+                continue
+            break
+        else:
+            raise RuntimeError("low-rank capacities did not converge")
+        self._lr_cap = cap
+        sm = smax.cpu().numpy()
+        return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3])), (int(sm[4]), int(sm[5]), int(sm[6]))
+
+    def _replay(self, arr, shape):
+        if arr is None:
+            return None
+        return torch.as_tensor(np.asarray(arr)).to(self.device, self.dtype).reshape(shape).contiguous()
+
     def mcmc_low_rank_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
                             steps: int, width: float, step_offset: int = 0, seed: int = 0, counter: int = 0,
                             replay_noise=None, replay_log_u=None, cap_changed: Optional[int] = None):
@@ -397,57 +446,45 @@ class FireWaveFunction:
         capacity is kept for the next call.  Returns (n_accept per walker, static_max, (n_changed_hout,
         n_changed_pair_same, n_changed_pair_diff)) with the maxima over steps and walkers."""
         p = self._params(params)
-        r = electrons
-        assert r.is_contiguous() and r.dtype == self.dtype
-        B, n = r.shape[0], self.n_electrons
-        n_acc = torch.zeros(B, dtype=torch.int32, device=self.device)
-        smax = torch.zeros(7, dtype=torch.int32, device=self.device)
-        noise = None
-        if replay_noise is not None:
-            noise = torch.as_tensor(np.asarray(replay_noise)).to(self.device, self.dtype).reshape(steps, B, 3).contiguous()
-        logu = None if replay_log_u is None else torch.as_tensor(replay_log_u).to(self.device, self.dtype).contiguous()
-        r0 = r.clone()
-        lp0 = logpsi.clone()
-        limit = min(n, _lib.LOW_RANK_MAX_CHANGED)
-        if cap_changed is None:
-            # e and its neighbours before and after the move: about twice the mean degree, at least 16
-            cap_changed = self._lr_cap or max(16, 2 * static.n_pairs // max(1, n) + 1)
-        cap = min(int(cap_changed), limit)
-        lib = _lib.load()
-        for _ in range(6):
-            self._status.zero_()
-            r.copy_(r0)
-            logpsi.copy_(lp0)
-            n_acc.zero_()
-            smax.zero_()
-            prob = self._problem(B, static)
-            ws = self._workspace(prob, cap)
-            _lib.check(lib.fire_mcmc_low_rank_block(
-                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
-                C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(logpsi.data_ptr()),
-                int(steps), int(step_offset), float(width), int(cap), C.c_uint64(seed), C.c_uint64(counter),
-                C.c_void_p(noise.data_ptr()) if noise is not None else None,
-                C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
-                C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
-                C.c_void_p(self._status.data_ptr())), "fire_mcmc_low_rank_block")
-            st = self._read_status()
-            flags = int(st[0])
-            if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
-                static = self._grown(st, static)
-                continue
-            if flags & _lib.FLAG_CHANGED_OVERFLOW:
-                need = int(st[4])
-                if need > limit:
-                    raise RuntimeError(f"a changed set of {need} electrons exceeds the low-rank block's limit of "
-                                       f"{limit}; use mcmc_single_block")
-                cap = min(limit, max(need, int(need * 1.1) + 1))
-                continue
-            break
-        else:
-            raise RuntimeError("low-rank capacities did not converge")
-        self._lr_cap = cap
-        sm = smax.cpu().numpy()
-        return n_acc, StaticArgs(int(sm[0]), int(sm[1]), 0, int(sm[3])), (int(sm[4]), int(sm[5]), int(sm[6]))
+        B = electrons.shape[0]
+        noise = self._replay(replay_noise, (steps, B, 3))
+        logu = self._replay(replay_log_u, (steps, B))
+
+        def launch(fn, prob, ws, cap, n_acc, smax):
+            return fn(self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()),
+                      C.c_void_p(self.Z_dev.data_ptr()), C.c_void_p(p.prepared.data_ptr()),
+                      C.c_void_p(electrons.data_ptr()), C.c_void_p(logpsi.data_ptr()), int(steps), int(step_offset),
+                      float(width), int(cap), C.c_uint64(seed), C.c_uint64(counter),
+                      C.c_void_p(noise.data_ptr()) if noise is not None else None,
+                      C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                      C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                      C.c_void_p(self._status.data_ptr()))
+
+        return self._low_rank("fire_mcmc_low_rank_block", electrons, logpsi, static, cap_changed, launch)
+
+    def mcmc_low_rank_jump_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
+                                 steps: int, sigma: float = 2.0, seed: int = 0, counter: int = 0, replay_draws=None,
+                                 replay_log_u=None, cap_changed: Optional[int] = None):
+        """In-place Metropolis block of jumps to the nuclei (``proposal_jump_to_atom``, ``mcmc.py:164-193``) evaluated
+        by the low-rank update of a cached state: the proposals, draws (replay_draws [steps, B, 5]) and acceptance of
+        ``mcmc_jump_block``, each walker moving its own electron.  Outputs and capacities as
+        ``mcmc_low_rank_block``."""
+        p = self._params(params)
+        B = electrons.shape[0]
+        draws = self._replay(replay_draws, (steps, B, 5))
+        logu = self._replay(replay_log_u, (steps, B))
+
+        def launch(fn, prob, ws, cap, n_acc, smax):
+            return fn(self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()),
+                      C.c_void_p(self.Z_dev.data_ptr()), C.c_void_p(p.prepared.data_ptr()),
+                      C.c_void_p(electrons.data_ptr()), C.c_void_p(logpsi.data_ptr()), int(steps), float(sigma),
+                      int(cap), C.c_uint64(seed), C.c_uint64(counter),
+                      C.c_void_p(draws.data_ptr()) if draws is not None else None,
+                      C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                      C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                      C.c_void_p(self._status.data_ptr()))
+
+        return self._low_rank("fire_mcmc_low_rank_jump_block", electrons, logpsi, static, cap_changed, launch)
 
     def ecp_energy(self, params, electrons, static: StaticArgs, ecp, seed: int = 0, counter: int = 0,
                    replay_rotations=None, cap_changed: Optional[int] = None):

@@ -142,3 +142,32 @@ def test_ecp_energy_matches_oracle(cuda_lib):
         ref = E.local_term(ecp, r[w]) + E.nonlocal_term(prob, p, ecp, r[w], rot[w])
         assert abs(got[w].item() - ref) <= 1e-8 * max(1.0, abs(ref)), w
     assert changed[0] >= 1
+
+
+@pytest.mark.parametrize("name", ["h10", "c2h6"])
+def test_low_rank_jump_block_matches_oracle(cuda_lib, name):
+    """FP64 build: jumps to the nuclei evaluated from the state (fire_mcmc_low_rank_jump_block, each walker moving its
+    own electron) take the oracle's decisions (mcmc_jump_block, full evaluations) wherever the margin is clear of
+    rounding, with the same final positions (1e-12) and log|psi| (1e-8 relative)."""
+    wf, mol, nu, r, p, rr, static = _setup(name, "fp64")
+    B = r.shape[0]
+    steps, sigma = 12, 2.0
+    rng = np.random.default_rng(41)
+    draws = np.concatenate([rng.uniform(size=(steps, B, 2)), rng.standard_normal((steps, B, 3))], axis=2)
+    logu = np.log(rng.uniform(size=(steps, B)))
+    dp = wf._params(p)
+    logpsi = torch.zeros(B, dtype=torch.float64, device="cuda")
+    n_acc, _, changed = wf.mcmc_low_rank_jump_block(dp, rr, logpsi, static, steps, sigma, replay_draws=draws,
+                                                    replay_log_u=logu)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    got_r, got_n = rr.cpu().numpy(), n_acc.cpu().numpy()
+    checked = 0
+    for w in range(B):
+        r_ref, lp_ref, na, mg = O.mcmc_jump_block(prob, p, r[w].astype(np.float64), draws[:, w], logu[:, w],
+                                                  float(np.float32(sigma)))
+        if np.all(np.abs(mg[np.isfinite(mg)]) > 1e-6):
+            checked += 1
+            assert got_n[w] == na, w
+            np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
+            np.testing.assert_allclose(logpsi[w].item(), 0.5 * lp_ref, rtol=1e-8)
+    assert checked > 0 and changed[0] >= 1
