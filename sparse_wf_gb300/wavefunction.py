@@ -674,13 +674,15 @@ def make_width_scheduler(window_size: int = 20, target_pmove: float = 0.5, error
 
 def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, proposal: str = "all-electron",
               sweeps: float = 2.0, jump_steps: int = 0, max_cluster_size: int = 5, max_cluster_radius: float = 2.0,
-              sweep_type: str = "sequential"):
+              sweep_type: str = "sequential", low_rank: bool = False):
     """``make_mcmc`` (``mcmc.py:278-346``) for the "all-electron" proposal (``steps`` moves of every electron) and
     the "single-electron" proposal (``int(sweeps * n_el)`` one-electron moves in sequential order, the reference's
     default; ``init_width`` 0.5 there, ``config/default.yaml``), preceded by ``jump_steps`` jumps to the nuclei
     (sigma 2, ``mcmc.py:320-326, 332-335``; 20 in the reference's defaults); "cluster-update" runs
     ``int(sweeps * n_el)`` cluster moves (``mcmc.py:305-316``; sequential sweeps must be whole):
-    ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed."""
+    ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed.  low_rank
+    evaluates the single-electron moves and the jumps from a state per walker (``mcmc_low_rank_block``,
+    ``mcmc_low_rank_jump_block``) instead of in full; stats then also hold the move statics."""
     proposal = proposal.lower()
     if proposal not in ("all-electron", "single-electron", "cluster-update"):
         raise ValueError(f"Invalid proposal: {proposal}")
@@ -697,7 +699,12 @@ def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, pr
         _, logpsi = wf.signed(p, r, static)
         stats = {}
         if jump_steps > 0:  # the reference keeps the jump block's statics apart (static_max["mcmc_jump"])
-            n_jump, smax_jump = wf.mcmc_jump_block(p, r, logpsi, static, jump_steps, 2.0, seed=int(key), counter=1)
+            if low_rank:
+                n_jump, smax_jump, stats["changed_max_jump"] = wf.mcmc_low_rank_jump_block(
+                    p, r, logpsi, static, jump_steps, 2.0, seed=int(key), counter=1)
+            else:
+                n_jump, smax_jump = wf.mcmc_jump_block(p, r, logpsi, static, jump_steps, 2.0, seed=int(key),
+                                                       counter=1)
             stats["pmove_jump"] = float(n_jump.float().mean().item()) / jump_steps
             stats["static_max_jump"] = smax_jump
         if proposal == "all-electron":
@@ -705,6 +712,9 @@ def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, pr
         elif proposal == "cluster-update":
             n_acc, smax = wf.mcmc_cluster_block(p, r, logpsi, static, n_steps, float(width), max_cluster_size,
                                                 max_cluster_radius, sweep_type, seed=int(key))
+        elif low_rank:
+            n_acc, smax, stats["changed_max"] = wf.mcmc_low_rank_block(p, r, logpsi, static, n_steps, float(width),
+                                                                       seed=int(key))
         else:
             n_acc, smax = wf.mcmc_single_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
         stats.update(pmove=float(n_acc.float().mean().item()) / max(n_steps, 1), static_max=smax, stepsize=width)

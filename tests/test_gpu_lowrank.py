@@ -171,3 +171,18 @@ def test_low_rank_jump_block_matches_oracle(cuda_lib, name):
             np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
             np.testing.assert_allclose(logpsi[w].item(), 0.5 * lp_ref, rtol=1e-8)
     assert checked > 0 and changed[0] >= 1
+
+
+def test_make_mcmc_low_rank_matches_full(cuda_lib):
+    """make_mcmc(low_rank=True) with jumps and single-electron moves: the same chain as the full-evaluation blocks
+    (Philox draws, FP64 build) up to walkers whose decisions sit within rounding of the threshold."""
+    from sparse_wf_gb300.wavefunction import make_mcmc
+
+    wf, mol, nu, r, p, rr, static = _setup("h10", "fp64")
+    full, _ = make_mcmc(wf, proposal="single-electron", sweeps=1.0, jump_steps=4, init_width=0.3)
+    lowr, _ = make_mcmc(wf, proposal="single-electron", sweeps=1.0, jump_steps=4, init_width=0.3, low_rank=True)
+    ra, sa = full(7, p, rr, static, 0.3)
+    rb, sb = lowr(7, p, rr, static, 0.3)
+    same = np.all(np.abs(ra.cpu().numpy() - rb.cpu().numpy()) < 1e-10, axis=(1, 2))
+    assert same.sum() >= len(same) - 1
+    assert sb["changed_max"][0] >= 1 and sb["changed_max_jump"][0] >= 1
