@@ -328,3 +328,28 @@ def test_low_rank_wrapper_rejects_sets_beyond_the_limit(monkeypatch):
     wf, mol, r = _fake_wf(monkeypatch, fake)
     with pytest.raises(RuntimeError, match="limit of 18"):
         wf.mcmc_low_rank_block(P.init_params(wf.dims, 0), r, torch.zeros(2), StaticArgs(40, 40, 0, 8), 5, 0.5)
+
+
+def test_low_rank_jump_and_ecp_argument_checks(lib):
+    """fire_mcmc_low_rank_jump_block and fire_ecp_energy reject bad arguments before any CUDA call, through the
+    declared ctypes signatures (pointers never dereferenced): a non-positive sigma, a zero or too large capacity,
+    a missing or malformed fire_ecp (more than 4 non-local channels, a quadrature above 12 points, a one-point grid)."""
+    prob = _lib.Problem(82, 41, 32, 4, 5.0, 20.0, 2500, 40, 0, 0)
+    d = C.c_void_p(16)
+
+    def jump(sigma, cap):
+        return lib.fire_mcmc_low_rank_jump_block(None, C.byref(prob), d, d, d, d, d, 4, sigma, cap, 0, 0, None, None,
+                                                 None, None, d, C.c_size_t(1), d)
+
+    assert jump(0.0, 32) == 1 and jump(2.0, 0) == 1 and jump(2.0, 129) == 2
+
+    def ecp(**kw):
+        f = dict(n_ecp=2, n_grid=100, n_l=2, max_quad=4)
+        f.update(kw)
+        e = _lib.Ecp(f["n_ecp"], f["n_grid"], f["n_l"], f["max_quad"], d, d, d, d, d, d)
+        return lib.fire_ecp_energy(None, C.byref(prob), d, d, d, d, C.byref(e), 32, 0, 0, None, d, None, d,
+                                   C.c_size_t(1), d)
+
+    assert lib.fire_ecp_energy(None, C.byref(prob), d, d, d, d, None, 32, 0, 0, None, d, None, d, C.c_size_t(1),
+                               d) == 1
+    assert ecp(n_l=5) == 1 and ecp(max_quad=13) == 1 and ecp(n_grid=1) == 1 and ecp(n_ecp=0) == 1
