@@ -26,6 +26,7 @@
  *   fire_mcmc_low_rank_block  mcmc.py:100-111, 196-275 with model/wave_function.py:226-287
  *                       log_psi_with_state / log_psi_low_rank_update (the state-carrying single-electron block)
  *   fire_mcmc_low_rank_jump_block  mcmc.py:164-193 proposal_jump_to_atom with the low-rank state
+ *   fire_mcmc_low_rank_cluster_block  mcmc.py:119-161 proposal_cluster_update with the low-rank state
  *   fire_ecp_energy     pseudopotentials.py:205-219, 272-398 local and non-local pseudopotential terms
  *   fire_embedding      model/new_sparse_model.py:483-551 NewSparseEmbedding.apply
  *                       (used by the initialiser, new_sparse_model.py:378-379)
@@ -305,6 +306,19 @@ fire_status fire_mcmc_low_rank_jump_block(void* stream, const fire_problem* prob
                                           const void* replay_draws, const void* replay_log_u, int32_t* n_accept,
                                           int32_t* static_max, void* workspace, size_t workspace_bytes,
                                           int32_t* status);
+
+/* Metropolis block of cluster updates (proposal_cluster_update, mcmc.py:119-161, make_mcmc "cluster-update",
+ * mcmc.py:305-316) evaluated by the low-rank update of a cached state: the proposals, draws and replay of
+ * fire_mcmc_cluster_block, the moved set being the cluster's index list (the center's k closest electrons, those
+ * beyond max_cluster_radius padded, whose padding enters the move statics like an out-of-range JAX gather: as
+ * electron n - 1).  State, capacity, workspace and static_max [7] as fire_mcmc_low_rank_block. */
+fire_status fire_mcmc_low_rank_cluster_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                             const void* prepared, void* r, void* logpsi, int32_t steps,
+                                             int32_t step_offset, float width, int32_t max_cluster_size,
+                                             float max_cluster_radius, int32_t random_sweep, int32_t cap_changed,
+                                             uint64_t seed, uint64_t counter, const void* replay_draws,
+                                             const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
+                                             void* workspace, size_t workspace_bytes, int32_t* status);
 
 /* The unit-sphere quadrature of n_points (1, 2, 4, 6 or 12) points fire_ecp_energy uses (make_spherical_grid,
  * pseudopotentials.py:44-133), points [n_points, 3] (host, float64); equal weights 1 / n_points.  Host only. */

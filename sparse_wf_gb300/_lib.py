@@ -32,6 +32,7 @@ SYMBOLS = [
     "fire_embedding", "fire_mcmc_block", "fire_potential_energy", "fire_profile_enable", "fire_profile_report",
     "fire_gemm_mixed", "fire_triplets_static", "fire_mcmc_single_block", "fire_mcmc_jump_block",
     "fire_mcmc_cluster_block", "fire_low_rank_workspace_size", "fire_mcmc_low_rank_block", "fire_mcmc_low_rank_jump_block",
+    "fire_mcmc_low_rank_cluster_block",
     "fire_ecp_quadrature",
     "fire_ecp_energy",
 ]
@@ -95,6 +96,8 @@ def load() -> C.CDLL:
                                       vp], i32),
         "fire_mcmc_low_rank_jump_block": ([vp, P, vp, vp, vp, vp, vp, i32, f32, i32, u64, u64, vp, vp, vp, vp, vp,
                                            sz, vp], i32),
+        "fire_mcmc_low_rank_cluster_block": ([vp, P, vp, vp, vp, vp, vp, i32, i32, f32, i32, f32, i32, i32, u64, u64,
+                                              vp, vp, vp, vp, vp, sz, vp], i32),
         "fire_ecp_quadrature": ([i32, C.POINTER(C.c_double)], i32),
         "fire_ecp_energy": ([vp, P, vp, vp, vp, vp, C.POINTER(Ecp), i32, u64, u64, vp, vp, vp, vp, sz, vp], i32),
         "fire_potential_energy": ([vp, P, vp, vp, vp, vp], i32),

@@ -1045,7 +1045,7 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
       else if (kind == MC_CLUSTER)
         k_propose_cluster<T><<<c.Wc, 32, 0, s>>>(rr + (size_t)w0 * n * 3, rn, plr, n, w0, p->n_walkers, st, offset, ck,
                                                  (T)cradius, (T)width, crandom, seed, counter,
-                                                 reinterpret_cast<const T*>(noise));
+                                                 reinterpret_cast<const T*>(noise), nullptr);
       else if (kind == MC_JUMP)
         k_propose_jump<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, rn, plr, n, w0, p->n_walkers, st, R, Z,
                                                p->n_nuc, (T)width, seed, counter, reinterpret_cast<const T*>(noise),
@@ -1092,24 +1092,25 @@ LrPlan make_lr_plan(const fire_problem* p, int Wc, int KS) {
   };
   take(Q.vals, G * F, es);
   take(Q.B, W * NDET * n * (size_t)ainv_ld((int)n), es);
+  const size_t WM = W * CLUSTER_KMAX;  // moved slots: one per walker, up to a cluster's size
   take(Q.S, R, 4);
   take(Q.S_cnt, W, 4);
-  take(Q.en_cnt_p, W, 4);
-  take(Q.en_idx_p, W * p->cap_nuc, 4);
+  take(Q.en_cnt_p, WM, 4);
+  take(Q.en_idx_p, WM * p->cap_nuc, 4);
   take(Q.counts_p, W * 4, 4);
   take(Q.acc, W, 4);
-  take(Q.moved, W, 4);
-  take(Q.re_p, W * 3, es);
-  take(Q.E5p, W * 5 * F, es);
+  take(Q.moved, WM, 4);
+  take(Q.re_p, WM * 3, es);
+  take(Q.E5p, WM * 5 * F, es);
   take(Q.HS, R * F, es);
   take(Q.B1S, R * F, es);
   take(Q.hS, R * F, es);
   take(Q.rawU, R * DN, es);
   take(Q.rawD, R * DN, es);
-  take(Q.coefE, NDET * W * K8, es);
-  take(Q.coefD, NDET * W * K8, es);
-  take(Q.env_p, W * DN, es);
-  take(Q.env_pD, W * DN, es);
+  take(Q.coefE, NDET * WM * K8, es);
+  take(Q.coefD, NDET * WM * K8, es);
+  take(Q.env_p, WM * DN, es);
+  take(Q.env_pD, WM * DN, es);
   take(Q.aS, R * HEADS, es);
   take(Q.vS, R * F, es);
   take(Q.oS, R * 2, es);
@@ -1195,10 +1196,10 @@ cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi, void* sign, in
 }
 
 // log|psi'| (into c.P.lpn) and its sign (into sgn_out, may be null) of the chunk's proposal c.P.rn, in which walker w
-// moved electron moved[w] (the plan's moved buffer), from the state; the proposal's rows stay in the plan's scratch
-// for the commit.
+// moved the electrons moved[w][0..KM) (the plan's moved buffer, padded with FIRE_NO_NEIGHBOUR), from the state; the
+// proposal's rows stay in the plan's scratch for the commit.
 template <typename T>
-cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int32_t* static_max, T* sgn_out) {
+cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, int32_t* static_max, T* sgn_out) {
   const fire_problem* p = c.p;
   const int n = p->n_el, nu = p->n_up, N = p->n_nuc, Wc = c.Wc, DN = NDET * n, rows = Wc * KS;
   const int K8 = N * NENV_ORB;
@@ -1210,39 +1211,40 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int32_t* stat
   const int* moved = c.template buf<int>(Q.moved);
   Prof pr("low_rank_step", s);
   g_nlaunch++;
-  k_lr_select<T><<<Wc, 256, 0, s>>>(r_chunk, rn, n, nu, moved, c.R, N, (T)p->cutoff, (T)p->cutoff_1el, c.nb, KS, S,
+  k_lr_select<T><<<Wc, 256, 0, s>>>(r_chunk, rn, n, nu, moved, KM, c.R, N, (T)p->cutoff, (T)p->cutoff_1el, c.nb, KS, S,
                                     S_cnt, c.template buf<T>(Q.re_p), c.template buf<int>(Q.en_cnt_p),
                                     c.template buf<int>(Q.en_idx_p), c.template buf<int>(Q.counts_p), static_max,
                                     c.status);
-  // ElecInit of the moved electron (one row per walker), then its GLU / Dense / Dense
+  // ElecInit of the moved electrons (KM rows per walker), then their GLU / Dense / Dense
   {
+    const int ME = Wc * KM;
     Nbr nbe = c.nb;
     nbe.en_cnt = c.template buf<int>(Q.en_cnt_p);
     nbe.en_idx = c.template buf<int>(Q.en_idx_p);
     T* E5a = c.template buf<T>(c.P.E5a);
     T* Z1 = c.template buf<T>(c.P.Z1);
     g_nlaunch++;
-    k_elec_init<T, 0><<<Wc, 256, 0, s>>>(c.template buf<T>(Q.re_p), c.R, nbe, c.W, (T)(1.0 / p->cutoff_1el), E5a);
+    k_elec_init<T, 0><<<ME, 256, 0, s>>>(c.template buf<T>(Q.re_p), c.R, nbe, c.W, (T)(1.0 / p->cutoff_1el), E5a);
     GemmP<T> g = gp0<T>();
     g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_GLU_W]; g.ldb = 2 * F; g.C = Z1; g.ldc = 2 * F;
-    g.M = Wc; g.N = 2 * F; g.K = F;
+    g.M = ME; g.N = 2 * F; g.K = F;
     gemm<T, EPI_PLAIN>(c, g);
     g_nlaunch++;
-    k_glu<T, 0><<<nblk((long)Wc * F), 256, 0, s>>>(Z1, E5a, Wc);
+    k_glu<T, 0><<<nblk((long)ME * F), 256, 0, s>>>(Z1, E5a, ME);
     g = gp0<T>();
     g.A = E5a; g.lda = F; g.B = c.W.w[FIRE_P_EI_DENSE_W]; g.ldb = F; g.C = Z1; g.ldc = F;
-    g.bias = c.W.w[FIRE_P_EI_DENSE_B]; g.bias_period = 1; g.M = Wc; g.N = F; g.K = F;
+    g.bias = c.W.w[FIRE_P_EI_DENSE_B]; g.bias_period = 1; g.M = ME; g.N = F; g.K = F;
     gemm<T, EPI_PLAIN>(c, g);
     g_nlaunch++;
-    k_silu5<T, 0><<<nblk((long)Wc * F), 256, 0, s>>>(Z1, Wc);
+    k_silu5<T, 0><<<nblk((long)ME * F), 256, 0, s>>>(Z1, ME);
     g = gp0<T>();
     g.A = Z1; g.lda = F; g.B = c.W.w[FIRE_P_EI_OUT_W]; g.ldb = 5 * F; g.C = c.template buf<T>(Q.E5p);
-    g.ldc = 5 * F; g.bias = c.W.w[FIRE_P_EI_OUT_B]; g.bias_period = 1; g.M = Wc; g.N = 5 * F; g.K = F;
+    g.ldc = 5 * F; g.bias = c.W.w[FIRE_P_EI_OUT_B]; g.bias_period = 1; g.M = ME; g.N = 5 * F; g.K = F;
     gemm<T, EPI_PLAIN>(c, g);
   }
   // messages and update MLP of the changed centers
   g_nlaunch++;
-  k_lr_contract<T><<<dim3(KS, Wc), 256, 0, s>>>(rn, n, nu, (T)p->cutoff, moved, S, S_cnt, KS, c.W,
+  k_lr_contract<T><<<dim3(KS, Wc), 256, 0, s>>>(rn, n, nu, (T)p->cutoff, moved, KM, S, S_cnt, KS, c.W,
                                                 c.template buf<T>(c.P.E5o), c.template buf<T>(Q.E5p),
                                                 c.template buf<T>(Q.HS));
   const Planes HS{Q.HS, 0, 0}, B1S{Q.B1S, 0, 0}, hS{Q.hS, 0, 0};
@@ -1267,19 +1269,20 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int32_t* stat
     T* coefU = c.template buf<T>(Q.coefE);
     T* coefD = c.template buf<T>(Q.coefD);
     g_nlaunch++;
-    k_lr_env_coef<T><<<nblk((long)Wc * K8), 256, 0, s>>>(rn, c.R, c.W.w[PR_ENV_UP_SP], c.W.w[PR_ENV_DN_SP], moved, n,
-                                                         nu, N, Wc, coefU, coefD);
+    const int ME = Wc * KM;
+    k_lr_env_coef<T><<<nblk((long)ME * K8), 256, 0, s>>>(rn, c.R, c.W.w[PR_ENV_UP_SP], c.W.w[PR_ENV_DN_SP], moved,
+                                                         KM, n, nu, N, Wc, coefU, coefD);
     for (int sp = 0; sp < 2; ++sp)
       for (int d = 0; d < NDET; ++d) {
         GemmP<T> g = gp0<T>();
-        g.A = (sp == 0 ? coefU : coefD) + (size_t)d * Wc * K8; g.lda = K8;
+        g.A = (sp == 0 ? coefU : coefD) + (size_t)d * ME * K8; g.lda = K8;
         g.B = c.W.w[sp == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (size_t)d * K8 * n; g.ldb = n;
-        g.C = c.template buf<T>(sp == 0 ? Q.env_p : Q.env_pD) + (size_t)d * n; g.ldc = DN; g.M = Wc; g.N = n;
+        g.C = c.template buf<T>(sp == 0 ? Q.env_p : Q.env_pD) + (size_t)d * n; g.ldc = DN; g.M = ME; g.N = n;
         g.K = K8; g.n_el = 1; g.env_ns = 1; g.env_soff = 0; g.env_nv = 1;
         gemm<T, EPI_ENV>(c, g);
       }
     g_nlaunch++;
-    k_lr_env_add<T><<<nblk((long)Wc * DN), 256, 0, s>>>((long)Wc * DN, c.template buf<T>(Q.env_p),
+    k_lr_env_add<T><<<nblk((long)ME * DN), 256, 0, s>>>((long)ME * DN, c.template buf<T>(Q.env_p),
                                                         c.template buf<T>(Q.env_pD));
   }
   // determinant lemma
@@ -1288,7 +1291,7 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int32_t* stat
     cudaFuncSetAttribute(k_lr_det<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     g_nlaunch++;
     k_lr_det<T><<<dim3(NDET, Wc), 256, smem, s>>>(
-        S, S_cnt, KS, n, moved, c.template buf<T>(Q.rawU), c.template buf<T>(c.P.env), c.template buf<T>(Q.env_p),
+        S, S_cnt, KS, n, moved, KM, c.template buf<T>(Q.rawU), c.template buf<T>(c.P.env), c.template buf<T>(Q.env_p),
         c.template buf<T>(c.P.Apl), c.template buf<T>(Q.B), c.template buf<double>(c.P.ld),
         c.template buf<double>(c.P.sd), c.template buf<T>(Q.V), c.template buf<double>(Q.Minv),
         c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p));
@@ -1338,8 +1341,8 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, int32_t* stat
 // state, the Metropolis test with the proposals' log ratios plr (may be null), and on acceptance the state's rows and
 // the Woodbury update of the inverse.
 template <typename T>
-cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int st, uint64_t seed, uint64_t counter,
-                    const void* logu, int32_t* n_accept, int32_t* static_max, const T* plr) {
+cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, void* logpsi, int st, uint64_t seed,
+                    uint64_t counter, const void* logu, int32_t* n_accept, int32_t* static_max, const T* plr) {
   const fire_problem* p = c.p;
   const int n = p->n_el, Wc = c.Wc;
   cudaStream_t s = c.s;
@@ -1348,7 +1351,7 @@ cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int
   int* S_cnt = c.template buf<int>(Q.S_cnt);
   int* acc = c.template buf<int>(Q.acc);
   const int* moved = c.template buf<int>(Q.moved);
-  const cudaError_t ev = lr_evaluate<T>(c, Q, KS, rr, static_max, nullptr);
+  const cudaError_t ev = lr_evaluate<T>(c, Q, KS, KM, rr, static_max, nullptr);
   if (ev != cudaSuccess) return ev;
   T* lpn = c.template buf<T>(c.P.lpn);
   g_nlaunch++;
@@ -1357,8 +1360,8 @@ cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, T* rr, void* logpsi, int
                                  static_max, plr, acc);
   // accepted walkers: rows into the state, Woodbury update of the inverse
   g_nlaunch++;
-  k_lr_commit<T><<<dim3(KS + 1, Wc), 256, 0, s>>>(
-      acc, S, S_cnt, KS, n, moved, c.template buf<T>(Q.hS), c.template buf<T>(Q.rawU), c.template buf<T>(Q.env_p),
+  k_lr_commit<T><<<dim3(KS + KM, Wc), 256, 0, s>>>(
+      acc, S, S_cnt, KS, n, moved, KM, c.template buf<T>(Q.hS), c.template buf<T>(Q.rawU), c.template buf<T>(Q.env_p),
       c.template buf<T>(Q.aS), c.template buf<T>(Q.vS), c.template buf<T>(Q.oS), c.template buf<T>(Q.E5p),
       c.template buf<int>(Q.en_cnt_p), c.template buf<int>(Q.en_idx_p), c.template buf<int>(Q.counts_p),
       c.template buf<double>(Q.ld_p), c.template buf<double>(Q.sd_p), c.template buf<T>(c.P.B2X),
@@ -1440,7 +1443,7 @@ fire_status run_ecp(const fire_problem* p, cudaStream_t s, const float* R, const
         g_nlaunch++;
         k_ecp_point<T><<<c.Wc, 128, 0, s>>>(c.r, c.template buf<T>(c.P.rn), n, e, k, R, ecp, qt, w0, seed, counter,
                                             reinterpret_cast<const T*>(rot), pt, c.template buf<int>(Q.moved));
-        if (lr_evaluate<T>(c, Q, KS, rr, static_max, c.template buf<T>(Q.sgn_p)) != cudaSuccess)
+        if (lr_evaluate<T>(c, Q, KS, 1, rr, static_max, c.template buf<T>(Q.sgn_p)) != cudaSuccess)
           return launch_status("pseudopotential ratio");
         g_nlaunch++;
         k_ecp_accum<T><<<nblk(c.Wc), 256, 0, s>>>(c.Wc, pt, c.template buf<T>(c.P.lpn), c.template buf<T>(Q.sgn_p),
@@ -1452,15 +1455,17 @@ fire_status run_ecp(const fire_problem* p, cudaStream_t s, const float* R, const
   return launch_status(__func__);
 }
 
-// Low-rank one-electron block (mcmc_steps_low_rank): per chunk the state from one value-path evaluation, then every
+// Low-rank Metropolis block (mcmc_steps_low_rank): per chunk the state from one value-path evaluation, then every
 // step from the state.  kind MC_SINGLE: proposal_single_electron (electron (offset + step) mod n moved by width
 // eps); MC_JUMP: proposal_jump_to_atom (a random electron per walker to a random nucleus, width = sigma, the
-// proposal's log ratio in the test).
+// proposal's log ratio in the test); MC_CLUSTER: proposal_cluster_update (ck electrons at most within cradius of a
+// sequential or random center, its validity in the test).
 template <typename T>
 fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
                         void* r, void* logpsi, int steps, int offset, float width, int KS, uint64_t seed,
                         uint64_t counter, const void* noise, const void* logu, int32_t* n_accept,
-                        int32_t* static_max, void* ws, size_t wsb, int32_t* status, int kind = MC_SINGLE) {
+                        int32_t* static_max, void* ws, size_t wsb, int32_t* status, int kind = MC_SINGLE, int ck = 1,
+                        float cradius = 0.f, int crandom = 0) {
   const int Wc = choose_chunk_lr(p, wsb, KS);
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
@@ -1473,10 +1478,15 @@ fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, c
     c.r = rr + (size_t)w0 * n * 3;
     if (chunk_state<T>(c, Q, logpsi, nullptr, w0) != cudaSuccess) return launch_status("low-rank state");
     int* moved = c.template buf<int>(Q.moved);
-    T* plr = kind == MC_JUMP ? c.template buf<T>(c.P.plr) : nullptr;
+    T* plr = (kind == MC_JUMP || kind == MC_CLUSTER) ? c.template buf<T>(c.P.plr) : nullptr;
+    const int KM = kind == MC_CLUSTER ? ck : 1;
     for (int st = 0; st < steps; ++st) {
       g_nlaunch++;
-      if (kind == MC_JUMP)
+      if (kind == MC_CLUSTER)
+        k_propose_cluster<T><<<c.Wc, 32, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), plr, n, w0,
+                                                 p->n_walkers, st, offset, ck, (T)cradius, (T)width, crandom, seed,
+                                                 counter, reinterpret_cast<const T*>(noise), moved);
+      else if (kind == MC_JUMP)
         k_propose_jump<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), plr, n, w0,
                                                p->n_walkers, st, R, Z, p->n_nuc, (T)width, seed, counter,
                                                reinterpret_cast<const T*>(noise), moved);
@@ -1484,7 +1494,7 @@ fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, c
         k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), n, w0,
                                                  p->n_walkers, st, offset, (T)width, seed, counter,
                                                  reinterpret_cast<const T*>(noise), moved);
-      if (lr_step<T>(c, Q, KS, rr, logpsi, st, seed, counter, logu, n_accept, static_max, plr) != cudaSuccess)
+      if (lr_step<T>(c, Q, KS, KM, rr, logpsi, st, seed, counter, logu, n_accept, static_max, plr) != cudaSuccess)
         return launch_status("low-rank step");
     }
   }
@@ -1785,6 +1795,31 @@ fire_status fire_mcmc_low_rank_jump_block(void* stream, const fire_problem* prob
                                replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
   return run_mcmc_lr<float>(prob, s, R, Z, prepared, r, logpsi, steps, 0, sigma, KS, seed, counter, replay_draws,
                             replay_log_u, n_accept, static_max, workspace, workspace_bytes, status, MC_JUMP);
+}
+
+fire_status fire_mcmc_low_rank_cluster_block(void* stream, const fire_problem* prob, const float* R, const float* Z,
+                                             const void* prepared, void* r, void* logpsi, int32_t steps,
+                                             int32_t step_offset, float width, int32_t max_cluster_size,
+                                             float max_cluster_radius, int32_t random_sweep, int32_t cap_changed,
+                                             uint64_t seed, uint64_t counter, const void* replay_draws,
+                                             const void* replay_log_u, int32_t* n_accept, int32_t* static_max,
+                                             void* workspace, size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !R || !Z || !prepared || !r || !logpsi || !workspace || steps < 0 || step_offset < 0 ||
+      max_cluster_size < 1 || !(max_cluster_radius >= 0.f) || cap_changed < 1)
+    return FIRE_ERR_INVALID;
+  if ((replay_draws == nullptr) != (replay_log_u == nullptr)) return FIRE_ERR_INVALID;
+  if (max_cluster_size > CLUSTER_KMAX || prob->n_el > ELOC_MAX_EL || cap_changed > LR_KMAX)
+    return FIRE_ERR_UNSUPPORTED;
+  const int k = std::min<int>(max_cluster_size, prob->n_el);
+  const int KS = std::min<int>(cap_changed, prob->n_el);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (prob->precision == FIRE_PREC_FP64)
+    return run_mcmc_lr<double>(prob, s, R, Z, prepared, r, logpsi, steps, step_offset, width, KS, seed, counter,
+                               replay_draws, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status,
+                               MC_CLUSTER, k, max_cluster_radius, random_sweep ? 1 : 0);
+  return run_mcmc_lr<float>(prob, s, R, Z, prepared, r, logpsi, steps, step_offset, width, KS, seed, counter,
+                            replay_draws, replay_log_u, n_accept, static_max, workspace, workspace_bytes, status,
+                            MC_CLUSTER, k, max_cluster_radius, random_sweep ? 1 : 0);
 }
 
 fire_status fire_ecp_quadrature(int32_t n_points, double* points) {

@@ -439,11 +439,11 @@ __global__ void __launch_bounds__(256) k_edge_contract(const T* __restrict__ r, 
 // Low-rank step, value path (NewSparseEmbedding.low_rank_update, new_sparse_model.py:553-629): one CTA (256
 // threads, thread = feature) per changed center c = S[w][slot] of walker w.  Its neighbours are taken in the proposed
 // configuration rn, ascending like the pair list, and the messages are those of k_edge_contract; the ElecInit rows
-// (h0 | ct_same | ct_diff | nb_same | nb_diff) come from the state E5 [W][n][5F] except for the moved electron
-// e = moved[w], whose row is E5p [W][5F].  Output HS [W][KS][F] = h0[c] + sum of the messages (before the update MLP).
+// (h0 | ct_same | ct_diff | nb_same | nb_diff) come from the state E5 [W][n][5F] except for the moved electrons
+// moved[w][0..KM), whose rows are E5p [W][KM][5F].  Output HS [W][KS][F] = h0[c] + sum of the messages (before the update MLP).
 template <typename T>
 __global__ void __launch_bounds__(256) k_lr_contract(const T* __restrict__ rn, int n, int n_up, T cutoff,
-                                                     const int* __restrict__ moved, const int* __restrict__ S,
+                                                     const int* __restrict__ moved, int KM, const int* __restrict__ S,
                                                      const int* __restrict__ S_cnt, int KS,
                                                      Weights<T> W, const T* __restrict__ E5, const T* __restrict__ E5p,
                                                      T* __restrict__ HS) {
@@ -456,7 +456,15 @@ __global__ void __launch_bounds__(256) k_lr_contract(const T* __restrict__ rn, i
   __shared__ int wcnt[8];
   const int slot = blockIdx.x, w = blockIdx.y, f = threadIdx.x, lane = f & 31, wid = f >> 5;
   if (slot >= min(S_cnt[w], KS)) return;
-  const int c = S[(size_t)w * KS + slot], e = moved[w];
+  const int c = S[(size_t)w * KS + slot];
+  __shared__ int sm[CLUSTER_KMAX];
+  if (f < KM) sm[f] = moved[(size_t)w * KM + f];
+  __syncthreads();
+  auto e5row = [&](int j) -> const T* {
+    for (int t = 0; t < KM; ++t)
+      if (sm[t] == j) return E5p + ((size_t)w * KM + t) * 5 * F;
+    return E5 + ((size_t)w * n + j) * 5 * F;
+  };
   const T* rw = rn + (size_t)w * n * 3;
   const T rx = rw[3 * c], ry = rw[3 * c + 1], rz = rw[3 * c + 2];
   // neighbours of c after the move, ascending: 256 candidates per pass, compacted across the block
@@ -492,7 +500,7 @@ __global__ void __launch_bounds__(256) k_lr_contract(const T* __restrict__ rn, i
     for (int q = 0; q < 4; ++q) we[s][q] = We[q * F + f];
     be[s] = W.w[s == 0 ? FIRE_P_EESAME_EDGE_B : FIRE_P_EEDIFF_EDGE_B][f];
   }
-  const T* ec = c == e ? E5p + (size_t)w * 5 * F : E5 + ((size_t)w * n + c) * 5 * F;
+  const T* ec = e5row(c);
   const T h0 = ec[f], cts = ec[F + f], ctd = ec[2 * F + f];
   T ax = T(0);
   for (int k0 = 0; k0 < deg; k0 += EB) {
@@ -523,7 +531,7 @@ __global__ void __launch_bounds__(256) k_lr_contract(const T* __restrict__ rn, i
 #pragma unroll
       for (int u = 0; u < 4; ++u) E += we[s][u] * sS[q][u];
       E += be[s];
-      const T* ej = j == e ? E5p + (size_t)w * 5 * F : E5 + ((size_t)w * n + j) * 5 * F;
+      const T* ej = e5row(j);
       const T u = E + ((same ? cts : ctd) + ej[(same ? 3 : 4) * F + f]);
       T y, d1, d2;
       silu3(u, y, d1, d2);
@@ -534,10 +542,10 @@ __global__ void __launch_bounds__(256) k_lr_contract(const T* __restrict__ rn, i
   HS[((size_t)w * KS + slot) * F + f] = h0 + ax;
 }
 
-template __global__ void k_lr_contract<float>(const float*, int, int, float, const int*, const int*, const int*,
+template __global__ void k_lr_contract<float>(const float*, int, int, float, const int*, int, const int*, const int*,
                                               int, Weights<float>, const float*, const float*, float*);
-template __global__ void k_lr_contract<double>(const double*, int, int, double, const int*, const int*, const int*,
-                                               int, Weights<double>, const double*, const double*, double*);
+template __global__ void k_lr_contract<double>(const double*, int, int, double, const int*, int, const int*,
+                                               const int*, int, Weights<double>, const double*, const double*, double*);
 
 #define FIRE_INST_EMBED(T, NT)                                                                              \
   template __global__ void k_elec_init<T, NT>(const T*, const float*, Nbr, Weights<T>, T, T*);            \

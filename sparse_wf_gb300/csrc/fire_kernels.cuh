@@ -28,8 +28,8 @@ __global__ void k_silu5(T* Z, int G);
 template <typename T, int NT>
 __global__ void k_edge_contract(const T* r, Nbr nb, Layout L, Weights<T> W, const T* E5o, T* X, T* Lp, T* Jp);
 template <typename T>
-__global__ void k_lr_contract(const T* rn, int n, int n_up, T cutoff, const int* moved, const int* S, const int* S_cnt,
-                              int KS, Weights<T> W, const T* E5, const T* E5p, T* HS);
+__global__ void k_lr_contract(const T* rn, int n, int n_up, T cutoff, const int* moved, int KM, const int* S,
+                              const int* S_cnt, int KS, Weights<T> W, const T* E5, const T* E5p, T* HS);
 
 // fire_det.cu
 template <typename T, int NV>
@@ -80,7 +80,7 @@ __global__ void k_accept(T* r, const T* rn, T* logpsi, const T* logpsi_new, int 
 template <typename T>
 __global__ void k_propose_cluster(const T* r, T* rn, T* plr, int n, int w0, int B, int step, int offset, int k,
                                   T radius, T width, int random_sweep, uint64_t seed, uint64_t counter,
-                                  const T* replay);
+                                  const T* replay, int* moved_idx);
 template <typename T>
 __global__ void k_propose_jump(const T* r, T* rn, T* plr, int n, int w0, int B, int step, const float* R,
                                const float* Z, int N, T sigma, uint64_t seed, uint64_t counter, const T* replay,
@@ -88,25 +88,26 @@ __global__ void k_propose_jump(const T* r, T* rn, T* plr, int n, int w0, int B, 
 
 // fire_lowrank.cu
 template <typename T>
-__global__ void k_lr_select(const T* r, const T* rn, int n, int n_up, const int* moved, const float* R, int N,
+__global__ void k_lr_select(const T* r, const T* rn, int n, int n_up, const int* moved, int KM, const float* R, int N,
                             T cutoff, T cutoff_1el, Nbr nb, int KS, int* S, int* S_cnt, T* re_p, int* en_cnt_p,
                             int* en_idx_p, int* counts_p, int32_t* static_max, int32_t* status);
 template <typename T>
-__global__ void k_lr_env_coef(const T* rn, const float* R, const T* sp_up, const T* sp_dn, const int* moved, int n,
-                              int n_up, int N, int Wc, T* coefU, T* coefD);
+__global__ void k_lr_env_coef(const T* rn, const float* R, const T* sp_up, const T* sp_dn, const int* moved, int KM,
+                              int n, int n_up, int N, int Wc, T* coefU, T* coefD);
 template <typename T>
 __global__ void k_lr_env_add(long total, T* env_p, const T* env_d);
 template <typename T>
 __global__ void k_lr_orb(const int* S, const int* S_cnt, int KS, int n_up, int DN, T* rawU, const T* rawD);
 template <typename T>
-__global__ void k_lr_det(const int* S, const int* S_cnt, int KS, int n, const int* moved, const T* rawS, const T* env,
+__global__ void k_lr_det(const int* S, const int* S_cnt, int KS, int n, const int* moved, int KM, const T* rawS,
+                         const T* env,
                          const T* env_p, const T* Apl, const T* B, const double* ld, const double* sd, T* V,
                          double* Minv, double* ld_p, double* sd_p);
 template <typename T>
 __global__ void k_lr_jsums(int n, int n_up, const int* S, const int* S_cnt, int KS, const T* aX, const T* vals,
                            const T* Xo, const T* aS, const T* vS, const T* oS, T* Ax, T* JM);
 template <typename T>
-__global__ void k_lr_commit(const int* accf, const int* S, const int* S_cnt, int KS, int n, const int* moved,
+__global__ void k_lr_commit(const int* accf, const int* S, const int* S_cnt, int KS, int n, const int* moved, int KM,
                             const T* hS,
                             const T* rawS, const T* env_p, const T* aS, const T* vS, const T* oS, const T* E5p,
                             const int* en_cnt_p, const int* en_idx_p, const int* counts_p, const double* ld_p,

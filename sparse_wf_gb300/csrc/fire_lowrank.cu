@@ -31,49 +31,63 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kAcc = LR_KMAX / 8;  // accumulators per thread of the Woodbury products (8 warps share the k columns)
 }  // namespace
 
-// One CTA (256 threads) per walker of the chunk.  r: the chunk's current positions; rn: the proposal (r with
-// electron e = moved[w] moved).  nb: the state's e-n counts [W][n] and statics [W][4].  Outputs S [W][KS] (the first
-// KS members), S_cnt [W] (the true size), re_p [W][3] (e's new position), en_cnt_p [W], en_idx_p [W][cap_nuc],
-// counts_p [W][4] (the proposal's statics, triplets 0); static_max [7] entries 4..6 take the move statics.
+// One CTA (256 threads) per walker of the chunk.  r: the chunk's current positions; rn: the proposal, in which walker
+// w moved the electrons moved[w][0..KM) (entries >= n are padding: NO_NEIGHBOUR of a cluster's index list).  nb: the
+// state's e-n counts [W][n] and statics [W][4].  Outputs S [W][KS] (the first KS members of the changed set), S_cnt
+// [W] (its true size), per moved slot t the new position re_p [W][KM][3] and e-n list en_cnt_p [W][KM], en_idx_p
+// [W][KM][cap_nuc], the proposal's statics counts_p [W][4] (triplets 0); static_max [7] entries 4..6 take the move
+// statics.  The changed set holds the moved electrons and every electron within the cutoff of a gathered moved entry
+// before or after the move, a padded entry gathering electron n - 1 as an out-of-range JAX gather clamps
+// (get_low_rank_pair_indices, model/new_sparse_model.py:439-474).
 template <typename T>
 __global__ void __launch_bounds__(256) k_lr_select(const T* __restrict__ r, const T* __restrict__ rn, int n, int n_up,
-                                                   const int* __restrict__ moved, const float* __restrict__ R, int N,
-                                                   T cutoff, T cutoff_1el,
-                                                   Nbr nb, int KS, int* __restrict__ S, int* __restrict__ S_cnt,
-                                                   T* __restrict__ re_p, int* __restrict__ en_cnt_p,
-                                                   int* __restrict__ en_idx_p, int* __restrict__ counts_p,
-                                                   int32_t* __restrict__ static_max, int32_t* status) {
+                                                   const int* __restrict__ moved, int KM, const float* __restrict__ R,
+                                                   int N, T cutoff, T cutoff_1el, Nbr nb, int KS, int* __restrict__ S,
+                                                   int* __restrict__ S_cnt, T* __restrict__ re_p,
+                                                   int* __restrict__ en_cnt_p, int* __restrict__ en_idx_p,
+                                                   int* __restrict__ counts_p, int32_t* __restrict__ static_max,
+                                                   int32_t* status) {
   __shared__ int wcnt[8];
   __shared__ int emx[8];
   __shared__ int red[32 * 4];
   __shared__ int sS[LR_KMAX];
-  __shared__ int ce_s;
+  __shared__ int sm[CLUSTER_KMAX];
+  __shared__ int ce_max;
   const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int e = moved[w];
   const unsigned lt = (1u << lane) - 1u;
   const T* ro = r + (size_t)w * n * 3;
   const T* rp = rn + (size_t)w * n * 3;
-  const T xo = ro[3 * e], yo = ro[3 * e + 1], zo = ro[3 * e + 2];
-  const T xn = rp[3 * e], yn = rp[3 * e + 1], zn = rp[3 * e + 2];
-  const bool se = e < n_up;
-  // S in ascending order, 256 candidates per pass; dv: e's old same / old diff / new same / new diff neighbours
+  if (tid < KM) sm[tid] = moved[(size_t)w * KM + tid];
+  if (tid == 0) ce_max = 0;
+  __syncthreads();
+  // S in ascending order, 256 candidates per pass; dv: the change of the directed pair counts (same, diff spin), each
+  // pair (m, j) of a moved m counted twice when j stays and once when j moves too (its own term counts the other)
   int cnt = 0;
-  int dv[4] = {0, 0, 0, 0};
+  int dv[2] = {0, 0};
   for (int j0 = 0; j0 < n; j0 += 256) {
     const int j = j0 + tid;
-    bool aff = j == e;
-    if (j < n && j != e) {
-      const bool io = exact_dist(xo, yo, zo, ro[3 * j], ro[3 * j + 1], ro[3 * j + 2]) < cutoff;
-      const bool in = exact_dist(xn, yn, zn, rp[3 * j], rp[3 * j + 1], rp[3 * j + 2]) < cutoff;
-      const bool same = (j < n_up) == se;
-      dv[0] += io && same;
-      dv[1] += io && !same;
-      dv[2] += in && same;
-      dv[3] += in && !same;
-      aff = io || in;
+    bool aff = false;
+    if (j < n) {
+      bool isM = false;
+      for (int t = 0; t < KM; ++t) isM |= sm[t] == j;
+      aff = isM;
+      const bool sj = j < n_up;
+      for (int t = 0; t < KM; ++t) {
+        const int m = min(sm[t], n - 1);
+        if (m == j) continue;
+        const bool io = exact_dist(ro[3 * m], ro[3 * m + 1], ro[3 * m + 2], ro[3 * j], ro[3 * j + 1], ro[3 * j + 2]) <
+                        cutoff;
+        const bool in = exact_dist(rp[3 * m], rp[3 * m + 1], rp[3 * m + 2], rp[3 * j], rp[3 * j + 1], rp[3 * j + 2]) <
+                        cutoff;
+        aff |= io || in;
+        if (sm[t] < n) {
+          const int d = (isM ? 1 : 2) * ((int)in - (int)io);
+          dv[((m < n_up) == sj) ? 0 : 1] += d;
+        }
+      }
     }
-    const unsigned m = __ballot_sync(kFull, aff);
-    if (lane == 0) wcnt[wid] = __popc(m);
+    const unsigned mk = __ballot_sync(kFull, aff);
+    if (lane == 0) wcnt[wid] = __popc(mk);
     __syncthreads();
     int off = cnt, tot = 0;
 #pragma unroll
@@ -81,7 +95,7 @@ __global__ void __launch_bounds__(256) k_lr_select(const T* __restrict__ r, cons
       off += q < wid ? wcnt[q] : 0;
       tot += wcnt[q];
     }
-    const int pos = off + __popc(m & lt);
+    const int pos = off + __popc(mk & lt);
     if (aff && pos < KS) {
       S[(size_t)w * KS + pos] = j;
       sS[pos] = j;
@@ -89,7 +103,7 @@ __global__ void __launch_bounds__(256) k_lr_select(const T* __restrict__ r, cons
     cnt += tot;
     __syncthreads();
   }
-  block_sum<int, 4>(dv, red);
+  block_sum<int, 2>(dv, red);
   // neighbours of the changed centers after the move, by spin (one warp per center; lane 0 keeps the counts)
   const int k = min(cnt, KS);
   int pc[2] = {0, 0};
@@ -107,38 +121,54 @@ __global__ void __launch_bounds__(256) k_lr_select(const T* __restrict__ r, cons
     }
   }
   if (lane != 0) pc[0] = pc[1] = 0;
-  // e-n maximum of the other electrons (the state's lists) and e's list at its new position (warp 0)
+  // e-n maximum of the electrons that stay (the state's lists); the moved electrons' lists at their new positions
+  // (one warp per moved slot; padded slots get an empty list)
   int em = 0;
-  for (int i = tid; i < n; i += blockDim.x)
-    if (i != e) em = max(em, nb.en_cnt[(size_t)w * n + i]);
+  for (int i = tid; i < n; i += blockDim.x) {
+    bool isM = false;
+    for (int t = 0; t < KM; ++t) isM |= sm[t] == i;
+    if (!isM) em = max(em, nb.en_cnt[(size_t)w * n + i]);
+  }
   em = warp_max(em);
   if (lane == 0) emx[wid] = em;
-  if (wid == 0) {
+  for (int t = wid; t < KM; t += 8) {
+    const int m = sm[t];
+    const size_t slot = (size_t)w * KM + t;
+    if (m >= n) {
+      if (lane == 0) {
+        en_cnt_p[slot] = 0;
+        re_p[3 * slot] = re_p[3 * slot + 1] = re_p[3 * slot + 2] = T(0);
+      }
+      continue;
+    }
+    const T xn = rp[3 * m], yn = rp[3 * m + 1], zn = rp[3 * m + 2];
     int ce = 0;
     for (int I0 = 0; I0 < N; I0 += 32) {
       const int I = I0 + lane;
       bool in = false;
       if (I < N) in = exact_dist(xn, yn, zn, (T)R[3 * I], (T)R[3 * I + 1], (T)R[3 * I + 2]) < cutoff_1el;
-      const unsigned m = __ballot_sync(kFull, in);
-      const int pos = ce + __popc(m & lt);
-      if (in && pos < nb.cap_nuc) en_idx_p[(size_t)w * nb.cap_nuc + pos] = I;
-      ce += __popc(m);
+      const unsigned mk = __ballot_sync(kFull, in);
+      const int pos = ce + __popc(mk & lt);
+      if (in && pos < nb.cap_nuc) en_idx_p[slot * nb.cap_nuc + pos] = I;
+      ce += __popc(mk);
     }
-    if (lane == 0) ce_s = ce;
+    if (lane == 0) {
+      en_cnt_p[slot] = min(ce, nb.cap_nuc);
+      re_p[3 * slot] = xn;
+      re_p[3 * slot + 1] = yn;
+      re_p[3 * slot + 2] = zn;
+      atomicMax(&ce_max, ce);
+    }
   }
   block_sum<int, 2>(pc, red);
   if (tid == 0) {
-    int ee = ce_s;
+    int ee = ce_max;
     for (int q = 0; q < 8; ++q) ee = max(ee, emx[q]);
-    counts_p[w * 4 + 0] = nb.counts[w * 4 + 0] + 2 * (dv[2] - dv[0]);
-    counts_p[w * 4 + 1] = nb.counts[w * 4 + 1] + 2 * (dv[3] - dv[1]);
+    counts_p[w * 4 + 0] = nb.counts[w * 4 + 0] + dv[0];
+    counts_p[w * 4 + 1] = nb.counts[w * 4 + 1] + dv[1];
     counts_p[w * 4 + 2] = 0;
     counts_p[w * 4 + 3] = ee;
     S_cnt[w] = cnt;
-    en_cnt_p[w] = min(ce_s, nb.cap_nuc);
-    re_p[3 * w] = xn;
-    re_p[3 * w + 1] = yn;
-    re_p[3 * w + 2] = zn;
     if (static_max) {
       atomicMax(&static_max[4], cnt);
       atomicMax(&static_max[5], pc[0]);
@@ -148,9 +178,9 @@ __global__ void __launch_bounds__(256) k_lr_select(const T* __restrict__ r, cons
       set_flag(status, FIRE_FLAG_CHANGED_OVERFLOW);
       max_word(status, 4, cnt);
     }
-    if (ce_s > nb.cap_nuc) {
+    if (ce_max > nb.cap_nuc) {
       set_flag(status, FIRE_FLAG_NUC_OVERFLOW);
-      max_word(status, 2, ce_s);
+      max_word(status, 2, ce_max);
     }
   }
 }
@@ -167,34 +197,44 @@ __global__ void __launch_bounds__(256) k_lr_orb(const int* __restrict__ S, const
   for (int q = threadIdx.x; q < DN; q += blockDim.x) rawU[row + q] = rawD[row + q];
 }
 
-// Envelope coefficients of each walker's moved electron e = moved[w] at its new position, with the softplus scales
-// of e's spin: coefU / coefD [NDET][W][N * 8] hold exp(-|r_e - R_I| sp[I][d][k]) for the walkers whose e is spin up /
-// down and zeros for the others, so that the two spins' contractions with their own envelope weights add up to e's
-// row.  One thread per (walker, nucleus, k).
+// Envelope coefficients of the moved electrons at their new positions, one row per moved slot (walker w, slot t,
+// electron e = moved[w][t]), with the softplus scales of e's spin: coefU / coefD [NDET][W KM][N * 8] hold
+// exp(-|r_e - R_I| sp[I][d][k]) in the set of e's spin and zeros in the other (both zero for a padded slot), so that
+// the two spins' contractions with their own envelope weights add up to e's row.  One thread per (row, nucleus, k).
 template <typename T>
 __global__ void k_lr_env_coef(const T* __restrict__ rn, const float* __restrict__ R, const T* __restrict__ sp_up,
-                              const T* __restrict__ sp_dn, const int* __restrict__ moved, int n, int n_up, int N,
-                              int Wc, T* __restrict__ coefU, T* __restrict__ coefD) {
+                              const T* __restrict__ sp_dn, const int* __restrict__ moved, int KM, int n, int n_up,
+                              int N, int Wc, T* __restrict__ coefU, T* __restrict__ coefD) {
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long)Wc * N * NENV_ORB) return;
-  const int k = (int)(idx % NENV_ORB), I = (int)((idx / NENV_ORB) % N), w = (int)(idx / ((long)NENV_ORB * N));
-  const int e = moved[w];
+  const long rows = (long)Wc * KM;
+  if (idx >= rows * N * NENV_ORB) return;
+  const int k = (int)(idx % NENV_ORB), I = (int)((idx / NENV_ORB) % N);
+  const long row = idx / ((long)NENV_ORB * N);
+  const int w = (int)(row / KM), e = moved[row];
+  const int K8 = N * NENV_ORB;
+  if (e >= n) {
+#pragma unroll
+    for (int d = 0; d < NDET; ++d) {
+      coefU[((long)d * rows + row) * K8 + I * NENV_ORB + k] = T(0);
+      coefD[((long)d * rows + row) * K8 + I * NENV_ORB + k] = T(0);
+    }
+    return;
+  }
   const bool up = e < n_up;
   const T* x = rn + ((size_t)w * n + e) * 3;
   const T dx = x[0] - (T)R[3 * I], dy = x[1] - (T)R[3 * I + 1], dz = x[2] - (T)R[3 * I + 2];
   const T rho = dsqrt(dx * dx + dy * dy + dz * dz);
-  const int K8 = N * NENV_ORB;
   const T* sp = up ? sp_up : sp_dn;
 #pragma unroll
   for (int d = 0; d < NDET; ++d) {
-    const long o = ((long)d * Wc + w) * K8 + I * NENV_ORB + k;
+    const long o = ((long)d * rows + row) * K8 + I * NENV_ORB + k;
     const T v = dexp(-sp[(I * NDET + d) * NENV_ORB + k] * rho);
     coefU[o] = up ? v : T(0);
     coefD[o] = up ? T(0) : v;
   }
 }
 
-// env_p [W][DN] += env_d [W][DN]: the spin-down contraction added to the spin-up one (one of the two is zero).
+// env_p [W KM][DN] += env_d [W KM][DN]: the spin-down contraction added to the spin-up one (one of the two is zero).
 template <typename T>
 __global__ void k_lr_env_add(long total, T* __restrict__ env_p, const T* __restrict__ env_d) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,8 +242,8 @@ __global__ void k_lr_env_add(long total, T* __restrict__ env_p, const T* __restr
 }
 
 // One CTA (256 threads) per (determinant d, walker w).  rawS [W][KS][DN]: raw orbital rows of S; env, Apl
-// [W][n][DN]: the state's envelope and orbital-matrix rows; env_p [W][DN]: the envelope row of the moved electron
-// e = moved[w] after the move.  B: the
+// [W][n][DN]: the state's envelope and orbital-matrix rows; env_p [W][KM][DN]: the envelope rows of the moved
+// electrons moved[w][0..KM) after the move.  B: the
 // transposed inverse, B[((w NDET + d) n + i) nA + sh + o] = (A^-1)[o][i] with nA = ainv_ld(n), sh = (d n) mod 4.
 // Writes V [W][NDET][KS][n] (A'[S] - A[S]), Minv [W][NDET][KS][KS] (double) and the proposal's slogdet
 // (ld_p, sd_p) = (ld + log|det M|, sd sign(det M)).  A set larger than KS (flagged by k_lr_select) gives sign 0:
@@ -211,7 +251,7 @@ __global__ void k_lr_env_add(long total, T* __restrict__ env_p, const T* __restr
 // of T (the staged V and B[S] columns).
 template <typename T>
 __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const int* __restrict__ S_cnt, int KS,
-                                                int n, const int* __restrict__ moved, const T* __restrict__ rawS,
+                                                int n, const int* __restrict__ moved, int KM, const T* __restrict__ rawS,
                                                 const T* __restrict__ env,
                                                 const T* __restrict__ env_p, const T* __restrict__ Apl,
                                                 const T* __restrict__ B, const double* __restrict__ ld,
@@ -227,7 +267,7 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
   __shared__ double fac[LR_KMAX];
   __shared__ int piv_row;
   const int d = blockIdx.x, w = blockIdx.y, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int e = moved[w], cnt = S_cnt[w];
+  const int cnt = S_cnt[w];
   const size_t md = (size_t)w * NDET + d;
   if (cnt > KS) {
     if (tid == 0) {
@@ -245,7 +285,9 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
   T* Vw = V + md * KS * n;
   for (long q = tid; q < (long)k * n; q += blockDim.x) {
     const int a = (int)(q / n), o = (int)(q - (long)a * n), c = sS[a];
-    const T* er = c == e ? env_p + (size_t)w * DN : env + ((size_t)w * n + c) * DN;
+    const T* er = env + ((size_t)w * n + c) * DN;
+    for (int t = 0; t < KM; ++t)
+      if (moved[(size_t)w * KM + t] == c) er = env_p + ((size_t)w * KM + t) * DN;
     const T an = rawS[((size_t)w * KS + a) * DN + (size_t)d * n + o] * er[(size_t)d * n + o];
     Vw[(size_t)a * n + o] = an - Apl[((size_t)w * n + c) * DN + (size_t)d * n + o];
   }
@@ -409,11 +451,12 @@ __global__ void __launch_bounds__(256) k_lr_jsums(int n, int n_up, const int* __
 
 // On acceptance (accf[w] != 0) the proposal's rows go into the state.  Blocks 0..KS-1: the rows of that slot's
 // changed center (embedding h, raw orbital and orbital-matrix rows, attention weight / value rows, MLP rows);
-// block KS: the moved electron's ElecInit and envelope rows, its e-n list, the statics and the slogdets.
+// blocks KS..KS+KM-1: a moved electron's ElecInit and envelope rows and its e-n list, block KS also the statics and
+// the slogdets.
 template <typename T>
 __global__ void __launch_bounds__(256) k_lr_commit(const int* __restrict__ accf, const int* __restrict__ S,
                                                    const int* __restrict__ S_cnt, int KS, int n,
-                                                   const int* __restrict__ moved,
+                                                   const int* __restrict__ moved, int KM,
                                                    const T* __restrict__ hS, const T* __restrict__ rawS,
                                                    const T* __restrict__ env_p, const T* __restrict__ aS,
                                                    const T* __restrict__ vS, const T* __restrict__ oS,
@@ -426,26 +469,34 @@ __global__ void __launch_bounds__(256) k_lr_commit(const int* __restrict__ accf,
                                                    double* __restrict__ ld, double* __restrict__ sd) {
   const int slot = blockIdx.x, w = blockIdx.y, tid = threadIdx.x;
   if (!accf[w]) return;
-  const int DN = NDET * n, e = moved[w];
-  if (slot == KS) {
-    const size_t g = (size_t)w * n + e;
-    for (int q = tid; q < 5 * F; q += blockDim.x) E5o[g * 5 * F + q] = E5p[(size_t)w * 5 * F + q];
-    for (int q = tid; q < DN; q += blockDim.x) env[g * DN + q] = env_p[(size_t)w * DN + q];
-    const int ce = en_cnt_p[w];
-    for (int q = tid; q < ce; q += blockDim.x) nb.en_idx[g * nb.cap_nuc + q] = en_idx_p[(size_t)w * nb.cap_nuc + q];
-    if (tid == 0) nb.en_cnt[g] = ce;
-    if (tid < 4) nb.counts[w * 4 + tid] = counts_p[w * 4 + tid];
-    if (tid < NDET) {
-      ld[(size_t)w * NDET + tid] = ld_p[(size_t)w * NDET + tid];
-      sd[(size_t)w * NDET + tid] = sd_p[(size_t)w * NDET + tid];
+  const int DN = NDET * n;
+  if (slot >= KS) {
+    const int t = slot - KS;
+    const size_t ms = (size_t)w * KM + t;
+    if (t == 0) {
+      if (tid < 4) nb.counts[w * 4 + tid] = counts_p[w * 4 + tid];
+      if (tid < NDET) {
+        ld[(size_t)w * NDET + tid] = ld_p[(size_t)w * NDET + tid];
+        sd[(size_t)w * NDET + tid] = sd_p[(size_t)w * NDET + tid];
+      }
     }
+    const int e = moved[ms];
+    if (e >= n) return;
+    const size_t g = (size_t)w * n + e;
+    for (int q = tid; q < 5 * F; q += blockDim.x) E5o[g * 5 * F + q] = E5p[ms * 5 * F + q];
+    for (int q = tid; q < DN; q += blockDim.x) env[g * DN + q] = env_p[ms * DN + q];
+    const int ce = en_cnt_p[ms];
+    for (int q = tid; q < ce; q += blockDim.x) nb.en_idx[g * nb.cap_nuc + q] = en_idx_p[ms * nb.cap_nuc + q];
+    if (tid == 0) nb.en_cnt[g] = ce;
     return;
   }
   if (slot >= min(S_cnt[w], KS)) return;
   const int c = S[(size_t)w * KS + slot];
   const size_t g = (size_t)w * n + c, row = (size_t)w * KS + slot;
-  // e's own envelope row is read from the proposal (block KS overwrites the state's row concurrently)
-  const T* er = c == e ? env_p + (size_t)w * DN : env + g * DN;
+  // a moved electron's envelope row is read from the proposal (the blocks from KS on overwrite the state's row)
+  const T* er = env + g * DN;
+  for (int t = 0; t < KM; ++t)
+    if (moved[(size_t)w * KM + t] == c) er = env_p + ((size_t)w * KM + t) * DN;
   for (int q = tid; q < F; q += blockDim.x) {
     h[g * F + q] = hS[row * F + q];
     vals[g * F + q] = vS[row * F + q];
@@ -597,18 +648,19 @@ __global__ void __launch_bounds__(256) k_lr_wb_apply(const int* __restrict__ acc
 }
 
 #define FIRE_INST_LR(T)                                                                                             \
-  template __global__ void k_lr_select<T>(const T*, const T*, int, int, const int*, const float*, int, T, T, Nbr, int, \
-                                          int*, int*, T*, int*, int*, int*, int32_t*, int32_t*);                     \
+  template __global__ void k_lr_select<T>(const T*, const T*, int, int, const int*, int, const float*, int, T, T, Nbr, \
+                                          int, int*, int*, T*, int*, int*, int*, int32_t*, int32_t*);                \
   template __global__ void k_lr_env_coef<T>(const T*, const float*, const T*, const T*, const int*, int, int, int, int,  \
-                                            T*, T*);                                                                  \
+                                            int, T*, T*);                                                             \
   template __global__ void k_lr_env_add<T>(long, T*, const T*);                                                      \
   template __global__ void k_lr_orb<T>(const int*, const int*, int, int, int, T*, const T*);                         \
-  template __global__ void k_lr_det<T>(const int*, const int*, int, int, const int*, const T*, const T*, const T*,   \
+  template __global__ void k_lr_det<T>(const int*, const int*, int, int, const int*, int, const T*, const T*, const T*, \
                                        const T*, const T*, const double*, const double*, T*, double*, double*,       \
                                        double*);                                                                      \
   template __global__ void k_lr_jsums<T>(int, int, const int*, const int*, int, const T*, const T*, const T*,        \
                                          const T*, const T*, const T*, T*, T*);                                       \
-  template __global__ void k_lr_commit<T>(const int*, const int*, const int*, int, int, const int*, const T*, const T*, \
+  template __global__ void k_lr_commit<T>(const int*, const int*, const int*, int, int, const int*, int, const T*,     \
+                                          const T*,                                                                  \
                                           const T*, const T*, const T*, const T*, const T*, const int*, const int*,   \
                                           const int*, const double*, const double*, T*, T*, T*, T*, T*, T*, T*, T*, \
                                           Nbr, double*, double*);                                                     \

@@ -194,7 +194,8 @@ __device__ int closest_k(PosFn pos, int n, const T (&c)[3], int k, T radius, int
 template <typename T>
 __global__ void k_propose_cluster(const T* __restrict__ r, T* __restrict__ rn, T* __restrict__ plr, int n, int w0,
                                   int B, int step, int offset, int k, T radius, T width, int random_sweep,
-                                  uint64_t seed, uint64_t counter, const T* __restrict__ replay) {
+                                  uint64_t seed, uint64_t counter, const T* __restrict__ replay,
+                                  int* __restrict__ moved_idx) {
   const int w = blockIdx.x;
   const long gw = w0 + w;
   const T* src = r + (long)w * 3 * n;
@@ -282,6 +283,8 @@ __global__ void k_propose_cluster(const T* __restrict__ r, T* __restrict__ rn, T
   for (int i = 0; i < cnt; ++i)
     for (int c = 0; c < 3; ++c) dst[3 * sel[i] + c] = chosen >= 0 ? moved[i][c] : first[i][c];
   plr[w] = chosen >= 0 ? T(0) : T(-INFINITY);
+  if (moved_idx)  // the cluster's index list, closest first, FIRE_NO_NEIGHBOUR beyond the radius (mcmc.py:141-143)
+    for (int i = 0; i < k; ++i) moved_idx[(long)w * k + i] = i < cnt ? sel[i] : FIRE_NO_NEIGHBOUR;
 }
 
 // Accept if 2 (logpsi_new - logpsi_old) > log u (mcmc.py:68-73); one CTA per walker.
@@ -337,9 +340,9 @@ template __global__ void k_propose_jump<float>(const float*, float*, float*, int
 template __global__ void k_propose_jump<double>(const double*, double*, double*, int, int, int, int, const float*,
                                                 const float*, int, double, uint64_t, uint64_t, const double*, int*);
 template __global__ void k_propose_cluster<float>(const float*, float*, float*, int, int, int, int, int, int, float,
-                                                  float, int, uint64_t, uint64_t, const float*);
+                                                  float, int, uint64_t, uint64_t, const float*, int*);
 template __global__ void k_propose_cluster<double>(const double*, double*, double*, int, int, int, int, int, int,
-                                                   double, double, int, uint64_t, uint64_t, const double*);
+                                                   double, double, int, uint64_t, uint64_t, const double*, int*);
 template __global__ void k_accept<float>(float*, const float*, float*, const float*, int, int, int, int, uint64_t,
                                          uint64_t, const float*, int32_t*, const int*, int32_t*, const float*, int32_t*);
 template __global__ void k_accept<double>(double*, const double*, double*, const double*, int, int, int, int,

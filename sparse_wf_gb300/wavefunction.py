@@ -462,6 +462,36 @@ class FireWaveFunction:
 
         return self._low_rank("fire_mcmc_low_rank_block", electrons, logpsi, static, cap_changed, launch)
 
+    def mcmc_low_rank_cluster_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
+                                    steps: int, width: float, max_cluster_size: int = 5,
+                                    max_cluster_radius: float = 2.0, sweep_type: str = "sequential",
+                                    step_offset: int = 0, seed: int = 0, counter: int = 0, replay_draws=None,
+                                    replay_log_u=None, cap_changed: Optional[int] = None):
+        """In-place Metropolis block of cluster updates (``proposal_cluster_update``, ``mcmc.py:119-161``) evaluated by
+        the low-rank update of a cached state: the proposals, draws (replay_draws [steps, B, 1 + 15 k]) and acceptance
+        of ``mcmc_cluster_block``, the cluster's electrons moved together.  Outputs and capacities as
+        ``mcmc_low_rank_block``."""
+        if sweep_type not in ("sequential", "random"):
+            raise ValueError(f"Invalid sweep_type: {sweep_type}")
+        p = self._params(params)
+        B = electrons.shape[0]
+        k = min(int(max_cluster_size), self.n_electrons)
+        draws = self._replay(replay_draws, (steps, B, 1 + 15 * k))
+        logu = self._replay(replay_log_u, (steps, B))
+
+        def launch(fn, prob, ws, cap, n_acc, smax):
+            return fn(self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()),
+                      C.c_void_p(self.Z_dev.data_ptr()), C.c_void_p(p.prepared.data_ptr()),
+                      C.c_void_p(electrons.data_ptr()), C.c_void_p(logpsi.data_ptr()), int(steps), int(step_offset),
+                      float(width), int(max_cluster_size), float(max_cluster_radius),
+                      int(sweep_type == "random"), int(cap), C.c_uint64(seed), C.c_uint64(counter),
+                      C.c_void_p(draws.data_ptr()) if draws is not None else None,
+                      C.c_void_p(logu.data_ptr()) if logu is not None else None, C.c_void_p(n_acc.data_ptr()),
+                      C.c_void_p(smax.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                      C.c_void_p(self._status.data_ptr()))
+
+        return self._low_rank("fire_mcmc_low_rank_cluster_block", electrons, logpsi, static, cap_changed, launch)
+
     def mcmc_low_rank_jump_block(self, params, electrons: torch.Tensor, logpsi: torch.Tensor, static: StaticArgs,
                                  steps: int, sigma: float = 2.0, seed: int = 0, counter: int = 0, replay_draws=None,
                                  replay_log_u=None, cap_changed: Optional[int] = None):
@@ -681,8 +711,9 @@ def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, pr
     (sigma 2, ``mcmc.py:320-326, 332-335``; 20 in the reference's defaults); "cluster-update" runs
     ``int(sweeps * n_el)`` cluster moves (``mcmc.py:305-316``; sequential sweeps must be whole):
     ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed.  low_rank
-    evaluates the single-electron moves and the jumps from a state per walker (``mcmc_low_rank_block``,
-    ``mcmc_low_rank_jump_block``) instead of in full; stats then also hold the move statics."""
+    evaluates the single-electron moves, the cluster updates and the jumps from a state per walker
+    (``mcmc_low_rank_block``, ``mcmc_low_rank_cluster_block``, ``mcmc_low_rank_jump_block``) instead of in full;
+    stats then also hold the move statics."""
     proposal = proposal.lower()
     if proposal not in ("all-electron", "single-electron", "cluster-update"):
         raise ValueError(f"Invalid proposal: {proposal}")
@@ -709,6 +740,10 @@ def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, pr
             stats["static_max_jump"] = smax_jump
         if proposal == "all-electron":
             n_acc, smax = wf.mcmc_block(p, r, logpsi, static, n_steps, float(width), seed=int(key))
+        elif proposal == "cluster-update" and low_rank:
+            n_acc, smax, stats["changed_max"] = wf.mcmc_low_rank_cluster_block(
+                p, r, logpsi, static, n_steps, float(width), max_cluster_size, max_cluster_radius, sweep_type,
+                seed=int(key))
         elif proposal == "cluster-update":
             n_acc, smax = wf.mcmc_cluster_block(p, r, logpsi, static, n_steps, float(width), max_cluster_size,
                                                 max_cluster_radius, sweep_type, seed=int(key))

@@ -186,3 +186,39 @@ def test_make_mcmc_low_rank_matches_full(cuda_lib):
     same = np.all(np.abs(ra.cpu().numpy() - rb.cpu().numpy()) < 1e-10, axis=(1, 2))
     assert same.sum() >= len(same) - 1
     assert sb["changed_max"][0] >= 1 and sb["changed_max_jump"][0] >= 1
+
+
+@pytest.mark.parametrize("random_sweep", [False, True])
+def test_low_rank_cluster_block_matches_oracle(cuda_lib, random_sweep):
+    """FP64 build: cluster updates (k = 4 within radius 1.2 on H10, so the index lists carry padding) evaluated from the
+    state take the decisions of the oracle's state-carrying block (cluster_low_rank_block) where the margin is clear of
+    rounding, with its final positions (1e-12), log|psi| (1e-8) and move statics, padded entries gathering electron
+    n - 1."""
+    wf, mol, nu, r, p, rr, static = _setup("h10", "fp64")
+    B, n = r.shape[0], mol.n_el
+    steps, k, radius, width = n + 2, 4, 1.2, 0.3
+    rng = np.random.default_rng(43)
+    draws = np.concatenate([rng.uniform(size=(steps, B, 1)), rng.standard_normal((steps, B, 15 * k))], axis=2)
+    logu = np.log(rng.uniform(size=(steps, B)))
+    dp = wf._params(p)
+    logpsi = torch.zeros(B, dtype=torch.float64, device="cuda")
+    n_acc, _, changed = wf.mcmc_low_rank_cluster_block(
+        dp, rr, logpsi, static, steps, width, k, radius, "random" if random_sweep else "sequential", step_offset=1,
+        replay_draws=draws, replay_log_u=logu)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    got_r, got_n = rr.cpu().numpy(), n_acc.cpu().numpy()
+    cmax = np.zeros(3, np.int64)
+    checked = 0
+    for w in range(B):
+        r_ref, lp_ref, na, mg, cm = O.cluster_low_rank_block(prob, p, r[w].astype(np.float64), draws[:, w],
+                                                             logu[:, w], float(np.float32(width)), k,
+                                                             float(np.float32(radius)), random_sweep=random_sweep,
+                                                             offset=1)
+        cmax = np.maximum(cmax, cm)
+        if np.all(np.abs(mg[np.isfinite(mg)]) > 1e-6):
+            checked += 1
+            assert got_n[w] == na, w
+            np.testing.assert_allclose(got_r[w], r_ref, atol=1e-12)
+            np.testing.assert_allclose(logpsi[w].item(), 0.5 * lp_ref, rtol=1e-8)
+    assert checked > 0
+    assert tuple(changed) == tuple(int(x) for x in cmax)
