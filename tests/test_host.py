@@ -353,3 +353,17 @@ def test_low_rank_jump_and_ecp_argument_checks(lib):
     assert lib.fire_ecp_energy(None, C.byref(prob), d, d, d, d, None, 32, 0, 0, None, d, None, d, C.c_size_t(1),
                                d) == 1
     assert ecp(n_l=5) == 1 and ecp(max_quad=13) == 1 and ecp(n_grid=1) == 1 and ecp(n_ecp=0) == 1
+
+
+def test_low_rank_cluster_argument_checks(lib):
+    """fire_mcmc_low_rank_cluster_block rejects, before any CUDA call and through its ctypes signature, a zero
+    capacity, a negative radius, half a replay (1), and a cluster above 16 electrons or a capacity above 128 (2)."""
+    prob = _lib.Problem(82, 41, 32, 4, 5.0, 20.0, 2500, 40, 0, 0)
+    d = C.c_void_p(16)
+
+    def call(k=5, radius=2.0, cap=32, draws=None, logu=None):
+        return lib.fire_mcmc_low_rank_cluster_block(None, C.byref(prob), d, d, d, d, d, 4, 0, 0.2, k, radius, 0, cap,
+                                                    0, 0, draws, logu, None, None, d, C.c_size_t(1), d)
+
+    assert call(cap=0) == 1 and call(radius=-1.0) == 1 and call(draws=d) == 1
+    assert call(k=17) == 2 and call(cap=129) == 2
