@@ -367,3 +367,42 @@ def test_low_rank_cluster_argument_checks(lib):
 
     assert call(cap=0) == 1 and call(radius=-1.0) == 1 and call(draws=d) == 1
     assert call(k=17) == 2 and call(cap=129) == 2
+
+
+def test_checkpoint_round_trip_and_reference_mapping(tmp_path):
+    """checkpoint.save / load keep every parameter slot, the walkers, the width scheduler's state and the step;
+    load_reference_params reads an expanded checkpoint (leaf paths joined by "/", loggers.py:191-208) through an
+    explicit mapping, applies per-leaf transforms, checks shapes and reports unmapped leaves."""
+    from sparse_wf_gb300 import checkpoint
+    from sparse_wf_gb300.wavefunction import make_width_scheduler
+
+    mol = systems.alkane(2)
+    nu, _ = systems.spin_counts(mol)
+    dims = P.ModelDims(mol.n_el, nu, mol.n_nuc)
+    p = P.init_params(dims, 3)
+    r = systems.init_electrons(mol, 4, 2)
+    init, update = make_width_scheduler(window_size=3)
+    ws = update(update(init(0.4), 0.6), 0.7)
+    checkpoint.save(str(tmp_path / "c.npz"), p, r, ws, 17)
+    back = checkpoint.load(str(tmp_path / "c.npz"), dims)
+    for k in p:
+        np.testing.assert_array_equal(back["params"][k], p[k])
+    np.testing.assert_array_equal(back["electrons"], r)
+    assert back["step"] == 17 and back["width_state"] == ws
+    # an expanded reference checkpoint with made-up leaf paths; one stored transposed, one extra leaf
+    leaves = {f"embedding/{k}": v for k, v in p.items()}
+    leaves["embedding/orb_up_W"] = p["orb_up_W"].T
+    leaves["opt/unused"] = np.zeros(3)
+    (tmp_path / "ref").mkdir()
+    np.savez(tmp_path / "ref" / "params.npz", **leaves)
+    mapping = {k: f"embedding/{k}" for k in p}
+    mapping["orb_up_W"] = ("embedding/orb_up_W", np.transpose)
+    got = checkpoint.load_reference_params(str(tmp_path / "ref"), dims, mapping)
+    for k in p:
+        np.testing.assert_array_equal(got["params"][k], p[k])
+    assert got["unused_leaves"] == ["opt/unused"]
+    with pytest.raises(ValueError):
+        checkpoint.load_reference_params(str(tmp_path / "ref"), dims, {**mapping, "orb_up_W": "embedding/orb_up_W"})
+    with pytest.raises(KeyError):
+        checkpoint.load_reference_params(str(tmp_path / "ref"), dims, {k: v for k, v in mapping.items()
+                                                                         if k != "cusp"})
