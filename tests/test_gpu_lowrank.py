@@ -31,6 +31,33 @@ def _draws(B, steps, seed):
     return rng.standard_normal((steps, B, 3)), np.log(rng.uniform(size=(steps, B)))
 
 
+@pytest.mark.parametrize("steps", [1, 2, 3])
+@pytest.mark.parametrize("name", ["h10", "c2h6"])
+def test_low_rank_forced_accept_stages(cuda_lib, name, steps):
+    """Stages of the low-rank step, FP64 build, every proposal accepted (log u = -inf): after 1 step log|psi| is the
+    low-rank evaluation of the proposal alone (changed rows, determinant lemma, Jastrow sums); after 2 and 3 steps it
+    also depends on the commit of the previous rows and the Woodbury update of the inverse.  Each is compared with a
+    full evaluation of the final positions (1e-10)."""
+    wf, mol, nu, r, p, rr, static = _setup(name, "fp64")
+    B, n = r.shape[0], mol.n_el
+    noise, _ = _draws(B, steps, 53)
+    logu = np.full((steps, B), -1e300)
+    dp = wf._params(p)
+    logpsi = torch.zeros(B, dtype=torch.float64, device="cuda")
+    n_acc, _, _ = wf.mcmc_low_rank_block(dp, rr, logpsi, static, steps, 0.4, step_offset=2, replay_noise=noise,
+                                         replay_log_u=logu)
+    assert n_acc.cpu().numpy().tolist() == [steps] * B
+    prob = O.Problem(mol.R, mol.Z, nu)
+    got = rr.cpu().numpy()
+    for w in range(B):
+        expect = r[w].astype(np.float64).copy()
+        for s_ in range(steps):
+            e = (2 + s_) % n
+            expect[e] += float(np.float32(0.4)) * noise[s_, w]
+        np.testing.assert_allclose(got[w], expect, atol=1e-12)
+        np.testing.assert_allclose(logpsi[w].item(), O.logpsi(prob, p, expect)[1], rtol=1e-10)
+
+
 @pytest.mark.parametrize("name", ["h10", "c2h6"])
 def test_low_rank_block_replay_matches_oracle(cuda_lib, name):
     """FP64 build: the decisions of the oracle's state-carrying block (mcmc_low_rank_block) wherever its Metropolis
