@@ -2,10 +2,11 @@
 
 ``FireWaveFunction`` follows ``MoonLikeWaveFunction`` (``src/sparse_wf/model/wave_function.py:67-221``)
 for the ``new_sparse`` embedding: ``init``, ``get_static_input``, ``signed``, ``__call__``,
-``kinetic_energy``; ``make_local_energy`` follows ``hamiltonian.py:49-83`` (all-electron, no
-pseudopotentials) and ``make_mcmc`` the all-electron branch of ``mcmc.py:278-346``.  Every numerical
-call goes to ``libfire.so`` through its C ABI (``include/fire.h``) on the current CUDA stream; torch
-only provides device memory and streams.
+``kinetic_energy``, the Metropolis blocks of every proposal (evaluated in full or, the ``*_low_rank_*`` ones, from
+a state per walker) and the pseudopotential energy; ``make_local_energy`` follows ``hamiltonian.py:49-83``,
+``make_mcmc`` ``mcmc.py:278-346`` and ``make_width_scheduler`` ``mcmc.py:349-378``.  Every numerical call goes
+to ``libfire.so`` through its C ABI (``include/fire.h``) on the current CUDA stream; torch only provides device
+memory and streams.
 
 Static shapes: the reference compiles for padded ``StaticArgs`` sizes and grows them on the host
 (``static_args.py:62-84``).  Here the sizes are capacities of the device buffers; the kernels report
