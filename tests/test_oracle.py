@@ -342,3 +342,29 @@ def test_parameter_jvp_closed_forms():
     assert np.sign(j1) == J1[0]
     got = O.logpsi_jvp(prob, p, w, {"log_bias": np.ones_like(p["log_bias"])})
     assert abs(got - n / j1) <= 1e-10 * max(1.0, abs(n / j1))
+
+
+def test_isolated_electron_empty_neighbour_list():
+    """An electron without e-e neighbours (a hydrogen atom 30 bohr from an H4 chain, its electron near its nucleus):
+    its pair lists are empty, its row of the sparse Jacobian holds only the self position, and the sparse forward
+    Laplacian still equals the finite-difference gradient and Laplacian of log|psi| (FP64)."""
+    from make_golden import make_params
+    from sparse_wf_gb300 import systems
+
+    R = np.array([[0.0, 0, 0], [1.8, 0, 0], [3.6, 0, 0], [5.4, 0, 0], [35.4, 0, 0]], np.float32)
+    mol = systems.Molecule("H4+H", R, np.ones(5, np.int64))
+    nu, _ = systems.spin_counts(mol)
+    rng = np.random.default_rng(2)
+    w = np.concatenate([R[:4] + 0.5 * rng.standard_normal((4, 3)), R[4:] + 0.3 * rng.standard_normal((1, 3))])
+    w = w.astype(np.float32)
+    _, p, _, _ = make_params(mol, nu, w)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    inc = O.in_cutoff_matrix(w, prob.cutoff)
+    iso = int(np.nonzero(~inc.any(1))[0][0])
+    assert not inc[iso].any() and not inc[:, iso].any()
+    w = w.astype(np.float64)
+    v, j, l = O.logpsi_fl(prob, p, w)
+    y0, G, L = _fd(lambda x: O.logpsi(prob, p, x.reshape(-1, 3))[1], w.reshape(-1), 2e-4)
+    assert abs(v - y0) < 1e-12 * abs(y0)
+    np.testing.assert_allclose(j, G, rtol=1e-6, atol=1e-6 * np.abs(G).max())
+    assert rel(-0.5 * (l + j @ j), -0.5 * (L + G @ G)) < 1e-5
