@@ -406,3 +406,41 @@ def test_checkpoint_round_trip_and_reference_mapping(tmp_path):
     with pytest.raises(KeyError):
         checkpoint.load_reference_params(str(tmp_path / "ref"), dims, {k: v for k, v in mapping.items()
                                                                          if k != "cusp"})
+
+
+def test_ragged_autotuner_selection(monkeypatch):
+    """ragged.Autotuner without a GPU (RaggedBatch and the CUDA calls faked): candidates whose workspaces exceed the
+    HBM budget are not built, the fastest of the rest is kept per batch signature (a second call is a cache hit),
+    and no fitting candidate raises."""
+    from sparse_wf_gb300 import ragged
+
+    built, clock = [], [0.0]
+    cost = {(1, 64): 3.0, (2, 64): 1.0, (4, 64): 2.0}
+
+    class FakeBatch:
+        def __init__(self, mols, walkers, precision, lanes, chunk, device):
+            self.key = (lanes, chunk)
+            built.append(self.key)
+
+        def workspace_bytes(self):
+            return [10e9 * self.key[0]]
+
+        def run(self):
+            pass
+
+        def replay(self):
+            clock[0] += cost[self.key]
+
+    monkeypatch.setattr(ragged, "RaggedBatch", FakeBatch)
+    monkeypatch.setattr(ragged.time, "perf_counter", lambda: clock[0])
+    monkeypatch.setattr(ragged.torch.cuda, "synchronize", lambda *a: None)
+    monkeypatch.setattr(ragged.torch.cuda, "empty_cache", lambda *a: None)
+    tuner = ragged.Autotuner(candidates=[(1, 64), (2, 64), (4, 64), (8, 32)], budget_bytes=45e9, reps=2)
+    mols = [systems.alkane(2), systems.alkane(3)]
+    best = tuner.tune(mols, [64, 128])
+    assert (best["lanes"], best["chunk"]) == (2, 64) and best["seconds"] == 1.0
+    assert [t["lanes"] for t in best["trials"]] == [1, 2, 4]  # 8 lanes (80 GB) exceeds the budget
+    n_built = len(built)
+    assert tuner.tune(mols, [64, 128]) is best and len(built) == n_built
+    with pytest.raises(RuntimeError):
+        ragged.Autotuner(candidates=[(8, 32)], budget_bytes=45e9).tune(mols, [64, 128])
