@@ -444,3 +444,63 @@ def test_ragged_autotuner_selection(monkeypatch):
     assert tuner.tune(mols, [64, 128]) is best and len(built) == n_built
     with pytest.raises(RuntimeError):
         ragged.Autotuner(candidates=[(8, 32)], budget_bytes=45e9).tune(mols, [64, 128])
+
+
+def test_serving_loop_admission_retry_and_completion():
+    """ServingEngine.run's host loop without a GPU (launch, completion and workspace faked): requests are admitted in
+    arrival order to free slots, a request whose state would exceed the HBM budget waits until memory is released, a
+    capacity overflow sends its request back to the front of the queue with grown capacities, and every request
+    completes once with its latency recorded."""
+    from sparse_wf_gb300 import serving
+    from sparse_wf_gb300.wavefunction import StaticArgs
+
+    class Event:
+        def __init__(self, ready):
+            self.ready = ready
+
+        def query(self):
+            return self.ready()
+
+    class FakeModel:
+        static = StaticArgs(10, 10, 0, 4)
+
+    class Engine(serving.ServingEngine):
+        def __init__(self):
+            self.lanes, self.budget, self.in_use, self.max_walkers, self.ws_bytes = 2, 3000.0, 0, 4096, 1 << 30
+            self.log, self.overflowed, self.peak = [], set(), 0
+
+        def model(self, n_carbon):
+            return FakeModel()
+
+        def warm(self, trace):
+            pass
+
+        def _ws_need(self, m, walkers, static):
+            return 1
+
+        def _state_bytes(self, req, m):
+            return req.walkers
+
+        def _launch(self, req, lane, static, now):
+            self.log.append((req.rid, lane, static.n_pairs_same))
+            self.peak = max(self.peak, self.in_use)
+            t0 = serving.time.perf_counter()
+            return serving._Active(req, lane, static, req.walkers, None, None, None, None, None, None, {},
+                                   Event(lambda: serving.time.perf_counter() - t0 > 0.01))
+
+        def _finish(self, a, now):
+            if a.req.rid == 1 and a.req.rid not in self.overflowed:
+                self.overflowed.add(a.req.rid)
+                return StaticArgs(20, 20, 0, 6)
+            a.req.done = now
+            return None
+
+    trace = [serving.Request(rid=i, kind="eloc", n_carbon=4, walkers=w, arrival=0.0)
+             for i, w in enumerate([1000, 1500, 2000, 500])]
+    eng = Engine()
+    eng.run(trace, timeout=30.0)
+    assert [rid for rid, _, _ in eng.log[:2]] == [0, 1]
+    assert eng.peak <= 3000  # the 2000-walker request waited for memory
+    retried = [x for x in eng.log if x[0] == 1]
+    assert len(retried) == 2 and retried[1][2] == 20 and trace[1].retries == 1
+    assert all(np.isfinite(r.done) and r.done >= r.arrival for r in trace) and len(eng.log) == 5
