@@ -504,3 +504,25 @@ def test_serving_loop_admission_retry_and_completion():
     retried = [x for x in eng.log if x[0] == 1]
     assert len(retried) == 2 and retried[1][2] == 20 and trace[1].retries == 1
     assert all(np.isfinite(r.done) and r.done >= r.arrival for r in trace) and len(eng.log) == 5
+
+
+def test_bench_reference_arm_json_contract():
+    """bench.py --impl reference (the CPU arm: the oracle port on bounded samples) prints one JSON line with the
+    contract's keys, impl "reference", a cpu_baseline describing the run and an e2e object without host-device bytes."""
+    import json
+    import subprocess
+    import sys
+
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--system", "c2h6",
+                          "--steps", "1", "--warmup", "0", "--cpu-sample", "1", "--walkers", "64"],
+                         capture_output=True, text=True, timeout=600, cwd=str(ROOT))
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
