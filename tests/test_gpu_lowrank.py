@@ -249,3 +249,31 @@ def test_low_rank_cluster_block_matches_oracle(cuda_lib, random_sweep):
             np.testing.assert_allclose(logpsi[w].item(), 0.5 * lp_ref, rtol=1e-8)
     assert checked > 0
     assert tuple(changed) == tuple(int(x) for x in cmax)
+
+
+def test_ecp_energy_local_channel_only(cuda_lib):
+    """Stage of the pseudopotential energy: element data with only a local channel (no non-local channels, so no
+    quadrature point is active); fire_ecp_energy then equals the oracle's local term (1e-10), which isolates the
+    radial tables and k_ecp_local from the low-rank ratios."""
+    from oracle import ecp_oracle as E
+    from sparse_wf_gb300 import params as P, systems
+    from sparse_wf_gb300.ecp import EcpTables
+
+    carbon = (2, [(-1, [[], [(14.0, 4.0)], [(8.0, 50.0)], [(13.0, -25.0)]])])
+    mol = systems.alkane(2)
+    tables = EcpTables(mol.Z, {6: carbon}, n_quad={6: 4})
+    assert tables.v_nl.shape[1] == 0
+    val = systems.Molecule("C2H6-valence", mol.R, tables.z_eff)
+    nu, _ = systems.spin_counts(val)
+    r = systems.init_electrons(val, 3, 93).astype(np.float64)
+    dims = P.ModelDims(val.n_el, nu, val.n_nuc)
+    p = P.unpack_params(dims, *P.pack_params(dims, P.init_params(dims, 0), np.float32))
+    wf = FireWaveFunction(val, precision="fp64")
+    rr = torch.from_numpy(r).cuda()
+    s = wf.get_static_input(rr)
+    static = StaticArgs(s.n_pairs_same, s.n_pairs_diff, s.n_triplets, s.n_neighbours_en)
+    got, _ = wf.ecp_energy(wf._params(p), rr, static, tables.device("cuda"))
+    ecp = E.Ecp(mol.Z, mol.R, {6: (2, [(-1, carbon[1][0][1]), (0, [[]])])}, n_quad={6: 4})
+    for w in range(len(r)):
+        ref = E.local_term(ecp, r[w])
+        assert abs(got[w].item() - ref) <= 1e-10 * max(1.0, abs(ref)), w
