@@ -526,3 +526,45 @@ def test_bench_reference_arm_json_contract():
     assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_ecp_energy_wrapper_reruns(monkeypatch):
+    """FireWaveFunction.ecp_energy's host loop against a fake library: a changed-set overflow reruns with the set the
+    device reported, a pair overflow first grows the neighbour capacity, and the energies and move statics come back
+    from the last call."""
+    import torch
+
+    from sparse_wf_gb300.ecp import EcpTables
+    from sparse_wf_gb300.wavefunction import StaticArgs
+
+    class Fake(_FakeLowRankLib):
+        def fire_ecp_energy(self, stream, prob, R, Z, prepared, r, ecp, cap, seed, counter, rot, out, smax, ws, wsb,
+                            status):
+            pr = prob._obj
+            self.calls.append((int(cap), int(pr.cap_pairs), ecp._obj.n_ecp, ecp._obj.max_quad))
+            st = (C.c_int32 * _lib.STATUS_WORDS).from_address(status.value)
+            if self.pair_overflow and len(self.calls) == 1:
+                st[0] |= _lib.FLAG_PAIR_OVERFLOW
+                st[1] = 4 * pr.cap_pairs
+                return 0
+            if cap < self.need:
+                st[0] |= _lib.FLAG_CHANGED_OVERFLOW
+                st[4] = self.need
+                return 0
+            o = (C.c_float * pr.n_walkers).from_address(out.value)
+            for k in range(pr.n_walkers):
+                o[k] = 1.5 + k
+            sm = (C.c_int32 * 7).from_address(smax.value)
+            for k, v in enumerate([0, 0, 0, 0, self.need, 7, 8]):
+                sm[k] = v
+            return 0
+
+    fake = Fake(need=12, pair_overflow=True)
+    wf, mol, r = _fake_wf(monkeypatch, fake)
+    carbon = (2, [(-1, [[], [(14.0, 4.0)]]), (0, [[], [], [(7.0, 50.0)]])])
+    tables = EcpTables(systems.alkane(2).Z, {6: carbon}, n_quad={6: 4})
+    out, changed = wf.ecp_energy(P.init_params(wf.dims, 0), r, StaticArgs(40, 40, 0, 8), tables.device("cpu"),
+                                 cap_changed=4)
+    caps, pairs, n_ecp, qmax = zip(*fake.calls)
+    assert caps == (4, 4, 14) and pairs[1] > pairs[0] and set(n_ecp) == {2} and set(qmax) == {4}
+    assert out.tolist() == [1.5, 2.5] and changed == (12, 7, 8) and wf._lr_cap == 14
