@@ -1,7 +1,5 @@
 """Edge cases of the local-energy path through the C ABI: an electron with an empty e-e neighbour list (its row of the
-sparse Jacobian holds only the self position, its pair lists and triplets are empty).
-
-Skipped until their first run on a GB300: written after the last GPU run that could have executed them."""
+sparse Jacobian holds only the self position, its pair lists and triplets are empty)."""
 import numpy as np
 import pytest
 
@@ -10,7 +8,7 @@ from sparse_wf_gb300.wavefunction import FireWaveFunction
 
 from test_gpu_parity import _check_local_energy
 
-pytestmark = [pytest.mark.gpu, pytest.mark.skip(reason="edge cases not yet run on a GPU")]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64", "mixed"])

@@ -1,10 +1,7 @@
 """Parity of the low-rank single-electron block (fire_mcmc_low_rank_block: mcmc_steps_low_rank with the state-carrying
 log_psi_low_rank_update, mcmc.py:196-275, model/wave_function.py:226-287) with the oracle's state-carrying block and
 with the device's full-evaluation block, on replayed draws; and of the pseudopotential energy (fire_ecp_energy), whose
-psi ratios come from the same low-rank evaluation, with the oracle's restatement.
-
-The whole module is skipped until these kernels have had their first run on a GB300: they are compiled and their
-index arithmetic was checked by reading, but not yet executed."""
+psi ratios come from the same low-rank evaluation, with the oracle's restatement."""
 import numpy as np
 import pytest
 import torch
@@ -13,7 +10,7 @@ from helpers import case
 from oracle import fire_oracle as O
 from sparse_wf_gb300.wavefunction import FireWaveFunction, StaticArgs
 
-pytestmark = [pytest.mark.gpu, pytest.mark.skip(reason="low-rank kernels not yet run on a GPU")]
+pytestmark = pytest.mark.gpu
 
 
 def _setup(name, precision):
@@ -137,8 +134,11 @@ def test_low_rank_capacity_overflow_reruns(cuda_lib):
 
 def test_ecp_energy_matches_oracle(cuda_lib):
     """fire_ecp_energy in the FP64 build with replayed rotations: the local term plus the non-local quadrature with
-    low-rank psi ratios against the oracle's restatement (oracle/ecp_oracle.py), 1e-8 relative, on C2H6 with a
-    synthetic pseudised carbon (2 core electrons, local, s and p channels; tetrahedral quadrature)."""
+    low-rank psi ratios against the oracle's restatement (oracle/ecp_oracle.py), 1e-7 relative, on C2H6 with a
+    synthetic pseudised carbon (2 core electrons, local, s and p channels; tetrahedral quadrature).  Each ratio is
+    exp(log|psi'| - log|psi|) of two FP64 evaluations that agree with the oracle to ~1e-10 relative in log|psi|
+    (the forced-accept bound), i.e. a few 1e-9 in the ratio; the channel weights (up to 50 here, times 2l + 1) add
+    an order of magnitude over the sum."""
     from oracle import ecp_oracle as E
     from sparse_wf_gb300 import params as P, systems
     from sparse_wf_gb300.ecp import EcpTables
@@ -167,7 +167,7 @@ def test_ecp_energy_matches_oracle(cuda_lib):
     ecp = E.Ecp(mol.Z, mol.R, {6: carbon}, n_quad={6: 4})
     for w in range(len(r)):
         ref = E.local_term(ecp, r[w]) + E.nonlocal_term(prob, p, ecp, r[w], rot[w])
-        assert abs(got[w].item() - ref) <= 1e-8 * max(1.0, abs(ref)), w
+        assert abs(got[w].item() - ref) <= 1e-7 * max(1.0, abs(ref)), w
     assert changed[0] >= 1
 
 
@@ -206,7 +206,7 @@ def test_make_mcmc_low_rank_matches_full(cuda_lib):
     from sparse_wf_gb300.wavefunction import make_mcmc
 
     wf, mol, nu, r, p, rr, static = _setup("h10", "fp64")
-    full, _ = make_mcmc(wf, proposal="single-electron", sweeps=1.0, jump_steps=4, init_width=0.3)
+    full, _ = make_mcmc(wf, proposal="single-electron", sweeps=1.0, jump_steps=4, init_width=0.3, low_rank=False)
     lowr, _ = make_mcmc(wf, proposal="single-electron", sweeps=1.0, jump_steps=4, init_width=0.3, low_rank=True)
     ra, sa = full(7, p, rr, static, 0.3)
     rb, sb = lowr(7, p, rr, static, 0.3)
