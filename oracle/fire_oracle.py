@@ -1229,3 +1229,74 @@ def cluster_low_rank_block(prob, p, r, draws, log_u, width, k, radius, random_sw
         return rn, idx, plr
 
     return mcmc_low_rank_block(prob, p, r, propose, log_u)
+
+
+# =============================================================================== Philox draws of the device blocks
+# The device Metropolis blocks draw from Philox4x32-10 (Salmon, Moraes, Dror & Shaw, "Parallel random numbers: as
+# easy as 1, 2, 3", SC'11): 10 rounds of the multiply-xor round function with the Weyl key schedule.  This numpy
+# restatement regenerates the all-electron block's draws on the CPU, so that the CPU baseline can run the same
+# Metropolis block as the device (the reference itself draws from jax's threefry, which cannot be reproduced here).
+PHILOX_M = (0xD2511F53, 0xCD9E8D57)
+PHILOX_W = (0x9E3779B9, 0xBB67AE85)
+_U32 = np.uint64(0xFFFFFFFF)
+
+
+def philox4x32_10(ctr, key):
+    """Philox4x32-10 of counters ctr [..., 4] under keys key [..., 2] (uint32 values): [..., 4] uint32."""
+    ctr = np.asarray(ctr, np.uint64)
+    key = np.asarray(key, np.uint64)
+    c0, c1, c2, c3 = (ctr[..., i] for i in range(4))
+    k0, k1 = key[..., 0], key[..., 1]
+    m0, m1 = np.uint64(PHILOX_M[0]), np.uint64(PHILOX_M[1])
+    for _ in range(10):
+        p0, p1 = m0 * c0, m1 * c2  # 32 x 32 -> 64-bit products, exact in uint64
+        c0, c1, c2, c3 = (p1 >> np.uint64(32)) ^ c1 ^ k0, p1 & _U32, (p0 >> np.uint64(32)) ^ c3 ^ k1, p0 & _U32
+        k0 = (k0 + np.uint64(PHILOX_W[0])) & _U32
+        k1 = (k1 + np.uint64(PHILOX_W[1])) & _U32
+    return np.stack([c0, c1, c2, c3], -1).astype(np.uint32)
+
+
+def _philox_key(seed, counter):
+    k = (int(seed) ^ ((int(counter) >> 32) * 0x9E3779B97F4A7C15)) & 0xFFFFFFFFFFFFFFFF
+    return np.array([k & 0xFFFFFFFF, k >> 32], np.uint64)
+
+
+def _u01(x):
+    return ((np.asarray(x, np.uint64) >> np.uint64(8)).astype(np.float64) + 0.5) * (1.0 / 16777216.0)
+
+
+def philox_all_electron_noise(seed, counter, step, walker, n):
+    """The device's all-electron proposal normals eps [n, 3] (float32) of one walker and step: counter (step,
+    walker, electron, counter), Box-Muller on the four uniforms."""
+    ctr = np.zeros((n, 4), np.uint64)
+    ctr[:, 0], ctr[:, 1], ctr[:, 2], ctr[:, 3] = step, walker, np.arange(n), int(counter) & 0xFFFFFFFF
+    x = philox4x32_10(ctr, np.broadcast_to(_philox_key(seed, counter), (n, 2)))
+    r1, t1 = np.sqrt(-2.0 * np.log(_u01(x[:, 0]))), 2.0 * np.pi * _u01(x[:, 1])
+    r2, t2 = np.sqrt(-2.0 * np.log(_u01(x[:, 2]))), 2.0 * np.pi * _u01(x[:, 3])
+    return np.stack([r1 * np.cos(t1), r1 * np.sin(t1), r2 * np.cos(t2)], -1).astype(np.float32)
+
+
+def philox_log_u(seed, counter, step, walker):
+    """The device's Metropolis log-uniform of one walker and step: counter (step, walker, 0xFFFFFFFF, counter)."""
+    ctr = np.array([[step, walker, 0xFFFFFFFF, int(counter) & 0xFFFFFFFF]], np.uint64)
+    return float(np.log(_u01(philox4x32_10(ctr, _philox_key(seed, counter)[None])[0, 0])))
+
+
+def mcmc_block_philox(prob, p, r, steps, width, seed, counter, walker):
+    """The all-electron Metropolis block (``mcmc.py:38-97``) of walker index ``walker`` with the device's Philox
+    draws: positions stay float32 (r' = r + width eps, one rounding), log|psi| in FP64.  Returns (r float32,
+    n_accept, margins)."""
+    r = np.asarray(r, np.float32)
+    w32 = np.float32(width)
+    lp = 2.0 * logpsi(prob, p, r.astype(np.float64))[1]
+    n_acc, margins = 0, []
+    for s in range(steps):
+        eps = philox_all_electron_noise(seed, counter, s, walker, r.shape[0])
+        rn = (r.astype(np.float64) + np.float64(w32) * eps.astype(np.float64)).astype(np.float32)
+        lpn = 2.0 * logpsi(prob, p, rn.astype(np.float64))[1]
+        m = (lpn - lp) - philox_log_u(seed, counter, s, walker)
+        margins.append(m)
+        if m > 0:
+            r, lp = rn, lpn
+            n_acc += 1
+    return r, n_acc, np.array(margins)

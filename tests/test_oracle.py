@@ -368,3 +368,20 @@ def test_isolated_electron_empty_neighbour_list():
     assert abs(v - y0) < 1e-12 * abs(y0)
     np.testing.assert_allclose(j, G, rtol=1e-6, atol=1e-6 * np.abs(G).max())
     assert rel(-0.5 * (l + j @ j), -0.5 * (L + G @ G)) < 1e-5
+
+
+def test_philox_known_answers():
+    """The numpy Philox4x32-10 (the CPU replay of the device draws) against the generator's published known-answer
+    vectors (Salmon et al., SC'11, Random123 kat_vectors): zero counter and key, all-ones, and the pi digits."""
+    cases = [([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+             ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+             ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+              [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1])]
+    for ctr, key, want in cases:
+        assert O.philox4x32_10(ctr, key).tolist() == want
+    # vectorised over counters: each row as its own call
+    ctr = np.array([[s, w, e, 3] for s in range(2) for w in range(3) for e in range(4)], np.uint64)
+    key = np.broadcast_to(np.array([7, 0], np.uint64), (len(ctr), 2))
+    many = O.philox4x32_10(ctr, key)
+    for k in range(len(ctr)):
+        assert many[k].tolist() == O.philox4x32_10(ctr[k], key[k]).tolist()
