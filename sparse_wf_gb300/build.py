@@ -71,6 +71,35 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+def jax_ffi_include() -> Path | None:
+    """jaxlib's FFI header directory (xla/ffi/api/ffi.h), or None where jax is not installed."""
+    try:
+        import jax
+    except ImportError:
+        return None
+    inc = Path(jax.ffi.include_dir())
+    return inc if (inc / "xla" / "ffi" / "api" / "ffi.h").exists() else None
+
+
+def build_xla(force: bool = False) -> Path | None:
+    """Builds libfire_xla.so (the XLA FFI handlers of xla/fire_xla.cc, linked with libfire.so) where jax is
+    installed; returns None (nothing built) where it is not."""
+    inc = jax_ffi_include()
+    if inc is None:
+        return None
+    lib = build(force)
+    out = PKG / "libfire_xla.so"
+    src = PKG / "xla" / "fire_xla.cc"
+    if not force and out.exists() and out.stat().st_mtime > max(src.stat().st_mtime, lib.stat().st_mtime):
+        return out
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{inc}",
+           "-x", "cu", str(src), "-o", str(out), f"-L{PKG}", "-lfire", f"-Xlinker=-rpath,{PKG}", "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
+    return out
+
+
 if __name__ == "__main__":
     t = build(force="--force" in sys.argv, verbose=True)
     print(t)
