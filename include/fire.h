@@ -43,7 +43,7 @@ extern "C" {
 
 #define FIRE_NO_NEIGHBOUR 1000000 /* model/graph_utils.py:14 NO_NEIGHBOUR */
 #define FIRE_STATUS_WORDS 8
-#define FIRE_ABI_VERSION 1
+#define FIRE_ABI_VERSION 2
 
 typedef enum {
   FIRE_OK = 0,
@@ -61,8 +61,10 @@ typedef enum {
 #define FIRE_FLAG_SINGULAR 16         /* an orbital matrix had a zero pivot */
 #define FIRE_FLAG_TIMEOUT 32          /* a bounded wait on a tensor-core completion barrier gave up */
 #define FIRE_FLAG_CHANGED_OVERFLOW 64 /* a low-rank step's changed set exceeded cap_changed */
+#define FIRE_FLAG_REFINE_OVERFLOW 128 /* more ill-conditioned walkers than refine_cap (status[5] = their number) */
 /* status[1] = max pairs of any walker seen, status[2] = max e-n neighbours seen,
- * status[3] = max triplets (sum_m deg(m)^2) seen, status[4] = max changed set of a low-rank step seen;
+ * status[3] = max triplets (sum_m deg(m)^2) seen, status[4] = max changed set of a low-rank step seen,
+ * status[5] = ill-conditioned walkers of the last fire_local_energy call (FP32 and mixed, refine_cap > 0);
  * the host grows capacities from these, like StaticScheduler (static_args.py:62-84). */
 
 typedef enum {
@@ -84,7 +86,16 @@ typedef struct {
   int32_t cap_nuc;       /* capacity: e-n neighbours per electron */
   int32_t precision;     /* fire_precision */
   int32_t chunk_walkers; /* walkers per internal pass; 0 = choose from the workspace */
+  int32_t refine_cap;    /* FP32 / mixed fire_local_energy: at most this many ill-conditioned walkers per call are
+                            evaluated again with FP64 orbital-matrix values (see fire_local_energy); 0 = none */
+  float refine_ratio;    /* a walker is ill-conditioned when (|lap| + |grad|^2) / 2 > refine_ratio |E_loc|
+                            (<= 0: FIRE_REFINE_RATIO) */
+  float refine_kappa;    /* ... or when its determinant-weighted condition number
+                            sum_d |w_d| kappa_F(A_d) / |sum_d w_d| exceeds refine_kappa (<= 0: FIRE_REFINE_KAPPA) */
 } fire_problem;
+
+#define FIRE_REFINE_RATIO 8.0f
+#define FIRE_REFINE_KAPPA 1.0e5f
 
 /* Parameter slots of the flat parameter blob (float32), in blob order.  Shapes with
  * F = 256, D = 4 determinants, n = n_el, N = n_nuc are given by fire_param_layout. */
@@ -120,7 +131,8 @@ int32_t fire_abi_version(void);
 fire_status fire_param_layout(const fire_problem* prob, int64_t* offsets);
 
 /* bytes of the prepared-parameter buffer (derived weights: folded scales, fused attention
- * query/key weights, BF16 copies for the mixed path). */
+ * query/key weights, BF16 copies for the mixed path, FP64 copies for the refinement pass of the FP32 and
+ * mixed local energy). */
 fire_status fire_prepared_size(const fire_problem* prob, size_t* bytes);
 
 /* bytes of workspace needed to process `chunk` walkers per pass (chunk <= 0: the whole batch). */
@@ -181,12 +193,25 @@ typedef struct {
   void* jastrow;   /* [B] log Jastrow value */
   void* grad;      /* [B, n_el, 3] gradient of log|psi| */
   void* lap;       /* [B] Laplacian of log|psi| */
+  int32_t* refined;/* [B] 1 for the walkers the refinement pass evaluated again, else 0 */
+  double* cond;    /* [B] sum_d |w_d| kappa_F(A_d) / |sum_d w_d| of the first pass (w_d the signed determinant
+                      weights, kappa_F = ||A||_F ||A^-1||_F of orbital matrix d); 0 in the FP64 build */
 } fire_eloc_debug;
 
 /* logpsi, sign, e_loc: [B] in the walkers' dtype (may be NULL except e_loc);
  * e_stats: [2] float64 = (mean, std) of e_loc over the batch (may be NULL).
  * Up to 798 electrons (the orbital matrices are eliminated in shared memory); larger problems return
- * FIRE_ERR_UNSUPPORTED, here and in fire_logpsi and the Metropolis blocks. */
+ * FIRE_ERR_UNSUPPORTED, here and in fire_logpsi and the Metropolis blocks.
+ * FP32 and mixed precision: near a node of psi, E_loc is the small difference of two large terms
+ * (lap log psi and |grad log psi|^2), and the FP32 rounding of the value planes that lead to the orbital
+ * matrices moves it by up to ~2e-6 of their size; an orbital matrix of large condition number amplifies that
+ * rounding in the same way.  A walker whose (|lap| + |grad|^2) / 2 exceeds refine_ratio |E_loc|, whose
+ * determinant-weighted condition number (debug->cond) exceeds refine_kappa, or whose E_loc is not finite is
+ * ill-conditioned: with refine_cap > 0, up to refine_cap of them are evaluated once more after the batch, with
+ * the values of the embedding, orbitals, envelopes and orbital matrices, their LU and inverse in FP64 (the
+ * derivative planes on the FP32 CUDA cores), and their results replace the first ones.  status[5] reports how
+ * many walkers were ill-conditioned; more than refine_cap sets FIRE_FLAG_REFINE_OVERFLOW (the others keep their
+ * first results).  The workspace must then hold the refinement pass as well (fire_workspace_size does). */
 fire_status fire_local_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,
                               const void* prepared, const void* r, void* logpsi, void* sign,
                               void* e_loc, double* e_stats, const fire_eloc_debug* debug,

@@ -21,6 +21,7 @@ FLAG_TRIPLET_OVERFLOW = 8
 FLAG_SINGULAR = 16
 FLAG_TIMEOUT = 32
 FLAG_CHANGED_OVERFLOW = 64
+FLAG_REFINE_OVERFLOW = 128
 LOW_RANK_MAX_CHANGED = 128  # LR_KMAX: capacity limit of a low-rank step's changed set
 TRIPLETS_STATIC_MAX_WORDS = 4 * 1024 * 1024  # FIRE_TRIPLETS_STATIC_MAX_WORDS
 ERRORS = {1: "invalid argument", 2: "unsupported size", 3: "workspace too small", 4: "CUDA launch failed"}
@@ -42,7 +43,8 @@ class Problem(C.Structure):
     _fields_ = [
         ("n_el", C.c_int32), ("n_up", C.c_int32), ("n_nuc", C.c_int32), ("n_walkers", C.c_int32),
         ("cutoff", C.c_float), ("cutoff_1el", C.c_float), ("cap_pairs", C.c_int32), ("cap_nuc", C.c_int32),
-        ("precision", C.c_int32), ("chunk_walkers", C.c_int32),
+        ("precision", C.c_int32), ("chunk_walkers", C.c_int32), ("refine_cap", C.c_int32),
+        ("refine_ratio", C.c_float), ("refine_kappa", C.c_float),
     ]
 
 
@@ -59,7 +61,7 @@ class Ecp(C.Structure):
 
 class ElocDebug(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in
-                ("kinetic", "potential", "logdet", "sign_det", "jastrow", "grad", "lap")]
+                ("kinetic", "potential", "logdet", "sign_det", "jastrow", "grad", "lap", "refined", "cond")]
 
 
 _lib = None

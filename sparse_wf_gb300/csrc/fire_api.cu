@@ -154,10 +154,24 @@ void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
   off[TC_COUNT] = o;
 }
 
+// Byte offset of the FP64 prepared weights (the refinement pass's) in an FP32 / mixed prepared buffer: after the
+// float slots and, in the mixed path, the BF16 tensor-core weights.
+size_t prep64_offset(const fire_problem* p) {
+  int64_t off[PR_COUNT + 1];
+  prep_offsets(p, off);
+  size_t end = (size_t)off[PR_COUNT] * 4;
+  if (p->precision == FIRE_PREC_MIXED) {
+    size_t to[TC_COUNT + 1];
+    tc_offsets(p, end, to);
+    end = to[TC_COUNT];
+  }
+  return (end + 255) / 256 * 256;
+}
+
 bool valid(const fire_problem* p) {
   return p && p->n_el >= 2 && p->n_el <= MAX_EL && p->n_up >= 0 && p->n_up <= p->n_el && p->n_nuc >= 1 &&
          p->n_walkers >= 1 && p->cutoff > 0 && p->cutoff_1el > 0 && p->cap_pairs >= 1 && p->cap_nuc >= 1 &&
-         p->precision >= 0 && p->precision <= 2;
+         p->precision >= 0 && p->precision <= 2 && p->refine_cap >= 0;
 }
 
 // ------------------------------------------------------------------------------ workspace plan
@@ -170,7 +184,7 @@ struct Plan {
   size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, Zr2, jsqr;
   size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, plr, tile_mask, aD1, aD2, ajsq;
   // double
-  size_t ld, sd, dlap, gjw, enn;
+  size_t ld, sd, dlap, cond, gjw, enn;
   size_t total;
 };
 
@@ -227,7 +241,7 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
     take(P.lapA, G * DN, es);
     take(P.Jorb, Jr * DN, es);
     take(P.Ainv, W * NDET * n * (size_t)ainv_ld((int)n), es);
-    take(P.dgrad, W * NDET * n * 3, es);
+    take(P.dgrad, W * NDET * n * 3, 8);
   }
   take(P.aX, G * HEADS, es);
   take(P.Ax, W * 2 * 272, es);
@@ -270,20 +284,65 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
   take(P.ld, W * NDET, 8);
   take(P.sd, W * NDET, 8);
   take(P.dlap, W * NDET, 8);
+  if (fl) take(P.cond, W * NDET, 8);
   P.total = (o + 255) / 256 * 256;
   return P;
 }
 
+// ---- refinement pass of the FP32 / mixed local energy (see fire_local_energy in fire.h)
+// Walkers refined per call: refine_cap, at most the batch; none in the FP64 build.
+int refine_walkers(const fire_problem* p) {
+  return p->precision == FIRE_PREC_FP64 ? 0 : std::min(p->refine_cap, p->n_walkers);
+}
+// The FP64 value path's problem for KF walkers.
+fire_problem refine_problem64(const fire_problem* p, int KF) {
+  fire_problem q = *p;
+  q.precision = FIRE_PREC_FP64;
+  q.n_walkers = KF;
+  q.chunk_walkers = KF;
+  q.refine_cap = 0;
+  return q;
+}
+// Workspace of one pass over KC refined walkers, at offset 0 once the batch's chunks are done: the chunk plan of
+// the KC walkers, the FP64 value-path plan of the same walkers, their positions in the walkers' dtype and in FP64.
+struct RefineLayout {
+  size_t c64, r_ref, r64, total;
+};
+RefineLayout refine_layout(const fire_problem* p, int KC) {
+  RefineLayout L;
+  fire_problem pr = *p;
+  pr.n_walkers = KC;
+  const fire_problem p64 = refine_problem64(p, KC);
+  const size_t n3 = (size_t)KC * p->n_el * 3;
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  L.c64 = up(make_plan(&pr, KC, true).total);
+  L.r_ref = up(L.c64 + make_plan(&p64, KC, false).total);
+  L.r64 = up(L.r_ref + n3 * elem_size(p));
+  L.total = up(L.r64 + n3 * 8);
+  return L;
+}
+// Total workspace of the local energy with chunks of Wc walkers: the larger of the chunk plan and the refinement
+// pass (in passes of at most Wc walkers), then the list of ill-conditioned walkers (KF indices, their count and
+// one count per pass), which lives through both.
+size_t eloc_ws_bytes(const fire_problem* p, int Wc, size_t* list_off) {
+  const int KF = refine_walkers(p);
+  size_t t = make_plan(p, Wc, true).total;
+  if (KF > 0) t = std::max(t, refine_layout(p, std::min(KF, Wc)).total);
+  if (list_off) *list_off = t;
+  return KF > 0 ? t + ((size_t)(2 * KF + 1) * 4 + 255) / 256 * 256 : t;
+}
+
 int choose_chunk(const fire_problem* p, size_t ws_bytes, bool fl) {
   int B = p->n_walkers;
+  auto need = [&](int c) { return fl ? eloc_ws_bytes(p, c, nullptr) : make_plan(p, c, fl).total; };
   if (p->chunk_walkers > 0) {
     const int c = std::min(B, p->chunk_walkers);
-    return make_plan(p, c, fl).total <= ws_bytes ? c : 0;
+    return need(c) <= ws_bytes ? c : 0;
   }
   int lo = 0, hi = B;
   while (lo < hi) {  // largest c with plan(c) <= ws
     const int mid = (lo + hi + 1) / 2;
-    if (make_plan(p, mid, fl).total <= ws_bytes) lo = mid; else hi = mid - 1;
+    if (need(mid) <= ws_bytes) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
@@ -689,7 +748,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
 // working matrix in the workspace (k_gj_global).  Its shared memory (two panel buffers of n x 17 eight-byte
 // elements plus ~2.5 KB) limits the inverse, and so the local energy, to ELOC_MAX_EL electrons.
 template <typename S, typename TI, typename TO, bool INV>
-cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv) {
+cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv, double* cond = nullptr) {
   const int n = c.p->n_el;
   constexpr int BW = GJG_BW_DECL;
   const size_t smem =
@@ -701,7 +760,7 @@ cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv) {
   g_nlaunch++;
   kern<<<c.Wc * NDET, GJG_THREADS_DECL, smem, c.s>>>(A, n, c.template buf<S>(c.P.gjw),
                                                       c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
-                                                      Ainv, c.status);
+                                                      cond, Ainv, c.status);
   return cudaPeekAtLastError();
 }
 
@@ -862,20 +921,43 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   return cudaPeekAtLastError();
 }
 
+// Ill-conditioned walkers of a local-energy call: the first pass appends them to idx (count cnt, capacity cap);
+// the refinement pass evaluates the chunk of their positions with the orbital matrices of c64 (FP64 values of the
+// same walkers) and writes its results to their rows.
+struct Refine {
+  int32_t* idx = nullptr;
+  int32_t* cnt = nullptr;
+  int cap = 0;
+  const Ctx<double>* c64 = nullptr;
+};
+
 template <typename T>
-cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fire_eloc_debug* dbg) {
+cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fire_eloc_debug* dbg,
+                       const Refine& rf = Refine()) {
   setup_ctx(c, true);
   stage_neighbors(c, true);
   stage_embedding<T, 3>(c);
   stage_update<T, 3>(c);
   stage_orbitals<T, 3>(c);
   {
-    // orbital-matrix inverse: native FP64 in the FP64 build, double-FP32 (48-bit significand) otherwise
+    // orbital-matrix inverse: native FP64 in the FP64 build, double-FP32 (48-bit significand) otherwise; the
+    // refinement pass eliminates the FP64 orbital matrices of its walkers in FP64
     Prof pr("gauss_jordan", c.s);
-    if constexpr (sizeof(T) == 8)
+    if constexpr (sizeof(T) == 8) {
       launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
-    else
-      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+    } else if (rf.c64) {
+      const Ctx<double>& c64 = *rf.c64;
+      launch_gjg<double, double, T, true>(c64, c64.template buf<double>(c64.P.Apl), c.template buf<T>(c.P.Ainv));
+      const size_t nb = sizeof(double) * (size_t)c.Wc * NDET;
+      cudaMemcpyAsync(c.template buf<double>(c.P.ld), c64.template buf<double>(c64.P.ld), nb,
+                      cudaMemcpyDeviceToDevice, c.s);
+      cudaMemcpyAsync(c.template buf<double>(c.P.sd), c64.template buf<double>(c64.P.sd), nb,
+                      cudaMemcpyDeviceToDevice, c.s);
+    } else {
+      // the condition numbers of the orbital matrices feed the ill-conditioned test of the assembly
+      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv),
+                                   rf.idx ? c.template buf<double>(c.P.cond) : nullptr);
+    }
   }
   cudaMemsetAsync(c.template buf<double>(c.P.dlap), 0, sizeof(double) * c.Wc * NDET, c.s);
   {
@@ -888,7 +970,7 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       g_nlaunch++;
       kern<<<grid, threads, smem, c.s>>>(c.nb, c.L, c.template buf<T>(c.P.Jorb), c.template buf<T>(c.P.Ainv),
-                                         c.template buf<T>(c.P.lapA), c.template buf<T>(c.P.dgrad),
+                                         c.template buf<T>(c.P.lapA), c.template buf<double>(c.P.dgrad),
                                          c.template buf<double>(c.P.dlap), c.status);
     };
     if constexpr (sizeof(T) == 4) {
@@ -908,11 +990,22 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
   o.sign = sign;
   o.eloc = eloc;
   if (dbg) o.dbg = *dbg;
+  if (rf.c64) {  // refinement pass: walker w of the chunk is batch walker idx[w]
+    o.wmap = rf.idx;
+    o.wcnt = rf.cnt;
+  } else if (rf.idx) {
+    o.ref_idx = rf.idx;
+    o.ref_cnt = rf.cnt;
+    o.ref_cap = rf.cap;
+    o.ref_ratio = c.p->refine_ratio > 0.f ? (double)c.p->refine_ratio : (double)FIRE_REFINE_RATIO;
+    o.ref_kappa = c.p->refine_kappa > 0.f ? (double)c.p->refine_kappa : (double)FIRE_REFINE_KAPPA;
+    o.cond = c.template buf<double>(c.P.cond);
+  }
   Prof pr("assemble", c.s);
   g_nlaunch++;
   k_assemble<T, true><<<c.Wc, 256, 3 * c.p->n_el * sizeof(double), c.s>>>(
       c.p->n_el, c.p->n_up, c.p->n_nuc, c.w0, c.r, c.R, c.Z, c.W, c.template buf<double>(c.P.ld),
-      c.template buf<double>(c.P.sd), c.template buf<T>(c.P.dgrad), c.template buf<double>(c.P.dlap),
+      c.template buf<double>(c.P.sd), c.template buf<double>(c.P.dgrad), c.template buf<double>(c.P.dlap),
       c.template buf<T>(c.P.JAx), c.template buf<T>(c.P.JAj), c.template buf<T>(c.P.JAl), c.template buf<T>(c.P.JMx),
       c.template buf<T>(c.P.JMj), c.template buf<T>(c.P.JMl), o, c.status);
   return cudaPeekAtLastError();
@@ -952,6 +1045,78 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
   return c;
 }
 
+// Positions of the walkers of one refinement pass: entries k0 .. k0 + KC - 1 of the list.  r_ref [k] (walkers'
+// dtype) and r64 [k] (FP64) = walker idx[k0 + k] of the batch while k0 + k < min(cnt, KF) (a copy of the first
+// entry, or of walker 0, beyond); sub_cnt = the pass's number of listed walkers.  The first pass reports the count
+// in status[5] and an overflow of the capacity KF.
+template <typename T>
+__global__ void k_refine_gather(const T* __restrict__ r, int n, const int32_t* __restrict__ idx,
+                                const int32_t* __restrict__ cnt, int KF, int k0, int KC, T* __restrict__ r_ref,
+                                double* __restrict__ r64, int32_t* __restrict__ sub_cnt, int32_t* status) {
+  const int k = blockIdx.x, c = min(*cnt, KF);
+  const int src = k0 + k < c ? idx[k0 + k] : (c > 0 ? idx[0] : 0);
+  for (int q = threadIdx.x; q < 3 * n; q += blockDim.x) {
+    const T v = r[(size_t)src * 3 * n + q];
+    r_ref[(size_t)k * 3 * n + q] = v;
+    r64[(size_t)k * 3 * n + q] = (double)v;
+  }
+  if (k == 0 && threadIdx.x == 0) {
+    *sub_cnt = max(0, min(KC, c - k0));
+    if (k0 == 0) {
+      max_word(status, 5, *cnt);
+      if (*cnt > KF) set_flag(status, FIRE_FLAG_REFINE_OVERFLOW);
+    }
+  }
+}
+
+// The refinement pass over the ill-conditioned walkers of the batch (rf.idx, rf.cnt): the FP64 value path
+// (embedding, update, envelopes, orbitals) of their positions, then the chunk evaluation of the same positions with
+// those orbital matrices eliminated in FP64 and the derivative planes on the FP32 CUDA cores; the results go to the
+// walkers' rows.  The list is evaluated in passes of KC <= Wc walkers (the batch's chunk size, so that they fit
+// the workspace); a pass whose walkers are all beyond the count exits in its assembly.
+template <typename T>
+cudaError_t refine_pass(const fire_problem* p, int Wc, cudaStream_t s, const float* R, const float* Z,
+                        const void* prepared, const T* r, void* logpsi, void* sign, void* eloc,
+                        const fire_eloc_debug* dbg, unsigned char* ws, int32_t* status, Refine rf) {
+  const int KF = rf.cap, KC = std::min(KF, Wc), n = p->n_el;
+  const RefineLayout L = refine_layout(p, KC);
+  T* r_ref = reinterpret_cast<T*>(ws + L.r_ref);
+  double* r64 = reinterpret_cast<double*>(ws + L.r64);
+  int32_t* sub_cnt = rf.cnt + 1;  // one count per pass
+  const fire_problem p64 = refine_problem64(p, KC);
+  fire_problem pr_ = *p;
+  pr_.n_walkers = KC;
+  pr_.chunk_walkers = KC;
+  pr_.precision = FIRE_PREC_FP32;  // derivative planes on the CUDA cores in FP32 (the float slots are shared)
+  Prof pr("refine", s);
+  for (int k0 = 0, j = 0; k0 < KF; k0 += KC, ++j) {
+    g_nlaunch++;
+    k_refine_gather<T><<<KC, 128, 0, s>>>(r, n, rf.idx, rf.cnt, KF, k0, KC, r_ref, r64, sub_cnt + j, status);
+    Ctx<double> c64 = make_ctx<double>(&p64, s, R, Z,
+                                       reinterpret_cast<const unsigned char*>(prepared) + prep64_offset(p), status,
+                                       ws + L.c64, KC, false);
+    c64.w0 = 0;
+    c64.Wc = KC;
+    c64.r = r64;
+    setup_ctx(c64, false);
+    stage_neighbors(c64, false);
+    stage_embedding<double, 0>(c64);
+    stage_update<double, 0>(c64);
+    stage_orbitals<double, 0>(c64);
+    Ctx<T> c = make_ctx<T>(&pr_, s, R, Z, prepared, status, ws, KC, true);
+    c.w0 = 0;
+    c.Wc = KC;
+    c.r = r_ref;
+    Refine sub = rf;
+    sub.idx = rf.idx + k0;
+    sub.cnt = sub_cnt + j;
+    sub.c64 = &c64;
+    const cudaError_t e = chunk_eloc<T>(c, logpsi, sign, eloc, dbg, sub);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaPeekAtLastError();
+}
+
 template <typename T>
 fire_status run_eloc(const fire_problem* p, cudaStream_t s, const float* R, const float* Z, const void* prepared,
                      const void* r, void* logpsi, void* sign, void* eloc, double* stats, const fire_eloc_debug* dbg,
@@ -960,11 +1125,27 @@ fire_status run_eloc(const fire_problem* p, cudaStream_t s, const float* R, cons
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, true);
   const T* rr = reinterpret_cast<const T*>(r);
+  Refine rf;
+  if constexpr (sizeof(T) == 4) {
+    rf.cap = refine_walkers(p);
+    if (rf.cap > 0) {
+      size_t list_off = 0;
+      eloc_ws_bytes(p, Wc, &list_off);
+      rf.idx = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(ws) + list_off);
+      rf.cnt = rf.idx + rf.cap;
+      cudaMemsetAsync(rf.cnt, 0, sizeof(int32_t), s);
+    }
+  }
   for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {
     c.w0 = w0;
     c.Wc = std::min(Wc, p->n_walkers - w0);
     c.r = rr + (size_t)w0 * p->n_el * 3;
-    if (chunk_eloc<T>(c, logpsi, sign, eloc, dbg) != cudaSuccess) return launch_status("local_energy chunk");
+    if (chunk_eloc<T>(c, logpsi, sign, eloc, dbg, rf) != cudaSuccess) return launch_status("local_energy chunk");
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (rf.cap > 0 && refine_pass<T>(p, Wc, s, R, Z, prepared, rr, logpsi, sign, eloc, dbg,
+                                     reinterpret_cast<unsigned char*>(ws), status, rf) != cudaSuccess)
+      return launch_status("local_energy refinement");
   }
   g_nlaunch++;
   if (stats) k_stats<T><<<1, 1024, 0, s>>>(reinterpret_cast<const T*>(eloc), p->n_walkers, stats);
@@ -1519,18 +1700,14 @@ fire_status fire_prepared_size(const fire_problem* prob, size_t* bytes) {
   int64_t off[PR_COUNT + 1];
   prep_offsets(prob, off);
   *bytes = (size_t)off[PR_COUNT] * elem_size(prob);
-  if (prob->precision == FIRE_PREC_MIXED) {
-    size_t to[TC_COUNT + 1];
-    tc_offsets(prob, *bytes, to);
-    *bytes = to[TC_COUNT];
-  }
+  if (prob->precision != FIRE_PREC_FP64) *bytes = prep64_offset(prob) + (size_t)off[PR_COUNT] * 8;
   return FIRE_OK;
 }
 
 fire_status fire_workspace_size(const fire_problem* prob, int32_t chunk, size_t* bytes) {
   if (!valid(prob) || !bytes) return FIRE_ERR_INVALID;
   const int c = chunk > 0 ? std::min(chunk, prob->n_walkers) : prob->n_walkers;
-  *bytes = make_plan(prob, c, true).total;
+  *bytes = eloc_ws_bytes(prob, c, nullptr);
   return FIRE_OK;
 }
 
@@ -1547,6 +1724,11 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (prob->precision == FIRE_PREC_FP64) return prepare_impl<double>(s, prob, blob, offsets_host, prepared);
   fire_status st = prepare_impl<float>(s, prob, blob, offsets_host, prepared);
+  if (st == FIRE_OK) {  // the FP64 copy of the refinement pass
+    const fire_problem p64 = refine_problem64(prob, 1);
+    st = prepare_impl<double>(s, &p64, blob, offsets_host,
+                              reinterpret_cast<unsigned char*>(prepared) + prep64_offset(prob));
+  }
   if (st != FIRE_OK || prob->precision != FIRE_PREC_MIXED) return st;
   int64_t off[PR_COUNT + 1];
   prep_offsets(prob, off);

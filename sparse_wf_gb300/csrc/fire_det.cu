@@ -91,11 +91,13 @@ constexpr int GJG_BW = 16, GJG_THREADS = 512;
 // A: element (i, o) of matrix (w, d) at A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]).
 // Outputs: logdet[w * NDET + d], sign[...] (double); if INV the inverse, transposed and aligned for
 // k_detlap: Ainv[((w * NDET + d) * n + i) * ainv_ld(n) + sh + o] = (A^-1)[o][i] with sh = (d n) mod 4 and zeros
-// in the other entries of the row, written after undoing the column permutation.
+// in the other entries of the row, written after undoing the column permutation; if INV and cond is not null,
+// cond[w * NDET + d] = ||A||_F ||A^-1||_F (the Frobenius condition number, >= the 2-norm one).
 template <typename S, typename TI, typename TO, bool INV>
 __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restrict__ A, int n, S* __restrict__ work,
                                                              double* __restrict__ logdet, double* __restrict__ sign,
-                                                             TO* __restrict__ Ainv, int32_t* status) {
+                                                             double* __restrict__ cond, TO* __restrict__ Ainv,
+                                                             int32_t* status) {
   extern __shared__ __align__(16) unsigned char gj_smem[];
   constexpr int BW = GJG_BW, LD = GJG_BW + 1;  // shared rows padded: column walks spread over the banks
   const int mat = blockIdx.x;
@@ -112,14 +114,30 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   int* perm = reinterpret_cast<int*>(rj + BW);  // [n]
   int* piv = perm + n;                     // [BW]
   int* rowmap = piv + BW;                  // [n] source row of every row after the panel's interchanges
-  __shared__ S redv[32];
+  static_assert(sizeof(S) == 8, "redv doubles as the double reduction buffer");
+  __shared__ __align__(8) S redv[32];
   __shared__ int redi[32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarp = blockDim.x >> 5;
+  double sq = 0.0;  // ||A||_F^2, then ||A^-1||_F^2 (condition number output)
   for (int e = tid; e < n * n; e += blockDim.x) {
     const int i = e / n, o = e - i * n;
-    Mb[0][e] = (S)A[((long)(w * n + i) * NDET + d) * n + o];
+    const TI a = A[((long)(w * n + i) * NDET + d) * n + o];
+    Mb[0][e] = (S)a;
+    sq += (double)a * (double)a;
+  }
+  // the block sums of the condition number go through redv (8-byte elements; no static shared memory is added,
+  // so that the largest matrix still fits): thread 0 keeps ||A||_F^2
+  double* redd = reinterpret_cast<double*>(redv);
+  double a2 = 0.0;
+  if (INV && cond) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if (lane == 0) redd[wid] = sq;
+    sq = 0.0;
   }
   __syncthreads();
+  if (INV && cond && tid == 0)  // before the first panel's barrier, after which redv is written again
+    for (int q = 0; q < nwarp; ++q) a2 += redd[q];
   double ld = 0.0;
   int neg = 0, sing = 0;
   const int npan = (n + BW - 1) / BW;
@@ -359,7 +377,11 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
     S* tile = pan;  // [32][n]
     for (int o0 = 0; o0 < n; o0 += 32) {
       const int ro = min(32, n - o0);
-      for (int e = tid; e < ro * n; e += blockDim.x) tile[e] = M[(size_t)o0 * n + e];
+      for (int e = tid; e < ro * n; e += blockDim.x) {
+        const S v = M[(size_t)o0 * n + e];
+        tile[e] = v;
+        sq += (double)v * (double)v;
+      }
       __syncthreads();
       for (int e = tid; e < n * 32; e += blockDim.x) {
         const int i = e >> 5, r = e & 31;
@@ -371,6 +393,17 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
     for (int e = tid; e < n * npad; e += blockDim.x) {
       const int i = e / npad, q = e - i * npad;
       out[(size_t)i * nA + (q < sh ? q : n + q)] = TO(0);
+    }
+    if (cond) {  // kappa_F = ||A||_F ||A^-1||_F
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+      if (lane == 0) redd[wid] = sq;
+      __syncthreads();
+      if (tid == 0) {
+        double b2 = 0.0;
+        for (int q = 0; q < nwarp; ++q) b2 += redd[q];
+        cond[mat] = sqrt(a2 * b2);
+      }
     }
   }
 }
@@ -411,7 +444,7 @@ __device__ __forceinline__ void ld_quad(const double* p, double (&v)[4]) {
 template <typename T, int NT, int CLO, int CHI>
 __global__ void __launch_bounds__(NT) k_detlap(Nbr nb, Layout L, const T* __restrict__ Jp,
                                                const T* __restrict__ AinvT, const T* __restrict__ lapA,
-                                               T* __restrict__ grad, double* __restrict__ lap, int32_t* status) {
+                                               double* __restrict__ grad, double* __restrict__ lap, int32_t* status) {
   constexpr int JROWS = dl_jrows(CHI), STAGE = dl_stage_elems(CHI), BLD = CHI + 1;
   constexpr int MAXT = ((3 * CHI + 3) / 4 * ((CHI + 3) / 4) + NT - 1) / NT;  // 4 x 4 tiles per thread
   constexpr int RPT = (4 * CHI + NT - 1) / NT;                              // staged rows per thread
@@ -563,8 +596,8 @@ __global__ void __launch_bounds__(NT) k_detlap(Nbr nb, Layout L, const T* __rest
     atomicAdd(&lap[w * NDET + d], sum);
   }
   if (tid < 3) {
-    T gsum = T(0);
-    for (int k = 0; k < cnt; ++k) gsum += Bm[(3 * k + tid) * BLD + k];
+    double gsum = 0.0;  // kept in double: near a node |grad log psi|^2 is ~1e4 |E_loc|
+    for (int k = 0; k < cnt; ++k) gsum += (double)Bm[(3 * k + tid) * BLD + k];
     grad[(((size_t)w * NDET + d) * n + m) * 3 + tid] = gsum;
   }
 }
@@ -577,18 +610,22 @@ template __global__ void k_env_coef<double, 1>(const double*, const float*, cons
                                                int, double*);
 template __global__ void k_env_coef<double, 5>(const double*, const float*, const double*, int, int, int, int,
                                                int, double*);
-template __global__ void k_gj_global<df64, float, float, false>(const float*, int, df64*, double*, double*, float*,
-                                                                 int32_t*);
-template __global__ void k_gj_global<df64, float, float, true>(const float*, int, df64*, double*, double*, float*,
-                                                                int32_t*);
+template __global__ void k_gj_global<df64, float, float, false>(const float*, int, df64*, double*, double*, double*,
+                                                                 float*, int32_t*);
+template __global__ void k_gj_global<df64, float, float, true>(const float*, int, df64*, double*, double*, double*,
+                                                                float*, int32_t*);
+// FP64 elimination of FP64 orbital matrices with the inverse in FP32 (the refinement pass of the FP32 / mixed local
+// energy, whose determinant Laplacian reads an FP32 inverse)
+template __global__ void k_gj_global<double, double, float, true>(const double*, int, double*, double*, double*,
+                                                                   double*, float*, int32_t*);
 template __global__ void k_gj_global<double, double, double, true>(const double*, int, double*, double*, double*,
-                                                                    double*, int32_t*);
+                                                                    double*, double*, int32_t*);
 template __global__ void k_gj_global<double, double, double, false>(const double*, int, double*, double*, double*,
-                                                                     double*, int32_t*);
+                                                                     double*, double*, int32_t*);
 template __global__ void k_detlap<float, 128, 0, DL_CSPLIT>(Nbr, Layout, const float*, const float*, const float*,
-                                                            float*, double*, int32_t*);
+                                                            double*, double*, int32_t*);
 template __global__ void k_detlap<float, 256, DL_CSPLIT, DL_CMAX>(Nbr, Layout, const float*, const float*,
-                                                                  const float*, float*, double*, int32_t*);
+                                                                  const float*, double*, double*, int32_t*);
 template __global__ void k_detlap<double, 256, 0, DL_CMAX>(Nbr, Layout, const double*, const double*,
                                                             const double*, double*, double*, int32_t*);
 

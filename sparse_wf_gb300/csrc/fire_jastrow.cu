@@ -343,7 +343,7 @@ template <typename T, bool FLM>
 __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0, const T* __restrict__ r,
                                                   const float* __restrict__ R, const float* __restrict__ Z,
                                                   Weights<T> W, const double* __restrict__ ld,
-                                                  const double* __restrict__ sd, const T* __restrict__ dgrad,
+                                                  const double* __restrict__ sd, const double* __restrict__ dgrad,
                                                   const double* __restrict__ dlap, const T* __restrict__ JAx,
                                                   const T* __restrict__ JAj, const T* __restrict__ JAl,
                                                   const T* __restrict__ JMx, const T* __restrict__ JMj,
@@ -352,6 +352,8 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
   double* grad_s = reinterpret_cast<double*>(as_smem);  // [3n]
   __shared__ double red[32 * 6];
   const int w = blockIdx.x, tid = threadIdx.x;
+  if (out.wmap && w >= *out.wcnt) return;
+  const long row = out.wmap ? (long)out.wmap[w] : (long)w0 + w;  // output row of this walker
   const T* rw = r + (size_t)w * n * 3;
   double cval, clap, pot;
   cusp_and_potential<T>(rw, R, Z, n, n_up, N, W.w[FIRE_P_CUSP], out.enn ? *out.enn : 0.0, grad_s, cval, clap, pot,
@@ -374,8 +376,8 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
   const double sgn = ((S < 0) != (J1 < 0)) ? -1.0 : 1.0;
   if (!FLM) {
     if (tid == 0) {
-      reinterpret_cast<T*>(out.logpsi)[w0 + w] = (T)logpsi;
-      if (out.sign) reinterpret_cast<T*>(out.sign)[w0 + w] = (T)sgn;
+      reinterpret_cast<T*>(out.logpsi)[row] = (T)logpsi;
+      if (out.sign) reinterpret_cast<T*>(out.sign)[row] = (T)sgn;
       if (!isfinite(logpsi)) set_flag(status, FIRE_FLAG_NONFINITE);
     }
     return;
@@ -386,7 +388,7 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
   for (int tt = tid; tt < T3; tt += blockDim.x) {
     double lse_j = 0.0, dj2 = 0.0;
     for (int d = 0; d < NDET; ++d) {
-      const double gj = (double)dgrad[(((size_t)w * NDET + d) * n) * 3 + tt];
+      const double gj = dgrad[(((size_t)w * NDET + d) * n) * 3 + tt];
       lse_j += wd[d] * gj;
       dj2 += wd[d] * gj * gj;
     }
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
     a_lse2 += lse_j * lse_j;
     a_dj2 += dj2;
     a_J1j2 += J1j * J1j;
-    if (out.dbg.grad) reinterpret_cast<T*>(out.dbg.grad)[(size_t)(w0 + w) * T3 + tt] = (T)tot;
+    if (out.dbg.grad) reinterpret_cast<T*>(out.dbg.grad)[(size_t)row * T3 + tt] = (T)tot;
   }
   double vv[4] = {a_tot2, a_lse2, a_dj2, a_J1j2};
   block_sum<double, 4>(vv, red);
@@ -413,17 +415,30 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
     const double lap = lse_l + lj_l + clap;
     const double ekin = -0.5 * (lap + vv[0]);
     const double eloc = ekin + pot;
-    reinterpret_cast<T*>(out.eloc)[w0 + w] = (T)eloc;
-    if (out.logpsi) reinterpret_cast<T*>(out.logpsi)[w0 + w] = (T)logpsi;
-    if (out.sign) reinterpret_cast<T*>(out.sign)[w0 + w] = (T)sgn;
-    if (out.dbg.kinetic) reinterpret_cast<T*>(out.dbg.kinetic)[w0 + w] = (T)ekin;
-    if (out.dbg.potential) reinterpret_cast<T*>(out.dbg.potential)[w0 + w] = (T)pot;
-    if (out.dbg.lap) reinterpret_cast<T*>(out.dbg.lap)[w0 + w] = (T)lap;
-    if (out.dbg.jastrow) reinterpret_cast<T*>(out.dbg.jastrow)[w0 + w] = (T)(J0 + log(fabs(J1)) + cval);
+    reinterpret_cast<T*>(out.eloc)[row] = (T)eloc;
+    if (out.logpsi) reinterpret_cast<T*>(out.logpsi)[row] = (T)logpsi;
+    if (out.sign) reinterpret_cast<T*>(out.sign)[row] = (T)sgn;
+    if (out.dbg.kinetic) reinterpret_cast<T*>(out.dbg.kinetic)[row] = (T)ekin;
+    if (out.dbg.potential) reinterpret_cast<T*>(out.dbg.potential)[row] = (T)pot;
+    if (out.dbg.lap) reinterpret_cast<T*>(out.dbg.lap)[row] = (T)lap;
+    if (out.dbg.jastrow) reinterpret_cast<T*>(out.dbg.jastrow)[row] = (T)(J0 + log(fabs(J1)) + cval);
     if (out.dbg.logdet)
-      for (int d = 0; d < NDET; ++d) out.dbg.logdet[(size_t)(w0 + w) * NDET + d] = ld[w * NDET + d];
+      for (int d = 0; d < NDET; ++d) out.dbg.logdet[(size_t)row * NDET + d] = ld[w * NDET + d];
     if (out.dbg.sign_det)
-      for (int d = 0; d < NDET; ++d) out.dbg.sign_det[(size_t)(w0 + w) * NDET + d] = sd[w * NDET + d];
+      for (int d = 0; d < NDET; ++d) out.dbg.sign_det[(size_t)row * NDET + d] = sd[w * NDET + d];
+    if (out.dbg.refined) out.dbg.refined[row] = out.wmap ? 1 : 0;
+    // determinant-weighted condition number of the orbital matrices: the factor by which their rounding enters
+    // the derivatives of log sum_d w_d det A_d
+    double cw = 0.0;
+    if (out.cond) {
+      for (int d = 0; d < NDET; ++d) cw += fabs(wd[d]) * out.cond[w * NDET + d];
+      cw /= fabs(S);
+    }
+    if (out.dbg.cond && !out.wmap) out.dbg.cond[row] = cw;
+    if (out.ref_idx && !(0.5 * (fabs(lap) + vv[0]) <= out.ref_ratio * fabs(eloc) && cw <= out.ref_kappa)) {
+      const int slot = atomicAdd(out.ref_cnt, 1);
+      if (slot < out.ref_cap) out.ref_idx[slot] = (int32_t)row;
+    }
     if (!isfinite(eloc) || !isfinite(logpsi)) set_flag(status, FIRE_FLAG_NONFINITE);
   }
 }
@@ -518,11 +533,11 @@ __global__ void k_stats(const T* __restrict__ e, int B, double* __restrict__ out
   template __global__ void k_readout_in<T, true>(int, const T*, const T*, const T*, T*, T*, T*);                  \
   template __global__ void k_readout_in<T, false>(int, const T*, const T*, const T*, T*, T*, T*);                 \
   template __global__ void k_assemble<T, true>(int, int, int, int, const T*, const float*, const float*,          \
-                                               Weights<T>, const double*, const double*, const T*, const double*, \
-                                               const T*, const T*, const T*, const T*, const T*, const T*,        \
-                                               AssembleOut, int32_t*);                                           \
+                                               Weights<T>, const double*, const double*, const double*,          \
+                                               const double*, const T*, const T*, const T*, const T*, const T*,   \
+                                               const T*, AssembleOut, int32_t*);                                 \
   template __global__ void k_assemble<T, false>(int, int, int, int, const T*, const float*, const float*,         \
-                                                Weights<T>, const double*, const double*, const T*,              \
+                                                Weights<T>, const double*, const double*, const double*,         \
                                                 const double*, const T*, const T*, const T*, const T*, const T*,  \
                                                 const T*, AssembleOut, int32_t*);                                \
   template __global__ void k_potential<T>(int, int, const T*, const float*, const float*, T*);                    \

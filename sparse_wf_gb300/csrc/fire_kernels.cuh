@@ -36,10 +36,11 @@ template <typename T, int NV>
 __global__ void k_env_coef(const T* r, const float* R, const T* sp, int n, int n_s, int s_off, int N, int Wn,
                            T* coef);
 template <typename S, typename TI, typename TO, bool INV>
-__global__ void k_gj_global(const TI* A, int n, S* work, double* logdet, double* sign, TO* Ainv, int32_t* status);
+__global__ void k_gj_global(const TI* A, int n, S* work, double* logdet, double* sign, double* cond, TO* Ainv,
+                            int32_t* status);
 constexpr int GJG_BW_DECL = 16, GJG_THREADS_DECL = 512;
 template <typename T, int NT, int CLO, int CHI>
-__global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* lapA, T* grad, double* lap,
+__global__ void k_detlap(Nbr nb, Layout L, const T* Jp, const T* Ainv, const T* lapA, double* grad, double* lap,
                          int32_t* status);
 
 // fire_jastrow.cu
@@ -57,7 +58,7 @@ template <typename T, bool FLM>
 __global__ void k_readout_in(int n, const T* Ax, const T* Al, const T* AJ, T* RX, T* RJ, T* RL);
 template <typename T, bool FLM>
 __global__ void k_assemble(int n, int n_up, int N, int w0, const T* r, const float* R, const float* Z,
-                           Weights<T> W, const double* ld, const double* sd, const T* dgrad, const double* dlap,
+                           Weights<T> W, const double* ld, const double* sd, const double* dgrad, const double* dlap,
                            const T* JAx, const T* JAj, const T* JAl, const T* JMx, const T* JMj, const T* JMl,
                            AssembleOut out, int32_t* status);
 template <typename T>

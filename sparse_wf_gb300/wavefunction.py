@@ -104,6 +104,14 @@ class FireWaveFunction:
         self._ws: Optional[torch.Tensor] = None
         self._status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=self.device)
         self._lr_cap = 0  # changed-set capacity of the last low-rank block (grown on overflow, like the statics)
+        # FP32 / mixed local energy: ill-conditioned walkers ((|lap| + |grad|^2) / 2 > refine_ratio |E_loc|, or a
+        # determinant-weighted condition number of the orbital matrices above refine_kappa) are evaluated again with
+        # FP64 orbital-matrix values; the capacity of that pass follows the counts the device reports
+        self.refine = precision != "fp64"
+        self.refine_ratio = 8.0
+        self.refine_kappa = 1.0e5
+        self._refine_cap = 0
+        self.last_refined = 0
         _lib.load()
 
     # ------------------------------------------------------------------ plumbing
@@ -114,12 +122,16 @@ class FireWaveFunction:
     def _stream(self):
         return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
-    def _problem(self, n_walkers: int, static: Optional[StaticArgs]) -> _lib.Problem:
+    def _problem(self, n_walkers: int, static: Optional[StaticArgs], refine: bool = False) -> _lib.Problem:
         cap_p = static.n_pairs if static is not None else 1
         cap_n = static.n_neighbours_en if static is not None else 1
+        cap_r = 0
+        if refine and self.refine:
+            # the last call's count padded; at least 2 % of the batch (and 2 walkers)
+            cap_r = min(int(n_walkers), max(self._refine_cap, 2, -(-2 * int(n_walkers) // 100)))
         return _lib.Problem(self.n_electrons, self.n_up, self.n_nuclei, int(n_walkers), self.cutoff,
                             self.cutoff_1el, max(1, int(cap_p)), max(1, int(cap_n)), _lib.PREC[self.precision],
-                            self.chunk_walkers)
+                            self.chunk_walkers, cap_r, float(self.refine_ratio), float(self.refine_kappa))
 
     def _workspace(self, prob: _lib.Problem, cap_changed: int = 0) -> torch.Tensor:
         """Workspace of the local-energy and value paths, or (cap_changed > 0) of the low-rank block."""
@@ -157,17 +169,24 @@ class FireWaveFunction:
         static = StaticArgs(half, pairs - half, max(static.n_triplets, int(st[3])), nucs)
         return static.round_with_padding(1.1, self.n_electrons, self.n_up, self.n_nuclei)
 
-    def _run(self, fn, static: StaticArgs, n_walkers: int, retries: int = 4):
-        """Runs fn(problem, workspace) with overflow-driven capacity growth; returns the static used."""
+    def _run(self, fn, static: StaticArgs, n_walkers: int, retries: int = 4, refine: bool = False):
+        """Runs fn(problem, workspace) with overflow-driven capacity growth; returns the static used.  With refine
+        (the local energy) the refinement capacity follows the device's count of ill-conditioned walkers: a call
+        that found more than its capacity is repeated with the count."""
         for _ in range(retries):
             self._status.zero_()
-            prob = self._problem(n_walkers, static)
+            prob = self._problem(n_walkers, static, refine)
             fn(prob, self._workspace(prob))
             st = self._read_status()
             flags = int(st[0])
             if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
                 static = self._grown(st, static)
                 continue
+            if refine and prob.refine_cap > 0:
+                self.last_refined = int(st[5])
+                self._refine_cap = int(st[5]) + int(st[5]) // 4 + 1
+                if flags & _lib.FLAG_REFINE_OVERFLOW:
+                    continue
             if flags & _lib.FLAG_NONFINITE:
                 pass  # NaNs propagate to the caller like the reference (train.py:263-264)
             return static
@@ -284,7 +303,8 @@ class FireWaveFunction:
                          logdet=torch.empty((B, 4), dtype=torch.float64, device=self.device),
                          sign_det=torch.empty((B, 4), dtype=torch.float64, device=self.device),
                          jastrow=torch.empty(B, **dev), grad=torch.empty((B, self.n_electrons, 3), **dev),
-                         lap=torch.empty(B, **dev))
+                         lap=torch.empty(B, **dev), refined=torch.zeros(B, dtype=torch.int32, device=self.device),
+                         cond=torch.zeros(B, dtype=torch.float64, device=self.device))
             for k, v in dbg_t.items():
                 setattr(dbg, k, v.data_ptr())
 
@@ -296,8 +316,9 @@ class FireWaveFunction:
                 C.byref(dbg) if debug else None, C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
                 C.c_void_p(self._status.data_ptr())), "fire_local_energy")
 
-        used = self._run(fn, static, B)
-        return eloc, dict(logpsi=logpsi, sign=sign, stats=stats, debug=dbg_t, static=used)
+        self.last_refined = 0
+        used = self._run(fn, static, B, refine=True)
+        return eloc, dict(logpsi=logpsi, sign=sign, stats=stats, debug=dbg_t, static=used, refined=self.last_refined)
 
     def kinetic_energy(self, params, electrons, static: StaticArgs):
         """``kinetic_energy`` (``wave_function.py:215-221``) through the sparse forward Laplacian."""

@@ -20,7 +20,7 @@ namespace {
 
 fire_problem make_problem(int64_t n_walkers, int64_t n_el, int64_t n_nuc, int32_t n_up, float cutoff,
                           float cutoff_1el, int32_t cap_pairs, int32_t cap_nuc, int32_t precision, int32_t chunk) {
-  fire_problem p;
+  fire_problem p{};  // refine_cap 0: no refinement pass (the handler has no host loop that sizes its capacity)
   p.n_el = static_cast<int32_t>(n_el);
   p.n_up = n_up;
   p.n_nuc = static_cast<int32_t>(n_nuc);

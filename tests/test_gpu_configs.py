@@ -1,0 +1,70 @@
+"""Parity at the benchmark configurations, CUDA path (C ABI) against the oracle on the same walkers and parameters:
+
+  H10 chain, 512 walkers (FP32 and FP64 build);
+  C10H22, 16 walkers (FP32, mixed, FP64 build);
+  C40H82, 2 walkers (FP64 build, FP32 and mixed), the size of the headline benchmark.
+
+Parameters are random-init (seed 0, normalize scales from walker 0), walkers drawn around the nuclei (sigma 1 bohr),
+as in the benchmark.  Tolerances: FP64 build 1e-10 relative on log|psi| and E_loc; FP32 1e-5 on log|psi| and the
+per-walker local-energy contract of helpers.check_eloc_contract (1e-5 of the magnitude of the terms E_loc is summed
+from, every ill-conditioned walker refined), mixed the same contract at 1e-4."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import check_eloc_contract, oracle_batch
+from sparse_wf_gb300 import systems
+from sparse_wf_gb300.wavefunction import FireWaveFunction, StaticArgs
+
+pytestmark = pytest.mark.gpu
+CASES = {"h10": (lambda: systems.hydrogen_chain(10, 1.8), 512), "c10h22": (lambda: systems.alkane(10), 16),
+         "c40h82": (lambda: systems.alkane(40), 2)}
+
+
+def _inputs(name):
+    from make_golden import make_params
+
+    make, B = CASES[name]
+    mol = make()
+    nu, _ = systems.spin_counts(mol)
+    r = systems.init_electrons(mol, B, 1000)
+    _, p, _, _ = make_params(mol, nu, r[0], seed=0, activate=False)
+    return mol, nu, r, p
+
+
+_REF = {}
+
+
+def _oracle(name):
+    if name not in _REF:
+        mol, nu, r, p = _inputs(name)
+        _REF[name] = oracle_batch(mol, nu, p, r)
+    return _REF[name]
+
+
+def _run(name, precision):
+    mol, nu, r, p = _inputs(name)
+    wf = FireWaveFunction(mol, precision=precision)
+    rr = torch.from_numpy(r.astype(np.float64) if precision == "fp64" else r).cuda()
+    s = wf.get_static_input(rr)
+    static = StaticArgs(s.n_pairs_same, s.n_pairs_diff, s.n_triplets, s.n_neighbours_en)
+    e, aux = wf.local_energy_full(p, rr, static, debug=True)
+    return wf, e.double().cpu().numpy(), aux
+
+
+@pytest.mark.parametrize("name,precision", [("h10", "fp64"), ("h10", "fp32"), ("c10h22", "fp64"), ("c10h22", "fp32"),
+                                            ("c10h22", "mixed"), ("c40h82", "fp64"), ("c40h82", "fp32"),
+                                            ("c40h82", "mixed")])
+def test_config_local_energy(cuda_lib, name, precision):
+    ref = _oracle(name)
+    wf, got, aux = _run(name, precision)
+    lp = aux["logpsi"].double().cpu().numpy()
+    if precision == "fp64":
+        assert np.all(np.abs(lp - ref["logpsi"]) <= 1e-10 * np.maximum(1, np.abs(ref["logpsi"])))
+        assert np.all(np.abs(got - ref["eloc"]) <= 1e-10 * np.abs(ref["eloc"]))
+        return
+    assert np.all(np.abs(lp - ref["logpsi"]) <= 1e-5 * np.maximum(1, np.abs(ref["logpsi"])))
+    dbg = aux["debug"]
+    check_eloc_contract(precision, wf, got, ref["eloc"], ref["ks"], ref["epot"], dbg["refined"].cpu().numpy() > 0,
+                        lap=dbg["lap"].double().cpu().numpy(), lap_ref=ref["lap"],
+                        grad=dbg["grad"].double().cpu().numpy(), grad_ref=ref["grad"])

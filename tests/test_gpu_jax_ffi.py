@@ -21,6 +21,7 @@ def test_local_energy_custom_call_matches_ctypes(cuda_lib):
     jax.config.update("jax_enable_x64", True)
     mol, nu, r, p, _, _ = case("c2h6")
     wf = FireWaveFunction(mol, precision="mixed")
+    wf.refine = False  # the custom call runs without the refinement pass
     dp = wf._params(p)
     rr = torch.from_numpy(r).cuda()
     s = wf.get_static_input(rr)
