@@ -3,9 +3,9 @@
 
 Workload (default): all-trans C40H82 (322 electrons, 122 nuclei), 2048 walkers drawn around the nuclei
 (sigma = 1 bohr), random-init default-architecture parameters (seed 0), e-e cutoff 5 bohr.  The walkers
-first go through a 20-step all-electron Metropolis block (Gaussian proposals, width 0.1 bohr; one
-untimed and one timed block); then one step = one local-energy evaluation (sparse forward Laplacian +
-Coulomb potential) of every walker.  Synthetic data: there is no dataset; molecules, walkers and
+first go through one 20-step all-electron Metropolis block (Gaussian proposals, width 0.1 bohr, Philox draws
+of seed 1000; a warm-up block runs on a copy); then one step = one local-energy evaluation (sparse forward
+Laplacian + Coulomb potential) of every walker.  Synthetic data: there is no dataset; molecules, walkers and
 parameters are generated here.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp32] [--impl reference]
@@ -14,8 +14,9 @@ Prints one JSON line (rank 0).  `value` is the headline path's device-resident t
 already in HBM; default the mixed path), `e2e` the same metric through the public API with the walkers
 copied from pinned host memory and E_loc copied back inside the timed region.  `fp32_path` times the
 plain FP32 path on the same walkers the same way; `accuracy` compares both with the FP64 build on a
-sample of the walkers.  `--impl reference` times the CPU oracle port of the reference algorithm
-(numpy, FP64, all host threads) on a bounded sample of the same workload.
+sample of the walkers.  `--impl reference` times the CPU oracle (the numpy FP64 restatement of the reference
+algorithm) on a sample of the same workload: the same parameters, the same Metropolis block replayed from the
+same Philox draws, one walker per host core.
 """
 from __future__ import annotations
 
@@ -53,17 +54,18 @@ def parse():
     ap.add_argument("--mcmc-single-steps", type=int, default=32,
                     help="single-electron Metropolis steps timed on a copy of the walkers (0: skip)")
     ap.add_argument("--mcmc-single-width", type=float, default=0.5)
-    ap.add_argument("--mcmc-low-rank-steps", type=int, default=0,
+    ap.add_argument("--mcmc-low-rank-steps", type=int, default=32,
                     help="single-electron steps of the low-rank block, timed on a copy of the walkers (0: skip)")
     ap.add_argument("--acc-walkers", type=int, default=256, help="walkers checked against the FP64 build")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
-    ap.add_argument("--serving-requests", type=int, default=40, help="requests of the serving segment (0: skip)")
-    ap.add_argument("--serving-rate", type=float, default=3.0, help="offered load, requests per second")
-    ap.add_argument("--serving-carbons", default="4,20", help="alkane sizes C_n of the serving requests (min,max)")
-    ap.add_argument("--serving-walkers", default="256,1024", help="walkers per serving request (min,max)")
-    ap.add_argument("--ragged", action="store_true",
-                    help="also time the 64-alkane ragged batch: one CUDA-graph launch vs one call per molecule")
-    ap.add_argument("--cpu-sample", type=int, default=2, help="walkers in the CPU baseline sample")
+    ap.add_argument("--serving-requests", type=int, default=20, help="requests of the serving segment (0: skip)")
+    ap.add_argument("--serving-rate", type=float, default=200.0, help="offered load, requests per second")
+    ap.add_argument("--serving-carbons", default="4,60", help="alkane sizes C_n of the serving requests (min,max)")
+    ap.add_argument("--serving-walkers", default="256,2048", help="walkers per serving request (min,max)")
+    ap.add_argument("--no-ragged", action="store_true",
+                    help="skip the 64-alkane ragged batch (one CUDA-graph launch vs one call per molecule)")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="walkers in the CPU samples (0: one per host core, at most 16)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -73,6 +75,57 @@ def molecule(name):
     from sparse_wf_gb300 import systems
 
     return systems.alkane(SYSTEMS[name])
+
+
+def workload_config(args, mol):
+    """The workload both arms report (identical in the reference arm's line and in this one)."""
+    return {"workload": f"{mol.name} all-trans, {args.walkers} walkers per GPU after a {args.mcmc_steps}-step "
+                        f"all-electron Metropolis block (width {args.mcmc_width} bohr, Philox draws of seed 1000); "
+                        f"step = local energy (sparse forward Laplacian + Coulomb) of every walker",
+            "n_el": mol.n_el, "n_nuc": mol.n_nuc, "walkers_per_gpu": args.walkers, "mcmc_steps": args.mcmc_steps,
+            "mcmc_width_bohr": args.mcmc_width, "params": "random init, seed 0; normalize scales from walker 0",
+            "l2": "inputs larger than L2: every step streams GB-scale planes",
+            "parallelism": f"walker shards x{args.gpus}"}
+
+
+# ------------------------------------------------------------------------ CPU oracle pool
+# The CPU baseline and the reference arm time the oracle (numpy FP64, one walker per process, one BLAS thread
+# each).  The pool is started with "spawn": a process forked from one that holds a CUDA context can hang.
+_POOL = {}
+
+
+def _pool_init(R, Z, n_up, params):
+    from oracle import fire_oracle as O
+
+    _POOL["prob"] = O.Problem(R, Z, n_up)
+    _POOL["p"] = params
+
+
+def _pool_eloc(r):
+    import numpy as np
+    from oracle import fire_oracle as O
+
+    return float(O.local_energy(_POOL["prob"], _POOL["p"], np.asarray(r, np.float64)))
+
+
+def _pool_mcmc(job):
+    from oracle import fire_oracle as O
+
+    walker, r, steps, width, seed, counter = job
+    r_new, n_acc, margins = O.mcmc_block_philox(_POOL["prob"], _POOL["p"], r, steps, width, seed, counter, walker)
+    return r_new, n_acc, float(min(abs(m) for m in margins)) if len(margins) else float("inf")
+
+
+def oracle_pool(mol, n_up, params, procs):
+    import multiprocessing as mp
+
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[k] = "1"
+    return mp.get_context("spawn").Pool(procs, initializer=_pool_init, initargs=(mol.R, mol.Z, n_up, params))
+
+
+def cpu_sample_size(args):
+    return args.cpu_sample if args.cpu_sample > 0 else max(1, min(os.cpu_count() or 1, 16))
 
 
 def measured_peaks():
@@ -147,20 +200,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(mol, r, params, n_up, sample):
-    """The oracle (numpy FP64 port of the reference algorithm) on `sample` walkers, all host threads."""
-    from oracle import fire_oracle as O
+def cpu_baseline(pool, walkers):
+    """Oracle E_loc of `walkers` (one per process of `pool`), timed: (walker-evals/s, energies, seconds)."""
     import numpy as np
 
-    prob = O.Problem(mol.R, mol.Z, n_up)
     t0 = time.perf_counter()
-    e = [O.local_energy(prob, params, r[k].astype(np.float64)) for k in range(sample)]
+    e = pool.map(_pool_eloc, [w for w in walkers], chunksize=1)
     dt = time.perf_counter() - t0
-    return sample / dt, np.array(e), dt
+    return len(walkers) / dt, np.array(e), dt
 
 
 def run_reference(args):
-    """CPU reference arm: the oracle port timed on bounded samples of the workload."""
+    """CPU reference arm: the oracle (numpy FP64 restatement of the reference algorithm) on a sample of the same
+    workload: the reference's own initialisation of the parameters (normalize scales from walker 0, computed by the
+    oracle in FP64), the first S walkers of the same initial set, the benchmark's Metropolis block replayed from the
+    device's Philox draws (float32 positions, as on the device), then W + K steps of E_loc of the S walkers, one per
+    host core."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -172,23 +227,36 @@ def run_reference(args):
 
     mol = molecule(args.system)
     n_up, _ = systems.spin_counts(mol)
-    r = systems.init_electrons(mol, max(args.cpu_sample, 1), 1000)
-    _, p, _, _ = make_params(mol, n_up, r[0])
-    for _ in range(min(args.warmup, 1)):
-        cpu_baseline(mol, r, p, n_up, 1)
-    rates = []
-    for _ in range(args.steps):
-        rate, _, _ = cpu_baseline(mol, r, p, n_up, args.cpu_sample)
-        rates.append(rate)
-    v = statistics.median(rates)
-    cores = os.cpu_count()
-    sample = f"{args.cpu_sample} of {args.walkers} {mol.name} walkers per step, numpy FP64 oracle port"
+    S = cpu_sample_size(args)
+    r = systems.init_electrons(mol, args.walkers * args.gpus, 1000)[:max(S, 1)]
+    _, p, _, _ = make_params(mol, n_up, r[0], seed=0, activate=False)
+    t_setup = time.perf_counter()
+    acc, closest = 0.0, float("inf")
+    with oracle_pool(mol, n_up, p, S) as pool:
+        if args.mcmc_steps > 0:
+            res = pool.map(_pool_mcmc, [(w, r[w], args.mcmc_steps, args.mcmc_width, 1000, 0) for w in range(S)],
+                           chunksize=1)
+            r = np.stack([x[0] for x in res])
+            acc = float(np.mean([x[1] for x in res])) / args.mcmc_steps
+            closest = min(x[2] for x in res)
+        t_setup = time.perf_counter() - t_setup
+        for _ in range(args.warmup):
+            cpu_baseline(pool, r)
+        times = []
+        for _ in range(args.steps):
+            _, _, dt = cpu_baseline(pool, r)
+            times.append(dt)
+    ms = 1e3 * statistics.mean(times)
+    v = S / (ms / 1e3)
+    sample = (f"{S} of the {args.walkers} {mol.name} walkers per step (one per host core), after the same "
+              f"{args.mcmc_steps}-step Metropolis block replayed from the device's Philox draws "
+              f"(acceptance {acc:.3f}, smallest |margin| {closest:.2e}; set-up {t_setup:.0f} s); numpy FP64 oracle"
+              if args.mcmc_steps > 0 else f"{S} of the {args.walkers} {mol.name} walkers per step")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * args.walkers / v, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{mol.name} all-trans, {args.walkers} walkers, local energy", "n_el": mol.n_el},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args, mol),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": S, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -292,17 +360,19 @@ def main():
     wf.chunk_walkers = args.chunk if args.chunk > 0 else choose_chunk(wf, B, static, args.ws_gb)
     stream = torch.cuda.current_stream(dev)
 
-    # Metropolis block (all-electron Gaussian proposals) that moves the walkers before the E_loc steps:
-    # one untimed block, then one timed block
+    # Metropolis block (all-electron Gaussian proposals, Philox draws of seed 1000 + rank, counter 0) that moves the
+    # walkers before the E_loc steps; an untimed warm-up block (counter 1) runs on a copy first
     mcmc = None
     if args.mcmc_steps > 0:
         _, logpsi = wf.signed(dp, r_dev, static)
-        wf.mcmc_block(dp, r_dev, logpsi, static, args.mcmc_steps, args.mcmc_width, seed=1000 + rank, counter=0)
+        r_w, lp_w = r_dev.clone(), logpsi.clone()
+        wf.mcmc_block(dp, r_w, lp_w, static, args.mcmc_steps, args.mcmc_width, seed=1000 + rank, counter=1)
+        del r_w, lp_w
         blk = {}
 
         def block():
             blk["acc"], blk["smax"] = wf.mcmc_block(dp, r_dev, logpsi, static, args.mcmc_steps, args.mcmc_width,
-                                                    seed=1000 + rank, counter=1)
+                                                    seed=1000 + rank, counter=0)
 
         ms_block, _ = time_steps(block, 1, stream, dist, world)
         acc = float(blk["acc"].float().mean().item()) / args.mcmc_steps
@@ -359,6 +429,7 @@ def main():
         ms, (eloc, aux) = time_steps(step, args.steps, stream, dist, world)
     total_walkers = args.walkers * world
     value = total_walkers / (ms / 1e3)
+    refined = {args.precision: int(aux.get("refined", 0))}  # ill-conditioned walkers of the last timed step
 
     # per-stage device times (CUDA events around every stage / contraction launch) for the roofline
     _lib.profile_enable(True)
@@ -372,10 +443,12 @@ def main():
     peaks, peak_kind = measured_peaks()
     g_launches, g_ms = prof.get("gemm", (0, float("nan")))
     achieved = flops / (g_ms / 1e3) / 1e12
-    roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+    # the contractions run inside a seconds-long step: the sustained bf16 figure is their ceiling
+    peak = peaks["bf16_tflops_sustained"]
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
                 "kernel": "all dense contractions of one step (k_gemm_tca + k_env_tc + k_gemm)", "launches": g_launches,
-                "avg_launch_ms": g_ms / max(g_launches, 1), "peak_source": f"bf16 dense burst, {peak_kind}",
+                "avg_launch_ms": g_ms / max(g_launches, 1), "peak_source": f"bf16 dense sustained, {peak_kind}",
                 "flops_per_step": flops}
     stages = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items() if k != "kernels_launched"}
 
@@ -429,7 +502,8 @@ def main():
         for _ in range(args.warmup):
             e32, aux32 = step32()
             st32 = aux32["static"]
-        ms32, (e32, _) = time_steps(step32, args.steps, stream, dist, world)
+        ms32, (e32, aux32) = time_steps(step32, args.steps, stream, dist, world)
+        refined["fp32"] = int(aux32.get("refined", 0))
         e_path["fp32"] = e32.double().cpu().numpy()
         fp32 = {"value": total_walkers / (ms32 / 1e3), "unit": UNIT, "ms_per_step": ms32,
                 "chunk_walkers": wf32.chunk_walkers}
@@ -438,6 +512,8 @@ def main():
     if e64 is not None:
         accuracy = {"walkers": K, "reference": "FP64 build of the same kernels (FP64 oracle to <= 1e-10)"}
         accuracy.update({k: energy_error(v[:K], e64) for k, v in e_path.items()})
+        for k in e_path:  # walkers of the whole batch that went through the FP64 refinement pass
+            accuracy[k]["refined_fraction"] = refined.get(k, 0) / B
 
     # serving segment: Poisson-arriving E_loc / 10-step MCMC requests of mixed molecule sizes (rank 0)
     serving = None
@@ -459,7 +535,7 @@ def main():
             torch.cuda.empty_cache()
 
     ragged = None
-    if rank == 0 and args.ragged:
+    if rank == 0 and not args.no_ragged:
         from sparse_wf_gb300.ragged import RaggedBatch, ragged_alkanes
 
         wf._ws = None
@@ -480,16 +556,20 @@ def main():
         del rb
         torch.cuda.empty_cache()
 
-    # CPU baseline + oracle check on the same walkers (rank 0)
+    # CPU baseline + oracle check on the same post-Metropolis walkers (rank 0): the oracle, one walker per core
     cpu = None
     check = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, e_ref, dt = cpu_baseline(mol, r_np, params, n_up, args.cpu_sample)
-        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{args.cpu_sample} of {B} {mol.name} walkers, numpy FP64 oracle, {dt:.1f} s"}
-        got = e_path[args.precision][: args.cpu_sample]
-        check = {"walkers": args.cpu_sample, "max_abs_err_mHa": float(np.abs(got - e_ref).max() * 1e3),
-                 "reference": "FP64 oracle"}
+        S = min(cpu_sample_size(args), B)
+        with oracle_pool(mol, n_up, params, S) as pool:
+            rate, e_ref, dt = cpu_baseline(pool, r_np[:S])
+        cpu = {"value": rate, "unit": UNIT, "cores": S, "kind": "port",
+               "sample": f"{S} of the {B} post-Metropolis {mol.name} walkers (one per host core), numpy FP64 "
+                         f"oracle, {dt:.1f} s"}
+        check = {"walkers": S, "reference": "FP64 oracle"}
+        for k, v in e_path.items():
+            d = np.abs(v[:S] - e_ref)
+            check[k] = {"max_abs_err_mHa": float(d.max() * 1e3), "max_rel_err": float((d / np.abs(e_ref)).max())}
 
     if rank == 0:
         st = aux["stats"].cpu().numpy()
@@ -498,14 +578,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16/f32",
             "data": "synthetic",
-            "config": {"workload": f"{mol.name} all-trans, {args.walkers} walkers per GPU after a "
-                                   f"{args.mcmc_steps}-step Metropolis block; step = local energy "
-                                   f"(sparse forward Laplacian + Coulomb) of every walker",
-                       "n_el": mol.n_el, "n_nuc": mol.n_nuc, "walkers_per_gpu": args.walkers,
-                       "precision": args.precision, "chunk_walkers": wf.chunk_walkers,
-                       "mean_pairs_per_walker": pairs, "cap_pairs": static.n_pairs,
-                       "l2": "inputs larger than L2: every step streams GB-scale planes",
-                       "parallelism": f"walker shards x{world}", "E_mean": float(st[0]), "E_std": float(st[1])},
+            "config": workload_config(args, mol),
+            "run": {"precision": args.precision, "chunk_walkers": wf.chunk_walkers, "mean_pairs_per_walker": pairs,
+                    "cap_pairs": static.n_pairs, "E_mean": float(st[0]), "E_std": float(st[1]),
+                    "refined_walkers": refined},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": int(prof.get("kernels_launched", (0, 0))[0]) * args.steps,
             "fp32_path": fp32, "mixed_over_fp32": (value / fp32["value"]) if fp32 else None,

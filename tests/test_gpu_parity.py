@@ -320,3 +320,45 @@ def test_make_mcmc_steps(cuda_lib, proposal):
     assert 0.0 <= stats["pmove"] <= 1.0 and 0.0 <= stats["pmove_jump"] <= 1.0
     assert stats["static_max"].n_pairs_same + stats["static_max"].n_pairs_diff > 0
     assert stats["static_max_jump"].n_pairs_same + stats["static_max_jump"].n_pairs_diff > 0
+
+
+def test_mcmc_philox_draws_match_cpu_replay(cuda_lib):
+    """The device's all-electron block draws (Philox4x32-10, Box-Muller) equal the oracle's numpy replay
+    (philox_all_electron_noise, philox_log_u): every accepted walker moved by exactly width * eps of that replay
+    (float32 positions), and the FP64 build takes the replayed Metropolis decision wherever its margin is clear
+    of rounding.  This is what lets the CPU baseline run the benchmark's Metropolis block on the same walkers."""
+    wf, mol, nu, r, p = _wf("c2h6", "fp32")
+    rr = torch.from_numpy(r).cuda().contiguous()
+    r0 = r.copy()
+    static = _static(wf, rr)
+    dp = wf._params(p)
+    _, logpsi = wf.signed(dp, rr, static)
+    width, seed = 0.02, 1234  # small moves of all 18 electrons: most proposals are accepted
+    n_acc, _ = wf.mcmc_block(dp, rr, logpsi, static, 1, width, seed=seed, counter=5)
+    got = rr.cpu().numpy()
+    acc = n_acc.cpu().numpy()
+    assert acc.sum() > 0
+    for w in range(r.shape[0]):
+        eps = O.philox_all_electron_noise(seed, 5, 0, w, mol.n_el)
+        want = (r0[w].astype(np.float64) + np.float64(np.float32(width)) * eps.astype(np.float64)).astype(np.float32)
+        if acc[w]:
+            np.testing.assert_allclose(got[w], want, rtol=0, atol=4e-6)
+        else:
+            np.testing.assert_array_equal(got[w], r0[w])
+    # decisions: FP64 build against the oracle's replayed block, 2 steps
+    wf64 = FireWaveFunction(mol, precision="fp64")
+    r64 = torch.from_numpy(r0.astype(np.float64)).cuda().contiguous()
+    st64 = _static(wf64, r64)
+    dp64 = wf64._params(p)
+    _, lp64 = wf64.signed(dp64, r64, st64)
+    n64, _ = wf64.mcmc_block(dp64, r64, lp64, st64, 2, width, seed=seed, counter=5)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    checked = 0
+    for w in range(r.shape[0]):
+        # the oracle keeps float32 positions (the FP32 path's), the FP64 build doubles: margins within ~1e-5 of zero
+        # may differ
+        _, na, mg = O.mcmc_block_philox(prob, p, r0[w], 2, width, seed, 5, w)
+        if np.all(np.abs(mg) > 1e-3):
+            checked += 1
+            assert int(n64[w]) == na
+    assert checked > 0

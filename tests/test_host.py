@@ -526,6 +526,16 @@ def test_bench_reference_arm_json_contract():
     assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    # the same workload description as the GPU arm's line, and the Metropolis block replayed before the steps
+    import argparse
+
+    import bench
+    from sparse_wf_gb300 import systems
+
+    args = argparse.Namespace(walkers=64, gpus=1, mcmc_steps=20, mcmc_width=0.1)
+    assert d["config"] == bench.workload_config(args, systems.alkane(2))
+    assert "Metropolis block replayed" in d["cpu_baseline"]["sample"]
+    assert abs(d["ms_per_step"] / 1e3 - d["cpu_baseline"]["cores"] / d["value"]) < 1e-9
 
 
 def test_ecp_energy_wrapper_reruns(monkeypatch):
