@@ -170,7 +170,9 @@ fire_status fire_triplets(void* stream, const fire_problem* prob, const void* r,
  * pass device scratch (a handler inside another runtime's executable, a host program without a memory
  * pool).  Needs n_walkers * (2 * n_el + 1 + 2 * cap_pairs) <= FIRE_TRIPLETS_STATIC_MAX_WORDS, else
  * FIRE_ERR_UNSUPPORTED before any CUDA call.  The first call on a device (that device current) looks
- * the array up with cudaGetSymbolAddress; make it before any stream capture.  The stream must belong
+ * the array up with cudaGetSymbolAddress; make it before any stream capture.  The address is cached with
+ * the CUDA context it belongs to: after cudaDeviceReset (or a new primary context) the next call looks it
+ * up again, so make that call before any stream capture too.  The stream must belong
  * to the current device.  Calls that can overlap on one device (other streams, other host threads)
  * race on the shared array; calls ordered on one stream do not. */
 #define FIRE_TRIPLETS_STATIC_MAX_WORDS (4 * 1024 * 1024)

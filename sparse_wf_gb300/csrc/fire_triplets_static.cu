@@ -12,12 +12,15 @@
 // nothing.  The array has a fixed maximum size; larger requests are rejected.
 //
 // Set-up: the first call on each device (with that device current) looks the array's device address
-// up with cudaGetSymbolAddress and caches it; that first call should come before any stream capture.
+// up with cudaGetSymbolAddress and caches it with the unique id of the current CUDA context; a call in a
+// different context (after cudaDeviceReset, or once the primary context has been created again) looks it up
+// afresh.  A call that does the look-up should come before any stream capture.
 // Nothing in the scratch needs to start at zero: k_neighbors writes deg, rowptr (n + 1 entries), and
 // -- when the walker's pair list fits -- nbr and rev for every pair, before k_triplets reads them, and
 // k_triplets skips a walker whose pair list overflowed.  There is one scratch array per device, so two
 // calls that may run at the same time on one device (different streams, or different host threads)
 // race on it; calls ordered on one stream do not.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -40,8 +43,37 @@ static __device__ __align__(256) int g_triplet_scratch[FIRE_TRIPLETS_STATIC_MAX_
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 int* g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};  // unique id of the context the cached address belongs to
 
-// Device address of the current device's scratch array (looked up once per device).
+// Unique id of the current CUDA context (cuCtxGetId, never reused within a process), 0 if there is none or the
+// driver cannot tell; the driver entry points come through the runtime, so the library needs no -lcuda.
+unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrent)(CUcontext*);
+  typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    cudaGetLastError();
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+// Device address of the current device's scratch array (looked up once per device and context).
 fire_status current_scratch(int** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
@@ -49,7 +81,8 @@ fire_status current_scratch(int** out) {
     return FIRE_ERR_CUDA;
   }
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_scratch_ptr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_triplet_scratch);
     if (e != cudaSuccess || p == nullptr) {
@@ -60,6 +93,7 @@ fire_status current_scratch(int** out) {
       return FIRE_ERR_CUDA;
     }
     g_scratch_ptr[dev] = static_cast<int*>(p);
+    g_scratch_ctx[dev] = current_context_id();  // the look-up made the context current if there was none
   }
   *out = g_scratch_ptr[dev];
   return FIRE_OK;
