@@ -180,7 +180,7 @@ struct Plan {
   size_t deg, rowptr, nbr, rev, en_cnt, en_idx, counts, pos_off, pos_ctr, pos_dep, dep_pos;
   // T
   size_t E5a, Z1, E5o, HX, HL, HJ, B1X, B1L, B1J, B2X, B2L, B2J, Zx, Zx2, jsq;
-  size_t env, rawx, rjs, Apl, lapA, Jorb, coef_up, coef_dn, Ainv, dgrad;
+  size_t env, rawx, rjs, Apl, lapA, Jorb, coef_up, coef_dn, Ainv, dgrad, env_lo, Apl_lo;
   size_t aX, aJ, aL, Ax, Al, AJ, RX, RJ, RL, R1X, R1J, R1L, R2X, R2J, R2L, Zr, Zr2, jsqr;
   size_t JAx, JAj, JAl, Xo2, Jo2, Lo2, JMx, JMl, JMj, rn, lpn, plr, tile_mask, aD1, aD2, ajsq;
   // double
@@ -234,6 +234,10 @@ Plan make_plan(const fire_problem* p, int Wc, bool fl) {
   take(P.env, G * NV * DN, es);
   take(P.rawx, G * DN, es);
   take(P.Apl, G * DN, es);
+  if (es == 4) {  // FP32 / mixed: the low parts of the compensated envelope values and orbital matrices
+    take(P.env_lo, G * DN, 4);
+    take(P.Apl_lo, G * DN, 4);
+  }
   take(P.coef_up, NDET * W * nu * NV * N * NENV_ORB, es);
   take(P.coef_dn, NDET * W * nd * NV * N * NENV_ORB, es);
   if (fl) {
@@ -544,6 +548,25 @@ cudaError_t gemm(const Ctx<T>& c, GemmP<T> g, int tc_id = -1) {
   return launch_gemm<T, MODE>(g, c.s);
 }
 
+// compensated value contraction (FP32 and mixed paths): low parts into C_lo / read from env_lo, row stride ld_lo
+template <int MODE>
+cudaError_t gemm_comp(const Ctx<float>& c, const GemmP<float>& g, float* C_lo, const float* env_lo, long ld_lo) {
+  Prof pr("gemm", c.s);
+  g_nlaunch++;
+  return launch_gemm_comp<MODE>(g, C_lo, env_lo, ld_lo, c.s);
+}
+
+// Value-plane contraction of a dense layer (EPI_PLAIN or EPI_SILU_X): compensated in the FP32 and mixed paths.
+template <typename T, int MODE>
+cudaError_t value_gemm(const Ctx<T>& c, const GemmP<T>& g) {
+  if constexpr (sizeof(T) == 4) {
+    static_assert(MODE == EPI_PLAIN || MODE == EPI_SILU_X, "value_gemm: plain or SiLU layers");
+    return gemm_comp<MODE == EPI_PLAIN ? COMP_PLAIN : COMP_SILU>(c, g, nullptr, nullptr, 0);
+  } else {
+    return gemm<T, MODE>(c, g);
+  }
+}
+
 // neighbour lists (+ layout for the forward-Laplacian path)
 template <typename T>
 cudaError_t stage_neighbors(Ctx<T>& c, bool fl) {
@@ -571,19 +594,25 @@ cudaError_t stage_neighbors(Ctx<T>& c, bool fl) {
 // CUDA cores the value rows, read with a stride of NV rows: the value plane stays FP32.
 template <typename T>
 cudaError_t ei_gemm(Ctx<T>& c, const GemmP<T>& g, int NV, int tc_id) {
-  if (!(c.mixed && NV > 1)) return gemm<T, EPI_PLAIN>(c, g);
+  if (NV == 1) return value_gemm<T, EPI_PLAIN>(c, g);
+  GemmP<T> gv = g;  // the value rows (every NV-th row), compensated in the FP32 and mixed paths
+  gv.lda = g.lda * NV;
+  gv.ldc = g.ldc * NV;
+  gv.M = g.M / NV;
+  gv.bias_period = g.bias ? 1 : 0;
+  if (!c.mixed) {
+    // FP32 (and FP64): all rows by the CUDA-core contraction; in FP32 the value rows once more, compensated
+    cudaError_t e = gemm<T, EPI_PLAIN>(c, g);
+    if (e != cudaSuccess || sizeof(T) == 8) return e;
+    return value_gemm<T, EPI_PLAIN>(c, gv);
+  }
   GemmP<T> gt = g;
   gt.bias = nullptr;
   gt.bias_period = 0;
   gt.row_skip = NV;
   cudaError_t e = gemm<T, EPI_PLAIN>(c, gt, tc_id);
   if (e != cudaSuccess) return e;
-  GemmP<T> gv = g;
-  gv.lda = g.lda * NV;
-  gv.ldc = g.ldc * NV;
-  gv.M = g.M / NV;
-  gv.bias_period = g.bias ? 1 : 0;
-  return gemm<T, EPI_PLAIN>(c, gv);
+  return value_gemm<T, EPI_PLAIN>(c, gv);
 }
 
 template <typename T, int NT>
@@ -640,7 +669,7 @@ cudaError_t silu_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt, c
     g.aux0 = c.template buf<T>(zx);
     g.aux2 = c.template buf<T>(c.P.Zx2);
   }
-  gemm<T, EPI_SILU_X>(c, g);
+  value_gemm<T, EPI_SILU_X>(c, g);
   if (!fl) return cudaPeekAtLastError();
   cudaMemsetAsync(c.template buf<T>(jsq), 0, sizeof(T) * (size_t)rowsX * N, c.s);
   g = gp0<T>();
@@ -663,7 +692,7 @@ cudaError_t linear_layer(Ctx<T>& c, bool fl, Planes in, Planes out, const T* Wt,
   GemmP<T> g = gp0<T>();
   g.A = c.template buf<T>(in.X); g.lda = K; g.B = Wt; g.ldb = N; g.bias = b; g.bias_period = 1;
   g.C = c.template buf<T>(out.X); g.ldc = N; g.M = rowsX; g.N = N; g.K = K;
-  gemm<T, EPI_PLAIN>(c, g);
+  value_gemm<T, EPI_PLAIN>(c, g);
   if (!fl) return cudaPeekAtLastError();
   g.A = c.template buf<T>(in.J); g.bias = nullptr; g.C = c.template buf<T>(out.J); g.M = rowsJcap;
   g.M_dev = rowsJdev; g.M_scale = rowsJdev ? 3 : 1;
@@ -718,7 +747,16 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
       g.B = c.W.w[s == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (long)d * K8 * n; g.ldb = n;
       g.C = env + (long)d * n; g.ldc = (long)DN * (NV / nvc); g.M = (int)rows; g.N = n; g.K = (int)K8;
       g.n_el = n; g.env_ns = ns; g.env_soff = s == 0 ? 0 : nu; g.env_nv = nvc;
-      gemm<T, EPI_ENV>(c, g);
+      if constexpr (sizeof(T) == 4) {
+        // the value rows by the compensated contraction (hi into the carrier, lo into env_lo); with derivative
+        // rows in the same coefficient block (FP32 forward Laplacian) the plain contraction takes those first
+        if (nvc > 1) gemm<T, EPI_ENV>(c, g);
+        GemmP<float> gv = g;
+        gv.lda = (long)nvc * K8; gv.M = c.Wc * ns; gv.ldc = (long)NV * DN; gv.env_nv = 1;
+        gemm_comp<COMP_ENV>(c, gv, c.template buf<float>(c.P.env_lo) + (long)d * n, nullptr, DN);
+      } else {
+        gemm<T, EPI_ENV>(c, g);
+      }
     }
   }
   GemmP<T> g = gp0<T>();
@@ -726,7 +764,10 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   g.ldb = DN; g.bias = c.W.w[FIRE_P_ORB_UP_B]; g.bias2 = c.W.w[FIRE_P_ORB_DN_B];
   g.C = c.template buf<T>(c.P.Apl); g.ldc = DN; g.M = G; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
   g.aux0 = c.template buf<T>(c.P.rawx); g.aux1 = env; g.ld_aux = DN; g.env_nv = NV;
-  gemm<T, EPI_ORB_X>(c, g);
+  if constexpr (sizeof(T) == 4)
+    gemm_comp<COMP_ORB>(c, g, c.template buf<float>(c.P.Apl_lo), c.template buf<float>(c.P.env_lo), DN);
+  else
+    gemm<T, EPI_ORB_X>(c, g);
   if (!fl) return cudaPeekAtLastError();
   g = gp0<T>();
   g.A = c.template buf<T>(c.P.B2J); g.lda = F; g.B = c.W.w[PR_ORB_UP_W_S1]; g.B2 = c.W.w[PR_ORB_DN_W_S1];
@@ -748,7 +789,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
 // working matrix in the workspace (k_gj_global).  Its shared memory (two panel buffers of n x 17 eight-byte
 // elements plus ~2.5 KB) limits the inverse, and so the local energy, to ELOC_MAX_EL electrons.
 template <typename S, typename TI, typename TO, bool INV>
-cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv, double* cond = nullptr) {
+cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, const TI* A_lo, TO* Ainv, double* cond = nullptr) {
   const int n = c.p->n_el;
   constexpr int BW = GJG_BW_DECL;
   const size_t smem =
@@ -758,7 +799,7 @@ cudaError_t launch_gjg(const Ctx<TI>& c, const TI* A, TO* Ainv, double* cond = n
   const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   g_nlaunch++;
-  kern<<<c.Wc * NDET, GJG_THREADS_DECL, smem, c.s>>>(A, n, c.template buf<S>(c.P.gjw),
+  kern<<<c.Wc * NDET, GJG_THREADS_DECL, smem, c.s>>>(A, A_lo, n, c.template buf<S>(c.P.gjw),
                                                       c.template buf<double>(c.P.ld), c.template buf<double>(c.P.sd),
                                                       cond, Ainv, c.status);
   return cudaPeekAtLastError();
@@ -902,9 +943,9 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   // energy), native FP64 in the FP64 build
   Prof pr_lu("lu", c.s);
   if constexpr (sizeof(T) == 8)
-    launch_gjg<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
+    launch_gjg<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (const T*)nullptr, (T*)nullptr);
   else
-    launch_gjg<df64, T, T, false>(c, c.template buf<T>(c.P.Apl), (T*)nullptr);
+    launch_gjg<df64, T, T, false>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Apl_lo), (T*)nullptr);
   stage_jastrow<T, 0>(c);
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
@@ -944,10 +985,11 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
     // refinement pass eliminates the FP64 orbital matrices of its walkers in FP64
     Prof pr("gauss_jordan", c.s);
     if constexpr (sizeof(T) == 8) {
-      launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv));
+      launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), (const T*)nullptr, c.template buf<T>(c.P.Ainv));
     } else if (rf.c64) {
       const Ctx<double>& c64 = *rf.c64;
-      launch_gjg<double, double, T, true>(c64, c64.template buf<double>(c64.P.Apl), c.template buf<T>(c.P.Ainv));
+      launch_gjg<double, double, T, true>(c64, c64.template buf<double>(c64.P.Apl), (const double*)nullptr,
+                                          c.template buf<T>(c.P.Ainv));
       const size_t nb = sizeof(double) * (size_t)c.Wc * NDET;
       cudaMemcpyAsync(c.template buf<double>(c.P.ld), c64.template buf<double>(c64.P.ld), nb,
                       cudaMemcpyDeviceToDevice, c.s);
@@ -955,7 +997,8 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
                       cudaMemcpyDeviceToDevice, c.s);
     } else {
       // the condition numbers of the orbital matrices feed the ill-conditioned test of the assembly
-      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Ainv),
+      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Apl_lo),
+                                   c.template buf<T>(c.P.Ainv),
                                    rf.idx ? c.template buf<double>(c.P.cond) : nullptr);
     }
   }
@@ -1357,9 +1400,10 @@ cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi, void* sign, in
   {
     Prof pr("gauss_jordan", c.s);
     if constexpr (sizeof(T) == 8)
-      launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(Q.B));
+      launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), (const T*)nullptr, c.template buf<T>(Q.B));
     else
-      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(Q.B));
+      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Apl_lo),
+                                   c.template buf<T>(Q.B));
   }
   stage_jastrow<T, 0>(c);
   const Planes B2{c.P.B2X, 0, 0}, VL{Q.vals, 0, 0};

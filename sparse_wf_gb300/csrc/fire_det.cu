@@ -88,13 +88,15 @@ constexpr int GJG_BW = 16, GJG_THREADS = 512;
 //     column as: interchange rows k_t <-> p_t, then x <- x - W~ x[k_0 .. k_{b-1}];
 //  3. every other column (LU: every column right of the panel) is streamed through shared memory in chunks
 //     of GJG_BW columns and updated with that rank-b product.
-// A: element (i, o) of matrix (w, d) at A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]).
+// A: element (i, o) of matrix (w, d) at A[((w * n + i) * NDET + d) * n + o]  (the orbital plane [G][D * n]);
+// A_lo (double-FP32 elimination only, may be null): the low parts of the same elements.
 // Outputs: logdet[w * NDET + d], sign[...] (double); if INV the inverse, transposed and aligned for
 // k_detlap: Ainv[((w * NDET + d) * n + i) * ainv_ld(n) + sh + o] = (A^-1)[o][i] with sh = (d n) mod 4 and zeros
 // in the other entries of the row, written after undoing the column permutation; if INV and cond is not null,
 // cond[w * NDET + d] = ||A||_F ||A^-1||_F (the Frobenius condition number, >= the 2-norm one).
 template <typename S, typename TI, typename TO, bool INV>
-__global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restrict__ A, int n, S* __restrict__ work,
+__global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restrict__ A, const TI* __restrict__ A_lo,
+                                                             int n, S* __restrict__ work,
                                                              double* __restrict__ logdet, double* __restrict__ sign,
                                                              double* __restrict__ cond, TO* __restrict__ Ainv,
                                                              int32_t* status) {
@@ -121,8 +123,12 @@ __global__ void __launch_bounds__(GJG_THREADS, 2) k_gj_global(const TI* __restri
   double sq = 0.0;  // ||A||_F^2, then ||A^-1||_F^2 (condition number output)
   for (int e = tid; e < n * n; e += blockDim.x) {
     const int i = e / n, o = e - i * n;
-    const TI a = A[((long)(w * n + i) * NDET + d) * n + o];
-    Mb[0][e] = (S)a;
+    const long ia = ((long)(w * n + i) * NDET + d) * n + o;
+    const TI a = A[ia];
+    if constexpr (std::is_same<S, df64>::value && std::is_same<TI, float>::value)
+      Mb[0][e] = A_lo ? df64(a, A_lo[ia]) : S(a);  // the compensated orbital values: a normalised hi + lo pair
+    else
+      Mb[0][e] = (S)a;
     sq += (double)a * (double)a;
   }
   // the block sums of the condition number go through redv (8-byte elements; no static shared memory is added,
@@ -610,17 +616,17 @@ template __global__ void k_env_coef<double, 1>(const double*, const float*, cons
                                                int, double*);
 template __global__ void k_env_coef<double, 5>(const double*, const float*, const double*, int, int, int, int,
                                                int, double*);
-template __global__ void k_gj_global<df64, float, float, false>(const float*, int, df64*, double*, double*, double*,
+template __global__ void k_gj_global<df64, float, float, false>(const float*, const float*, int, df64*, double*, double*, double*,
                                                                  float*, int32_t*);
-template __global__ void k_gj_global<df64, float, float, true>(const float*, int, df64*, double*, double*, double*,
+template __global__ void k_gj_global<df64, float, float, true>(const float*, const float*, int, df64*, double*, double*, double*,
                                                                 float*, int32_t*);
 // FP64 elimination of FP64 orbital matrices with the inverse in FP32 (the refinement pass of the FP32 / mixed local
 // energy, whose determinant Laplacian reads an FP32 inverse)
-template __global__ void k_gj_global<double, double, float, true>(const double*, int, double*, double*, double*,
+template __global__ void k_gj_global<double, double, float, true>(const double*, const double*, int, double*, double*, double*,
                                                                    double*, float*, int32_t*);
-template __global__ void k_gj_global<double, double, double, true>(const double*, int, double*, double*, double*,
+template __global__ void k_gj_global<double, double, double, true>(const double*, const double*, int, double*, double*, double*,
                                                                     double*, double*, int32_t*);
-template __global__ void k_gj_global<double, double, double, false>(const double*, int, double*, double*, double*,
+template __global__ void k_gj_global<double, double, double, false>(const double*, const double*, int, double*, double*, double*,
                                                                      double*, double*, int32_t*);
 template __global__ void k_detlap<float, 128, 0, DL_CSPLIT>(Nbr, Layout, const float*, const float*, const float*,
                                                             double*, double*, int32_t*);

@@ -281,4 +281,150 @@ inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
   return cudaPeekAtLastError();
 }
 
+
+// ----------------------------------------------------------------------------- compensated value contraction
+// FP32 and mixed paths: the value planes (one row per node) feed the orbital matrices, whose inverse amplifies
+// their rounding by the condition number in the derivatives of log det.  k_gemm_comp computes them with
+// compensated dot products (Ogita, Rump and Oishi's Dot2: every product split exactly with an FMA, every partial
+// sum with TwoSum, the errors gathered in a second accumulator), i.e. as if in twice the working precision and
+// then rounded once; the orbital-matrix values and the envelope values they are made of also leave the kernel as
+// unevaluated hi + lo float pairs, so that the double-FP32 elimination sees them to ~2^-48.
+//   COMP_PLAIN  C = a.b + bias (bias on rows with row % bias_period == 0)
+//   COMP_SILU   C = silu(z), z = a.b + bias; with aux0 set also silu'(z) (aux0) and silu''(z) (aux2)
+//   COMP_ENV    envelope value rows (EPI_ENV's row map, env_nv = 1): hi into C, lo into C_lo [g][ld_lo]
+//   COMP_ORB    orbital values (EPI_ORB_X): raw = a.b + bias (per-spin weights and bias), rawx (aux0) = raw,
+//               C + C_lo = raw (env + env_lo) with env = aux1 [row * env_nv * ld_aux], env_lo [row * ld_lo]
+enum CompMode { COMP_PLAIN = 0, COMP_SILU, COMP_ENV, COMP_ORB };
+constexpr int CBM = 64, CBN = 64, CBK = 16, CTHREADS = 256;
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* __restrict__ C_lo,
+                                                        const float* __restrict__ env_lo, long ld_lo) {
+  __shared__ __align__(16) float As[CBK][CBM + 4];
+  __shared__ __align__(16) float Bs[CBK][CBN];
+  const int rows = p.M;
+  const int m0 = blockIdx.y * CBM, n0 = blockIdx.x * CBN;
+  if (m0 >= rows) return;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  int passes = 1, first_spin = 0;
+  if (p.B2) {  // per-spin weights: a pass per spin present in the tile
+    int up = 0, dn = 0;
+    if (tid < CBM && m0 + tid < rows) {
+      if (((m0 + tid) % p.n_el) < p.n_up) up = 1; else dn = 1;
+    }
+    up = __syncthreads_or(up);
+    dn = __syncthreads_or(dn);
+    first_spin = up ? 0 : 1;
+    passes = up + dn;
+  }
+  for (int pass = 0; pass < passes; ++pass) {
+    const int spin = first_spin + pass;
+    const float* Bp = spin == 0 ? p.B : p.B2;
+    float hi[4][4], lo[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.f;
+    for (int k0 = 0; k0 < p.K; k0 += CBK) {
+      // A tile 64 x 16 and B tile 16 x 64: four elements per thread each
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = tid + u * CTHREADS;
+        const int ar = e >> 4, ak = e & 15;
+        const int gr = m0 + ar, gk = k0 + ak;
+        As[ak][ar] = (gr < rows && gk < p.K) ? p.A[(long)gr * p.lda + gk] : 0.f;
+        const int bk = e >> 6, bc = e & 63;
+        const int gk2 = k0 + bk, gc = n0 + bc;
+        Bs[bk][bc] = (gk2 < p.K && gc < p.N) ? Bp[(long)gk2 * p.ldb + gc] : 0.f;
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int kk = 0; kk < CBK; ++kk) {
+        float a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          a[i] = As[kk][ty + 16 * i];
+          b[i] = Bs[kk][tx + 16 * i];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float pr = a[i] * b[j];
+            const float pe = fmaf(a[i], b[j], -pr);
+            float s, e;
+            two_sum(hi[i][j], pr, s, e);
+            hi[i][j] = s;
+            lo[i][j] += e + pe;
+          }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int row = m0 + ty + 16 * i;
+      if (row >= rows) continue;
+      if (p.B2 && (((row % p.n_el) < p.n_up) ? 0 : 1) != spin) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int col = n0 + tx + 16 * j;
+        if (col >= p.N) continue;
+        float h = hi[i][j], l = lo[i][j];
+        if (MODE == COMP_PLAIN || MODE == COMP_SILU || MODE == COMP_ORB) {
+          const float* bias = (MODE == COMP_ORB && spin == 1) ? p.bias2 : p.bias;
+          const bool has_b = bias && (MODE != COMP_PLAIN || (p.bias_period > 0 && row % p.bias_period == 0));
+          if (has_b) {
+            float s, e;
+            two_sum(h, bias[col], s, e);
+            h = s;
+            l += e;
+          }
+        }
+        float s, e;  // normalised pair: s = fl(h + l)
+        two_sum(h, l, s, e);
+        if (MODE == COMP_PLAIN) {
+          p.C[(long)row * p.ldc + col] = s;
+        } else if (MODE == COMP_SILU) {
+          p.C[(long)row * p.ldc + col] = silu(s);
+          if (p.aux0) {
+            float y, d1, d2;
+            silu3(s, y, d1, d2);
+            p.aux0[(long)row * p.ld_aux + col] = d1;
+            p.aux2[(long)row * p.ld_aux + col] = d2;
+          }
+        } else if (MODE == COMP_ENV) {
+          const int g = (row / p.env_ns) * p.n_el + p.env_soff + row % p.env_ns;
+          p.C[(long)g * p.ldc + col] = s;
+          C_lo[(long)g * ld_lo + col] = e;
+        } else {  // COMP_ORB
+          p.aux0[(long)row * p.ld_aux + col] = s;
+          const float eh = p.aux1[(long)row * p.env_nv * p.ld_aux + col], el = env_lo[(long)row * ld_lo + col];
+          const float ph = s * eh;
+          const float pl = fmaf(s, eh, -ph) + (s * el + e * eh);
+          float oh, ol;
+          two_sum(ph, pl, oh, ol);
+          p.C[(long)row * p.ldc + col] = oh;
+          C_lo[(long)row * ld_lo + col] = ol;
+        }
+      }
+    }
+    if (pass + 1 < passes) __syncthreads();
+  }
+}
+
+template <int MODE>
+inline cudaError_t launch_gemm_comp(const GemmP<float>& p, float* C_lo, const float* env_lo, long ld_lo,
+                                    cudaStream_t s) {
+  dim3 grid((p.N + CBN - 1) / CBN, (p.M + CBM - 1) / CBM);
+  if (grid.y == 0 || grid.x == 0) return cudaSuccess;
+  k_gemm_comp<MODE><<<grid, CTHREADS, 0, s>>>(p, C_lo, env_lo, ld_lo);
+  return cudaPeekAtLastError();
+}
+
 }  // namespace fire

@@ -36,7 +36,7 @@ template <typename T, int NV>
 __global__ void k_env_coef(const T* r, const float* R, const T* sp, int n, int n_s, int s_off, int N, int Wn,
                            T* coef);
 template <typename S, typename TI, typename TO, bool INV>
-__global__ void k_gj_global(const TI* A, int n, S* work, double* logdet, double* sign, double* cond, TO* Ainv,
+__global__ void k_gj_global(const TI* A, const TI* A_lo, int n, S* work, double* logdet, double* sign, double* cond, TO* Ainv,
                             int32_t* status);
 constexpr int GJG_BW_DECL = 16, GJG_THREADS_DECL = 512;
 template <typename T, int NT, int CLO, int CHI>
