@@ -1788,7 +1788,8 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
     for (int m = 0; m < cnt; ++m) {
       const float* src = reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot] + (size_t)m * K * N;
       g_nlaunch++;
-      if (tc_tiled(k, K)) split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s);
+      if (tc_tiled(k, K))  // envelope weights (k_env_tc, A split elementwise on chip) keep the elementwise split
+        split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s, kTcSrc[k].kind != -1);
       else split_transpose(src, (int)K, (int)N, hi + (size_t)m * N * K, lo + (size_t)m * N * K, s);
     }
   }
@@ -2101,7 +2102,7 @@ fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const
   g_nlaunch += 2;
   TcWeights wt{};
   if (K <= 256) {
-    split_tiles(W, K, N, hi, s);
+    split_tiles(W, K, N, hi, s, true);
     wt.tiles = hi;
   } else {
     split_transpose(W, K, N, hi, hi + (size_t)N * K, s);

@@ -132,6 +132,27 @@ __device__ __forceinline__ void cp_async_wait_tc(int n) {
   else if (n == 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
   else asm volatile("cp.async.wait_group 3;" ::: "memory");
 }
+// a = hi + lo on the grid of step sc = 2^(e - 7) of a row whose largest magnitude is in [2^e, 2^(e+1)) (inv = 1 / sc):
+// hi = sc rint(a / sc) is an integer multiple of sc of magnitude <= 256 sc (exact in BF16), a - hi is exact in FP32
+// and |a - hi| <= sc / 2; two values as BF16 pairs (first value in the low half).  Products of two such hi parts
+// are integers times sc_a sc_b below 2^16, so up to 256 of them sum exactly in an FP32 accumulator.
+__device__ __forceinline__ void split_grid_bf16x2(float a, float b, float sc, float inv, uint32_t& hi, uint32_t& lo) {
+  const float ha = rintf(a * inv) * sc, hb = rintf(b * inv) * sc;
+  const __nv_bfloat162 h = __floats2bfloat162_rn(ha, hb);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - ha, b - hb);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+// the grid step of a row (or column) of largest magnitude mx: (sc, inv), or (0, 0) when mx is 0 or not finite
+__device__ __forceinline__ void grid_step(float mx, float& sc, float& inv) {
+  if (mx > 0.f && mx <= 3.0e38f) {
+    const int e = ilogbf(mx);
+    sc = ldexpf(1.f, e - 7);
+    inv = ldexpf(1.f, 7 - e);
+  } else {
+    sc = inv = 0.f;
+  }
+}
 // a = hi + lo for two values: BF16 pairs (first value in the low half)
 __device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
@@ -266,7 +287,7 @@ __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int nod
 template <int MODE>
 __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows, int m0, int n0, uint32_t tacc,
                                                  int spin_filter, int tma, const CUtensorMap* tmC, float* stg,
-                                                 int& nst, int warp, int lane) {
+                                                 int& nst, int warp, int lane, bool two_acc = false) {
   const int quad = warp & 3, half = warp >> 2;
   const int row = m0 + quad * 32 + lane;
   const bool valid = row < rows;
@@ -285,6 +306,12 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
   for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
     float v[16];
     tmem_ld16(base + (uint32_t)c0, v);
+    if (two_acc) {  // the exact hi x hi sums plus the cross terms, TCP_BN columns further on
+      float v2[16];
+      tmem_ld16(base + (uint32_t)(TCP_BN + c0), v2);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) v[k] += v2[k];
+    }
     const int spin = spin_filter < 0 ? 0 : spin_filter;
     const bool full = n0 + c0 + 15 < p.N;
     const bool use_tma = tma_warp && full;
@@ -594,16 +621,24 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcs(GemmP<float> p, con
 // apart, 8-row groups 128 bytes apart).  A is a ring of 64-deep blocks: block kb is released once the MMAs of
 // the last column tile have read it, so the next row tile's conversion overlaps the current tile's tail.
 // Warp roles: 0-7 epilogue, 8-11 A converters, 12 (lane 0) MMA issuer, 13 (lane 0) weight loader.
+// Splitting: every row of A (and, at preparation, every column of the weights) is split on the grid of its own
+// largest magnitude (split_grid_bf16x2), so that the hi x hi products of a row and a column are integer multiples
+// of one step and their sum over K <= 256 is exact in FP32 whatever order and rounding the tensor core's
+// accumulation uses; they accumulate in one TMEM accumulator and the cross terms a_hi w_lo + a_lo w_hi in a second
+// one (~2^-8 of the result, so their accumulation rounding is ~2^-32 of it); the epilogue adds the two.  The
+// a_lo w_lo term (~2^-18 of a product, unbiased) is left out.
 constexpr int TCA_THREADS = 448, TCA_KB = 4, TCA_BSTAGES = 2;
 struct TcaCfg {
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;  // one BF16 plane of a 128 x 64 block
   static constexpr int A_BLOCK = 2 * A_BYTES;        // hi + lo
   static constexpr int B_BLOCK = 2 * TCP_BN * TC_BK * 2;  // one tiled weight block (hi + lo)
   static constexpr int STG_BYTES = TcCfg::STG_BYTES;
-  static constexpr int TOTAL = TCA_KB * A_BLOCK + TCA_BSTAGES * B_BLOCK + STG_BYTES + 256;
+  static constexpr int RMAX_BYTES = 2 * 2 * TC_BM * 4;  // row maxima: [row tile parity][k half][128 rows]
+  static constexpr int TOTAL = TCA_KB * A_BLOCK + TCA_BSTAGES * B_BLOCK + STG_BYTES + RMAX_BYTES + 256;
 };
 struct TcaBar {
   uint64_t afull[TCA_KB], aempty[TCA_KB], bfull[TCA_BSTAGES], bempty[TCA_BSTAGES], tfull[2], tempty[2];
+  uint64_t rmax;  // the converters' row maxima of a row tile are complete
   uint32_t tmem;
   int abort;
 };
@@ -617,7 +652,9 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
   unsigned char* ares = tc_smem;                                   // [kb][hi, lo][128 x 64], LBO 128, SBO 1024
   unsigned char* bst = tc_smem + TCA_KB * TcaCfg::A_BLOCK;         // [stage][hi, lo][8 k-groups][128 rows][16 B]
   float* stg = reinterpret_cast<float*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK);
-  TcaBar* bars = reinterpret_cast<TcaBar*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK + TcaCfg::STG_BYTES);
+  float* rpart = reinterpret_cast<float*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK + TcaCfg::STG_BYTES);
+  TcaBar* bars = reinterpret_cast<TcaBar*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK + TcaCfg::STG_BYTES +
+                                           TcaCfg::RMAX_BYTES);
   volatile int* abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -641,12 +678,13 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
       mbar_init(smem_u32(&bars->tfull[b]), 1);
       mbar_init(smem_u32(&bars->tempty[b]), 256);
     }
+    mbar_init(smem_u32(&bars->rmax), 128);
     bars->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 12) {
+  if (warp == 12) {  // two accumulator pairs (exact hi x hi sums, cross terms): all 512 columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem)),
-                 "r"(2 * TCP_BN));
+                 "r"(4 * TCP_BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   proxy_fence();
@@ -689,8 +727,44 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
         cp_async_commit_tc();
         ++issued;
       }
-      for (int kb = 0; kb < issued; ++kb) {
-        cp_async_wait_tc(issued - 1 - kb);
+      if (issued < nk) break;  // aborted
+      // the grid of every row: its largest magnitude over K.  A row's k-groups belong to lanes r8, r8 + 8, r8 + 16,
+      // r8 + 24 of two warps (k halves lw & 1); each warp writes its half's maxima, and the converters meet on an
+      // mbarrier (bounded wait) before reading the other half's.  The buffer alternates between row tiles: a warp
+      // writing row tile t + 2 has passed the barrier of t + 1, so every reader of t is done.
+      cp_async_wait_tc(0);
+      float mx[8];
+#pragma unroll
+      for (int it = 0; it < 8; ++it) mx[it] = 0.f;
+      for (int kb = 0; kb < nk; ++kb) {
+        const unsigned char* a_hi = ares + kb * TcaCfg::A_BLOCK;
+        const unsigned char* a_lo = a_hi + TcaCfg::A_BYTES;
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+          const int blk = lw + 4 * it;
+          const uint32_t off = tc_off((blk >> 1) * 8 + r8, (blk & 1) * 32 + kq8 * 8);
+          const float4 x = *reinterpret_cast<const float4*>(a_hi + off);
+          const float4 y = *reinterpret_cast<const float4*>(a_lo + off);
+          mx[it] = fmaxf(mx[it], fmaxf(fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fmaxf(fabsf(x.z), fabsf(x.w))),
+                                       fmaxf(fmaxf(fabsf(y.x), fabsf(y.y)), fmaxf(fabsf(y.z), fabsf(y.w)))));
+        }
+      }
+      float* part = rpart + (ua & 1) * 2 * TC_BM;
+#pragma unroll
+      for (int it = 0; it < 8; ++it) {
+        mx[it] = fmaxf(mx[it], __shfl_xor_sync(0xffffffffu, mx[it], 8));
+        mx[it] = fmaxf(mx[it], __shfl_xor_sync(0xffffffffu, mx[it], 16));
+        if (kq8 == 0) part[(lw & 1) * TC_BM + ((lw + 4 * it) >> 1) * 8 + r8] = mx[it];
+      }
+      tc_arrive(&bars->rmax);
+      if (!tc_wait(&bars->rmax, (uint32_t)(ua & 1), abort)) break;
+      float sc[8], inv[8];
+#pragma unroll
+      for (int it = 0; it < 8; ++it) {
+        const int r = ((lw + 4 * it) >> 1) * 8 + r8;
+        grid_step(fmaxf(part[r], part[TC_BM + r]), sc[it], inv[it]);
+      }
+      for (int kb = 0; kb < nk; ++kb) {
         unsigned char* a_hi = ares + kb * TcaCfg::A_BLOCK;
         unsigned char* a_lo = a_hi + TcaCfg::A_BYTES;
 #pragma unroll
@@ -701,17 +775,23 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
           const float4 x = *reinterpret_cast<const float4*>(a_hi + off);
           const float4 y = *reinterpret_cast<const float4*>(a_lo + off);
           uint4 hi, lo;
-          split_bf16x2(x.x, x.y, hi.x, lo.x);
-          split_bf16x2(x.z, x.w, hi.y, lo.y);
-          split_bf16x2(y.x, y.y, hi.z, lo.z);
-          split_bf16x2(y.z, y.w, hi.w, lo.w);
+          if (inv[it] != 0.f) {
+            split_grid_bf16x2(x.x, x.y, sc[it], inv[it], hi.x, lo.x);
+            split_grid_bf16x2(x.z, x.w, sc[it], inv[it], hi.y, lo.y);
+            split_grid_bf16x2(y.x, y.y, sc[it], inv[it], hi.z, lo.z);
+            split_grid_bf16x2(y.z, y.w, sc[it], inv[it], hi.w, lo.w);
+          } else {  // an all-zero (or non-finite) row
+            split_bf16x2(x.x, x.y, hi.x, lo.x);
+            split_bf16x2(x.z, x.w, hi.y, lo.y);
+            split_bf16x2(y.x, y.y, hi.z, lo.z);
+            split_bf16x2(y.z, y.w, hi.w, lo.w);
+          }
           *reinterpret_cast<uint4*>(a_hi + off) = hi;
           *reinterpret_cast<uint4*>(a_lo + off) = lo;
         }
         proxy_fence();
         tc_arrive(&bars->afull[kb]);
       }
-      if (issued < nk) break;  // aborted
       ++ua;
     }
     cp_async_wait_tc(0);
@@ -746,7 +826,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
           const long ub = uc >> 1;
           if (ub > 0 && !tc_wait(&bars->tempty[b], (uint32_t)((ub - 1) & 1), abort)) break;
           tc_fence_after();
-          const uint32_t acc_t = tmem + (uint32_t)(b * TCP_BN);
+          const uint32_t acc_t = tmem + (uint32_t)(b * 2 * TCP_BN);  // hi x hi sums; cross terms TCP_BN further
           for (int kb = 0; kb < nk; ++kb, ++bc) {
             if (j == 0 && !tc_wait(&bars->afull[kb], (uint32_t)(ua & 1), abort)) break;
             const int s2 = (int)(bc % TCA_BSTAGES);
@@ -760,8 +840,8 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
               const uint64_t dah = tc_desc(ah + sa), dal = tc_desc(al + sa);
               const uint64_t dbh = tc_desc_s(bh + sb, 2048, 128), dbl = tc_desc_s(bl + sb, 2048, 128);
               tc_mma(acc_t, dah, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-              tc_mma(acc_t, dah, dbl, idesc, 1u);
-              tc_mma(acc_t, dal, dbh, idesc, 1u);
+              tc_mma(acc_t + TCP_BN, dah, dbl, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+              tc_mma(acc_t + TCP_BN, dal, dbh, idesc, 1u);
             }
             tc_commit(smem_u32(&bars->bempty[s2]));
             if (j == nt - 1) tc_commit(smem_u32(&bars->aempty[kb]));
@@ -784,8 +864,8 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
         const int b = (int)(uc & 1);
         if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
         tc_fence_after();
-        tc_epilogue_tile<MODE>(p, rows, m0, j * TCP_BN, tmem + (uint32_t)(b * TCP_BN), spin_filter, tma, &tmC, stg,
-                               nst, warp, lane);
+        tc_epilogue_tile<MODE>(p, rows, m0, j * TCP_BN, tmem + (uint32_t)(b * 2 * TCP_BN), spin_filter, tma, &tmC,
+                               stg, nst, warp, lane, true);
         tc_fence_before();
         tc_arrive(&bars->tempty[b]);
         ++uc;
@@ -834,7 +914,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
   __syncthreads();
   tc_fence_after();
   if (warp == 12) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TCP_BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(4 * TCP_BN));
   }
 }
 
