@@ -491,6 +491,10 @@ struct Ctx {
   Nbr nb;
   Layout L;
   bool mixed = false;
+  // FP32 / mixed: value planes by the compensated contraction and the orbital matrices as hi + lo pairs (the local
+  // energy, log|psi| and the low-rank state); the Metropolis blocks' proposals, which only compare log|psi| values,
+  // take the plain contraction
+  bool comp = true;
   TcWeights tcw[TC_COUNT];
   template <typename U>
   U* buf(size_t off) const {
@@ -561,6 +565,7 @@ template <typename T, int MODE>
 cudaError_t value_gemm(const Ctx<T>& c, const GemmP<T>& g) {
   if constexpr (sizeof(T) == 4) {
     static_assert(MODE == EPI_PLAIN || MODE == EPI_SILU_X, "value_gemm: plain or SiLU layers");
+    if (!c.comp) return gemm<T, MODE>(c, g);
     return gemm_comp<MODE == EPI_PLAIN ? COMP_PLAIN : COMP_SILU>(c, g, nullptr, nullptr, 0);
   } else {
     return gemm<T, MODE>(c, g);
@@ -747,15 +752,15 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
       g.B = c.W.w[s == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (long)d * K8 * n; g.ldb = n;
       g.C = env + (long)d * n; g.ldc = (long)DN * (NV / nvc); g.M = (int)rows; g.N = n; g.K = (int)K8;
       g.n_el = n; g.env_ns = ns; g.env_soff = s == 0 ? 0 : nu; g.env_nv = nvc;
-      if constexpr (sizeof(T) == 4) {
+      if (sizeof(T) == 8 || !c.comp) {
+        gemm<T, EPI_ENV>(c, g);
+      } else if constexpr (sizeof(T) == 4) {
         // the value rows by the compensated contraction (hi into the carrier, lo into env_lo); with derivative
         // rows in the same coefficient block (FP32 forward Laplacian) the plain contraction takes those first
         if (nvc > 1) gemm<T, EPI_ENV>(c, g);
         GemmP<float> gv = g;
         gv.lda = (long)nvc * K8; gv.M = c.Wc * ns; gv.ldc = (long)NV * DN; gv.env_nv = 1;
         gemm_comp<COMP_ENV>(c, gv, c.template buf<float>(c.P.env_lo) + (long)d * n, nullptr, DN);
-      } else {
-        gemm<T, EPI_ENV>(c, g);
       }
     }
   }
@@ -764,10 +769,14 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   g.ldb = DN; g.bias = c.W.w[FIRE_P_ORB_UP_B]; g.bias2 = c.W.w[FIRE_P_ORB_DN_B];
   g.C = c.template buf<T>(c.P.Apl); g.ldc = DN; g.M = G; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
   g.aux0 = c.template buf<T>(c.P.rawx); g.aux1 = env; g.ld_aux = DN; g.env_nv = NV;
-  if constexpr (sizeof(T) == 4)
-    gemm_comp<COMP_ORB>(c, g, c.template buf<float>(c.P.Apl_lo), c.template buf<float>(c.P.env_lo), DN);
-  else
+  if constexpr (sizeof(T) == 4) {
+    if (c.comp)
+      gemm_comp<COMP_ORB>(c, g, c.template buf<float>(c.P.Apl_lo), c.template buf<float>(c.P.env_lo), DN);
+    else
+      gemm<T, EPI_ORB_X>(c, g);
+  } else {
     gemm<T, EPI_ORB_X>(c, g);
+  }
   if (!fl) return cudaPeekAtLastError();
   g = gp0<T>();
   g.A = c.template buf<T>(c.P.B2J); g.lda = F; g.B = c.W.w[PR_ORB_UP_W_S1]; g.B2 = c.W.w[PR_ORB_DN_W_S1];
@@ -945,7 +954,8 @@ cudaError_t chunk_logpsi(Ctx<T>& c, void* logpsi, void* sign, int w0_out) {
   if constexpr (sizeof(T) == 8)
     launch_gjg<double, T, T, false>(c, c.template buf<T>(c.P.Apl), (const T*)nullptr, (T*)nullptr);
   else
-    launch_gjg<df64, T, T, false>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Apl_lo), (T*)nullptr);
+    launch_gjg<df64, T, T, false>(c, c.template buf<T>(c.P.Apl), c.comp ? c.template buf<T>(c.P.Apl_lo) : nullptr,
+                                  (T*)nullptr);
   stage_jastrow<T, 0>(c);
   AssembleOut o;
   std::memset(&o, 0, sizeof(o));
@@ -1253,6 +1263,7 @@ fire_status run_mcmc(const fire_problem* p, cudaStream_t s, const float* R, cons
   const int Wc = choose_chunk(p, wsb, false);
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
+  c.comp = false;  // proposals are only compared by their log|psi|: plain value contractions
   T* rr = reinterpret_cast<T*>(r);
   const int n = p->n_el;
   for (int w0 = 0; w0 < p->n_walkers; w0 += Wc) {

@@ -726,16 +726,17 @@ def make_width_scheduler(window_size: int = 20, target_pmove: float = 0.5, error
 
 def make_mcmc(wf: FireWaveFunction, steps: int = 20, init_width: float = 0.1, proposal: str = "all-electron",
               sweeps: float = 2.0, jump_steps: int = 0, max_cluster_size: int = 5, max_cluster_radius: float = 2.0,
-              sweep_type: str = "sequential", low_rank: bool = False):
+              sweep_type: str = "sequential", low_rank: bool = True):
     """``make_mcmc`` (``mcmc.py:278-346``) for the "all-electron" proposal (``steps`` moves of every electron) and
     the "single-electron" proposal (``int(sweeps * n_el)`` one-electron moves in sequential order, the reference's
     default; ``init_width`` 0.5 there, ``config/default.yaml``), preceded by ``jump_steps`` jumps to the nuclei
     (sigma 2, ``mcmc.py:320-326, 332-335``; 20 in the reference's defaults); "cluster-update" runs
     ``int(sweeps * n_el)`` cluster moves (``mcmc.py:305-316``; sequential sweeps must be whole):
     ``mcmc_step(key, params, electrons, static, width) -> (electrons, stats)`` with key an integer seed.  low_rank
-    evaluates the single-electron moves, the cluster updates and the jumps from a state per walker
-    (``mcmc_low_rank_block``, ``mcmc_low_rank_cluster_block``, ``mcmc_low_rank_jump_block``) instead of in full;
-    stats then also hold the move statics."""
+    (the default, as the reference's ``mcmc_steps_low_rank``) evaluates the single-electron moves, the cluster updates
+    and the jumps from a state per walker (``mcmc_low_rank_block``, ``mcmc_low_rank_cluster_block``,
+    ``mcmc_low_rank_jump_block``); low_rank=False evaluates every proposal in full.  stats then also hold the move
+    statics."""
     proposal = proposal.lower()
     if proposal not in ("all-electron", "single-electron", "cluster-update"):
         raise ValueError(f"Invalid proposal: {proposal}")
