@@ -92,10 +92,16 @@ typedef struct {
                             (<= 0: FIRE_REFINE_RATIO) */
   float refine_kappa;    /* ... or when its determinant-weighted condition number
                             sum_d |w_d| kappa_F(A_d) / |sum_d w_d| exceeds refine_kappa (<= 0: FIRE_REFINE_KAPPA) */
+  float refine_ks;       /* ... or when (|lap| + |grad|^2) / 2 exceeds refine_ks Hartree (<= 0: FIRE_REFINE_KS) */
 } fire_problem;
 
-#define FIRE_REFINE_RATIO 8.0f
+/* Defaults of the ill-conditioned test.  After compensation the FP32 value planes move E_loc by ~1e-7 of the
+ * kinetic terms (|lap| + |grad|^2) / 2, randomly signed: the walkers above FIRE_REFINE_KS carry errors of a few mHa
+ * and dominate the error of a batch mean, the walkers above FIRE_REFINE_RATIO |E_loc| (near a node) the relative
+ * error of their own E_loc. */
+#define FIRE_REFINE_RATIO 100.0f
 #define FIRE_REFINE_KAPPA 1.0e5f
+#define FIRE_REFINE_KS 3.0e4f
 
 /* Parameter slots of the flat parameter blob (float32), in blob order.  Shapes with
  * F = 256, D = 4 determinants, n = n_el, N = n_nuc are given by fire_param_layout. */
@@ -207,7 +213,7 @@ typedef struct {
  * FP32 and mixed precision: near a node of psi, E_loc is the small difference of two large terms
  * (lap log psi and |grad log psi|^2), and the FP32 rounding of the value planes that lead to the orbital
  * matrices moves it by up to ~2e-6 of their size; an orbital matrix of large condition number amplifies that
- * rounding in the same way.  A walker whose (|lap| + |grad|^2) / 2 exceeds refine_ratio |E_loc|, whose
+ * rounding in the same way.  A walker whose (|lap| + |grad|^2) / 2 exceeds refine_ratio |E_loc| or refine_ks, whose
  * determinant-weighted condition number (debug->cond) exceeds refine_kappa, or whose E_loc is not finite is
  * ill-conditioned: with refine_cap > 0, up to refine_cap of them are evaluated once more after the batch, with
  * the values of the embedding, orbitals, envelopes and orbital matrices, their LU and inverse in FP64 (the

@@ -1052,6 +1052,7 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
     o.ref_cap = rf.cap;
     o.ref_ratio = c.p->refine_ratio > 0.f ? (double)c.p->refine_ratio : (double)FIRE_REFINE_RATIO;
     o.ref_kappa = c.p->refine_kappa > 0.f ? (double)c.p->refine_kappa : (double)FIRE_REFINE_KAPPA;
+    o.ref_ks = c.p->refine_ks > 0.f ? (double)c.p->refine_ks : (double)FIRE_REFINE_KS;
     o.cond = c.template buf<double>(c.P.cond);
   }
   Prof pr("assemble", c.s);

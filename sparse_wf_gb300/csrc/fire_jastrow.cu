@@ -435,7 +435,8 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
       cw /= fabs(S);
     }
     if (out.dbg.cond && !out.wmap) out.dbg.cond[row] = cw;
-    if (out.ref_idx && !(0.5 * (fabs(lap) + vv[0]) <= out.ref_ratio * fabs(eloc) && cw <= out.ref_kappa)) {
+    const double ks = 0.5 * (fabs(lap) + vv[0]);
+    if (out.ref_idx && !(ks <= out.ref_ratio * fabs(eloc) && ks <= out.ref_ks && cw <= out.ref_kappa)) {
       const int slot = atomicAdd(out.ref_cnt, 1);
       if (slot < out.ref_cap) out.ref_idx[slot] = (int32_t)row;
     }

@@ -87,21 +87,24 @@ def oracle_batch(mol, n_up, params, walkers):
 ELOC_TOL = {"fp32": 1e-5, "mixed": 1e-4}
 
 
-def check_eloc_contract(precision, wf, got, eloc, ks, epot, refined, lap=None, lap_ref=None, grad=None, grad_ref=None):
+def check_eloc_contract(precision, wf, got, eloc, ks, epot, refined, lap=None, lap_ref=None, grad=None, grad_ref=None,
+                        tol=None):
     """Per-walker local-energy contract of the FP32 (1e-5) and mixed (1e-4) paths against the FP64 oracle.
 
     E_loc = -(lap log psi + |grad log psi|^2) / 2 + V is a sum of terms that cancel: near a node of psi the two
     kinetic terms, and for a walker whose kinetic energy balances its potential energy (E_loc crosses zero) the
     kinetic and potential terms.  Its error is held relative to the magnitude of those terms,
-    S = ks + |V| with ks = (|lap log psi| + |grad log psi|^2) / 2, the scale the reference's own float32 energy test
-    also works against (it allows 1e-2 of |E_kin|): |dE_loc| <= tol S on every walker, |d lap| <= 2 tol S and
-    |d grad| <= tol sqrt(2 S).  Every walker whose ks exceeds 1.05 refine_ratio |E_loc| must have gone through the
-    device's FP64 refinement pass.  Returns the fraction of walkers within tol |E_loc|."""
-    tol = ELOC_TOL[precision]
+    S = ks + |V| with ks = (|lap log psi| + |grad log psi|^2) / 2 (the reference's own float32 energy test allows 1e-2
+    of |E_kin|): |dE_loc| <= tol S on every walker, |d lap| <= 2 tol S and |d grad| <= tol sqrt(2 S).  Every walker
+    whose ks exceeds 1.05 refine_ratio |E_loc| must have gone through the
+    device's FP64 refinement pass, and so must every walker whose ks exceeds 1.05 refine_ks.  Returns the fraction of
+    walkers within tol |E_loc|."""
+    tol = ELOC_TOL[precision] if tol is None else tol
     eloc, ks, epot = np.asarray(eloc, np.float64), np.asarray(ks, np.float64), np.asarray(epot, np.float64)
     S = ks + np.abs(epot)
     err = np.abs(np.asarray(got, np.float64) - eloc)
-    assert np.all(refined[ks > 1.05 * wf.refine_ratio * np.abs(eloc)]), (ks / np.abs(eloc), refined)
+    must = (ks > 1.05 * wf.refine_ratio * np.abs(eloc)) | (ks > 1.05 * wf.refine_ks)
+    assert np.all(refined[must]), (ks / np.abs(eloc), refined)
     assert np.all(err <= tol * S), (np.max(err / S), int(np.argmax(err / S)), int(refined.sum()))
     if lap is not None:
         dl = np.abs(np.asarray(lap, np.float64) - lap_ref)
