@@ -68,10 +68,14 @@ typedef enum {
  * the host grows capacities from these, like StaticScheduler (static_args.py:62-84). */
 
 typedef enum {
-  FIRE_PREC_FP32 = 0,  /* FP32 SIMT; orbital LU and inverse in double-FP32 (48-bit significand) */
-  FIRE_PREC_MIXED = 1, /* derivative planes of the contractions on tensor cores in split BF16 (three BF16
-                          products per FP32 product, FP32 accumulation), value planes FP32, orbital LU and
-                          inverse in double-FP32 */
+  FIRE_PREC_FP32 = 0,  /* FP32 SIMT; value planes by compensated (twice-the-working-precision) dot products, the
+                          orbital-matrix values as hi + lo float pairs; orbital LU and inverse in double-FP32
+                          (48-bit significand) */
+  FIRE_PREC_MIXED = 1, /* derivative planes of the contractions on tensor cores: K <= 256 with every row of A and
+                          column of W scaled and split on the grid of its largest value into FP16 hi + lo (the
+                          hi x hi sums exact in one FP32 accumulator, the cross terms in a second; ~2^-20 of a row's
+                          largest value per element), K > 256 (the envelope rows) in split BF16 (three products per
+                          FP32 product); value planes, orbital LU and inverse as in FIRE_PREC_FP32 */
   FIRE_PREC_FP64 = 2   /* everything in FP64 (validation build of the same kernels) */
 } fire_precision;
 
@@ -386,8 +390,10 @@ fire_status fire_profile_enable(int32_t on);
 fire_status fire_profile_report(char* buf, size_t len);
 
 /* The mixed-precision tensor-core contraction alone: C[M, N] = A[M, K] W[K, N] (all float32, row-major,
- * device), computed with split-BF16 operands on tcgen05 (three BF16 products per element pair, FP32
- * accumulation).  workspace: the split weights, 32768 * ceil(N / 128) * ceil(K / 64) bytes for K <= 256,
+ * device), on tcgen05.  K <= 256: rows of A and columns of W scaled and split on the grid of their largest
+ * value into FP16 hi + lo, the hi x hi sums exact in one FP32 accumulator and the two cross products in a second;
+ * K > 256: elementwise split BF16, three BF16 products per element pair, one FP32 accumulator.  workspace: the
+ * split weights, 32768 * ceil(N / 128) * ceil(K / 64) + 4 * N bytes for K <= 256 (tiles, column scales),
  * else 4 * N * K bytes.  K % 8 == 0, N % 4 == 0
  * and 16-byte aligned A and C (else FIRE_ERR_UNSUPPORTED); K > 256 streams the weights through the
  * pipeline instead of keeping them in shared memory. */

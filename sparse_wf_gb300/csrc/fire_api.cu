@@ -140,6 +140,10 @@ void tc_shape(int k, const fire_problem* p, size_t* K, size_t* N, int* cnt) {
   *cnt = kind == -1 ? NDET : 1;
 }
 bool tc_tiled(int k, size_t K) { return K <= 256 || kTcSrc[k].kind == -1; }
+// the A-resident kernel's slots (K <= 256, not the envelope): FP16 scaled-grid tiles followed by N column scales
+bool tc_grid(int k, size_t K) { return K <= 256 && kTcSrc[k].kind != -1; }
+// byte offset of a grid slot's column scales from its tiles (one matrix per grid slot)
+size_t tc_cs_offset(size_t K, size_t N) { return tc_tiles_bytes(K, N); }
 // byte offsets of the BF16 region (tc_off[TC_COUNT] = end)
 void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
   size_t o = (float_bytes + 255) / 256 * 256;
@@ -149,6 +153,7 @@ void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
     int cnt;
     tc_shape(k, p, &K, &N, &cnt);
     o += tc_tiled(k, K) ? (size_t)cnt * tc_tiles_bytes(K, N) : 2 * (size_t)cnt * N * K * sizeof(__nv_bfloat16);
+    if (tc_grid(k, K)) o += (size_t)cnt * N * sizeof(float);
     o = (o + 255) / 256 * 256;
   }
   off[TC_COUNT] = o;
@@ -1091,10 +1096,14 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
       int cnt;
       tc_shape(k, p, &K, &N, &cnt);
       const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
-      if (tc_tiled(k, K)) c.tcw[k] = TcWeights{nullptr, nullptr, hi, nullptr};
-      else c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr};
+      if (tc_grid(k, K))
+        c.tcw[k] = TcWeights{nullptr, nullptr, hi, nullptr,
+                             reinterpret_cast<const float*>(base + to[k] + tc_cs_offset(K, N)), nullptr};
+      else if (tc_tiled(k, K)) c.tcw[k] = TcWeights{nullptr, nullptr, hi, nullptr, nullptr, nullptr};
+      else c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr, nullptr, nullptr};
     }
     c.tcw[TC_ORB_UP].tiles2 = c.tcw[TC_ORB_DN].tiles;
+    c.tcw[TC_ORB_UP].cs2 = c.tcw[TC_ORB_DN].cs;
   }
   return c;
 }
@@ -1801,7 +1810,8 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
       const float* src = reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot] + (size_t)m * K * N;
       g_nlaunch++;
       if (tc_tiled(k, K))  // envelope weights (k_env_tc, A split elementwise on chip) keep the elementwise split
-        split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s, kTcSrc[k].kind != -1);
+        split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s,
+                    tc_grid(k, K) ? reinterpret_cast<float*>(base + to[k] + tc_cs_offset(K, N)) : nullptr);
       else split_transpose(src, (int)K, (int)N, hi + (size_t)m * N * K, lo + (size_t)m * N * K, s);
     }
   }
@@ -2107,15 +2117,17 @@ fire_status fire_potential_energy(void* stream, const fire_problem* prob, const 
 fire_status fire_gemm_mixed(void* stream, int32_t M, int32_t N, int32_t K, const float* A, const float* W, float* C,
                             void* workspace, size_t workspace_bytes, int32_t* status) {
   if (M < 1 || N < 1 || K < 8 || K % 8 != 0 || !A || !W || !C || !workspace) return FIRE_ERR_INVALID;
-  const size_t need = K <= 256 ? tc_tiles_bytes(K, N) : 4 * (size_t)N * K;
+  const size_t need = K <= 256 ? tc_tiles_bytes(K, N) + 4 * (size_t)N : 4 * (size_t)N * K;
   if (workspace_bytes < need) return FIRE_ERR_WORKSPACE;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(workspace);
   g_nlaunch += 2;
   TcWeights wt{};
   if (K <= 256) {
-    split_tiles(W, K, N, hi, s, true);
+    float* cs = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(workspace) + tc_tiles_bytes(K, N));
+    split_tiles(W, K, N, hi, s, cs);
     wt.tiles = hi;
+    wt.cs = cs;
   } else {
     split_transpose(W, K, N, hi, hi + (size_t)N * K, s);
     wt.hi = hi;

@@ -38,8 +38,11 @@ struct Layout {
 struct TcWeights {
   const __nv_bfloat16* hi;  // split weights transposed [N][K] (hi, lo): the streamed-weight kernel (K > 256)
   const __nv_bfloat16* lo;
-  const __nv_bfloat16* tiles;   // split weights pre-tiled for the A-resident kernel (K <= 256)
+  const __nv_bfloat16* tiles;   // split weights pre-tiled for the A-resident kernel (K <= 256: FP16 hi / lo of the
+                                // column-scaled weights; the envelope kernel: BF16 hi / lo)
   const __nv_bfloat16* tiles2;  // the other spin's tiles, or nullptr
+  const float* cs;              // K <= 256: the column scales of tiles [N] (powers of two), else nullptr
+  const float* cs2;             // ... of tiles2
 };
 // Envelope derivative rows of the mixed path (k_env_tc): electrons of one spin block (ns per walker, offset
 // soff) of Wc walkers, determinant d.  C = env + d n, row stride ldc floats, nv carrier rows per electron;

@@ -19,10 +19,11 @@ __global__ void k_split_transpose(const float* __restrict__ W, int K, int N, __n
 }
 
 // hi/lo split of W[K][N] into tiles of 128 columns x 64 K: tile (j, kb) at block j * ceil(K / 64) + kb holds the
-// hi plane then the lo plane, each [8 k-groups][128 columns][8 k] (zero padding beyond N and K).  grid: every
-// column split on the grid of its largest magnitude (split_grid_bf16x2; the A-resident kernel, K <= 256), else
-// elementwise (the envelope kernel).
-__global__ void k_split_tiles(const float* __restrict__ W, int K, int N, __nv_bfloat16* __restrict__ Bt, int grid) {
+// hi plane then the lo plane, each [8 k-groups][128 columns][8 k] (zero padding beyond N and K).  With cs (the
+// A-resident kernel, K <= 256): every column scaled and split on the grid of its largest magnitude in FP16
+// (split_grid_f16x2), its scale in cs[n]; else an elementwise BF16 split (the envelope kernel).
+__global__ void k_split_tiles(const float* __restrict__ W, int K, int N, __nv_bfloat16* __restrict__ Bt,
+                              float* __restrict__ cs) {
   const int nkt = (K + 63) / 64, nnt = (N + 127) / 128;
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over (block, g, r, e)
   if (idx >= (long)nnt * nkt * 8192) return;
@@ -32,17 +33,19 @@ __global__ void k_split_tiles(const float* __restrict__ W, int K, int N, __nv_bf
   const int n = j * 128 + r, k = kb * 64 + g * 8 + e;
   const float v = (n < N && k < K) ? W[(long)k * N + n] : 0.f;
   __nv_bfloat16* base = Bt + blk * 16384;
-  if (grid && n < N) {
-    float mx = 0.f;
-    for (int q = 0; q < K; ++q) mx = fmaxf(mx, fabsf(W[(long)q * N + n]));
-    float sc, inv;
-    grid_step(mx, sc, inv);
-    if (inv != 0.f) {
-      const float h = rintf(v * inv) * sc;
-      base[w] = __float2bfloat16_rn(h);
-      base[8192 + w] = __float2bfloat16_rn(v - h);
-      return;
+  if (cs) {
+    float inv = 0.f, sc = 0.f;
+    if (n < N) {
+      float mx = 0.f;
+      for (int q = 0; q < K; ++q) mx = fmaxf(mx, fabsf(W[(long)q * N + n]));
+      grid_scales(grid_code(mx), inv, sc);
+      if (kb == 0 && g == 0 && e == 0) cs[n] = sc;
     }
+    const float x = v * inv, h = rintf(x);
+    __half* hb = reinterpret_cast<__half*>(base);
+    hb[w] = __float2half_rn(h);
+    hb[8192 + w] = __float2half_rn(x - h);
+    return;
   }
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
   base[w] = h;
@@ -64,9 +67,9 @@ __global__ void k_tile_mask(GemmP<float> p, int* mask) {
   if (threadIdx.x == 0) mask[m_tile] = up | (dn << 1);
 }
 
-cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s, bool grid) {
+cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s, float* cs) {
   const long tot = (long)((N + 127) / 128) * ((K + 63) / 64) * 8192;
-  k_split_tiles<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, Bt, grid && K <= TCP_KMAX ? 1 : 0);
+  k_split_tiles<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, Bt, K <= TCP_KMAX ? cs : nullptr);
   return cudaPeekAtLastError();
 }
 

@@ -16,6 +16,7 @@
 // mbarriers; every wait is bounded and reports FIRE_FLAG_TIMEOUT.
 #pragma once
 #include <cuda.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cstring>
@@ -53,6 +54,16 @@ __device__ __forceinline__ uint64_t tc_desc_s(uint32_t saddr, uint32_t lbo, uint
   d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
   d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
   d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// FP16 A and B (the scaled-grid split of the A-resident kernel)
+template <int BN>
+__device__ __forceinline__ uint32_t tc_idesc_f16() {
+  uint32_t d = 0;
+  d |= 1u << 4;                       // D format F32; A and B format F16 (0)
+  d |= (uint32_t)(BN >> 3) << 17;     // N / 8
+  d |= (uint32_t)(TC_BM >> 4) << 24;  // M / 16
   return d;
 }
 
@@ -132,26 +143,40 @@ __device__ __forceinline__ void cp_async_wait_tc(int n) {
   else if (n == 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
   else asm volatile("cp.async.wait_group 3;" ::: "memory");
 }
-// a = hi + lo on the grid of step sc = 2^(e - 7) of a row whose largest magnitude is in [2^e, 2^(e+1)) (inv = 1 / sc):
-// hi = sc rint(a / sc) is an integer multiple of sc of magnitude <= 256 sc (exact in BF16), a - hi is exact in FP32
-// and |a - hi| <= sc / 2; two values as BF16 pairs (first value in the low half).  Products of two such hi parts
-// are integers times sc_a sc_b below 2^16, so up to 256 of them sum exactly in an FP32 accumulator.
-__device__ __forceinline__ void split_grid_bf16x2(float a, float b, float sc, float inv, uint32_t& hi, uint32_t& lo) {
-  const float ha = rintf(a * inv) * sc, hb = rintf(b * inv) * sc;
-  const __nv_bfloat162 h = __floats2bfloat162_rn(ha, hb);
-  const __nv_bfloat162 l = __floats2bfloat162_rn(a - ha, b - hb);
+// Scaled-grid split (the A-resident kernel, K <= 256).  A row of A (or a column of W) whose largest magnitude is in
+// [2^e, 2^(e+1)) is scaled by 2^(7 - e) (exactly), so its values lie in (-256, 256); each scaled value x is split
+// into hi = rint(x), an integer of magnitude <= 256, and lo = x - hi (exact in FP32, |lo| <= 1/2), both stored in
+// FP16 (hi exactly; lo to 2^-12 of itself, i.e. to 2^-20 of the row's largest value).  Products of two hi parts are
+// integers below 2^16, so up to 256 of them sum exactly in an FP32 accumulator, whatever order and rounding the
+// tensor core's accumulation uses; the epilogue multiplies by the row's and the column's scale 2^(e - 7).
+// Exponent code of a row: ilogb of its largest magnitude clamped to >= -120, GRID_ZERO for an all-zero row,
+// GRID_NAN when the row holds an infinity or a NaN.
+constexpr int GRID_ZERO = -32768, GRID_NAN = 32767;
+__device__ __forceinline__ int grid_code(float mx) {
+  if (mx == 0.f) return GRID_ZERO;
+  if (!(mx <= 3.4e38f)) return GRID_NAN;
+  return max(ilogbf(mx), -120);
+}
+// (inverse scale applied to the values, scale the epilogue applies) of an exponent code
+__device__ __forceinline__ void grid_scales(int code, float& inv, float& sc) {
+  if (code == GRID_ZERO) {
+    inv = 0.f;
+    sc = 0.f;
+  } else if (code == GRID_NAN) {
+    inv = 0.f;
+    sc = __int_as_float(0x7fc00000);
+  } else {
+    inv = ldexpf(1.f, 7 - code);
+    sc = ldexpf(1.f, code - 7);
+  }
+}
+__device__ __forceinline__ void split_grid_f16x2(float a, float b, float inv, uint32_t& hi, uint32_t& lo) {
+  const float xa = a * inv, xb = b * inv;
+  const float ha = rintf(xa), hb = rintf(xb);
+  const __half2 h = __floats2half2_rn(ha, hb);
+  const __half2 l = __floats2half2_rn(xa - ha, xb - hb);
   hi = *reinterpret_cast<const uint32_t*>(&h);
   lo = *reinterpret_cast<const uint32_t*>(&l);
-}
-// the grid step of a row (or column) of largest magnitude mx: (sc, inv), or (0, 0) when mx is 0 or not finite
-__device__ __forceinline__ void grid_step(float mx, float& sc, float& inv) {
-  if (mx > 0.f && mx <= 3.0e38f) {
-    const int e = ilogbf(mx);
-    sc = ldexpf(1.f, e - 7);
-    inv = ldexpf(1.f, 7 - e);
-  } else {
-    sc = inv = 0.f;
-  }
 }
 // a = hi + lo for two values: BF16 pairs (first value in the low half)
 __device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
@@ -287,7 +312,8 @@ __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int nod
 template <int MODE>
 __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows, int m0, int n0, uint32_t tacc,
                                                  int spin_filter, int tma, const CUtensorMap* tmC, float* stg,
-                                                 int& nst, int warp, int lane, bool two_acc = false) {
+                                                 int& nst, int warp, int lane, bool two_acc = false,
+                                                 float row_sc = 1.f, const float* col_sc = nullptr) {
   const int quad = warp & 3, half = warp >> 2;
   const int row = m0 + quad * 32 + lane;
   const bool valid = row < rows;
@@ -311,6 +337,13 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
       tmem_ld16(base + (uint32_t)(TCP_BN + c0), v2);
 #pragma unroll
       for (int k = 0; k < 16; ++k) v[k] += v2[k];
+    }
+    if (col_sc) {  // undo the scaled-grid split: row scale times column scale (powers of two: exact)
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const int col = n0 + c0 + k;
+        v[k] *= row_sc * (col < p.N ? col_sc[col] : 0.f);
+      }
     }
     const int spin = spin_filter < 0 ? 0 : spin_filter;
     const bool full = n0 + c0 + 15 < p.N;
@@ -621,38 +654,43 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcs(GemmP<float> p, con
 // apart, 8-row groups 128 bytes apart).  A is a ring of 64-deep blocks: block kb is released once the MMAs of
 // the last column tile have read it, so the next row tile's conversion overlaps the current tile's tail.
 // Warp roles: 0-7 epilogue, 8-11 A converters, 12 (lane 0) MMA issuer, 13 (lane 0) weight loader.
-// Splitting: every row of A (and, at preparation, every column of the weights) is split on the grid of its own
-// largest magnitude (split_grid_bf16x2), so that the hi x hi products of a row and a column are integer multiples
-// of one step and their sum over K <= 256 is exact in FP32 whatever order and rounding the tensor core's
-// accumulation uses; they accumulate in one TMEM accumulator and the cross terms a_hi w_lo + a_lo w_hi in a second
-// one (~2^-8 of the result, so their accumulation rounding is ~2^-32 of it); the epilogue adds the two.  The
-// a_lo w_lo term (~2^-18 of a product, unbiased) is left out.
+// Splitting: every row of A (and, at preparation, every column of the weights) is scaled and split on the grid of
+// its own largest magnitude (split_grid_f16x2, FP16 operands), so that the hi x hi products of a row and a column are
+// integers and their sum over K <= 256 is exact in FP32 whatever order and rounding the tensor core's accumulation
+// uses; they accumulate in one TMEM accumulator and the cross terms a_hi w_lo + a_lo w_hi in a second one (~2^-8 of
+// the result, so their accumulation rounding is ~2^-32 of it); the epilogue adds the two and applies the row and
+// column scales.  The a_lo w_lo term (< 2^-18 of a product, unbiased) is left out; the per-element error is ~2^-20
+// of the row's (column's) largest value.
 constexpr int TCA_THREADS = 448, TCA_KB = 4, TCA_BSTAGES = 2;
 struct TcaCfg {
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;  // one BF16 plane of a 128 x 64 block
   static constexpr int A_BLOCK = 2 * A_BYTES;        // hi + lo
   static constexpr int B_BLOCK = 2 * TCP_BN * TC_BK * 2;  // one tiled weight block (hi + lo)
   static constexpr int STG_BYTES = TcCfg::STG_BYTES;
-  static constexpr int RMAX_BYTES = 2 * 2 * TC_BM * 4;  // row maxima: [row tile parity][k half][128 rows]
+  // row exponent codes (int16): the converters' halves [row tile parity][k half][128 rows], then the rows' codes for
+  // the epilogue [row tile mod 4][128 rows]
+  static constexpr int RMAX_BYTES = 2 * 2 * TC_BM * 2 + 4 * TC_BM * 2;
   static constexpr int TOTAL = TCA_KB * A_BLOCK + TCA_BSTAGES * B_BLOCK + STG_BYTES + RMAX_BYTES + 256;
 };
 struct TcaBar {
   uint64_t afull[TCA_KB], aempty[TCA_KB], bfull[TCA_BSTAGES], bempty[TCA_BSTAGES], tfull[2], tempty[2];
-  uint64_t rmax;  // the converters' row maxima of a row tile are complete
+  uint64_t rmax;      // the converters' row maxima of a row tile are complete
+  uint64_t rsfull[4];  // the row codes of row tile t (slot t mod 4) are written
   uint32_t tmem;
   int abort;
 };
 
 // Bt: tiled weights [ceil(N / 128)][ceil(K / 64)] blocks of TcaCfg::B_BLOCK bytes
 template <int MODE>
-__global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, const __nv_bfloat16* Bt, int spin_filter,
-                                                            const int* tile_mask, int32_t* status,
+__global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, const __nv_bfloat16* Bt, const float* col_sc,
+                                                            int spin_filter, const int* tile_mask, int32_t* status,
                                                             const __grid_constant__ CUtensorMap tmC, int tma) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   unsigned char* ares = tc_smem;                                   // [kb][hi, lo][128 x 64], LBO 128, SBO 1024
   unsigned char* bst = tc_smem + TCA_KB * TcaCfg::A_BLOCK;         // [stage][hi, lo][8 k-groups][128 rows][16 B]
   float* stg = reinterpret_cast<float*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK);
-  float* rpart = reinterpret_cast<float*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK + TcaCfg::STG_BYTES);
+  int16_t* rpart = reinterpret_cast<int16_t*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK + TcaCfg::STG_BYTES);
+  int16_t* rcode = rpart + 2 * 2 * TC_BM;
   TcaBar* bars = reinterpret_cast<TcaBar*>(bst + TCA_BSTAGES * TcaCfg::B_BLOCK + TcaCfg::STG_BYTES +
                                            TcaCfg::RMAX_BYTES);
   volatile int* abort = &bars->abort;
@@ -679,6 +717,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
       mbar_init(smem_u32(&bars->tempty[b]), 256);
     }
     mbar_init(smem_u32(&bars->rmax), 128);
+    for (int q = 0; q < 4; ++q) mbar_init(smem_u32(&bars->rsfull[q]), 128);
     bars->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -728,10 +767,10 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
         ++issued;
       }
       if (issued < nk) break;  // aborted
-      // the grid of every row: its largest magnitude over K.  A row's k-groups belong to lanes r8, r8 + 8, r8 + 16,
-      // r8 + 24 of two warps (k halves lw & 1); each warp writes its half's maxima, and the converters meet on an
-      // mbarrier (bounded wait) before reading the other half's.  The buffer alternates between row tiles: a warp
-      // writing row tile t + 2 has passed the barrier of t + 1, so every reader of t is done.
+      // the grid of every row: the exponent of its largest magnitude over K.  A row's k-groups belong to lanes r8,
+      // r8 + 8, r8 + 16, r8 + 24 of two warps (k halves lw & 1); each warp writes its half's code, and the converters
+      // meet on an mbarrier (bounded wait) before reading the other half's.  The buffer alternates between row tiles:
+      // a warp writing row tile t + 2 has passed the barrier of t + 1, so every reader of t is done.
       cp_async_wait_tc(0);
       float mx[8];
 #pragma unroll
@@ -749,21 +788,28 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
                                        fmaxf(fmaxf(fabsf(y.x), fabsf(y.y)), fmaxf(fabsf(y.z), fabsf(y.w)))));
         }
       }
-      float* part = rpart + (ua & 1) * 2 * TC_BM;
+      int16_t* part = rpart + (ua & 1) * 2 * TC_BM;
 #pragma unroll
       for (int it = 0; it < 8; ++it) {
         mx[it] = fmaxf(mx[it], __shfl_xor_sync(0xffffffffu, mx[it], 8));
         mx[it] = fmaxf(mx[it], __shfl_xor_sync(0xffffffffu, mx[it], 16));
-        if (kq8 == 0) part[(lw & 1) * TC_BM + ((lw + 4 * it) >> 1) * 8 + r8] = mx[it];
+        if (kq8 == 0) part[(lw & 1) * TC_BM + ((lw + 4 * it) >> 1) * 8 + r8] = (int16_t)grid_code(mx[it]);
       }
       tc_arrive(&bars->rmax);
       if (!tc_wait(&bars->rmax, (uint32_t)(ua & 1), abort)) break;
-      float sc[8], inv[8];
+      // the rows' codes for the epilogue (slot ua mod 4; the epilogue of row tile ua - 4 finished before the MMAs of
+      // row tile ua - 1, whose completion released these A blocks), published by an mbarrier of their own
+      int16_t* codes = rcode + (ua & 3) * TC_BM;
+      float inv[8];
 #pragma unroll
       for (int it = 0; it < 8; ++it) {
         const int r = ((lw + 4 * it) >> 1) * 8 + r8;
-        grid_step(fmaxf(part[r], part[TC_BM + r]), sc[it], inv[it]);
+        const int code = max((int)part[r], (int)part[TC_BM + r]);
+        float sc;
+        grid_scales(code, inv[it], sc);
+        if (kq8 == 0 && (lw & 1) == 0) codes[r] = (int16_t)code;
       }
+      tc_arrive(&bars->rsfull[ua & 3]);
       for (int kb = 0; kb < nk; ++kb) {
         unsigned char* a_hi = ares + kb * TcaCfg::A_BLOCK;
         unsigned char* a_lo = a_hi + TcaCfg::A_BYTES;
@@ -775,17 +821,10 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
           const float4 x = *reinterpret_cast<const float4*>(a_hi + off);
           const float4 y = *reinterpret_cast<const float4*>(a_lo + off);
           uint4 hi, lo;
-          if (inv[it] != 0.f) {
-            split_grid_bf16x2(x.x, x.y, sc[it], inv[it], hi.x, lo.x);
-            split_grid_bf16x2(x.z, x.w, sc[it], inv[it], hi.y, lo.y);
-            split_grid_bf16x2(y.x, y.y, sc[it], inv[it], hi.z, lo.z);
-            split_grid_bf16x2(y.z, y.w, sc[it], inv[it], hi.w, lo.w);
-          } else {  // an all-zero (or non-finite) row
-            split_bf16x2(x.x, x.y, hi.x, lo.x);
-            split_bf16x2(x.z, x.w, hi.y, lo.y);
-            split_bf16x2(y.x, y.y, hi.z, lo.z);
-            split_bf16x2(y.z, y.w, hi.w, lo.w);
-          }
+          split_grid_f16x2(x.x, x.y, inv[it], hi.x, lo.x);
+          split_grid_f16x2(x.z, x.w, inv[it], hi.y, lo.y);
+          split_grid_f16x2(y.x, y.y, inv[it], hi.z, lo.z);
+          split_grid_f16x2(y.z, y.w, inv[it], hi.w, lo.w);
           *reinterpret_cast<uint4*>(a_hi + off) = hi;
           *reinterpret_cast<uint4*>(a_lo + off) = lo;
         }
@@ -816,7 +855,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
   } else if (warp == 12) {
     // ------------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = tc_idesc<TCP_BN>();
+      const uint32_t idesc = tc_idesc_f16<TCP_BN>();
       const uint32_t a0 = smem_u32(ares), b0 = smem_u32(bst);
       long ua = 0, bc = 0, uc = 0;
       for (int m = blockIdx.x; m < mt && !*abort; m += gridDim.x) {
@@ -855,17 +894,22 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
     }
   } else {
     // ------------------------------------------------------------------ epilogue (warps 0-7, 256 threads)
-    long uc = 0;
+    long uc = 0, ue = 0;
     int nst = 0;
     for (int m = blockIdx.x; m < mt && !*abort; m += gridDim.x) {
       if (skip(m)) continue;
       const int m0 = m * TC_BM;
+      // this thread's row scale (the converters' code of row m0 + 32 (warp % 4) + lane)
+      if (!tc_wait(&bars->rsfull[ue & 3], (uint32_t)((ue >> 2) & 1), abort)) break;
+      float inv_unused, row_sc;
+      grid_scales((int)rcode[(ue & 3) * TC_BM + (warp & 3) * 32 + lane], inv_unused, row_sc);
+      ++ue;
       for (int j = 0; j < nt && !*abort; ++j) {
         const int b = (int)(uc & 1);
         if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
         tc_fence_after();
         tc_epilogue_tile<MODE>(p, rows, m0, j * TCP_BN, tmem + (uint32_t)(b * 2 * TCP_BN), spin_filter, tma, &tmC,
-                               stg, nst, warp, lane, true);
+                               stg, nst, warp, lane, true, row_sc, col_sc);
         tc_fence_before();
         tc_arrive(&bars->tempty[b]);
         ++uc;
@@ -930,8 +974,8 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
   CUtensorMap tmC;
   std::memset(&tmC, 0, sizeof(tmC));
   const int tma = tc_c_map(p, &tmC) ? 1 : 0;
-  if (p.K <= TCP_KMAX) {  // A-resident kernel with pre-tiled weights
-    if (!wt.tiles) return cudaErrorInvalidValue;
+  if (p.K <= TCP_KMAX) {  // A-resident kernel with pre-tiled, column-scaled weights
+    if (!wt.tiles || !wt.cs || (wt.tiles2 && !wt.cs2)) return cudaErrorInvalidValue;
     constexpr int smem = TcaCfg::TOTAL;
     cudaError_t e = cudaFuncSetAttribute(k_gemm_tca<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
@@ -941,10 +985,10 @@ inline cudaError_t launch_gemm_tc(const GemmP<float>& p, const TcWeights& wt, in
     if (wt.tiles2) {
       if (!mask_buf) return cudaErrorInvalidValue;
       k_tile_mask<<<(unsigned)mt, TC_BM, 0, s>>>(p, mask_buf);
-      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles, 0, mask_buf, status, tmC, tma);
-      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles2, 1, mask_buf, status, tmC, tma);
+      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles, wt.cs, 0, mask_buf, status, tmC, tma);
+      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles2, wt.cs2, 1, mask_buf, status, tmC, tma);
     } else {
-      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles, -1, nullptr, status, tmC, tma);
+      k_gemm_tca<MODE><<<grid, TCA_THREADS, smem, s>>>(p, wt.tiles, wt.cs, -1, nullptr, status, tmC, tma);
     }
     return cudaPeekAtLastError();
   }
