@@ -284,18 +284,20 @@ inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
 
 // ----------------------------------------------------------------------------- compensated value contraction
 // FP32 and mixed paths: the value planes (one row per node) feed the orbital matrices, whose inverse amplifies
-// their rounding by the condition number in the derivatives of log det.  k_gemm_comp computes them with
-// compensated dot products (Ogita, Rump and Oishi's Dot2: every product split exactly with an FMA, every partial
-// sum with TwoSum, the errors gathered in a second accumulator), i.e. as if in twice the working precision and
-// then rounded once; the orbital-matrix values and the envelope values they are made of also leave the kernel as
-// unevaluated hi + lo float pairs, so that the double-FP32 elimination sees them to ~2^-48.
+// their rounding by the condition number in the derivatives of log det.  k_gemm_comp sums every dot product in
+// chunks of CCH terms: each chunk is one fused multiply-add chain (no product is rounded on its own), and the chunk
+// sums are added to a hi + lo pair with TwoSum (Knuth), so that only the short chains round; the result is
+// rounded once.  Against a plain FP32 dot product over K = 256 this cuts the rounding error of random-signed terms
+// ~7x (the chains' error grows with sqrt(CCH), not with the length of the whole sum) at ~2.75 operations per term.
+// The orbital-matrix values and the envelope values they are made of also leave the kernel as unevaluated hi + lo
+// float pairs, so that the double-FP32 elimination sees them to ~2^-48.
 //   COMP_PLAIN  C = a.b + bias (bias on rows with row % bias_period == 0)
 //   COMP_SILU   C = silu(z), z = a.b + bias; with aux0 set also silu'(z) (aux0) and silu''(z) (aux2)
 //   COMP_ENV    envelope value rows (EPI_ENV's row map, env_nv = 1): hi into C, lo into C_lo [g][ld_lo]
 //   COMP_ORB    orbital values (EPI_ORB_X): raw = a.b + bias (per-spin weights and bias), rawx (aux0) = raw,
 //               C + C_lo = raw (env + env_lo) with env = aux1 [row * env_nv * ld_aux], env_lo [row * ld_lo]
 enum CompMode { COMP_PLAIN = 0, COMP_SILU, COMP_ENV, COMP_ORB };
-constexpr int CBM = 64, CBN = 64, CBK = 16, CTHREADS = 256;
+constexpr int CBM = 64, CBN = 64, CBK = 16, CCH = 4, CTHREADS = 256;
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
@@ -303,11 +305,13 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// 64 x 64 outputs per CTA, 4 x 4 per thread (rows 4 ty.., columns 4 tx..); A and B tiles of 16 k staged in shared
+// memory (A transposed), the next tile prefetched into registers while the current one is summed.
 template <int MODE>
 __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* __restrict__ C_lo,
                                                         const float* __restrict__ env_lo, long ld_lo) {
-  __shared__ __align__(16) float As[CBK][CBM + 4];
-  __shared__ __align__(16) float Bs[CBK][CBN];
+  __shared__ __align__(16) float As[2][CBK][CBM];
+  __shared__ __align__(16) float Bs[2][CBK][CBN];
   const int rows = p.M;
   const int m0 = blockIdx.y * CBM, n0 = blockIdx.x * CBN;
   if (m0 >= rows) return;
@@ -323,90 +327,123 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
     first_spin = up ? 0 : 1;
     passes = up + dn;
   }
+  const int ar = tid >> 2, aq = (tid & 3) * 4;   // A: row ar, k aq..aq+3 of the tile
+  const int bk = tid >> 4, bc = (tid & 15) * 4;  // B: k bk, columns bc..bc+3
+  const bool va = p.lda % 4 == 0 && (reinterpret_cast<uintptr_t>(p.A) & 15) == 0;
   for (int pass = 0; pass < passes; ++pass) {
     const int spin = first_spin + pass;
     const float* Bp = spin == 0 ? p.B : p.B2;
+    const bool vb = p.ldb % 4 == 0 && (reinterpret_cast<uintptr_t>(Bp) & 15) == 0;
+    float ra[4], rb[4];
+    auto load = [&](int k0) {
+      const int gr = m0 + ar, gk = k0 + aq;
+      if (va && gr < rows && gk + 3 < p.K) {
+        const float4 q = *reinterpret_cast<const float4*>(p.A + (long)gr * p.lda + gk);
+        ra[0] = q.x; ra[1] = q.y; ra[2] = q.z; ra[3] = q.w;
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) ra[u] = (gr < rows && gk + u < p.K) ? p.A[(long)gr * p.lda + gk + u] : 0.f;
+      }
+      const int gk2 = k0 + bk, gc = n0 + bc;
+      if (vb && gk2 < p.K && gc + 3 < p.N) {
+        const float4 q = *reinterpret_cast<const float4*>(Bp + (long)gk2 * p.ldb + gc);
+        rb[0] = q.x; rb[1] = q.y; rb[2] = q.z; rb[3] = q.w;
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) rb[u] = (gk2 < p.K && gc + u < p.N) ? Bp[(long)gk2 * p.ldb + gc + u] : 0.f;
+      }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) As[buf][aq + u][ar] = ra[u];
+      *reinterpret_cast<float4*>(&Bs[buf][bk][bc]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
+    };
     float hi[4][4], lo[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.f;
+    load(0);
+    store(0);
+    __syncthreads();
+    int buf = 0;
     for (int k0 = 0; k0 < p.K; k0 += CBK) {
-      // A tile 64 x 16 and B tile 16 x 64: four elements per thread each
+      const bool more = k0 + CBK < p.K;
+      if (more) load(k0 + CBK);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int e = tid + u * CTHREADS;
-        const int ar = e >> 4, ak = e & 15;
-        const int gr = m0 + ar, gk = k0 + ak;
-        As[ak][ar] = (gr < rows && gk < p.K) ? p.A[(long)gr * p.lda + gk] : 0.f;
-        const int bk = e >> 6, bc = e & 63;
-        const int gk2 = k0 + bk, gc = n0 + bc;
-        Bs[bk][bc] = (gk2 < p.K && gc < p.N) ? Bp[(long)gk2 * p.ldb + gc] : 0.f;
-      }
-      __syncthreads();
-#pragma unroll 4
-      for (int kk = 0; kk < CBK; ++kk) {
-        float a[4], b[4];
+      for (int c = 0; c < CBK; c += CCH) {
+        float t[4][4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          a[i] = As[kk][ty + 16 * i];
-          b[i] = Bs[kk][tx + 16 * i];
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) t[i][j] = 0.f;
+#pragma unroll
+        for (int kk = c; kk < c + CCH; ++kk) {
+          const float4 a = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+          const float4 b = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+          const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) t[i][j] = fmaf(av[i], bv[j], t[i][j]);
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const float pr = a[i] * b[j];
-            const float pe = fmaf(a[i], b[j], -pr);
-            float s, e;
-            two_sum(hi[i][j], pr, s, e);
-            hi[i][j] = s;
-            lo[i][j] += e + pe;
+            float s2, e;
+            two_sum(hi[i][j], t[i][j], s2, e);
+            hi[i][j] = s2;
+            lo[i][j] += e;
           }
       }
-      __syncthreads();
+      if (more) {
+        store(buf ^ 1);
+        __syncthreads();
+        buf ^= 1;
+      }
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const int row = m0 + ty + 16 * i;
+      const int row = m0 + ty * 4 + i;
       if (row >= rows) continue;
       if (p.B2 && (((row % p.n_el) < p.n_up) ? 0 : 1) != spin) continue;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const int col = n0 + tx + 16 * j;
+        const int col = n0 + tx * 4 + j;
         if (col >= p.N) continue;
         float h = hi[i][j], l = lo[i][j];
         if (MODE == COMP_PLAIN || MODE == COMP_SILU || MODE == COMP_ORB) {
           const float* bias = (MODE == COMP_ORB && spin == 1) ? p.bias2 : p.bias;
           const bool has_b = bias && (MODE != COMP_PLAIN || (p.bias_period > 0 && row % p.bias_period == 0));
           if (has_b) {
-            float s, e;
-            two_sum(h, bias[col], s, e);
-            h = s;
+            float s2, e;
+            two_sum(h, bias[col], s2, e);
+            h = s2;
             l += e;
           }
         }
-        float s, e;  // normalised pair: s = fl(h + l)
-        two_sum(h, l, s, e);
+        float s2, e;  // normalised pair: s2 = fl(h + l)
+        two_sum(h, l, s2, e);
         if (MODE == COMP_PLAIN) {
-          p.C[(long)row * p.ldc + col] = s;
+          p.C[(long)row * p.ldc + col] = s2;
         } else if (MODE == COMP_SILU) {
-          p.C[(long)row * p.ldc + col] = silu(s);
+          p.C[(long)row * p.ldc + col] = silu(s2);
           if (p.aux0) {
             float y, d1, d2;
-            silu3(s, y, d1, d2);
+            silu3(s2, y, d1, d2);
             p.aux0[(long)row * p.ld_aux + col] = d1;
             p.aux2[(long)row * p.ld_aux + col] = d2;
           }
         } else if (MODE == COMP_ENV) {
           const int g = (row / p.env_ns) * p.n_el + p.env_soff + row % p.env_ns;
-          p.C[(long)g * p.ldc + col] = s;
+          p.C[(long)g * p.ldc + col] = s2;
           C_lo[(long)g * ld_lo + col] = e;
         } else {  // COMP_ORB
-          p.aux0[(long)row * p.ld_aux + col] = s;
+          p.aux0[(long)row * p.ld_aux + col] = s2;
           const float eh = p.aux1[(long)row * p.env_nv * p.ld_aux + col], el = env_lo[(long)row * ld_lo + col];
-          const float ph = s * eh;
-          const float pl = fmaf(s, eh, -ph) + (s * el + e * eh);
+          const float ph = s2 * eh;
+          const float pl = fmaf(s2, eh, -ph) + (s2 * el + e * eh);
           float oh, ol;
           two_sum(ph, pl, oh, ol);
           p.C[(long)row * p.ldc + col] = oh;
