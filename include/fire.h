@@ -73,8 +73,8 @@ typedef enum {
                           (48-bit significand) */
   FIRE_PREC_MIXED = 1, /* derivative planes of the contractions on tensor cores: K <= 256 with every row of A and
                           column of W scaled and split on the grid of its largest value into FP16 hi + lo (the
-                          hi x hi sums exact in one FP32 accumulator, the cross terms in a second; ~2^-20 of a row's
-                          largest value per element), K > 256 (the envelope rows) in split BF16 (three products per
+                          hi x hi sums exact in one FP32 accumulator, the three other products in a second, four
+                          MMAs per product; ~2^-20 of a row's largest value per element), K > 256 (the envelope rows) in split BF16 (three products per
                           FP32 product); value planes, orbital LU and inverse as in FIRE_PREC_FP32 */
   FIRE_PREC_FP64 = 2   /* everything in FP64 (validation build of the same kernels) */
 } fire_precision;
@@ -104,7 +104,7 @@ typedef struct {
  * and dominate the error of a batch mean, the walkers above FIRE_REFINE_RATIO |E_loc| (near a node) the relative
  * error of their own E_loc. */
 #define FIRE_REFINE_RATIO 100.0f
-#define FIRE_REFINE_KAPPA 1.0e5f
+#define FIRE_REFINE_KAPPA 1.0e6f
 #define FIRE_REFINE_KS 3.0e4f
 
 /* Parameter slots of the flat parameter blob (float32), in blob order.  Shapes with
@@ -391,7 +391,7 @@ fire_status fire_profile_report(char* buf, size_t len);
 
 /* The mixed-precision tensor-core contraction alone: C[M, N] = A[M, K] W[K, N] (all float32, row-major,
  * device), on tcgen05.  K <= 256: rows of A and columns of W scaled and split on the grid of their largest
- * value into FP16 hi + lo, the hi x hi sums exact in one FP32 accumulator and the two cross products in a second;
+ * value into FP16 hi + lo, the hi x hi sums exact in one FP32 accumulator and the three other products in a second;
  * K > 256: elementwise split BF16, three BF16 products per element pair, one FP32 accumulator.  workspace: the
  * split weights, 32768 * ceil(N / 128) * ceil(K / 64) + 4 * N bytes for K <= 256 (tiles, column scales),
  * else 4 * N * K bytes.  K % 8 == 0, N % 4 == 0

@@ -284,11 +284,11 @@ inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
 
 // ----------------------------------------------------------------------------- compensated value contraction
 // FP32 and mixed paths: the value planes (one row per node) feed the orbital matrices, whose inverse amplifies
-// their rounding by the condition number in the derivatives of log det.  k_gemm_comp sums every dot product in
-// chunks of CCH terms: each chunk is one fused multiply-add chain (no product is rounded on its own), and the chunk
-// sums are added to a hi + lo pair with TwoSum (Knuth), so that only the short chains round; the result is
-// rounded once.  Against a plain FP32 dot product over K = 256 this cuts the rounding error of random-signed terms
-// ~7x (the chains' error grows with sqrt(CCH), not with the length of the whole sum) at ~2.75 operations per term.
+// their rounding by the condition number in the derivatives of log det.  k_gemm_comp computes them with
+// compensated dot products (Ogita, Rump and Oishi's Dot2: every product split exactly with an FMA, every partial
+// sum with TwoSum (Knuth), the errors gathered in a second accumulator), i.e. as if in twice the working precision
+// and then rounded once: the error is ~2^-24 of the result even where the terms cancel (the orbital values are
+// small differences of large products), which a shorter FMA chain per partial sum does not give.
 // The orbital-matrix values and the envelope values they are made of also leave the kernel as unevaluated hi + lo
 // float pairs, so that the double-FP32 elimination sees them to ~2^-48.
 //   COMP_PLAIN  C = a.b + bias (bias on rows with row % bias_period == 0)
@@ -297,7 +297,7 @@ inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
 //   COMP_ORB    orbital values (EPI_ORB_X): raw = a.b + bias (per-spin weights and bias), rawx (aux0) = raw,
 //               C + C_lo = raw (env + env_lo) with env = aux1 [row * env_nv * ld_aux], env_lo [row * ld_lo]
 enum CompMode { COMP_PLAIN = 0, COMP_SILU, COMP_ENV, COMP_ORB };
-constexpr int CBM = 64, CBN = 64, CBK = 16, CCH = 4, CTHREADS = 256;
+constexpr int CBM = 64, CBN = 64, CBK = 16, CTHREADS = 256;
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
@@ -370,31 +370,21 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
     for (int k0 = 0; k0 < p.K; k0 += CBK) {
       const bool more = k0 + CBK < p.K;
       if (more) load(k0 + CBK);
-#pragma unroll
-      for (int c = 0; c < CBK; c += CCH) {
-        float t[4][4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) t[i][j] = 0.f;
-#pragma unroll
-        for (int kk = c; kk < c + CCH; ++kk) {
-          const float4 a = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
-          const float4 b = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
-          const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) t[i][j] = fmaf(av[i], bv[j], t[i][j]);
-        }
+#pragma unroll 4
+      for (int kk = 0; kk < CBK; ++kk) {
+        const float4 a = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+        const float4 b = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
+            const float pr = av[i] * bv[j];
+            const float pe = fmaf(av[i], bv[j], -pr);
             float s2, e;
-            two_sum(hi[i][j], t[i][j], s2, e);
+            two_sum(hi[i][j], pr, s2, e);
             hi[i][j] = s2;
-            lo[i][j] += e;
+            lo[i][j] += e + pe;
           }
       }
       if (more) {

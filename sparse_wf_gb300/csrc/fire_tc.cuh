@@ -657,10 +657,10 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_gemm_tcs(GemmP<float> p, con
 // Splitting: every row of A (and, at preparation, every column of the weights) is scaled and split on the grid of
 // its own largest magnitude (split_grid_f16x2, FP16 operands), so that the hi x hi products of a row and a column are
 // integers and their sum over K <= 256 is exact in FP32 whatever order and rounding the tensor core's accumulation
-// uses; they accumulate in one TMEM accumulator and the cross terms a_hi w_lo + a_lo w_hi in a second one (~2^-8 of
-// the result, so their accumulation rounding is ~2^-32 of it); the epilogue adds the two and applies the row and
-// column scales.  The a_lo w_lo term (< 2^-18 of a product, unbiased) is left out; the per-element error is ~2^-20
-// of the row's (column's) largest value.
+// uses; they accumulate in one TMEM accumulator and the terms a_hi w_lo + a_lo w_hi + a_lo w_lo in a second one (~2^-8
+// of the result, so their accumulation rounding is ~2^-32 of it); the epilogue adds the two and applies the row and
+// column scales.  (a_lo w_lo is kept: on the grid lo reaches half a step, 2^-8 of the row's largest value, so the
+// term is ~2^-16 of a product.)  The per-element error is ~2^-20 of the row's (column's) largest value.
 constexpr int TCA_THREADS = 448, TCA_KB = 4, TCA_BSTAGES = 2;
 struct TcaCfg {
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;  // one BF16 plane of a 128 x 64 block
@@ -881,6 +881,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1) k_gemm_tca(GemmP<float> p, con
               tc_mma(acc_t, dah, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
               tc_mma(acc_t + TCP_BN, dah, dbl, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
               tc_mma(acc_t + TCP_BN, dal, dbh, idesc, 1u);
+              tc_mma(acc_t + TCP_BN, dal, dbl, idesc, 1u);
             }
             tc_commit(smem_u32(&bars->bempty[s2]));
             if (j == nt - 1) tc_commit(smem_u32(&bars->aempty[kb]));

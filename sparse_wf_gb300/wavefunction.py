@@ -110,7 +110,7 @@ class FireWaveFunction:
         # reports (the defaults of fire.h)
         self.refine = precision != "fp64"
         self.refine_ratio = 100.0
-        self.refine_kappa = 1.0e5
+        self.refine_kappa = 1.0e6
         self.refine_ks = 3.0e4
         self._refine_cap = 0
         self.last_refined = 0
