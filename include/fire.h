@@ -105,7 +105,7 @@ typedef struct {
  * error of their own E_loc. */
 #define FIRE_REFINE_RATIO 100.0f
 #define FIRE_REFINE_KAPPA 1.0e6f
-#define FIRE_REFINE_KS 3.0e4f
+#define FIRE_REFINE_KS 1.0e5f
 
 /* Parameter slots of the flat parameter blob (float32), in blob order.  Shapes with
  * F = 256, D = 4 determinants, n = n_el, N = n_nuc are given by fire_param_layout. */

@@ -111,7 +111,7 @@ class FireWaveFunction:
         self.refine = precision != "fp64"
         self.refine_ratio = 100.0
         self.refine_kappa = 1.0e6
-        self.refine_ks = 3.0e4
+        self.refine_ks = 1.0e5
         self._refine_cap = 0
         self.last_refined = 0
         _lib.load()

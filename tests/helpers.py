@@ -95,7 +95,8 @@ def check_eloc_contract(precision, wf, got, eloc, ks, epot, refined, lap=None, l
     kinetic terms, and for a walker whose kinetic energy balances its potential energy (E_loc crosses zero) the
     kinetic and potential terms.  Its error is held relative to the magnitude of those terms,
     S = ks + |V| with ks = (|lap log psi| + |grad log psi|^2) / 2 (the reference's own float32 energy test allows 1e-2
-    of |E_kin|): |dE_loc| <= tol S on every walker, |d lap| <= 2 tol S and |d grad| <= tol sqrt(2 S).  Every walker
+    of |E_kin|): |dE_loc| <= tol S on every walker, and on every walker away from a node (ks <= 8 |E_loc|)
+    |d lap| <= 2 tol S and |d grad| <= tol sqrt(2 S).  Every walker
     whose ks exceeds 1.05 refine_ratio |E_loc| must have gone through the
     device's FP64 refinement pass, and so must every walker whose ks exceeds 1.05 refine_ks.  Returns the fraction of
     walkers within tol |E_loc|."""
@@ -106,10 +107,14 @@ def check_eloc_contract(precision, wf, got, eloc, ks, epot, refined, lap=None, l
     must = (ks > 1.05 * wf.refine_ratio * np.abs(eloc)) | (ks > 1.05 * wf.refine_ks)
     assert np.all(refined[must]), (ks / np.abs(eloc), refined)
     assert np.all(err <= tol * S), (np.max(err / S), int(np.argmax(err / S)), int(refined.sum()))
+    # the forward Laplacian's two outputs on their own, where they do not cancel: near a node lap log psi and
+    # |grad log psi|^2 both grow like 1 / d^2 with the distance d to the node while their sum stays finite, and a
+    # rounding of psi that moves the node moves them in opposite directions
+    calm = ks <= 8 * np.abs(eloc)
     if lap is not None:
         dl = np.abs(np.asarray(lap, np.float64) - lap_ref)
-        assert np.all(dl <= 2 * tol * S), np.max(dl / S)
+        assert np.all(dl[calm] <= 2 * tol * S[calm]), np.max(dl[calm] / S[calm])
     if grad is not None:
         dg = np.linalg.norm((np.asarray(grad, np.float64) - grad_ref).reshape(len(S), -1), axis=1)
-        assert np.all(dg <= tol * np.sqrt(2 * S)), np.max(dg / np.sqrt(2 * S))
+        assert np.all(dg[calm] <= tol * np.sqrt(2 * S[calm])), np.max(dg[calm] / np.sqrt(2 * S[calm]))
     return float(np.mean(err <= tol * np.abs(eloc)))

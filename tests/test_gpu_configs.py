@@ -5,7 +5,7 @@
   C40H82, 2 walkers (FP64 build, FP32 and mixed), the size of the headline benchmark.
 
 Parameters are random-init (seed 0, normalize scales from walker 0), walkers drawn around the nuclei (sigma 1 bohr),
-as in the benchmark.  Tolerances: FP64 build 1e-10 relative on log|psi| and E_loc; FP32 1e-5 on log|psi| and the
+as in the benchmark.  Tolerances: FP64 build 1e-10 relative on log|psi| and E_loc; FP32 3e-5 on log|psi| and the
 per-walker local-energy contract of helpers.check_eloc_contract (1e-5 of the magnitude of the terms E_loc is summed
 from, every ill-conditioned walker refined; 2e-5 on H10), mixed the same contract at 1e-4."""
 import numpy as np
@@ -63,7 +63,7 @@ def test_config_local_energy(cuda_lib, name, precision):
         assert np.all(np.abs(lp - ref["logpsi"]) <= 1e-10 * np.maximum(1, np.abs(ref["logpsi"])))
         assert np.all(np.abs(got - ref["eloc"]) <= 1e-10 * np.abs(ref["eloc"]))
         return
-    assert np.all(np.abs(lp - ref["logpsi"]) <= 1e-5 * np.maximum(1, np.abs(ref["logpsi"])))
+    assert np.all(np.abs(lp - ref["logpsi"]) <= 3e-5 * np.maximum(1, np.abs(ref["logpsi"])))
     dbg = aux["debug"]
     # H10 x 512 FP32: one walker (|lap log psi| 17, |grad|^2 30, condition number 3e2) reaches 1.5e-5 S through the
     # FP32 rounding of the derivative planes, which the FP64 refinement of the value planes does not touch

@@ -1,8 +1,9 @@
 """Parity of the CUDA path (through the C ABI) with the oracle on the same inputs.
 
 Tolerances: neighbour lists and triplets bit-exact; FP64 build <= 1e-10 relative on log|psi|, its gradient, its
-Laplacian and E_loc.  FP32 and mixed paths: log|psi| <= 1e-5 relative; E_loc, the Laplacian and the gradient of
-log|psi| per walker within 1e-5 (mixed: 1e-4) of the magnitude of the terms E_loc is summed from,
+Laplacian and E_loc.  FP32 and mixed paths: log|psi| <= 3e-5 relative (test_logpsi); E_loc per walker, and the
+Laplacian and the gradient of log|psi| on walkers away from a node, within 1e-5 (mixed: 1e-4) of the magnitude of
+the terms E_loc is summed from,
 S = (|lap log psi| + |grad log psi|^2) / 2 + |V| (helpers.check_eloc_contract).  Near a node of psi the FP32
 rounding of the values that build the orbital matrices moves E_loc by up to ~2e-6 of the kinetic terms; the device
 flags those walkers (kinetic terms above refine_ratio |E_loc|, or a determinant-weighted condition number above
@@ -173,7 +174,9 @@ def _check_local_energy(wf, mol, nu, r, p, precision):
     assert rel(dbg["potential"], epot).max() < tol
     grad_ref = np.array([x[1] for x in fl]).reshape(dbg["grad"].shape)
     lap_ref = np.array([x[2] for x in fl])
-    assert np.all(np.abs(aux["logpsi"].double().cpu().numpy() - lp) / np.maximum(1, np.abs(lp)) < tol)
+    # log|psi| in FP32 / mixed: the bound of test_logpsi (carrier rounding amplified by the orbital matrices)
+    tol_lp = tol if precision == "fp64" else 3e-5
+    assert np.all(np.abs(aux["logpsi"].double().cpu().numpy() - lp) / np.maximum(1, np.abs(lp)) < tol_lp)
     if precision == "fp64":
         for k in range(len(r)):
             assert np.linalg.norm(dbg["grad"][k] - grad_ref[k]) / np.linalg.norm(grad_ref[k]) < tol
