@@ -140,10 +140,11 @@ void tc_shape(int k, const fire_problem* p, size_t* K, size_t* N, int* cnt) {
   *cnt = kind == -1 ? NDET : 1;
 }
 bool tc_tiled(int k, size_t K) { return K <= 256 || kTcSrc[k].kind == -1; }
-// the A-resident kernel's slots (K <= 256, not the envelope): FP16 scaled-grid tiles followed by N column scales
-bool tc_grid(int k, size_t K) { return K <= 256 && kTcSrc[k].kind != -1; }
-// byte offset of a grid slot's column scales from its tiles (one matrix per grid slot)
-size_t tc_cs_offset(size_t K, size_t N) { return tc_tiles_bytes(K, N); }
+// FP16 scaled-grid tiles followed by the column scales (cnt x N floats): the A-resident kernel's slots (K <= 256) and
+// the envelope kernel's (K = 8 N <= ENV_TC_KMAX, hi parts narrowed by grid_hb so that the K-long sums stay exact)
+bool tc_grid(int k, size_t K) { return K <= 256 || (kTcSrc[k].kind == -1 && K <= (size_t)ENV_TC_KMAX); }
+// byte offset of a grid slot's column scales from its tiles
+size_t tc_cs_offset(size_t K, size_t N, int cnt) { return (size_t)cnt * tc_tiles_bytes(K, N); }
 // byte offsets of the BF16 region (tc_off[TC_COUNT] = end)
 void tc_offsets(const fire_problem* p, size_t float_bytes, size_t* off) {
   size_t o = (float_bytes + 255) / 256 * 256;
@@ -728,7 +729,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
     const long tot = (long)c.Wc * ns * N * NENV_ORB, K8 = (long)N * NENV_ORB;
     // mixed path: the derivative rows come from k_env_tc (coefficients generated on chip, tensor cores), so
     // only the value coefficients are materialised, for the FP32 contraction of the value rows
-    const bool tc_env = sizeof(T) == 4 && c.mixed && NV > 1;
+    const bool tc_env = sizeof(T) == 4 && c.mixed && NV > 1 && NENV_ORB * N <= ENV_TC_KMAX;
     const int nvc = tc_env ? 1 : NV;  // coefficient rows per electron
     g_nlaunch++;
     if (tc_env)
@@ -744,7 +745,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
           const long ldc = (long)DN;
           const uintptr_t a = reinterpret_cast<uintptr_t>(C);
           const int vec = (a % 16 == 0 && ldc % 4 == 0) ? 4 : ((a % 8 == 0 && ldc % 2 == 0) ? 2 : 1);
-          const EnvTcP ep{c.r, c.R, sp, C, ldc, n, ns, s == 0 ? 0 : nu, N, c.Wc, d, NV, vec};
+          const EnvTcP ep{c.r, c.R, sp, C, ldc, n, ns, s == 0 ? 0 : nu, N, c.Wc, d, NV, vec, c.tcw[slot].cs + (size_t)d * n};
           Prof pg("gemm", c.s);
           g_nlaunch++;
           const cudaError_t e =
@@ -1096,9 +1097,9 @@ Ctx<T> make_ctx(const fire_problem* p, cudaStream_t s, const float* R, const flo
       int cnt;
       tc_shape(k, p, &K, &N, &cnt);
       const __nv_bfloat16* hi = reinterpret_cast<const __nv_bfloat16*>(base + to[k]);
-      if (tc_grid(k, K))
+      if (tc_grid(k, K) && tc_tiled(k, K))
         c.tcw[k] = TcWeights{nullptr, nullptr, hi, nullptr,
-                             reinterpret_cast<const float*>(base + to[k] + tc_cs_offset(K, N)), nullptr};
+                             reinterpret_cast<const float*>(base + to[k] + tc_cs_offset(K, N, cnt)), nullptr};
       else if (tc_tiled(k, K)) c.tcw[k] = TcWeights{nullptr, nullptr, hi, nullptr, nullptr, nullptr};
       else c.tcw[k] = TcWeights{hi, hi + (size_t)cnt * N * K, nullptr, nullptr, nullptr, nullptr};
     }
@@ -1809,9 +1810,11 @@ fire_status fire_prepare_params(void* stream, const fire_problem* prob, const fl
     for (int m = 0; m < cnt; ++m) {
       const float* src = reinterpret_cast<const float*>(prepared) + off[kTcSrc[k].slot] + (size_t)m * K * N;
       g_nlaunch++;
-      if (tc_tiled(k, K))  // envelope weights (k_env_tc, A split elementwise on chip) keep the elementwise split
+      if (tc_tiled(k, K))
         split_tiles(src, (int)K, (int)N, hi + (size_t)m * tc_tiles_bytes(K, N) / 2, s,
-                    tc_grid(k, K) ? reinterpret_cast<float*>(base + to[k] + tc_cs_offset(K, N)) : nullptr);
+                    tc_grid(k, K)
+                        ? reinterpret_cast<float*>(base + to[k] + tc_cs_offset(K, N, cnt)) + (size_t)m * N
+                        : nullptr);
       else split_transpose(src, (int)K, (int)N, hi + (size_t)m * N * K, lo + (size_t)m * N * K, s);
     }
   }

@@ -7,37 +7,46 @@
 //   jac: -a e (r_g - R_I) / rho,   lap: e (a^2 - 2 a / rho),   e = exp(-a rho), rho = |r_g - R_I|.
 // The coefficient matrix (8 N columns for each of 4 rows per electron) is never written to memory.  Four
 // producer warps compute every 128 x 64 A block -- 32 electrons x 4 planes (plane-major: tile row
-// v * 32 + electron) by 8 nuclei x 8 envelopes -- directly into shared memory as split BF16 (hi + lo, as in
-// k_gemm_tca): one thread per (electron, nucleus) evaluates rho once and the 8 exponentials and writes whole
-// 16-byte core-matrix rows.  The determinant's pre-tiled split weights stream in by bulk copies; three
-// BF16 MMAs per 16-deep step into a TMEM accumulator, two accumulators so that the epilogue of one tile
-// overlaps the MMAs of the next; every wait is bounded.  The value row (coefficient e) stays on the FP32
-// CUDA-core contraction.
+// v * 32 + electron) by 8 nuclei x 8 envelopes -- directly into shared memory: one thread per (electron,
+// nucleus) evaluates rho once and the 8 exponentials and writes whole 16-byte core-matrix rows.
+// The split is the scaled grid of k_gemm_tca (fire_tc.cuh) with hi parts narrowed to 2^(grid_hb(8 N) + 1), so that
+// the hi x hi sums over all 8 N stay exact in FP32: a first sweep over the tile's nuclei gives every row's largest
+// coefficient (the four producer warps meet on an mbarrier), then each block is written as FP16 hi + lo of the
+// scaled coefficients.  The determinant's pre-tiled weights (split the same way, column scales beside them) stream
+// in by bulk copies; four FP16 MMAs per 16-deep step, hi x hi into one TMEM accumulator and the other three products
+// into a second, two accumulator pairs so that the epilogue of one tile overlaps the MMAs of the next; the epilogue
+// adds the pair and applies the row and column scales.  Every wait is bounded.  The value row (coefficient e) stays
+// on the compensated CUDA-core contraction.
 #include "fire_tc.cuh"
 
 namespace fire {
 
 constexpr int ENV_THREADS = 448, ENV_STAGES = 3;
 struct EnvCfg {
-  static constexpr int A_BYTES = TC_BM * TC_BK * 2;       // one BF16 plane of a 128 x 64 A block
+  static constexpr int A_BYTES = TC_BM * TC_BK * 2;       // one FP16 plane of a 128 x 64 A block
   static constexpr int A_BLOCK = 2 * A_BYTES;             // hi + lo
   static constexpr int B_BLOCK = 2 * TCP_BN * TC_BK * 2;  // one pre-tiled weight block (hi + lo)
   static constexpr int STAGE = A_BLOCK + B_BLOCK;
-  static constexpr int TOTAL = ENV_STAGES * STAGE + 256;
+  // row exponent codes (int16): the producer warps' maxima [tile parity][warp][plane][electron], then the rows'
+  // codes for the epilogue [tile mod 8][128 rows]: the producers run at most 3 blocks ahead of the MMAs and those
+  // at most 2 tiles ahead of the epilogue, i.e. at most 5 tiles ahead of its reads with one block per tile
+  static constexpr int CODE_SLOTS = 8;
+  static constexpr int CODE_BYTES = 2 * 4 * 4 * 32 * 2 + CODE_SLOTS * TC_BM * 2;
+  static constexpr int TOTAL = ENV_STAGES * STAGE + CODE_BYTES + 256;
 };
 struct EnvBar {
   uint64_t afull[ENV_STAGES], bfull[ENV_STAGES], empty[ENV_STAGES], tfull[2], tempty[2];
+  uint64_t rmax;       // the producers' row maxima of a tile are complete
+  uint64_t rsfull[EnvCfg::CODE_SLOTS];  // the row codes of tile t (slot t mod 8) are written
   uint32_t tmem;
   int abort;
 };
 
-// the 4 derivative coefficients of the 8 envelopes of nucleus I for an electron at (rx, ry, rz), split into
-// BF16 hi and lo planes: word w of plane v holds envelopes 2w (low half) and 2w + 1
+// the 4 derivative coefficients of the 8 envelopes of nucleus I for an electron at (rx, ry, rz) (zero when !ok)
 // Rn: nuclear positions [N][3]; spd: this determinant's exponents of nucleus I at spd + I * sps (shared memory,
 // sps = NENV_ORB, when staged; else the global table, sps = NDET * NENV_ORB)
-__device__ __forceinline__ void env_coef_rows(const float* Rn, const float* spd, int sps, bool ok, float rx, float ry,
-                                              float rz, int I, uint4 (&hi)[4], uint4 (&lo)[4]) {
-  float c[4][NENV_ORB];
+__device__ __forceinline__ void env_coef_vals(const float* Rn, const float* spd, int sps, bool ok, float rx, float ry,
+                                              float rz, int I, float (&c)[4][NENV_ORB]) {
   if (ok) {
     const float dx = rx - Rn[3 * I], dy = ry - Rn[3 * I + 1], dz = rz - Rn[3 * I + 2];
     const float rho = sqrtf(dx * dx + dy * dy + dz * dz);
@@ -59,20 +68,6 @@ __device__ __forceinline__ void env_coef_rows(const float* Rn, const float* spd,
 #pragma unroll
       for (int k = 0; k < NENV_ORB; ++k) c[v][k] = 0.f;
   }
-#pragma unroll
-  for (int v = 0; v < 4; ++v) {
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-      const __nv_bfloat162 hb = __floats2bfloat162_rn(c[v][2 * w], c[v][2 * w + 1]);
-      const float2 hf = __bfloat1622float2(hb);
-      const __nv_bfloat162 lb = __floats2bfloat162_rn(c[v][2 * w] - hf.x, c[v][2 * w + 1] - hf.y);
-      h[w] = *reinterpret_cast<const uint32_t*>(&hb);
-      l[w] = *reinterpret_cast<const uint32_t*>(&lb);
-    }
-    hi[v] = make_uint4(h[0], h[1], h[2], h[3]);
-    lo[v] = make_uint4(l[0], l[1], l[2], l[3]);
-  }
 }
 
 // Bt: the determinant's tiled split weights [ceil(n / 128)][ceil(8 N / 64)] blocks of EnvCfg::B_BLOCK bytes.
@@ -80,7 +75,9 @@ __device__ __forceinline__ void env_coef_rows(const float* Rn, const float* spd,
 __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_bfloat16* Bt, int32_t* status,
                                                            int stage_params) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];  // [stage][A hi, A lo, B hi, B lo]
-  EnvBar* bars = reinterpret_cast<EnvBar*>(tc_smem + ENV_STAGES * EnvCfg::STAGE);
+  int16_t* rpart = reinterpret_cast<int16_t*>(tc_smem + ENV_STAGES * EnvCfg::STAGE);  // [2][4 warps][4][32]
+  int16_t* rcode = rpart + 2 * 4 * 4 * 32;                                            // [8][128]
+  EnvBar* bars = reinterpret_cast<EnvBar*>(tc_smem + ENV_STAGES * EnvCfg::STAGE + EnvCfg::CODE_BYTES);
   // the nuclear positions and this determinant's exponents, staged once (stage_params) after the barriers
   float* Rsm = reinterpret_cast<float*>(tc_smem + EnvCfg::TOTAL);
   float* spsm = Rsm + 3 * p.N;
@@ -89,6 +86,7 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
   const int n_e = p.Wc * p.ns;
   const int mt = (n_e + 31) / 32, nt = (p.n + TCP_BN - 1) / TCP_BN;
   const int nk = (NENV_ORB * p.N + TC_BK - 1) / TC_BK;
+  const int hb = grid_hb(NENV_ORB * p.N);  // hi parts of at most 2^(hb + 1): the 8 N-long hi x hi sums are exact
   const int groups = gridDim.x / nt;
   const int j = blockIdx.x % nt, m_first = blockIdx.x / nt;
   if (m_first >= mt) return;
@@ -104,12 +102,14 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
       mbar_init(smem_u32(&bars->tfull[b]), 1);
       mbar_init(smem_u32(&bars->tempty[b]), 256);
     }
+    mbar_init(smem_u32(&bars->rmax), 128);
+    for (int q = 0; q < EnvCfg::CODE_SLOTS; ++q) mbar_init(smem_u32(&bars->rsfull[q]), 128);
     bars->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 12) {
+  if (warp == 12) {  // two accumulator pairs (exact hi x hi sums, the other products): all 512 columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem)),
-                 "r"(2 * TCP_BN));
+                 "r"(4 * TCP_BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (stage_params) {
@@ -131,8 +131,8 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
     // ------------------------------------------------------------------ A producers (128 threads)
     // thread (lw, lane): electron lane of the tile, nuclei 2 lw and 2 lw + 1 of every 8-nucleus block
     const int lw = warp - 8;
-    long kc = 0;
-    for (int m = m_first; m < mt && !*abort; m += groups) {
+    long kc = 0, ut = 0;
+    for (int m = m_first; m < mt && !*abort; m += groups, ++ut) {
       const int e = m * 32 + lane;
       const bool ve = e < n_e;
       float rx = 0.f, ry = 0.f, rz = 0.f;
@@ -142,26 +142,63 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
         ry = p.r[3 * g + 1];
         rz = p.r[3 * g + 2];
       }
+      // first sweep: this thread's largest coefficient of every plane over its nuclei; the four warps' maxima meet
+      // in shared memory (the buffer alternates between tiles: a warp writing tile t + 2 has passed the barrier of
+      // tile t + 1, so every reader of tile t is done)
+      float mx[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int kb = 0; kb < nk; ++kb)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int I = kb * 8 + 2 * lw + q;
+          float c[4][NENV_ORB];
+          env_coef_vals(Rn, spd, sps, ve && I < p.N, rx, ry, rz, I, c);
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+#pragma unroll
+            for (int k = 0; k < NENV_ORB; ++k) mx[v] = fmaxf(mx[v], fabsf(c[v][k]));
+        }
+      int16_t* part = rpart + (ut & 1) * 4 * 4 * 32;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) part[(lw * 4 + v) * 32 + lane] = (int16_t)grid_code(mx[v]);
+      tc_arrive(&bars->rmax);
+      if (!tc_wait(&bars->rmax, (uint32_t)(ut & 1), abort)) break;
+      float inv[4];
+      int16_t* codes = rcode + (ut % EnvCfg::CODE_SLOTS) * TC_BM;  // the epilogue has read tile ut - 8's codes
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        int code = part[v * 32 + lane];
+#pragma unroll
+        for (int w2 = 1; w2 < 4; ++w2) code = max(code, (int)part[(w2 * 4 + v) * 32 + lane]);
+        float sc;
+        grid_scales(code, inv[v], sc, hb);
+        if (lw == 0) codes[v * 32 + lane] = (int16_t)code;
+      }
+      tc_arrive(&bars->rsfull[ut % EnvCfg::CODE_SLOTS]);
       for (int kb = 0; kb < nk; ++kb, ++kc) {
-        const int s = (int)(kc % ENV_STAGES);
+        const int st = (int)(kc % ENV_STAGES);
         const long use = kc / ENV_STAGES;
-        if (use > 0 && !tc_wait(&bars->empty[s], (uint32_t)((use - 1) & 1), abort)) break;
-        unsigned char* a_hi = tc_smem + s * EnvCfg::STAGE;
+        if (use > 0 && !tc_wait(&bars->empty[st], (uint32_t)((use - 1) & 1), abort)) break;
+        unsigned char* a_hi = tc_smem + st * EnvCfg::STAGE;
         unsigned char* a_lo = a_hi + EnvCfg::A_BYTES;
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
           const int il = 2 * lw + q, I = kb * 8 + il;
-          uint4 hi[4], lo[4];
-          env_coef_rows(Rn, spd, sps, ve && I < p.N, rx, ry, rz, I, hi, lo);
+          float c[4][NENV_ORB];
+          env_coef_vals(Rn, spd, sps, ve && I < p.N, rx, ry, rz, I, c);
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
+            uint4 hi, lo;
+            split_grid_f16x2(c[v][0], c[v][1], inv[v], hi.x, lo.x);
+            split_grid_f16x2(c[v][2], c[v][3], inv[v], hi.y, lo.y);
+            split_grid_f16x2(c[v][4], c[v][5], inv[v], hi.z, lo.z);
+            split_grid_f16x2(c[v][6], c[v][7], inv[v], hi.w, lo.w);
             const uint32_t off = tc_off(v * 32 + lane, il * 8);
-            *reinterpret_cast<uint4*>(a_hi + off) = hi[v];
-            *reinterpret_cast<uint4*>(a_lo + off) = lo[v];
+            *reinterpret_cast<uint4*>(a_hi + off) = hi;
+            *reinterpret_cast<uint4*>(a_lo + off) = lo;
           }
         }
         proxy_fence();
-        tc_arrive(&bars->afull[s]);
+        tc_arrive(&bars->afull[st]);
       }
     }
   } else if (warp == 13) {
@@ -183,14 +220,14 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
   } else if (warp == 12) {
     // ------------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = tc_idesc<TCP_BN>();
+      const uint32_t idesc = tc_idesc_f16<TCP_BN>();
       long kc = 0, uc = 0;
       for (int m = m_first; m < mt && !*abort; m += groups) {
         const int b = (int)(uc & 1);
         const long ub = uc >> 1;
         if (ub > 0 && !tc_wait(&bars->tempty[b], (uint32_t)((ub - 1) & 1), abort)) break;
         tc_fence_after();
-        const uint32_t acc_t = tmem + (uint32_t)(b * TCP_BN);
+        const uint32_t acc_t = tmem + (uint32_t)(b * 2 * TCP_BN);  // hi x hi sums; the rest TCP_BN further
         for (int kb = 0; kb < nk; ++kb, ++kc) {
           const int s = (int)(kc % ENV_STAGES);
           const uint32_t par = (uint32_t)((kc / ENV_STAGES) & 1);
@@ -204,8 +241,9 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
             const uint64_t dah = tc_desc(ah + sa), dal = tc_desc(al + sa);
             const uint64_t dbh = tc_desc_s(bh + sb, 2048, 128), dbl = tc_desc_s(bl + sb, 2048, 128);
             tc_mma(acc_t, dah, dbh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-            tc_mma(acc_t, dah, dbl, idesc, 1u);
-            tc_mma(acc_t, dal, dbh, idesc, 1u);
+            tc_mma(acc_t + TCP_BN, dah, dbl, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            tc_mma(acc_t + TCP_BN, dal, dbh, idesc, 1u);
+            tc_mma(acc_t + TCP_BN, dal, dbl, idesc, 1u);
           }
           tc_commit(smem_u32(&bars->empty[s]));
         }
@@ -221,6 +259,11 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
     long uc = 0;
     for (int m = m_first; m < mt && !*abort; m += groups) {
       const int b = (int)(uc & 1);
+      // this row's scale (plane quad, electron lane), published by the producers for tile uc
+      const int slot = (int)(uc % EnvCfg::CODE_SLOTS);
+      if (!tc_wait(&bars->rsfull[slot], (uint32_t)((uc / EnvCfg::CODE_SLOTS) & 1), abort)) break;
+      float inv_unused, row_sc;
+      grid_scales((int)rcode[slot * TC_BM + quad * 32 + lane], inv_unused, row_sc, hb);
       if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
       tc_fence_after();
       const int e = m * 32 + lane;
@@ -229,12 +272,15 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
         const long g = (long)(e / p.ns) * p.n + p.soff + e % p.ns;
         out = p.C + (g * p.nv + quad + 1) * p.ldc;
       }
-      const uint32_t base = tmem + (uint32_t)(b * TCP_BN) + ((uint32_t)(quad * 32) << 16);
+      const uint32_t base = tmem + (uint32_t)(b * 2 * TCP_BN) + ((uint32_t)(quad * 32) << 16);
       for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
         const int col = n0 + c0;
         if (col >= p.n) break;  // warp-uniform
-        float v[16];
+        float v[16], v2[16];
         tmem_ld16(base + (uint32_t)c0, v);
+        tmem_ld16(base + (uint32_t)(TCP_BN + c0), v2);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = (v[k] + v2[k]) * row_sc * (col + k < p.n ? p.cs[col + k] : 0.f);
         if (!out) continue;
         if (p.vec == 4 && col + 15 < p.n) {
 #pragma unroll
@@ -294,7 +340,7 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
   __syncthreads();
   tc_fence_after();
   if (warp == 12) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TCP_BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(4 * TCP_BN));
   }
 }
 
@@ -306,7 +352,8 @@ cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cu
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (num_sms <= 0) num_sms = 1;
   }
-  if (!Bt || (reinterpret_cast<uintptr_t>(Bt) & 15) != 0) return cudaErrorInvalidValue;
+  if (!Bt || !p.cs || (reinterpret_cast<uintptr_t>(Bt) & 15) != 0 || NENV_ORB * p.N > ENV_TC_KMAX)
+    return cudaErrorInvalidValue;
   const long n_e = (long)p.Wc * p.ns;
   if (n_e <= 0 || p.n <= 0) return cudaSuccess;
   const long mt = (n_e + 31) / 32, nt = (p.n + TCP_BN - 1) / TCP_BN;

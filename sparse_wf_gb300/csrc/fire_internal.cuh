@@ -54,7 +54,10 @@ struct EnvTcP {
   float* C;
   long ldc;
   int n, ns, soff, N, Wc, d, nv, vec;
+  const float* cs;  // column scales of this determinant's weights [n] (powers of two)
 };
+// longest envelope contraction (8 N) that k_env_tc splits on an exact grid (hi parts of at most 2^(grid_hb + 1))
+constexpr int ENV_TC_KMAX = 4096;
 // k_detlap staging: up to chi positions per dependency (3 J rows each, DL_CMAX at most), contraction chunks of
 // DL_OC elements in shared-memory rows of DL_LD (16-byte aligned; consecutive rows on distinct bank quads); + 4
 // rows because a thread's strided tile rows may run past the last one; DL_STAGES chunks in flight.  Jobs with

@@ -136,8 +136,8 @@ __global__ void k_ecp_store(int Wc, int w0, const double* acc, T* out);
 
 // fire_tc.cu (host launchers)
 cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __nv_bfloat16* lo, cudaStream_t s);
-// cs (K <= 256, the A-resident kernel): FP16 scaled-grid split of every column, its scale into cs [N]; nullptr: an
-// elementwise BF16 split (the envelope kernel)
+// cs: FP16 scaled-grid split of every column (hi parts bounded for an exact sum over K), its scale into cs [N];
+// nullptr: an elementwise BF16 split
 cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s, float* cs);
 cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cudaStream_t s);
 template <typename T>

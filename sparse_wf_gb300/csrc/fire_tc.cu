@@ -19,11 +19,11 @@ __global__ void k_split_transpose(const float* __restrict__ W, int K, int N, __n
 }
 
 // hi/lo split of W[K][N] into tiles of 128 columns x 64 K: tile (j, kb) at block j * ceil(K / 64) + kb holds the
-// hi plane then the lo plane, each [8 k-groups][128 columns][8 k] (zero padding beyond N and K).  With cs (the
-// A-resident kernel, K <= 256): every column scaled and split on the grid of its largest magnitude in FP16
-// (split_grid_f16x2), its scale in cs[n]; else an elementwise BF16 split (the envelope kernel).
+// hi plane then the lo plane, each [8 k-groups][128 columns][8 k] (zero padding beyond N and K).  With cs: every
+// column scaled and split on the grid of its largest magnitude in FP16 (hi parts of at most 2^(hb + 1), hb =
+// grid_hb(K)), its scale in cs[n]; else an elementwise BF16 split.
 __global__ void k_split_tiles(const float* __restrict__ W, int K, int N, __nv_bfloat16* __restrict__ Bt,
-                              float* __restrict__ cs) {
+                              float* __restrict__ cs, int hb) {
   const int nkt = (K + 63) / 64, nnt = (N + 127) / 128;
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over (block, g, r, e)
   if (idx >= (long)nnt * nkt * 8192) return;
@@ -38,7 +38,7 @@ __global__ void k_split_tiles(const float* __restrict__ W, int K, int N, __nv_bf
     if (n < N) {
       float mx = 0.f;
       for (int q = 0; q < K; ++q) mx = fmaxf(mx, fabsf(W[(long)q * N + n]));
-      grid_scales(grid_code(mx), inv, sc);
+      grid_scales(grid_code(mx), inv, sc, hb);
       if (kb == 0 && g == 0 && e == 0) cs[n] = sc;
     }
     const float x = v * inv, h = rintf(x);
@@ -69,7 +69,7 @@ __global__ void k_tile_mask(GemmP<float> p, int* mask) {
 
 cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s, float* cs) {
   const long tot = (long)((N + 127) / 128) * ((K + 63) / 64) * 8192;
-  k_split_tiles<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, Bt, K <= TCP_KMAX ? cs : nullptr);
+  k_split_tiles<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, K, N, Bt, cs, grid_hb(K));
   return cudaPeekAtLastError();
 }
 

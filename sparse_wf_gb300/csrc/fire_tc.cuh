@@ -157,8 +157,9 @@ __device__ __forceinline__ int grid_code(float mx) {
   if (!(mx <= 3.4e38f)) return GRID_NAN;
   return max(ilogbf(mx), -120);
 }
-// (inverse scale applied to the values, scale the epilogue applies) of an exponent code
-__device__ __forceinline__ void grid_scales(int code, float& inv, float& sc) {
+// (inverse scale applied to the values, scale the epilogue applies) of an exponent code, for hi parts of at most
+// 2^(hb + 1) in magnitude (hb = 7 for K <= 256; grid_hb gives hb for longer sums)
+__device__ __forceinline__ void grid_scales(int code, float& inv, float& sc, int hb = 7) {
   if (code == GRID_ZERO) {
     inv = 0.f;
     sc = 0.f;
@@ -166,9 +167,16 @@ __device__ __forceinline__ void grid_scales(int code, float& inv, float& sc) {
     inv = 0.f;
     sc = __int_as_float(0x7fc00000);
   } else {
-    inv = ldexpf(1.f, 7 - code);
-    sc = ldexpf(1.f, code - 7);
+    inv = ldexpf(1.f, hb - code);
+    sc = ldexpf(1.f, code - hb);
   }
+}
+// the largest hb for which K products of two hi parts (each <= 2^(hb + 1)) sum exactly in FP32:
+// K 2^(2 hb + 2) <= 2^24
+__host__ __device__ inline int grid_hb(int K) {
+  int l = 0;
+  while ((1 << l) < K) ++l;
+  return (22 - l) / 2;
 }
 __device__ __forceinline__ void split_grid_f16x2(float a, float b, float inv, uint32_t& hi, uint32_t& lo) {
   const float xa = a * inv, xb = b * inv;
