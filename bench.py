@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--mcmc-single-width", type=float, default=0.5)
     ap.add_argument("--mcmc-low-rank-steps", type=int, default=32,
                     help="single-electron steps of the low-rank block, timed on a copy of the walkers (0: skip)")
-    ap.add_argument("--acc-walkers", type=int, default=256, help="walkers checked against the FP64 build")
+    ap.add_argument("--acc-walkers", type=int, default=1024, help="walkers checked against the FP64 build")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
     ap.add_argument("--serving-requests", type=int, default=20, help="requests of the serving segment (0: skip)")
     ap.add_argument("--serving-rate", type=float, default=200.0, help="offered load, requests per second")
