@@ -728,18 +728,23 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
     const T* sp = c.W.w[s == 0 ? PR_ENV_UP_SP : PR_ENV_DN_SP];
     const long tot = (long)c.Wc * ns * N * NENV_ORB, K8 = (long)N * NENV_ORB;
     // mixed path: the derivative rows come from k_env_tc (coefficients generated on chip, tensor cores), so
-    // only the value coefficients are materialised, for the FP32 contraction of the value rows
-    const bool tc_env = sizeof(T) == 4 && c.mixed && NV > 1 && NENV_ORB * N <= ENV_TC_KMAX;
+    // only the value coefficients are materialised, for the compensated FP32 contraction of the value rows; the
+    // Metropolis blocks' plain value rows come from k_env_tc as well (value tiles), with no coefficients in memory
+    const bool tc_ok = sizeof(T) == 4 && c.mixed && NENV_ORB * N <= ENV_TC_KMAX;
+    const bool tc_env = tc_ok && NV > 1;
+    const bool tc_val = tc_ok && NV == 1 && !c.comp;
     const int nvc = tc_env ? 1 : NV;  // coefficient rows per electron
-    g_nlaunch++;
-    if (tc_env)
-      k_env_coef<T, 1><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, sp, n, ns, s == 0 ? 0 : nu, N, c.Wc, coef);
-    else
-      k_env_coef<T, NV><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, sp, n, ns, s == 0 ? 0 : nu, N, c.Wc, coef);
+    if (!tc_val) {
+      g_nlaunch++;
+      if (tc_env)
+        k_env_coef<T, 1><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, sp, n, ns, s == 0 ? 0 : nu, N, c.Wc, coef);
+      else
+        k_env_coef<T, NV><<<nblk(tot), 256, 0, c.s>>>(c.r, c.R, sp, n, ns, s == 0 ? 0 : nu, N, c.Wc, coef);
+    }
     const long rows = (long)c.Wc * ns * nvc;
     for (int d = 0; d < NDET; ++d) {
       if constexpr (sizeof(T) == 4) {
-        if (tc_env) {
+        if (tc_env || tc_val) {
           const int slot = s == 0 ? TC_ENV_UP : TC_ENV_DN;
           float* C = env + (long)d * n;
           const long ldc = (long)DN;
@@ -748,9 +753,10 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
           const EnvTcP ep{c.r, c.R, sp, C, ldc, n, ns, s == 0 ? 0 : nu, N, c.Wc, d, NV, vec, c.tcw[slot].cs + (size_t)d * n};
           Prof pg("gemm", c.s);
           g_nlaunch++;
-          const cudaError_t e =
-              env_tc(ep, c.tcw[slot].tiles + (size_t)d * tc_tiles_bytes((size_t)K8, (size_t)n) / 2, c.status, c.s);
+          const cudaError_t e = env_tc(ep, c.tcw[slot].tiles + (size_t)d * tc_tiles_bytes((size_t)K8, (size_t)n) / 2,
+                                       c.status, c.s, tc_val);
           if (e != cudaSuccess) return e;
+          if (tc_val) continue;
         }
       }
       GemmP<T> g = gp0<T>();

@@ -70,8 +70,26 @@ __device__ __forceinline__ void env_coef_vals(const float* Rn, const float* spd,
   }
 }
 
+// the value coefficients exp(-a rho) of the 8 envelopes of nucleus I (zero when !ok)
+__device__ __forceinline__ void env_value_vals(const float* Rn, const float* spd, int sps, bool ok, float rx, float ry,
+                                               float rz, int I, float (&c)[NENV_ORB]) {
+  if (ok) {
+    const float dx = rx - Rn[3 * I], dy = ry - Rn[3 * I + 1], dz = rz - Rn[3 * I + 2];
+    const float rho = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float* a = spd + (long)I * sps;
+#pragma unroll
+    for (int k = 0; k < NENV_ORB; ++k) c[k] = expf(-a[k] * rho);
+  } else {
+#pragma unroll
+    for (int k = 0; k < NENV_ORB; ++k) c[k] = 0.f;
+  }
+}
+
 // Bt: the determinant's tiled split weights [ceil(n / 128)][ceil(8 N / 64)] blocks of EnvCfg::B_BLOCK bytes.
-// Each CTA owns one 128-column slice of the output (blockIdx.x % nt) and walks the 32-electron tiles.
+// Each CTA owns one 128-column slice of the output (blockIdx.x % nt) and walks the tiles of 32 electrons (4
+// derivative planes), or with VAL of 128 electrons (the value plane only: the Metropolis blocks' value path, whose
+// plain FP32 contraction it replaces at the same ~2^-19 accuracy; each producer thread then owns a whole row).
+template <bool VAL>
 __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_bfloat16* Bt, int32_t* status,
                                                            int stage_params) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];  // [stage][A hi, A lo, B hi, B lo]
@@ -84,7 +102,8 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
   volatile int* abort = &bars->abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n_e = p.Wc * p.ns;
-  const int mt = (n_e + 31) / 32, nt = (p.n + TCP_BN - 1) / TCP_BN;
+  constexpr int ET = VAL ? 128 : 32;  // electrons per tile
+  const int mt = (n_e + ET - 1) / ET, nt = (p.n + TCP_BN - 1) / TCP_BN;
   const int nk = (NENV_ORB * p.N + TC_BK - 1) / TC_BK;
   const int hb = grid_hb(NENV_ORB * p.N);  // hi parts of at most 2^(hb + 1): the 8 N-long hi x hi sums are exact
   const int groups = gridDim.x / nt;
@@ -133,6 +152,54 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
     const int lw = warp - 8;
     long kc = 0, ut = 0;
     for (int m = m_first; m < mt && !*abort; m += groups, ++ut) {
+      if constexpr (VAL) {
+        // one row (electron m * 128 + 32 lw + lane) per thread: its own maximum gives its grid, no exchange
+        const int row = lw * 32 + lane, ev = m * 128 + row;
+        const bool vv = ev < n_e;
+        float vx = 0.f, vy = 0.f, vz = 0.f;
+        if (vv) {
+          const long g = (long)(ev / p.ns) * p.n + p.soff + ev % p.ns;
+          vx = p.r[3 * g];
+          vy = p.r[3 * g + 1];
+          vz = p.r[3 * g + 2];
+        }
+        float mxv = 0.f;
+        for (int I = 0; I < p.N; ++I) {
+          float c[NENV_ORB];
+          env_value_vals(Rn, spd, sps, vv, vx, vy, vz, I, c);
+#pragma unroll
+          for (int k = 0; k < NENV_ORB; ++k) mxv = fmaxf(mxv, c[k]);
+        }
+        const int code = grid_code(mxv);
+        float inv, sc;
+        grid_scales(code, inv, sc, hb);
+        rcode[(ut % EnvCfg::CODE_SLOTS) * TC_BM + row] = (int16_t)code;
+        tc_arrive(&bars->rsfull[ut % EnvCfg::CODE_SLOTS]);
+        for (int kb = 0; kb < nk; ++kb, ++kc) {
+          const int st = (int)(kc % ENV_STAGES);
+          const long use = kc / ENV_STAGES;
+          if (use > 0 && !tc_wait(&bars->empty[st], (uint32_t)((use - 1) & 1), abort)) break;
+          unsigned char* a_hi = tc_smem + st * EnvCfg::STAGE;
+          unsigned char* a_lo = a_hi + EnvCfg::A_BYTES;
+#pragma unroll 2
+          for (int il = 0; il < 8; ++il) {
+            const int I = kb * 8 + il;
+            float c[NENV_ORB];
+            env_value_vals(Rn, spd, sps, vv && I < p.N, vx, vy, vz, I, c);
+            uint4 hi, lo;
+            split_grid_f16x2(c[0], c[1], inv, hi.x, lo.x);
+            split_grid_f16x2(c[2], c[3], inv, hi.y, lo.y);
+            split_grid_f16x2(c[4], c[5], inv, hi.z, lo.z);
+            split_grid_f16x2(c[6], c[7], inv, hi.w, lo.w);
+            const uint32_t off = tc_off(row, il * 8);
+            *reinterpret_cast<uint4*>(a_hi + off) = hi;
+            *reinterpret_cast<uint4*>(a_lo + off) = lo;
+          }
+          proxy_fence();
+          tc_arrive(&bars->afull[st]);
+        }
+        continue;
+      }
       const int e = m * 32 + lane;
       const bool ve = e < n_e;
       float rx = 0.f, ry = 0.f, rz = 0.f;
@@ -266,11 +333,13 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
       grid_scales((int)rcode[slot * TC_BM + quad * 32 + lane], inv_unused, row_sc, hb);
       if (!tc_wait(&bars->tfull[b], (uint32_t)((uc >> 1) & 1), abort)) break;
       tc_fence_after();
-      const int e = m * 32 + lane;
+      // derivative tiles: plane quad of electron m * 32 + lane (carrier row quad + 1); value tiles: electron
+      // m * 128 + 32 quad + lane (carrier row 0)
+      const int e = VAL ? m * 128 + quad * 32 + lane : m * 32 + lane;
       float* out = nullptr;
       if (e < n_e) {
         const long g = (long)(e / p.ns) * p.n + p.soff + e % p.ns;
-        out = p.C + (g * p.nv + quad + 1) * p.ldc;
+        out = p.C + (g * p.nv + (VAL ? 0 : quad + 1)) * p.ldc;
       }
       const uint32_t base = tmem + (uint32_t)(b * 2 * TCP_BN) + ((uint32_t)(quad * 32) << 16);
       for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
@@ -344,7 +413,7 @@ __global__ void __launch_bounds__(ENV_THREADS, 1) k_env_tc(EnvTcP p, const __nv_
   }
 }
 
-cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cudaStream_t s) {
+cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cudaStream_t s, bool value_rows) {
   static int num_sms = 0;
   if (num_sms == 0) {
     int dev = 0;
@@ -356,7 +425,7 @@ cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cu
     return cudaErrorInvalidValue;
   const long n_e = (long)p.Wc * p.ns;
   if (n_e <= 0 || p.n <= 0) return cudaSuccess;
-  const long mt = (n_e + 31) / 32, nt = (p.n + TCP_BN - 1) / TCP_BN;
+  const long mt = (n_e + (value_rows ? 127 : 31)) / (value_rows ? 128 : 32), nt = (p.n + TCP_BN - 1) / TCP_BN;
   const long groups = std::max<long>(1, std::min<long>(mt, num_sms / nt));
   // the nuclear positions and this determinant's exponents go to shared memory when they fit
   static int smem_max = 0;
@@ -368,9 +437,10 @@ cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cu
   const size_t staged = (size_t)EnvCfg::TOTAL + sizeof(float) * (3 + NENV_ORB) * (size_t)p.N;
   const int stage_params = staged <= (size_t)smem_max ? 1 : 0;
   const int smem = stage_params ? (int)staged : EnvCfg::TOTAL;
-  const cudaError_t e = cudaFuncSetAttribute(k_env_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  auto kern = value_rows ? k_env_tc<true> : k_env_tc<false>;
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_env_tc<<<(unsigned)(groups * nt), ENV_THREADS, smem, s>>>(p, Bt, status, stage_params);
+  kern<<<(unsigned)(groups * nt), ENV_THREADS, smem, s>>>(p, Bt, status, stage_params);
   return cudaPeekAtLastError();
 }
 

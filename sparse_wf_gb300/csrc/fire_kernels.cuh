@@ -139,7 +139,8 @@ cudaError_t split_transpose(const float* W, int K, int N, __nv_bfloat16* hi, __n
 // cs: FP16 scaled-grid split of every column (hi parts bounded for an exact sum over K), its scale into cs [N];
 // nullptr: an elementwise BF16 split
 cudaError_t split_tiles(const float* W, int K, int N, __nv_bfloat16* Bt, cudaStream_t s, float* cs);
-cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cudaStream_t s);
+// value_rows: the value plane only (128 electrons per tile), else the 4 derivative planes (32 electrons per tile)
+cudaError_t env_tc(const EnvTcP& p, const __nv_bfloat16* Bt, int32_t* status, cudaStream_t s, bool value_rows);
 template <typename T>
 struct GemmP;
 cudaError_t gemm_tc(int mode, int bn, const GemmP<float>& p, const TcWeights& wt, int* mask_buf, int32_t* status,

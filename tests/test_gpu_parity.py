@@ -368,3 +368,25 @@ def test_mcmc_philox_draws_match_cpu_replay(cuda_lib):
             checked += 1
             assert int(n64[w]) == na
     assert checked > 0
+
+
+@pytest.mark.parametrize("name", ["c2h6", "c10h22"])
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_mcmc_value_path_logpsi(cuda_lib, name, precision):
+    """The Metropolis blocks evaluate proposals with the plain value contractions (and, in the mixed path, the
+    envelope value rows on the tensor cores): one step with zero displacement that accepts every proposal leaves
+    the block's own log|psi| of the walkers, which must match the oracle like fire_logpsi's (3e-5 relative)."""
+    wf, mol, nu, r, p = _wf(name, precision)
+    rr = torch.from_numpy(r).cuda().contiguous()
+    static = _static(wf, rr)
+    dp = wf._params(p)
+    _, logpsi = wf.signed(dp, rr, static)
+    logpsi.fill_(-1e30)  # any proposal is accepted; the block stores the proposals' log|psi|
+    B = r.shape[0]
+    n_acc, _ = wf.mcmc_block(dp, rr, logpsi, static, 1, 0.1, replay_noise=np.zeros((1, B, mol.n_el, 3)),
+                             replay_log_u=np.zeros((1, B)))
+    assert int(n_acc.sum()) == B
+    prob = O.Problem(mol.R, mol.Z, nu)
+    ref = np.array([O.logpsi(prob, p, w)[1] for w in r.astype(np.float64)])
+    err = np.abs(logpsi.double().cpu().numpy() - ref) / np.maximum(1.0, np.abs(ref))
+    assert err.max() < 3e-5, err.max()
