@@ -285,12 +285,10 @@ inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
 // ----------------------------------------------------------------------------- compensated value contraction
 // FP32 and mixed paths: the value planes (one row per node) feed the orbital matrices, whose inverse amplifies
 // their rounding by the condition number in the derivatives of log det.  k_gemm_comp computes them with
-// compensated dot products: every product split exactly with an FMA (its rounding error gathered in its own
-// accumulator), the products summed with Kahan's compensated summation (Kahan 1965; error <= 2 eps |sum| +
-// O(K eps^2) sum |terms|, whatever the signs and the order), i.e. as if in twice the working precision and then
-// rounded once: the error is ~2^-24 of the result even where the terms cancel (the orbital values are small
-// differences of large products), which a shorter FMA chain per partial sum does not give.  Seven operations per
-// term (Dot2 with TwoSum takes ten).
+// compensated dot products (Ogita, Rump and Oishi's Dot2: every product split exactly with an FMA, every partial
+// sum with TwoSum (Knuth), the errors gathered in a second accumulator), i.e. as if in twice the working precision
+// and then rounded once: the error is ~2^-24 of the result even where the terms cancel (the orbital values are
+// small differences of large products), which a shorter FMA chain per partial sum does not give.
 // The orbital-matrix values and the envelope values they are made of also leave the kernel as unevaluated hi + lo
 // float pairs, so that the double-FP32 elimination sees them to ~2^-48.
 //   COMP_PLAIN  C = a.b + bias (bias on rows with row % bias_period == 0)
@@ -360,12 +358,11 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
       for (int u = 0; u < 4; ++u) As[buf][aq + u][ar] = ra[u];
       *reinterpret_cast<float4*>(&Bs[buf][bk][bc]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
     };
-    // Kahan sum hi with compensation cc (the negated low part of the running sum), product errors in lo
-    float hi[4][4], cc[4][4], lo[4][4];
+    float hi[4][4], lo[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) hi[i][j] = cc[i][j] = lo[i][j] = 0.f;
+      for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.f;
     load(0);
     store(0);
     __syncthreads();
@@ -383,11 +380,11 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
             const float pr = av[i] * bv[j];
-            lo[i][j] += fmaf(av[i], bv[j], -pr);
-            const float y = pr - cc[i][j];
-            const float t = hi[i][j] + y;
-            cc[i][j] = (t - hi[i][j]) - y;
-            hi[i][j] = t;
+            const float pe = fmaf(av[i], bv[j], -pr);
+            float s2, e;
+            two_sum(hi[i][j], pr, s2, e);
+            hi[i][j] = s2;
+            lo[i][j] += e + pe;
           }
       }
       if (more) {
@@ -405,7 +402,7 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
       for (int j = 0; j < 4; ++j) {
         const int col = n0 + tx * 4 + j;
         if (col >= p.N) continue;
-        float h = hi[i][j], l = lo[i][j] - cc[i][j];
+        float h = hi[i][j], l = lo[i][j];
         if (MODE == COMP_PLAIN || MODE == COMP_SILU || MODE == COMP_ORB) {
           const float* bias = (MODE == COMP_ORB && spin == 1) ? p.bias2 : p.bias;
           const bool has_b = bias && (MODE != COMP_PLAIN || (p.bias_period > 0 && row % p.bias_period == 0));
