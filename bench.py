@@ -136,17 +136,21 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def gemm_flops(n, N, pairs):
-    """Algorithmic FLOPs (2 per multiply-add) of the dense contractions of one walker's E_loc."""
+def gemm_flops(n, N, pairs, value_rows=True, derivative_rows=True):
+    """Algorithmic FLOPs (2 per multiply-add) of the dense contractions of one walker's E_loc: of the value rows
+    (one per node), of the derivative rows (Jacobian and Laplacian rows; the mixed path's tensor-core share), or
+    both."""
     F, D = 256, 4
-    rows = 2 * n + 3 * (n + pairs)  # value + Laplacian rows + Jacobian rows of a sparse node
-    f = 5 * n * 2 * F * (2 * F + F + 5 * F)  # ElecInit GLU / Dense / Dense on [x, jac(3), lap]
+    rows = (n if value_rows else 0) + ((n + 3 * (n + pairs)) if derivative_rows else 0)  # rows of a sparse node
+    e5 = (1 if value_rows else 0) + (4 if derivative_rows else 0)  # ElecInit / envelope rows per electron
+    f = e5 * n * 2 * F * (2 * F + F + 5 * F)  # ElecInit GLU / Dense / Dense on [x, jac(3), lap]
     f += 2 * rows * 2 * F * F  # update MLP
-    f += 5 * n * 2 * (8 * N) * n * D  # envelope contraction
+    f += e5 * n * 2 * (8 * N) * n * D  # envelope contraction
     f += rows * 2 * F * D * n  # orbitals (needed spin only)
     f += rows * 2 * F * F  # attention values
     f += 2 * rows * 2 * F * F  # MLP Jastrow hidden layers
-    f += (3 * n + 2) * 2 * (2 * F * F + F * F + 2 * F)  # attention readout MLP (dense tangents)
+    if value_rows and derivative_rows:
+        f += (3 * n + 2) * 2 * (2 * F * F + F * F + 2 * F)  # attention readout MLP (dense tangents)
     return float(f)
 
 
@@ -439,17 +443,29 @@ def main():
     _lib.profile_enable(False)
     counts = wf.neighbor_lists(r_dev[: min(B, 64)], static)["counts"]
     pairs = float(np.mean(counts[:, 0] + counts[:, 1]))
-    flops = gemm_flops(mol.n_el, mol.n_nuc, pairs) * B
     peaks, peak_kind = measured_peaks()
-    g_launches, g_ms = prof.get("gemm", (0, float("nan")))
-    achieved = flops / (g_ms / 1e3) / 1e12
     # the contractions run inside a seconds-long step: the sustained bf16 figure is their ceiling
     peak = peaks["bf16_tflops_sustained"]
+    if args.precision == "mixed":
+        # the tensor-core contractions (the Jacobian and Laplacian rows): their FLOPs over their launches' time
+        flops = gemm_flops(mol.n_el, mol.n_nuc, pairs, value_rows=False) * B
+        g_launches, g_ms = prof.get("gemm_tc", (0, float("nan")))
+        kernel = "tensor-core contractions of one step (k_gemm_tca, k_env_tc: the Jacobian and Laplacian rows)"
+    else:
+        flops = gemm_flops(mol.n_el, mol.n_nuc, pairs) * B
+        g_launches = prof.get("gemm", (0, 0.0))[0] + prof.get("gemm_comp", (0, 0.0))[0]
+        g_ms = prof.get("gemm", (0, 0.0))[1] + prof.get("gemm_comp", (0, 0.0))[1]
+        kernel = "all dense contractions of one step (CUDA cores: k_gemm, k_gemm_comp)"
+    achieved = flops / (g_ms / 1e3) / 1e12
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
-                "kernel": "all dense contractions of one step (k_gemm_tca + k_env_tc + k_gemm)", "launches": g_launches,
+                "frac": achieved / peak, "traffic": None, "kernel": kernel, "launches": g_launches,
                 "avg_launch_ms": g_ms / max(g_launches, 1), "peak_source": f"bf16 dense sustained, {peak_kind}",
                 "flops_per_step": flops}
+    # the CUDA-core value-row contractions beside it (compensated; their FLOPs over their launches' time)
+    vc_launches, vc_ms = prof.get("gemm_comp", (0, float("nan")))
+    vflops = gemm_flops(mol.n_el, mol.n_nuc, pairs, derivative_rows=False) * B
+    roofline["value_rows"] = {"kernel": "k_gemm_comp (compensated value rows)", "launches": vc_launches, "ms": vc_ms,
+                              "flops_per_step": vflops, "tflops": vflops / (vc_ms / 1e3) / 1e12}
     stages = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items() if k != "kernels_launched"}
 
     # end to end through the public API: pinned host walkers in, E_loc out, every step

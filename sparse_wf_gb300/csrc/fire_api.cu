@@ -547,10 +547,12 @@ GemmP<T> gp0() {
 
 template <typename T, int MODE>
 cudaError_t gemm(const Ctx<T>& c, GemmP<T> g, int tc_id = -1) {
-  Prof pr("gemm", c.s);
+  // profile stages: "gemm_tc" the tensor-core contractions, "gemm" the CUDA-core ones
+  const bool tc = sizeof(T) == 4 && c.mixed && tc_id >= 0;
+  Prof pr(tc ? "gemm_tc" : "gemm", c.s);
   g_nlaunch++;
   if constexpr (sizeof(T) == 4) {
-    if (c.mixed && tc_id >= 0) {
+    if (tc) {
       const int bn = g.N > 256 ? 128 : 256;
       return gemm_tc(MODE, bn, g, c.tcw[tc_id], c.template buf<int>(c.P.tile_mask), c.status, c.s);
     }
@@ -561,7 +563,7 @@ cudaError_t gemm(const Ctx<T>& c, GemmP<T> g, int tc_id = -1) {
 // compensated value contraction (FP32 and mixed paths): low parts into C_lo / read from env_lo, row stride ld_lo
 template <int MODE>
 cudaError_t gemm_comp(const Ctx<float>& c, const GemmP<float>& g, float* C_lo, const float* env_lo, long ld_lo) {
-  Prof pr("gemm", c.s);
+  Prof pr("gemm_comp", c.s);
   g_nlaunch++;
   return launch_gemm_comp<MODE>(g, C_lo, env_lo, ld_lo, c.s);
 }
@@ -751,7 +753,7 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
           const uintptr_t a = reinterpret_cast<uintptr_t>(C);
           const int vec = (a % 16 == 0 && ldc % 4 == 0) ? 4 : ((a % 8 == 0 && ldc % 2 == 0) ? 2 : 1);
           const EnvTcP ep{c.r, c.R, sp, C, ldc, n, ns, s == 0 ? 0 : nu, N, c.Wc, d, NV, vec, c.tcw[slot].cs + (size_t)d * n};
-          Prof pg("gemm", c.s);
+          Prof pg("gemm_tc", c.s);
           g_nlaunch++;
           const cudaError_t e = env_tc(ep, c.tcw[slot].tiles + (size_t)d * tc_tiles_bytes((size_t)K8, (size_t)n) / 2,
                                        c.status, c.s, tc_val);
