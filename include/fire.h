@@ -15,6 +15,7 @@
  *                       :399-437 get_static_input, :476-481 get_neighbouring_nuclei
  *   fire_triplets       model/sparse_fwd_lap.py:252-291 _get_triplet_indices
  *   fire_logpsi         model/wave_function.py:183-198 MoonLikeWaveFunction.signed
+ *   fire_logpsi_grad    preconditioner.py:185-191 jax.grad(log_p) per walker (the SPRING Jacobian rows)
  *   fire_local_energy   hamiltonian.py:69-81 local_energy (kinetic via
  *                       wave_function.py:215-221, potential via hamiltonian.py:15-26),
  *                       batched like update.py:95-100 and reduced like update.py:130-134
@@ -195,6 +196,18 @@ fire_status fire_triplets_static(void* stream, const fire_problem* prob, const v
 fire_status fire_logpsi(void* stream, const fire_problem* prob, const float* R, const float* Z,
                         const void* prepared, const void* r, void* sign, void* logpsi,
                         void* workspace, size_t workspace_bytes, int32_t* status);
+
+/* Per-walker gradient of log|psi| with respect to every parameter: the rows of the Jacobian that the dense SPRING
+ * preconditioner contracts (preconditioner.py:185-191 jax.grad of log_p vmapped over the walkers, called from
+ * update.py:177-191).  grad: [B, L] in the walkers' dtype with L = offsets[FIRE_P_COUNT] of fire_param_layout;
+ * walker w's derivative with respect to blob element k is grad[w * L + k] (the padding between slots is 0).
+ * sign, logpsi: [B] as fire_logpsi.  Reverse mode through the value path on the CUDA cores, the orbital matrices
+ * inverted in double-FP32 (FP64 in the FP64 build); FIRE_PREC_MIXED computes it as FIRE_PREC_FP32.  The workspace
+ * is sized by fire_logpsi_grad_workspace_size (walkers per pass: prob->chunk_walkers, else as many as fit). */
+fire_status fire_logpsi_grad_workspace_size(const fire_problem* prob, int32_t chunk, size_t* bytes);
+fire_status fire_logpsi_grad(void* stream, const fire_problem* prob, const float* R, const void* prepared,
+                             const void* r, void* sign, void* logpsi, void* grad, void* workspace,
+                             size_t workspace_bytes, int32_t* status);
 
 /* Optional intermediate outputs of fire_local_energy (any pointer may be NULL). */
 typedef struct {

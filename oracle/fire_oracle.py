@@ -437,7 +437,10 @@ def _contract(prob, p, r, ei, h, same_pairs, diff_pairs):
         if len(ct) == 0:
             continue
         gamma, edge = _edge_value(p, tag, r[ct], r[nbi], cutoff_eff)
-        np.add.at(h, ct, gamma * silu(edge + mct[ct] + mnb[nbi]))
+        msg = gamma * silu(edge + mct[ct] + mnb[nbi])
+        if np.iscomplexobj(msg) and not np.iscomplexobj(h):
+            h = h.astype(msg.dtype)  # complex-step parameters of the e-e edges (logpsi_jvp)
+        np.add.at(h, ct, msg)
     return h
 
 

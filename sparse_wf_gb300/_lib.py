@@ -36,6 +36,7 @@ SYMBOLS = [
     "fire_mcmc_low_rank_cluster_block",
     "fire_ecp_quadrature",
     "fire_ecp_energy",
+    "fire_logpsi_grad_workspace_size", "fire_logpsi_grad",
 ]
 
 
@@ -107,6 +108,8 @@ def load() -> C.CDLL:
         "fire_profile_report": ([C.c_char_p, sz], i32),
         "fire_gemm_mixed": ([vp, i32, i32, i32, vp, vp, vp, vp, sz, vp], i32),
         "fire_triplets_static": ([vp, P, vp, i32, vp, vp, vp, vp, vp], i32),
+        "fire_logpsi_grad_workspace_size": ([P, i32, C.POINTER(sz)], i32),
+        "fire_logpsi_grad": ([vp, P, vp, vp, vp, vp, vp, vp, vp, sz, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -1758,6 +1758,10 @@ fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, c
 
 }  // namespace
 
+namespace fire {
+void prep_offsets_host(const fire_problem* p, int64_t* off) { prep_offsets(p, off); }
+}  // namespace fire
+
 // ================================================================================== C ABI
 extern "C" {
 
@@ -1911,6 +1915,30 @@ fire_status fire_logpsi(void* stream, const fire_problem* prob, const float* R, 
   if (prob->precision == FIRE_PREC_FP64)
     return run_logpsi<double>(prob, s, R, Z, prepared, r, sign, logpsi, workspace, workspace_bytes, status);
   return run_logpsi<float>(prob, s, R, Z, prepared, r, sign, logpsi, workspace, workspace_bytes, status);
+}
+
+fire_status fire_logpsi_grad_workspace_size(const fire_problem* prob, int32_t chunk, size_t* bytes) {
+  if (!valid(prob) || !bytes) return FIRE_ERR_INVALID;
+  *bytes = fire::grad_workspace_bytes(prob, chunk);
+  return FIRE_OK;
+}
+
+fire_status fire_logpsi_grad(void* stream, const fire_problem* prob, const float* R, const void* prepared,
+                             const void* r, void* sign, void* logpsi, void* grad, void* workspace,
+                             size_t workspace_bytes, int32_t* status) {
+  if (!valid(prob) || !R || !prepared || !r || !sign || !logpsi || !grad || !workspace) return FIRE_ERR_INVALID;
+  if (prob->n_el > ELOC_MAX_EL) return FIRE_ERR_UNSUPPORTED;
+  int64_t off[FIRE_P_COUNT + 1];
+  blob_offsets(prob, off);
+  // the edge bias of each e-e filter follows its edge kernel in the blob (one reduction writes both)
+  if (off[FIRE_P_EESAME_EDGE_B] != off[FIRE_P_EESAME_EDGE_W] + 4 * F ||
+      off[FIRE_P_EEDIFF_EDGE_B] != off[FIRE_P_EEDIFF_EDGE_W] + 4 * F)
+    return FIRE_ERR_UNSUPPORTED;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const fire_status st = fire::grad_dispatch(prob, s, R, prepared, r, sign, logpsi, grad, workspace,
+                                             workspace_bytes, status);
+  if (st != FIRE_OK) return st;
+  return launch_status(__func__);
 }
 
 fire_status fire_local_energy(void* stream, const fire_problem* prob, const float* R, const float* Z,

@@ -118,4 +118,11 @@ struct AssembleOut {
 // > refine_ks, or when its orbital matrices are ill-conditioned: sum_d |w_d| kappa_F(A_d) / |sum_d w_d| > refine_kappa
 // (see fire.h).
 
+// Prepared-parameter slot offsets (elements of the compute type) and the per-walker parameter gradient of log|psi|
+// (fire_grad.cu), behind fire_logpsi_grad.
+void prep_offsets_host(const fire_problem* p, int64_t* off);
+size_t grad_workspace_bytes(const fire_problem* p, int chunk);
+fire_status grad_dispatch(const fire_problem* p, cudaStream_t s, const float* R, const void* prepared, const void* r,
+                          void* sign, void* logpsi, void* grad, void* ws, size_t ws_bytes, int32_t* status);
+
 }  // namespace fire

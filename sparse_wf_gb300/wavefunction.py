@@ -24,7 +24,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .params import ModelDims, init_params, pack_params, param_offsets
+from .params import ModelDims, init_params, pack_params, param_offsets, unpack_params
 from .systems import Molecule, spin_counts
 
 
@@ -172,14 +172,14 @@ class FireWaveFunction:
         static = StaticArgs(half, pairs - half, max(static.n_triplets, int(st[3])), nucs)
         return static.round_with_padding(1.1, self.n_electrons, self.n_up, self.n_nuclei)
 
-    def _run(self, fn, static: StaticArgs, n_walkers: int, retries: int = 4, refine: bool = False):
+    def _run(self, fn, static: StaticArgs, n_walkers: int, retries: int = 4, refine: bool = False, ws_fn=None):
         """Runs fn(problem, workspace) with overflow-driven capacity growth; returns the static used.  With refine
         (the local energy) the refinement capacity follows the device's count of ill-conditioned walkers: a call
         that found more than its capacity is repeated with the count."""
         for _ in range(retries):
             self._status.zero_()
             prob = self._problem(n_walkers, static, refine)
-            fn(prob, self._workspace(prob))
+            fn(prob, ws_fn(prob) if ws_fn is not None else self._workspace(prob))
             st = self._read_status()
             flags = int(st[0])
             if flags & (_lib.FLAG_PAIR_OVERFLOW | _lib.FLAG_NUC_OVERFLOW):
@@ -288,6 +288,53 @@ class FireWaveFunction:
 
     def __call__(self, params, electrons, static: StaticArgs):
         return self.signed(params, electrons, static)[1]
+
+    def logpsi_grad(self, params, electrons, static: StaticArgs, chunk: int = 0, ws_gb: float = 8.0):
+        """Per-walker gradient of log|psi| with respect to every parameter (the rows of the Jacobian that SPRING
+        contracts: ``jax.grad`` of ``log_p`` vmapped over the walkers, ``preconditioner.py:185-191``).
+
+        Returns (grad [B, L] in the blob layout of ``fire_param_layout``, sign [B], log|psi| [B]); ``unflatten_grad``
+        splits a row into the parameter slots.  chunk: walkers per internal pass (0: as many as a workspace of
+        ws_gb gigabytes holds)."""
+        p = self._params(params)
+        r = self._electrons(electrons)
+        B = r.shape[0]
+        L = int(p.offsets[-1])
+        grad = torch.empty((B, L), dtype=self.dtype, device=self.device)
+        sign = torch.empty(B, dtype=self.dtype, device=self.device)
+        logpsi = torch.empty(B, dtype=self.dtype, device=self.device)
+        lib = _lib.load()
+
+        def ws_fn(prob):
+            nbytes = C.c_size_t()
+            c = int(chunk)
+            if c <= 0:
+                _lib.check(lib.fire_logpsi_grad_workspace_size(C.byref(prob), 1, C.byref(nbytes)),
+                           "fire_logpsi_grad_workspace_size")
+                c = max(1, min(B, int(ws_gb * 1e9) // max(1, int(nbytes.value))))
+            prob.chunk_walkers = c
+            _lib.check(lib.fire_logpsi_grad_workspace_size(C.byref(prob), c, C.byref(nbytes)),
+                       "fire_logpsi_grad_workspace_size")
+            need = int(nbytes.value)
+            if self._ws is None or self._ws.numel() < need:
+                self._ws = None
+                self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+            return self._ws
+
+        def fn(prob, ws):
+            _lib.check(lib.fire_logpsi_grad(
+                self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(p.prepared.data_ptr()),
+                C.c_void_p(r.data_ptr()), C.c_void_p(sign.data_ptr()), C.c_void_p(logpsi.data_ptr()),
+                C.c_void_p(grad.data_ptr()), C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel()),
+                C.c_void_p(self._status.data_ptr())), "fire_logpsi_grad")
+
+        self._run(fn, static, B, ws_fn=ws_fn)
+        return grad, sign, logpsi
+
+    def unflatten_grad(self, row) -> dict[str, np.ndarray]:
+        """One gradient row (blob layout) as {slot: array shaped like the parameter}."""
+        row = np.asarray(row.cpu() if isinstance(row, torch.Tensor) else row)
+        return unpack_params(self.dims, row, param_offsets(self.dims))
 
     def local_energy_full(self, params, electrons, static: StaticArgs, debug: bool = False):
         """E_loc per walker plus (log|psi|, sign, (mean, std) in FP64, debug dict, static used)."""

@@ -1,0 +1,71 @@
+"""Per-walker parameter gradient of log|psi| (fire_logpsi_grad) against the oracle's directional derivatives.
+
+The reference builds the rows of SPRING's Jacobian as jax.grad of log|psi| with respect to the flattened parameters,
+vmapped over the walkers (preconditioner.py:185-191).  The oracle's logpsi_jvp gives <grad, v> exactly (complex step)
+for any parameter direction v, so every slot is checked on its own: v random on that slot and zero elsewhere.
+Tolerance per slot and walker: |<g, v> - jvp| <= tol * sum_k |g_k v_k| + tol * 1e-3 * (the largest such sum of the
+walker), tol = 1e-9 in the FP64 build and 1e-4 in FP32 (reverse mode through FP32 value rows; the orbital matrices
+are inverted in double-FP32)."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import case
+from oracle import fire_oracle as O
+from sparse_wf_gb300.params import PARAM_SLOT_NAMES
+from sparse_wf_gb300.wavefunction import FireWaveFunction, StaticArgs
+
+pytestmark = pytest.mark.gpu
+TOL = {"fp64": 1e-9, "fp32": 1e-4}  # measured worst on GB300: 0 (below the floor) and 1.1e-6
+
+
+def _grad(name, precision, n_walkers, chunk=0):
+    mol, nu, r, p, blob, offs = case(name)
+    r = r[:n_walkers]
+    wf = FireWaveFunction(mol, precision=precision)
+    rr = torch.from_numpy(r.astype(np.float64) if precision == "fp64" else r).cuda()
+    s = wf.get_static_input(rr)
+    static = StaticArgs(s.n_pairs_same, s.n_pairs_diff, s.n_triplets, s.n_neighbours_en)
+    g, sign, lp = wf.logpsi_grad(p, rr, static, chunk=chunk)
+    sign_ref, lp_ref = wf.signed(p, rr, static)
+    return mol, nu, r, p, wf, g.double().cpu().numpy(), sign.cpu().numpy(), lp.double().cpu().numpy(), \
+        sign_ref.cpu().numpy(), lp_ref.double().cpu().numpy()
+
+
+@pytest.mark.parametrize("name,precision,n_walkers", [("h10", "fp64", 3), ("h10", "fp32", 3), ("c2h6", "fp64", 2),
+                                                      ("c2h6", "fp32", 2)])
+def test_logpsi_grad_matches_oracle_per_slot(cuda_lib, name, precision, n_walkers):
+    mol, nu, r, p, wf, g, sign, lp, sign_ref, lp_ref = _grad(name, precision, n_walkers)
+    np.testing.assert_array_equal(sign, sign_ref)
+    np.testing.assert_allclose(lp, lp_ref, rtol=1e-10 if precision == "fp64" else 1e-5, atol=0)
+    prob = O.Problem(mol.R, mol.Z, nu)
+    rng = np.random.default_rng(7)
+    tol = TOL[precision]
+    bad, worst = [], 0.0
+    for w in range(len(r)):
+        gw = wf.unflatten_grad(g[w])
+        rw = r[w].astype(np.float64)
+        rows = []
+        for slot in PARAM_SLOT_NAMES:
+            v = rng.standard_normal(np.shape(p[slot]))
+            ref = O.logpsi_jvp(prob, p, rw, {slot: v})
+            rows.append((slot, float(np.sum(gw[slot] * v)), ref, float(np.sum(np.abs(gw[slot] * v)))))
+        # a floor of tol * 1e-3 of the walker's largest slot term: the attention query bias cancels in the softmax,
+        # its exact derivative is 0 and both sides are rounding noise
+        floor = tol * 1e-3 * max(x[3] for x in rows)
+        for slot, got, ref, scale in rows:
+            err = abs(got - ref) / (scale + 1e-300)
+            if abs(got - ref) > floor:
+                worst = max(worst, err)
+            if abs(got - ref) > tol * scale + floor:
+                bad.append((w, slot, got, ref, err))
+    print(f"{name} {precision}: worst |<g,v> - jvp| / sum|g v| = {worst:.2e}")
+    assert not bad, bad[:20]
+
+
+def test_logpsi_grad_chunked_equals_whole(cuda_lib):
+    """Several internal passes (one walker each) give the rows of one pass over the batch."""
+    *_, g1, _, lp1, _, _ = _grad("h10", "fp64", 3)
+    *_, g2, _, lp2, _, _ = _grad("h10", "fp64", 3, chunk=1)
+    np.testing.assert_allclose(g2, g1, rtol=1e-12, atol=1e-12 * np.abs(g1).max())
+    np.testing.assert_allclose(lp2, lp1, rtol=1e-13)

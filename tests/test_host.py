@@ -28,7 +28,7 @@ def header_symbols():
 
 def test_library_exports_every_header_symbol(lib):
     syms = header_symbols()
-    assert len(syms) == 25
+    assert len(syms) == 27
     assert sorted(syms) == sorted(_lib.SYMBOLS)
     for s in syms:
         assert hasattr(lib, s), s
