@@ -58,6 +58,8 @@ def parse():
                     help="single-electron steps of the low-rank block, timed on a copy of the walkers (0: skip)")
     ap.add_argument("--acc-walkers", type=int, default=1024, help="walkers checked against the FP64 build")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
+    ap.add_argument("--grad-walkers", type=int, default=256,
+                    help="walkers of the per-walker parameter-gradient segment (0: skip)")
     ap.add_argument("--serving-requests", type=int, default=20, help="requests of the serving segment (0: skip)")
     ap.add_argument("--serving-rate", type=float, default=200.0, help="offered load, requests per second")
     ap.add_argument("--serving-carbons", default="4,60", help="alkane sizes C_n of the serving requests (min,max)")
@@ -531,6 +533,38 @@ def main():
         for k in e_path:  # walkers of the whole batch that went through the FP64 refinement pass
             accuracy[k]["refined_fraction"] = refined.get(k, 0) / B
 
+    # per-walker gradient of log|psi| with respect to every parameter (the SPRING Jacobian rows) on the first
+    # post-Metropolis walkers: one untimed call, one timed call; rows checked against the FP64 build on 4 walkers
+    param_grad = None
+    Bg = min(args.grad_walkers, B)
+    if Bg > 0:
+        wf._ws = None
+        torch.cuda.empty_cache()
+        rg = r_dev[:Bg].contiguous()
+        out = {}
+
+        def grad_step():
+            out["g"], _, _ = wf.logpsi_grad(dp, rg, static)
+
+        grad_step()
+        ms_g, _ = time_steps(grad_step, 1, stream, dist, world)
+        Kg = min(4, Bg)
+        g32 = out["g"][:Kg].double().cpu().numpy()
+        L = int(out["g"].shape[1])
+        del out["g"]
+        wf._ws = None
+        torch.cuda.empty_cache()
+        wf64g = FireWaveFunction(mol, precision="fp64", device=dev)
+        r64g = r_dev[:Kg].double()
+        g64 = wf64g.logpsi_grad(params, r64g, wf64g.get_static_input(r64g))[0].cpu().numpy()
+        del wf64g
+        torch.cuda.empty_cache()
+        rel_row = np.linalg.norm(g32 - g64, axis=1) / np.linalg.norm(g64, axis=1)
+        param_grad = {"walkers": Bg * world, "ms": ms_g, "walker_grads_per_s": Bg * world / (ms_g / 1e3),
+                      "params_per_walker": L, "output_gb": Bg * L * 4 / 1e9,
+                      "precision": "fp32 (reverse mode on the CUDA cores)",
+                      "fp32_vs_fp64_row_rel_err_max": float(rel_row.max()), "checked_walkers": Kg}
+
     # serving segment: Poisson-arriving E_loc / 10-step MCMC requests of mixed molecule sizes (rank 0)
     serving = None
     if rank == 0 and args.serving_requests > 0:
@@ -602,7 +636,7 @@ def main():
             "gpu_launches": int(prof.get("kernels_launched", (0, 0))[0]) * args.steps,
             "fp32_path": fp32, "mixed_over_fp32": (value / fp32["value"]) if fp32 else None,
             "accuracy": accuracy, "mcmc": mcmc, "serving": serving, "ragged": ragged, "stages_ms": stages,
-            "oracle_check": check,
+            "oracle_check": check, "param_grad": param_grad,
         }
         print(json.dumps(line))
     if world > 1:

@@ -33,7 +33,8 @@ def _grad(name, precision, n_walkers, chunk=0):
 
 
 @pytest.mark.parametrize("name,precision,n_walkers", [("h10", "fp64", 3), ("h10", "fp32", 3), ("c2h6", "fp64", 2),
-                                                      ("c2h6", "fp32", 2)])
+                                                      ("c2h6", "fp32", 2), ("c10h22", "fp64", 1),
+                                                      ("c10h22", "fp32", 1)])
 def test_logpsi_grad_matches_oracle_per_slot(cuda_lib, name, precision, n_walkers):
     mol, nu, r, p, wf, g, sign, lp, sign_ref, lp_ref = _grad(name, precision, n_walkers)
     np.testing.assert_array_equal(sign, sign_ref)
