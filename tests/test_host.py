@@ -408,6 +408,73 @@ def test_checkpoint_round_trip_and_reference_mapping(tmp_path):
                                                                          if k != "cusp"})
 
 
+def _reference_tree(p):
+    """The nested leaf dict of a reference MoonLikeParams built from parameter slots through REFERENCE_LEAVES
+    (scalar slots split into their scalar leaves, stored with shape ())."""
+    from sparse_wf_gb300.checkpoint import REFERENCE_LEAVES
+
+    flat = {}
+    for slot, src in REFERENCE_LEAVES.items():
+        if isinstance(src, tuple):
+            for q, v in zip(src, np.asarray(p[slot]).reshape(-1)):
+                flat[q] = np.asarray(v, np.float32).reshape(())
+        else:
+            flat[src] = np.asarray(p[slot], np.float32)
+    tree = {}
+    for path, v in flat.items():
+        node = tree
+        *head, leaf = path.split("/")
+        for h in head:
+            node = node.setdefault(h, {})
+        node[leaf] = v
+    return flat, tree
+
+
+def test_reference_checkpoint_default_mapping_npz_and_msgpack(tmp_path):
+    """The default leaf mapping reads an expanded params.npz (tree_to_flat_dict paths, loggers.py:191-208) and a flax
+    msgpack TrainingState (api.py:294-331) written with flax's extension types (1 = ndarray, 3 = numpy scalar) into
+    the same parameter slots; extra optimizer leaves are reported, a wrong shape raises."""
+    from sparse_wf_gb300 import checkpoint, params as P
+
+    dims = P.ModelDims(6, 3, 4)
+    p = P.init_params(dims, 3)
+    p["scales"] = np.array([0.7, 1.3])
+    flat, tree = _reference_tree(p)
+    (tmp_path / "exp").mkdir()
+    np.savez(tmp_path / "exp" / "params.npz", **flat)
+    got = checkpoint.load_reference_params(str(tmp_path / "exp"), dims)
+    for k in p:
+        np.testing.assert_array_equal(got["params"][k], np.asarray(p[k], np.float32).astype(np.float64), err_msg=k)
+    assert got["unused_leaves"] == []
+    msgpack = pytest.importorskip("msgpack")
+
+    def ext(o):
+        if isinstance(o, np.ndarray):
+            return msgpack.ExtType(1, msgpack.packb((o.shape, o.dtype.name, o.tobytes("C")), use_bin_type=True))
+        if isinstance(o, np.generic):
+            return msgpack.ExtType(3, msgpack.packb((o.dtype.name, o.tobytes()), use_bin_type=True))
+        raise TypeError(type(o))
+
+    r = np.random.default_rng(0).standard_normal((5, 6, 3)).astype(np.float32)
+    state = {"key": np.array([0, 42], np.uint32), "params": tree, "electrons": r,
+             "opt_state": {"natgrad": {"last_grad": np.zeros(7, np.float32)}}, "step": np.int64(123),
+             "width_state": {"width": np.float32(0.1), "pmoves": np.zeros(20, np.float32), "i": 3}}
+    (tmp_path / "chkpt000123.msgpk").write_bytes(msgpack.packb(state, default=ext, use_bin_type=True))
+    got = checkpoint.load_reference_msgpack(str(tmp_path / "chkpt000123.msgpk"), dims)
+    for k in p:
+        np.testing.assert_array_equal(got["params"][k], np.asarray(p[k], np.float32).astype(np.float64), err_msg=k)
+    np.testing.assert_array_equal(got["electrons"], r)
+    assert got["step"] == 123 and got["unused_leaves"] == []
+    leaves = checkpoint.read_reference_msgpack(str(tmp_path / "chkpt000123.msgpk"))
+    assert leaves["width_state/i"] == 3 and leaves["opt_state/natgrad/last_grad"].shape == (7,)
+    bad = dict(flat)
+    bad["to_orbitals/params/to_orbitals_up/kernel"] = np.zeros((3, 3), np.float32)
+    (tmp_path / "bad").mkdir()
+    np.savez(tmp_path / "bad" / "params.npz", **bad)
+    with pytest.raises(ValueError):
+        checkpoint.load_reference_params(str(tmp_path / "bad"), dims)
+
+
 def test_ragged_autotuner_selection(monkeypatch):
     """ragged.Autotuner without a GPU (RaggedBatch and the CUDA calls faked): candidates whose workspaces exceed the
     HBM budget are not built, the fastest of the rest is kept per batch signature (a second call is a cache hit),
