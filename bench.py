@@ -138,6 +138,12 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, ncu) of the tensor-core contractions of one mixed-path
+# C40H82 local energy, per walker: 6.615 GB over the 25 k_gemm_tca / k_env_tc launches of a 16-walker step.  Every
+# launch's rows, and so its traffic, grow in proportion to the walkers.
+TC_TRAFFIC_PER_WALKER = {("c40h82", "mixed"): 6.615e9 / 16}
+
+
 def gemm_flops(n, N, pairs, value_rows=True, derivative_rows=True):
     """Algorithmic FLOPs (2 per multiply-add) of the dense contractions of one walker's E_loc: of the value rows
     (one per node), of the derivative rows (Jacobian and Laplacian rows; the mixed path's tensor-core share), or
@@ -459,8 +465,10 @@ def main():
         g_ms = prof.get("gemm", (0, 0.0))[1] + prof.get("gemm_comp", (0, 0.0))[1]
         kernel = "all dense contractions of one step (CUDA cores: k_gemm, k_gemm_comp)"
     achieved = flops / (g_ms / 1e3) / 1e12
+    tpw = TC_TRAFFIC_PER_WALKER.get((args.system, args.precision))
+    traffic = tpw * B / max(g_launches, 1) if tpw else None  # bytes per launch, like achieved
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "kernel": kernel, "launches": g_launches,
+                "frac": achieved / peak, "traffic": traffic, "kernel": kernel, "launches": g_launches,
                 "avg_launch_ms": g_ms / max(g_launches, 1), "peak_source": f"bf16 dense sustained, {peak_kind}",
                 "flops_per_step": flops}
     # the CUDA-core value-row contractions beside it (compensated; their FLOPs over their launches' time)

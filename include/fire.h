@@ -44,7 +44,7 @@ extern "C" {
 
 #define FIRE_NO_NEIGHBOUR 1000000 /* model/graph_utils.py:14 NO_NEIGHBOUR */
 #define FIRE_STATUS_WORDS 8
-#define FIRE_ABI_VERSION 2
+#define FIRE_ABI_VERSION 3
 
 typedef enum {
   FIRE_OK = 0,
@@ -98,6 +98,8 @@ typedef struct {
   float refine_kappa;    /* ... or when its determinant-weighted condition number
                             sum_d |w_d| kappa_F(A_d) / |sum_d w_d| exceeds refine_kappa (<= 0: FIRE_REFINE_KAPPA) */
   float refine_ks;       /* ... or when (|lap| + |grad|^2) / 2 exceeds refine_ks Hartree (<= 0: FIRE_REFINE_KS) */
+  float refine_kscond;   /* ... or when (|lap| + |grad|^2) / 2 times that condition number exceeds refine_kscond Hartree
+                            (<= 0: FIRE_REFINE_KSCOND) */
 } fire_problem;
 
 /* Defaults of the ill-conditioned test.  After compensation the FP32 value planes move E_loc by ~1e-7 of the
@@ -107,6 +109,10 @@ typedef struct {
 #define FIRE_REFINE_RATIO 100.0f
 #define FIRE_REFINE_KAPPA 1.0e6f
 #define FIRE_REFINE_KS 1.0e5f
+/* The compensated value planes leave E_loc errors of ~(1-4)e-12 (|lap| + |grad|^2) / 2 kappa on C40H82 walkers
+ * (kappa the determinant-weighted condition number): the product bound catches the walkers whose terms and
+ * conditioning are each below their own bound but whose error is several mHa. */
+#define FIRE_REFINE_KSCOND 1.0e10f
 
 /* Parameter slots of the flat parameter blob (float32), in blob order.  Shapes with
  * F = 256, D = 4 determinants, n = n_el, N = n_nuc are given by fire_param_layout. */

@@ -46,6 +46,7 @@ class Problem(C.Structure):
         ("cutoff", C.c_float), ("cutoff_1el", C.c_float), ("cap_pairs", C.c_int32), ("cap_nuc", C.c_int32),
         ("precision", C.c_int32), ("chunk_walkers", C.c_int32), ("refine_cap", C.c_int32),
         ("refine_ratio", C.c_float), ("refine_kappa", C.c_float), ("refine_ks", C.c_float),
+        ("refine_kscond", C.c_float),
     ]
 
 

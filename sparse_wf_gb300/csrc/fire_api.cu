@@ -1067,6 +1067,7 @@ cudaError_t chunk_eloc(Ctx<T>& c, void* logpsi, void* sign, void* eloc, const fi
     o.ref_ratio = c.p->refine_ratio > 0.f ? (double)c.p->refine_ratio : (double)FIRE_REFINE_RATIO;
     o.ref_kappa = c.p->refine_kappa > 0.f ? (double)c.p->refine_kappa : (double)FIRE_REFINE_KAPPA;
     o.ref_ks = c.p->refine_ks > 0.f ? (double)c.p->refine_ks : (double)FIRE_REFINE_KS;
+    o.ref_kscond = c.p->refine_kscond > 0.f ? (double)c.p->refine_kscond : (double)FIRE_REFINE_KSCOND;
     o.cond = c.template buf<double>(c.P.cond);
   }
   Prof pr("assemble", c.s);

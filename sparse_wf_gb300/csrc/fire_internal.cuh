@@ -105,6 +105,7 @@ struct AssembleOut {
   double ref_ratio;
   double ref_kappa;
   double ref_ks;
+  double ref_kscond;
   // input: kappa_F of every orbital matrix of the launch [Wc * NDET] (null: the condition test is skipped)
   const double* cond;
   // output rows: walker w of the launch writes row wmap[w] when w < *wcnt and nothing otherwise (null: w0 + w)
@@ -115,7 +116,8 @@ struct AssembleOut {
 // A walker is ill-conditioned, and its orbital-matrix values are recomputed in FP64 by the refinement pass of
 // the FP32 and mixed local energy, when the two terms that cancel in its kinetic energy exceed its local energy by
 // the problem's refine_ratio or its refine_ks Hartree: (|lap log psi| + |grad log psi|^2) / 2 > refine_ratio |E_loc| or
-// > refine_ks, or when its orbital matrices are ill-conditioned: sum_d |w_d| kappa_F(A_d) / |sum_d w_d| > refine_kappa
+// > refine_ks, or when its orbital matrices are ill-conditioned: sum_d |w_d| kappa_F(A_d) / |sum_d w_d| > refine_kappa,
+// or when the product of the two, (|lap| + |grad|^2) / 2 times that condition number, exceeds refine_kscond
 // (see fire.h).
 
 // Prepared-parameter slot offsets (elements of the compute type) and the per-walker parameter gradient of log|psi|

@@ -436,7 +436,8 @@ __global__ void __launch_bounds__(256) k_assemble(int n, int n_up, int N, int w0
     }
     if (out.dbg.cond && !out.wmap) out.dbg.cond[row] = cw;
     const double ks = 0.5 * (fabs(lap) + vv[0]);
-    if (out.ref_idx && !(ks <= out.ref_ratio * fabs(eloc) && ks <= out.ref_ks && cw <= out.ref_kappa)) {
+    if (out.ref_idx &&
+        !(ks <= out.ref_ratio * fabs(eloc) && ks <= out.ref_ks && cw <= out.ref_kappa && ks * cw <= out.ref_kscond)) {
       const int slot = atomicAdd(out.ref_cnt, 1);
       if (slot < out.ref_cap) out.ref_idx[slot] = (int32_t)row;
     }

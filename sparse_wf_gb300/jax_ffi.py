@@ -4,7 +4,8 @@ The reference evaluates ``local_energy(key, params, electrons, static)`` per wal
 ``batched_energy_fn`` (``update.py:95-100``) inside ``jax.pmap`` (``update.py:221-222``), and its Metropolis step
 ``MCStep`` (``mcmc.py:329-344``) the same way.  ``local_energy`` and ``mcmc_block`` below are one XLA custom call
 each over the whole walker batch, served by the handlers of ``xla/fire_xla.cc`` (``FireLocalEnergy``,
-``FireMcmcBlock``) on top of ``libfire.so``; the library's workspace comes from XLA's scratch allocator.
+``FireMcmcBlock``) on top of ``libfire.so``; ``logpsi_grad`` (``FireLogpsiGrad``) gives the per-walker parameter
+gradient that the dense SPRING preconditioner contracts (``preconditioner.py:190-191``); the library's workspace comes from XLA's scratch allocator.
 
 Parameters go in as the prepared buffer of ``fire_prepare_params`` (``DeviceParams.prepared`` as a uint8 array).
 The status words come back as an output: a set flag in ``status[0]`` means the capacities in ``static`` were too
@@ -44,6 +45,7 @@ def _register():
     lib = ctypes.cdll.LoadLibrary(str(XLA_LIB))
     jax.ffi.register_ffi_target("fire_local_energy", jax.ffi.pycapsule(lib.FireLocalEnergy), platform="CUDA")
     jax.ffi.register_ffi_target("fire_mcmc_block", jax.ffi.pycapsule(lib.FireMcmcBlock), platform="CUDA")
+    jax.ffi.register_ffi_target("fire_logpsi_grad", jax.ffi.pycapsule(lib.FireLogpsiGrad), platform="CUDA")
     _registered = True
 
 
@@ -85,3 +87,20 @@ def mcmc_block(prepared, R, Z, electrons, logpsi, static, n_up, steps, width, se
     return jax.ffi.ffi_call("fire_mcmc_block", out)(
         R, Z, prepared, electrons, logpsi, steps=np.int32(steps), width=np.float32(width), seed=np.int64(seed),
         counter=np.int64(counter), **_attrs(static, n_up, precision, cutoff, cutoff_1el, chunk))
+
+
+def logpsi_grad(prepared, R, electrons, static, n_up, n_params, cutoff=5.0, cutoff_1el=20.0, chunk=0):
+    """Per-walker gradient of log|psi| with respect to every parameter (``jac_fn`` of the dense SPRING
+    preconditioner, ``preconditioner.py:190-191``, as rows): electrons [B, n, 3] float32 -> (grad [B, n_params] in
+    the blob layout of ``fire_param_layout``, logpsi [B], sign [B], status [8]).  chunk: walkers per internal pass
+    (0: the whole batch in one workspace)."""
+    import jax
+    import jax.numpy as jnp
+
+    _register()
+    B = electrons.shape[0]
+    out = (jax.ShapeDtypeStruct((B, n_params), jnp.float32), jax.ShapeDtypeStruct((B,), jnp.float32),
+           jax.ShapeDtypeStruct((B,), jnp.float32), jax.ShapeDtypeStruct((8,), jnp.int32))
+    attrs = _attrs(static, n_up, 0, cutoff, cutoff_1el, chunk)
+    del attrs["precision"]
+    return jax.ffi.ffi_call("fire_logpsi_grad", out)(R, prepared, electrons, **attrs)

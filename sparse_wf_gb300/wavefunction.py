@@ -105,13 +105,14 @@ class FireWaveFunction:
         self._status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=self.device)
         self._lr_cap = 0  # changed-set capacity of the last low-rank block (grown on overflow, like the statics)
         # FP32 / mixed local energy: ill-conditioned walkers ((|lap| + |grad|^2) / 2 above refine_ratio |E_loc| or
-        # refine_ks Hartree, or a determinant-weighted condition number of the orbital matrices above refine_kappa) are
-        # evaluated again with FP64 orbital-matrix values; the capacity of that pass follows the counts the device
+        # refine_ks Hartree, a determinant-weighted condition number of the orbital matrices above refine_kappa, or the
+        # product of the two above refine_kscond) are evaluated again with FP64 orbital-matrix values; the capacity of that pass follows the counts the device
         # reports (the defaults of fire.h)
         self.refine = precision != "fp64"
         self.refine_ratio = 100.0
         self.refine_kappa = 1.0e6
         self.refine_ks = 1.0e5
+        self.refine_kscond = 1.0e10
         self._refine_cap = 0
         self.last_refined = 0
         _lib.load()
@@ -134,7 +135,7 @@ class FireWaveFunction:
         return _lib.Problem(self.n_electrons, self.n_up, self.n_nuclei, int(n_walkers), self.cutoff,
                             self.cutoff_1el, max(1, int(cap_p)), max(1, int(cap_n)), _lib.PREC[self.precision],
                             self.chunk_walkers, cap_r, float(self.refine_ratio), float(self.refine_kappa),
-                            float(self.refine_ks))
+                            float(self.refine_ks), float(self.refine_kscond))
 
     def _workspace(self, prob: _lib.Problem, cap_changed: int = 0) -> torch.Tensor:
         """Workspace of the local-energy and value paths, or (cap_changed > 0) of the low-rank block."""

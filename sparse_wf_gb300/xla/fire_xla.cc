@@ -1,6 +1,7 @@
-// fire_xla.cc -- XLA FFI handlers over libfire.so: the local-energy and Metropolis-block custom calls that replace
-// the reference's jitted per-walker calls (batched_energy_fn, update.py:95-100, 153-157; MCStep, mcmc.py:329-344)
-// with one call over the whole walker batch.  Compiled only where jaxlib ships the FFI header
+// fire_xla.cc -- XLA FFI handlers over libfire.so: the local-energy, Metropolis-block and parameter-gradient custom
+// calls that replace the reference's jitted per-walker calls (batched_energy_fn, update.py:95-100, 153-157; MCStep,
+// mcmc.py:329-344; jac_fn = batched_vmap(jax.grad(log_p)), preconditioner.py:190-191) with one call over the whole
+// walker batch.  Compiled only where jaxlib ships the FFI header
 // (jax.ffi.include_dir()), and linked with libfire.so.
 //
 // Every buffer comes from XLA; the library's workspace is taken from XLA's scratch allocator, so no cudaMalloc runs
@@ -95,6 +96,29 @@ ffi::Error McmcBlock(cudaStream_t stream, ffi::ScratchAllocator scratch, ffi::Bu
   return to_error(st, "fire_mcmc_block");
 }
 
+// electrons [B, n_el, 3] float32 -> grad [B, L] (d log|psi| / d parameter, the blob layout of fire_param_layout),
+// logpsi [B], sign [B]: the rows of SPRING's Jacobian.
+ffi::Error LogpsiGrad(cudaStream_t stream, ffi::ScratchAllocator scratch, ffi::Buffer<ffi::F32> R,
+                      ffi::Buffer<ffi::U8> prepared, ffi::Buffer<ffi::F32> r, int32_t n_up, float cutoff,
+                      float cutoff_1el, int32_t cap_pairs, int32_t cap_nuc, int32_t chunk,
+                      ffi::ResultBuffer<ffi::F32> grad, ffi::ResultBuffer<ffi::F32> logpsi,
+                      ffi::ResultBuffer<ffi::F32> sign, ffi::ResultBuffer<ffi::S32> status) {
+  const auto d = r.dimensions();
+  if (d.size() != 3 || d[2] != 3)
+    return ffi::Error(ffi::ErrorCode::kInvalidArgument, "fire_logpsi_grad: electrons must be float32 [B, n_el, 3]");
+  fire_problem p = make_problem(d[0], d[1], R.dimensions()[0], n_up, cutoff, cutoff_1el, cap_pairs, cap_nuc,
+                                FIRE_PREC_FP32, chunk);
+  size_t bytes = 0;
+  fire_status st = fire_logpsi_grad_workspace_size(&p, chunk, &bytes);
+  if (st != FIRE_OK) return to_error(st, "fire_logpsi_grad_workspace_size");
+  auto ws = scratch.Allocate(bytes, 256);
+  if (!ws.has_value()) return ffi::Error(ffi::ErrorCode::kResourceExhausted, "fire_logpsi_grad: workspace");
+  cudaMemsetAsync(status->typed_data(), 0, FIRE_STATUS_WORDS * sizeof(int32_t), stream);
+  st = fire_logpsi_grad(stream, &p, R.typed_data(), prepared.typed_data(), r.typed_data(), sign->typed_data(),
+                        logpsi->typed_data(), grad->typed_data(), *ws, bytes, status->typed_data());
+  return to_error(st, "fire_logpsi_grad");
+}
+
 }  // namespace
 
 XLA_FFI_DEFINE_HANDLER_SYMBOL(FireLocalEnergy, LocalEnergy,
@@ -142,4 +166,22 @@ XLA_FFI_DEFINE_HANDLER_SYMBOL(FireMcmcBlock, McmcBlock,
                                   .Ret<ffi::Buffer<ffi::F32>>()   // log|psi| after the block
                                   .Ret<ffi::Buffer<ffi::S32>>()   // accepted moves per walker
                                   .Ret<ffi::Buffer<ffi::S32>>()   // static maxima [4]
+                                  .Ret<ffi::Buffer<ffi::S32>>());  // status words
+
+XLA_FFI_DEFINE_HANDLER_SYMBOL(FireLogpsiGrad, LogpsiGrad,
+                              ffi::Ffi::Bind()
+                                  .Ctx<ffi::PlatformStream<cudaStream_t>>()
+                                  .Ctx<ffi::ScratchAllocator>()
+                                  .Arg<ffi::Buffer<ffi::F32>>()  // R
+                                  .Arg<ffi::Buffer<ffi::U8>>()   // prepared parameters
+                                  .Arg<ffi::Buffer<ffi::F32>>()  // electrons
+                                  .Attr<int32_t>("n_up")
+                                  .Attr<float>("cutoff")
+                                  .Attr<float>("cutoff_1el")
+                                  .Attr<int32_t>("cap_pairs")
+                                  .Attr<int32_t>("cap_nuc")
+                                  .Attr<int32_t>("chunk")
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // gradient rows [B, L]
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // logpsi
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // sign
                                   .Ret<ffi::Buffer<ffi::S32>>());  // status words

@@ -32,7 +32,7 @@ def test_library_exports_every_header_symbol(lib):
     assert sorted(syms) == sorted(_lib.SYMBOLS)
     for s in syms:
         assert hasattr(lib, s), s
-    assert lib.fire_abi_version() == 2
+    assert lib.fire_abi_version() == 3
 
 
 def test_header_slot_enum_matches_python():
