@@ -804,6 +804,22 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
   g.ldb = DN; g.C = c.template buf<T>(c.P.lapA); g.ldc = DN; g.M = G; g.N = DN; g.K = F; g.n_el = n; g.n_up = nu;
   g.aux1 = env; g.aux2 = c.template buf<T>(c.P.rjs); g.aux3 = c.template buf<T>(c.P.rawx); g.ld_aux = DN;
   g.env_nv = 5;
+  if constexpr (sizeof(T) == 4) {
+    if (c.mixed) {
+      // the Laplacian rows' product rule reads nine planes per output; as the tensor-core epilogue it left the MMAs
+      // idle (one CTA of 8 epilogue warps per SM), so the contraction stores plain values and a streaming kernel
+      // at full occupancy applies the rule in place
+      GemmP<T> gp = g;
+      gp.aux0 = nullptr; gp.aux1 = nullptr; gp.aux2 = nullptr; gp.aux3 = nullptr; gp.env_nv = 1;
+      const cudaError_t e = gemm<T, EPI_PLAIN>(c, gp, TC_ORB_UP);
+      if (e != cudaSuccess) return e;
+      const long q = (long)G * (DN / 4);
+      g_nlaunch++;
+      k_orb_lap<<<nblk(q), 256, 0, c.s>>>(c.template buf<float>(c.P.lapA), env, c.template buf<float>(c.P.rawx),
+                                          c.template buf<float>(c.P.rjs), G, DN);
+      return cudaPeekAtLastError();
+    }
+  }
   gemm<T, EPI_ORB_L>(c, g, TC_ORB_UP);
   return cudaPeekAtLastError();
 }

@@ -608,6 +608,30 @@ __global__ void __launch_bounds__(NT) k_detlap(Nbr nb, Layout L, const T* __rest
   }
 }
 
+// One thread per 4 consecutive orbital columns of one electron (DN % 4 == 0, every plane 16-byte aligned).  env: the
+// envelope carrier [G][5][DN] (value, Jacobian xyz, Laplacian), raw [G][DN], rjs: the raw orbitals' self Jacobian
+// rows [G][3][DN] (written by the Jacobian contraction's epilogue).
+__global__ void k_orb_lap(float* __restrict__ lapA, const float* __restrict__ env, const float* __restrict__ raw,
+                          const float* __restrict__ rjs, long G, int DN) {
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x, nq = (long)DN / 4;
+  if (q >= G * nq) return;
+  const long g = q / nq;
+  const int c = (int)(q - g * nq) * 4;
+  const float* e = env + g * 5 * DN + c;
+  const float* rj = rjs + g * 3 * DN + c;
+  float4* out = reinterpret_cast<float4*>(lapA + g * DN + c);
+  const float4 a = *out, ex = *reinterpret_cast<const float4*>(e), el = *reinterpret_cast<const float4*>(e + 4 * DN),
+               rw = *reinterpret_cast<const float4*>(raw + g * DN + c);
+  float4 v = make_float4(a.x * ex.x + el.x * rw.x, a.y * ex.y + el.y * rw.y, a.z * ex.z + el.z * rw.z,
+                         a.w * ex.w + el.w * rw.w);
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const float4 r = *reinterpret_cast<const float4*>(rj + t * DN), ej = *reinterpret_cast<const float4*>(e + (1 + t) * DN);
+    v.x += 2.f * r.x * ej.x; v.y += 2.f * r.y * ej.y; v.z += 2.f * r.z * ej.z; v.w += 2.f * r.w * ej.w;
+  }
+  *out = v;
+}
+
 template __global__ void k_env_coef<float, 1>(const float*, const float*, const float*, int, int, int, int, int,
                                               float*);
 template __global__ void k_env_coef<float, 5>(const float*, const float*, const float*, int, int, int, int, int,

@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(256) gk_wgrad(WgP<T> p) {
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) c[a][b] = T(0);
+#pragma unroll
   for (int sg = 0; sg < 2; ++sg) {
     const int rows = p.s[sg].rows;
     const long rb = p.s[sg].base + (long)w * p.s[sg].wstride;
@@ -194,6 +195,49 @@ __global__ void __launch_bounds__(256) gk_wgrad(WgP<T> p) {
       else
         p.bias[(long)w * p.ldw + nc] = c[u][v];
     }
+  }
+}
+
+// The same reduction for K + (bias ? 1 : 0) <= 16 over many rows (the edge and pair filters' 4- to 16-row weights):
+// one CTA per 64 columns and walker, 4 row groups of 64 threads; each thread keeps its column's K sums in registers
+// (the X row is a broadcast load, the Y row a coalesced one) and the row groups are summed through shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) gk_wgrad_skinny(WgP<T> p) {
+  constexpr int KS = 16;
+  __shared__ T red[3][KS][64];
+  const int c = threadIdx.x & 63, rg = threadIdx.x >> 6;
+  const int n0 = blockIdx.x * 64, w = blockIdx.z, nc = n0 + c;
+  T acc[KS];
+#pragma unroll
+  for (int k = 0; k < KS; ++k) acc[k] = T(0);
+  if (nc < p.N) {
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+      const long rb = p.s[sg].base + (long)w * p.s[sg].wstride;
+      for (int r = rg; r < p.s[sg].rows; r += 4) {
+        const T* x = p.X + (rb + r) * p.ldx;
+        const T y = p.Y[(rb + r) * p.ldy + nc];
+#pragma unroll
+        for (int k = 0; k < KS; ++k) {
+          const T xv = k < p.K ? x[k] : (k == p.K && p.bias ? T(1) : T(0));
+          acc[k] += xv * y;
+        }
+      }
+    }
+  }
+  if (rg > 0) {
+#pragma unroll
+    for (int k = 0; k < KS; ++k) red[rg - 1][k][c] = acc[k];
+  }
+  __syncthreads();
+  if (rg > 0 || nc >= p.N) return;
+#pragma unroll
+  for (int k = 0; k < KS; ++k) {
+    const T v = acc[k] + red[0][k][c] + red[1][k][c] + red[2][k][c];
+    if (k < p.K)
+      p.out[(long)w * p.ldw + (long)(k / p.grp) * p.grp_stride + (long)(k % p.grp) * p.ldo + nc] = v;
+    else if (k == p.K && p.bias)
+      p.bias[(long)w * p.ldw + nc] = v;
   }
 }
 
@@ -1231,6 +1275,10 @@ template <typename T>
 void wgrad(cudaStream_t s, int Wc, WgP<T> p) {
   const int Ke = p.K + (p.bias ? 1 : 0);
   if (p.grp <= 0) p.grp = p.K > 0 ? p.K : 1;
+  if (Ke <= 16) {
+    gk_wgrad_skinny<T><<<dim3((unsigned)((p.N + 63) / 64), 1, (unsigned)Wc), 256, 0, s>>>(p);
+    return;
+  }
   dim3 grid((unsigned)((p.N + 63) / 64), (unsigned)((Ke + 63) / 64), (unsigned)Wc);
   gk_wgrad<T><<<grid, 256, 0, s>>>(p);
 }

@@ -32,6 +32,9 @@ __global__ void k_lr_contract(const T* rn, int n, int n_up, T cutoff, const int*
                               const int* S_cnt, int KS, Weights<T> W, const T* E5, const T* E5p, T* HS);
 
 // fire_det.cu
+// Orbital Laplacian rows from the plain contraction of the embedding's Laplacian rows (in place):
+// lapA = lap_raw env + raw lap_env + 2 sum_xyz raw_jac env_jac  (the product rule of the orbital x envelope).
+__global__ void k_orb_lap(float* lapA, const float* env, const float* raw, const float* rjs, long G, int DN);
 template <typename T, int NV>
 __global__ void k_env_coef(const T* r, const float* R, const T* sp, int n, int n_s, int s_off, int N, int Wn,
                            T* coef);
