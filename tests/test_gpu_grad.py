@@ -70,3 +70,26 @@ def test_logpsi_grad_chunked_equals_whole(cuda_lib):
     *_, g2, _, lp2, _, _ = _grad("h10", "fp64", 3, chunk=1)
     np.testing.assert_allclose(g2, g1, rtol=1e-12, atol=1e-12 * np.abs(g1).max())
     np.testing.assert_allclose(lp2, lp1, rtol=1e-13)
+
+
+def test_logpsi_grad_c40h82_fp32_against_fp64_build(cuda_lib):
+    """At the benchmark molecule (C40H82, 2 walkers) the FP32 rows against the FP64 build's rows of the same
+    kernels (the FP64 build matches the oracle slot by slot on the smaller molecules): 1e-3 of the row norm."""
+    from make_golden import make_params
+    from sparse_wf_gb300 import systems
+
+    mol = systems.alkane(40)
+    nu, _ = systems.spin_counts(mol)
+    r = systems.init_electrons(mol, 2, 1000)
+    _, p, _, _ = make_params(mol, nu, r[0], seed=0, activate=True)
+    rows = {}
+    for prec in ("fp32", "fp64"):
+        wf = FireWaveFunction(mol, precision=prec)
+        rr = torch.from_numpy(r.astype(np.float64) if prec == "fp64" else r).cuda()
+        s = wf.get_static_input(rr)
+        g, _, _ = wf.logpsi_grad(p, rr, StaticArgs(s.n_pairs_same, s.n_pairs_diff, s.n_triplets, s.n_neighbours_en))
+        rows[prec] = g.double().cpu().numpy()
+    err = np.linalg.norm(rows["fp32"] - rows["fp64"], axis=1) / np.linalg.norm(rows["fp64"], axis=1)
+    print(f"C40H82 FP32 vs FP64 gradient rows: {err}")
+    assert np.all(err < 1e-3), err
+
