@@ -1235,9 +1235,13 @@ GPlan make_gplan(const fire_problem* p, int Wc) {
   return P;
 }
 
+// Walkers per pass: prob->chunk_walkers when its plan fits the workspace (0 when it does not), else the most that fit.
 int grad_chunk(const fire_problem* p, size_t ws_bytes) {
   const int B = p->n_walkers;
-  if (p->chunk_walkers > 0) return std::min(p->chunk_walkers, B);
+  if (p->chunk_walkers > 0) {
+    const int c = std::min(p->chunk_walkers, B);
+    return make_gplan(p, c).total <= ws_bytes ? c : 0;
+  }
   int lo = 1, hi = B;
   if (make_gplan(p, 1).total > ws_bytes) return 0;
   while (lo < hi) {

@@ -109,6 +109,29 @@ def test_low_rank_block_sizes_and_argument_checks(lib):
     assert call(big, 32) == 2
 
 
+def test_logpsi_grad_sizes_and_argument_checks(lib):
+    """fire_logpsi_grad_workspace_size grows with the walkers per pass; fire_logpsi_grad rejects a workspace too small
+    for the requested pass (FIRE_ERR_WORKSPACE, 3), more than 798 electrons (2) and missing outputs (1) before any CUDA
+    call (the pointers are never dereferenced)."""
+    prob = _lib.Problem(82, 41, 32, 64, 5.0, 20.0, 2500, 40, 0, 0)
+    a, b = C.c_size_t(), C.c_size_t()
+    assert lib.fire_logpsi_grad_workspace_size(C.byref(prob), 4, C.byref(a)) == 0
+    assert lib.fire_logpsi_grad_workspace_size(C.byref(prob), 8, C.byref(b)) == 0
+    assert b.value > a.value > 0
+    dummy = C.c_void_p(16)
+
+    def call(pr, ws_bytes, grad=dummy):
+        return lib.fire_logpsi_grad(None, C.byref(pr), dummy, dummy, dummy, dummy, dummy, grad, dummy,
+                                    C.c_size_t(ws_bytes), dummy)
+
+    prob.chunk_walkers = 8
+    assert call(prob, a.value) == 3  # the plan of 8 walkers per pass does not fit 4 walkers' workspace
+    assert call(prob, 1) == 3
+    assert call(prob, b.value, grad=None) == 1
+    big = _lib.Problem(800, 400, 100, 4, 5.0, 20.0, 100, 10, 0, 0)
+    assert call(big, b.value) == 2
+
+
 def test_static_padding_mirrors_reference():
     from sparse_wf_gb300.wavefunction import StaticArgs
 
