@@ -253,25 +253,16 @@ __device__ __forceinline__ void tc_store4(const GemmP<float>& p, int row, int no
   st4(p.C + (long)row * p.ldc + col, tc_val4<MODE>(p, row, node, col, a, spin));
 }
 
-// The per-center operand of the SiLU and orbital Jacobian epilogues for 16 columns (silu' of the center's row, or the
-// center's envelope values), loaded at the start of a chunk so that its L2 latency overlaps the chunk's TMEM loads and
-// (SILU_J) its squared-value sums.
-template <int MODE>
-__device__ __forceinline__ void tc_pre16(const GemmP<float>& p, int node, int col0, float4 (&q)[4]) {
-  if (MODE == EPI_SILU_J || MODE == EPI_ORB_J) {
-    const float* d = MODE == EPI_SILU_J ? p.aux1 + (long)node * p.ld_aux + col0 : p.aux1 + (long)node * 5 * p.ld_aux + col0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) q[u] = ld4(d + 4 * u);
-  }
-}
-
 // Epilogue values of 16 consecutive columns (col0 + 15 < N) of one row, into o: all operand loads are
-// issued before the first store so that their latencies overlap.  q: tc_pre16's operand (SILU_J, ORB_J).
+// issued before the first store so that their latencies overlap.
 template <int MODE>
 __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int node, int col0, const float (&v)[16],
-                                         int spin, float4 (&o)[4], const float4 (&q)[4]) {
+                                         int spin, float4 (&o)[4]) {
   if (MODE == EPI_SILU_J) {
-    const float4(&dd)[4] = q;
+    const float* d = p.aux1 + (long)node * p.ld_aux + col0;
+    float4 dd[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) dd[u] = ld4(d + 4 * u);
 #pragma unroll
     for (int u = 0; u < 4; ++u)
       o[u] = make_float4(v[4 * u] * dd[u].x, v[4 * u + 1] * dd[u].y, v[4 * u + 2] * dd[u].z, v[4 * u + 3] * dd[u].w);
@@ -292,7 +283,9 @@ __device__ __forceinline__ void tc_val16(const GemmP<float>& p, int row, int nod
     const int pos = row / 3, t = row - 3 * pos;
     const float* env = p.aux1 + (long)node * 5 * p.ld_aux + col0;
     const bool self = p.dep_map[pos] == node;
-    const float4(&ex)[4] = q;
+    float4 ex[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ex[u] = ld4(env + 4 * u);
     if (self) {
       float4 raw[4], ej[4];
 #pragma unroll
@@ -345,8 +338,6 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
   }
   const uint32_t base = tacc + ((uint32_t)(quad * 32) << 16);
   for (int c0 = half * (TCP_BN / 2); c0 < (half + 1) * (TCP_BN / 2); c0 += 16) {
-    float4 q[4];
-    if ((MODE == EPI_SILU_J || MODE == EPI_ORB_J) && mine && n0 + c0 + 15 < p.N) tc_pre16<MODE>(p, node, n0 + c0, q);
     float v[16];
     tmem_ld16(base + (uint32_t)c0, v);
     if (two_acc) {  // the exact hi x hi sums plus the cross terms, TCP_BN columns further on
@@ -397,7 +388,7 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
     }
     if (use_tma) {
       float4 o[4];
-      tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o, q);
+      tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
 #pragma unroll
       for (int u = 0; u < 4; ++u)  // the tensor map's 64-byte swizzle (staging buffers are 512-byte aligned)
         *reinterpret_cast<float4*>(sb + lane * 16 + 4 * (u ^ ((lane >> 1) & 3))) = o[u];
@@ -411,7 +402,7 @@ __device__ __forceinline__ void tc_epilogue_tile(const GemmP<float>& p, int rows
     } else if (mine) {
       if (full) {
         float4 o[4];
-        tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o, q);
+        tc_val16<MODE>(p, row, node, n0 + c0, v, spin, o);
 #pragma unroll
         for (int u = 0; u < 4; ++u) st4(p.C + (long)row * p.ldc + n0 + c0 + 4 * u, o[u]);
       } else {
