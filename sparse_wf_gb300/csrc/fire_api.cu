@@ -349,6 +349,10 @@ int choose_chunk(const fire_problem* p, size_t ws_bytes, bool fl) {
     const int c = std::min(B, p->chunk_walkers);
     return need(c) <= ws_bytes ? c : 0;
   }
+  // the rows of a pass's largest contraction (the Jacobian planes; the electron rows of the value path) stay within
+  // the 65535 row tiles of 64 that a launch grid's y dimension holds
+  const long rows_per_walker = fl ? 3L * (p->n_el + p->cap_pairs) : (long)p->n_el;
+  B = (int)std::min<long>(B, std::max<long>(1, 65535L * 64 / rows_per_walker));
   int lo = 0, hi = B;
   while (lo < hi) {  // largest c with plan(c) <= ws
     const int mid = (lo + hi + 1) / 2;

@@ -104,6 +104,15 @@ class FireWaveFunction:
         self._ws: Optional[torch.Tensor] = None
         self._status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=self.device)
         self._lr_cap = 0  # changed-set capacity of the last low-rank block (grown on overflow, like the statics)
+        # walkers per pass of the low-rank blocks and the pseudopotential energy (0: as many as lr_ws_gb holds; the
+        # per-walker state is far smaller than the local energy's planes, and one pass over the batch makes every
+        # step's launches serve all walkers)
+        self.lr_chunk_walkers = 0
+        self.lr_ws_gb = 64.0
+        # walkers per pass of the value path (log|psi| and the Metropolis blocks that evaluate every proposal in full;
+        # 0: as many as the workspace holds, which, sized for the local energy's planes, holds several times the
+        # local energy's pass)
+        self.value_chunk_walkers = 0
         # FP32 / mixed local energy: ill-conditioned walkers ((|lap| + |grad|^2) / 2 above refine_ratio |E_loc| or
         # refine_ks Hartree, a determinant-weighted condition number of the orbital matrices above refine_kappa, or the
         # product of the two above refine_kscond) are evaluated again with FP64 orbital-matrix values; the capacity of that pass follows the counts the device
@@ -141,7 +150,7 @@ class FireWaveFunction:
         """Workspace of the local-energy and value paths, or (cap_changed > 0) of the low-rank block."""
         lib = _lib.load()
         nbytes = C.c_size_t()
-        chunk = self.chunk_walkers if self.chunk_walkers > 0 else prob.n_walkers
+        chunk = prob.chunk_walkers if prob.chunk_walkers > 0 else prob.n_walkers
         if cap_changed > 0:
             _lib.check(lib.fire_low_rank_workspace_size(C.byref(prob), chunk, int(cap_changed), C.byref(nbytes)),
                        "fire_low_rank_workspace_size")
@@ -152,6 +161,20 @@ class FireWaveFunction:
             self._ws = None
             self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
         return self._ws
+
+    def _lr_problem(self, n_walkers: int, static: StaticArgs, cap: int) -> _lib.Problem:
+        """The problem of a low-rank call with its walkers per pass (lr_chunk_walkers, else what lr_ws_gb holds)."""
+        prob = self._problem(n_walkers, static)
+        c = int(self.lr_chunk_walkers)
+        if c <= 0:
+            nbytes = C.c_size_t()
+            _lib.check(_lib.load().fire_low_rank_workspace_size(C.byref(prob), 1, int(cap), C.byref(nbytes)),
+                       "fire_low_rank_workspace_size")
+            c = int(self.lr_ws_gb * 1e9) // max(1, int(nbytes.value))
+            # the changed rows of a pass (walkers x cap) and its electron rows stay within 65535 row tiles of 64
+            c = min(c, 65535 * 64 // max(self.n_electrons, int(cap)))
+        prob.chunk_walkers = max(1, min(int(n_walkers), c))
+        return prob
 
     def _electrons(self, electrons) -> torch.Tensor:
         r = torch.as_tensor(electrons)
@@ -278,6 +301,7 @@ class FireWaveFunction:
         logpsi = torch.empty(B, dtype=self.dtype, device=self.device)
 
         def fn(prob, ws):
+            prob.chunk_walkers = int(self.value_chunk_walkers)
             _lib.check(_lib.load().fire_logpsi(
                 self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
                 C.c_void_p(p.prepared.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(sign.data_ptr()),
@@ -401,6 +425,7 @@ class FireWaveFunction:
         lp0 = logpsi.clone()
 
         def fn(prob, ws):
+            prob.chunk_walkers = int(self.value_chunk_walkers)
             r.copy_(r0)
             logpsi.copy_(lp0)
             n_acc.zero_()
@@ -440,6 +465,7 @@ class FireWaveFunction:
         lp0 = logpsi.clone()
 
         def fn(prob, ws):
+            prob.chunk_walkers = int(self.value_chunk_walkers)
             r.copy_(r0)
             logpsi.copy_(lp0)
             n_acc.zero_()
@@ -480,7 +506,7 @@ class FireWaveFunction:
             logpsi.copy_(lp0)
             n_acc.zero_()
             smax.zero_()
-            prob = self._problem(B, static)
+            prob = self._lr_problem(B, static, cap)
             _lib.check(launch(fn, prob, self._workspace(prob, cap), cap, n_acc, smax), fn_name)
             st = self._read_status()
             flags = int(st[0])
@@ -611,7 +637,7 @@ class FireWaveFunction:
         for _ in range(6):
             self._status.zero_()
             smax.zero_()
-            prob = self._problem(B, static)
+            prob = self._lr_problem(B, static, cap)
             ws = self._workspace(prob, cap)
             _lib.check(lib.fire_ecp_energy(
                 self._stream(), C.byref(prob), C.c_void_p(self.R_dev.data_ptr()), C.c_void_p(self.Z_dev.data_ptr()),
@@ -660,6 +686,7 @@ class FireWaveFunction:
         lp0 = logpsi.clone()
 
         def fn(prob, ws):
+            prob.chunk_walkers = int(self.value_chunk_walkers)
             r.copy_(r0)
             logpsi.copy_(lp0)
             n_acc.zero_()
@@ -704,6 +731,7 @@ class FireWaveFunction:
         lp0 = logpsi.clone()
 
         def fn(prob, ws):
+            prob.chunk_walkers = int(self.value_chunk_walkers)
             r.copy_(r0)
             logpsi.copy_(lp0)
             n_acc.zero_()
