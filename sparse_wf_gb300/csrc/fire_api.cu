@@ -1453,8 +1453,8 @@ cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi, void* sign, in
     if constexpr (sizeof(T) == 8)
       launch_gjg<double, T, T, true>(c, c.template buf<T>(c.P.Apl), (const T*)nullptr, c.template buf<T>(Q.B));
     else
-      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl), c.template buf<T>(c.P.Apl_lo),
-                                   c.template buf<T>(Q.B));
+      launch_gjg<df64, T, T, true>(c, c.template buf<T>(c.P.Apl),
+                                   c.comp ? c.template buf<T>(c.P.Apl_lo) : nullptr, c.template buf<T>(Q.B));
   }
   stage_jastrow<T, 0>(c);
   const Planes B2{c.P.B2X, 0, 0}, VL{Q.vals, 0, 0};
@@ -1745,6 +1745,9 @@ fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, c
   const int Wc = choose_chunk_lr(p, wsb, KS);
   if (Wc <= 0) return FIRE_ERR_WORKSPACE;
   Ctx<T> c = make_ctx<T>(p, s, R, Z, prepared, status, ws, Wc, false);
+  // the Metropolis test only compares log|psi| values: plain value contractions for the state and the changed rows,
+  // as in the blocks that evaluate every proposal in full (the pseudopotential energy keeps the compensated ones)
+  c.comp = false;
   const LrPlan Q = make_lr_plan(p, Wc, KS);
   T* rr = reinterpret_cast<T*>(r);
   const int n = p->n_el;
