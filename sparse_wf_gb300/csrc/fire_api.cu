@@ -1475,7 +1475,8 @@ cudaError_t chunk_state(Ctx<T>& c, const LrPlan& Q, void* logpsi, void* sign, in
 // moved the electrons moved[w][0..KM) (the plan's moved buffer, padded with FIRE_NO_NEIGHBOUR), from the state; the
 // proposal's rows stay in the plan's scratch for the commit.
 template <typename T>
-cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, int32_t* static_max, T* sgn_out) {
+cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, int32_t* static_max, T* sgn_out,
+                        int mover_spin = -1) {
   const fire_problem* p = c.p;
   const int n = p->n_el, nu = p->n_up, N = p->n_nuc, Wc = c.Wc, DN = NDET * n, rows = Wc * KS;
   const int K8 = N * NENV_ORB;
@@ -1540,7 +1541,8 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, int32
   k_lr_orb<T><<<dim3(KS, Wc), 256, 0, s>>>(S, S_cnt, KS, nu, DN, c.template buf<T>(Q.rawU),
                                            c.template buf<T>(Q.rawD));
   // envelope row of the moved electron at its new position: coefficients of its own spin (zero in the other spin's
-  // set), both spins' contractions, their sum
+  // set), both spins' contractions, their sum; when every walker moves an electron of one spin (mover_spin >= 0, the
+  // sequential single-electron sweep) that spin's contractions alone, straight into env_p
   {
     T* coefU = c.template buf<T>(Q.coefE);
     T* coefD = c.template buf<T>(Q.coefD);
@@ -1548,6 +1550,16 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, int32
     const int ME = Wc * KM;
     k_lr_env_coef<T><<<nblk((long)ME * K8), 256, 0, s>>>(rn, c.R, c.W.w[PR_ENV_UP_SP], c.W.w[PR_ENV_DN_SP], moved,
                                                          KM, n, nu, N, Wc, coefU, coefD);
+    if (mover_spin >= 0) {
+      for (int d = 0; d < NDET; ++d) {
+        GemmP<T> g = gp0<T>();
+        g.A = (mover_spin == 0 ? coefU : coefD) + (size_t)d * ME * K8; g.lda = K8;
+        g.B = c.W.w[mover_spin == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (size_t)d * K8 * n; g.ldb = n;
+        g.C = c.template buf<T>(Q.env_p) + (size_t)d * n; g.ldc = DN; g.M = ME; g.N = n;
+        g.K = K8; g.n_el = 1; g.env_ns = 1; g.env_soff = 0; g.env_nv = 1;
+        gemm<T, EPI_ENV>(c, g);
+      }
+    } else {
     for (int sp = 0; sp < 2; ++sp)
       for (int d = 0; d < NDET; ++d) {
         GemmP<T> g = gp0<T>();
@@ -1560,6 +1572,7 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, int32
     g_nlaunch++;
     k_lr_env_add<T><<<nblk((long)ME * DN), 256, 0, s>>>((long)ME * DN, c.template buf<T>(Q.env_p),
                                                         c.template buf<T>(Q.env_pD));
+    }
   }
   // determinant lemma
   {
@@ -1618,7 +1631,8 @@ cudaError_t lr_evaluate(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, int32
 // the Woodbury update of the inverse.
 template <typename T>
 cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, void* logpsi, int st, uint64_t seed,
-                    uint64_t counter, const void* logu, int32_t* n_accept, int32_t* static_max, const T* plr) {
+                    uint64_t counter, const void* logu, int32_t* n_accept, int32_t* static_max, const T* plr,
+                    int mover_spin = -1) {
   const fire_problem* p = c.p;
   const int n = p->n_el, Wc = c.Wc;
   cudaStream_t s = c.s;
@@ -1627,7 +1641,7 @@ cudaError_t lr_step(Ctx<T>& c, const LrPlan& Q, int KS, int KM, T* rr, void* log
   int* S_cnt = c.template buf<int>(Q.S_cnt);
   int* acc = c.template buf<int>(Q.acc);
   const int* moved = c.template buf<int>(Q.moved);
-  const cudaError_t ev = lr_evaluate<T>(c, Q, KS, KM, rr, static_max, nullptr);
+  const cudaError_t ev = lr_evaluate<T>(c, Q, KS, KM, rr, static_max, nullptr, mover_spin);
   if (ev != cudaSuccess) return ev;
   T* lpn = c.template buf<T>(c.P.lpn);
   g_nlaunch++;
@@ -1773,7 +1787,11 @@ fire_status run_mcmc_lr(const fire_problem* p, cudaStream_t s, const float* R, c
         k_propose_single<T><<<c.Wc, 128, 0, s>>>(rr + (size_t)w0 * n * 3, c.template buf<T>(c.P.rn), n, w0,
                                                  p->n_walkers, st, offset, (T)width, seed, counter,
                                                  reinterpret_cast<const T*>(noise), moved);
-      if (lr_step<T>(c, Q, KS, KM, rr, logpsi, st, seed, counter, logu, n_accept, static_max, plr) != cudaSuccess)
+      // the sequential sweep moves electron (offset + st) mod n of every walker: one spin per step
+      const int mover = kind == MC_SINGLE ? (int)(((long)offset + st) % n) : -1;
+      const int mover_spin = mover < 0 ? -1 : (mover < p->n_up ? 0 : 1);
+      if (lr_step<T>(c, Q, KS, KM, rr, logpsi, st, seed, counter, logu, n_accept, static_max, plr, mover_spin) !=
+          cudaSuccess)
         return launch_status("low-rank step");
     }
   }

@@ -22,6 +22,9 @@
 //  k_lr_commit  on acceptance, the proposal's rows into the state.
 //  k_lr_wb_z, k_lr_wb_q, k_lr_wb_apply
 //               on acceptance, the Woodbury update of the transposed inverse: B' = B - (B V^T)(M^-T B[S, :]).
+#include <type_traits>
+
+#include "fire_df64.cuh"
 #include "fire_internal.cuh"
 
 namespace fire {
@@ -258,13 +261,16 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
                                                 const double* __restrict__ sd, T* __restrict__ V,
                                                 double* __restrict__ Minv, double* __restrict__ ld_p,
                                                 double* __restrict__ sd_p) {
+  // the k x k elimination in double precision: FP64 in the FP64 build, double-FP32 otherwise (the FP32 pipes run it
+  // several times faster than GB300's FP64 pipe)
+  using SE = typename std::conditional<sizeof(T) == 8, double, df64>::type;
   extern __shared__ __align__(16) unsigned char lr_smem[];
-  double* Ms = reinterpret_cast<double*>(lr_smem);            // [k][k], row stride k
+  SE* Ms = reinterpret_cast<SE*>(lr_smem);                      // [k][k], row stride k
   T* Vt = reinterpret_cast<T*>(Ms + (size_t)KS * KS);          // [KS][33]
   T* Bt = Vt + (size_t)KS * 33;                                // [KS][33]
   __shared__ int sS[LR_KMAX];
   __shared__ int perm[LR_KMAX];
-  __shared__ double fac[LR_KMAX];
+  __shared__ SE fac[LR_KMAX];
   __shared__ int piv_row;
   const int d = blockIdx.x, w = blockIdx.y, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int cnt = S_cnt[w];
@@ -279,7 +285,7 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
   const int k = cnt;
   const int DN = NDET * n, nA = ainv_ld(n), sh = (d * n) & 3;
   for (int a = tid; a < k; a += blockDim.x) sS[a] = S[(size_t)w * KS + a];
-  for (int q = tid; q < k * k; q += blockDim.x) Ms[q] = (q / k == q % k) ? 1.0 : 0.0;
+  for (int q = tid; q < k * k; q += blockDim.x) Ms[q] = (q / k == q % k) ? SE(1.0) : SE(0.0);
   __syncthreads();
   // V rows: A'[S] - A[S] (the orbital-matrix rows are raw * envelope, as in the value path)
   T* Vw = V + md * KS * n;
@@ -306,7 +312,7 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
       T s = T(0);
 #pragma unroll 8
       for (int oo = 0; oo < 32; ++oo) s += Vt[a * 33 + oo] * Bt[b * 33 + oo];
-      Ms[q] += (double)s;
+      Ms[q] += SE(s);
     }
     __syncthreads();
   }
@@ -320,7 +326,7 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
       double best = -1.0;
       int bi = t;
       for (int i = t + lane; i < k; i += 32) {
-        const double v = fabs(Ms[i * k + t]);
+        const double v = fabs((double)Ms[i * k + t]);
         if (v > best) {
           best = v;
           bi = i;
@@ -344,31 +350,32 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
     const int p = piv_row;
     if (p != t) {
       for (int q = tid; q < k; q += blockDim.x) {
-        const double x = Ms[t * k + q];
+        const SE x = Ms[t * k + q];
         Ms[t * k + q] = Ms[p * k + q];
         Ms[p * k + q] = x;
       }
       neg ^= 1;
     }
     __syncthreads();
-    const double pv = Ms[t * k + t];
-    if (pv == 0.0) {
+    const SE pv = Ms[t * k + t];
+    const double pvd = (double)pv;
+    if (pvd == 0.0) {
       singular = true;
       break;
     }
-    ldet += log(fabs(pv));
-    if (pv < 0.0) neg ^= 1;
-    const double ip = 1.0 / pv;
+    ldet += log(fabs(pvd));
+    if (pvd < 0.0) neg ^= 1;
+    const SE ip = SE(1.0) / pv;
     __syncthreads();
     for (int q = tid; q < k; q += blockDim.x) {
       Ms[t * k + q] = q == t ? ip : Ms[t * k + q] * ip;
-      fac[q] = q == t ? 0.0 : Ms[q * k + t];
+      fac[q] = q == t ? SE(0.0) : Ms[q * k + t];
     }
     __syncthreads();
     for (int q = tid; q < k * k; q += blockDim.x) {
       const int i = q / k, c = q - i * k;
       if (i == t) continue;
-      Ms[q] = c == t ? -fac[i] * Ms[t * k + t] : Ms[q] - fac[i] * Ms[t * k + c];
+      Ms[q] = c == t ? -(fac[i] * Ms[t * k + t]) : df_sub_mul(Ms[q], fac[i], Ms[t * k + c]);
     }
     __syncthreads();
   }
@@ -377,7 +384,7 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
       const int p = perm[t];
       if (p != t)
         for (int i = tid; i < k; i += blockDim.x) {
-          const double x = Ms[i * k + t];
+          const SE x = Ms[i * k + t];
           Ms[i * k + t] = Ms[i * k + p];
           Ms[i * k + p] = x;
         }
@@ -387,7 +394,7 @@ __global__ void __launch_bounds__(256) k_lr_det(const int* __restrict__ S, const
   double* Mo = Minv + md * KS * KS;
   for (int q = tid; q < k * k; q += blockDim.x) {
     const int a = q / k, b = q - a * k;
-    Mo[(size_t)a * KS + b] = singular ? 0.0 : Ms[q];
+    Mo[(size_t)a * KS + b] = singular ? 0.0 : (double)Ms[q];
   }
   if (tid == 0) {
     ld_p[md] = ld[md] + (singular ? 0.0 : ldet);
