@@ -505,6 +505,8 @@ struct Ctx {
   // energy, log|psi| and the low-rank state); the Metropolis blocks' proposals, which only compare log|psi| values,
   // take the plain contraction
   bool comp = true;
+  // the refinement pass's FP64 value path: its envelope value rows by the double-FP32 compensated contraction
+  bool env_df = false;
   TcWeights tcw[TC_COUNT];
   template <typename U>
   U* buf(size_t off) const {
@@ -770,6 +772,15 @@ cudaError_t stage_orbitals(Ctx<T>& c) {
       g.B = c.W.w[s == 0 ? PR_ENV_UP_PI : PR_ENV_DN_PI] + (long)d * K8 * n; g.ldb = n;
       g.C = env + (long)d * n; g.ldc = (long)DN * (NV / nvc); g.M = (int)rows; g.N = n; g.K = (int)K8;
       g.n_el = n; g.env_ns = ns; g.env_soff = s == 0 ? 0 : nu; g.env_nv = nvc;
+      if constexpr (sizeof(T) == 8) {
+        if (c.env_df && nvc == 1) {
+          Prof pg("gemm", c.s);
+          g_nlaunch++;
+          const cudaError_t e = launch_gemm_env_df(g, c.s);
+          if (e != cudaSuccess) return e;
+          continue;
+        }
+      }
       if (sizeof(T) == 8 || !c.comp) {
         gemm<T, EPI_ENV>(c, g);
       } else if constexpr (sizeof(T) == 4) {
@@ -1190,6 +1201,7 @@ cudaError_t refine_pass(const fire_problem* p, int Wc, cudaStream_t s, const flo
                                        ws + L.c64, KC, false);
     c64.w0 = 0;
     c64.Wc = KC;
+    c64.env_df = true;
     c64.r = r64;
     setup_ctx(c64, false);
     stage_neighbors(c64, false);

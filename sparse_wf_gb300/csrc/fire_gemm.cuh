@@ -445,6 +445,97 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
   }
 }
 
+// Envelope value rows of the refinement pass (EPI_ENV's row map, env_nv = 1) on the FP32 pipes: A holds FP64
+// coefficients, B weights whose values are exact in FP32 (the float32 parameter blob's), C is FP64.  Each a is split
+// into a_hi + a_lo floats; a_hi b by Dot2 (as in k_gemm_comp), a_lo b by FP32 FMAs into the low accumulator, and the
+// result hi + lo leaves as a double: ~2^-44 of the terms' magnitude, where the FP64 pipe (~1/64 of the FP32 rate)
+// would spend most of the pass.
+template <int V = 0>  // a template so that every translation unit that includes this header may hold it
+__global__ void __launch_bounds__(CTHREADS) k_gemm_env_df(GemmP<double> p) {
+  __shared__ __align__(16) float Ah[2][CBK][CBM];
+  __shared__ __align__(16) float Al[2][CBK][CBM];
+  __shared__ __align__(16) float Bs[2][CBK][CBN];
+  const int rows = p.M;
+  const int m0 = blockIdx.y * CBM, n0 = blockIdx.x * CBN;
+  if (m0 >= rows) return;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int ar = tid >> 2, aq = (tid & 3) * 4;   // A: row ar, k aq..aq+3 of the tile
+  const int bk = tid >> 4, bc = (tid & 15) * 4;  // B: k bk, columns bc..bc+3
+  double ra[4];
+  float rb[4];
+  auto load = [&](int k0) {
+    const int gr = m0 + ar, gk = k0 + aq;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ra[u] = (gr < rows && gk + u < p.K) ? p.A[(long)gr * p.lda + gk + u] : 0.0;
+    const int gk2 = k0 + bk, gc = n0 + bc;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) rb[u] = (gk2 < p.K && gc + u < p.N) ? (float)p.B[(long)gk2 * p.ldb + gc + u] : 0.f;
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float h = __double2float_rn(ra[u]);
+      Ah[buf][aq + u][ar] = h;
+      Al[buf][aq + u][ar] = __double2float_rn(ra[u] - (double)h);
+    }
+    *reinterpret_cast<float4*>(&Bs[buf][bk][bc]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
+  };
+  float hi[4][4], lo[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.f;
+  load(0);
+  store(0);
+  __syncthreads();
+  int buf = 0;
+  for (int k0 = 0; k0 < p.K; k0 += CBK) {
+    const bool more = k0 + CBK < p.K;
+    if (more) load(k0 + CBK);
+#pragma unroll 4
+    for (int kk = 0; kk < CBK; ++kk) {
+      const float4 a = *reinterpret_cast<const float4*>(&Ah[buf][kk][ty * 4]);
+      const float4 al = *reinterpret_cast<const float4*>(&Al[buf][kk][ty * 4]);
+      const float4 b = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+      const float av[4] = {a.x, a.y, a.z, a.w}, alv[4] = {al.x, al.y, al.z, al.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float pr = av[i] * bv[j];
+          const float pe = fmaf(av[i], bv[j], -pr);
+          float s2, e;
+          two_sum(hi[i][j], pr, s2, e);
+          hi[i][j] = s2;
+          lo[i][j] = fmaf(alv[i], bv[j], lo[i][j] + (e + pe));
+        }
+    }
+    if (more) {
+      store(buf ^ 1);
+      __syncthreads();
+      buf ^= 1;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int row = m0 + ty * 4 + i;
+    if (row >= rows) continue;
+    const int g = (row / p.env_ns) * p.n_el + p.env_soff + row % p.env_ns;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int col = n0 + tx * 4 + j;
+      if (col < p.N) p.C[(long)g * p.ldc + col] = (double)hi[i][j] + (double)lo[i][j];
+    }
+  }
+}
+
+inline cudaError_t launch_gemm_env_df(const GemmP<double>& p, cudaStream_t s) {
+  dim3 grid((p.N + CBN - 1) / CBN, (p.M + CBM - 1) / CBM);
+  if (grid.y == 0 || grid.x == 0) return cudaSuccess;
+  k_gemm_env_df<0><<<grid, CTHREADS, 0, s>>>(p);
+  return cudaPeekAtLastError();
+}
+
 template <int MODE>
 inline cudaError_t launch_gemm_comp(const GemmP<float>& p, float* C_lo, const float* env_lo, long ld_lo,
                                     cudaStream_t s) {
