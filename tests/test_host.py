@@ -628,6 +628,41 @@ def test_bench_reference_arm_json_contract():
     assert abs(d["ms_per_step"] / 1e3 - d["cpu_baseline"]["cores"] / d["value"]) < 1e-9
 
 
+def test_low_rank_pass_size_from_its_own_workspace(monkeypatch):
+    """The low-rank blocks size their walkers per pass from their own workspace, not the local energy's pass: as many
+    walkers as lr_ws_gb holds at the block's per-walker size (the fake library's workspace grows by 1000 bytes per
+    walker and changed-set slot), or lr_chunk_walkers when set; the workspace is requested for that pass."""
+    import torch
+
+    from sparse_wf_gb300.wavefunction import StaticArgs
+
+    class Fake(_FakeLowRankLib):
+        def __init__(self):
+            super().__init__(need=1)
+            self.sizes = []
+
+        def fire_low_rank_workspace_size(self, prob, chunk, cap, nbytes):
+            self.sizes.append(int(chunk))
+            nbytes._obj.value = 1000 * int(chunk) * int(cap)
+            return 0
+
+        def fire_mcmc_low_rank_block(self, stream, prob, *args):
+            self.calls.append(int(prob._obj.chunk_walkers))
+            return 0
+
+    fake = Fake()
+    wf, mol, _ = _fake_wf(monkeypatch, fake)
+    r = torch.from_numpy(systems.init_electrons(mol, 7, 5)).contiguous()
+    lp = torch.zeros(7)
+    wf.chunk_walkers = 2  # the local energy's pass: not the low-rank block's
+    wf.lr_ws_gb = 25e-6   # 25 kB: 6 walkers at 4 changed-set slots
+    wf.mcmc_low_rank_block(P.init_params(wf.dims, 0), r, lp, StaticArgs(40, 40, 0, 8), 1, 0.3, cap_changed=4)
+    assert fake.calls == [6] and fake.sizes[-1] == 6
+    wf.lr_chunk_walkers = 3
+    wf.mcmc_low_rank_block(P.init_params(wf.dims, 0), r, lp, StaticArgs(40, 40, 0, 8), 1, 0.3, cap_changed=4)
+    assert fake.calls[-1] == 3 and fake.sizes[-1] == 3
+
+
 def test_ecp_energy_wrapper_reruns(monkeypatch):
     """FireWaveFunction.ecp_energy's host loop against a fake library: a changed-set overflow reruns with the set the
     device reported, a pair overflow first grows the neighbour capacity, and the energies and move statics come back
