@@ -284,11 +284,22 @@ inline cudaError_t launch_gemm(const GemmP<T>& p, cudaStream_t s) {
 
 // ----------------------------------------------------------------------------- compensated value contraction
 // FP32 and mixed paths: the value planes (one row per node) feed the orbital matrices, whose inverse amplifies
-// their rounding by the condition number in the derivatives of log det.  k_gemm_comp computes them with
-// compensated dot products (Ogita, Rump and Oishi's Dot2: every product split exactly with an FMA, every partial
-// sum with TwoSum (Knuth), the errors gathered in a second accumulator), i.e. as if in twice the working precision
-// and then rounded once: the error is ~2^-24 of the result even where the terms cancel (the orbital values are
-// small differences of large products), which a shorter FMA chain per partial sum does not give.
+// their rounding by the condition number in the derivatives of log det.  k_gemm_comp computes them as compensated
+// dot products, as if in twice the working precision and then rounded once: the error is ~2^-24 of the result even
+// where the terms cancel (the orbital values are small differences of large products), which a shorter FMA chain
+// per partial sum does not give.
+// The exact part of every product is summed on a power-of-two grid instead of by a TwoSum per product (Ogita, Rump
+// and Oishi's Dot2), in the spirit of Rump's error-free extraction against a fixed power of two:
+//   - each column of B is bounded over the whole K by |b| < 2^eb, and each row of a staged 16-k tile of A is
+//     scaled by a power of two so that |a'| < 1 (the row's scale 2^ea kept beside the tile);
+//   - t = fma(a', b, 3 * 2^eb) then lies in [2^(eb+1), 2^(eb+2)], where floats are evenly spaced by G = 2^(eb-22),
+//     so bits(t) - bits(3 * 2^eb) is the product rounded to that grid, counted in steps and summed exactly in a
+//     32-bit integer (at most 16 * 2^22 per tile);
+//   - fma(a', b, 3 * 2^eb - t) is the exact remainder below G / 2, summed in FP32;
+//   - after each tile the step count leaves as xh + xl (xh its FP32 rounding, |xl| <= 2), and (xh G, xl G + rest),
+//     scaled back by 2^ea, join a hi + lo pair by one TwoSum.
+// That is five FP32/integer operations per product where Dot2 takes ten, with the same worst-case error on
+// envelope- and orbital-like operands (~2^-42 of sum |a b|; measured against exact sums in a CPU restatement).
 // The orbital-matrix values and the envelope values they are made of also leave the kernel as unevaluated hi + lo
 // float pairs, so that the double-FP32 elimination sees them to ~2^-48.
 //   COMP_PLAIN  C = a.b + bias (bias on rows with row % bias_period == 0)
@@ -305,13 +316,54 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// Grid of a column whose values are bounded by m >= 0: |b| < 2^eb (eb in [-100, 119]); sg = 3 * 2^eb, g = 2^(eb-22)
+// (the spacing of the floats in [2^(eb+1), 2^(eb+2)]), sb16 = 16 bits(sg) (the offset of 16 summed products).
+// A non-finite or huge bound gives NaN, which every output of the column then carries.
+__device__ __forceinline__ void comp_grid_col(float m, float& sg, float& g, unsigned& sb16) {
+  const int field = (__float_as_int(m) >> 23) & 0xff;
+  int eb = field - 126;  // m < 2^(field - 126)
+  if (eb < -100) eb = -100;
+  if (field == 255 || eb > 119) {
+    sg = g = __int_as_float(0x7fc00000);
+    sb16 = 0u;
+    return;
+  }
+  sg = 3.f * __int_as_float((eb + 127) << 23);
+  g = __int_as_float((eb + 105) << 23);
+  sb16 = 16u * (unsigned)__float_as_int(sg);
+}
+
+// Scale of a row tile whose values are bounded by m >= 0: inv = 2^-ea (|a| inv < 1), sc = 2^ea; a non-finite or
+// huge bound gives NaN.
+__device__ __forceinline__ void comp_grid_row(float m, float& inv, float& sc) {
+  if (m == 0.f) {
+    inv = sc = 1.f;
+    return;
+  }
+  const int field = (__float_as_int(m) >> 23) & 0xff;
+  int ea = field - 126;  // m < 2^ea
+  if (ea < -125) ea = -125;
+  if (field == 255 || ea > 126) {
+    inv = sc = __int_as_float(0x7fc00000);
+    return;
+  }
+  inv = __int_as_float((127 - ea) << 23);
+  sc = __int_as_float((127 + ea) << 23);
+}
+
 // 64 x 64 outputs per CTA, 4 x 4 per thread (rows 4 ty.., columns 4 tx..); A and B tiles of 16 k staged in shared
-// memory (A transposed), the next tile prefetched into registers while the current one is summed.
+// memory (A transposed and scaled per row), the next tile prefetched into registers while the current one is
+// summed.  Before the first tile every pass bounds its 64 columns of B over the whole K.
 template <int MODE>
-__global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* __restrict__ C_lo,
-                                                        const float* __restrict__ env_lo, long ld_lo) {
+__global__ void __launch_bounds__(CTHREADS, 2) k_gemm_comp(GemmP<float> p, float* __restrict__ C_lo,
+                                                           const float* __restrict__ env_lo, long ld_lo) {
   __shared__ __align__(16) float As[2][CBK][CBM];
   __shared__ __align__(16) float Bs[2][CBK][CBN];
+  __shared__ __align__(16) float Asc[2][CBM];     // 2^ea of every row of the staged A tile
+  __shared__ float Bmx[CTHREADS / 32][CBN];       // per-warp column maxima of |B|
+  __shared__ __align__(16) float Csg[CBN];        // per column: 3 * 2^eb, the grid spacing 2^(eb-22), 16 bits(3 * 2^eb)
+  __shared__ __align__(16) float Cg[CBN];
+  __shared__ __align__(16) unsigned Cs16[CBN];
   const int rows = p.M;
   const int m0 = blockIdx.y * CBM, n0 = blockIdx.x * CBN;
   if (m0 >= rows) return;
@@ -334,6 +386,39 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
     const int spin = first_spin + pass;
     const float* Bp = spin == 0 ? p.B : p.B2;
     const bool vb = p.ldb % 4 == 0 && (reinterpret_cast<uintptr_t>(Bp) & 15) == 0;
+    // the bounds of this CTA's columns over the whole K: 16 threads per k row (4 columns each), k strided by 16
+    {
+      const int c4 = (tid & 15) * 4, gc = n0 + c4;
+      float m[4] = {0.f, 0.f, 0.f, 0.f};
+      if (vb && gc + 3 < p.N) {
+#pragma unroll 4
+        for (int k = tid >> 4; k < p.K; k += 16) {
+          const float4 q = *reinterpret_cast<const float4*>(Bp + (long)k * p.ldb + gc);
+          m[0] = fmaxf(m[0], fabsf(q.x));
+          m[1] = fmaxf(m[1], fabsf(q.y));
+          m[2] = fmaxf(m[2], fabsf(q.z));
+          m[3] = fmaxf(m[3], fabsf(q.w));
+        }
+      } else {
+        for (int k = tid >> 4; k < p.K; k += 16) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (gc + u < p.N) m[u] = fmaxf(m[u], fabsf(Bp[(long)k * p.ldb + gc + u]));
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        m[u] = fmaxf(m[u], __shfl_xor_sync(0xffffffffu, m[u], 16));  // the warp's two k rows
+        if ((tid & 16) == 0) Bmx[tid >> 5][c4 + u] = m[u];
+      }
+    }
+    __syncthreads();
+    if (tid < CBN) {  // one column each; read after the barrier that follows the first tile's staging
+      float m = 0.f;
+#pragma unroll
+      for (int w = 0; w < CTHREADS / 32; ++w) m = fmaxf(m, Bmx[w][tid]);
+      comp_grid_col(m, Csg[tid], Cg[tid], Cs16[tid]);
+    }
     float ra[4], rb[4];
     auto load = [&](int k0) {
       const int gr = m0 + ar, gk = k0 + aq;
@@ -353,19 +438,35 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
         for (int u = 0; u < 4; ++u) rb[u] = (gk2 < p.K && gc + u < p.N) ? Bp[(long)gk2 * p.ldb + gc + u] : 0.f;
       }
     };
+    // A's 16 values of row ar are held by the 4 lanes tid ^ {0, 1, 2, 3}: their maximum scales the row
     auto store = [&](int buf) {
+      float m = fmaxf(fmaxf(fabsf(ra[0]), fabsf(ra[1])), fmaxf(fabsf(ra[2]), fabsf(ra[3])));
+      m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+      m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+      float inv, sc;
+      comp_grid_row(m, inv, sc);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) As[buf][aq + u][ar] = ra[u];
+      for (int u = 0; u < 4; ++u) As[buf][aq + u][ar] = ra[u] * inv;
+      if ((tid & 3) == 0) Asc[buf][ar] = sc;
       *reinterpret_cast<float4*>(&Bs[buf][bk][bc]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
     };
-    float hi[4][4], lo[4][4];
+    float hi[4][4], lo[4][4], rh[4][4];
+    unsigned ti[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.f;
+      for (int j = 0; j < 4; ++j) {
+        hi[i][j] = lo[i][j] = rh[i][j] = 0.f;
+        ti[i][j] = 0u;
+      }
     load(0);
     store(0);
     __syncthreads();
+    float sg[4];
+    {
+      const float4 s4 = *reinterpret_cast<const float4*>(&Csg[tx * 4]);
+      sg[0] = s4.x; sg[1] = s4.y; sg[2] = s4.z; sg[3] = s4.w;
+    }
     int buf = 0;
     for (int k0 = 0; k0 < p.K; k0 += CBK) {
       const bool more = k0 + CBK < p.K;
@@ -379,12 +480,33 @@ __global__ void __launch_bounds__(CTHREADS) k_gemm_comp(GemmP<float> p, float* _
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const float pr = av[i] * bv[j];
-            const float pe = fmaf(av[i], bv[j], -pr);
+            const float t = fmaf(av[i], bv[j], sg[j]);  // the product on the grid, offset by 3 * 2^eb
+            ti[i][j] += (unsigned)__float_as_int(t);
+            rh[i][j] += fmaf(av[i], bv[j], sg[j] - t);  // its exact remainder
+          }
+      }
+      // the tile's sums into the hi + lo pairs: the step count (< 2^26) as its FP32 rounding xh plus xl (|xl| <= 2)
+      {
+        const float4 s4 = *reinterpret_cast<const float4*>(&Asc[buf][ty * 4]);
+        const float4 g4 = *reinterpret_cast<const float4*>(&Cg[tx * 4]);
+        const uint4 o4 = *reinterpret_cast<const uint4*>(&Cs16[tx * 4]);
+        const float sv[4] = {s4.x, s4.y, s4.z, s4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w};
+        const unsigned sb16[4] = {o4.x, o4.y, o4.z, o4.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int d = (int)(ti[i][j] - sb16[j]);
+            const float xh = __int2float_rn(d);
+            const float xl = __int2float_rn(d - __float2int_rn(xh));
+            const float uh = xh * gg[j] * sv[i];
+            const float ul = fmaf(xl, gg[j], rh[i][j]) * sv[i];
             float s2, e;
-            two_sum(hi[i][j], pr, s2, e);
+            two_sum(hi[i][j], uh, s2, e);
             hi[i][j] = s2;
-            lo[i][j] += e + pe;
+            lo[i][j] += e + ul;
+            ti[i][j] = 0u;
+            rh[i][j] = 0.f;
           }
       }
       if (more) {
