@@ -2,11 +2,14 @@
 //
 // C[M, N] = A[M, K] * W[K, N] for the Jacobian and Laplacian planes of the sparse forward Laplacian,
 // with the same epilogues as the CUDA-core GEMM (fire_gemm.cuh).  A is an FP32 plane; while it is
-// staged into shared memory every element is split into two BF16 numbers, a = a_hi + a_lo
-// (a_hi = bf16(a), a_lo = bf16(a - a_hi)).  The weights are pre-split the same way and stored
-// transposed (K contiguous).  Each 16-deep K step issues three BF16 MMAs into one FP32 accumulator in
-// tensor memory:  a_hi b_hi + a_hi b_lo + a_lo b_hi  (relative error ~2^-17 per product instead of
-// BF16's 2^-9).
+// staged into shared memory every element is split into two 16-bit numbers, a = a_hi + a_lo.  The
+// weights are pre-split the same way and stored transposed (K contiguous).
+//   - k_gemm_tca (K <= 256) splits on a power-of-two grid per row of A and per column of W into FP16 hi + lo
+//     and issues four FP16 MMAs per 16-deep K step: the exact hi x hi sums into one TMEM accumulator, the three
+//     cross terms into a second (the splitting comment before k_gemm_tca has the details);
+//   - k_gemm_tcs (K > 256) splits elementwise into BF16, a_hi = bf16(a), a_lo = bf16(a - a_hi), and issues
+//     three BF16 MMAs into one FP32 accumulator:  a_hi b_hi + a_hi b_lo + a_lo b_hi  (relative error ~2^-17
+//     per product instead of BF16's 2^-9).
 //
 // Two kernels share the epilogues: k_gemm_tca (K <= 256; the A tile stays in shared memory, the pre-tiled
 // weights stream in by bulk copies) and k_gemm_tcs (K > 256; A and weight k-tiles stream together).  Tiles
