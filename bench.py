@@ -66,11 +66,72 @@ def parse():
     ap.add_argument("--serving-walkers", default="256,2048", help="walkers per serving request (min,max)")
     ap.add_argument("--no-ragged", action="store_true",
                     help="skip the 64-alkane ragged batch (one CUDA-graph launch vs one call per molecule)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the smaller configurations (H10 x 512: FP32 and FP64; C10H22 x 4096: mixed and FP32)")
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="walkers in the CPU samples (0: one per host core, at most 16)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
+
+
+def config_segments(args, dev, stream):
+    """The benchmark's smaller configurations beside the headline one (world size 1), on walkers drawn around the
+    nuclei (sigma 1 bohr, seed 1000; no Metropolis block) with random-init parameters (seed 0, normalize scales
+    from walker 0):
+      C1: H10 chain (1.8 bohr spacing), 512 walkers: the FP32 path and the FP64 build;
+      C2: C10H22, 4096 walkers: the mixed and the plain FP32 path.
+    Each path is timed like the headline step (warm-up steps, then timed steps) and its per-walker and mean-energy
+    error stated against the FP64 build of the same kernels on the same walkers and parameters (all 512 walkers of
+    C1, the first 1024 of C2)."""
+    import numpy as np
+    import torch
+
+    from sparse_wf_gb300 import systems
+    from sparse_wf_gb300.wavefunction import FireWaveFunction
+
+    out = {}
+    for key, mol, walkers, paths, K in (("C1", systems.hydrogen_chain(10, 1.8), 512, ("fp32", "fp64"), 512),
+                                        ("C2", systems.alkane(10), 4096, ("mixed", "fp32"), 1024)):
+        n_up, _ = systems.spin_counts(mol)
+        r_np = systems.init_electrons(mol, walkers, 1000)
+        seg = {"molecule": mol.name, "n_el": mol.n_el, "walkers": walkers, "error_walkers": K}
+        params, e = None, {}
+        # the timed paths, then (C2) the FP64 build once on the first K walkers as the reference
+        runs = [(p, walkers, True) for p in paths] + ([("fp64", K, False)] if "fp64" not in paths else [])
+        for prec, nw, timed in runs:
+            wf = FireWaveFunction(mol, precision=prec, device=dev)
+            if params is None:
+                params = wf.init(0, r_np[:1])
+            rr = r_np[:nw].astype(np.float64) if prec == "fp64" else r_np[:nw]
+            r = torch.from_numpy(rr).to(dev)
+            static = wf.get_static_input(r).round_with_padding(1.1, mol.n_el, n_up, mol.n_nuc)
+            wf.chunk_walkers = choose_chunk(wf, nw, static, args.ws_gb) if timed else min(nw, 64)
+            dp = wf._params(params)
+            st = {"static": static}
+
+            def step():
+                return wf.local_energy_full(dp, r, st["static"])
+
+            if timed:
+                for _ in range(args.warmup):
+                    eloc, aux = step()
+                    st["static"] = aux["static"]
+                ms, (eloc, aux) = time_steps(step, args.steps, stream, None, 1)
+                seg[prec] = {"value": nw / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+                             "chunk_walkers": wf.chunk_walkers, "refined_walkers": int(aux.get("refined", 0))}
+            else:
+                eloc, aux = step()
+            e[prec] = eloc.double().cpu().numpy()
+            del wf, dp, r, step
+            torch.cuda.empty_cache()
+        for prec in paths:
+            if prec != "fp64":
+                seg[prec]["error_vs_fp64"] = energy_error(e[prec][:K], e["fp64"][:K])
+        if "mixed" in seg and "fp32" in seg:
+            seg["mixed_over_fp32"] = seg["mixed"]["value"] / seg["fp32"]["value"]
+        out[key] = seg
+    return out
 
 
 def molecule(name):
@@ -441,6 +502,7 @@ def main():
         ms, (eloc, aux) = time_steps(step, args.steps, stream, dist, world)
     total_walkers = args.walkers * world
     value = total_walkers / (ms / 1e3)
+    e_stats = aux["stats"].cpu().numpy()
     refined = {args.precision: int(aux.get("refined", 0))}  # ill-conditioned walkers of the last timed step
 
     # per-stage device times (CUDA events around every stage / contraction launch) for the roofline
@@ -614,6 +676,18 @@ def main():
         del rb
         torch.cuda.empty_cache()
 
+    # the smaller configurations (C1, C2), after every segment of the headline workload; a failure there is
+    # recorded in the line instead of ending the run
+    configs = None
+    if world == 1 and not args.no_configs:
+        wf._ws = None
+        torch.cuda.empty_cache()
+        try:
+            configs = config_segments(args, dev, stream)
+        except Exception as exc:
+            configs = {"error": f"{type(exc).__name__}: {exc}"[:400]}
+        torch.cuda.empty_cache()
+
     # CPU baseline + oracle check on the same post-Metropolis walkers (rank 0): the oracle, one walker per core
     cpu = None
     check = None
@@ -630,7 +704,7 @@ def main():
             check[k] = {"max_abs_err_mHa": float(d.max() * 1e3), "max_rel_err": float((d / np.abs(e_ref)).max())}
 
     if rank == 0:
-        st = aux["stats"].cpu().numpy()
+        st = e_stats
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -644,7 +718,7 @@ def main():
             "gpu_launches": int(prof.get("kernels_launched", (0, 0))[0]) * args.steps,
             "fp32_path": fp32, "mixed_over_fp32": (value / fp32["value"]) if fp32 else None,
             "accuracy": accuracy, "mcmc": mcmc, "serving": serving, "ragged": ragged, "stages_ms": stages,
-            "oracle_check": check, "param_grad": param_grad,
+            "oracle_check": check, "param_grad": param_grad, "configs": configs,
         }
         print(json.dumps(line))
     if world > 1:

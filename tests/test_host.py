@@ -703,3 +703,72 @@ def test_ecp_energy_wrapper_reruns(monkeypatch):
     caps, pairs, n_ecp, qmax = zip(*fake.calls)
     assert caps == (4, 4, 14) and pairs[1] > pairs[0] and set(n_ecp) == {2} and set(qmax) == {4}
     assert out.tolist() == [1.5, 2.5] and changed == (12, 7, 8) and wf._lr_cap == 14
+
+
+def test_bench_config_segments_with_a_fake_wavefunction(monkeypatch):
+    """bench.config_segments (C1: H10 x 512, FP32 and FP64; C2: C10H22 x 4096, mixed and FP32, each against the FP64
+    build) driven on the CPU by a stand-in wavefunction whose E_loc is a fixed function of the walkers plus a
+    per-precision offset, and by stand-ins for the device timer and the workspace-sized pass: the segment's own
+    bookkeeping (which walkers, which reference, the error and ratio entries) is what is checked."""
+    import argparse
+
+    import torch
+
+    import bench
+    from sparse_wf_gb300 import wavefunction
+
+    offset = {"fp64": 0.0, "fp32": 2e-6, "mixed": -3e-6}
+    calls = []
+
+    class FakeStatic:
+        def round_with_padding(self, *a):
+            return self
+
+    class FakeWF:
+        def __init__(self, mol, precision, device):
+            self.mol, self.precision, self.chunk_walkers = mol, precision, 0
+
+        def init(self, seed, r):
+            assert seed == 0 and r.shape[0] == 1
+            return {"seeded": True}
+
+        def get_static_input(self, r):
+            return FakeStatic()
+
+        def _params(self, p):
+            assert p == {"seeded": True}
+            return p
+
+        def local_energy_full(self, dp, r, static):
+            assert r.dtype == (torch.float64 if self.precision == "fp64" else torch.float32)
+            calls.append((self.mol.name, self.precision, r.shape[0], self.chunk_walkers))
+            e = r.double().sum(dim=(1, 2)) + offset[self.precision]
+            return e, {"static": static, "refined": 1, "stats": torch.zeros(2)}
+
+    monkeypatch.setattr(wavefunction, "FireWaveFunction", FakeWF)
+    monkeypatch.setattr(bench, "choose_chunk", lambda wf, nw, static, ws_gb: nw // 2)
+
+    def fake_time(step, n, stream, dist, world):
+        out = None
+        for _ in range(n):
+            out = step()
+        return 2.0, out
+
+    monkeypatch.setattr(bench, "time_steps", fake_time)
+    args = argparse.Namespace(steps=2, warmup=1, ws_gb=48.0)
+    out = bench.config_segments(args, torch.device("cpu"), None)
+    c1, c2 = out["C1"], out["C2"]
+    assert c1["walkers"] == 512 and c1["n_el"] == 10 and c1["error_walkers"] == 512
+    assert set(c1) >= {"fp32", "fp64"} and "mixed" not in c1 and "mixed_over_fp32" not in c1
+    assert c1["fp32"]["value"] == 512 / 2e-3 and c1["fp32"]["refined_walkers"] == 1
+    assert abs(c1["fp32"]["error_vs_fp64"]["mean_energy_err_mHa"] - 2e-3) < 1e-9
+    assert "error_vs_fp64" not in c1["fp64"]
+    assert c2["walkers"] == 4096 and c2["n_el"] == 82 and c2["error_walkers"] == 1024
+    assert abs(c2["mixed"]["error_vs_fp64"]["max_abs_mHa"] - 3e-3) < 1e-9
+    assert abs(c2["mixed_over_fp32"] - 1.0) < 1e-12 and "fp64" not in c2
+    # the timed paths run warm-up + timed steps on every walker in workspace-sized passes; C2's FP64 reference runs
+    # once on the first 1024 walkers in passes of 64
+    c2_calls = [c for c in calls if c[0] == c2["molecule"]]
+    assert [c for c in c2_calls if c[1] == "fp64"] == [(c2["molecule"], "fp64", 1024, 64)]
+    assert sum(1 for c in c2_calls if c[1] == "mixed") == 3 and all(c[2:] == (4096, 2048) for c in c2_calls
+                                                                      if c[1] != "fp64")
