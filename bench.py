@@ -56,7 +56,9 @@ def parse():
     ap.add_argument("--mcmc-single-width", type=float, default=0.5)
     ap.add_argument("--mcmc-low-rank-steps", type=int, default=32,
                     help="single-electron steps of the low-rank block, timed on a copy of the walkers (0: skip)")
-    ap.add_argument("--acc-walkers", type=int, default=1024, help="walkers checked against the FP64 build")
+    ap.add_argument("--acc-walkers", type=int, default=1024,
+                    help="walkers checked against the FP64 build (0: no comparison with the FP64 build, and so no "
+                         "smaller configurations either)")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the FP32 path beside the mixed one")
     ap.add_argument("--grad-walkers", type=int, default=256,
                     help="walkers of the per-walker parameter-gradient segment (0: skip)")
@@ -676,10 +678,10 @@ def main():
         del rb
         torch.cuda.empty_cache()
 
-    # the smaller configurations (C1, C2), after every segment of the headline workload; a failure there is
-    # recorded in the line instead of ending the run
+    # the smaller configurations (C1, C2), after every segment of the headline workload and only with the
+    # comparisons against the FP64 build; a failure there is recorded in the line instead of ending the run
     configs = None
-    if world == 1 and not args.no_configs:
+    if world == 1 and not args.no_configs and args.acc_walkers > 0:
         wf._ws = None
         torch.cuda.empty_cache()
         try:
