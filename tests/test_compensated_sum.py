@@ -28,13 +28,23 @@ def _field(m):
     return (m.astype(f32).view(np.int32) >> 23) & 0xff
 
 
+def _nanmax_abs(x, axis):
+    """fmaxf semantics: NaN entries are skipped unless every entry is NaN."""
+    with np.errstate(all="ignore"):
+        m = np.nanmax(np.where(np.isnan(x), -np.inf, np.abs(x)), axis=axis)
+    return np.where(np.all(np.isnan(x), axis=axis), np.nan, m).astype(f32)
+
+
 def grid_sum(A, B):
     """hi + lo of A @ B as the kernel forms them (returned as float64 hi + lo)."""
     M, K = A.shape
     N = B.shape[1]
-    eb = np.maximum(_field(np.abs(B).max(axis=0)) - 126, -100)
-    assert np.all(eb <= 119)
+    mb = _nanmax_abs(B, 0)
+    eb = np.maximum(_field(mb) - 126, -100)
+    bad_col = (_field(mb) == 255) | (eb > 119)  # a non-finite or huge bound: the column's outputs are NaN
+    eb = np.where(bad_col, 0, eb)
     sg = (f32(3) * np.ldexp(f32(1), eb)).astype(f32)[None, :]
+    sg = np.where(bad_col[None, :], f32(np.nan), sg).astype(f32)
     g = np.ldexp(f32(1), eb - 22).astype(f32)[None, :]
     sb16 = (16 * sg.view(np.uint32).astype(np.uint64)) % (1 << 32)
     hi = np.zeros((M, N), f32)
@@ -44,29 +54,38 @@ def grid_sum(A, B):
         Bt = np.zeros((KT, N), f32)
         w = min(KT, K - k0)
         At[:, :w], Bt[:w] = A[:, k0:k0 + w], B[k0:k0 + w]
-        m = np.abs(At).max(axis=1)
+        m = _nanmax_abs(At, 1)
         ea = np.where(m > 0, np.maximum(_field(m) - 126, -125), 0)
-        assert np.all(ea <= 126)
-        a_s = (At * np.ldexp(f32(1), -ea).astype(f32)[:, None]).astype(f32)
-        sa = np.ldexp(f32(1), ea).astype(f32)[:, None]
+        bad_row = (_field(m) == 255) | (ea > 126)
+        ea = np.where(bad_row, 0, ea)
+        inv = np.where(bad_row, f32(np.nan), np.ldexp(f32(1), -ea)).astype(f32)
+        a_s = (At * inv[:, None]).astype(f32)
+        sa = np.where(bad_row, f32(np.nan), np.ldexp(f32(1), ea)).astype(f32)[:, None]
         ti = np.zeros((M, N), np.uint64)
         rh = np.zeros((M, N), f32)
         for kk in range(KT):
             a, b = a_s[:, kk:kk + 1], Bt[kk:kk + 1]
-            t = _fma(a, b, sg)
-            assert np.all((t >= 2 * sg / 3) & (t <= 4 * sg / 3))  # one binade: bits are linear in the value
+            with np.errstate(invalid="ignore"):
+                t = _fma(a, b, sg)
+                fin = np.isfinite(t)
+                assert np.all(((t >= 2 * sg / 3) & (t <= 4 * sg / 3))[fin])  # one binade: bits linear in the value
+            t = np.where(fin, t, f32(np.nan)).astype(f32)
             ti = (ti + t.view(np.uint32).astype(np.uint64)) % (1 << 32)
-            rh = (rh + _fma(a, b, (sg - t).astype(f32))).astype(f32)
+            with np.errstate(invalid="ignore"):
+                rh = (rh + _fma(a, b, (sg - t).astype(f32))).astype(f32)
         d = ((ti - sb16) % (1 << 32)).astype(np.int64)
         d = np.where(d >= 1 << 31, d - (1 << 32), d)
-        assert np.all(np.abs(d) <= 1 << 26)
+        ok = np.isfinite(rh)  # a NaN anywhere in the tile's products reaches the remainder sum
+        assert np.all(np.abs(d[ok]) <= 1 << 26)
+        d = np.where(ok, d, 0)
         xh = d.astype(f32)
         xl = (d - xh.astype(np.int64)).astype(f32)
         assert np.all(np.abs(xl) <= 2)
-        uh = (xh * g * sa).astype(f32)
-        ul = (_fma(xl, g, rh) * sa).astype(f32)
-        hi, e = _two_sum(hi, uh)
-        lo = (lo + (e + ul).astype(f32)).astype(f32)
+        with np.errstate(invalid="ignore"):
+            uh = (xh * g * sa).astype(f32)
+            ul = (_fma(xl, g, rh) * sa).astype(f32)
+            hi, e = _two_sum(hi, uh)
+            lo = (lo + (e + ul).astype(f32)).astype(f32)
     return hi.astype(f64) + lo.astype(f64)
 
 
@@ -124,3 +143,24 @@ def test_grid_sum_cancellation_and_zero_rows():
     scale = np.abs(A).astype(f64) @ np.abs(B).astype(f64)
     assert np.all(got[3] == 0) and np.all(got[:, 2] == 0)
     assert np.all(np.abs((got - exact).astype(f64)) <= 1e-12 * scale)
+
+
+def test_grid_sum_non_finite_operands_give_nan():
+    """A NaN or an infinity in a row of A or a column of B makes every output it reaches NaN (the bound of a row or
+    column that holds an infinity is non-finite, and NaN products reach the remainder sum); the other outputs are
+    untouched."""
+    rng = np.random.default_rng(7)
+    A, B = _operands("orbital", rng, M=6, N=5)
+    A[1, 17] = np.nan
+    A[2, 40] = np.inf
+    B[100, 3] = -np.inf
+    got = grid_sum(A, B)
+    bad = np.zeros(got.shape, bool)
+    bad[1, :] = bad[2, :] = bad[:, 3] = True
+    assert np.all(np.isnan(got[bad]))
+    exact = A[~np.isin(np.arange(6), [1, 2])].astype(np.longdouble) @ B.astype(np.longdouble)
+    rows = np.setdiff1d(np.arange(6), [1, 2])
+    cols = np.setdiff1d(np.arange(5), [3])
+    scale = np.abs(A[rows]).astype(f64) @ np.abs(B).astype(f64)
+    err = np.abs((got[np.ix_(rows, cols)] - exact[:, cols]).astype(f64)) / scale[:, cols]
+    assert np.all(np.isfinite(got[np.ix_(rows, cols)])) and err.max() <= 1e-12
