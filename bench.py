@@ -108,7 +108,10 @@ def config_segments(args, dev, stream):
             rr = r_np[:nw].astype(np.float64) if prec == "fp64" else r_np[:nw]
             r = torch.from_numpy(rr).to(dev)
             static = wf.get_static_input(r).round_with_padding(1.1, mol.n_el, n_up, mol.n_nuc)
-            wf.chunk_walkers = choose_chunk(wf, nw, static, args.ws_gb) if timed else min(nw, 64)
+            # walkers per pass: the workspace budget, and (as the library's own choice does) at most 65535 row
+            # tiles of 64 for the pass's Jacobian planes
+            grid_cap = max(1, 65535 * 64 // (3 * (mol.n_el + static.n_pairs)))
+            wf.chunk_walkers = min(choose_chunk(wf, nw, static, args.ws_gb), grid_cap) if timed else min(nw, 64)
             dp = wf._params(params)
             st = {"static": static}
 

@@ -721,6 +721,8 @@ def test_bench_config_segments_with_a_fake_wavefunction(monkeypatch):
     calls = []
 
     class FakeStatic:
+        n_pairs = 2200
+
         def round_with_padding(self, *a):
             return self
 
@@ -770,5 +772,8 @@ def test_bench_config_segments_with_a_fake_wavefunction(monkeypatch):
     # once on the first 1024 walkers in passes of 64
     c2_calls = [c for c in calls if c[0] == c2["molecule"]]
     assert [c for c in c2_calls if c[1] == "fp64"] == [(c2["molecule"], "fp64", 1024, 64)]
-    assert sum(1 for c in c2_calls if c[1] == "mixed") == 3 and all(c[2:] == (4096, 2048) for c in c2_calls
+    # C2's passes: the workspace would allow 2048 walkers, the launch grid's 65535 row tiles of 64 allow 612
+    assert 65535 * 64 // (3 * (82 + 2200)) == 612
+    assert sum(1 for c in c2_calls if c[1] == "mixed") == 3 and all(c[2:] == (4096, 612) for c in c2_calls
                                                                       if c[1] != "fp64")
+    assert all(c[3] == 256 for c in calls if c[0] == c1["molecule"])  # C1: the workspace's 512 // 2
