@@ -346,7 +346,10 @@ int choose_chunk(const fire_problem* p, size_t ws_bytes, bool fl) {
   int B = p->n_walkers;
   auto need = [&](int c) { return fl ? eloc_ws_bytes(p, c, nullptr) : make_plan(p, c, fl).total; };
   if (p->chunk_walkers > 0) {
-    const int c = std::min(B, p->chunk_walkers);
+    int c = std::min(B, p->chunk_walkers);
+    // a fixed pass is reduced to what the CUDA-core contraction of the Jacobian planes can launch: 65535 row tiles
+    // of 128 in the grid's y dimension
+    if (fl) c = (int)std::min<long>(c, std::max<long>(1, 65535L * 128 / (3L * (p->n_el + p->cap_pairs))));
     return need(c) <= ws_bytes ? c : 0;
   }
   // the rows of a pass's largest contraction (the Jacobian planes; the electron rows of the value path) stay within
