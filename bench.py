@@ -713,7 +713,8 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16/f32",
+            # mixed: FP16 hi + lo operands on the tensor cores with FP32 accumulation, FP32 on the CUDA cores
+            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f16/f32",
             "data": "synthetic",
             "config": workload_config(args, mol),
             "run": {"precision": args.precision, "chunk_walkers": wf.chunk_walkers, "mean_pairs_per_walker": pairs,
